@@ -1,0 +1,138 @@
+/*
+ * rbg_gb300.h -- C ABI of the GB300 (sm_103a) AVOS transitive-closure library.
+ *
+ * One shared library, librbg_gb300.so, exports every entry point below.  Conventions:
+ *   - plain pointers and sizes only; device buffers are owned by the caller;
+ *   - the library never allocates device memory behind the caller's back: every entry
+ *     point that needs scratch takes a caller-provided `workspace` whose size the matching
+ *     *_workspace_bytes query returns;
+ *   - each call is ordered on the caller's CUDA stream (`stream`, a cudaStream_t; 0 is the
+ *     legacy default stream); calls that report a status synchronise that stream before
+ *     they return;
+ *   - every entry point returns an int32 status (RBG_OK or an RBG_ERR_* code) and never
+ *     throws across the ABI.
+ *
+ * Reference behaviour replaced (paths are within rappdw/redblackgraph):
+ *   AVOS algebra       redblackgraph/core/src/redblackgraph/rbg_math.c.in:30-121
+ *   dense closure      redblackgraph/core/src/redblackgraph/warshall.c.in:51-135
+ *                      redblackgraph/sparse/csgraph/_shortest_path.pyx:213-389
+ *   dense product      redblackgraph/core/src/redblackgraph/redblack.c.src:554-594
+ *   sparse product     redblackgraph/sparse/sparsetools/rbm_math.h:117-222,
+ *                      redblackgraph/gpu/spgemm.py:32-119
+ *   squaring closure   redblackgraph/sparse/csgraph/transitive_closure.py:198-380,
+ *                      redblackgraph/gpu/transitive_closure.py:26-184
+ */
+#ifndef RBG_GB300_H
+#define RBG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void *rbg_stream_t; /* a cudaStream_t */
+
+/* storage types, in the order of the reference's per-type loops (warshall.c.in:32-43) */
+#define RBG_DTYPE_INT8 0
+#define RBG_DTYPE_UINT8 1
+#define RBG_DTYPE_INT16 2
+#define RBG_DTYPE_UINT16 3
+#define RBG_DTYPE_INT32 4
+#define RBG_DTYPE_UINT32 5
+#define RBG_DTYPE_INT64 6
+#define RBG_DTYPE_UINT64 7
+
+/* status codes */
+#define RBG_OK 0
+#define RBG_ERR_OVERFLOW 1 /* Python: OverflowError (rbg_math.c.in:103-118)           */
+#define RBG_ERR_CYCLE 2    /* Python: ValueError / CycleError (warshall.c.in:82-86)    */
+#define RBG_ERR_CAPACITY 3 /* Python: RuntimeError (capacity of a fixed buffer)       */
+#define RBG_ERR_NOMEM 4    /* workspace too small or HBM budget exceeded              */
+#define RBG_ERR_TIMEOUT 5  /* a bounded device wait gave up                           */
+#define RBG_ERR_INVALID 6  /* bad argument                                            */
+#define RBG_ERR_CUDA (-1)  /* a CUDA runtime call failed                              */
+
+/* event bits reported in rbg_result_t.flags */
+#define RBG_EV_OVF_SIZE 1u  /* msb(x)+msb(y) >= bits                                 */
+#define RBG_EV_OVF_ONES 2u  /* product equals RED_ONE (all ones)                     */
+#define RBG_EV_HANG 4u      /* the reference's MSB loop would never return here      */
+#define RBG_EV_CYCLE 8u     /* a vertex reaches itself                               */
+#define RBG_EV_RISK 16u     /* internal: clean-lane product reached the top bit      */
+#define RBG_EV_UNCLEAN 32u  /* internal: input outside the clean regime              */
+#define RBG_EV_WIDE 64u     /* internal: 64-bit values do not fit 32-bit lanes       */
+#define RBG_EV_TIMEOUT 128u /* a bounded wait gave up                                */
+
+/* mode bits for the dense closure */
+#define RBG_MODE_CYTHON 1u      /* Cython floyd_warshall semantics (int32 only)          */
+#define RBG_MODE_TRIANGULAR 2u  /* assume_upper_triangular loop (_shortest_path.pyx:365) */
+#define RBG_MODE_FORCE_EXACT 4u /* always run the sequential-order kernel                */
+#define RBG_MODE_FORCE_WIDE 8u  /* 64-bit storage: skip the 32-bit lane attempt          */
+
+/* which kernel path produced a result */
+#define RBG_PATH_BLOCKED32 1
+#define RBG_PATH_BLOCKED64 2
+#define RBG_PATH_EXACT 3
+
+typedef struct rbg_result {
+    int32_t status;   /* RBG_OK or RBG_ERR_*                                         */
+    uint32_t flags;   /* RBG_EV_* bits seen                                          */
+    int64_t diameter; /* MSB of the largest value written (warshall.c.in:89,106)     */
+    int64_t k, i, j;  /* loop position of the event that decided `status`, else -1   */
+    int32_t path;     /* RBG_PATH_* that produced the result                         */
+    int32_t reserved;
+} rbg_result_t;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int32_t rbg_version(void);
+
+/* Scratch bytes rbg_fw_dense needs for an n x n matrix of `dtype` under `mode`. */
+int32_t rbg_fw_dense_workspace_bytes(int32_t dtype, int64_t n, uint32_t mode, int64_t *bytes);
+
+/*
+ * Dense AVOS transitive closure of one n x n matrix (row-major, leading dimensions in
+ * elements).  Replaces the `warshall` gufunc loop {T}_warshall
+ * (redblackgraph/core/src/redblackgraph/warshall.c.in:51-107, reached from
+ * redblackgraph/core/redblack.py:49-50) and, with RBG_MODE_CYTHON, _floyd_warshall_avos
+ * (redblackgraph/sparse/csgraph/_shortest_path.pyx:340-389).  `in` and `out` are device
+ * pointers and may be equal.  Results (W, diameter and the error the reference raises) are
+ * bit-exact with the reference; `result` (host memory) receives status, diameter and the
+ * location of the deciding event.  Synchronises `stream`.
+ */
+int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_t ld_in, void *out,
+                     int64_t ld_out, uint32_t mode, void *workspace, int64_t workspace_bytes,
+                     rbg_result_t *result, rbg_stream_t stream);
+
+/* Scratch bytes rbg_avos_matmul needs. */
+int32_t rbg_avos_matmul_workspace_bytes(int32_t dtype, int64_t m, int64_t q, int64_t p,
+                                        int64_t *bytes);
+
+/*
+ * Dense AVOS product C[m,p] = A[m,q] (x) B[q,p] (row-major device buffers) under the C core
+ * scalar semantics.  Replaces the AVOS einsum inner loop
+ * {T}_sum_of_products_contig_contig_outstride0_two (redblackgraph/core/src/redblackgraph/
+ * redblack.c.src:554-594) behind rb.array @ (redblackgraph/core/redblack.py:14-38).
+ * Returns RBG_ERR_OVERFLOW when any product overflows (OverflowError in the reference);
+ * `flags` (host) receives the RBG_EV_* bits.  Synchronises `stream`.
+ */
+int32_t rbg_avos_matmul(int32_t dtype, int64_t m, int64_t q, int64_t p, const void *A, int64_t lda,
+                        const void *B, int64_t ldb, void *C, int64_t ldc, void *workspace,
+                        int64_t workspace_bytes, uint32_t *flags, rbg_stream_t stream);
+
+/*
+ * Element-wise AVOS sum (op 0) or product (op 1) of two device arrays of n elements:
+ * z[i] = x[i] (+) y[i] or x[i] (x) y[i] (the product's bits are the unsigned result the C core
+ * returns).  Replaces c_avos_sum / c_avos_product (redblackgraph/core/src/redblackgraph/
+ * redblackgraphmodule.c:491-533) and avos_sum_kernel / avos_product_kernel
+ * (redblackgraph/gpu/avos_kernels.py:150-176).  Returns RBG_ERR_OVERFLOW when a product
+ * overflows.  `workspace` needs 256 bytes.  Synchronises `stream`.
+ */
+int32_t rbg_avos_elementwise(int32_t op, int32_t dtype, int64_t n, const void *x, const void *y,
+                             void *z, void *workspace, int64_t workspace_bytes, uint32_t *flags,
+                             rbg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RBG_GB300_H */

@@ -1,0 +1,209 @@
+"""ctypes front-end of the CPU oracle (``avos_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+baseline legs of ``bench.py`` -- always as the checker or the timed CPU reference, never
+on the product path.  Every function restates one reference routine; the C file cites the
+reference file:line for each.
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+
+RBG_OK, RBG_ERR_OVERFLOW, RBG_ERR_CYCLE = 0, 1, 2
+EV_OVF_SIZE, EV_OVF_ONES, EV_HANG = 1, 2, 4
+
+_SUFFIX = {
+    np.dtype(np.int8): "i8", np.dtype(np.uint8): "u8",
+    np.dtype(np.int16): "i16", np.dtype(np.uint16): "u16",
+    np.dtype(np.int32): "i32", np.dtype(np.uint32): "u32",
+    np.dtype(np.int64): "i64", np.dtype(np.uint64): "u64",
+}
+_CTYPE = {
+    "i8": ctypes.c_int8, "u8": ctypes.c_uint8, "i16": ctypes.c_int16, "u16": ctypes.c_uint16,
+    "i32": ctypes.c_int32, "u32": ctypes.c_uint32, "i64": ctypes.c_int64, "u64": ctypes.c_uint64,
+}
+_UCTYPE = {
+    "i8": ctypes.c_uint8, "u8": ctypes.c_uint8, "i16": ctypes.c_uint16, "u16": ctypes.c_uint16,
+    "i32": ctypes.c_uint32, "u32": ctypes.c_uint32, "i64": ctypes.c_uint64, "u64": ctypes.c_uint64,
+}
+
+_lib = None
+
+
+def build() -> Path:
+    """Compile the oracle with its Makefile (idempotent)."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        _lib = ctypes.CDLL(str(LIB_PATH))
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    p = ctypes.c_void_p
+    i64 = ctypes.c_int64
+    for s in _SUFFIX.values():
+        T, U = _CTYPE[s], _UCTYPE[s]
+        getattr(L, f"orc_avos_sum_{s}").restype = T
+        getattr(L, f"orc_avos_sum_{s}").argtypes = [T, T]
+        getattr(L, f"orc_avos_product_{s}").restype = ctypes.c_int
+        getattr(L, f"orc_avos_product_{s}").argtypes = [T, T, ctypes.POINTER(U)]
+        getattr(L, f"orc_msb_{s}").restype = ctypes.c_int
+        getattr(L, f"orc_msb_{s}").argtypes = [T]
+        getattr(L, f"orc_warshall_{s}").restype = ctypes.c_int
+        getattr(L, f"orc_warshall_{s}").argtypes = [i64, p, ctypes.c_int, p, p]
+        getattr(L, f"orc_matmul_{s}").restype = ctypes.c_int
+        getattr(L, f"orc_matmul_{s}").argtypes = [i64, i64, i64, p, p, p, p]
+    L.orc_fw_cython_i32.restype = ctypes.c_int
+    L.orc_fw_cython_i32.argtypes = [i64, p, ctypes.c_int, p, p]
+    L.orc_cy_product.restype = ctypes.c_int32
+    L.orc_cy_product.argtypes = [ctypes.c_int32, ctypes.c_int32]
+    L.orc_cy_sum.restype = ctypes.c_int32
+    L.orc_cy_sum.argtypes = [ctypes.c_int32, ctypes.c_int32]
+    L.orc_spgemm_pass1.restype = i64
+    L.orc_spgemm_pass1.argtypes = [i64, i64, p, p, p, p, p]
+    for s in ("i64", "u64"):
+        getattr(L, f"orc_spgemm_pass2_{s}").restype = i64
+        getattr(L, f"orc_spgemm_pass2_{s}").argtypes = [i64, i64, p, p, p, p, p, p, p, p, p, p]
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def suffix(dtype) -> str:
+    return _SUFFIX[np.dtype(dtype)]
+
+
+# ----------------------------------------------------------------------------- scalars
+def avos_sum(x, y, dtype=np.int64):
+    s = suffix(dtype)
+    T = _CTYPE[s]
+    return getattr(lib(), f"orc_avos_sum_{s}")(T(int(x)).value, T(int(y)).value)
+
+
+def avos_product(x, y, dtype=np.int64):
+    """Return (unsigned result, event flags) of the C core's avos_product."""
+    s = suffix(dtype)
+    T, U = _CTYPE[s], _UCTYPE[s]
+    out = U(0)
+    ev = getattr(lib(), f"orc_avos_product_{s}")(T(int(x)).value, T(int(y)).value,
+                                                  ctypes.byref(out))
+    return out.value, ev
+
+
+def cy_product(x, y):
+    return lib().orc_cy_product(int(np.int32(x)), int(np.int32(y)))
+
+
+def cy_sum(x, y):
+    return lib().orc_cy_sum(int(np.int32(x)), int(np.int32(y)))
+
+
+# ----------------------------------------------------------------------------- dense
+def warshall(a: np.ndarray, triangular: bool = False):
+    """C core ``warshall`` on one square matrix.
+
+    Returns ``(W, diameter, status, info)``; ``status`` is 0, RBG_ERR_OVERFLOW or
+    RBG_ERR_CYCLE (the exception the reference raises), ``info`` = [kind, flags, k, i, j].
+    """
+    w = np.ascontiguousarray(a).copy()
+    n = w.shape[0]
+    assert w.shape == (n, n)
+    d = np.zeros(1, np.int64)
+    info = np.zeros(5, np.int64)
+    st = getattr(lib(), f"orc_warshall_{suffix(w.dtype)}")(n, _ptr(w), int(triangular),
+                                                            _ptr(d), _ptr(info))
+    return w, int(d[0]), int(st), info
+
+
+def fw_cython(a: np.ndarray, triangular: bool = False):
+    """Cython ``floyd_warshall`` (int32): returns ``(W, diameter, status, info)``."""
+    w = np.ascontiguousarray(a, dtype=np.int32).copy()
+    n = w.shape[0]
+    d = np.zeros(1, np.int64)
+    info = np.zeros(4, np.int64)
+    st = lib().orc_fw_cython_i32(n, _ptr(w), int(triangular), _ptr(d), _ptr(info))
+    return w, int(d[0]), int(st), info
+
+
+def matmul(a: np.ndarray, b: np.ndarray):
+    """Dense AVOS product ``a @ b`` (C core einsum 'ij,jk'); returns ``(C, status, flags)``."""
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b, dtype=a.dtype)
+    m, q = a.shape
+    q2, p = b.shape
+    assert q == q2
+    c = np.zeros((m, p), a.dtype)
+    fl = np.zeros(1, np.int64)
+    st = getattr(lib(), f"orc_matmul_{suffix(a.dtype)}")(m, q, p, _ptr(a), _ptr(b), _ptr(c),
+                                                         _ptr(fl))
+    return c, int(st), int(fl[0])
+
+
+# ----------------------------------------------------------------------------- sparse
+def spgemm(indptr_a, indices_a, data_a, indptr_b, indices_b, data_b, n_row, n_col):
+    """rbm_matmat_pass1 + pass2 on 64-bit values and int64 indices.
+
+    Inputs must be canonical CSR (sorted, no duplicates), data already 64-bit.
+    Returns ``(indptr, indices, data, flags)`` with columns in the reference's
+    accumulator order.
+    """
+    ap = np.ascontiguousarray(indptr_a, np.int64)
+    aj = np.ascontiguousarray(indices_a, np.int64)
+    bp = np.ascontiguousarray(indptr_b, np.int64)
+    bj = np.ascontiguousarray(indices_b, np.int64)
+    ax = np.ascontiguousarray(data_a)
+    bx = np.ascontiguousarray(data_b, ax.dtype)
+    s = suffix(ax.dtype)
+    assert s in ("i64", "u64")
+    cp = np.zeros(n_row + 1, np.int64)
+    nnz = lib().orc_spgemm_pass1(n_row, n_col, _ptr(ap), _ptr(aj), _ptr(bp), _ptr(bj), _ptr(cp))
+    cj = np.zeros(max(nnz, 1), np.int64)
+    cx = np.zeros(max(nnz, 1), ax.dtype)
+    fl = np.zeros(1, np.int64)
+    nnz2 = getattr(lib(), f"orc_spgemm_pass2_{s}")(n_row, n_col, _ptr(ap), _ptr(aj), _ptr(ax),
+                                                   _ptr(bp), _ptr(bj), _ptr(bx), _ptr(cp),
+                                                   _ptr(cj), _ptr(cx), _ptr(fl))
+    return cp, cj[:nnz2], cx[:nnz2], int(fl[0])
+
+
+def rb_matmul_csr(a, b):
+    """``rb_matrix.__matmul__`` (rbm.py:39-122) on scipy CSR inputs: canonicalise,
+    upcast values to 64 bits (with the unsigned RED_ONE remap), pass 1/2, cast back.
+    Returns a scipy ``csr_matrix`` and the product event flags."""
+    import scipy.sparse as sp
+    a = sp.csr_matrix(a, copy=True)
+    b = sp.csr_matrix(b, copy=True)
+    for m in (a, b):
+        m.sort_indices()
+        m.sum_duplicates()
+    out_dtype = np.promote_types(a.dtype, b.dtype)
+    wide = np.dtype(np.uint64) if out_dtype.kind == "u" else np.dtype(np.int64)
+
+    def widen(m):
+        d = np.asarray(m.data).astype(wide)
+        if out_dtype.kind == "u" and m.data.dtype.itemsize < 8:
+            d[m.data == np.iinfo(m.data.dtype).max] = np.iinfo(wide).max
+        return d
+
+    cp, cj, cx, fl = spgemm(a.indptr, a.indices, widen(a), b.indptr, b.indices, widen(b),
+                            a.shape[0], b.shape[1])
+    res = sp.csr_matrix((cx.astype(out_dtype), cj, cp), shape=(a.shape[0], b.shape[1]))
+    return res, fl

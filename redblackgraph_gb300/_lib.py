@@ -1,0 +1,114 @@
+"""ctypes binding of ``librbg_gb300.so`` -- the only way the Python layer reaches the GPU.
+
+The library is the product: there is no CPU fallback.  Loading fails loudly when the
+library has not been built, and every call that needs a device fails loudly without one.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "librbg_gb300.so"
+
+# dtype codes (include/rbg_gb300.h)
+DTYPE_CODE = {
+    np.dtype(np.int8): 0, np.dtype(np.uint8): 1, np.dtype(np.int16): 2, np.dtype(np.uint16): 3,
+    np.dtype(np.int32): 4, np.dtype(np.uint32): 5, np.dtype(np.int64): 6, np.dtype(np.uint64): 7,
+}
+
+RBG_OK = 0
+RBG_ERR_OVERFLOW = 1
+RBG_ERR_CYCLE = 2
+RBG_ERR_CAPACITY = 3
+RBG_ERR_NOMEM = 4
+RBG_ERR_TIMEOUT = 5
+RBG_ERR_INVALID = 6
+RBG_ERR_CUDA = -1
+
+EV_OVF_SIZE, EV_OVF_ONES, EV_HANG, EV_CYCLE = 1, 2, 4, 8
+
+MODE_CYTHON = 1
+MODE_TRIANGULAR = 2
+MODE_FORCE_EXACT = 4
+MODE_FORCE_WIDE = 8
+
+PATH_BLOCKED32, PATH_BLOCKED64, PATH_EXACT = 1, 2, 3
+
+
+class RbgResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("flags", ctypes.c_uint32),
+        ("diameter", ctypes.c_int64),
+        ("k", ctypes.c_int64),
+        ("i", ctypes.c_int64),
+        ("j", ctypes.c_int64),
+        ("path", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+# (name, restype, argtypes) of every exported entry point; include/rbg_gb300.h declares them
+_P = ctypes.c_void_p
+_I32, _U32, _I64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
+SIGNATURES = [
+    ("rbg_version", _I32, []),
+    ("rbg_fw_dense_workspace_bytes", _I32, [_I32, _I64, _U32, ctypes.POINTER(_I64)]),
+    ("rbg_fw_dense", _I32, [_I32, _I64, _P, _I64, _P, _I64, _U32, _P, _I64,
+                            ctypes.POINTER(RbgResult), _P]),
+    ("rbg_avos_matmul_workspace_bytes", _I32, [_I32, _I64, _I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_avos_matmul", _I32, [_I32, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
+                               ctypes.POINTER(_U32), _P]),
+    ("rbg_avos_elementwise", _I32, [_I32, _I32, _I64, _P, _P, _P, _P, _I64, ctypes.POINTER(_U32), _P]),
+]
+
+_lib = None
+
+
+def load(path: Path | None = None) -> ctypes.CDLL:
+    """Load (once) and declare the native library; raises when it is missing."""
+    global _lib
+    if _lib is None:
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise RuntimeError(
+                f"native library {p} is missing: build it with "
+                "`python -m redblackgraph_gb300.build` (nvcc, sm_103a)")
+        lib = ctypes.CDLL(str(p))
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def exported_symbols():
+    return [name for name, _, _ in SIGNATURES]
+
+
+def dtype_code(dtype) -> int:
+    try:
+        return DTYPE_CODE[np.dtype(dtype)]
+    except KeyError:
+        raise TypeError(f"unsupported dtype {dtype}: AVOS kernels take 8/16/32/64-bit integers")
+
+
+def check(rc: int, what: str) -> None:
+    """Map a non-result status (argument / CUDA / memory errors) to a Python exception."""
+    if rc == RBG_OK:
+        return
+    if rc == RBG_ERR_INVALID:
+        raise ValueError(f"{what}: invalid argument")
+    if rc == RBG_ERR_NOMEM:
+        raise MemoryError(f"{what}: workspace too small or device memory budget exceeded")
+    if rc == RBG_ERR_CUDA:
+        raise RuntimeError(f"{what}: CUDA error")
+    if rc == RBG_ERR_CAPACITY:
+        raise RuntimeError(f"{what}: fixed-capacity buffer exceeded")
+    if rc == RBG_ERR_TIMEOUT:
+        raise TimeoutError(f"{what}: bounded device wait timed out")
+    raise RuntimeError(f"{what}: status {rc}")

@@ -1,0 +1,6 @@
+"""Dense AVOS API mirroring redblackgraph.core (redblackgraph/core/__init__.py)."""
+from .warshall import warshall
+from .avos import einsum, avos_sum, avos_product
+from .redblack import array, transitive_closure
+
+__all__ = ["warshall", "einsum", "avos_sum", "avos_product", "array", "transitive_closure"]

@@ -1,0 +1,909 @@
+// fw_dense.cu -- dense AVOS transitive closure (Floyd-Warshall) for GB300 (sm_103a).
+//
+// Reference: redblackgraph/core/src/redblackgraph/warshall.c.in:51-107 (C core gufunc) and
+// redblackgraph/sparse/csgraph/_shortest_path.pyx:340-389 (Cython).  Both run the in-place
+// sequential triple loop k, i, j; the closure value of every cell AND the diameter (MSB of the
+// largest value ever written, including values later replaced, warshall.c.in:89) depend on that
+// order.  This file reproduces it exactly with two paths:
+//
+// 1. Blocked path ("snapshot-exact" blocked Floyd-Warshall), for inputs in the clean regime
+//    (off-diagonal values 0 or in [2, 2^(bits-1)), diagonal in {-1, 0, 1}).  There row k and
+//    column k are invariant during round k, so a round block K = [K0, K0+64) factors into
+//      phase 1  the 64x64 diagonal tile, sequential in k, which also records the row and column
+//               snapshots d_{k-1}(k, .) and d_{k-1}(., k) inside the tile;
+//      phase 2  the row panel (K, J) and column panel (I, K): forward substitution with those
+//               snapshots gives d_{k-1}(k, j) and d_{k-1}(i, k) for every k in K (kept in two
+//               panel buffers) and the end-of-round panel values;
+//      phase 3  every other cell: W(i,j) <- W(i,j) (+) sum_k CP(i,k) (x) RP(k,j), where CP/RP are
+//               exactly the operands the sequential loop uses at step k.
+//    Because the operands are the sequential ones, the set of products -- hence overflow and
+//    cycle detection -- is identical to the reference, and the result needs no distributivity.
+//    The running maximum is recovered per cell from its first valid product in k order (bit
+//    masks over the round), which is the value the sequential loop writes first.
+//    Arithmetic runs in 32-bit lanes (64-bit lanes when values need them): x (x) y is a single
+//    multiply-add x * 2^msb(y) + (y - 2^msb(y)); (+) is an unsigned min with "zero" encoded as
+//    any word with the top bit set.
+//
+// 2. Exact path: one k per step, all (i, j) in parallel, with the reference's full scalar
+//    semantics (identities, parity filters, wrap, overflow/cycle signalling).  It replays the
+//    in-place order (rows above k see the old row k, rows below see the new one; W(i,k) changes
+//    at j = k) and tracks the sequential index of every error event so the exception raised is
+//    the reference's (the C core keeps the LAST error set; Cython raises at the FIRST cycle).
+//    Used for unclean inputs, and re-run whenever the blocked path saw a cycle or a product
+//    reaching the top bit.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+#include "rbg_internal.cuh"
+
+namespace rbg {
+
+constexpr int FW_B = 64;         // round width (k block) and diagonal tile edge
+constexpr int FW_P = 128;        // panel tile length / phase-3 tile rows
+constexpr int FW_THREADS = 256;
+
+__global__ void status_init_kernel(DevStatus *st, int count) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) {
+        DevStatus s;
+        memset(&s, 0, sizeof(s));
+        s.mx_signed = 0;
+        s.mx_unsigned = 0;
+        s.last_ovf = -1;
+        s.last_cycle = -1;
+        s.first_hang = LLONG_MAX;
+        s.first_cycle = LLONG_MAX;
+        s.first_ovf = LLONG_MAX;
+        st[t] = s;
+    }
+}
+
+int grid_for(int64_t work, int threads) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    int64_t blocks = (work + threads - 1) / threads;
+    int64_t cap = (int64_t)sms * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+// ------------------------------------------------------------------------------------------
+// device helpers
+// ------------------------------------------------------------------------------------------
+template <typename U> struct signed_of;
+template <> struct signed_of<uint32_t> { typedef int32_t type; };
+template <> struct signed_of<uint64_t> { typedef int64_t type; };
+
+template <typename U> __device__ __forceinline__ U umin(U a, U b) { return a < b ? a : b; }
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// Reduce a per-thread running max and OR of flags into the status block.
+__device__ __forceinline__ void flush_status(DevStatus *st, unsigned long long mx, unsigned flags) {
+    mx = warp_max_u64(mx);
+    for (int o = 16; o > 0; o >>= 1) flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+    if ((threadIdx.x & 31) == 0) {
+        if (mx) atomicMax(&st->mx, mx);
+        if (flags) atomicOr(&st->flags, flags);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// convert: storage T -> lane work matrix U (clean-regime check, d_0 contribution)
+// ------------------------------------------------------------------------------------------
+// Work encoding: valid off-diagonal values as is; zeros, the diagonal, the padding and (in
+// triangular mode) the ignored lower triangle as all ones.  `lbits` is the effective width
+// min(storage bits, lane bits).  The running maximum must include d_0(i, j), the value the
+// reference writes at k = 0 (warshall.c.in:88-89); later rounds add each cell's first value.
+template <typename T, typename U>
+__global__ void __launch_bounds__(FW_THREADS)
+fw_convert_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, U *__restrict__ work,
+                  int64_t np, int lbits, int sbits, int triangular, DevStatus *st) {
+    typedef typename utype<T>::type TU;
+    typedef lane<U> L;
+    const TU tmax = (TU)~(TU)0;
+    const unsigned long long slimit = 1ull << (sbits - 1);   // storage top bit
+    const unsigned long long llimit = 1ull << (lbits - 1);   // effective lane top bit
+    unsigned flags = 0;
+    unsigned long long mx = 0;
+    const int64_t total = np * np;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx / np, j = idx - i * np;
+        U w = L::inf;
+        if (i < n && j < n) {
+            TU v = (TU)in[i * ld_in + j];
+            if (i == j) {
+                if (!(v == 0 || v == 1 || v == tmax)) flags |= RBG_EV_UNCLEAN;
+            } else if (!(triangular && i > j) && v != 0) {
+                unsigned long long uv = (unsigned long long)v;
+                if (v == 1 || v == tmax || uv >= slimit) {
+                    flags |= RBG_EV_UNCLEAN;
+                } else if (uv >= llimit) {
+                    flags |= RBG_EV_WIDE;
+                } else {
+                    w = (U)uv;
+                }
+            }
+            // d_0 = W(i,j) (+) W(i,0) (x) W(0,j); row 0 / column 0 products are identities
+            if (!(triangular && i > j) && i != j) {
+                U d0 = w;
+                if (i > 0 && j > 0 && !(triangular && i > 0)) {
+                    TU a = (TU)in[i * ld_in], b = (TU)in[j];
+                    bool ok = a != 0 && b != 0 && a != 1 && b != 1 && a != tmax && b != tmax &&
+                              (unsigned long long)a < llimit && (unsigned long long)b < llimit;
+                    if (ok) {
+                        bool risk = false;
+                        U p = L::product((U)a, (U)b, lbits, risk);
+                        if (!risk) d0 = umin(d0, p);
+                    }
+                }
+                if (L::valid(d0) && (unsigned long long)d0 > mx) mx = (unsigned long long)d0;
+            }
+        }
+        work[idx] = w;
+    }
+    flush_status(st, mx, flags);
+}
+
+// ------------------------------------------------------------------------------------------
+// kernel A: phase 1 (diagonal tile, recomputed by every CTA in shared memory) + phase 2
+// (one 64 x 128 row-panel tile or one 128 x 64 column-panel tile per CTA)
+// ------------------------------------------------------------------------------------------
+template <typename U> struct PanelSmem {
+    U D[FW_B][FW_B + 1];     // diagonal tile, updated in place
+    U RS[FW_B][FW_B];        // RS[t][b] = row t at step t   (d_{t-1}(t, b))
+    U CS[FW_B][FW_B];        // CS[a][t] = column t at step t (d_{t-1}(a, t))
+    int msbRS[FW_B];         // max msb over valid RS[t][.]
+    int msbCS[FW_B];         // max msb over valid CS[.][t]
+    U P[FW_P * FW_B];        // the panel tile (row panel: [64][128], column panel: [128][64])
+    int any;
+};
+
+template <typename U>
+__device__ void fw_phase1(PanelSmem<U> &S, const U *__restrict__ work, int64_t np, int64_t K0,
+                          int lbits, bool report, unsigned &flags, unsigned long long &mx) {
+    typedef lane<U> L;
+    typedef typename signed_of<U>::type SU;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < FW_B * FW_B; e += FW_THREADS) {
+        int a = e / FW_B, b = e % FW_B;
+        S.D[a][b] = work[(K0 + a) * np + K0 + b];
+    }
+    __syncthreads();
+    bool risk = false, cyc = false;
+    SU smx = 0;
+    for (int t = 0; t < FW_B; ++t) {
+        // snapshots: row t and column t do not change at step t (the diagonal is encoded zero)
+        for (int e = tid; e < FW_B; e += FW_THREADS) {
+            S.RS[t][e] = S.D[t][e];
+            S.CS[e][t] = S.D[e][t];
+        }
+        for (int e = tid; e < FW_B * FW_B; e += FW_THREADS) {
+            int a = e / FW_B, b = e % FW_B;
+            if (a == t || b == t) continue;
+            U p = L::product(S.D[a][t], S.D[t][b], lbits, risk);
+            if (a == b) {
+                if (L::valid(p)) cyc = true;
+            } else {
+                U v = umin(S.D[a][b], p);
+                S.D[a][b] = v;
+                smx = max(smx, (SU)v);   // encoded zeros are negative as signed
+            }
+        }
+        __syncthreads();
+    }
+    // per-step maxima of the snapshots, for the risk test of phase 2
+    for (int t = tid; t < FW_B; t += FW_THREADS) {
+        int mr = -1000, mc = -1000;
+        for (int b = 0; b < FW_B; ++b) {
+            U r = S.RS[t][b], c = S.CS[b][t];
+            if (L::valid(r)) mr = max(mr, msb_nz<U>(r));
+            if (L::valid(c)) mc = max(mc, msb_nz<U>(c));
+        }
+        S.msbRS[t] = mr;
+        S.msbCS[t] = mc;
+    }
+    if (report) {
+        if (risk) flags |= RBG_EV_RISK;
+        if (cyc) flags |= RBG_EV_CYCLE;
+        if (smx > 0 && (unsigned long long)smx > mx) mx = (unsigned long long)smx;
+    }
+    __syncthreads();
+}
+
+template <typename U>
+__global__ void __launch_bounds__(FW_THREADS)
+fw_panel_kernel(U *__restrict__ work, int64_t np, int64_t K0, U *__restrict__ cpbuf,
+                U *__restrict__ rpbuf, U *__restrict__ diagbuf, int *__restrict__ anyCP,
+                int *__restrict__ anyRP, int lbits, DevStatus *st) {
+    typedef lane<U> L;
+    typedef typename signed_of<U>::type SU;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
+    const int tid = threadIdx.x;
+    const int ntp = (int)(np / FW_P);
+    const bool rowPanel = blockIdx.x < (unsigned)ntp;
+    const int tile = rowPanel ? blockIdx.x : blockIdx.x - ntp;
+    unsigned flags = 0;
+    unsigned long long mx = 0;
+
+    fw_phase1<U>(S, work, np, K0, lbits, blockIdx.x == 0, flags, mx);
+    if (blockIdx.x == 0) {
+        // every CTA of this launch reads the diagonal tile from `work`, so its end-of-round
+        // value goes to a side buffer; the phase-3 launch copies it back
+        for (int e = tid; e < FW_B * FW_B; e += FW_THREADS) {
+            int a = e / FW_B, b = e % FW_B;
+            U v = S.D[a][b];
+            diagbuf[e] = lane<U>::valid(v) ? v : lane<U>::inf;
+        }
+    }
+    if (tid == 0) S.any = 0;
+    const int64_t T0 = (int64_t)tile * FW_P;
+    bool risk = false;
+    SU smx = 0;
+    int any = 0;
+    if (rowPanel) {
+        // P[a][j], a in K (64 rows), j in [T0, T0+128); columns inside K are the diagonal tile
+        for (int e = tid; e < FW_B * FW_P; e += FW_THREADS) {
+            int a = e / FW_P, j = e % FW_P;
+            int64_t gj = T0 + j;
+            bool inK = gj >= K0 && gj < K0 + FW_B;
+            S.P[e] = inK ? L::inf : work[(K0 + a) * np + gj];
+        }
+        __syncthreads();
+        const int j = tid % FW_P;           // this thread's column
+        const int a0 = tid / FW_P;          // rows a0, a0+2, ...
+        for (int t = 0; t < FW_B; ++t) {
+            U y = S.P[t * FW_P + j];        // row t is invariant at step t
+            if (a0 == 0) rpbuf[(int64_t)t * np + T0 + j] = y;
+            any |= L::valid(y);
+            U m, low;
+            L::split(y, m, low);
+            if (L::valid(y) && S.msbCS[t] + msb_nz<U>(y) >= lbits - 1) risk = true;
+#pragma unroll 8
+            for (int a = a0; a < FW_B; a += FW_THREADS / FW_P) {
+                if (a == t) continue;
+                U x = S.CS[a][t];
+                U p = L::valid(x) ? L::mul(x, m, low) : L::inf;
+                U v = umin(S.P[a * FW_P + j], p);
+                S.P[a * FW_P + j] = v;
+                smx = max(smx, (SU)v);
+            }
+            __syncthreads();
+        }
+        for (int e = tid; e < FW_B * FW_P; e += FW_THREADS) {
+            int a = e / FW_P, jj = e % FW_P;
+            int64_t gj = T0 + jj;
+            if (!(gj >= K0 && gj < K0 + FW_B)) {
+                U v = S.P[e];
+                work[(K0 + a) * np + gj] = L::valid(v) ? v : L::inf;
+            }
+        }
+    } else {
+        // P[i][b], i in [T0, T0+128), b in K; rows inside K are the diagonal tile
+        for (int e = tid; e < FW_P * FW_B; e += FW_THREADS) {
+            int i = e / FW_B, b = e % FW_B;
+            int64_t gi = T0 + i;
+            bool inK = gi >= K0 && gi < K0 + FW_B;
+            S.P[e] = inK ? L::inf : work[gi * np + K0 + b];
+        }
+        __syncthreads();
+        const int i = tid % FW_P;           // this thread's row
+        const int b0 = tid / FW_P;          // columns b0, b0+2, ...
+        for (int t = 0; t < FW_B; ++t) {
+            U x = S.P[i * FW_B + t];        // column t is invariant at step t
+            if (b0 == 0) cpbuf[(T0 + i) * FW_B + t] = x;
+            any |= L::valid(x);
+            const bool xv = L::valid(x);
+            if (xv && msb_nz<U>(x) + S.msbRS[t] >= lbits - 1) risk = true;
+#pragma unroll 8
+            for (int b = b0; b < FW_B; b += FW_THREADS / FW_P) {
+                if (b == t) continue;
+                U y = S.RS[t][b];
+                U p = L::inf;
+                if (xv && L::valid(y)) {
+                    int s = msb_nz<U>(y);
+                    p = (x << s) | (y ^ (((U)1) << s));
+                }
+                U v = umin(S.P[i * FW_B + b], p);
+                S.P[i * FW_B + b] = v;
+                smx = max(smx, (SU)v);
+            }
+            __syncthreads();
+        }
+        for (int e = tid; e < FW_P * FW_B; e += FW_THREADS) {
+            int ii = e / FW_B, b = e % FW_B;
+            int64_t gi = T0 + ii;
+            if (!(gi >= K0 && gi < K0 + FW_B)) {
+                U v = S.P[e];
+                work[gi * np + K0 + b] = L::valid(v) ? v : L::inf;
+            }
+        }
+    }
+    if (any) atomicOr(&S.any, 1);
+    __syncthreads();
+    if (tid == 0) (rowPanel ? anyRP : anyCP)[tile] = S.any;
+    if (risk) flags |= RBG_EV_RISK;
+    if (smx > 0 && (unsigned long long)smx > mx) mx = (unsigned long long)smx;
+    flush_status(st, mx, flags);
+}
+
+// ------------------------------------------------------------------------------------------
+// kernel B: phase 3 over BM x BN tiles, register micro-tiles TM x TN, 256 threads
+// ------------------------------------------------------------------------------------------
+template <typename U, int BN> struct TileSmem {
+    U CPt[FW_B][FW_P];       // CPt[t][i] = d_{t-1}(i, t)
+    U RPm[FW_B][BN];         // 2^msb(d_{t-1}(t, j)) (0 for zero)
+    U RPl[FW_B][BN];         // d_{t-1}(t, j) - 2^msb   (inf for zero)
+    unsigned long long maskC[FW_P];   // bit t: CPt[t][i] valid
+    unsigned long long maskR[BN];     // bit t: RP(t, j) valid
+    int msbR[FW_B];                   // max msb over valid RP(t, .) in this tile
+    int active[FW_B];
+    int nactive;
+    unsigned long long colAny, rowAny;
+};
+
+template <typename U, int BN, int TM, int TN>
+__global__ void __launch_bounds__(FW_THREADS)
+fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict__ cpbuf,
+               const U *__restrict__ rpbuf, const U *__restrict__ diagbuf,
+               const int *__restrict__ anyCP, const int *__restrict__ anyRP, int lbits,
+               DevStatus *st) {
+    typedef lane<U> L;
+    constexpr int BM = FW_P;
+    constexpr int TX = BN / TN;           // threads along columns
+    constexpr int TY = BM / TM;           // threads along rows
+    static_assert(TX * TY == FW_THREADS, "micro-tile layout must use 256 threads");
+    constexpr int HN = TN / 2;            // each thread owns two column groups of HN
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
+
+    const int tI = blockIdx.y, tJ = blockIdx.x;
+    if (tI == 0 && tJ == 0) {
+        // end-of-round diagonal tile from the panel launch (no other CTA stores those cells)
+        for (int e = threadIdx.x; e < FW_B * FW_B; e += FW_THREADS)
+            work[(K0 + e / FW_B) * np + K0 + e % FW_B] = diagbuf[e];
+    }
+    if (!anyCP[tI] || !anyRP[(int)(((int64_t)tJ * BN) / FW_P)]) return;
+    const int64_t I0 = (int64_t)tI * BM, J0 = (int64_t)tJ * BN;
+    const int tid = threadIdx.x;
+    if (tid == 0) { S.colAny = 0; S.rowAny = 0; S.nactive = 0; }
+    __syncthreads();
+
+    // ---- stage the column-panel snapshots (transposed) and row masks
+    for (int r = tid; r < BM; r += FW_THREADS) {
+        unsigned long long m = 0;
+        const U *src = cpbuf + (I0 + r) * FW_B;
+#pragma unroll 4
+        for (int t = 0; t < FW_B; ++t) {
+            U x = src[t];
+            bool v = L::valid(x);
+            S.CPt[t][r] = v ? x : L::inf;
+            m |= (unsigned long long)v << t;
+        }
+        S.maskC[r] = m;
+        if (m) atomicOr(&S.colAny, m);
+    }
+    // ---- stage the row-panel snapshots as (m, low) pairs and column masks
+    for (int e = tid; e < FW_B * BN; e += FW_THREADS) {
+        int t = e / BN, c = e % BN;
+        U y = rpbuf[(int64_t)t * np + J0 + c];
+        U m, low;
+        L::split(y, m, low);
+        S.RPm[t][c] = m;
+        S.RPl[t][c] = low;
+    }
+    __syncthreads();
+    for (int c = tid; c < BN; c += FW_THREADS) {
+        unsigned long long m = 0;
+        for (int t = 0; t < FW_B; ++t) m |= (unsigned long long)(S.RPm[t][c] != 0) << t;
+        S.maskR[c] = m;
+        if (m) atomicOr(&S.rowAny, m);
+    }
+    for (int t = tid; t < FW_B; t += FW_THREADS) {
+        int mr = -1000;
+        for (int c = 0; c < BN; ++c) {
+            U m = S.RPm[t][c];
+            if (m) mr = max(mr, msb_nz<U>(m));
+        }
+        S.msbR[t] = mr;
+    }
+    __syncthreads();
+    const unsigned long long act = S.colAny & S.rowAny;
+    if (act == 0) return;   // uniform across the block
+    if (tid == 0) {
+        int na = 0;
+        unsigned long long a = act;
+        while (a) { int t = __ffsll((long long)a) - 1; S.active[na++] = t; a &= a - 1; }
+        S.nactive = na;
+    }
+    // risk: some computed product x (x) y with msb(x) + msb(y) >= lbits - 1
+    bool risk = false;
+    for (int e = tid; e < FW_B * BM; e += FW_THREADS) {
+        int t = e / BM, r = e % BM;
+        U x = S.CPt[t][r];
+        if (L::valid(x) && S.msbR[t] > -1 && msb_nz<U>(x) + S.msbR[t] >= lbits - 1) risk = true;
+    }
+    __syncthreads();
+
+    // ---- accumulators
+    const int ty = tid / TX, tx = tid % TX;
+    const int r0 = ty * TM;
+    int cidx[TN];
+#pragma unroll
+    for (int c = 0; c < TN; ++c) cidx[c] = (c < HN) ? tx * HN + c : BN / 2 + tx * HN + (c - HN);
+    U acc[TM][TN];
+    unsigned long long wasInf = 0;
+#pragma unroll
+    for (int r = 0; r < TM; ++r) {
+        const U *row = work + (I0 + r0 + r) * np + J0;
+#pragma unroll
+        for (int c = 0; c < TN; ++c) {
+            U v = row[cidx[c]];
+            acc[r][c] = v;
+            wasInf |= (unsigned long long)(!L::valid(v)) << (r * TN + c);
+        }
+    }
+
+    const int na = S.nactive;
+    for (int q = 0; q < na; ++q) {
+        const int t = S.active[q];
+        U x[TM], m[TN], l[TN];
+#pragma unroll
+        for (int r = 0; r < TM; ++r) x[r] = S.CPt[t][r0 + r];
+#pragma unroll
+        for (int c = 0; c < TN; ++c) { m[c] = S.RPm[t][cidx[c]]; l[c] = S.RPl[t][cidx[c]]; }
+#pragma unroll
+        for (int r = 0; r < TM; ++r)
+#pragma unroll
+            for (int c = 0; c < TN; ++c) acc[r][c] = umin(acc[r][c], x[r] * m[c] + l[c]);
+    }
+
+    // ---- write back, cycle test on the global diagonal, first values for the running max
+    unsigned flags = risk ? RBG_EV_RISK : 0u;
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int r = 0; r < TM; ++r) {
+        const int64_t gi = I0 + r0 + r;
+        const bool rowInK = gi >= K0 && gi < K0 + FW_B;
+        U *row = work + gi * np + J0;
+#pragma unroll
+        for (int c = 0; c < TN; ++c) {
+            const int64_t gj = J0 + cidx[c];
+            if (rowInK || (gj >= K0 && gj < K0 + FW_B)) continue;
+            U v = acc[r][c];
+            const bool valid = L::valid(v);
+            if (gi == gj) {
+                if (valid) flags |= RBG_EV_CYCLE;
+                continue;   // the diagonal stays encoded zero
+            }
+            if (valid && ((wasInf >> (r * TN + c)) & 1ull)) {
+                unsigned long long both = S.maskC[r0 + r] & S.maskR[cidx[c]];
+                int kf = __ffsll((long long)both) - 1;
+                U first = S.CPt[kf][r0 + r] * S.RPm[kf][cidx[c]] + S.RPl[kf][cidx[c]];
+                if ((unsigned long long)first > mx) mx = (unsigned long long)first;
+            }
+            row[cidx[c]] = valid ? v : L::inf;
+        }
+    }
+    flush_status(st, mx, flags);
+}
+
+// ------------------------------------------------------------------------------------------
+// finalize: lane work matrix -> storage T (restores the diagonal and, in triangular mode, the
+// untouched lower triangle from the input)
+// ------------------------------------------------------------------------------------------
+template <typename T, typename U>
+__global__ void __launch_bounds__(FW_THREADS)
+fw_finalize_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, const U *__restrict__ work,
+                   int64_t np, T *__restrict__ out, int64_t ld_out, int triangular) {
+    const int64_t total = n * n;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx / n, j = idx - i * n;
+        T v;
+        if (i == j || (triangular && i > j)) {
+            v = in[i * ld_in + j];
+        } else {
+            U w = work[i * np + j];
+            v = lane<U>::valid(w) ? (T)w : (T)0;
+        }
+        out[i * ld_out + j] = v;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// exact path: sequential order, full reference semantics
+// ------------------------------------------------------------------------------------------
+// SEM = 0: C core (any T).  SEM = 1: Cython (int32).
+template <typename T, int SEM>
+__device__ __forceinline__ T ex_product(T x, T y, unsigned &ev) {
+    if (SEM == 1) return (T)cy_product((int32_t)x, (int32_t)y);
+    return (T)avos_product<T>(x, y, ev);
+}
+template <typename T, int SEM> __device__ __forceinline__ T ex_sum(T a, T b) {
+    if (SEM == 1) return (T)cy_sum((int32_t)a, (int32_t)b);
+    return avos_sum<T>(a, b);
+}
+
+template <typename T, int SEM>
+__device__ __forceinline__ void ex_event(DevStatus *st, unsigned ev, bool diag, T p,
+                                         long long seq, unsigned &flags) {
+    if (SEM == 0 && ev) {
+        flags |= ev;
+        if (ev & RBG_EV_HANG) atomicMin(&st->first_hang, seq);
+        if (ev & (RBG_EV_OVF_SIZE | RBG_EV_OVF_ONES)) {
+            atomicMax(&st->last_ovf, seq);
+            atomicMin(&st->first_ovf, seq);
+        }
+    }
+    if (diag && !(p == (T)-1 || p == 0 || p == 1)) {
+        flags |= RBG_EV_CYCLE;
+        atomicMax(&st->last_cycle, seq);
+        atomicMin(&st->first_cycle, seq);
+    }
+}
+
+template <typename T, int SEM>
+__device__ __forceinline__ void ex_track(T v, long long &smax, unsigned long long &umax) {
+    typedef typename utype<T>::type TU;
+    if (SEM == 0 && (TU)(~v) == 0) return;   // warshall.c.in:89 skips all ones
+    if (utype<T>::is_signed) {
+        long long s = (long long)v;
+        if (s > smax) smax = s;
+    } else {
+        unsigned long long u = (unsigned long long)(TU)v;
+        if (u > umax) umax = u;
+    }
+}
+
+__device__ __forceinline__ void flush_exact(DevStatus *st, long long smax, unsigned long long umax,
+                                            unsigned flags) {
+    for (int o = 16; o > 0; o >>= 1) {
+        long long s2 = __shfl_xor_sync(0xffffffffu, smax, o);
+        unsigned long long u2 = __shfl_xor_sync(0xffffffffu, umax, o);
+        unsigned f2 = __shfl_xor_sync(0xffffffffu, flags, o);
+        smax = s2 > smax ? s2 : smax;
+        umax = u2 > umax ? u2 : umax;
+        flags |= f2;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (smax > 0) atomicMax(&st->mx_signed, smax);
+        if (umax > 0) atomicMax(&st->mx_unsigned, umax);
+        if (flags) atomicOr(&st->flags, flags);
+    }
+}
+
+// Row k of round k (i == k in the reference loop), plus the old row / column copies.
+template <typename T, int SEM>
+__global__ void __launch_bounds__(FW_THREADS)
+fw_exact_row_kernel(T *__restrict__ w, int64_t ld, int64_t n, int64_t k, int triangular,
+                    T *__restrict__ oldrow, T *__restrict__ oldcol, T *__restrict__ newrow,
+                    DevStatus *st) {
+    unsigned flags = 0;
+    long long smax = 0;
+    unsigned long long umax = 0;
+    const T old_kk = w[k * ld + k];
+    unsigned ev0 = 0;
+    const T new_kk = ex_sum<T, SEM>(old_kk, ex_product<T, SEM>(old_kk, old_kk, ev0));
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const T oj = w[k * ld + j];
+        oldrow[j] = oj;
+        oldcol[j] = w[j * ld + k];
+        T nv = oj;
+        if (!triangular || j >= k) {
+            unsigned ev = 0;
+            T x = (j <= k) ? old_kk : new_kk;
+            T p = ex_product<T, SEM>(x, oj, ev);
+            long long seq = ((long long)k * n + k) * n + j;
+            ex_event<T, SEM>(st, ev, j == k, p, seq, flags);
+            nv = ex_sum<T, SEM>(oj, p);
+            ex_track<T, SEM>(nv, smax, umax);
+        }
+        newrow[j] = nv;
+    }
+    flush_exact(st, smax, umax, flags);
+}
+
+template <typename T, int SEM>
+__global__ void __launch_bounds__(FW_THREADS)
+fw_exact_cells_kernel(T *__restrict__ w, int64_t ld, int64_t n, int64_t k, int triangular,
+                      const T *__restrict__ oldrow, const T *__restrict__ oldcol,
+                      const T *__restrict__ newrow, DevStatus *st) {
+    unsigned flags = 0;
+    long long smax = 0;
+    unsigned long long umax = 0;
+    const int64_t total = n * n;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx / n, j = idx - i * n;
+        if (i == k) {
+            w[k * ld + j] = newrow[j];
+            continue;
+        }
+        if (triangular && !(i < k && j >= k)) continue;
+        const T* rowk = (i < k) ? oldrow : newrow;   // rows above k run before row k
+        const T old_a = oldcol[i];
+        unsigned ev = 0;
+        T x = old_a;
+        if (j > k) {
+            unsigned ev2 = 0;   // W(i,k) was updated at j == k (its events counted there)
+            x = ex_sum<T, SEM>(old_a, ex_product<T, SEM>(old_a, rowk[k], ev2));
+        }
+        T p = ex_product<T, SEM>(x, rowk[j], ev);
+        long long seq = ((long long)k * n + i) * n + j;
+        ex_event<T, SEM>(st, ev, i == j, p, seq, flags);
+        T nv = ex_sum<T, SEM>(w[i * ld + j], p);
+        w[i * ld + j] = nv;
+        ex_track<T, SEM>(nv, smax, umax);
+    }
+    flush_exact(st, smax, umax, flags);
+}
+
+template <typename T, int SEM>
+static int run_exact(const T *in, int64_t ld_in, T *out, int64_t ld_out, int64_t n, int triangular,
+                     unsigned char *ws, DevStatus *st, cudaStream_t stream) {
+    if (in != out)
+        RBG_CUDA_TRY(cudaMemcpy2DAsync(out, ld_out * sizeof(T), in, ld_in * sizeof(T),
+                                       n * sizeof(T), n, cudaMemcpyDeviceToDevice, stream));
+    T *oldrow = reinterpret_cast<T *>(ws);
+    T *oldcol = oldrow + align_up(n, 32);
+    T *newrow = oldcol + align_up(n, 32);
+    const int gr = grid_for(n, FW_THREADS);
+    const int gc = grid_for(n * n, FW_THREADS);
+    for (int64_t k = 0; k < n; ++k) {
+        fw_exact_row_kernel<T, SEM><<<gr, FW_THREADS, 0, stream>>>(out, ld_out, n, k, triangular,
+                                                                   oldrow, oldcol, newrow, st);
+        fw_exact_cells_kernel<T, SEM><<<gc, FW_THREADS, 0, stream>>>(out, ld_out, n, k, triangular,
+                                                                     oldrow, oldcol, newrow, st);
+    }
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// host driver
+// ------------------------------------------------------------------------------------------
+struct FwLayout {
+    int64_t np;
+    size_t off_status, off_work, off_cp, off_rp, off_diag, off_anyc, off_anyr, off_exact, total;
+};
+
+static FwLayout fw_layout(int64_t n, int dtype, bool wide_possible) {
+    FwLayout L;
+    L.np = align_up((size_t)std::max<int64_t>(n, 1), FW_P);
+    const size_t ub = wide_possible ? 8 : 4;   // largest lane size that may be needed
+    size_t o = 0;
+    L.off_status = o; o += 256;
+    L.off_work = o; o = align_up(o + (size_t)L.np * L.np * ub, 256);
+    L.off_cp = o; o = align_up(o + (size_t)L.np * FW_B * ub, 256);
+    L.off_rp = o; o = align_up(o + (size_t)L.np * FW_B * ub, 256);
+    L.off_diag = o; o = align_up(o + (size_t)FW_B * FW_B * ub, 256);
+    L.off_anyc = o; o = align_up(o + (size_t)(L.np / FW_P) * 4, 256);
+    L.off_anyr = o; o = align_up(o + (size_t)(L.np / FW_P) * 4, 256);
+    L.off_exact = o; o = align_up(o + 3 * align_up((size_t)n, 32) * dtype_bytes(dtype) + 256, 256);
+    L.total = o;
+    return L;
+}
+
+template <typename U> static size_t panel_smem() { return sizeof(PanelSmem<U>); }
+template <typename U, int BN> static size_t tile_smem() { return sizeof(TileSmem<U, BN>); }
+
+static int read_status(DevStatus *d, DevStatus *h, cudaStream_t stream) {
+    RBG_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+    RBG_CUDA_TRY(cudaStreamSynchronize(stream));
+    return RBG_OK;
+}
+
+template <typename U> struct TileCfg;
+template <> struct TileCfg<uint32_t> { static const int BN = 128, TM = 8, TN = 8; };
+template <> struct TileCfg<uint64_t> { static const int BN = 64, TM = 8, TN = 4; };
+
+template <typename U>
+static int configure_kernels() {
+    typedef TileCfg<U> C;
+    RBG_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)panel_smem<U>()));
+    RBG_CUDA_TRY(cudaFuncSetAttribute(fw_tile_kernel<U, C::BN, C::TM, C::TN>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tile_smem<U, C::BN>()));
+    return RBG_OK;
+}
+
+// One blocked run in lanes U (conversion + all rounds); the caller finalizes only when the
+// status is clean, so an in-place call keeps its input for an exact re-run.
+template <typename T, typename U>
+static int run_blocked(const T *in, int64_t ld_in, int64_t n, int triangular, unsigned char *ws,
+                       const FwLayout &Ly, DevStatus *h, cudaStream_t stream) {
+    typedef TileCfg<U> C;
+    static bool configured = false;
+    if (!configured) {
+        int rc = configure_kernels<U>();
+        if (rc) return rc;
+        configured = true;
+    }
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + Ly.off_status);
+    U *work = reinterpret_cast<U *>(ws + Ly.off_work);
+    U *cp = reinterpret_cast<U *>(ws + Ly.off_cp);
+    U *rp = reinterpret_cast<U *>(ws + Ly.off_rp);
+    U *diag = reinterpret_cast<U *>(ws + Ly.off_diag);
+    int *anyc = reinterpret_cast<int *>(ws + Ly.off_anyc);
+    int *anyr = reinterpret_cast<int *>(ws + Ly.off_anyr);
+    const int64_t np = Ly.np;
+    const int sbits = (int)sizeof(T) * 8;
+    const int lbits = std::min<int>(sbits, (int)sizeof(U) * 8);
+
+    status_init_kernel<<<1, 32, 0, stream>>>(st, 1);
+    fw_convert_kernel<T, U><<<grid_for(np * np, FW_THREADS), FW_THREADS, 0, stream>>>(
+        in, ld_in, n, work, np, lbits, sbits, triangular, st);
+    RBG_CUDA_TRY(cudaGetLastError());
+    int rc = read_status(st, h, stream);
+    if (rc) return rc;
+    if (h->flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE)) return RBG_OK;   // caller decides
+
+    const int ntp = (int)(np / FW_P);
+    const dim3 tgrid((unsigned)(np / C::BN), (unsigned)ntp);
+    const size_t psm = panel_smem<U>(), tsm = tile_smem<U, C::BN>();
+    for (int64_t K0 = 0; K0 < n; K0 += FW_B) {
+        fw_panel_kernel<U><<<2 * ntp, FW_THREADS, psm, stream>>>(work, np, K0, cp, rp, diag, anyc,
+                                                                 anyr, lbits, st);
+        fw_tile_kernel<U, C::BN, C::TM, C::TN><<<tgrid, FW_THREADS, tsm, stream>>>(
+            work, np, K0, cp, rp, diag, anyc, anyr, lbits, st);
+    }
+    RBG_CUDA_TRY(cudaGetLastError());
+    return read_status(st, h, stream);
+}
+
+template <typename T, typename U>
+static int finalize_blocked(const T *in, int64_t ld_in, int64_t n, T *out, int64_t ld_out,
+                            int triangular, unsigned char *ws, const FwLayout &Ly,
+                            cudaStream_t stream) {
+    const U *work = reinterpret_cast<const U *>(ws + Ly.off_work);
+    fw_finalize_kernel<T, U><<<grid_for(n * n, FW_THREADS), FW_THREADS, 0, stream>>>(
+        in, ld_in, n, work, Ly.np, out, ld_out, triangular);
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+static void decode_seq(long long seq, int64_t n, rbg_result_t *r) {
+    if (seq < 0 || seq == LLONG_MAX) { r->k = r->i = r->j = -1; return; }
+    r->j = seq % n;
+    r->i = (seq / n) % n;
+    r->k = seq / n / n;
+}
+
+template <typename T>
+static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_out, uint32_t mode,
+                      unsigned char *ws, const FwLayout &Ly, rbg_result_t *res, cudaStream_t stream) {
+    const bool cython = (mode & RBG_MODE_CYTHON) != 0;
+    const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
+    DevStatus h;
+    memset(res, 0, sizeof(*res));
+    res->k = res->i = res->j = -1;
+    bool need_exact = (mode & RBG_MODE_FORCE_EXACT) != 0;
+    if (!need_exact) {
+        bool wide = sizeof(T) == 8 && (mode & RBG_MODE_FORCE_WIDE);
+        if (!wide) {
+            int rc = run_blocked<T, uint32_t>(in, ld_in, n, triangular, ws, Ly, &h, stream);
+            if (rc) return rc;
+            const unsigned f = h.flags;
+            if (f & (RBG_EV_UNCLEAN | RBG_EV_CYCLE)) need_exact = true;
+            else if (f & (RBG_EV_WIDE | RBG_EV_RISK)) {
+                if (sizeof(T) == 8) wide = true;   // values need 64-bit lanes
+                else need_exact = true;            // the reference itself reaches the top bit
+            } else {
+                rc = finalize_blocked<T, uint32_t>(in, ld_in, n, out, ld_out, triangular, ws, Ly, stream);
+                if (rc) return rc;
+                res->path = RBG_PATH_BLOCKED32;
+            }
+        }
+        if (wide && !need_exact) {
+            int rc = run_blocked<T, uint64_t>(in, ld_in, n, triangular, ws, Ly, &h, stream);
+            if (rc) return rc;
+            if (h.flags & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_RISK | RBG_EV_WIDE)) need_exact = true;
+            else {
+                rc = finalize_blocked<T, uint64_t>(in, ld_in, n, out, ld_out, triangular, ws, Ly, stream);
+                if (rc) return rc;
+                res->path = RBG_PATH_BLOCKED64;
+            }
+        }
+        if (res->path) {
+            RBG_CUDA_TRY(cudaStreamSynchronize(stream));
+            res->status = RBG_OK;
+            res->flags = h.flags;
+            res->diameter = h.mx ? msb_u64(h.mx) : 0;
+            return RBG_OK;
+        }
+    }
+    // exact path
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + Ly.off_status);
+    status_init_kernel<<<1, 32, 0, stream>>>(st, 1);
+    int rc = cython ? run_exact<T, 1>(in, ld_in, out, ld_out, n, triangular, ws + Ly.off_exact, st, stream)
+                    : run_exact<T, 0>(in, ld_in, out, ld_out, n, triangular, ws + Ly.off_exact, st, stream);
+    if (rc) return rc;
+    rc = read_status(st, &h, stream);
+    if (rc) return rc;
+    res->path = RBG_PATH_EXACT;
+    res->flags = h.flags;
+    typedef typename utype<T>::type TU;
+    if (cython) {
+        if (h.first_cycle != LLONG_MAX) {
+            res->status = RBG_ERR_CYCLE;
+            decode_seq(h.first_cycle, n, res);
+            res->diameter = 0;
+        } else {
+            res->status = RBG_OK;
+            res->diameter = h.mx_signed > 1 ? msb_u64((unsigned long long)h.mx_signed) : 0;
+        }
+        return RBG_OK;
+    }
+    if (h.first_hang != LLONG_MAX) {
+        res->status = RBG_ERR_OVERFLOW;   // the reference would loop forever here
+        decode_seq(h.first_hang, n, res);
+        res->diameter = 0;
+        return RBG_OK;
+    }
+    if (h.last_ovf >= 0 || h.last_cycle >= 0) {
+        bool ovf_last = h.last_ovf > h.last_cycle;
+        res->status = ovf_last ? RBG_ERR_OVERFLOW : RBG_ERR_CYCLE;
+        decode_seq(ovf_last ? h.last_ovf : h.last_cycle, n, res);
+    } else {
+        res->status = RBG_OK;
+    }
+    unsigned long long mxv = utype<T>::is_signed ? (unsigned long long)std::max<long long>(h.mx_signed, 0)
+                                                 : h.mx_unsigned;
+    (void)sizeof(TU);
+    res->diameter = mxv ? msb_u64(mxv) : 0;
+    return RBG_OK;
+}
+
+}  // namespace rbg
+
+using namespace rbg;
+
+extern "C" int32_t rbg_version(void) { return 100; }
+
+extern "C" int32_t rbg_fw_dense_workspace_bytes(int32_t dtype, int64_t n, uint32_t mode, int64_t *bytes) {
+    if (!bytes || n < 0 || dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;
+    (void)mode;
+    FwLayout L = fw_layout(n, dtype, dtype_bytes(dtype) == 8);
+    *bytes = (int64_t)L.total;
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_t ld_in, void *out,
+                                int64_t ld_out, uint32_t mode, void *workspace, int64_t workspace_bytes,
+                                rbg_result_t *result, rbg_stream_t stream) {
+    if (!result || n < 0 || (n > 0 && (!in || !out || !workspace)) || ld_in < n || ld_out < n)
+        return RBG_ERR_INVALID;
+    const int bytes = dtype_bytes(dtype);
+    if (bytes == 0) return RBG_ERR_INVALID;
+    if ((mode & RBG_MODE_CYTHON) && dtype != RBG_DTYPE_INT32) return RBG_ERR_INVALID;
+    memset(result, 0, sizeof(*result));
+    result->k = result->i = result->j = -1;
+    if (n == 0) return RBG_OK;
+    FwLayout L = fw_layout(n, dtype, bytes == 8);
+    if (workspace_bytes < (int64_t)L.total) return RBG_ERR_NOMEM;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned char *ws = reinterpret_cast<unsigned char *>(workspace);
+    int rc = RBG_ERR_INVALID;
+    RBG_DISPATCH_DTYPE(dtype, T,
+        rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out),
+                           ld_out, mode, ws, L, result, s));
+    return rc;
+}

@@ -1,0 +1,11 @@
+"""GPU drop-in for ``redblackgraph.sparse.csgraph``'s closure functions."""
+from ._shortest_path import shortest_path, floyd_warshall, validate_graph
+from .transitive_closure import (
+    transitive_closure,
+    transitive_closure_floyd_warshall,
+    transitive_closure_dijkstra,
+)
+from .cycleerror import CycleError
+
+__all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
+           "transitive_closure_floyd_warshall", "transitive_closure_dijkstra", "CycleError"]

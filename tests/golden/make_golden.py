@@ -1,0 +1,257 @@
+"""Generate the golden fixtures by running the reference itself.
+
+Run in a container where the reference tree is mounted and built (``python oracle/ref_build.py``):
+
+    python tests/golden/make_golden.py
+
+Every expected value below comes from calling the reference's own code (C core ``warshall``,
+``rb.array @``, ``core.avos_sum/avos_product``, Cython ``floyd_warshall`` and
+``transitive_closure``, C++ ``rb_matrix @``).  Inputs where the reference would never return
+(its MSB loop on a negative signed operand) are detected first with the oracle and recorded
+without a reference answer.  Output: ``tests/golden/golden.npz`` + ``tests/golden/index.json``.
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import scipy.sparse as sp
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import refimport, oracle as O  # noqa: E402
+from redblackgraph_gb300 import synth  # noqa: E402
+
+DTYPES = [np.int8, np.uint8, np.int16, np.uint16, np.int32, np.uint32, np.int64, np.uint64]
+
+
+def exc_name(e):
+    return type(e).__name__
+
+
+_CHILD = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from oracle import refimport
+refimport.load()
+import redblackgraph.core as core
+from redblackgraph.core.redblack import array as rb_array
+A = np.load(sys.argv[2])
+try:
+    W, d = core.warshall(np.stack([A, A]).view(rb_array))
+    np.save(sys.argv[3], np.asarray(W[0]))
+    print("OK", int(np.asarray(d).reshape(-1)[0]))
+except Exception as e:
+    print("EXC", type(e).__name__)
+"""
+
+
+def ref_warshall_isolated(A):
+    """Run the reference gufunc in a child process: on an error it calls PyErr_Format from a
+    loop NumPy may run with the GIL released, which can crash the interpreter."""
+    import subprocess
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "a.npy", Path(td) / "w.npy"
+        np.save(fin, A)
+        r = subprocess.run([sys.executable, "-c", _CHILD, str(ROOT), str(fin), str(fout)],
+                           capture_output=True, text=True, timeout=120)
+        out = r.stdout.strip().split()
+        if r.returncode != 0 or not out:
+            return "crash", None, None
+        if out[0] == "OK":
+            return "ok", np.load(fout), int(out[1])
+        return out[1], None, None
+
+
+def main():
+    rbg = refimport.load()
+    import redblackgraph.core as core
+    from redblackgraph.core.redblack import array as rb_array
+    import redblackgraph.sparse.csgraph as csgraph
+    from redblackgraph.sparse import rb_matrix
+
+    arrays = {}
+    index = {"scalar": {}, "warshall": [], "cython": [], "matmul": [], "spgemm": [], "dijkstra": []}
+
+    # ---------------------------------------------------------------- scalar tables
+    r = list(range(-1, 16))
+    prod = np.array([[int(core.avos_product(x, y)) for y in r] for x in r], dtype=np.int64)
+    arrays["scalar_product_table"] = prod
+    r2 = list(range(-1, 4))
+    arrays["scalar_sum_table"] = np.array([[int(core.avos_sum(x, y)) for y in r2] for x in r2], np.int64)
+    index["scalar"]["edge_product"] = [str(9223372036854775807), "2", str(int(core.avos_product(9223372036854775807, 2)))]
+    ovf = []
+    for x, y in [(4294967296, 4294967296), (9223372036854775807, 3)]:
+        try:
+            core.avos_product(x, y)
+            ovf.append([str(x), str(y), "none"])
+        except Exception as e:  # noqa: BLE001
+            ovf.append([str(x), str(y), exc_name(e)])
+    index["scalar"]["overflow"] = ovf
+
+    # ---------------------------------------------------------------- warshall inputs
+    cases = []
+    ex5 = np.array([[-1, 2, 3, 0, 0], [0, -1, 0, 2, 0], [0, 0, 1, 0, 0], [0, 0, 0, -1, 0],
+                    [2, 0, 0, 0, 1]])
+    for dt in DTYPES:
+        cases.append(("example5", ex5.astype(dt)))
+    for n, g, s in [(7, 3, 1), (33, 5, 2), (64, 6, 3), (65, 7, 4), (100, 8, 5), (130, 9, 6),
+                    (200, 10, 7), (257, 12, 8), (300, 25, 9)]:
+        for dt in (np.int32, np.int64, np.uint32, np.int16):
+            cases.append((f"pedigree_n{n}_s{s}", synth.pedigree(n, g, s, dtype=dt)))
+    # the reference's random-test style: triu(randint(0,4), 1) with a +-1 diagonal
+    for seed in (42, 123, 456):
+        rs = np.random.RandomState(seed)
+        A = np.triu(rs.randint(0, 4, size=(20, 20)), k=1)
+        np.fill_diagonal(A, rs.choice([-1, 1], size=20))
+        for dt in (np.int32, np.int64):
+            cases.append((f"randtriu_s{seed}", A.astype(dt)))
+    # cycles
+    cyc = synth.pedigree(40, 6, 11, dtype=np.int32)
+    cyc[3, 30] = 2
+    cases.append(("cycle40", cyc))
+    cyc2 = synth.pedigree(150, 8, 12, dtype=np.int64)
+    cyc2[5, 140] = 3
+    cyc2[140, 5] = 2
+    cases.append(("cycle150", cyc2))
+    # deep chains: overflow / top-bit behaviour at small widths
+    for dt, depth in [(np.uint8, 9), (np.uint16, 17), (np.int8, 6), (np.int16, 14),
+                      (np.uint8, 7), (np.int32, 20)]:
+        n = depth + 1
+        A = np.zeros((n, n), np.int64)
+        np.fill_diagonal(A, [(-1 if i % 2 == 0 else 1) for i in range(n)])
+        for i in range(n - 1):
+            A[i + 1, i] = 2 if i % 2 == 0 else 3
+        cases.append((f"chain_{np.dtype(dt).name}_{depth}", A.astype(dt)))
+    # small error cases the reference answers without crashing (< ~300 cells)
+    c6 = np.zeros((6, 6), np.int64)
+    np.fill_diagonal(c6, [-1, 1, -1, 1, -1, 1])
+    c6[0, 1], c6[1, 2], c6[2, 3], c6[3, 0], c6[4, 0] = 3, 2, 3, 2, 2
+    for dt in (np.int32, np.uint32, np.int64):
+        cases.append(("cycle6", c6.astype(dt)))
+    c12 = synth.pedigree(12, 4, 5, dtype=np.int64)
+    c12[2, 11] = 2
+    cases.append(("cycle12", c12.astype(np.int32)))
+    for dt, depth in [(np.uint8, 8), (np.uint8, 10), (np.uint16, 16), (np.int8, 7), (np.int8, 8),
+                      (np.int16, 15), (np.uint32, 15)]:
+        n = depth + 1
+        A = np.zeros((n, n), np.int64)
+        np.fill_diagonal(A, [(-1 if i % 2 == 0 else 1) for i in range(n)])
+        for i in range(n - 1):
+            A[i + 1, i] = 3 if i % 2 == 0 else 2
+        if dt == np.uint32:   # wide edges: every edge spans 3 generations (values 8..15)
+            for i in range(n - 1):
+                A[i + 1, i] = 8 + (i % 8)
+        cases.append((f"chain3_{np.dtype(dt).name}_{depth}", A.astype(dt)))
+    # overflow and a cycle in one matrix: the reference raises the LAST error it set
+    oc = np.zeros((10, 10), np.int64)
+    np.fill_diagonal(oc, 1)
+    for i in range(9):
+        oc[i + 1, i] = 3
+    oc[0, 9] = 3
+    for dt in (np.uint8, np.int8, np.uint16):
+        cases.append(("ovf_cycle10", oc.astype(dt)))
+    # first-found longer than final (diameter counts values later replaced)
+    A = np.zeros((5, 5), np.int32)
+    np.fill_diagonal(A, [-1, -1, 1, -1, 1])
+    A[0, 1], A[1, 2], A[2, 3], A[0, 4], A[4, 3] = 2, 3, 2, 3, 2
+    cases.append(("first_found", A))
+
+    for ci, (name, A) in enumerate(cases):
+        key = f"w{ci}"
+        arrays[key + "_in"] = A
+        Wo, do, so, info = O.warshall(A)
+        rec = {"key": key, "name": name, "dtype": np.dtype(A.dtype).name, "n": int(A.shape[0])}
+        if info[1] & O.EV_HANG:
+            rec["reference"] = "hang"
+            rec["exception"] = "OverflowError"
+        elif so != 0:
+            kind, W2, d2 = ref_warshall_isolated(A)
+            if kind == "crash":
+                rec["reference"] = "crash"
+                rec["exception"] = {1: "OverflowError", 2: "ValueError"}[so]
+            elif kind == "ok":
+                arrays[key + "_W"] = W2
+                rec["diameter"] = d2
+                rec["exception"] = None
+            else:
+                rec["exception"] = kind
+        else:
+            try:
+                # The reference gufunc stores its diameter as an 8-byte npy_intp into a 4-byte
+                # int32 slot (warshall.c.in:106,146-149) and never advances that pointer over a
+                # batch (:128).  Closing a 2-stack of the same matrix keeps the spill in bounds.
+                W2, d2 = core.warshall(np.stack([A, A]).view(rb_array))
+                arrays[key + "_W"] = np.asarray(W2[0])
+                rec["diameter"] = int(np.asarray(d2).reshape(-1)[0])
+                rec["exception"] = None
+            except Exception as e:  # noqa: BLE001
+                rec["exception"] = exc_name(e)
+        index["warshall"].append(rec)
+
+        # Cython floyd_warshall on the int32 view (what validate_graph makes)
+        if A.dtype == np.int32:
+            for tri in ((False, True) if not np.tril(A, -1).any() else (False,)):
+                rec2 = {"key": key, "name": name, "triangular": tri}
+                try:
+                    W2, d2 = csgraph.floyd_warshall(A.copy(), assume_upper_triangular=tri)
+                    arrays[key + ("_cyT" if tri else "_cy")] = np.asarray(W2)
+                    rec2["diameter"] = int(d2)
+                    rec2["exception"] = None
+                except Exception as e:  # noqa: BLE001
+                    rec2["exception"] = exc_name(e)
+                    rec2["vertex"] = int(getattr(e, "vertex", -1))
+                index["cython"].append(rec2)
+
+    # ---------------------------------------------------------------- dense @
+    mm = [("example5", ex5)]
+    for s in (1, 2):
+        mm.append((f"ped40_s{s}", synth.pedigree(40, 6, s, dtype=np.int64)))
+    for ci, (name, A) in enumerate(mm):
+        for dt in DTYPES:
+            a = A.astype(dt)
+            key = f"m{ci}_{np.dtype(dt).name}"
+            arrays[key + "_in"] = a
+            rec = {"key": key, "name": name}
+            try:
+                C = rb_array(a) @ rb_array(a)
+                arrays[key + "_AA"] = np.asarray(C)
+                rec["exception"] = None
+            except Exception as e:  # noqa: BLE001
+                rec["exception"] = exc_name(e)
+            index["matmul"].append(rec)
+
+    # ---------------------------------------------------------------- rb_matrix @ (C++)
+    for ci, (n, g, s, dt) in enumerate([(50, 6, 1, np.int32), (200, 10, 2, np.int64),
+                                        (300, 12, 3, np.int32), (120, 8, 4, np.uint32)]):
+        M = synth.pedigree_csr(n, g, s, dtype=dt)
+        key = f"s{ci}"
+        arrays[key + "_indptr"], arrays[key + "_indices"], arrays[key + "_data"] = M.indptr, M.indices, M.data
+        R = rb_matrix(M)
+        C = (R @ R).tocsr()
+        C2 = sp.csr_matrix(C)
+        C2.sort_indices()
+        arrays[key + "_C_indptr"], arrays[key + "_C_indices"], arrays[key + "_C_data"] = C2.indptr, C2.indices, C2.data
+        index["spgemm"].append({"key": key, "n": n, "dtype": np.dtype(dt).name})
+
+    # ---------------------------------------------------------------- csgraph 'D' closure
+    for ci, (n, g, s) in enumerate([(60, 6, 21), (150, 9, 22)]):
+        M = synth.pedigree_csr(n, g, s, dtype=np.int32)
+        key = f"d{ci}"
+        arrays[key + "_in"] = M.toarray()
+        res = csgraph.transitive_closure(M, method="D")
+        arrays[key + "_W"] = np.asarray(res.W)
+        index["dijkstra"].append({"key": key, "diameter": int(res.diameter)})
+
+    np.savez_compressed(HERE / "golden.npz", **arrays)
+    (HERE / "index.json").write_text(json.dumps(index, indent=1))
+    print(f"wrote {len(arrays)} arrays, {len(index['warshall'])} warshall cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,34 @@
+"""The C-ABI library loads and exports every entry point include/rbg_gb300.h declares.
+CPU only: no compute call is made."""
+import ctypes
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    text = "\n".join(p.read_text() for p in (ROOT / "include").glob("*.h"))
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rbg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(native):
+    syms = declared_symbols()
+    assert len(syms) >= 6
+    for s in syms:
+        assert hasattr(native, s), s
+
+
+def test_python_binding_covers_header(native):
+    from redblackgraph_gb300 import _lib
+    assert sorted(_lib.exported_symbols()) == declared_symbols()
+
+
+def test_workspace_queries_without_gpu(native):
+    from redblackgraph_gb300 import _lib
+    n = ctypes.c_int64(0)
+    assert native.rbg_fw_dense_workspace_bytes(4, 1000, 0, ctypes.byref(n)) == 0
+    assert n.value >= 1024 * 1024 * 4
+    assert native.rbg_fw_dense_workspace_bytes(99, 10, 0, ctypes.byref(n)) == _lib.RBG_ERR_INVALID
+    assert native.rbg_version() > 0

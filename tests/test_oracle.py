@@ -1,0 +1,102 @@
+"""The CPU oracle against the reference's own answers (golden fixtures made by running the
+reference, tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+EXC = {0: None, 1: "OverflowError", 2: "ValueError"}
+
+
+def test_product_table(golden):
+    arrays, _ = golden
+    exp = arrays["scalar_product_table"]
+    r = range(-1, 16)
+    got = np.array([[O.avos_product(x, y, np.int64)[0] for y in r] for x in r], dtype=np.uint64)
+    assert (got.astype(np.int64) == exp).all()
+
+
+def test_sum_table(golden):
+    arrays, _ = golden
+    exp = arrays["scalar_sum_table"]
+    r = range(-1, 4)
+    got = np.array([[O.avos_sum(x, y, np.int64) for y in r] for x in r])
+    assert (got == exp).all()
+
+
+def test_edge_and_overflow(golden):
+    _, index = golden
+    x, y, z = index["scalar"]["edge_product"]
+    v, ev = O.avos_product(int(x), int(y), np.uint64)
+    assert v == int(z) and ev == 0
+    for x, y, exc in index["scalar"]["overflow"]:
+        v, ev = O.avos_product(int(x), int(y), np.uint64)
+        assert (ev & (O.EV_OVF_SIZE | O.EV_OVF_ONES)) != 0
+        assert exc == "OverflowError"
+
+
+def test_cython_scalar_matches_core_on_small_values():
+    for x in range(-1, 40):
+        for y in range(-1, 40):
+            v, ev = O.avos_product(x, y, np.int32)
+            assert O.cy_product(x, y) == np.int64(np.uint32(v).view(np.int32))
+            assert O.cy_sum(x, y) == O.avos_sum(x, y, np.int32) or (x < -1 or y < -1)
+
+
+def test_warshall_cases(golden):
+    arrays, index = golden
+    for rec in index["warshall"]:
+        A = arrays[rec["key"] + "_in"]
+        W, d, st, info = O.warshall(A)
+        assert EXC[st] == rec["exception"], rec
+        if rec["exception"] is None:
+            assert (W == arrays[rec["key"] + "_W"]).all(), rec
+            assert d == rec["diameter"], rec
+        if rec.get("reference") == "hang":
+            assert info[1] & O.EV_HANG
+
+
+def test_cython_cases(golden):
+    arrays, index = golden
+    for rec in index["cython"]:
+        A = arrays[rec["key"] + "_in"]
+        W, d, st, info = O.fw_cython(A, triangular=rec["triangular"])
+        if rec["exception"] == "CycleError":
+            assert st == O.RBG_ERR_CYCLE and info[2] == rec["vertex"], rec
+        else:
+            assert st == 0
+            assert (W == arrays[rec["key"] + ("_cyT" if rec["triangular"] else "_cy")]).all(), rec
+            assert d == rec["diameter"], rec
+
+
+def test_matmul_cases(golden):
+    arrays, index = golden
+    for rec in index["matmul"]:
+        A = arrays[rec["key"] + "_in"]
+        C, st, fl = O.matmul(A, A)
+        assert EXC[st] == rec["exception"]
+        if st == 0:
+            assert (C == arrays[rec["key"] + "_AA"]).all(), rec
+
+
+def test_spgemm_cases(golden):
+    import scipy.sparse as sp
+    arrays, index = golden
+    for rec in index["spgemm"]:
+        k = rec["key"]
+        n = rec["n"]
+        M = sp.csr_matrix((arrays[k + "_data"], arrays[k + "_indices"], arrays[k + "_indptr"]),
+                          shape=(n, n))
+        C, fl = O.rb_matmul_csr(M, M)
+        C.sort_indices()
+        assert (C.indptr == arrays[k + "_C_indptr"]).all()
+        assert (C.indices == arrays[k + "_C_indices"]).all()
+        assert (C.data == arrays[k + "_C_data"]).all()
+
+
+def test_warshall_triangular_equals_full_on_upper():
+    from redblackgraph_gb300 import synth
+    A = synth.pedigree(60, 6, 3, dtype=np.int32).T.copy()   # upper triangular
+    W1, d1, s1, _ = O.warshall(A)
+    W2, d2, s2, _ = O.warshall(A, triangular=True)
+    assert (W1 == W2).all() and d1 == d2 and s1 == s2 == 0
