@@ -163,70 +163,118 @@ fw_convert_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, U *__restr
 // kernel A: phase 1 (diagonal tile, recomputed by every CTA in shared memory) + phase 2
 // (one 64 x 128 row-panel tile or one 128 x 64 column-panel tile per CTA)
 // ------------------------------------------------------------------------------------------
+constexpr int PN_THREADS = 128;  // panel kernel: one thread per panel column / row
+constexpr int ROT = 8;           // steps between register rotations
+
 template <typename U> struct PanelSmem {
-    U D[FW_B][FW_B + 1];     // diagonal tile, updated in place
-    U RS[FW_B][FW_B];        // RS[t][b] = row t at step t   (d_{t-1}(t, b))
-    U CS[FW_B][FW_B];        // CS[a][t] = column t at step t (d_{t-1}(a, t))
-    int msbRS[FW_B];         // max msb over valid RS[t][.]
-    int msbCS[FW_B];         // max msb over valid CS[.][t]
-    U P[FW_P * FW_B];        // the panel tile (row panel: [64][128], column panel: [128][64])
+    U CSt[FW_B][2 * FW_B];   // CSt[t][a] = d_{t-1}(a, t); entries a and a + 64 are equal
+    U RSm[FW_B][2 * FW_B];   // d_{t-1}(t, b) split as 2^msb ...             (duplicated
+    U RSl[FW_B][2 * FW_B];   // ... and low bits; zero -> (0, inf)            the same way)
+    int msbRS[FW_B];         // max msb over valid d_{t-1}(t, .)
+    int msbCS[FW_B];         // max msb over valid d_{t-1}(., t)
     int any;
 };
 
+// R[r] <- R[(r + ROT) mod 64]: after q rotations, R[r] holds element (r + ROT q) mod 64, so the
+// element of step t = ROT q + s is always R[s] (a static register index).
+template <typename U> __device__ __forceinline__ void rotate64(U (&R)[FW_B]) {
+    U tmp[ROT];
+#pragma unroll
+    for (int r = 0; r < ROT; ++r) tmp[r] = R[r];
+#pragma unroll
+    for (int r = 0; r < FW_B - ROT; ++r) R[r] = R[r + ROT];
+#pragma unroll
+    for (int r = 0; r < ROT; ++r) R[FW_B - ROT + r] = tmp[r];
+}
+
+template <typename U> __device__ __forceinline__ int msb_or_neg(U v) {
+    return lane<U>::valid(v) ? msb_nz<U>(v) : -100000;
+}
+
+__device__ __forceinline__ void bar_sync_64() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
+// Phase 1: the 64 x 64 diagonal tile in sequential k order, threads 0..63, thread b holding
+// column b in registers.  At step t thread t publishes column t (the snapshot d_{t-1}(., t),
+// invariant during step t); every thread snapshots its row-t element d_{t-1}(t, b).
 template <typename U>
 __device__ void fw_phase1(PanelSmem<U> &S, const U *__restrict__ work, int64_t np, int64_t K0,
-                          int lbits, bool report, unsigned &flags, unsigned long long &mx) {
+                          int lbits, bool report, U *__restrict__ diagbuf, unsigned &flags,
+                          unsigned long long &mx) {
     typedef lane<U> L;
     typedef typename signed_of<U>::type SU;
-    const int tid = threadIdx.x;
-    for (int e = tid; e < FW_B * FW_B; e += FW_THREADS) {
-        int a = e / FW_B, b = e % FW_B;
-        S.D[a][b] = work[(K0 + a) * np + K0 + b];
+    const int b = threadIdx.x;
+    if (b < FW_B) {
+        U R[FW_B];
+#pragma unroll
+        for (int r = 0; r < FW_B; ++r) R[r] = work[(K0 + r) * np + K0 + b];
+        bool risk = false;
+        SU smx = 0;
+        for (int q = 0; q < FW_B / ROT; ++q) {
+            const int off = q * ROT;
+#pragma unroll
+            for (int s = 0; s < ROT; ++s) {
+                const int t = off + s;
+                if (b == t) {
+                    int mc = -100000;
+#pragma unroll
+                    for (int r = 0; r < FW_B; ++r) {
+                        const int a = (r + off) & (FW_B - 1);
+                        S.CSt[t][a] = R[r];
+                        S.CSt[t][a + FW_B] = R[r];
+                        mc = max(mc, msb_or_neg<U>(R[r]));
+                    }
+                    S.msbCS[t] = mc;
+                }
+                const U y = R[s];
+                U m, low;
+                L::split(y, m, low);
+                S.RSm[t][b] = m; S.RSm[t][b + FW_B] = m;
+                S.RSl[t][b] = low; S.RSl[t][b + FW_B] = low;
+                bar_sync_64();
+                if (L::valid(y) && S.msbCS[t] + msb_nz<U>(y) >= lbits - 1) risk = true;
+                const U *col = &S.CSt[t][off];
+#pragma unroll
+                for (int r = 0; r < FW_B; ++r) {
+                    const U v = umin(R[r], col[r] * m + low);
+                    R[r] = v;
+                    smx = max(smx, (SU)v);
+                }
+            }
+            rotate64<U>(R);
+        }
+        // R is back in natural order.  A valid diagonal cell means a cycle.
+        bool cyc = false;
+#pragma unroll
+        for (int r = 0; r < FW_B; ++r) {
+            if (r == b) cyc |= L::valid(R[r]);
+            else if (report) diagbuf[r * FW_B + b] = L::valid(R[r]) ? R[r] : L::inf;
+        }
+        if (report) {
+            diagbuf[b * FW_B + b] = L::inf;   // the diagonal stays encoded zero
+            if (risk) flags |= RBG_EV_RISK;
+            if (cyc) flags |= RBG_EV_CYCLE;
+            if (smx > 0) mx = (unsigned long long)smx;
+        }
     }
     __syncthreads();
-    bool risk = false, cyc = false;
-    SU smx = 0;
-    for (int t = 0; t < FW_B; ++t) {
-        // snapshots: row t and column t do not change at step t (the diagonal is encoded zero)
-        for (int e = tid; e < FW_B; e += FW_THREADS) {
-            S.RS[t][e] = S.D[t][e];
-            S.CS[e][t] = S.D[e][t];
-        }
-        for (int e = tid; e < FW_B * FW_B; e += FW_THREADS) {
-            int a = e / FW_B, b = e % FW_B;
-            if (a == t || b == t) continue;
-            U p = L::product(S.D[a][t], S.D[t][b], lbits, risk);
-            if (a == b) {
-                if (L::valid(p)) cyc = true;
-            } else {
-                U v = umin(S.D[a][b], p);
-                S.D[a][b] = v;
-                smx = max(smx, (SU)v);   // encoded zeros are negative as signed
-            }
-        }
-        __syncthreads();
-    }
-    // per-step maxima of the snapshots, for the risk test of phase 2
-    for (int t = tid; t < FW_B; t += FW_THREADS) {
-        int mr = -1000, mc = -1000;
-        for (int b = 0; b < FW_B; ++b) {
-            U r = S.RS[t][b], c = S.CS[b][t];
-            if (L::valid(r)) mr = max(mr, msb_nz<U>(r));
-            if (L::valid(c)) mc = max(mc, msb_nz<U>(c));
+    for (int t = threadIdx.x; t < FW_B; t += PN_THREADS) {
+        int mr = -100000;
+        for (int c = 0; c < FW_B; ++c) {
+            U rm = S.RSm[t][c];
+            if (rm) mr = max(mr, msb_nz<U>(rm));
         }
         S.msbRS[t] = mr;
-        S.msbCS[t] = mc;
-    }
-    if (report) {
-        if (risk) flags |= RBG_EV_RISK;
-        if (cyc) flags |= RBG_EV_CYCLE;
-        if (smx > 0 && (unsigned long long)smx > mx) mx = (unsigned long long)smx;
     }
     __syncthreads();
 }
 
+// Kernel A: phase 1 (recomputed by every CTA) + phase 2 for one panel tile per CTA:
+// blockIdx.x < ntp: row panel (K, J) columns [128 J, 128 J + 128), thread = column;
+// otherwise column panel (I, K) rows [128 I, 128 I + 128), thread = row.  Each thread runs
+// its own forward substitution over the 64 steps in registers; the snapshots d_{t-1}(t, j)
+// and d_{t-1}(i, t) go to rpbuf / cpbuf (t-major) for phase 3.
 template <typename U>
-__global__ void __launch_bounds__(FW_THREADS)
+__global__ void __launch_bounds__(PN_THREADS)
 fw_panel_kernel(U *__restrict__ work, int64_t np, int64_t K0, U *__restrict__ cpbuf,
                 U *__restrict__ rpbuf, U *__restrict__ diagbuf, int *__restrict__ anyCP,
                 int *__restrict__ anyRP, int lbits, DevStatus *st) {
@@ -240,98 +288,72 @@ fw_panel_kernel(U *__restrict__ work, int64_t np, int64_t K0, U *__restrict__ cp
     const int tile = rowPanel ? blockIdx.x : blockIdx.x - ntp;
     unsigned flags = 0;
     unsigned long long mx = 0;
-
-    fw_phase1<U>(S, work, np, K0, lbits, blockIdx.x == 0, flags, mx);
-    if (blockIdx.x == 0) {
-        // every CTA of this launch reads the diagonal tile from `work`, so its end-of-round
-        // value goes to a side buffer; the phase-3 launch copies it back
-        for (int e = tid; e < FW_B * FW_B; e += FW_THREADS) {
-            int a = e / FW_B, b = e % FW_B;
-            U v = S.D[a][b];
-            diagbuf[e] = lane<U>::valid(v) ? v : lane<U>::inf;
-        }
-    }
     if (tid == 0) S.any = 0;
+    fw_phase1<U>(S, work, np, K0, lbits, blockIdx.x == 0, diagbuf, flags, mx);
+
     const int64_t T0 = (int64_t)tile * FW_P;
-    bool risk = false;
+    const int64_t g = T0 + tid;                       // global column (row panel) / row
+    const bool inK = g >= K0 && g < K0 + FW_B;        // the diagonal tile's own cells
+    bool risk = false, any = false;
     SU smx = 0;
-    int any = 0;
+    U R[FW_B];
     if (rowPanel) {
-        // P[a][j], a in K (64 rows), j in [T0, T0+128); columns inside K are the diagonal tile
-        for (int e = tid; e < FW_B * FW_P; e += FW_THREADS) {
-            int a = e / FW_P, j = e % FW_P;
-            int64_t gj = T0 + j;
-            bool inK = gj >= K0 && gj < K0 + FW_B;
-            S.P[e] = inK ? L::inf : work[(K0 + a) * np + gj];
-        }
-        __syncthreads();
-        const int j = tid % FW_P;           // this thread's column
-        const int a0 = tid / FW_P;          // rows a0, a0+2, ...
-        for (int t = 0; t < FW_B; ++t) {
-            U y = S.P[t * FW_P + j];        // row t is invariant at step t
-            if (a0 == 0) rpbuf[(int64_t)t * np + T0 + j] = y;
-            any |= L::valid(y);
-            U m, low;
-            L::split(y, m, low);
-            if (L::valid(y) && S.msbCS[t] + msb_nz<U>(y) >= lbits - 1) risk = true;
-#pragma unroll 8
-            for (int a = a0; a < FW_B; a += FW_THREADS / FW_P) {
-                if (a == t) continue;
-                U x = S.CS[a][t];
-                U p = L::valid(x) ? L::mul(x, m, low) : L::inf;
-                U v = umin(S.P[a * FW_P + j], p);
-                S.P[a * FW_P + j] = v;
-                smx = max(smx, (SU)v);
+#pragma unroll
+        for (int r = 0; r < FW_B; ++r) R[r] = inK ? L::inf : work[(K0 + r) * np + g];
+        for (int q = 0; q < FW_B / ROT; ++q) {
+            const int off = q * ROT;
+#pragma unroll
+            for (int s = 0; s < ROT; ++s) {
+                const int t = off + s;
+                const U y = R[s];                     // row t is invariant at step t
+                rpbuf[(int64_t)t * np + g] = y;
+                const bool yv = L::valid(y);
+                any |= yv;
+                U m, low;
+                L::split(y, m, low);
+                if (yv && S.msbCS[t] + msb_nz<U>(y) >= lbits - 1) risk = true;
+                const U *col = &S.CSt[t][off];
+#pragma unroll
+                for (int r = 0; r < FW_B; ++r) {
+                    const U v = umin(R[r], col[r] * m + low);
+                    R[r] = v;
+                    smx = max(smx, (SU)v);
+                }
             }
-            __syncthreads();
+            rotate64<U>(R);
         }
-        for (int e = tid; e < FW_B * FW_P; e += FW_THREADS) {
-            int a = e / FW_P, jj = e % FW_P;
-            int64_t gj = T0 + jj;
-            if (!(gj >= K0 && gj < K0 + FW_B)) {
-                U v = S.P[e];
-                work[(K0 + a) * np + gj] = L::valid(v) ? v : L::inf;
-            }
+        if (!inK) {
+#pragma unroll
+            for (int r = 0; r < FW_B; ++r) work[(K0 + r) * np + g] = L::valid(R[r]) ? R[r] : L::inf;
         }
     } else {
-        // P[i][b], i in [T0, T0+128), b in K; rows inside K are the diagonal tile
-        for (int e = tid; e < FW_P * FW_B; e += FW_THREADS) {
-            int i = e / FW_B, b = e % FW_B;
-            int64_t gi = T0 + i;
-            bool inK = gi >= K0 && gi < K0 + FW_B;
-            S.P[e] = inK ? L::inf : work[gi * np + K0 + b];
-        }
-        __syncthreads();
-        const int i = tid % FW_P;           // this thread's row
-        const int b0 = tid / FW_P;          // columns b0, b0+2, ...
-        for (int t = 0; t < FW_B; ++t) {
-            U x = S.P[i * FW_B + t];        // column t is invariant at step t
-            if (b0 == 0) cpbuf[(T0 + i) * FW_B + t] = x;
-            any |= L::valid(x);
-            const bool xv = L::valid(x);
-            if (xv && msb_nz<U>(x) + S.msbRS[t] >= lbits - 1) risk = true;
-#pragma unroll 8
-            for (int b = b0; b < FW_B; b += FW_THREADS / FW_P) {
-                if (b == t) continue;
-                U y = S.RS[t][b];
-                U p = L::inf;
-                if (xv && L::valid(y)) {
-                    int s = msb_nz<U>(y);
-                    p = (x << s) | (y ^ (((U)1) << s));
+        U *row = work + g * np + K0;
+#pragma unroll
+        for (int r = 0; r < FW_B; ++r) R[r] = inK ? L::inf : row[r];
+        for (int q = 0; q < FW_B / ROT; ++q) {
+            const int off = q * ROT;
+#pragma unroll
+            for (int s = 0; s < ROT; ++s) {
+                const int t = off + s;
+                const U x = R[s];                     // column t is invariant at step t
+                cpbuf[(int64_t)t * np + g] = x;
+                const bool xv = L::valid(x);
+                any |= xv;
+                if (xv && msb_nz<U>(x) + S.msbRS[t] >= lbits - 1) risk = true;
+                const U *rm = &S.RSm[t][off];
+                const U *rl = &S.RSl[t][off];
+#pragma unroll
+                for (int r = 0; r < FW_B; ++r) {
+                    const U v = umin(R[r], x * rm[r] + rl[r]);
+                    R[r] = v;
+                    smx = max(smx, (SU)v);
                 }
-                U v = umin(S.P[i * FW_B + b], p);
-                S.P[i * FW_B + b] = v;
-                smx = max(smx, (SU)v);
             }
-            __syncthreads();
+            rotate64<U>(R);
         }
-        for (int e = tid; e < FW_P * FW_B; e += FW_THREADS) {
-            int ii = e / FW_B, b = e % FW_B;
-            int64_t gi = T0 + ii;
-            if (!(gi >= K0 && gi < K0 + FW_B)) {
-                U v = S.P[e];
-                work[gi * np + K0 + b] = L::valid(v) ? v : L::inf;
-            }
+        if (!inK) {
+#pragma unroll
+            for (int r = 0; r < FW_B; ++r) row[r] = L::valid(R[r]) ? R[r] : L::inf;
         }
     }
     if (any) atomicOr(&S.any, 1);
@@ -384,19 +406,11 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
     if (tid == 0) { S.colAny = 0; S.rowAny = 0; S.nactive = 0; }
     __syncthreads();
 
-    // ---- stage the column-panel snapshots (transposed) and row masks
-    for (int r = tid; r < BM; r += FW_THREADS) {
-        unsigned long long m = 0;
-        const U *src = cpbuf + (I0 + r) * FW_B;
-#pragma unroll 4
-        for (int t = 0; t < FW_B; ++t) {
-            U x = src[t];
-            bool v = L::valid(x);
-            S.CPt[t][r] = v ? x : L::inf;
-            m |= (unsigned long long)v << t;
-        }
-        S.maskC[r] = m;
-        if (m) atomicOr(&S.colAny, m);
+    // ---- stage the column-panel snapshots (t-major in global memory: coalesced)
+    for (int e = tid; e < FW_B * BM; e += FW_THREADS) {
+        int t = e / BM, r = e % BM;
+        U x = cpbuf[(int64_t)t * np + I0 + r];
+        S.CPt[t][r] = L::valid(x) ? x : L::inf;
     }
     // ---- stage the row-panel snapshots as (m, low) pairs and column masks
     for (int e = tid; e < FW_B * BN; e += FW_THREADS) {
@@ -408,6 +422,12 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
         S.RPl[t][c] = low;
     }
     __syncthreads();
+    for (int r = tid; r < BM; r += FW_THREADS) {
+        unsigned long long m = 0;
+        for (int t = 0; t < FW_B; ++t) m |= (unsigned long long)L::valid(S.CPt[t][r]) << t;
+        S.maskC[r] = m;
+        if (m) atomicOr(&S.colAny, m);
+    }
     for (int c = tid; c < BN; c += FW_THREADS) {
         unsigned long long m = 0;
         for (int t = 0; t < FW_B; ++t) m |= (unsigned long long)(S.RPm[t][c] != 0) << t;
@@ -760,7 +780,7 @@ static int run_blocked(const T *in, int64_t ld_in, int64_t n, int triangular, un
     const dim3 tgrid((unsigned)(np / C::BN), (unsigned)ntp);
     const size_t psm = panel_smem<U>(), tsm = tile_smem<U, C::BN>();
     for (int64_t K0 = 0; K0 < n; K0 += FW_B) {
-        fw_panel_kernel<U><<<2 * ntp, FW_THREADS, psm, stream>>>(work, np, K0, cp, rp, diag, anyc,
+        fw_panel_kernel<U><<<2 * ntp, PN_THREADS, psm, stream>>>(work, np, K0, cp, rp, diag, anyc,
                                                                  anyr, lbits, st);
         fw_tile_kernel<U, C::BN, C::TM, C::TN><<<tgrid, FW_THREADS, tsm, stream>>>(
             work, np, K0, cp, rp, diag, anyc, anyr, lbits, st);
