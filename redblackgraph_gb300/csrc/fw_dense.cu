@@ -160,209 +160,9 @@ fw_convert_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, U *__restr
 }
 
 // ------------------------------------------------------------------------------------------
-// kernel A: phase 1 (diagonal tile, recomputed by every CTA in shared memory) + phase 2
-// (one 64 x 128 row-panel tile or one 128 x 64 column-panel tile per CTA)
+// phases 1 and 2 (diagonal tile, then the row and column panels)
 // ------------------------------------------------------------------------------------------
-constexpr int PN_THREADS = 128;  // panel kernel: one thread per panel column / row
-constexpr int ROT = 8;           // steps between register rotations
-
-template <typename U> struct PanelSmem {
-    U CSt[FW_B][2 * FW_B];   // CSt[t][a] = d_{t-1}(a, t); entries a and a + 64 are equal
-    U RSm[FW_B][2 * FW_B];   // d_{t-1}(t, b) split as 2^msb ...             (duplicated
-    U RSl[FW_B][2 * FW_B];   // ... and low bits; zero -> (0, inf)            the same way)
-    int msbRS[FW_B];         // max msb over valid d_{t-1}(t, .)
-    int msbCS[FW_B];         // max msb over valid d_{t-1}(., t)
-    int any;
-};
-
-// R[r] <- R[(r + ROT) mod 64]: after q rotations, R[r] holds element (r + ROT q) mod 64, so the
-// element of step t = ROT q + s is always R[s] (a static register index).
-template <typename U> __device__ __forceinline__ void rotate64(U (&R)[FW_B]) {
-    U tmp[ROT];
-#pragma unroll
-    for (int r = 0; r < ROT; ++r) tmp[r] = R[r];
-#pragma unroll
-    for (int r = 0; r < FW_B - ROT; ++r) R[r] = R[r + ROT];
-#pragma unroll
-    for (int r = 0; r < ROT; ++r) R[FW_B - ROT + r] = tmp[r];
-}
-
-template <typename U> __device__ __forceinline__ int msb_or_neg(U v) {
-    return lane<U>::valid(v) ? msb_nz<U>(v) : -100000;
-}
-
-__device__ __forceinline__ void bar_sync_64() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
-
-// Phase 1: the 64 x 64 diagonal tile in sequential k order, threads 0..63, thread b holding
-// column b in registers.  At step t thread t publishes column t (the snapshot d_{t-1}(., t),
-// invariant during step t); every thread snapshots its row-t element d_{t-1}(t, b).
-template <typename U>
-__device__ void fw_phase1(PanelSmem<U> &S, const U *__restrict__ work, int64_t np, int64_t K0,
-                          int lbits, bool report, U *__restrict__ diagbuf, unsigned &flags,
-                          unsigned long long &mx) {
-    typedef lane<U> L;
-    typedef typename signed_of<U>::type SU;
-    const int b = threadIdx.x;
-    if (b < FW_B) {
-        U R[FW_B];
-#pragma unroll
-        for (int r = 0; r < FW_B; ++r) R[r] = work[(K0 + r) * np + K0 + b];
-        bool risk = false;
-        SU smx = 0;
-        for (int q = 0; q < FW_B / ROT; ++q) {
-            const int off = q * ROT;
-#pragma unroll
-            for (int s = 0; s < ROT; ++s) {
-                const int t = off + s;
-                if (b == t) {
-                    int mc = -100000;
-#pragma unroll
-                    for (int r = 0; r < FW_B; ++r) {
-                        const int a = (r + off) & (FW_B - 1);
-                        S.CSt[t][a] = R[r];
-                        S.CSt[t][a + FW_B] = R[r];
-                        mc = max(mc, msb_or_neg<U>(R[r]));
-                    }
-                    S.msbCS[t] = mc;
-                }
-                const U y = R[s];
-                U m, low;
-                L::split(y, m, low);
-                S.RSm[t][b] = m; S.RSm[t][b + FW_B] = m;
-                S.RSl[t][b] = low; S.RSl[t][b + FW_B] = low;
-                bar_sync_64();
-                if (L::valid(y) && S.msbCS[t] + msb_nz<U>(y) >= lbits - 1) risk = true;
-                const U *col = &S.CSt[t][off];
-#pragma unroll
-                for (int r = 0; r < FW_B; ++r) {
-                    const U v = umin(R[r], col[r] * m + low);
-                    R[r] = v;
-                    smx = max(smx, (SU)v);
-                }
-            }
-            rotate64<U>(R);
-        }
-        // R is back in natural order.  A valid diagonal cell means a cycle.
-        bool cyc = false;
-#pragma unroll
-        for (int r = 0; r < FW_B; ++r) {
-            if (r == b) cyc |= L::valid(R[r]);
-            else if (report) diagbuf[r * FW_B + b] = L::valid(R[r]) ? R[r] : L::inf;
-        }
-        if (report) {
-            diagbuf[b * FW_B + b] = L::inf;   // the diagonal stays encoded zero
-            if (risk) flags |= RBG_EV_RISK;
-            if (cyc) flags |= RBG_EV_CYCLE;
-            if (smx > 0) mx = (unsigned long long)smx;
-        }
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < FW_B; t += PN_THREADS) {
-        int mr = -100000;
-        for (int c = 0; c < FW_B; ++c) {
-            U rm = S.RSm[t][c];
-            if (rm) mr = max(mr, msb_nz<U>(rm));
-        }
-        S.msbRS[t] = mr;
-    }
-    __syncthreads();
-}
-
-// Kernel A: phase 1 (recomputed by every CTA) + phase 2 for one panel tile per CTA:
-// blockIdx.x < ntp: row panel (K, J) columns [128 J, 128 J + 128), thread = column;
-// otherwise column panel (I, K) rows [128 I, 128 I + 128), thread = row.  Each thread runs
-// its own forward substitution over the 64 steps in registers; the snapshots d_{t-1}(t, j)
-// and d_{t-1}(i, t) go to rpbuf / cpbuf (t-major) for phase 3.
-template <typename U>
-__global__ void __launch_bounds__(PN_THREADS)
-fw_panel_kernel(U *__restrict__ work, int64_t np, int64_t K0, U *__restrict__ cpbuf,
-                U *__restrict__ rpbuf, U *__restrict__ diagbuf, int *__restrict__ anyCP,
-                int *__restrict__ anyRP, int lbits, DevStatus *st) {
-    typedef lane<U> L;
-    typedef typename signed_of<U>::type SU;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
-    const int tid = threadIdx.x;
-    const int ntp = (int)(np / FW_P);
-    const bool rowPanel = blockIdx.x < (unsigned)ntp;
-    const int tile = rowPanel ? blockIdx.x : blockIdx.x - ntp;
-    unsigned flags = 0;
-    unsigned long long mx = 0;
-    if (tid == 0) S.any = 0;
-    fw_phase1<U>(S, work, np, K0, lbits, blockIdx.x == 0, diagbuf, flags, mx);
-
-    const int64_t T0 = (int64_t)tile * FW_P;
-    const int64_t g = T0 + tid;                       // global column (row panel) / row
-    const bool inK = g >= K0 && g < K0 + FW_B;        // the diagonal tile's own cells
-    bool risk = false, any = false;
-    SU smx = 0;
-    U R[FW_B];
-    if (rowPanel) {
-#pragma unroll
-        for (int r = 0; r < FW_B; ++r) R[r] = inK ? L::inf : work[(K0 + r) * np + g];
-        for (int q = 0; q < FW_B / ROT; ++q) {
-            const int off = q * ROT;
-#pragma unroll
-            for (int s = 0; s < ROT; ++s) {
-                const int t = off + s;
-                const U y = R[s];                     // row t is invariant at step t
-                rpbuf[(int64_t)t * np + g] = y;
-                const bool yv = L::valid(y);
-                any |= yv;
-                U m, low;
-                L::split(y, m, low);
-                if (yv && S.msbCS[t] + msb_nz<U>(y) >= lbits - 1) risk = true;
-                const U *col = &S.CSt[t][off];
-#pragma unroll
-                for (int r = 0; r < FW_B; ++r) {
-                    const U v = umin(R[r], col[r] * m + low);
-                    R[r] = v;
-                    smx = max(smx, (SU)v);
-                }
-            }
-            rotate64<U>(R);
-        }
-        if (!inK) {
-#pragma unroll
-            for (int r = 0; r < FW_B; ++r) work[(K0 + r) * np + g] = L::valid(R[r]) ? R[r] : L::inf;
-        }
-    } else {
-        U *row = work + g * np + K0;
-#pragma unroll
-        for (int r = 0; r < FW_B; ++r) R[r] = inK ? L::inf : row[r];
-        for (int q = 0; q < FW_B / ROT; ++q) {
-            const int off = q * ROT;
-#pragma unroll
-            for (int s = 0; s < ROT; ++s) {
-                const int t = off + s;
-                const U x = R[s];                     // column t is invariant at step t
-                cpbuf[(int64_t)t * np + g] = x;
-                const bool xv = L::valid(x);
-                any |= xv;
-                if (xv && msb_nz<U>(x) + S.msbRS[t] >= lbits - 1) risk = true;
-                const U *rm = &S.RSm[t][off];
-                const U *rl = &S.RSl[t][off];
-#pragma unroll
-                for (int r = 0; r < FW_B; ++r) {
-                    const U v = umin(R[r], x * rm[r] + rl[r]);
-                    R[r] = v;
-                    smx = max(smx, (SU)v);
-                }
-            }
-            rotate64<U>(R);
-        }
-        if (!inK) {
-#pragma unroll
-            for (int r = 0; r < FW_B; ++r) row[r] = L::valid(R[r]) ? R[r] : L::inf;
-        }
-    }
-    if (any) atomicOr(&S.any, 1);
-    __syncthreads();
-    if (tid == 0) (rowPanel ? anyRP : anyCP)[tile] = S.any;
-    if (risk) flags |= RBG_EV_RISK;
-    if (smx > 0 && (unsigned long long)smx > mx) mx = (unsigned long long)smx;
-    flush_status(st, mx, flags);
-}
+#include "fw_panels.cuh"
 
 // ------------------------------------------------------------------------------------------
 // kernel B: phase 3 over BM x BN tiles, register micro-tiles TM x TN, 256 threads
@@ -382,9 +182,8 @@ template <typename U, int BN> struct TileSmem {
 template <typename U, int BN, int TM, int TN>
 __global__ void __launch_bounds__(FW_THREADS)
 fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict__ cpbuf,
-               const U *__restrict__ rpbuf, const U *__restrict__ diagbuf,
-               const int *__restrict__ anyCP, const int *__restrict__ anyRP, int lbits,
-               DevStatus *st) {
+               const U *__restrict__ rpbuf, const int *__restrict__ anyCP,
+               const int *__restrict__ anyRP, int lbits, DevStatus *st) {
     typedef lane<U> L;
     constexpr int BM = FW_P;
     constexpr int TX = BN / TN;           // threads along columns
@@ -395,31 +194,47 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
     TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
 
     const int tI = blockIdx.y, tJ = blockIdx.x;
-    if (tI == 0 && tJ == 0) {
-        // end-of-round diagonal tile from the panel launch (no other CTA stores those cells)
-        for (int e = threadIdx.x; e < FW_B * FW_B; e += FW_THREADS)
-            work[(K0 + e / FW_B) * np + K0 + e % FW_B] = diagbuf[e];
-    }
     if (!anyCP[tI] || !anyRP[(int)(((int64_t)tJ * BN) / FW_P)]) return;
     const int64_t I0 = (int64_t)tI * BM, J0 = (int64_t)tJ * BN;
     const int tid = threadIdx.x;
     if (tid == 0) { S.colAny = 0; S.rowAny = 0; S.nactive = 0; }
     __syncthreads();
 
-    // ---- stage the column-panel snapshots (t-major in global memory: coalesced)
-    for (int e = tid; e < FW_B * BM; e += FW_THREADS) {
-        int t = e / BM, r = e % BM;
-        U x = cpbuf[(int64_t)t * np + I0 + r];
-        S.CPt[t][r] = L::valid(x) ? x : L::inf;
-    }
-    // ---- stage the row-panel snapshots as (m, low) pairs and column masks
-    for (int e = tid; e < FW_B * BN; e += FW_THREADS) {
-        int t = e / BN, c = e % BN;
-        U y = rpbuf[(int64_t)t * np + J0 + c];
-        U m, low;
-        L::split(y, m, low);
-        S.RPm[t][c] = m;
-        S.RPl[t][c] = low;
+    // ---- stage the panel snapshots: batched 16-byte loads, then shared-memory stores
+    {
+        constexpr int PER = 16 / sizeof(U);
+        constexpr int NC = FW_B * BM / PER / FW_THREADS;      // column-panel vectors per thread
+        constexpr int NR = FW_B * BN / PER / FW_THREADS;      // row-panel vectors per thread
+        uint4 vc[NC], vr[NR];
+#pragma unroll
+        for (int i = 0; i < NC; ++i) {
+            const int e = tid + i * FW_THREADS, t = e / (BM / PER), r = (e % (BM / PER)) * PER;
+            vc[i] = *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r);
+        }
+#pragma unroll
+        for (int i = 0; i < NR; ++i) {
+            const int e = tid + i * FW_THREADS, t = e / (BN / PER), c = (e % (BN / PER)) * PER;
+            vr[i] = *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c);
+        }
+#pragma unroll
+        for (int i = 0; i < NC; ++i) {
+            const int e = tid + i * FW_THREADS, t = e / (BM / PER), r = (e % (BM / PER)) * PER;
+            const U *w = reinterpret_cast<const U *>(&vc[i]);
+#pragma unroll
+            for (int k = 0; k < PER; ++k) S.CPt[t][r + k] = L::valid(w[k]) ? w[k] : L::inf;
+        }
+#pragma unroll
+        for (int i = 0; i < NR; ++i) {
+            const int e = tid + i * FW_THREADS, t = e / (BN / PER), c = (e % (BN / PER)) * PER;
+            const U *w = reinterpret_cast<const U *>(&vr[i]);
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                U m, low;
+                L::split(w[k], m, low);
+                S.RPm[t][c + k] = m;
+                S.RPl[t][c + k] = low;
+            }
+        }
     }
     __syncthreads();
     for (int r = tid; r < BM; r += FW_THREADS) {
@@ -468,14 +283,20 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
     for (int c = 0; c < TN; ++c) cidx[c] = (c < HN) ? tx * HN + c : BN / 2 + tx * HN + (c - HN);
     U acc[TM][TN];
     unsigned long long wasInf = 0;
+    static_assert(HN * sizeof(U) == 16, "each column group is one 16-byte vector");
 #pragma unroll
     for (int r = 0; r < TM; ++r) {
         const U *row = work + (I0 + r0 + r) * np + J0;
 #pragma unroll
-        for (int c = 0; c < TN; ++c) {
-            U v = row[cidx[c]];
-            acc[r][c] = v;
-            wasInf |= (unsigned long long)(!L::valid(v)) << (r * TN + c);
+        for (int half = 0; half < 2; ++half) {
+            uint4 v4 = *reinterpret_cast<const uint4 *>(row + cidx[half * HN]);
+            const U *w = reinterpret_cast<const U *>(&v4);
+#pragma unroll
+            for (int k = 0; k < HN; ++k) {
+                const int c = half * HN + k;
+                acc[r][c] = w[k];
+                wasInf |= (unsigned long long)(!L::valid(w[k])) << (r * TN + c);
+            }
         }
     }
 
@@ -496,28 +317,34 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
     // ---- write back, cycle test on the global diagonal, first values for the running max
     unsigned flags = risk ? RBG_EV_RISK : 0u;
     unsigned long long mx = 0;
+    // Cells of the row/column panel (in K) saw only encoded-zero products, so their
+    // accumulators still hold what the panel launch stored: writing them back is a no-op.
 #pragma unroll
     for (int r = 0; r < TM; ++r) {
         const int64_t gi = I0 + r0 + r;
-        const bool rowInK = gi >= K0 && gi < K0 + FW_B;
         U *row = work + gi * np + J0;
 #pragma unroll
-        for (int c = 0; c < TN; ++c) {
-            const int64_t gj = J0 + cidx[c];
-            if (rowInK || (gj >= K0 && gj < K0 + FW_B)) continue;
-            U v = acc[r][c];
-            const bool valid = L::valid(v);
-            if (gi == gj) {
-                if (valid) flags |= RBG_EV_CYCLE;
-                continue;   // the diagonal stays encoded zero
+        for (int half = 0; half < 2; ++half) {
+            uint4 v4;
+            U *w = reinterpret_cast<U *>(&v4);
+#pragma unroll
+            for (int k = 0; k < HN; ++k) {
+                const int c = half * HN + k;
+                const int64_t gj = J0 + cidx[c];
+                U v = acc[r][c];
+                const bool valid = L::valid(v);
+                if (gi == gj) {
+                    if (valid) flags |= RBG_EV_CYCLE;
+                    v = L::inf;   // the diagonal stays encoded zero
+                } else if (valid && ((wasInf >> (r * TN + c)) & 1ull)) {
+                    unsigned long long both = S.maskC[r0 + r] & S.maskR[cidx[c]];
+                    int kf = __ffsll((long long)both) - 1;
+                    U first = S.CPt[kf][r0 + r] * S.RPm[kf][cidx[c]] + S.RPl[kf][cidx[c]];
+                    if ((unsigned long long)first > mx) mx = (unsigned long long)first;
+                }
+                w[k] = L::valid(v) ? v : L::inf;
             }
-            if (valid && ((wasInf >> (r * TN + c)) & 1ull)) {
-                unsigned long long both = S.maskC[r0 + r] & S.maskR[cidx[c]];
-                int kf = __ffsll((long long)both) - 1;
-                U first = S.CPt[kf][r0 + r] * S.RPm[kf][cidx[c]] + S.RPl[kf][cidx[c]];
-                if ((unsigned long long)first > mx) mx = (unsigned long long)first;
-            }
-            row[cidx[c]] = valid ? v : L::inf;
+            *reinterpret_cast<uint4 *>(row + cidx[half * HN]) = v4;
         }
     }
     flush_status(st, mx, flags);
@@ -713,7 +540,7 @@ static FwLayout fw_layout(int64_t n, int dtype, bool wide_possible) {
     L.off_work = o; o = align_up(o + (size_t)L.np * L.np * ub, 256);
     L.off_cp = o; o = align_up(o + (size_t)L.np * FW_B * ub, 256);
     L.off_rp = o; o = align_up(o + (size_t)L.np * FW_B * ub, 256);
-    L.off_diag = o; o = align_up(o + (size_t)FW_B * FW_B * ub, 256);
+    L.off_diag = o; o = align_up(o + sizeof(RoundBuf<uint64_t>), 256);
     L.off_anyc = o; o = align_up(o + (size_t)(L.np / FW_P) * 4, 256);
     L.off_anyr = o; o = align_up(o + (size_t)(L.np / FW_P) * 4, 256);
     L.off_exact = o; o = align_up(o + 3 * align_up((size_t)n, 32) * dtype_bytes(dtype) + 256, 256);
@@ -739,6 +566,8 @@ static int configure_kernels() {
     typedef TileCfg<U> C;
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)panel_smem<U>()));
+    RBG_CUDA_TRY(cudaFuncSetAttribute(fw_diag_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(DiagSmem<U>)));
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_tile_kernel<U, C::BN, C::TM, C::TN>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)tile_smem<U, C::BN>()));
@@ -761,7 +590,7 @@ static int run_blocked(const T *in, int64_t ld_in, int64_t n, int triangular, un
     U *work = reinterpret_cast<U *>(ws + Ly.off_work);
     U *cp = reinterpret_cast<U *>(ws + Ly.off_cp);
     U *rp = reinterpret_cast<U *>(ws + Ly.off_rp);
-    U *diag = reinterpret_cast<U *>(ws + Ly.off_diag);
+    RoundBuf<U> *rb = reinterpret_cast<RoundBuf<U> *>(ws + Ly.off_diag);
     int *anyc = reinterpret_cast<int *>(ws + Ly.off_anyc);
     int *anyr = reinterpret_cast<int *>(ws + Ly.off_anyr);
     const int64_t np = Ly.np;
@@ -780,10 +609,12 @@ static int run_blocked(const T *in, int64_t ld_in, int64_t n, int triangular, un
     const dim3 tgrid((unsigned)(np / C::BN), (unsigned)ntp);
     const size_t psm = panel_smem<U>(), tsm = tile_smem<U, C::BN>();
     for (int64_t K0 = 0; K0 < n; K0 += FW_B) {
-        fw_panel_kernel<U><<<2 * ntp, PN_THREADS, psm, stream>>>(work, np, K0, cp, rp, diag, anyc,
-                                                                 anyr, lbits, st);
+        fw_diag_kernel<U><<<1, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(work, np, K0, rb, lbits, st);
+        RBG_CUDA_TRY(cudaMemsetAsync(anyc, 0, 2 * align_up((size_t)ntp * 4, 256), stream));
+        fw_panel_kernel<U><<<2 * (int)(np / PN_LINES), PN_THREADS, psm, stream>>>(
+            work, np, K0, rb, cp, rp, anyc, anyr, lbits, st);
         fw_tile_kernel<U, C::BN, C::TM, C::TN><<<tgrid, FW_THREADS, tsm, stream>>>(
-            work, np, K0, cp, rp, diag, anyc, anyr, lbits, st);
+            work, np, K0, cp, rp, anyc, anyr, lbits, st);
     }
     RBG_CUDA_TRY(cudaGetLastError());
     return read_status(st, h, stream);

@@ -1,0 +1,317 @@
+// fw_panels.cuh -- phases 1 and 2 of the snapshot-exact blocked Floyd-Warshall round.
+// Included by fw_dense.cu (which defines FW_B, FW_P, lane<>, umin, flush_status, DevStatus).
+//
+// Phase 1 (fw_diag_kernel, one CTA per round): the 64 x 64 diagonal tile in sequential k order.
+//   It writes the tile's end-of-round values and, into a round buffer, the snapshots
+//       cs[t][a] = d_{t-1}(a, t)   (column t as step t reads it)
+//       rs(t, b) = d_{t-1}(t, b)   (row t as step t reads it), stored split as (2^msb, low)
+//   with per-step maxima of msb (for the exact top-bit test) and validity masks.
+// Phase 2 (fw_panel_kernel, 64 panel columns or rows per CTA): each panel column (row panel) or
+//   row (column panel) is held in registers by four lanes and runs its forward substitution
+//       P(a, j) <- P(a, j) (+) cs[t][a] (x) P(t, j)      (row panel, t = K0..K0+63)
+//       P(i, b) <- P(i, b) (+) P(i, t) (x) rs(t, b)      (column panel)
+//   storing the step-t operands P(t, j) / P(i, t) (the phase-3 snapshots) t-major.
+#pragma once
+
+constexpr int DG_THREADS = 256;   // phase 1: 4 threads per column, 16 rows each
+constexpr int DG_ROWS = 16;
+
+// Round buffer (global memory, written by phase 1, read by phase 2).
+template <typename U> struct RoundBuf {
+    U cs[FW_B][FW_B];                 // cs[t][a]
+    U rsm[FW_B][FW_B];                // rsm[t][b] = 2^msb(rs(t,b)), 0 for zero
+    U rsl[FW_B][FW_B];                // rsl[t][b] = rs(t,b) - 2^msb, inf for zero
+    unsigned long long maskCS[FW_B];  // maskCS[a] bit t: cs[t][a] valid
+    unsigned long long maskRS[FW_B];  // maskRS[b] bit t: rs(t,b) valid
+    int msbCS[FW_B];                  // max msb over valid cs[t][.]
+    int msbRS[FW_B];                  // max msb over valid rs(t, .)
+};
+
+template <typename U> __device__ __forceinline__ int msb_or_neg(U v) {
+    return lane<U>::valid(v) ? msb_nz<U>(v) : -100000;
+}
+
+// Shared tables are read by four lane groups at element offsets 0, 16, 32, 48.  Padding each
+// 16-element group by one 16-byte vector puts the four groups' vectors in distinct banks.
+template <typename U> struct Pad {
+    static constexpr int P = 16 / (int)sizeof(U);
+    static constexpr int LD = FW_B + 4 * P;
+    __device__ __forceinline__ static int at(int c) { return c + P * (c >> 4); }
+};
+
+// 16 consecutive lane words from 16-byte aligned shared memory
+template <typename U> __device__ __forceinline__ void load16(const U *p, U (&x)[DG_ROWS]) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+    constexpr int PER = 16 / sizeof(U);
+#pragma unroll
+    for (int i = 0; i < DG_ROWS / PER; ++i) {
+        uint4 v = q[i];
+        const U *w = reinterpret_cast<const U *>(&v);
+#pragma unroll
+        for (int k = 0; k < PER; ++k) x[i * PER + k] = w[k];
+    }
+}
+
+// ------------------------------------------------------------------------------ phase 1
+template <typename U> struct DiagSmem {
+    U CS[FW_B][Pad<U>::LD];           // CS[t][Pad::at(a)]
+    U Y[FW_B][FW_B];                  // Y[t][b] = rs(t, b)
+    typename signed_of<U>::type colmax[FW_B][DG_THREADS / FW_B];
+};
+
+// Thread (b = tid % 64, h = tid / 64) holds rows a = 16 h + l (l = 0..15) of column b.  Steps
+// run in blocks of 16, fully unrolled, so the row of step t is the static register R[t % 16]
+// of the threads with h = t / 16.  One barrier per step: step t's writes go to slot t only.
+template <typename U>
+__global__ void __launch_bounds__(DG_THREADS)
+fw_diag_kernel(U *__restrict__ work, int64_t np, int64_t K0, RoundBuf<U> *__restrict__ rb,
+               int lbits, DevStatus *st) {
+    typedef lane<U> L;
+    typedef typename signed_of<U>::type SU;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DiagSmem<U> &S = *reinterpret_cast<DiagSmem<U> *>(smem_raw);
+    const int tid = threadIdx.x;
+    const int b = tid % FW_B, h = tid / FW_B;
+    U R[DG_ROWS];
+#pragma unroll
+    for (int l = 0; l < DG_ROWS; ++l) R[l] = work[(K0 + h * DG_ROWS + l) * np + K0 + b];
+    bool risk = false;
+    SU pm[4] = {0, 0, 0, 0};
+    for (int T = 0; T < FW_B / DG_ROWS; ++T) {
+#pragma unroll
+        for (int l = 0; l < DG_ROWS; ++l) {
+            const int t = T * DG_ROWS + l;
+            if (b == t) {   // publish column t (invariant during step t)
+                SU cm = -1;
+#pragma unroll
+                for (int r = 0; r < DG_ROWS; ++r) {
+                    S.CS[t][Pad<U>::at(h * DG_ROWS) + r] = R[r];
+                    cm = max(cm, (SU)R[r]);
+                }
+                S.colmax[t][h] = cm;
+            }
+            if (h == T) S.Y[t][b] = R[l];   // row t (invariant during step t)
+            __syncthreads();
+            const U y = S.Y[t][b];
+            U m, low;
+            L::split(y, m, low);
+            SU cm = max(max(S.colmax[t][0], S.colmax[t][1]), max(S.colmax[t][2], S.colmax[t][3]));
+            if (L::valid(y) && cm > 0 && msb_nz<U>((U)cm) + msb_nz<U>(y) >= lbits - 1) risk = true;
+            U x[DG_ROWS];
+            load16<U>(&S.CS[t][Pad<U>::at(h * DG_ROWS)], x);
+#pragma unroll
+            for (int r = 0; r < DG_ROWS; ++r) {
+                const U v = umin(R[r], x[r] * m + low);
+                R[r] = v;
+                pm[r & 3] = max(pm[r & 3], (SU)v);
+            }
+        }
+    }
+    // end-of-round tile; a valid diagonal cell means a cycle
+    bool cyc = false;
+#pragma unroll
+    for (int r = 0; r < DG_ROWS; ++r) {
+        const int a = h * DG_ROWS + r;
+        U v = R[r];
+        if (a == b) {
+            cyc |= L::valid(v);
+            v = L::inf;
+        }
+        work[(K0 + a) * np + K0 + b] = L::valid(v) ? v : L::inf;
+    }
+    __syncthreads();
+    // round buffer: snapshots, splits, masks and per-step maxima
+    for (int e = tid; e < FW_B * FW_B; e += DG_THREADS) {
+        const int t = e / FW_B, c = e % FW_B;
+        const U x = S.CS[t][Pad<U>::at(c)];
+        rb->cs[t][c] = L::valid(x) ? x : L::inf;
+        U m, low;
+        L::split(S.Y[t][c], m, low);
+        rb->rsm[t][c] = m;
+        rb->rsl[t][c] = low;
+    }
+    if (tid < FW_B) {
+        unsigned long long mc = 0, mr = 0;
+        int bc = -100000, br = -100000;
+        for (int t = 0; t < FW_B; ++t) {
+            const U x = S.CS[t][Pad<U>::at(tid)], y = S.Y[t][tid];
+            mc |= (unsigned long long)L::valid(x) << t;
+            mr |= (unsigned long long)L::valid(y) << t;
+            bc = max(bc, msb_or_neg<U>(S.CS[tid][Pad<U>::at(t)]));   // step tid's maximum
+            br = max(br, msb_or_neg<U>(S.Y[tid][t]));
+        }
+        rb->maskCS[tid] = mc;
+        rb->maskRS[tid] = mr;
+        rb->msbCS[tid] = bc;
+        rb->msbRS[tid] = br;
+    }
+    SU smx = max(max(pm[0], pm[1]), max(pm[2], pm[3]));
+    unsigned flags = (risk ? RBG_EV_RISK : 0u) | (cyc ? RBG_EV_CYCLE : 0u);
+    flush_status(st, smx > 0 ? (unsigned long long)smx : 0ull, flags);
+}
+
+// ------------------------------------------------------------------------------ phase 2
+// Four lanes of a warp share one panel column (row panel) or row (column panel), 16 cells
+// each.  The step-t operand P(t, j) / P(i, t) lives in lane h = t / 16 of the group and is
+// broadcast with a shuffle, so the 64 steps need no barrier.  Steps run in fully unrolled
+// blocks of 16, keeping every register index static.
+constexpr int PN_LINES = 64;                      // panel columns / rows per CTA
+constexpr int PN_THREADS = PN_LINES * 4;
+
+template <typename U> struct PanelSmem {
+    U CS[FW_B][Pad<U>::LD];           // row panel:    cs[t][a]    (padded)
+    U RSm[FW_B][Pad<U>::LD];          // column panel: rsm[t][b]   (padded)
+    U RSl[FW_B][Pad<U>::LD];          //               rsl[t][b]   (padded)
+    unsigned long long maskCS[FW_B];
+    unsigned long long maskRS[FW_B];
+    int msbCS[FW_B];
+    int msbRS[FW_B];
+    U Z[FW_B][PN_LINES];              // Z[t][line]: the line's step-t operand (its snapshot)
+    int any;
+};
+
+template <typename U> __device__ __forceinline__ U shfl_lane(U v, int src) {
+    if (sizeof(U) == 8) {
+        unsigned long long x = (unsigned long long)v;
+        return (U)__shfl_sync(0xffffffffu, x, src);
+    }
+    return (U)__shfl_sync(0xffffffffu, (unsigned)v, src);
+}
+
+template <typename U>
+__global__ void __launch_bounds__(PN_THREADS, 2)
+fw_panel_kernel(U *__restrict__ work, int64_t np, int64_t K0, const RoundBuf<U> *__restrict__ rb,
+                U *__restrict__ cpbuf, U *__restrict__ rpbuf, int *__restrict__ anyCP,
+                int *__restrict__ anyRP, int lbits, DevStatus *st) {
+    typedef lane<U> L;
+    typedef typename signed_of<U>::type SU;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
+    const int tid = threadIdx.x;
+    const int nct = (int)(np / PN_LINES);             // CTAs per panel
+    const bool rowPanel = blockIdx.x < (unsigned)nct;
+    const int cta = rowPanel ? blockIdx.x : blockIdx.x - nct;
+    if (tid == 0) S.any = 0;
+    {
+        // batched 16-byte loads first, then the shared-memory stores (no serial round trips)
+        constexpr int PER = 16 / sizeof(U);
+        constexpr int NV = FW_B * FW_B / PER / PN_THREADS;   // vectors per table per thread
+        uint4 va[NV], vb[NV];
+        const uint4 *ta = reinterpret_cast<const uint4 *>(rowPanel ? &rb->cs[0][0] : &rb->rsm[0][0]);
+        const uint4 *tb = reinterpret_cast<const uint4 *>(&rb->rsl[0][0]);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            va[i] = ta[tid + i * PN_THREADS];
+            if (!rowPanel) vb[i] = tb[tid + i * PN_THREADS];
+        }
+        U *da = rowPanel ? &S.CS[0][0] : &S.RSm[0][0];
+        U *db = &S.RSl[0][0];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const int e = (tid + i * PN_THREADS) * PER, t = e / FW_B, c = e % FW_B;
+            const int o = t * Pad<U>::LD + Pad<U>::at(c);
+            *reinterpret_cast<uint4 *>(da + o) = va[i];
+            if (!rowPanel) *reinterpret_cast<uint4 *>(db + o) = vb[i];
+        }
+    }
+    if (tid < FW_B) {
+        S.maskCS[tid] = rb->maskCS[tid];
+        S.maskRS[tid] = rb->maskRS[tid];
+        S.msbCS[tid] = rb->msbCS[tid];
+        S.msbRS[tid] = rb->msbRS[tid];
+    }
+    __syncthreads();
+
+    const int lanei = tid & 31;
+    const int h = lanei & 3;                          // cells h*16 .. h*16+15 of the line
+    const int grp = lanei & ~3;                       // first lane of this line's group
+    const int64_t g = (int64_t)cta * PN_LINES + (tid >> 2);   // global column / row
+    const bool inK = g >= K0 && g < K0 + FW_B;        // the diagonal tile's own cells
+    const int c0 = h * DG_ROWS;
+    bool risk = false;
+    unsigned long long seen = 0;                      // bit t: the step-t operand is valid
+    unsigned startInf = 0;                            // bit r: cell r was zero at round start
+    U R[DG_ROWS];
+    U *rowp = work + g * np + K0 + c0;                // column panel: this thread's cells
+    if (inK) {
+#pragma unroll
+        for (int r = 0; r < DG_ROWS; ++r) R[r] = L::inf;
+    } else if (rowPanel) {
+#pragma unroll
+        for (int r = 0; r < DG_ROWS; ++r) R[r] = work[(K0 + c0 + r) * np + g];
+    } else {
+        load16<U>(rowp, R);   // 16-byte aligned: K0 and c0 are multiples of 16
+    }
+#pragma unroll
+    for (int r = 0; r < DG_ROWS; ++r) startInf |= (unsigned)(!L::valid(R[r])) << r;
+    const int pc0 = Pad<U>::at(c0);
+    const U *tabA = rowPanel ? &S.CS[0][pc0] : &S.RSm[0][pc0];
+    const U *tabB = &S.RSl[0][pc0];
+    for (int T = 0; T < FW_B / DG_ROWS; ++T) {
+        // operands of step t are loaded one step ahead (registers double-buffered)
+        U xa[2][DG_ROWS], xb[2][DG_ROWS];
+        load16<U>(tabA + (T * DG_ROWS) * Pad<U>::LD, xa[0]);
+        if (!rowPanel) load16<U>(tabB + (T * DG_ROWS) * Pad<U>::LD, xb[0]);
+#pragma unroll
+        for (int l = 0; l < DG_ROWS; ++l) {
+            const int t = T * DG_ROWS + l;
+            const int cur = l & 1, nxt = cur ^ 1;
+            if (l + 1 < DG_ROWS) {
+                load16<U>(tabA + (t + 1) * Pad<U>::LD, xa[nxt]);
+                if (!rowPanel) load16<U>(tabB + (t + 1) * Pad<U>::LD, xb[nxt]);
+            }
+            const U z = shfl_lane<U>(R[l], grp | T);  // P(t, j) or P(i, t): invariant at step t
+            const bool zv = L::valid(z);
+            seen |= (unsigned long long)zv << t;
+            if (h == 0) S.Z[t][tid >> 2] = z;
+            if (rowPanel) {
+                U m, low;
+                L::split(z, m, low);
+                if (zv && S.msbCS[t] + msb_nz<U>(z) >= lbits - 1) risk = true;
+#pragma unroll
+                for (int r = 0; r < DG_ROWS; ++r) R[r] = umin(R[r], xa[cur][r] * m + low);
+            } else {
+                if (zv && msb_nz<U>(z) + S.msbRS[t] >= lbits - 1) risk = true;
+#pragma unroll
+                for (int r = 0; r < DG_ROWS; ++r) R[r] = umin(R[r], z * xa[cur][r] + xb[cur][r]);
+            }
+        }
+    }
+    __syncthreads();   // the snapshots (written by lane h == 0 of each group) are visible below
+    {
+        U *dst = rowPanel ? rpbuf : cpbuf;            // t-major, coalesced over the CTA's lines
+        const int64_t base = (int64_t)cta * PN_LINES;
+        for (int e = tid; e < FW_B * PN_LINES; e += PN_THREADS)
+            dst[(int64_t)(e / PN_LINES) * np + base + e % PN_LINES] = S.Z[e / PN_LINES][e % PN_LINES];
+    }
+    // write back; the running maximum needs each newly valid cell's first valid product
+    SU smx = 0;
+#pragma unroll
+    for (int r = 0; r < DG_ROWS; ++r) {
+        const U v = R[r];
+        const bool vv = L::valid(v);
+        const int c = c0 + r;
+        if (!inK) {
+            if (rowPanel) work[(K0 + c) * np + g] = vv ? v : L::inf;
+            else rowp[r] = vv ? v : L::inf;
+        }
+        if (vv && ((startInf >> r) & 1u)) {
+            const unsigned long long both = seen & (rowPanel ? S.maskCS[c] : S.maskRS[c]);
+            const int tf = __ffsll((long long)both) - 1;
+            U first;
+            const U zf = S.Z[tf][tid >> 2];
+            if (rowPanel) {
+                U m, low;
+                L::split(zf, m, low);
+                first = S.CS[tf][Pad<U>::at(c)] * m + low;
+            } else {
+                first = zf * S.RSm[tf][Pad<U>::at(c)] + S.RSl[tf][Pad<U>::at(c)];
+            }
+            smx = max(smx, (SU)first);
+        }
+    }
+    if (seen) atomicOr(&S.any, 1);
+    __syncthreads();
+    if (tid == 0) atomicOr((rowPanel ? anyRP : anyCP) + (int)((int64_t)cta * PN_LINES / FW_P), S.any);
+    flush_status(st, smx > 0 ? (unsigned long long)smx : 0ull, risk ? RBG_EV_RISK : 0u);
+}
