@@ -103,6 +103,25 @@ int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_t ld_in, vo
                      int64_t ld_out, uint32_t mode, void *workspace, int64_t workspace_bytes,
                      rbg_result_t *result, rbg_stream_t stream);
 
+/* Scratch bytes rbg_fw_batch needs for `count` matrices of sizes `sizes` (host array). */
+int32_t rbg_fw_batch_workspace_bytes(int32_t dtype, int64_t count, const int64_t *sizes,
+                                     uint32_t mode, int64_t *bytes);
+
+/*
+ * Dense AVOS closure of `count` independent matrices in one batched run: matrix i is
+ * sizes[i] x sizes[i], row-major and contiguous at element offset offsets[i] of the device
+ * buffers `in` / `out` (which may be equal).  Every round of every matrix is issued as one
+ * launch per kernel over all matrices still active, largest first.  Replaces the serial
+ * per-component loop of component_wise_closure
+ * (redblackgraph/sparse/csgraph/transitive_closure.py:161-190) and the gufunc batch loop
+ * {T}_gufunc_warshall (redblackgraph/core/src/redblackgraph/warshall.c.in:110-135); each
+ * matrix's W, diameter and error are those of rbg_fw_dense.  `results` (host, count entries)
+ * receives one rbg_result_t per matrix.  Synchronises `stream`.
+ */
+int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                     const void *in, void *out, uint32_t mode, void *workspace,
+                     int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream);
+
 /* Scratch bytes rbg_avos_matmul needs. */
 int32_t rbg_avos_matmul_workspace_bytes(int32_t dtype, int64_t m, int64_t q, int64_t p,
                                         int64_t *bytes);

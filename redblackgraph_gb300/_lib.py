@@ -59,6 +59,8 @@ SIGNATURES = [
     ("rbg_fw_dense_workspace_bytes", _I32, [_I32, _I64, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_dense", _I32, [_I32, _I64, _P, _I64, _P, _I64, _U32, _P, _I64,
                             ctypes.POINTER(RbgResult), _P]),
+    ("rbg_fw_batch_workspace_bytes", _I32, [_I32, _I64, _P, _U32, ctypes.POINTER(_I64)]),
+    ("rbg_fw_batch", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, _P, _P]),
     ("rbg_avos_matmul_workspace_bytes", _I32, [_I32, _I64, _I64, _I64, ctypes.POINTER(_I64)]),
     ("rbg_avos_matmul", _I32, [_I32, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
                                ctypes.POINTER(_U32), _P]),

@@ -35,6 +35,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <vector>
 #include "rbg_internal.cuh"
 
 namespace rbg {
@@ -102,6 +103,33 @@ __device__ __forceinline__ void flush_status(DevStatus *st, unsigned long long m
 }
 
 // ------------------------------------------------------------------------------------------
+// components: every kernel below works on a table of independent matrices (a batch; a single
+// closure is a batch of one).  Components are sorted by size, descending, so the components
+// still active in round r (n > 64 r) are a prefix of the table; each launch covers that prefix
+// and a CTA finds its component by binary search in the launch's CTA prefix sums.
+// ------------------------------------------------------------------------------------------
+struct FwComp {
+    int64_t n, np;            // size, padded size (a multiple of FW_P)
+    int64_t in_off, out_off;  // element offsets of the input / output matrices
+    int64_t ld_in, ld_out;    // their leading dimensions
+    int64_t work_off;         // lane offset of the np x np work matrix
+    int64_t cp_off, rp_off;   // lane offsets of the snapshot panels (FW_B x np each, t-major)
+    int64_t any_off;          // int offset of the panel flags (anyCP then anyRP, np / FW_P each)
+    int64_t rb_index;         // round-buffer index
+    int32_t triangular, status_index;
+};
+
+__device__ __forceinline__ int fw_find(const int64_t *__restrict__ prefix, int count, int64_t cta) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= cta) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ------------------------------------------------------------------------------------------
 // convert: storage T -> lane work matrix U (clean-regime check, d_0 contribution)
 // ------------------------------------------------------------------------------------------
 // Work encoding: valid off-diagonal values as is; zeros, the diagonal, the padding and (in
@@ -110,8 +138,17 @@ __device__ __forceinline__ void flush_status(DevStatus *st, unsigned long long m
 // reference writes at k = 0 (warshall.c.in:88-89); later rounds add each cell's first value.
 template <typename T, typename U>
 __global__ void __launch_bounds__(FW_THREADS)
-fw_convert_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, U *__restrict__ work,
-                  int64_t np, int lbits, int sbits, int triangular, DevStatus *st) {
+fw_convert_kernel(const T *__restrict__ in_base, U *__restrict__ work_base,
+                  const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix, int count,
+                  int lbits, int sbits, DevStatus *st_base) {
+    const int ci = fw_find(prefix, count, blockIdx.x);
+    const FwComp c = comps[ci];
+    const T *in = in_base + c.in_off;
+    U *work = work_base + c.work_off;
+    const int64_t n = c.n, np = c.np, ld_in = c.ld_in;
+    const int triangular = c.triangular;
+    DevStatus *st = st_base + c.status_index;
+    const int64_t cta0 = prefix[ci], ctas = prefix[ci + 1] - cta0;
     typedef typename utype<T>::type TU;
     typedef lane<U> L;
     const TU tmax = (TU)~(TU)0;
@@ -120,8 +157,8 @@ fw_convert_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, U *__restr
     unsigned flags = 0;
     unsigned long long mx = 0;
     const int64_t total = np * np;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t idx = ((int64_t)blockIdx.x - cta0) * blockDim.x + threadIdx.x; idx < total;
+         idx += ctas * blockDim.x) {
         const int64_t i = idx / np, j = idx - i * np;
         U w = L::inf;
         if (i < n && j < n) {
@@ -181,9 +218,9 @@ template <typename U, int BN> struct TileSmem {
 
 template <typename U, int BN, int TM, int TN>
 __global__ void __launch_bounds__(FW_THREADS)
-fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict__ cpbuf,
-               const U *__restrict__ rpbuf, const int *__restrict__ anyCP,
-               const int *__restrict__ anyRP, int lbits, DevStatus *st) {
+fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
+               const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix, int count,
+               int64_t K0, int lbits, DevStatus *st_base) {
     typedef lane<U> L;
     constexpr int BM = FW_P;
     constexpr int TX = BN / TN;           // threads along columns
@@ -193,7 +230,18 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
 
-    const int tI = blockIdx.y, tJ = blockIdx.x;
+    const int ci = fw_find(prefix, count, blockIdx.x);
+    const FwComp cmp = comps[ci];
+    const int64_t np = cmp.np;
+    U *work = work_base + cmp.work_off;
+    const U *cpbuf = work_base + cmp.cp_off;
+    const U *rpbuf = work_base + cmp.rp_off;
+    const int *anyCP = any_base + cmp.any_off;
+    const int *anyRP = anyCP + np / FW_P;
+    DevStatus *st = st_base + cmp.status_index;
+    const int64_t local = (int64_t)blockIdx.x - prefix[ci];
+    const int tJn = (int)(np / BN);
+    const int tI = (int)(local / tJn), tJ = (int)(local % tJn);
     if (!anyCP[tI] || !anyRP[(int)(((int64_t)tJ * BN) / FW_P)]) return;
     const int64_t I0 = (int64_t)tI * BM, J0 = (int64_t)tJ * BN;
     const int tid = threadIdx.x;
@@ -356,20 +404,31 @@ fw_tile_kernel(U *__restrict__ work, int64_t np, int64_t K0, const U *__restrict
 // ------------------------------------------------------------------------------------------
 template <typename T, typename U>
 __global__ void __launch_bounds__(FW_THREADS)
-fw_finalize_kernel(const T *__restrict__ in, int64_t ld_in, int64_t n, const U *__restrict__ work,
-                   int64_t np, T *__restrict__ out, int64_t ld_out, int triangular) {
+fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_base,
+                   T *__restrict__ out_base, const FwComp *__restrict__ comps,
+                   const int64_t *__restrict__ prefix, int count, const DevStatus *st_base) {
+    const int ci = fw_find(prefix, count, blockIdx.x);
+    const FwComp c = comps[ci];
+    // a component that needs another path keeps its input untouched (it may be in place)
+    if (st_base[c.status_index].flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE | RBG_EV_RISK | RBG_EV_CYCLE))
+        return;
+    const T *in = in_base + c.in_off;
+    const U *work = work_base + c.work_off;
+    T *out = out_base + c.out_off;
+    const int64_t n = c.n, np = c.np;
+    const int64_t cta0 = prefix[ci], ctas = prefix[ci + 1] - cta0;
     const int64_t total = n * n;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t idx = ((int64_t)blockIdx.x - cta0) * blockDim.x + threadIdx.x; idx < total;
+         idx += ctas * blockDim.x) {
         const int64_t i = idx / n, j = idx - i * n;
         T v;
-        if (i == j || (triangular && i > j)) {
-            v = in[i * ld_in + j];
+        if (i == j || (c.triangular && i > j)) {
+            v = in[i * c.ld_in + j];
         } else {
             U w = work[i * np + j];
             v = lane<U>::valid(w) ? (T)w : (T)0;
         }
-        out[i * ld_out + j] = v;
+        out[i * c.ld_out + j] = v;
     }
 }
 
@@ -526,59 +585,119 @@ static int run_exact(const T *in, int64_t ld_in, T *out, int64_t ld_out, int64_t
 // ------------------------------------------------------------------------------------------
 // host driver
 // ------------------------------------------------------------------------------------------
-struct FwLayout {
-    int64_t np;
-    size_t off_status, off_work, off_cp, off_rp, off_diag, off_anyc, off_anyr, off_exact, total;
-};
-
-static FwLayout fw_layout(int64_t n, int dtype, bool wide_possible) {
-    FwLayout L;
-    L.np = align_up((size_t)std::max<int64_t>(n, 1), FW_P);
-    const size_t ub = wide_possible ? 8 : 4;   // largest lane size that may be needed
-    size_t o = 0;
-    L.off_status = o; o += 256;
-    L.off_work = o; o = align_up(o + (size_t)L.np * L.np * ub, 256);
-    L.off_cp = o; o = align_up(o + (size_t)L.np * FW_B * ub, 256);
-    L.off_rp = o; o = align_up(o + (size_t)L.np * FW_B * ub, 256);
-    L.off_diag = o; o = align_up(o + sizeof(RoundBuf<uint64_t>), 256);
-    L.off_anyc = o; o = align_up(o + (size_t)(L.np / FW_P) * 4, 256);
-    L.off_anyr = o; o = align_up(o + (size_t)(L.np / FW_P) * 4, 256);
-    L.off_exact = o; o = align_up(o + 3 * align_up((size_t)n, 32) * dtype_bytes(dtype) + 256, 256);
-    L.total = o;
-    return L;
-}
-
-template <typename U> static size_t panel_smem() { return sizeof(PanelSmem<U>); }
-template <typename U, int BN> static size_t tile_smem() { return sizeof(TileSmem<U, BN>); }
-
-static int read_status(DevStatus *d, DevStatus *h, cudaStream_t stream) {
-    RBG_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
-    RBG_CUDA_TRY(cudaStreamSynchronize(stream));
-    return RBG_OK;
-}
-
 template <typename U> struct TileCfg;
 template <> struct TileCfg<uint32_t> { static const int BN = 128, TM = 8, TN = 8; };
 template <> struct TileCfg<uint64_t> { static const int BN = 64, TM = 8, TN = 4; };
+
+constexpr int CONV_ELEMS_PER_THREAD = 16;
+
+// Everything a (batched) blocked run needs on the host: the component table (sorted by size,
+// descending), the per-kernel CTA prefix sums, the per-round active counts and the workspace
+// layout.  A single matrix is a plan of one.
+struct FwPlan {
+    int count = 0;
+    std::vector<FwComp> comps;
+    std::vector<int64_t> pre_conv, pre_panel, pre_tile;
+    std::vector<int> active;                // active[r] = components with n > 64 r
+    size_t off_status = 0, off_comps = 0, off_pconv = 0, off_ppanel = 0, off_ptile = 0;
+    size_t off_rb = 0, off_any = 0, off_lanes = 0, off_exact = 0, total = 0;
+};
+
+// sizes[i], in_off[i], out_off[i] of component i (input order); lane = bytes per lane word
+static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int64_t *in_off,
+                       const int64_t *out_off, size_t lane, int triangular, int tile_bn,
+                       int elem_bytes) {
+    P.count = (int)count;
+    std::vector<int> order((size_t)count);
+    for (int64_t i = 0; i < count; ++i) order[(size_t)i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sizes[x] > sizes[y]; });
+    P.comps.assign((size_t)count, FwComp());
+    P.pre_conv.assign((size_t)count + 1, 0);
+    P.pre_panel.assign((size_t)count + 1, 0);
+    P.pre_tile.assign((size_t)count + 1, 0);
+    int64_t lanes = 0, anys = 0, maxn = 0;
+    for (int64_t k = 0; k < count; ++k) {
+        const int i = order[(size_t)k];
+        FwComp &c = P.comps[(size_t)k];
+        c.n = sizes[i];
+        c.np = (int64_t)align_up((size_t)std::max<int64_t>(c.n, 1), FW_P);
+        c.in_off = in_off[i];
+        c.out_off = out_off[i];
+        c.ld_in = c.ld_out = c.n;
+        c.work_off = lanes; lanes += c.np * c.np;
+        c.cp_off = lanes; lanes += (int64_t)FW_B * c.np;
+        c.rp_off = lanes; lanes += (int64_t)FW_B * c.np;
+        lanes = (int64_t)align_up((size_t)lanes, 64);
+        c.any_off = anys; anys += 2 * (c.np / FW_P);
+        c.rb_index = k;
+        c.triangular = triangular;
+        c.status_index = i;
+        const int64_t cells = c.np * c.np;
+        int64_t conv = (cells + FW_THREADS * CONV_ELEMS_PER_THREAD - 1) / (FW_THREADS * CONV_ELEMS_PER_THREAD);
+        P.pre_conv[(size_t)k + 1] = P.pre_conv[(size_t)k] + std::max<int64_t>(conv, 1);
+        const bool big = c.n > FW_B;   // n <= 64: the diagonal tile is the whole matrix
+        P.pre_panel[(size_t)k + 1] = P.pre_panel[(size_t)k] + (big ? 2 * (c.np / PN_LINES) : 0);
+        P.pre_tile[(size_t)k + 1] = P.pre_tile[(size_t)k] + (big ? (c.np / tile_bn) * (c.np / FW_P) : 0);
+        maxn = std::max(maxn, c.n);
+    }
+    const int rounds = (int)((maxn + FW_B - 1) / FW_B);
+    P.active.assign((size_t)rounds, 0);
+    for (int r = 0; r < rounds; ++r) {
+        int a = 0;
+        while (a < count && P.comps[(size_t)a].n > (int64_t)r * FW_B) ++a;
+        P.active[(size_t)r] = a;
+    }
+    size_t o = 0;
+    P.off_status = o; o = align_up(o + (size_t)count * sizeof(DevStatus), 256);
+    P.off_comps = o; o = align_up(o + (size_t)count * sizeof(FwComp), 256);
+    P.off_pconv = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
+    P.off_ppanel = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
+    P.off_ptile = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
+    P.off_rb = o; o = align_up(o + (size_t)count * (lane == 8 ? sizeof(RoundBuf<uint64_t>) : sizeof(RoundBuf<uint32_t>)), 256);
+    P.off_any = o; o = align_up(o + (size_t)anys * 4, 256);
+    P.off_lanes = o; o = align_up(o + (size_t)lanes * lane, 256);
+    P.off_exact = o; o = align_up(o + 3 * align_up((size_t)maxn, 32) * elem_bytes + 256, 256);
+    P.total = o;
+}
+
+static int read_status(DevStatus *d, DevStatus *h, int count, cudaStream_t stream) {
+    RBG_CUDA_TRY(cudaMemcpyAsync(h, d, (size_t)count * sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+    RBG_CUDA_TRY(cudaStreamSynchronize(stream));
+    return RBG_OK;
+}
 
 template <typename U>
 static int configure_kernels() {
     typedef TileCfg<U> C;
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)panel_smem<U>()));
+                                      (int)sizeof(PanelSmem<U>)));
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_diag_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(DiagSmem<U>)));
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_tile_kernel<U, C::BN, C::TM, C::TN>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)tile_smem<U, C::BN>()));
+                                      (int)sizeof(TileSmem<U, C::BN>)));
     return RBG_OK;
 }
 
-// One blocked run in lanes U (conversion + all rounds); the caller finalizes only when the
-// status is clean, so an in-place call keeps its input for an exact re-run.
+// Upload the plan's tables into the workspace.
+static int upload_plan(const FwPlan &P, unsigned char *ws, cudaStream_t stream) {
+    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_comps, P.comps.data(), P.comps.size() * sizeof(FwComp),
+                                 cudaMemcpyHostToDevice, stream));
+    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_pconv, P.pre_conv.data(), P.pre_conv.size() * 8,
+                                 cudaMemcpyHostToDevice, stream));
+    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ppanel, P.pre_panel.data(), P.pre_panel.size() * 8,
+                                 cudaMemcpyHostToDevice, stream));
+    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ptile, P.pre_tile.data(), P.pre_tile.size() * 8,
+                                 cudaMemcpyHostToDevice, stream));
+    return RBG_OK;
+}
+
+// Launch the whole blocked closure of a plan (conversion, every round, finalization) on
+// `stream`, without synchronising.  Components whose status asks for another path are left
+// untouched in `out` by the finalization.
 template <typename T, typename U>
-static int run_blocked(const T *in, int64_t ld_in, int64_t n, int triangular, unsigned char *ws,
-                       const FwLayout &Ly, DevStatus *h, cudaStream_t stream) {
+static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws, cudaStream_t stream,
+                          bool stop_after_convert, DevStatus *h_status) {
     typedef TileCfg<U> C;
     static bool configured = false;
     if (!configured) {
@@ -586,47 +705,43 @@ static int run_blocked(const T *in, int64_t ld_in, int64_t n, int triangular, un
         if (rc) return rc;
         configured = true;
     }
-    DevStatus *st = reinterpret_cast<DevStatus *>(ws + Ly.off_status);
-    U *work = reinterpret_cast<U *>(ws + Ly.off_work);
-    U *cp = reinterpret_cast<U *>(ws + Ly.off_cp);
-    U *rp = reinterpret_cast<U *>(ws + Ly.off_rp);
-    RoundBuf<U> *rb = reinterpret_cast<RoundBuf<U> *>(ws + Ly.off_diag);
-    int *anyc = reinterpret_cast<int *>(ws + Ly.off_anyc);
-    int *anyr = reinterpret_cast<int *>(ws + Ly.off_anyr);
-    const int64_t np = Ly.np;
+    const int cnt = P.count;
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + P.off_status);
+    const FwComp *comps = reinterpret_cast<const FwComp *>(ws + P.off_comps);
+    const int64_t *pconv = reinterpret_cast<const int64_t *>(ws + P.off_pconv);
+    const int64_t *ppanel = reinterpret_cast<const int64_t *>(ws + P.off_ppanel);
+    const int64_t *ptile = reinterpret_cast<const int64_t *>(ws + P.off_ptile);
+    RoundBuf<U> *rbs = reinterpret_cast<RoundBuf<U> *>(ws + P.off_rb);
+    int *any = reinterpret_cast<int *>(ws + P.off_any);
+    U *lanes = reinterpret_cast<U *>(ws + P.off_lanes);
     const int sbits = (int)sizeof(T) * 8;
     const int lbits = std::min<int>(sbits, (int)sizeof(U) * 8);
 
-    status_init_kernel<<<1, 32, 0, stream>>>(st, 1);
-    fw_convert_kernel<T, U><<<grid_for(np * np, FW_THREADS), FW_THREADS, 0, stream>>>(
-        in, ld_in, n, work, np, lbits, sbits, triangular, st);
+    status_init_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(st, cnt);
+    fw_convert_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
+        in, lanes, comps, pconv, cnt, lbits, sbits, st);
     RBG_CUDA_TRY(cudaGetLastError());
-    int rc = read_status(st, h, stream);
-    if (rc) return rc;
-    if (h->flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE)) return RBG_OK;   // caller decides
-
-    const int ntp = (int)(np / FW_P);
-    const dim3 tgrid((unsigned)(np / C::BN), (unsigned)ntp);
-    const size_t psm = panel_smem<U>(), tsm = tile_smem<U, C::BN>();
-    for (int64_t K0 = 0; K0 < n; K0 += FW_B) {
-        fw_diag_kernel<U><<<1, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(work, np, K0, rb, lbits, st);
-        RBG_CUDA_TRY(cudaMemsetAsync(anyc, 0, 2 * align_up((size_t)ntp * 4, 256), stream));
-        fw_panel_kernel<U><<<2 * (int)(np / PN_LINES), PN_THREADS, psm, stream>>>(
-            work, np, K0, rb, cp, rp, anyc, anyr, lbits, st);
-        fw_tile_kernel<U, C::BN, C::TM, C::TN><<<tgrid, FW_THREADS, tsm, stream>>>(
-            work, np, K0, cp, rp, anyc, anyr, lbits, st);
+    if (stop_after_convert) {
+        int rc = read_status(st, h_status, cnt, stream);
+        if (rc) return rc;
+        if (h_status[0].flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE)) return RBG_OK;
+    }
+    for (size_t r = 0; r < P.active.size(); ++r) {
+        const int a = P.active[r];
+        const int64_t K0 = (int64_t)r * FW_B;
+        fw_diag_kernel<U><<<a, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(lanes, any, rbs, comps, K0,
+                                                                           lbits, st);
+        if (P.pre_panel[(size_t)a] > 0)
+            fw_panel_kernel<U><<<(unsigned)P.pre_panel[(size_t)a], PN_THREADS, sizeof(PanelSmem<U>), stream>>>(
+                lanes, any, rbs, comps, ppanel, a, K0, lbits, st);
+        if (P.pre_tile[(size_t)a] > 0)
+            fw_tile_kernel<U, C::BN, C::TM, C::TN><<<(unsigned)P.pre_tile[(size_t)a], FW_THREADS,
+                                                    sizeof(TileSmem<U, C::BN>), stream>>>(
+                lanes, any, comps, ptile, a, K0, lbits, st);
     }
     RBG_CUDA_TRY(cudaGetLastError());
-    return read_status(st, h, stream);
-}
-
-template <typename T, typename U>
-static int finalize_blocked(const T *in, int64_t ld_in, int64_t n, T *out, int64_t ld_out,
-                            int triangular, unsigned char *ws, const FwLayout &Ly,
-                            cudaStream_t stream) {
-    const U *work = reinterpret_cast<const U *>(ws + Ly.off_work);
-    fw_finalize_kernel<T, U><<<grid_for(n * n, FW_THREADS), FW_THREADS, 0, stream>>>(
-        in, ld_in, n, work, Ly.np, out, ld_out, triangular);
+    fw_finalize_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
+        in, lanes, out, comps, pconv, cnt, st);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }
@@ -638,60 +753,40 @@ static void decode_seq(long long seq, int64_t n, rbg_result_t *r) {
     r->k = seq / n / n;
 }
 
-template <typename T>
-static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_out, uint32_t mode,
-                      unsigned char *ws, const FwLayout &Ly, rbg_result_t *res, cudaStream_t stream) {
-    const bool cython = (mode & RBG_MODE_CYTHON) != 0;
-    const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
-    DevStatus h;
-    memset(res, 0, sizeof(*res));
-    res->k = res->i = res->j = -1;
-    bool need_exact = (mode & RBG_MODE_FORCE_EXACT) != 0;
-    if (!need_exact) {
-        bool wide = sizeof(T) == 8 && (mode & RBG_MODE_FORCE_WIDE);
-        if (!wide) {
-            int rc = run_blocked<T, uint32_t>(in, ld_in, n, triangular, ws, Ly, &h, stream);
-            if (rc) return rc;
-            const unsigned f = h.flags;
-            if (f & (RBG_EV_UNCLEAN | RBG_EV_CYCLE)) need_exact = true;
-            else if (f & (RBG_EV_WIDE | RBG_EV_RISK)) {
-                if (sizeof(T) == 8) wide = true;   // values need 64-bit lanes
-                else need_exact = true;            // the reference itself reaches the top bit
-            } else {
-                rc = finalize_blocked<T, uint32_t>(in, ld_in, n, out, ld_out, triangular, ws, Ly, stream);
-                if (rc) return rc;
-                res->path = RBG_PATH_BLOCKED32;
-            }
-        }
-        if (wide && !need_exact) {
-            int rc = run_blocked<T, uint64_t>(in, ld_in, n, triangular, ws, Ly, &h, stream);
-            if (rc) return rc;
-            if (h.flags & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_RISK | RBG_EV_WIDE)) need_exact = true;
-            else {
-                rc = finalize_blocked<T, uint64_t>(in, ld_in, n, out, ld_out, triangular, ws, Ly, stream);
-                if (rc) return rc;
-                res->path = RBG_PATH_BLOCKED64;
-            }
-        }
-        if (res->path) {
-            RBG_CUDA_TRY(cudaStreamSynchronize(stream));
-            res->status = RBG_OK;
-            res->flags = h.flags;
-            res->diameter = h.mx ? msb_u64(h.mx) : 0;
-            return RBG_OK;
-        }
+template <typename U>
+static void single_plan(FwPlan &P, int64_t n, int64_t ld_in, int64_t ld_out, int triangular, int elem_bytes) {
+    const int64_t zero = 0;
+    build_plan(P, 1, &n, &zero, &zero, sizeof(U), triangular, TileCfg<U>::BN, elem_bytes);
+    P.comps[0].ld_in = ld_in;
+    P.comps[0].ld_out = ld_out;
+}
+
+static size_t single_workspace(int64_t n, int dtype) {
+    FwPlan P32, P64;
+    single_plan<uint32_t>(P32, n, n, n, 0, dtype_bytes(dtype));
+    size_t t = P32.total;
+    if (dtype_bytes(dtype) == 8) {
+        single_plan<uint64_t>(P64, n, n, n, 0, 8);
+        t = std::max(t, P64.total);
     }
-    // exact path
-    DevStatus *st = reinterpret_cast<DevStatus *>(ws + Ly.off_status);
+    return t;
+}
+
+// Exact sequential-order run; fills `res` from the reference's error conventions.
+template <typename T>
+static int exact_dense(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_out, bool cython,
+                       int triangular, unsigned char *ws, size_t off_status, size_t off_exact,
+                       rbg_result_t *res, cudaStream_t stream) {
+    DevStatus h;
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + off_status);
     status_init_kernel<<<1, 32, 0, stream>>>(st, 1);
-    int rc = cython ? run_exact<T, 1>(in, ld_in, out, ld_out, n, triangular, ws + Ly.off_exact, st, stream)
-                    : run_exact<T, 0>(in, ld_in, out, ld_out, n, triangular, ws + Ly.off_exact, st, stream);
+    int rc = cython ? run_exact<T, 1>(in, ld_in, out, ld_out, n, triangular, ws + off_exact, st, stream)
+                    : run_exact<T, 0>(in, ld_in, out, ld_out, n, triangular, ws + off_exact, st, stream);
     if (rc) return rc;
-    rc = read_status(st, &h, stream);
+    rc = read_status(st, &h, 1, stream);
     if (rc) return rc;
     res->path = RBG_PATH_EXACT;
     res->flags = h.flags;
-    typedef typename utype<T>::type TU;
     if (cython) {
         if (h.first_cycle != LLONG_MAX) {
             res->status = RBG_ERR_CYCLE;
@@ -710,16 +805,111 @@ static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_
         return RBG_OK;
     }
     if (h.last_ovf >= 0 || h.last_cycle >= 0) {
-        bool ovf_last = h.last_ovf > h.last_cycle;
+        const bool ovf_last = h.last_ovf > h.last_cycle;
         res->status = ovf_last ? RBG_ERR_OVERFLOW : RBG_ERR_CYCLE;
         decode_seq(ovf_last ? h.last_ovf : h.last_cycle, n, res);
     } else {
         res->status = RBG_OK;
     }
-    unsigned long long mxv = utype<T>::is_signed ? (unsigned long long)std::max<long long>(h.mx_signed, 0)
-                                                 : h.mx_unsigned;
-    (void)sizeof(TU);
+    const unsigned long long mxv = utype<T>::is_signed
+        ? (unsigned long long)std::max<long long>(h.mx_signed, 0) : h.mx_unsigned;
     res->diameter = mxv ? msb_u64(mxv) : 0;
+    return RBG_OK;
+}
+
+static void result_from_blocked(const DevStatus &h, int path, rbg_result_t *res) {
+    res->status = RBG_OK;
+    res->flags = h.flags;
+    res->diameter = h.mx ? msb_u64(h.mx) : 0;
+    res->path = path;
+}
+
+// Single matrix: 32-bit lanes, then 64-bit lanes when 64-bit values need them, then the exact
+// sequential-order kernel for anything outside the clean regime, cycles and top-bit products.
+template <typename T>
+static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_out, uint32_t mode,
+                      unsigned char *ws, rbg_result_t *res, cudaStream_t stream) {
+    const bool cython = (mode & RBG_MODE_CYTHON) != 0;
+    const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
+    memset(res, 0, sizeof(*res));
+    res->k = res->i = res->j = -1;
+    DevStatus h;
+    FwPlan P;
+    single_plan<uint32_t>(P, n, ld_in, ld_out, triangular, (int)sizeof(T));
+    if (!(mode & RBG_MODE_FORCE_EXACT)) {
+        bool wide = sizeof(T) == 8 && (mode & RBG_MODE_FORCE_WIDE);
+        if (!wide) {
+            int rc = upload_plan(P, ws, stream);
+            if (rc) return rc;
+            rc = launch_blocked<T, uint32_t>(P, in, out, ws, stream, true, &h);
+            if (rc) return rc;
+            if (!(h.flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE))) {
+                rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), &h, 1, stream);
+                if (rc) return rc;
+            }
+            const unsigned f = h.flags;
+            if (!(f & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_WIDE | RBG_EV_RISK))) {
+                result_from_blocked(h, RBG_PATH_BLOCKED32, res);
+                return RBG_OK;
+            }
+            wide = sizeof(T) == 8 && !(f & (RBG_EV_UNCLEAN | RBG_EV_CYCLE));
+        }
+        if (wide) {
+            FwPlan P64;
+            single_plan<uint64_t>(P64, n, ld_in, ld_out, triangular, (int)sizeof(T));
+            int rc = upload_plan(P64, ws, stream);
+            if (rc) return rc;
+            rc = launch_blocked<T, uint64_t>(P64, in, out, ws, stream, true, &h);
+            if (rc) return rc;
+            if (!(h.flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE))) {
+                rc = read_status(reinterpret_cast<DevStatus *>(ws + P64.off_status), &h, 1, stream);
+                if (rc) return rc;
+            }
+            if (!(h.flags & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_WIDE | RBG_EV_RISK))) {
+                result_from_blocked(h, RBG_PATH_BLOCKED64, res);
+                return RBG_OK;
+            }
+        }
+    }
+    return exact_dense<T>(n, in, ld_in, out, ld_out, cython, triangular, ws, P.off_status, P.off_exact,
+                          res, stream);
+}
+
+// Batch: every component in one blocked run with 32-bit lanes; components that need another
+// path (64-bit lanes, exact order) are then closed one by one with the single-matrix path,
+// reusing the workspace.
+template <typename T>
+static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offsets, const T *in, T *out,
+                      uint32_t mode, unsigned char *ws, rbg_result_t *results, cudaStream_t stream) {
+    const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
+    for (int64_t i = 0; i < count; ++i) {
+        memset(&results[i], 0, sizeof(rbg_result_t));
+        results[i].k = results[i].i = results[i].j = -1;
+    }
+    std::vector<char> redo((size_t)count, 1);
+    if (!(mode & (RBG_MODE_FORCE_EXACT | RBG_MODE_FORCE_WIDE))) {
+        FwPlan P;
+        build_plan(P, count, sizes, offsets, offsets, 4, triangular, TileCfg<uint32_t>::BN, (int)sizeof(T));
+        int rc = upload_plan(P, ws, stream);
+        if (rc) return rc;
+        rc = launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr);
+        if (rc) return rc;
+        std::vector<DevStatus> h((size_t)count);
+        rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), h.data(), (int)count, stream);
+        if (rc) return rc;
+        for (int64_t i = 0; i < count; ++i) {
+            if (!(h[(size_t)i].flags & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_WIDE | RBG_EV_RISK))) {
+                result_from_blocked(h[(size_t)i], RBG_PATH_BLOCKED32, &results[i]);
+                redo[(size_t)i] = 0;
+            }
+        }
+    }
+    for (int64_t i = 0; i < count; ++i) {
+        if (!redo[(size_t)i] || sizes[i] == 0) continue;
+        int rc = fw_dense_t<T>(sizes[i], in + offsets[i], sizes[i], out + offsets[i], sizes[i], mode, ws,
+                               &results[i], stream);
+        if (rc) return rc;
+    }
     return RBG_OK;
 }
 
@@ -732,8 +922,7 @@ extern "C" int32_t rbg_version(void) { return 100; }
 extern "C" int32_t rbg_fw_dense_workspace_bytes(int32_t dtype, int64_t n, uint32_t mode, int64_t *bytes) {
     if (!bytes || n < 0 || dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;
     (void)mode;
-    FwLayout L = fw_layout(n, dtype, dtype_bytes(dtype) == 8);
-    *bytes = (int64_t)L.total;
+    *bytes = (int64_t)single_workspace(n, dtype);
     return RBG_OK;
 }
 
@@ -748,13 +937,51 @@ extern "C" int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_
     memset(result, 0, sizeof(*result));
     result->k = result->i = result->j = -1;
     if (n == 0) return RBG_OK;
-    FwLayout L = fw_layout(n, dtype, bytes == 8);
-    if (workspace_bytes < (int64_t)L.total) return RBG_ERR_NOMEM;
+    if (workspace_bytes < (int64_t)single_workspace(n, dtype)) return RBG_ERR_NOMEM;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     unsigned char *ws = reinterpret_cast<unsigned char *>(workspace);
     int rc = RBG_ERR_INVALID;
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out),
-                           ld_out, mode, ws, L, result, s));
+                           ld_out, mode, ws, result, s));
+    return rc;
+}
+
+static size_t batch_workspace(int32_t dtype, int64_t count, const int64_t *sizes, uint32_t mode) {
+    std::vector<int64_t> off((size_t)count, 0);
+    FwPlan P;
+    build_plan(P, count, sizes, off.data(), off.data(), 4, (mode & RBG_MODE_TRIANGULAR) ? 1 : 0,
+               TileCfg<uint32_t>::BN, dtype_bytes(dtype));
+    int64_t maxn = 0;
+    for (int64_t i = 0; i < count; ++i) maxn = std::max(maxn, sizes[i]);
+    return std::max(P.total, single_workspace(maxn, dtype));
+}
+
+extern "C" int32_t rbg_fw_batch_workspace_bytes(int32_t dtype, int64_t count, const int64_t *sizes,
+                                                uint32_t mode, int64_t *bytes) {
+    if (!bytes || count < 0 || (count > 0 && !sizes) || dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;
+    for (int64_t i = 0; i < count; ++i)
+        if (sizes[i] < 0) return RBG_ERR_INVALID;
+    *bytes = (int64_t)batch_workspace(dtype, count, sizes, mode);
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                                const void *in, void *out, uint32_t mode, void *workspace,
+                                int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream) {
+    if (count < 0 || (count > 0 && (!sizes || !offsets || !in || !out || !workspace || !results)))
+        return RBG_ERR_INVALID;
+    if (dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;
+    if ((mode & RBG_MODE_CYTHON) && dtype != RBG_DTYPE_INT32) return RBG_ERR_INVALID;
+    if (count == 0) return RBG_OK;
+    for (int64_t i = 0; i < count; ++i)
+        if (sizes[i] < 0 || offsets[i] < 0) return RBG_ERR_INVALID;
+    if (workspace_bytes < (int64_t)batch_workspace(dtype, count, sizes, mode)) return RBG_ERR_NOMEM;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned char *ws = reinterpret_cast<unsigned char *>(workspace);
+    int rc = RBG_ERR_INVALID;
+    RBG_DISPATCH_DTYPE(dtype, T,
+        rc = fw_batch_t<T>(count, sizes, offsets, reinterpret_cast<const T *>(in), reinterpret_cast<T *>(out),
+                           mode, ws, results, s));
     return rc;
 }

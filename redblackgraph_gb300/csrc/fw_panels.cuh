@@ -64,13 +64,19 @@ template <typename U> struct DiagSmem {
 // of the threads with h = t / 16.  One barrier per step: step t's writes go to slot t only.
 template <typename U>
 __global__ void __launch_bounds__(DG_THREADS)
-fw_diag_kernel(U *__restrict__ work, int64_t np, int64_t K0, RoundBuf<U> *__restrict__ rb,
-               int lbits, DevStatus *st) {
+fw_diag_kernel(U *__restrict__ work_base, int *__restrict__ any_base, RoundBuf<U> *__restrict__ rbs,
+               const FwComp *__restrict__ comps, int64_t K0, int lbits, DevStatus *st_base) {
     typedef lane<U> L;
     typedef typename signed_of<U>::type SU;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DiagSmem<U> &S = *reinterpret_cast<DiagSmem<U> *>(smem_raw);
     const int tid = threadIdx.x;
+    const FwComp cmp = comps[blockIdx.x];             // one CTA per active component
+    U *work = work_base + cmp.work_off;
+    const int64_t np = cmp.np;
+    RoundBuf<U> *rb = rbs + cmp.rb_index;
+    DevStatus *st = st_base + cmp.status_index;
+    for (int e = tid; e < 2 * (int)(np / FW_P); e += DG_THREADS) any_base[cmp.any_off + e] = 0;
     const int b = tid % FW_B, h = tid / FW_B;
     U R[DG_ROWS];
 #pragma unroll
@@ -180,17 +186,29 @@ template <typename U> __device__ __forceinline__ U shfl_lane(U v, int src) {
 
 template <typename U>
 __global__ void __launch_bounds__(PN_THREADS, 2)
-fw_panel_kernel(U *__restrict__ work, int64_t np, int64_t K0, const RoundBuf<U> *__restrict__ rb,
-                U *__restrict__ cpbuf, U *__restrict__ rpbuf, int *__restrict__ anyCP,
-                int *__restrict__ anyRP, int lbits, DevStatus *st) {
+fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
+                const RoundBuf<U> *__restrict__ rbs, const FwComp *__restrict__ comps,
+                const int64_t *__restrict__ prefix, int count, int64_t K0, int lbits,
+                DevStatus *st_base) {
     typedef lane<U> L;
     typedef typename signed_of<U>::type SU;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
     const int tid = threadIdx.x;
+    const int ci = fw_find(prefix, count, blockIdx.x);
+    const FwComp cmp = comps[ci];
+    const int64_t np = cmp.np;
+    U *work = work_base + cmp.work_off;
+    U *cpbuf = work_base + cmp.cp_off;
+    U *rpbuf = work_base + cmp.rp_off;
+    int *anyCP = any_base + cmp.any_off;
+    int *anyRP = anyCP + np / FW_P;
+    const RoundBuf<U> *rb = rbs + cmp.rb_index;
+    DevStatus *st = st_base + cmp.status_index;
+    const int local = (int)((int64_t)blockIdx.x - prefix[ci]);
     const int nct = (int)(np / PN_LINES);             // CTAs per panel
-    const bool rowPanel = blockIdx.x < (unsigned)nct;
-    const int cta = rowPanel ? blockIdx.x : blockIdx.x - nct;
+    const bool rowPanel = local < nct;
+    const int cta = rowPanel ? local : local - nct;
     if (tid == 0) S.any = 0;
     {
         // batched 16-byte loads first, then the shared-memory stores (no serial round trips)

@@ -89,3 +89,51 @@ def warshall_host(A: np.ndarray, mode: int = 0) -> tuple[np.ndarray, int, _lib.R
     d = to_device(A, dev)
     out, res = fw_dense(d, out=d, mode=mode)
     return to_host(out), int(res.diameter), res
+
+
+def fw_batch(buf: torch.Tensor, sizes, offsets, out: torch.Tensor | None = None, mode: int = 0,
+             stream: torch.cuda.Stream | None = None) -> tuple[torch.Tensor, list]:
+    """Close many matrices packed in one flat device tensor ``buf``.
+
+    Matrix i is ``sizes[i] x sizes[i]`` at element offset ``offsets[i]``.  Returns
+    ``(out, results)`` with one ``RbgResult`` per matrix.
+    """
+    import numpy as np
+    if not buf.is_cuda or buf.ndim != 1:
+        raise ValueError("fw_batch takes a flat CUDA tensor")
+    sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    if sizes.shape != offsets.shape:
+        raise ValueError("sizes and offsets differ in length")
+    if sizes.size and int((offsets + sizes * sizes).max()) > buf.numel():
+        raise ValueError("a matrix extends past the end of the buffer")
+    if out is None:
+        out = torch.empty_like(buf)
+    count = int(sizes.size)
+    code = _lib.dtype_code(numpy_dtype(buf.dtype))
+    L = _lib.load()
+    nbytes = ctypes.c_int64(0)
+    _lib.check(L.rbg_fw_batch_workspace_bytes(code, count, sizes.ctypes.data, mode,
+                                              ctypes.byref(nbytes)), "fw_batch")
+    ws = default_workspace().get(nbytes.value, buf.device)
+    results = (_lib.RbgResult * max(count, 1))()
+    rc = L.rbg_fw_batch(code, count, sizes.ctypes.data, offsets.ctypes.data, buf.data_ptr(),
+                        out.data_ptr(), mode, ws.data_ptr(), ws.numel(), results,
+                        stream_handle(stream))
+    _lib.check(rc, "fw_batch")
+    return out, [results[i] for i in range(count)]
+
+
+def pack(mats):
+    """Pack host matrices into one flat array; returns (flat, sizes, offsets)."""
+    import numpy as np
+    sizes = np.array([m.shape[0] for m in mats], dtype=np.int64)
+    offsets = np.zeros_like(sizes)
+    if len(mats) > 1:
+        offsets[1:] = np.cumsum(sizes[:-1] * sizes[:-1])
+    total = int((sizes * sizes).sum())
+    dt = mats[0].dtype if mats else np.int32
+    flat = np.empty(total, dtype=dt)
+    for m, o in zip(mats, offsets):
+        flat[o:o + m.size] = np.ascontiguousarray(m).reshape(-1)
+    return flat, sizes, offsets

@@ -116,3 +116,22 @@ def forest(n: int, generations: int, seed: int, family: int = 64, reach: int = 2
     m.indices = m.indices.astype(np.int32)
     m.indptr = m.indptr.astype(np.int64 if m.nnz >= 2**31 else np.int32)
     return m
+
+
+def batch_edges(sizes, seeds, p_parent: float = 0.9):
+    """Edge lists of many pedigree components laid out one after another in a flat buffer of
+    dense matrices: returns (flat_index, value, offsets) with flat_index into that buffer."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    offsets = np.zeros_like(sizes)
+    if sizes.size > 1:
+        offsets[1:] = np.cumsum(sizes[:-1] * sizes[:-1])
+    idx, val = [], []
+    for n, s, o in zip(sizes, seeds, offsets):
+        n = int(n)
+        colors, c, p, v = pedigree_edges(n, generations_for(n), int(s), p_parent)
+        ar = np.arange(n, dtype=np.int64)
+        idx.append(o + ar * n + ar)
+        val.append(colors)
+        idx.append(o + c * n + p)
+        val.append(v)
+    return np.concatenate(idx), np.concatenate(val), offsets

@@ -1,0 +1,66 @@
+"""Batched dense closure (many components in one run) against the oracle, bit-exact."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def run_batch(mats, mode=0, in_place=False):
+    import torch
+    from redblackgraph_gb300.dense import fw_batch, pack
+    from redblackgraph_gb300.device import to_device, to_host
+    flat, sizes, offsets = pack(mats)
+    d = to_device(flat)
+    out, res = fw_batch(d, sizes, offsets, out=d if in_place else None, mode=mode)
+    torch.cuda.synchronize()
+    h = to_host(out)
+    return [h[o:o + n * n].reshape(n, n) for o, n in zip(offsets, sizes)], res
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64])
+def test_mixed_sizes_vs_oracle(native, dtype):
+    from redblackgraph_gb300 import synth
+    sizes, seeds = synth.batch_components(60, 3, 700, seed=5)
+    mats = [synth.pedigree(int(n), synth.generations_for(int(n)), int(s), dtype=dtype)
+            for n, s in zip(sizes, seeds)]
+    Ws, res = run_batch(mats)
+    for A, W, r in zip(mats, Ws, res):
+        Wo, do, so, _ = O.warshall(A)
+        assert r.status == so == 0
+        assert (W == Wo).all() and r.diameter == do
+
+
+def test_batch_with_fallbacks_in_place(native):
+    """Clean, unclean (exact path), cyclic and 64-bit-wide components in one batch."""
+    from redblackgraph_gb300 import synth, _lib
+    mats = [synth.pedigree(n, 8, n, dtype=np.int64) for n in (10, 70, 130, 257, 1)]
+    rs = np.random.RandomState(3)
+    U = np.triu(rs.randint(0, 4, size=(40, 40)), k=1)
+    np.fill_diagonal(U, rs.choice([-1, 1], size=40))
+    mats.append(U.astype(np.int64))
+    C = synth.pedigree(90, 8, 4, dtype=np.int64)
+    Wc, _, _, _ = O.warshall(C)
+    v, u = max(zip(*np.nonzero(np.tril(Wc, -1))), key=lambda t: t[0] - t[1])
+    C[u, v] = 2
+    mats.append(C)
+    Wd = synth.pedigree(150, 9, 6, dtype=np.int64)
+    mats.append(np.where(Wd > 1, Wd << 8, Wd))
+    Ws, res = run_batch(mats, in_place=True)
+    for A, W, r in zip(mats, Ws, res):
+        Wo, do, so, _ = O.warshall(A)
+        assert r.status == so
+        if so == 0:
+            assert (W == Wo).all() and r.diameter == do
+    assert res[5].path == _lib.PATH_EXACT and res[6].status == _lib.RBG_ERR_CYCLE
+    assert res[7].path == _lib.PATH_BLOCKED64
+
+
+def test_cython_batch(native):
+    from redblackgraph_gb300 import synth, _lib
+    mats = [synth.pedigree(n, 7, n + 1, dtype=np.int32) for n in (33, 64, 65, 200)]
+    Ws, res = run_batch(mats, mode=_lib.MODE_CYTHON)
+    for A, W, r in zip(mats, Ws, res):
+        Wo, do, so, _ = O.fw_cython(A)
+        assert r.status == so == 0 and (W == Wo).all() and r.diameter == do
