@@ -81,10 +81,23 @@ typedef struct rbg_result {
     int64_t k, i, j;  /* loop position of the event that decided `status`, else -1   */
     int32_t path;     /* RBG_PATH_* that produced the result                         */
     int32_t reserved;
+    int64_t executed; /* relaxations the blocked kernels executed (skipped tiles excluded) */
 } rbg_result_t;
 
 /* Library version (major*10000 + minor*100 + patch). */
 int32_t rbg_version(void);
+
+/* Number of kernel launches this library has issued since it was loaded (no reference
+ * counterpart: instrumentation for benchmarks). */
+int64_t rbg_launch_count(void);
+
+/* Start timing the blocked closure kernels with CUDA events recorded on the launching stream
+ * (no reference counterpart: benchmark instrumentation; one process-wide timer). */
+int32_t rbg_profile_begin(void);
+
+/* Stop timing; ms[k] and launches[k] (k = 0 tile, 1 panel, 2 diagonal, 3 convert/finalize)
+ * receive the summed kernel time and launch count since rbg_profile_begin. */
+int32_t rbg_profile_end(double *ms, int64_t *launches);
 
 /* Scratch bytes rbg_fw_dense needs for an n x n matrix of `dtype` under `mode`. */
 int32_t rbg_fw_dense_workspace_bytes(int32_t dtype, int64_t n, uint32_t mode, int64_t *bytes);

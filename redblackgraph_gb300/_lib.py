@@ -48,6 +48,7 @@ class RbgResult(ctypes.Structure):
         ("j", ctypes.c_int64),
         ("path", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+        ("executed", ctypes.c_int64),
     ]
 
 
@@ -56,6 +57,9 @@ _P = ctypes.c_void_p
 _I32, _U32, _I64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
 SIGNATURES = [
     ("rbg_version", _I32, []),
+    ("rbg_launch_count", _I64, []),
+    ("rbg_profile_begin", _I32, []),
+    ("rbg_profile_end", _I32, [_P, _P]),
     ("rbg_fw_dense_workspace_bytes", _I32, [_I32, _I64, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_dense", _I32, [_I32, _I64, _P, _I64, _P, _I64, _U32, _P, _I64,
                             ctypes.POINTER(RbgResult), _P]),

@@ -5,11 +5,8 @@
 // C core scalar semantics (rbg_math.c.in:30-121).  (+) is associative and commutative, so the
 // accumulation order does not change C; an OverflowError is raised when any product signals one.
 //
-// Two kernels:
-//  * clean-lane kernel: 32-bit lanes (values in [2, 2^31) or zero; the operands +-1 on either
-//    side are handled by a fix-up pass) -- one multiply-add and one min per term;
-//  * exact kernel: full semantics per term, used for inputs outside the clean regime and to
-//    decide the error when a clean product reaches the top bit.
+// One tiled kernel with the full scalar semantics per term (identities, parity filters, wrap,
+// overflow events), 64 x 64 outputs per CTA staged through shared memory.
 #include <cuda_runtime.h>
 #include <string.h>
 #include <algorithm>
@@ -85,6 +82,7 @@ static int matmul_t(int64_t m, int64_t q, int64_t p, const T *A, int64_t lda, co
         return RBG_OK;
     }
     dim3 grid((unsigned)((p + MM_T - 1) / MM_T), (unsigned)((m + MM_T - 1) / MM_T));
+    note_launches(1);
     mm_exact_kernel<T><<<grid, MM_THREADS, 0, s>>>(m, q, p, A, lda, B, ldb, C, ldc, dflags);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;

@@ -37,6 +37,7 @@ extern "C" int32_t rbg_avos_elementwise(int32_t op, int32_t dtype, int64_t n, co
     RBG_CUDA_TRY(cudaMemsetAsync(dflags, 0, sizeof(unsigned), s));
     if (n > 0) {
         const int g = grid_for(n, 256);
+        note_launches(1);
         RBG_DISPATCH_DTYPE(dtype, T,
             ew_kernel<T><<<g, 256, 0, s>>>(op, n, reinterpret_cast<const T *>(x),
                                            reinterpret_cast<const T *>(y), reinterpret_cast<T *>(z),

@@ -36,6 +36,7 @@
 #include <string.h>
 #include <algorithm>
 #include <vector>
+#include <atomic>
 #include "rbg_internal.cuh"
 
 namespace rbg {
@@ -58,6 +59,38 @@ __global__ void status_init_kernel(DevStatus *st, int count) {
         s.first_ovf = LLONG_MAX;
         st[t] = s;
     }
+}
+
+static std::atomic<long long> g_launches(0);
+void note_launches(int64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+// Opt-in per-kernel timing: CUDA events recorded on the launching stream around each launch of
+// the blocked kernels (0 = tile, 1 = panel, 2 = diagonal, 3 = convert + finalize).
+struct KernelTimer {
+    bool on = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[4];
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t get() {
+        if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+static KernelTimer g_timer;
+
+static cudaEvent_t timer_begin(int kid, cudaStream_t s) {
+    (void)kid;
+    if (!g_timer.on) return nullptr;
+    cudaEvent_t e = g_timer.get();
+    cudaEventRecord(e, s);
+    return e;
+}
+static void timer_end(int kid, cudaEvent_t start, cudaStream_t s) {
+    if (!g_timer.on || !start) return;
+    cudaEvent_t e = g_timer.get();
+    cudaEventRecord(e, s);
+    g_timer.pending[kid].push_back({start, e});
 }
 
 int grid_for(int64_t work, int threads) {
@@ -349,6 +382,7 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     }
 
     const int na = S.nactive;
+    if (tid == 0) atomicAdd(&st->executed, (unsigned long long)na * BM * BN);
     for (int q = 0; q < na; ++q) {
         const int t = S.active[q];
         U x[TM], m[TN], l[TN];
@@ -572,6 +606,7 @@ static int run_exact(const T *in, int64_t ld_in, T *out, int64_t ld_out, int64_t
     T *newrow = oldcol + align_up(n, 32);
     const int gr = grid_for(n, FW_THREADS);
     const int gc = grid_for(n * n, FW_THREADS);
+    note_launches(2 * n);
     for (int64_t k = 0; k < n; ++k) {
         fw_exact_row_kernel<T, SEM><<<gr, FW_THREADS, 0, stream>>>(out, ld_out, n, k, triangular,
                                                                    oldrow, oldcol, newrow, st);
@@ -717,6 +752,7 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     const int sbits = (int)sizeof(T) * 8;
     const int lbits = std::min<int>(sbits, (int)sizeof(U) * 8);
 
+    note_launches(2);
     status_init_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(st, cnt);
     fw_convert_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
         in, lanes, comps, pconv, cnt, lbits, sbits, st);
@@ -729,17 +765,27 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     for (size_t r = 0; r < P.active.size(); ++r) {
         const int a = P.active[r];
         const int64_t K0 = (int64_t)r * FW_B;
+        note_launches(1 + (P.pre_panel[(size_t)a] > 0) + (P.pre_tile[(size_t)a] > 0));
+        cudaEvent_t td = timer_begin(2, stream);
         fw_diag_kernel<U><<<a, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(lanes, any, rbs, comps, K0,
                                                                            lbits, st);
-        if (P.pre_panel[(size_t)a] > 0)
+        timer_end(2, td, stream);
+        if (P.pre_panel[(size_t)a] > 0) {
+            cudaEvent_t t0 = timer_begin(1, stream);
             fw_panel_kernel<U><<<(unsigned)P.pre_panel[(size_t)a], PN_THREADS, sizeof(PanelSmem<U>), stream>>>(
                 lanes, any, rbs, comps, ppanel, a, K0, lbits, st);
-        if (P.pre_tile[(size_t)a] > 0)
+            timer_end(1, t0, stream);
+        }
+        if (P.pre_tile[(size_t)a] > 0) {
+            cudaEvent_t t0 = timer_begin(0, stream);
             fw_tile_kernel<U, C::BN, C::TM, C::TN><<<(unsigned)P.pre_tile[(size_t)a], FW_THREADS,
                                                     sizeof(TileSmem<U, C::BN>), stream>>>(
                 lanes, any, comps, ptile, a, K0, lbits, st);
+            timer_end(0, t0, stream);
+        }
     }
     RBG_CUDA_TRY(cudaGetLastError());
+    note_launches(1);
     fw_finalize_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
         in, lanes, out, comps, pconv, cnt, st);
     RBG_CUDA_TRY(cudaGetLastError());
@@ -779,6 +825,7 @@ static int exact_dense(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld
                        rbg_result_t *res, cudaStream_t stream) {
     DevStatus h;
     DevStatus *st = reinterpret_cast<DevStatus *>(ws + off_status);
+    note_launches(1);
     status_init_kernel<<<1, 32, 0, stream>>>(st, 1);
     int rc = cython ? run_exact<T, 1>(in, ld_in, out, ld_out, n, triangular, ws + off_exact, st, stream)
                     : run_exact<T, 0>(in, ld_in, out, ld_out, n, triangular, ws + off_exact, st, stream);
@@ -818,6 +865,7 @@ static int exact_dense(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld
 }
 
 static void result_from_blocked(const DevStatus &h, int path, rbg_result_t *res) {
+    res->executed = (int64_t)h.executed;
     res->status = RBG_OK;
     res->flags = h.flags;
     res->diameter = h.mx ? msb_u64(h.mx) : 0;
@@ -918,6 +966,37 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
 using namespace rbg;
 
 extern "C" int32_t rbg_version(void) { return 100; }
+
+extern "C" int64_t rbg_launch_count(void) { return (int64_t)g_launches.load(); }
+
+extern "C" int32_t rbg_profile_begin(void) {
+    for (auto &v : g_timer.pending) {
+        for (auto &pr : v) { g_timer.pool.push_back(pr.first); g_timer.pool.push_back(pr.second); }
+        v.clear();
+    }
+    g_timer.on = true;
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_profile_end(double *ms, int64_t *launches) {
+    if (!ms || !launches) return RBG_ERR_INVALID;
+    g_timer.on = false;
+    for (int k = 0; k < 4; ++k) {
+        double tot = 0.0;
+        for (auto &pr : g_timer.pending[k]) {
+            float t = 0.f;
+            RBG_CUDA_TRY(cudaEventSynchronize(pr.second));
+            RBG_CUDA_TRY(cudaEventElapsedTime(&t, pr.first, pr.second));
+            tot += t;
+            g_timer.pool.push_back(pr.first);
+            g_timer.pool.push_back(pr.second);
+        }
+        ms[k] = tot;
+        launches[k] = (int64_t)g_timer.pending[k].size();
+        g_timer.pending[k].clear();
+    }
+    return RBG_OK;
+}
 
 extern "C" int32_t rbg_fw_dense_workspace_bytes(int32_t dtype, int64_t n, uint32_t mode, int64_t *bytes) {
     if (!bytes || n < 0 || dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;

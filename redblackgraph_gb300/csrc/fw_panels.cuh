@@ -76,6 +76,7 @@ fw_diag_kernel(U *__restrict__ work_base, int *__restrict__ any_base, RoundBuf<U
     const int64_t np = cmp.np;
     RoundBuf<U> *rb = rbs + cmp.rb_index;
     DevStatus *st = st_base + cmp.status_index;
+    if (tid == 0) atomicAdd(&st->executed, (unsigned long long)FW_B * FW_B * FW_B);
     for (int e = tid; e < 2 * (int)(np / FW_P); e += DG_THREADS) any_base[cmp.any_off + e] = 0;
     const int b = tid % FW_B, h = tid / FW_B;
     U R[DG_ROWS];
@@ -209,6 +210,7 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     const int nct = (int)(np / PN_LINES);             // CTAs per panel
     const bool rowPanel = local < nct;
     const int cta = rowPanel ? local : local - nct;
+    if (tid == 0) atomicAdd(&st->executed, (unsigned long long)PN_LINES * FW_B * FW_B);
     if (tid == 0) S.any = 0;
     {
         // batched 16-byte loads first, then the shared-memory stores (no serial round trips)

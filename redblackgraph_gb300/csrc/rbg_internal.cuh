@@ -20,7 +20,8 @@ struct DevStatus {
     long long first_hang;          // exact path: first index where the reference would hang
     long long first_cycle;         // exact path: first cycle index (Cython raises here)
     long long first_ovf;           // exact path: first overflow index
-    long long pad1[7];
+    unsigned long long executed;   // relaxations the blocked kernels executed (not skipped)
+    long long pad1[6];
 };
 static_assert(sizeof(DevStatus) == 128, "status block is 128 bytes");
 
@@ -36,6 +37,9 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // grid size for grid-stride loops: a multiple of the SM count
 int grid_for(int64_t work, int threads);
+
+// running count of kernel launches issued by this library (rbg_launch_count)
+void note_launches(int64_t k);
 
 template <typename T> struct dtype_of;
 template <> struct dtype_of<int8_t> { static const int value = RBG_DTYPE_INT8; };
