@@ -147,7 +147,8 @@ struct FwComp {
     int64_t ld_in, ld_out;    // their leading dimensions
     int64_t work_off;         // lane offset of the np x np work matrix
     int64_t cp_off, rp_off;   // lane offsets of the snapshot panels (FW_B x np each, t-major)
-    int64_t any_off;          // int offset of the panel flags (anyCP then anyRP, np / FW_P each)
+    int64_t any_off;          // int offset of the panel flags: one per 64-line group, column
+                              // panel then row panel (np / 64 each); 0 = all lines zero
     int64_t rb_index;         // round-buffer index
     int32_t triangular, status_index;
 };
@@ -250,7 +251,7 @@ template <typename U, int BN> struct TileSmem {
 };
 
 template <typename U, int BN, int TM, int TN>
-__global__ void __launch_bounds__(FW_THREADS)
+__global__ void __launch_bounds__(FW_THREADS, 2)
 fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
                const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix, int count,
                int64_t K0, int lbits, DevStatus *st_base) {
@@ -269,13 +270,19 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     U *work = work_base + cmp.work_off;
     const U *cpbuf = work_base + cmp.cp_off;
     const U *rpbuf = work_base + cmp.rp_off;
-    const int *anyCP = any_base + cmp.any_off;
-    const int *anyRP = anyCP + np / FW_P;
+    const int *anyCP = any_base + cmp.any_off;       // per 64-row group of the column panel
+    const int *anyRP = anyCP + np / FW_B;            // per 64-column group of the row panel
     DevStatus *st = st_base + cmp.status_index;
     const int64_t local = (int64_t)blockIdx.x - prefix[ci];
     const int tJn = (int)(np / BN);
     const int tI = (int)(local / tJn), tJ = (int)(local % tJn);
-    if (!anyCP[tI] || !anyRP[(int)(((int64_t)tJ * BN) / FW_P)]) return;
+    constexpr int GC = BN / FW_B;                    // 64-column groups in this tile
+    const bool cg0 = anyCP[2 * tI] != 0, cg1 = anyCP[2 * tI + 1] != 0;
+    bool rg[GC];
+    bool anyr = false;
+#pragma unroll
+    for (int gq = 0; gq < GC; ++gq) { rg[gq] = anyRP[tJ * GC + gq] != 0; anyr |= rg[gq]; }
+    if (!(cg0 || cg1) || !anyr) return;   // an all-zero panel group wrote no snapshots
     const int64_t I0 = (int64_t)tI * BM, J0 = (int64_t)tJ * BN;
     const int tid = threadIdx.x;
     if (tid == 0) { S.colAny = 0; S.rowAny = 0; S.nactive = 0; }
@@ -287,15 +294,17 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
         constexpr int NC = FW_B * BM / PER / FW_THREADS;      // column-panel vectors per thread
         constexpr int NR = FW_B * BN / PER / FW_THREADS;      // row-panel vectors per thread
         uint4 vc[NC], vr[NR];
+        const uint4 zero4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
 #pragma unroll
         for (int i = 0; i < NC; ++i) {
             const int e = tid + i * FW_THREADS, t = e / (BM / PER), r = (e % (BM / PER)) * PER;
-            vc[i] = *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r);
+            const bool live = (r < FW_B) ? cg0 : cg1;
+            vc[i] = live ? *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r) : zero4;
         }
 #pragma unroll
         for (int i = 0; i < NR; ++i) {
             const int e = tid + i * FW_THREADS, t = e / (BN / PER), c = (e % (BN / PER)) * PER;
-            vr[i] = *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c);
+            vr[i] = rg[c / FW_B] ? *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c) : zero4;
         }
 #pragma unroll
         for (int i = 0; i < NC; ++i) {
@@ -364,9 +373,13 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     for (int c = 0; c < TN; ++c) cidx[c] = (c < HN) ? tx * HN + c : BN / 2 + tx * HN + (c - HN);
     U acc[TM][TN];
     unsigned long long wasInf = 0;
+    unsigned rowWork = 0;   // bit r: row r0 + r has a nonzero operand at some active step
+#pragma unroll
+    for (int r = 0; r < TM; ++r) rowWork |= (unsigned)((S.maskC[r0 + r] & act) != 0) << r;
     static_assert(HN * sizeof(U) == 16, "each column group is one 16-byte vector");
 #pragma unroll
     for (int r = 0; r < TM; ++r) {
+        if (!((rowWork >> r) & 1u)) continue;       // cannot change: neither read nor written
         const U *row = work + (I0 + r0 + r) * np + J0;
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
@@ -382,12 +395,19 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     }
 
     const int na = S.nactive;
-    if (tid == 0) atomicAdd(&st->executed, (unsigned long long)na * BM * BN);
+    unsigned steps_done = 0;
     for (int q = 0; q < na; ++q) {
         const int t = S.active[q];
         U x[TM], m[TN], l[TN];
+        bool anyx = false;
 #pragma unroll
-        for (int r = 0; r < TM; ++r) x[r] = S.CPt[t][r0 + r];
+        for (int r = 0; r < TM; ++r) {
+            x[r] = S.CPt[t][r0 + r];
+            anyx |= L::valid(x[r]);
+        }
+        // the warp's 16 rows all zero at step t: every product is zero
+        if (!__any_sync(0xffffffffu, anyx)) continue;
+        ++steps_done;
 #pragma unroll
         for (int c = 0; c < TN; ++c) { m[c] = S.RPm[t][cidx[c]]; l[c] = S.RPl[t][cidx[c]]; }
 #pragma unroll
@@ -395,6 +415,8 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
 #pragma unroll
             for (int c = 0; c < TN; ++c) acc[r][c] = umin(acc[r][c], x[r] * m[c] + l[c]);
     }
+    if ((tid & 31) == 0 && steps_done)
+        atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * TM * TN);
 
     // ---- write back, cycle test on the global diagonal, first values for the running max
     unsigned flags = risk ? RBG_EV_RISK : 0u;
@@ -403,6 +425,7 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     // accumulators still hold what the panel launch stored: writing them back is a no-op.
 #pragma unroll
     for (int r = 0; r < TM; ++r) {
+        if (!((rowWork >> r) & 1u)) continue;
         const int64_t gi = I0 + r0 + r;
         U *row = work + gi * np + J0;
 #pragma unroll
@@ -663,7 +686,7 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
         c.cp_off = lanes; lanes += (int64_t)FW_B * c.np;
         c.rp_off = lanes; lanes += (int64_t)FW_B * c.np;
         lanes = (int64_t)align_up((size_t)lanes, 64);
-        c.any_off = anys; anys += 2 * (c.np / FW_P);
+        c.any_off = anys; anys += 2 * (c.np / FW_B);
         c.rb_index = k;
         c.triangular = triangular;
         c.status_index = i;

@@ -77,7 +77,7 @@ fw_diag_kernel(U *__restrict__ work_base, int *__restrict__ any_base, RoundBuf<U
     RoundBuf<U> *rb = rbs + cmp.rb_index;
     DevStatus *st = st_base + cmp.status_index;
     if (tid == 0) atomicAdd(&st->executed, (unsigned long long)FW_B * FW_B * FW_B);
-    for (int e = tid; e < 2 * (int)(np / FW_P); e += DG_THREADS) any_base[cmp.any_off + e] = 0;
+    for (int e = tid; e < 2 * (int)(np / FW_B); e += DG_THREADS) any_base[cmp.any_off + e] = 0;
     const int b = tid % FW_B, h = tid / FW_B;
     U R[DG_ROWS];
 #pragma unroll
@@ -202,15 +202,42 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     U *work = work_base + cmp.work_off;
     U *cpbuf = work_base + cmp.cp_off;
     U *rpbuf = work_base + cmp.rp_off;
-    int *anyCP = any_base + cmp.any_off;
-    int *anyRP = anyCP + np / FW_P;
+    int *anyCP = any_base + cmp.any_off;             // per 64-line group
+    int *anyRP = anyCP + np / FW_B;
     const RoundBuf<U> *rb = rbs + cmp.rb_index;
     DevStatus *st = st_base + cmp.status_index;
     const int local = (int)((int64_t)blockIdx.x - prefix[ci]);
     const int nct = (int)(np / PN_LINES);             // CTAs per panel
     const bool rowPanel = local < nct;
     const int cta = rowPanel ? local : local - nct;
-    if (tid == 0) atomicAdd(&st->executed, (unsigned long long)PN_LINES * FW_B * FW_B);
+
+    const int lanei = tid & 31;
+    const int h = lanei & 3;                          // cells h*16 .. h*16+15 of the line
+    const int grp = lanei & ~3;                       // first lane of this line's group
+    const int64_t g = (int64_t)cta * PN_LINES + (tid >> 2);   // global column / row
+    const bool inK = g >= K0 && g < K0 + FW_B;        // the diagonal tile's own cells
+    const int c0 = h * DG_ROWS;
+    bool risk = false;
+    unsigned steps_done = 0;                          // steps this warp did not skip
+    unsigned long long seen = 0;                      // bit t: the step-t operand is valid
+    unsigned startInf = 0;                            // bit r: cell r was zero at round start
+    U R[DG_ROWS];
+    U *rowp = work + g * np + K0 + c0;                // column panel: this thread's cells
+    if (inK) {
+#pragma unroll
+        for (int r = 0; r < DG_ROWS; ++r) R[r] = L::inf;
+    } else if (rowPanel) {
+#pragma unroll
+        for (int r = 0; r < DG_ROWS; ++r) R[r] = work[(K0 + c0 + r) * np + g];
+    } else {
+        load16<U>(rowp, R);   // 16-byte aligned: K0 and c0 are multiples of 16
+    }
+#pragma unroll
+    for (int r = 0; r < DG_ROWS; ++r) startInf |= (unsigned)(!L::valid(R[r])) << r;
+    // 64 lines that are all zero stay zero this round: no snapshots, no write-back, and the
+    // group flag stays 0 so the tile kernel reads none of them
+    if (!__syncthreads_or(startInf != (1u << DG_ROWS) - 1u)) return;
+
     if (tid == 0) S.any = 0;
     {
         // batched 16-byte loads first, then the shared-memory stores (no serial round trips)
@@ -242,28 +269,6 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     }
     __syncthreads();
 
-    const int lanei = tid & 31;
-    const int h = lanei & 3;                          // cells h*16 .. h*16+15 of the line
-    const int grp = lanei & ~3;                       // first lane of this line's group
-    const int64_t g = (int64_t)cta * PN_LINES + (tid >> 2);   // global column / row
-    const bool inK = g >= K0 && g < K0 + FW_B;        // the diagonal tile's own cells
-    const int c0 = h * DG_ROWS;
-    bool risk = false;
-    unsigned long long seen = 0;                      // bit t: the step-t operand is valid
-    unsigned startInf = 0;                            // bit r: cell r was zero at round start
-    U R[DG_ROWS];
-    U *rowp = work + g * np + K0 + c0;                // column panel: this thread's cells
-    if (inK) {
-#pragma unroll
-        for (int r = 0; r < DG_ROWS; ++r) R[r] = L::inf;
-    } else if (rowPanel) {
-#pragma unroll
-        for (int r = 0; r < DG_ROWS; ++r) R[r] = work[(K0 + c0 + r) * np + g];
-    } else {
-        load16<U>(rowp, R);   // 16-byte aligned: K0 and c0 are multiples of 16
-    }
-#pragma unroll
-    for (int r = 0; r < DG_ROWS; ++r) startInf |= (unsigned)(!L::valid(R[r])) << r;
     const int pc0 = Pad<U>::at(c0);
     const U *tabA = rowPanel ? &S.CS[0][pc0] : &S.RSm[0][pc0];
     const U *tabB = &S.RSl[0][pc0];
@@ -284,6 +289,10 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
             const bool zv = L::valid(z);
             seen |= (unsigned long long)zv << t;
             if (h == 0) S.Z[t][tid >> 2] = z;
+            // a zero step operand makes every product of the step a zero: skip the step when
+            // it is zero for the whole warp (closures of family trees are sparse)
+            if (!__any_sync(0xffffffffu, zv)) continue;
+            ++steps_done;
             if (rowPanel) {
                 U m, low;
                 L::split(z, m, low);
@@ -330,8 +339,10 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
             smx = max(smx, (SU)first);
         }
     }
+    if ((tid & 31) == 0 && steps_done)
+        atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * DG_ROWS);
     if (seen) atomicOr(&S.any, 1);
     __syncthreads();
-    if (tid == 0) atomicOr((rowPanel ? anyRP : anyCP) + (int)((int64_t)cta * PN_LINES / FW_P), S.any);
+    if (tid == 0) (rowPanel ? anyRP : anyCP)[cta] = S.any;
     flush_status(st, smx > 0 ? (unsigned long long)smx : 0ull, risk ? RBG_EV_RISK : 0u);
 }
