@@ -150,6 +150,7 @@ struct FwComp {
     int64_t any_off;          // int offset of the panel flags: one per 64-line group, column
                               // panel then row panel (np / 64 each); 0 = all lines zero
     int64_t rb_index;         // round-buffer index
+    int64_t occ_off;          // byte offset of the (np/64)^2 block-occupancy map (1 = nonzero)
     int32_t triangular, status_index;
 };
 
@@ -170,62 +171,76 @@ __device__ __forceinline__ int fw_find(const int64_t *__restrict__ prefix, int c
 // triangular mode) the ignored lower triangle as all ones.  `lbits` is the effective width
 // min(storage bits, lane bits).  The running maximum must include d_0(i, j), the value the
 // reference writes at k = 0 (warshall.c.in:88-89); later rounds add each cell's first value.
+constexpr int CONV_ROWS = 8;   // rows of the padded matrix per CTA in convert / finalize
+
 template <typename T, typename U>
 __global__ void __launch_bounds__(FW_THREADS)
 fw_convert_kernel(const T *__restrict__ in_base, U *__restrict__ work_base,
-                  const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix, int count,
-                  int lbits, int sbits, DevStatus *st_base) {
+                  unsigned char *__restrict__ occ_base, const FwComp *__restrict__ comps,
+                  const int64_t *__restrict__ prefix, int count, int lbits, int sbits,
+                  DevStatus *st_base) {
+    typedef typename utype<T>::type TU;
+    typedef lane<U> L;
     const int ci = fw_find(prefix, count, blockIdx.x);
     const FwComp c = comps[ci];
     const T *in = in_base + c.in_off;
     U *work = work_base + c.work_off;
-    const int64_t n = c.n, np = c.np, ld_in = c.ld_in;
+    const int64_t n = c.n, np = c.np, ld = c.ld_in;
     const int triangular = c.triangular;
     DevStatus *st = st_base + c.status_index;
-    const int64_t cta0 = prefix[ci], ctas = prefix[ci + 1] - cta0;
-    typedef typename utype<T>::type TU;
-    typedef lane<U> L;
+    unsigned char *occ = occ_base + c.occ_off;
+    const int nb = (int)(np / FW_B);
     const TU tmax = (TU)~(TU)0;
     const unsigned long long slimit = 1ull << (sbits - 1);   // storage top bit
     const unsigned long long llimit = 1ull << (lbits - 1);   // effective lane top bit
     unsigned flags = 0;
     unsigned long long mx = 0;
-    const int64_t total = np * np;
-    for (int64_t idx = ((int64_t)blockIdx.x - cta0) * blockDim.x + threadIdx.x; idx < total;
-         idx += ctas * blockDim.x) {
-        const int64_t i = idx / np, j = idx - i * np;
-        U w = L::inf;
-        if (i < n && j < n) {
-            TU v = (TU)in[i * ld_in + j];
-            if (i == j) {
-                if (!(v == 0 || v == 1 || v == tmax)) flags |= RBG_EV_UNCLEAN;
-            } else if (!(triangular && i > j) && v != 0) {
-                unsigned long long uv = (unsigned long long)v;
-                if (v == 1 || v == tmax || uv >= slimit) {
-                    flags |= RBG_EV_UNCLEAN;
-                } else if (uv >= llimit) {
-                    flags |= RBG_EV_WIDE;
-                } else {
-                    w = (U)uv;
-                }
-            }
-            // d_0 = W(i,j) (+) W(i,0) (x) W(0,j); row 0 / column 0 products are identities
-            if (!(triangular && i > j) && i != j) {
-                U d0 = w;
-                if (i > 0 && j > 0 && !(triangular && i > 0)) {
-                    TU a = (TU)in[i * ld_in], b = (TU)in[j];
-                    bool ok = a != 0 && b != 0 && a != 1 && b != 1 && a != tmax && b != tmax &&
-                              (unsigned long long)a < llimit && (unsigned long long)b < llimit;
-                    if (ok) {
-                        bool risk = false;
-                        U p = L::product((U)a, (U)b, lbits, risk);
-                        if (!risk) d0 = umin(d0, p);
+    const int64_t r0 = ((int64_t)blockIdx.x - prefix[ci]) * CONV_ROWS;
+    for (int64_t i = r0; i < r0 + CONV_ROWS && i < np; ++i) {
+        // W(i, 0) for the k = 0 product of d_0 (row 0 / column 0 products are identities)
+        const bool rowlive = i < n;
+        const TU wi0 = (rowlive && i > 0 && !triangular) ? (TU)in[i * ld] : (TU)0;
+        const bool xi = wi0 != 0 && wi0 != 1 && wi0 != tmax && (unsigned long long)wi0 < llimit;
+        U *wrow = work + i * np;
+        for (int64_t j0 = (int64_t)threadIdx.x * 4; j0 < np; j0 += (int64_t)FW_THREADS * 4) {
+            U w4[4];
+            bool live = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int64_t j = j0 + k;
+                U w = L::inf;
+                if (rowlive && j < n) {
+                    const TU v = (TU)in[i * ld + j];
+                    if (i == j) {
+                        if (!(v == 0 || v == 1 || v == tmax)) flags |= RBG_EV_UNCLEAN;
+                    } else if (!(triangular && i > j) && v != 0) {
+                        const unsigned long long uv = (unsigned long long)v;
+                        if (v == 1 || v == tmax || uv >= slimit) flags |= RBG_EV_UNCLEAN;
+                        else if (uv >= llimit) flags |= RBG_EV_WIDE;
+                        else w = (U)uv;
+                    }
+                    if (i != j && !(triangular && i > j)) {
+                        // d_0 = W(i,j) (+) W(i,0) (x) W(0,j): the value the reference writes at k = 0
+                        U d0 = w;
+                        if (xi && j > 0) {
+                            const TU b = (TU)in[j];
+                            if (b != 0 && b != 1 && b != tmax && (unsigned long long)b < llimit) {
+                                bool risk = false;
+                                const U p = L::product((U)wi0, (U)b, lbits, risk);
+                                if (!risk) d0 = umin(d0, p);
+                            }
+                        }
+                        if (L::valid(d0) && (unsigned long long)d0 > mx) mx = (unsigned long long)d0;
                     }
                 }
-                if (L::valid(d0) && (unsigned long long)d0 > mx) mx = (unsigned long long)d0;
+                w4[k] = w;
+                live |= L::valid(w);
             }
+            *reinterpret_cast<uint4 *>(wrow + j0) = *reinterpret_cast<const uint4 *>(w4);
+            if (sizeof(U) == 8)
+                *reinterpret_cast<uint4 *>(wrow + j0 + 2) = *reinterpret_cast<const uint4 *>(w4 + 2);
+            if (live) occ[(i / FW_B) * nb + j0 / FW_B] = 1;
         }
-        work[idx] = w;
     }
     flush_status(st, mx, flags);
 }
@@ -251,20 +266,16 @@ template <typename U, int BN> struct TileSmem {
 };
 
 template <typename U, int BN, int TM, int TN>
-__global__ void __launch_bounds__(FW_THREADS, 2)
-fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
-               const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix, int count,
-               int64_t K0, int lbits, DevStatus *st_base) {
+__device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t local, U *__restrict__ work_base,
+                                          const int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+                                          const FwComp *__restrict__ comps, int64_t K0, int lbits,
+                                          DevStatus *st_base) {
     typedef lane<U> L;
     constexpr int BM = FW_P;
     constexpr int TX = BN / TN;           // threads along columns
     constexpr int TY = BM / TM;           // threads along rows
     static_assert(TX * TY == FW_THREADS, "micro-tile layout must use 256 threads");
     constexpr int HN = TN / 2;            // each thread owns two column groups of HN
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
-
-    const int ci = fw_find(prefix, count, blockIdx.x);
     const FwComp cmp = comps[ci];
     const int64_t np = cmp.np;
     U *work = work_base + cmp.work_off;
@@ -272,8 +283,9 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     const U *rpbuf = work_base + cmp.rp_off;
     const int *anyCP = any_base + cmp.any_off;       // per 64-row group of the column panel
     const int *anyRP = anyCP + np / FW_B;            // per 64-column group of the row panel
+    unsigned char *occ = occ_base + cmp.occ_off;
+    const int nb = (int)(np / FW_B);
     DevStatus *st = st_base + cmp.status_index;
-    const int64_t local = (int64_t)blockIdx.x - prefix[ci];
     const int tJn = (int)(np / BN);
     const int tI = (int)(local / tJn), tJ = (int)(local % tJn);
     constexpr int GC = BN / FW_B;                    // 64-column groups in this tile
@@ -429,6 +441,7 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
         const int64_t gi = I0 + r0 + r;
         U *row = work + gi * np + J0;
 #pragma unroll
+        bool anyw = false;
         for (int half = 0; half < 2; ++half) {
             uint4 v4;
             U *w = reinterpret_cast<U *>(&v4);
@@ -448,11 +461,59 @@ fw_tile_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
                     if ((unsigned long long)first > mx) mx = (unsigned long long)first;
                 }
                 w[k] = L::valid(v) ? v : L::inf;
+                anyw |= L::valid(v);
             }
             *reinterpret_cast<uint4 *>(row + cidx[half * HN]) = v4;
+            if (anyw) occ[(gi / FW_B) * nb + (J0 + cidx[half * HN]) / FW_B] = 1;
+            anyw = false;
         }
     }
     flush_status(st, mx, flags);
+}
+
+// Tile worklist: candidate tile (I, J) of this round is an item when a 64-row group of its
+// column panel and a 64-column group of its row panel hold a nonzero snapshot.
+template <int BN>
+__global__ void fw_tile_list_kernel(const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix,
+                                    int count, const int *__restrict__ any_base, int2 *__restrict__ list,
+                                    int *__restrict__ counters) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= prefix[count]) return;
+    const int ci = fw_find(prefix, count, c);
+    const FwComp cmp = comps[ci];
+    const int64_t local = c - prefix[ci];
+    const int tJn = (int)(cmp.np / BN);
+    const int tI = (int)(local / tJn), tJ = (int)(local % tJn);
+    const int *anyCP = any_base + cmp.any_off;
+    const int *anyRP = anyCP + cmp.np / FW_B;
+    constexpr int GC = BN / FW_B;
+    bool r = false;
+#pragma unroll
+    for (int gq = 0; gq < GC; ++gq) r |= anyRP[tJ * GC + gq] != 0;
+    if (!r || !(anyCP[2 * tI] | anyCP[2 * tI + 1])) return;
+    const int slot = atomicAdd(&counters[CNT_TILE], 1);
+    list[slot] = make_int2(ci, (int)local);
+}
+
+template <typename U, int BN, int TM, int TN>
+__global__ void __launch_bounds__(FW_THREADS, 2)
+fw_tile_kernel(U *__restrict__ work_base, const int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+               const FwComp *__restrict__ comps, const int2 *__restrict__ list, int *__restrict__ counters,
+               int64_t K0, int lbits, DevStatus *st_base) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
+    __shared__ int s_item;
+    const int total = counters[CNT_TILE];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_TILE], 1);
+        __syncthreads();
+        const int i = s_item;
+        __syncthreads();
+        if (i >= total) break;
+        const int2 e = list[i];
+        tile_item<U, BN, TM, TN>(S, e.x, e.y, work_base, any_base, occ_base, comps, K0, lbits, st_base);
+        __syncthreads();
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -473,19 +534,19 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
     const U *work = work_base + c.work_off;
     T *out = out_base + c.out_off;
     const int64_t n = c.n, np = c.np;
-    const int64_t cta0 = prefix[ci], ctas = prefix[ci + 1] - cta0;
-    const int64_t total = n * n;
-    for (int64_t idx = ((int64_t)blockIdx.x - cta0) * blockDim.x + threadIdx.x; idx < total;
-         idx += ctas * blockDim.x) {
-        const int64_t i = idx / n, j = idx - i * n;
-        T v;
-        if (i == j || (c.triangular && i > j)) {
-            v = in[i * c.ld_in + j];
-        } else {
-            U w = work[i * np + j];
-            v = lane<U>::valid(w) ? (T)w : (T)0;
+    const int64_t r0 = ((int64_t)blockIdx.x - prefix[ci]) * CONV_ROWS;
+    for (int64_t i = r0; i < r0 + CONV_ROWS && i < n; ++i) {
+        const U *wrow = work + i * np;
+        for (int64_t j = threadIdx.x; j < n; j += FW_THREADS) {
+            T v;
+            if (i == j || (c.triangular && i > j)) {
+                v = in[i * c.ld_in + j];
+            } else {
+                const U w = wrow[j];
+                v = lane<U>::valid(w) ? (T)w : (T)0;
+            }
+            out[i * c.ld_out + j] = v;
         }
-        out[i * c.ld_out + j] = v;
     }
 }
 
@@ -647,7 +708,6 @@ template <typename U> struct TileCfg;
 template <> struct TileCfg<uint32_t> { static const int BN = 128, TM = 8, TN = 8; };
 template <> struct TileCfg<uint64_t> { static const int BN = 64, TM = 8, TN = 4; };
 
-constexpr int CONV_ELEMS_PER_THREAD = 16;
 
 // Everything a (batched) blocked run needs on the host: the component table (sorted by size,
 // descending), the per-kernel CTA prefix sums, the per-round active counts and the workspace
@@ -659,6 +719,7 @@ struct FwPlan {
     std::vector<int> active;                // active[r] = components with n > 64 r
     size_t off_status = 0, off_comps = 0, off_pconv = 0, off_ppanel = 0, off_ptile = 0;
     size_t off_rb = 0, off_any = 0, off_lanes = 0, off_exact = 0, total = 0;
+    size_t off_occ = 0, occ_bytes = 0, off_plist = 0, off_tlist = 0, off_counters = 0;
 };
 
 // sizes[i], in_off[i], out_off[i] of component i (input order); lane = bytes per lane word
@@ -673,7 +734,7 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
     P.pre_conv.assign((size_t)count + 1, 0);
     P.pre_panel.assign((size_t)count + 1, 0);
     P.pre_tile.assign((size_t)count + 1, 0);
-    int64_t lanes = 0, anys = 0, maxn = 0;
+    int64_t lanes = 0, anys = 0, maxn = 0, occs = 0;
     for (int64_t k = 0; k < count; ++k) {
         const int i = order[(size_t)k];
         FwComp &c = P.comps[(size_t)k];
@@ -688,11 +749,10 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
         lanes = (int64_t)align_up((size_t)lanes, 64);
         c.any_off = anys; anys += 2 * (c.np / FW_B);
         c.rb_index = k;
+        c.occ_off = occs; occs += (c.np / FW_B) * (c.np / FW_B);
         c.triangular = triangular;
         c.status_index = i;
-        const int64_t cells = c.np * c.np;
-        int64_t conv = (cells + FW_THREADS * CONV_ELEMS_PER_THREAD - 1) / (FW_THREADS * CONV_ELEMS_PER_THREAD);
-        P.pre_conv[(size_t)k + 1] = P.pre_conv[(size_t)k] + std::max<int64_t>(conv, 1);
+        P.pre_conv[(size_t)k + 1] = P.pre_conv[(size_t)k] + (c.np + CONV_ROWS - 1) / CONV_ROWS;
         const bool big = c.n > FW_B;   // n <= 64: the diagonal tile is the whole matrix
         P.pre_panel[(size_t)k + 1] = P.pre_panel[(size_t)k] + (big ? 2 * (c.np / PN_LINES) : 0);
         P.pre_tile[(size_t)k + 1] = P.pre_tile[(size_t)k] + (big ? (c.np / tile_bn) * (c.np / FW_P) : 0);
@@ -713,6 +773,11 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
     P.off_ptile = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
     P.off_rb = o; o = align_up(o + (size_t)count * (lane == 8 ? sizeof(RoundBuf<uint64_t>) : sizeof(RoundBuf<uint32_t>)), 256);
     P.off_any = o; o = align_up(o + (size_t)anys * 4, 256);
+    P.off_occ = o; P.occ_bytes = (size_t)occs; o = align_up(o + (size_t)occs, 256);
+    const int a0 = rounds > 0 ? P.active[0] : 0;
+    P.off_plist = o; o = align_up(o + (size_t)std::max<int64_t>(P.pre_panel[(size_t)a0], 1) * 8, 256);
+    P.off_tlist = o; o = align_up(o + (size_t)std::max<int64_t>(P.pre_tile[(size_t)a0], 1) * 8, 256);
+    P.off_counters = o; o = align_up(o + 64, 256);
     P.off_lanes = o; o = align_up(o + (size_t)lanes * lane, 256);
     P.off_exact = o; o = align_up(o + 3 * align_up((size_t)maxn, 32) * elem_bytes + 256, 256);
     P.total = o;
@@ -776,9 +841,27 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     const int lbits = std::min<int>(sbits, (int)sizeof(U) * 8);
 
     note_launches(2);
+    unsigned char *occ = ws + P.off_occ;
+    int2 *plist = reinterpret_cast<int2 *>(ws + P.off_plist);
+    int2 *tlist = reinterpret_cast<int2 *>(ws + P.off_tlist);
+    int *counters = reinterpret_cast<int *>(ws + P.off_counters);
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    const int64_t persist = 2 * (int64_t)sms;   // two CTAs per SM for both persistent kernels
+
+    RBG_CUDA_TRY(cudaMemsetAsync(occ, 0, std::max<size_t>(P.occ_bytes, 1), stream));
     status_init_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(st, cnt);
-    fw_convert_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
-        in, lanes, comps, pconv, cnt, lbits, sbits, st);
+    {
+        cudaEvent_t tc = timer_begin(3, stream);
+        fw_convert_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
+            in, lanes, occ, comps, pconv, cnt, lbits, sbits, st);
+        timer_end(3, tc, stream);
+    }
     RBG_CUDA_TRY(cudaGetLastError());
     if (stop_after_convert) {
         int rc = read_status(st, h_status, cnt, stream);
@@ -788,29 +871,38 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     for (size_t r = 0; r < P.active.size(); ++r) {
         const int a = P.active[r];
         const int64_t K0 = (int64_t)r * FW_B;
-        note_launches(1 + (P.pre_panel[(size_t)a] > 0) + (P.pre_tile[(size_t)a] > 0));
+        const int64_t np_ = P.pre_panel[(size_t)a], nt_ = P.pre_tile[(size_t)a];
+        note_launches(1 + (np_ > 0 ? 2 : 0) + (nt_ > 0 ? 2 : 0));
         cudaEvent_t td = timer_begin(2, stream);
-        fw_diag_kernel<U><<<a, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(lanes, any, rbs, comps, K0,
-                                                                           lbits, st);
+        fw_diag_kernel<U><<<a, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(lanes, any, rbs, comps, counters,
+                                                                           K0, lbits, st);
         timer_end(2, td, stream);
-        if (P.pre_panel[(size_t)a] > 0) {
+        if (np_ > 0) {
             cudaEvent_t t0 = timer_begin(1, stream);
-            fw_panel_kernel<U><<<(unsigned)P.pre_panel[(size_t)a], PN_THREADS, sizeof(PanelSmem<U>), stream>>>(
-                lanes, any, rbs, comps, ppanel, a, K0, lbits, st);
+            fw_panel_list_kernel<<<(unsigned)((np_ + 255) / 256), 256, 0, stream>>>(comps, ppanel, a, K0, occ,
+                                                                                    plist, counters);
+            fw_panel_kernel<U><<<(unsigned)std::min<int64_t>(np_, persist), PN_THREADS, sizeof(PanelSmem<U>),
+                                 stream>>>(lanes, any, occ, rbs, comps, plist, counters, K0, lbits, st);
             timer_end(1, t0, stream);
         }
-        if (P.pre_tile[(size_t)a] > 0) {
+        if (nt_ > 0) {
             cudaEvent_t t0 = timer_begin(0, stream);
-            fw_tile_kernel<U, C::BN, C::TM, C::TN><<<(unsigned)P.pre_tile[(size_t)a], FW_THREADS,
+            fw_tile_list_kernel<C::BN><<<(unsigned)((nt_ + 255) / 256), 256, 0, stream>>>(comps, ptile, a, any,
+                                                                                       tlist, counters);
+            fw_tile_kernel<U, C::BN, C::TM, C::TN><<<(unsigned)std::min<int64_t>(nt_, persist), FW_THREADS,
                                                     sizeof(TileSmem<U, C::BN>), stream>>>(
-                lanes, any, comps, ptile, a, K0, lbits, st);
+                lanes, any, occ, comps, tlist, counters, K0, lbits, st);
             timer_end(0, t0, stream);
         }
     }
     RBG_CUDA_TRY(cudaGetLastError());
     note_launches(1);
-    fw_finalize_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
-        in, lanes, out, comps, pconv, cnt, st);
+    {
+        cudaEvent_t tf = timer_begin(3, stream);
+        fw_finalize_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
+            in, lanes, out, comps, pconv, cnt, st);
+        timer_end(3, tf, stream);
+    }
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }

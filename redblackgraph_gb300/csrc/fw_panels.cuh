@@ -65,7 +65,8 @@ template <typename U> struct DiagSmem {
 template <typename U>
 __global__ void __launch_bounds__(DG_THREADS)
 fw_diag_kernel(U *__restrict__ work_base, int *__restrict__ any_base, RoundBuf<U> *__restrict__ rbs,
-               const FwComp *__restrict__ comps, int64_t K0, int lbits, DevStatus *st_base) {
+               const FwComp *__restrict__ comps, int *__restrict__ counters, int64_t K0, int lbits,
+               DevStatus *st_base) {
     typedef lane<U> L;
     typedef typename signed_of<U>::type SU;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -78,6 +79,7 @@ fw_diag_kernel(U *__restrict__ work_base, int *__restrict__ any_base, RoundBuf<U
     DevStatus *st = st_base + cmp.status_index;
     if (tid == 0) atomicAdd(&st->executed, (unsigned long long)FW_B * FW_B * FW_B);
     for (int e = tid; e < 2 * (int)(np / FW_B); e += DG_THREADS) any_base[cmp.any_off + e] = 0;
+    if (blockIdx.x == 0 && tid < 4) counters[tid] = 0;   // this round's worklists start empty
     const int b = tid % FW_B, h = tid / FW_B;
     U R[DG_ROWS];
 #pragma unroll
@@ -185,18 +187,17 @@ template <typename U> __device__ __forceinline__ U shfl_lane(U v, int src) {
     return (U)__shfl_sync(0xffffffffu, (unsigned)v, src);
 }
 
+// One panel item: 64 lines (a 64 x 64 block) of component ci's row panel (local < np / 64)
+// or column panel.
 template <typename U>
-__global__ void __launch_bounds__(PN_THREADS, 2)
-fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
-                const RoundBuf<U> *__restrict__ rbs, const FwComp *__restrict__ comps,
-                const int64_t *__restrict__ prefix, int count, int64_t K0, int lbits,
-                DevStatus *st_base) {
+__device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U *__restrict__ work_base,
+                                           int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+                                           const RoundBuf<U> *__restrict__ rbs,
+                                           const FwComp *__restrict__ comps, int64_t K0, int lbits,
+                                           DevStatus *st_base) {
     typedef lane<U> L;
     typedef typename signed_of<U>::type SU;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
     const int tid = threadIdx.x;
-    const int ci = fw_find(prefix, count, blockIdx.x);
     const FwComp cmp = comps[ci];
     const int64_t np = cmp.np;
     U *work = work_base + cmp.work_off;
@@ -204,10 +205,11 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     U *rpbuf = work_base + cmp.rp_off;
     int *anyCP = any_base + cmp.any_off;             // per 64-line group
     int *anyRP = anyCP + np / FW_B;
+    unsigned char *occ = occ_base + cmp.occ_off;     // (np/64)^2 block occupancy
+    const int nb = (int)(np / FW_B);
     const RoundBuf<U> *rb = rbs + cmp.rb_index;
     DevStatus *st = st_base + cmp.status_index;
-    const int local = (int)((int64_t)blockIdx.x - prefix[ci]);
-    const int nct = (int)(np / PN_LINES);             // CTAs per panel
+    const int nct = (int)(np / PN_LINES);             // items per panel
     const bool rowPanel = local < nct;
     const int cta = rowPanel ? local : local - nct;
 
@@ -315,6 +317,7 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     }
     // write back; the running maximum needs each newly valid cell's first valid product
     SU smx = 0;
+    bool wrote = false;
 #pragma unroll
     for (int r = 0; r < DG_ROWS; ++r) {
         const U v = R[r];
@@ -323,6 +326,7 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
         if (!inK) {
             if (rowPanel) work[(K0 + c) * np + g] = vv ? v : L::inf;
             else rowp[r] = vv ? v : L::inf;
+            wrote |= vv;
         }
         if (vv && ((startInf >> r) & 1u)) {
             const unsigned long long both = seen & (rowPanel ? S.maskCS[c] : S.maskRS[c]);
@@ -344,5 +348,57 @@ fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base,
     if (seen) atomicOr(&S.any, 1);
     __syncthreads();
     if (tid == 0) (rowPanel ? anyRP : anyCP)[cta] = S.any;
+    if (wrote) {
+        const int kb = (int)(K0 / FW_B);
+        occ[rowPanel ? (int64_t)kb * nb + cta : (int64_t)cta * nb + kb] = 1;
+    }
     flush_status(st, smx > 0 ? (unsigned long long)smx : 0ull, risk ? RBG_EV_RISK : 0u);
+}
+
+// Work counters of a round: [0] panel items, [1] panel cursor, [2] tile items, [3] tile cursor.
+// Reset by the diagonal kernel at the start of every round.
+constexpr int CNT_PANEL = 0, CUR_PANEL = 1, CNT_TILE = 2, CUR_TILE = 3;
+
+// Panel worklist: candidate c of this round's panel prefix -> item if its 64 x 64 block of the
+// work matrix holds a nonzero (a zero block stays zero and needs no forward substitution).
+__global__ void fw_panel_list_kernel(const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix,
+                                     int count, int64_t K0, const unsigned char *__restrict__ occ_base,
+                                     int2 *__restrict__ list, int *__restrict__ counters) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= prefix[count]) return;
+    const int ci = fw_find(prefix, count, c);
+    const FwComp cmp = comps[ci];
+    const int local = (int)(c - prefix[ci]);
+    const int nb = (int)(cmp.np / FW_B);
+    const bool rowPanel = local < nb;
+    const int grp = rowPanel ? local : local - nb;
+    const int kb = (int)(K0 / FW_B);
+    if (grp == kb) return;                           // the diagonal block itself
+    const unsigned char *occ = occ_base + cmp.occ_off;
+    if (!occ[rowPanel ? (int64_t)kb * nb + grp : (int64_t)grp * nb + kb]) return;
+    const int slot = atomicAdd(&counters[CNT_PANEL], 1);
+    list[slot] = make_int2(ci, local);
+}
+
+// Persistent panel kernel: CTAs pull items from the worklist until it is exhausted.
+template <typename U>
+__global__ void __launch_bounds__(PN_THREADS, 2)
+fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+                const RoundBuf<U> *__restrict__ rbs, const FwComp *__restrict__ comps,
+                const int2 *__restrict__ list, int *__restrict__ counters, int64_t K0, int lbits,
+                DevStatus *st_base) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
+    __shared__ int s_item;
+    const int total = counters[CNT_PANEL];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_PANEL], 1);
+        __syncthreads();
+        const int i = s_item;
+        __syncthreads();
+        if (i >= total) break;
+        const int2 e = list[i];
+        panel_item<U>(S, e.x, e.y, work_base, any_base, occ_base, rbs, comps, K0, lbits, st_base);
+        __syncthreads();
+    }
 }
