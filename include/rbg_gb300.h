@@ -116,6 +116,26 @@ int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_t ld_in, vo
                      int64_t ld_out, uint32_t mode, void *workspace, int64_t workspace_bytes,
                      rbg_result_t *result, rbg_stream_t stream);
 
+/* Largest n, and the size of the fixed device scratch array, of rbg_fw_dense_noalloc. */
+#define RBG_NOALLOC_MAX_N 1024
+#define RBG_NOALLOC_SCRATCH_BYTES (12u << 20)
+
+/*
+ * Dense AVOS closure that allocates nothing: same arguments, results and errors as
+ * rbg_fw_dense, but without a workspace.  This entry point has no counterpart in the
+ * reference.  It serves callers that cannot call cudaMalloc (allocation forbidden or unsafe
+ * where they run, or a host program that owns only its input and output buffers): the
+ * scratch is a 12 MiB array in the library's device image, which every GPU that loads the
+ * library holds until the process exits.  n must be at most RBG_NOALLOC_MAX_N, otherwise the
+ * call returns RBG_ERR_CAPACITY without touching the GPU.  The first call on a device looks up
+ * the array's device address; make that first call before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU race on it and must be serialised by the
+ * caller.  Synchronises `stream`.
+ */
+int32_t rbg_fw_dense_noalloc(int32_t dtype, int64_t n, const void *in, int64_t ld_in, void *out,
+                             int64_t ld_out, uint32_t mode, rbg_result_t *result,
+                             rbg_stream_t stream);
+
 /* Scratch bytes rbg_fw_batch needs for `count` matrices of sizes `sizes` (host array). */
 int32_t rbg_fw_batch_workspace_bytes(int32_t dtype, int64_t count, const int64_t *sizes,
                                      uint32_t mode, int64_t *bytes);

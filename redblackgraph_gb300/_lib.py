@@ -37,6 +37,8 @@ MODE_FORCE_WIDE = 8
 
 PATH_BLOCKED32, PATH_BLOCKED64, PATH_EXACT = 1, 2, 3
 
+NOALLOC_MAX_N = 1024   # include/rbg_gb300.h RBG_NOALLOC_MAX_N
+
 
 class RbgResult(ctypes.Structure):
     _fields_ = [
@@ -63,6 +65,8 @@ SIGNATURES = [
     ("rbg_fw_dense_workspace_bytes", _I32, [_I32, _I64, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_dense", _I32, [_I32, _I64, _P, _I64, _P, _I64, _U32, _P, _I64,
                             ctypes.POINTER(RbgResult), _P]),
+    ("rbg_fw_dense_noalloc", _I32, [_I32, _I64, _P, _I64, _P, _I64, _U32,
+                                    ctypes.POINTER(RbgResult), _P]),
     ("rbg_fw_batch_workspace_bytes", _I32, [_I32, _I64, _P, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_batch", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, _P, _P]),
     ("rbg_avos_matmul_workspace_bytes", _I32, [_I32, _I64, _I64, _I64, ctypes.POINTER(_I64)]),

@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <vector>
 #include <atomic>
+#include <mutex>
 #include "rbg_internal.cuh"
 
 namespace rbg {
@@ -1138,6 +1139,64 @@ extern "C" int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out),
                            ld_out, mode, ws, result, s));
+    return rc;
+}
+
+// ------------------------------------------------------------------------------------------
+// Closure without any device allocation by the caller.
+//
+// Some callers cannot call cudaMalloc at all: code running where allocation is forbidden or
+// would deadlock (inside a foreign allocator's callback, under an allocation-free real-time
+// policy), or a host program that only owns the input and output buffers and must not grow the
+// device heap.  rbg_fw_dense_noalloc takes its scratch from this file-scope device array
+// instead of a workspace argument.  Every GPU that loads the library holds the array until the
+// process exits.  All calls share it: each call clears or fully rewrites the scratch state it
+// reads, but two calls whose work overlaps on the GPU (different streams, or different host
+// threads on the same device) race on it and must be serialised by the caller.
+// ------------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[RBG_NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // the array's device address, per device
+
+// Device address of the scratch array on the current device.  In host code the array's name is
+// only a host-side stand-in, so the address is asked of the runtime once per device (with that
+// device current) and cached; this first call must come before any stream capture.
+static int noalloc_scratch(void **ptr) {
+    int dev = 0;
+    RBG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return RBG_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) return RBG_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *ptr = g_noalloc_ptr[dev];
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_fw_dense_noalloc(int32_t dtype, int64_t n, const void *in, int64_t ld_in, void *out,
+                                        int64_t ld_out, uint32_t mode, rbg_result_t *result,
+                                        rbg_stream_t stream) {
+    if (!result || n < 0 || (n > 0 && (!in || !out)) || ld_in < n || ld_out < n) return RBG_ERR_INVALID;
+    if (dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;
+    if ((mode & RBG_MODE_CYTHON) && dtype != RBG_DTYPE_INT32) return RBG_ERR_INVALID;
+    memset(result, 0, sizeof(*result));
+    result->k = result->i = result->j = -1;
+    if (n > RBG_NOALLOC_MAX_N || single_workspace(n, dtype) > (size_t)RBG_NOALLOC_SCRATCH_BYTES)
+        return RBG_ERR_CAPACITY;   // beyond what the fixed scratch array holds
+    if (n == 0) return RBG_OK;
+    void *ws = nullptr;
+    int rc = noalloc_scratch(&ws);
+    if (rc) return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    rc = RBG_ERR_INVALID;
+    RBG_DISPATCH_DTYPE(dtype, T,
+        rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out), ld_out,
+                           mode, reinterpret_cast<unsigned char *>(ws), result, s));
     return rc;
 }
 

@@ -1,0 +1,72 @@
+"""The dense closure entry point that allocates nothing (rbg_fw_dense_noalloc).
+
+It exists for callers that cannot call cudaMalloc -- code that runs where allocating is
+forbidden or unsafe, or a host program that owns only its input and output buffers.  Its
+scratch lives in a fixed array inside the library, shared by every call, so these tests check
+that its results equal the workspace entry point's (bit-exact integers) on two calls in a row
+with different inputs, and that a size beyond the array is refused.  This file is named to be
+collected last; it must pass alone in a fresh process as well as after the other tests.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _close_with_workspace(L, _lib, d, out):
+    import torch
+    from redblackgraph_gb300.device import numpy_dtype, stream_handle
+    n = d.shape[0]
+    code = _lib.dtype_code(numpy_dtype(d.dtype))
+    nbytes = ctypes.c_int64(0)
+    assert L.rbg_fw_dense_workspace_bytes(code, n, 0, ctypes.byref(nbytes)) == _lib.RBG_OK
+    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=d.device)
+    res = _lib.RbgResult()
+    rc = L.rbg_fw_dense(code, n, d.data_ptr(), n, out.data_ptr(), n, 0, ws.data_ptr(), ws.numel(),
+                        ctypes.byref(res), stream_handle())
+    assert rc == _lib.RBG_OK
+    return res
+
+
+def _close_without_workspace(L, _lib, d, out):
+    from redblackgraph_gb300.device import numpy_dtype, stream_handle
+    n = d.shape[0]
+    res = _lib.RbgResult()
+    rc = L.rbg_fw_dense_noalloc(_lib.dtype_code(numpy_dtype(d.dtype)), n, d.data_ptr(), n,
+                                out.data_ptr(), n, 0, ctypes.byref(res), stream_handle())
+    assert rc == _lib.RBG_OK
+    return res
+
+
+def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(native):
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.device import to_device, to_host
+    L = native
+    cases = [(700, 14, 11, np.int32), (_lib.NOALLOC_MAX_N, 16, 12, np.int64)]
+    for n, gens, seed, dtype in cases:          # two calls in a row, different inputs
+        A = synth.pedigree(n, gens, seed, dtype=dtype)
+        d = to_device(A)
+        ref_out = torch.empty_like(d)
+        ref = _close_with_workspace(L, _lib, d, ref_out)
+        out = torch.full_like(d, 7)             # stale contents must not leak into the result
+        res = _close_without_workspace(L, _lib, d, out)
+        torch.cuda.synchronize()
+        assert res.status == ref.status == _lib.RBG_OK
+        assert res.diameter == ref.diameter and res.path == ref.path
+        assert (to_host(out) == to_host(ref_out)).all()
+        assert (to_host(d) == A).all()          # the input is left untouched
+
+
+def test_noalloc_refuses_sizes_beyond_its_array(native):
+    import torch
+    from redblackgraph_gb300 import _lib
+    from redblackgraph_gb300.device import stream_handle
+    n = _lib.NOALLOC_MAX_N + 1
+    d = torch.zeros((n, n), dtype=torch.int32, device="cuda")
+    res = _lib.RbgResult()
+    rc = native.rbg_fw_dense_noalloc(4, n, d.data_ptr(), n, d.data_ptr(), n, 0, ctypes.byref(res),
+                                     stream_handle())
+    assert rc == _lib.RBG_ERR_CAPACITY
