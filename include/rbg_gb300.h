@@ -155,6 +155,71 @@ int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const i
                      const void *in, void *out, uint32_t mode, void *workspace,
                      int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream);
 
+/* ---------------------------------------------------------------------- sparse product */
+
+/* A CSR matrix in device memory: int64 row pointers, int32 column indices (sorted, no
+ * duplicates within a row), values of the call's dtype. */
+typedef struct rbg_csr {
+    int64_t n_rows, n_cols;
+    const int64_t *indptr;
+    const int32_t *indices;
+    const void *data;
+} rbg_csr_t;
+
+/* scalar semantics of the sparse product */
+#define RBG_SEM_C64 0  /* rb_matrix @: C core algebra on values widened to 64 bits, result cast
+                          back to the storage type (redblackgraph/sparse/rbm.py:83-121)        */
+#define RBG_SEM_CY32 1 /* redblackgraph.gpu: int32 values, Cython algebra, silent wrap
+                          (redblackgraph/gpu/spgemm_numeric.py:61-88)                          */
+
+/* Bytes of the workspace that lives from rbg_spgemm_count to rbg_spgemm_gather ("head"). */
+int32_t rbg_spgemm_head_bytes(int64_t n_rows, int64_t *bytes);
+
+/*
+ * Step 1 of C = A (x) B, optionally merged with R as one squaring step R (+) R^2 (R = A = B,
+ * R's value kept on magnitude ties, result int32: redblackgraph/sparse/csgraph/
+ * transitive_closure.py:272-357, redblackgraph/gpu/transitive_closure.py:77-156): counts the
+ * candidate products per row (replaces rbm_matmat_pass1, redblackgraph/sparse/sparsetools/
+ * rbm_math.h:117-156, and the symbolic phase, redblackgraph/gpu/spgemm_symbolic.py:250-353).
+ * `upper` keeps only columns j >= i (redblackgraph/gpu/spgemm.py:32-119).  Returns the total
+ * candidates and the number of rows that need the dense accumulator.  Synchronises `stream`.
+ */
+int32_t rbg_spgemm_count(const rbg_csr_t *A, const rbg_csr_t *B, const rbg_csr_t *R, int32_t upper,
+                         void *head, int64_t head_bytes, int64_t *total_candidates,
+                         int64_t *dense_rows, rbg_stream_t stream);
+
+/* Bytes of the second workspace ("tail") for the counts rbg_spgemm_count returned. */
+int32_t rbg_spgemm_tail_bytes(int64_t n_rows, int64_t n_cols, int64_t total_candidates,
+                              int64_t dense_rows, int64_t *bytes);
+
+/*
+ * Step 2: numeric product (replaces rbm_matmat_pass2, redblackgraph/sparse/sparsetools/
+ * rbm_math.h:165-222, and the numeric phase, redblackgraph/gpu/spgemm_numeric.py:104-327).
+ * Each row's columns come out sorted; zero sums are dropped.  Returns nnz(C) and the event
+ * flags (RBG_ERR_OVERFLOW when a RBG_SEM_C64 product overflows).  Synchronises `stream`.
+ */
+int32_t rbg_spgemm_numeric(int32_t sem, int32_t dtype, const rbg_csr_t *A, const rbg_csr_t *B,
+                           const rbg_csr_t *R, int32_t upper, void *head, void *tail,
+                           int64_t tail_bytes, int64_t total_candidates, int64_t dense_rows,
+                           int64_t *nnz, uint32_t *flags, rbg_stream_t stream);
+
+/* Step 3: write C into caller buffers: indptr (n_rows + 1, int64), indices (nnz, int32),
+ * data (nnz, dtype).  Ordered on `stream`, no synchronisation. */
+int32_t rbg_spgemm_gather(int32_t dtype, int64_t n_rows, int64_t n_cols, const void *head,
+                          const void *tail, int64_t total_candidates, int64_t dense_rows,
+                          int64_t *indptr, int32_t *indices, void *data, rbg_stream_t stream);
+
+/*
+ * Z = X (+) Y cell by cell with the squaring merge's magnitude rule (the value of smaller
+ * |value|, X's on a tie, zero results dropped; int32 values, sorted rows).  Replaces
+ * sparse_avos_sum_gpu (redblackgraph/gpu/transitive_closure.py:77-156).  Count step (head sized
+ * by rbg_spgemm_head_bytes; synchronises `stream`), then fill step into caller buffers.
+ */
+int32_t rbg_csr_merge_count(const rbg_csr_t *X, const rbg_csr_t *Y, void *head, int64_t head_bytes,
+                            int64_t *nnz, rbg_stream_t stream);
+int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, const void *head, int64_t *indptr,
+                           int32_t *indices, int32_t *data, rbg_stream_t stream);
+
 /* Scratch bytes rbg_avos_matmul needs. */
 int32_t rbg_avos_matmul_workspace_bytes(int32_t dtype, int64_t m, int64_t q, int64_t p,
                                         int64_t *bytes);

@@ -54,6 +54,13 @@ class RbgResult(ctypes.Structure):
     ]
 
 
+class RbgCsr(ctypes.Structure):
+    """rbg_csr_t: a device CSR matrix (int64 row pointers, int32 indices, values)."""
+    _fields_ = [("n_rows", ctypes.c_int64), ("n_cols", ctypes.c_int64),
+                ("indptr", ctypes.c_void_p), ("indices", ctypes.c_void_p),
+                ("data", ctypes.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported entry point; include/rbg_gb300.h declares them
 _P = ctypes.c_void_p
 _I32, _U32, _I64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
@@ -69,6 +76,17 @@ SIGNATURES = [
                                     ctypes.POINTER(RbgResult), _P]),
     ("rbg_fw_batch_workspace_bytes", _I32, [_I32, _I64, _P, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_batch", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, _P, _P]),
+    ("rbg_spgemm_head_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
+    ("rbg_spgemm_count", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr),
+                                _I32, _P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _P]),
+    ("rbg_spgemm_tail_bytes", _I32, [_I64, _I64, _I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_spgemm_numeric", _I32, [_I32, _I32, ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr),
+                                  ctypes.POINTER(RbgCsr), _I32, _P, _P, _I64, _I64, _I64,
+                                  ctypes.POINTER(_I64), ctypes.POINTER(_U32), _P]),
+    ("rbg_spgemm_gather", _I32, [_I32, _I64, _I64, _P, _P, _I64, _I64, _P, _P, _P, _P]),
+    ("rbg_csr_merge_count", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _I64,
+                                   ctypes.POINTER(_I64), _P]),
+    ("rbg_csr_merge_fill", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _P, _P, _P, _P]),
     ("rbg_avos_matmul_workspace_bytes", _I32, [_I32, _I64, _I64, _I64, ctypes.POINTER(_I64)]),
     ("rbg_avos_matmul", _I32, [_I32, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
                                ctypes.POINTER(_U32), _P]),

@@ -1,0 +1,732 @@
+// spgemm.cu -- sparse AVOS product C = A (x) B (CSR) and the squaring-closure step, sm_103a.
+//
+// References (paths within rappdw/redblackgraph):
+//   rb_matrix @      redblackgraph/sparse/rbm.py:39-122 -> rbm_matmat_pass1/pass2
+//                    redblackgraph/sparse/sparsetools/rbm_math.h:117-222 (values upcast to 64 bit,
+//                    C core scalar semantics, zero sums dropped, result cast back)
+//   gpu spgemm       redblackgraph/gpu/spgemm.py:32-119, spgemm_numeric.py:104-176 (int32 values,
+//                    the Cython scalar semantics, optional j >= i mask)
+//   squaring merge   redblackgraph/sparse/csgraph/transitive_closure.py:272-357 and
+//                    redblackgraph/gpu/transitive_closure.py:77-156 (R (+) R^2 taken per cell as
+//                    the value of smallest magnitude, R's value on a tie, zeros dropped)
+//
+// Design: one pass per output row, no global sort and no global hash.  The candidates of row i
+// (every product A[i,k] (x) B[k,j], plus R[i,.] for a squaring step) are gathered into shared
+// memory, sorted by column, and reduced: the (+) of the products of a column, then, for a
+// squaring step, the magnitude merge with R's entry.  Rows with at most 1024 candidates run
+// one per warp, up to 8192 one per block; longer rows use a dense per-block accumulator in the
+// workspace.  The output of every row is written compacted (columns ascending) at the row's
+// candidate offset; a scan of the row counts and a gather produce the final CSR.
+#include <cuda_runtime.h>
+#include <cub/cub.cuh>
+#include <string.h>
+#include <algorithm>
+#include <vector>
+#include "rbg_internal.cuh"
+
+namespace rbg {
+
+constexpr int SP_WARP_CAP = 1024;     // candidates per warp row
+constexpr int SP_WARPS = 4;           // warps per CTA in the warp kernel
+constexpr int SP_BLOCK_CAP = 8192;    // candidates per block row
+constexpr int SP_BLOCK_THREADS = 512;
+constexpr int SP_DENSE_BLOCKS = 8;    // concurrent dense-accumulator rows (one scratch slot each)
+
+// semantics of the scalar algebra
+constexpr int SEM_C64 = 0;   // C core on 64-bit compute values (rb_matrix @)
+constexpr int SEM_CY32 = 1;  // Cython semantics on int32 (the gpu module)
+
+// Products and sums: for SEM_C64 the compute values are the storage values widened to 64 bits
+// (unsigned storage uses the unsigned 64-bit algebra with RED_ONE widened to all ones).
+template <int SEM, bool UNS>
+__device__ __forceinline__ long long sp_mul(long long a, long long b, unsigned &ev) {
+    if (SEM == SEM_CY32) return (long long)cy_product((int32_t)a, (int32_t)b);
+    if (UNS) return (long long)avos_product<uint64_t>((uint64_t)a, (uint64_t)b, ev);
+    return (long long)avos_product<int64_t>((int64_t)a, (int64_t)b, ev);
+}
+template <int SEM, bool UNS>
+__device__ __forceinline__ long long sp_add(long long a, long long b) {
+    if (SEM == SEM_CY32) return (long long)cy_sum((int32_t)a, (int32_t)b);
+    if (UNS) return (long long)avos_sum<uint64_t>((uint64_t)a, (uint64_t)b);
+    return (long long)avos_sum<int64_t>((int64_t)a, (int64_t)b);
+}
+
+// Value as the storage type holds it: C-core results are computed in 64 bits and cast back to
+// the storage width (rbm.py:120-121), wrapping like numpy's astype.
+__device__ __forceinline__ long long sp_trunc(long long v, int bytes, int uns) {
+    if (bytes == 8) return v;
+    return uns ? (long long)(unsigned)v : (long long)(int)v;
+}
+
+// Magnitude merge of the squaring step: the smaller |value| wins, R's value on a tie (R comes
+// first in the reference's stable sort).  Magnitudes are taken in the storage type.
+__device__ __forceinline__ long long sp_minabs(long long r, long long s, int uns) {
+    unsigned long long ar = uns ? (unsigned long long)r : (r < 0 ? 0ull - (unsigned long long)r : (unsigned long long)r);
+    unsigned long long as = uns ? (unsigned long long)s : (s < 0 ? 0ull - (unsigned long long)s : (unsigned long long)s);
+    return as < ar ? s : r;
+}
+
+struct SpArgs {
+    int64_t n_rows, n_cols;
+    const int64_t *ap; const int *aj; const void *ax;   // A (CSR, int64 row pointers)
+    const int64_t *bp; const int *bj; const void *bx;   // B
+    const int64_t *rp; const int *rj; const void *rx;   // R for a squaring step (or null)
+    int upper;                                          // keep only j >= i
+    int elem_bytes;                                     // storage value bytes (4 or 8)
+    int uns;                                            // unsigned storage
+    int64_t *cand_off;                                  // exclusive scan of candidates (n+1)
+    int *ocol; long long *oval;                         // per-row compacted output (temp)
+    int64_t *rownnz;                                    // output count per row
+    long long *dense_val; unsigned *dense_mark;         // dense accumulators (SP_DENSE_BLOCKS rows)
+    int *big_rows; int *big_count;                      // rows for the block / dense kernels
+    unsigned *flags;
+};
+
+__device__ __forceinline__ long long sp_load(const void *x, int64_t i, int bytes, int uns) {
+    if (bytes == 8) return ((const long long *)x)[i];
+    const int v = ((const int *)x)[i];
+    if (uns) return v == -1 ? -1ll : (long long)(unsigned)v;   // RED_ONE widens to all ones
+    return (long long)v;
+}
+
+// ----------------------------------------------------------------------------- candidates
+// cand[i] = sum over k in A[i] of nnz(B[k]) (+ nnz(R[i]) for a squaring step).  Rows above the
+// warp capacity are listed for the block / dense kernels.
+__global__ void sp_count_kernel(SpArgs a, int64_t *cand) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= a.n_rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i == a.n_rows) { cand[i] = 0; continue; }
+        int64_t c = 0;
+        for (int64_t e = a.ap[i]; e < a.ap[i + 1]; ++e) {
+            const int k = a.aj[e];
+            c += a.bp[k + 1] - a.bp[k];
+        }
+        if (a.rp) c += a.rp[i + 1] - a.rp[i];
+        cand[i] = c;
+        if (c > SP_WARP_CAP) a.big_rows[atomicAdd(a.big_count, 1)] = (int)i;
+        if (c > SP_BLOCK_CAP) atomicAdd(a.big_count + 1, 1);
+    }
+}
+
+// Encoded candidate key: column << 1 | source (0 = R's own entry, 1 = a product), so that R's
+// entry of a column sorts before the products of that column.
+__device__ __forceinline__ unsigned sp_key(int col, int src) { return ((unsigned)col << 1) | (unsigned)src; }
+constexpr unsigned SP_PAD = 0xffffffffu;
+
+// Reduce the sorted run starting at `h` (keys[h] is the first key of its column) into one value;
+// returns false when the column has no nonzero result.
+template <int SEM, bool UNS>
+__device__ __forceinline__ bool sp_reduce_run(const unsigned *keys, const long long *vals, int h, int cnt,
+                                              bool merge, int bytes, long long &out) {
+    const unsigned col = keys[h] >> 1;
+    bool have_r = false;
+    long long r = 0, s = 0;
+    int e = h;
+    if ((keys[e] & 1u) == 0) { have_r = true; r = vals[e]; ++e; }
+    for (; e < cnt && (keys[e] >> 1) == col; ++e) s = sp_add<SEM, UNS>(s, vals[e]);
+    if (!merge) {
+        if (s == 0) return false;          // zero sums are dropped (rbm_math.h:207)
+        out = (SEM == SEM_CY32) ? s : sp_trunc(s, bytes, UNS);
+        return true;
+    }
+    long long v;
+    if (s == 0) v = r;                     // no entry of R^2 in this column
+    else {
+        const long long s_t = (SEM == SEM_CY32) ? s : sp_trunc(s, bytes, UNS);
+        v = have_r ? sp_minabs(r, s_t, UNS) : s_t;
+    }
+    v = (long long)(int)v;                 // the merged matrix is int32 (transitive_closure.py:327)
+    if (v == 0) return false;
+    out = v;
+    return true;
+}
+
+// Append the candidates of row i to (keys, vals) at *cnt (shared), using the calling group of
+// `nthreads` threads (a warp or a block); products use the group's lanes over each B row.
+template <int SEM, bool UNS>
+__device__ __forceinline__ void sp_gather(const SpArgs &a, int64_t i, bool merge, unsigned *keys, long long *vals,
+                                          int *cnt, int lane, int nthreads, unsigned &ev) {
+    if (merge && a.rp) {
+        for (int64_t e = a.rp[i] + lane; e < a.rp[i + 1]; e += nthreads) {
+            const int pos = atomicAdd(cnt, 1);
+            keys[pos] = sp_key(a.rj[e], 0);
+            vals[pos] = sp_load(a.rx, e, a.elem_bytes, a.uns);
+        }
+    }
+    for (int64_t e = a.ap[i]; e < a.ap[i + 1]; ++e) {
+        const int k = a.aj[e];
+        const long long av = sp_load(a.ax, e, a.elem_bytes, a.uns);
+        for (int64_t f = a.bp[k] + lane; f < a.bp[k + 1]; f += nthreads) {
+            const int j = a.bj[f];
+            if (a.upper && j < i) continue;
+            const long long p = sp_mul<SEM, UNS>(av, sp_load(a.bx, f, a.elem_bytes, a.uns), ev);
+            if (p == 0) continue;                    // a zero product adds nothing
+            if (j == i && p != -1 && p != 1) ev |= RBG_EV_CYCLE;   // a vertex reaches itself
+            const int pos = atomicAdd(cnt, 1);
+            keys[pos] = sp_key(j, 1);
+            vals[pos] = p;
+        }
+    }
+}
+
+struct WarpSync { __device__ void operator()() const { __syncwarp(); } };
+struct BlockSync { __device__ void operator()() const { __syncthreads(); } };
+
+// Bitonic sort of keys/vals[0, P) (P a power of two) by the calling group; sync() orders steps.
+template <typename Sync>
+__device__ __forceinline__ void sp_bitonic(unsigned *keys, long long *vals, int P, int lane, int nthreads, Sync sync) {
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int idx = lane; idx < P; idx += nthreads) {
+                const int ixj = idx ^ j;
+                if (ixj > idx) {
+                    const bool up = (idx & k) == 0;
+                    const unsigned ka = keys[idx], kb = keys[ixj];
+                    if ((ka > kb) == up) {
+                        keys[idx] = kb; keys[ixj] = ka;
+                        const long long t = vals[idx]; vals[idx] = vals[ixj]; vals[ixj] = t;
+                    }
+                }
+            }
+            sync();
+        }
+    }
+}
+
+// One row per warp (at most SP_WARP_CAP candidates), rows handed out by a grid-stride loop.
+template <int SEM, bool UNS>
+__global__ void __launch_bounds__(SP_WARPS * 32)
+sp_warp_kernel(SpArgs a, int merge) {
+    extern __shared__ __align__(16) unsigned char sp_smem[];
+    long long *svals = reinterpret_cast<long long *>(sp_smem);                      // [warps][cap]
+    unsigned *skeys = reinterpret_cast<unsigned *>(svals + SP_WARPS * SP_WARP_CAP);  // [warps][cap]
+    int *scnt = reinterpret_cast<int *>(skeys + SP_WARPS * SP_WARP_CAP);             // [warps]
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned *keys = skeys + w * SP_WARP_CAP;
+    long long *vals = svals + w * SP_WARP_CAP;
+    unsigned ev = 0;
+    const int64_t warps = (int64_t)gridDim.x * SP_WARPS;
+    for (int64_t i = (int64_t)blockIdx.x * SP_WARPS + w; i < a.n_rows; i += warps) {
+        const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
+        if (c > SP_WARP_CAP) continue;               // the block / dense kernels take it
+        if (lane == 0) scnt[w] = 0;
+        __syncwarp();
+        sp_gather<SEM, UNS>(a, i, merge != 0, keys, vals, &scnt[w], lane, 32, ev);
+        __syncwarp();
+        const int cnt = scnt[w];
+        int P = 1;
+        while (P < cnt) P <<= 1;
+        for (int idx = cnt + lane; idx < P; idx += 32) keys[idx] = SP_PAD;
+        __syncwarp();
+        sp_bitonic(keys, vals, P, lane, 32, WarpSync());
+        // heads of columns in ascending order, compacted with ballots
+        int64_t out = 0;
+        const int64_t base = a.cand_off[i];
+        for (int c0 = 0; c0 < cnt; c0 += 32) {
+            const int idx = c0 + lane;
+            long long v = 0;
+            bool keep = false;
+            if (idx < cnt && (idx == 0 || (keys[idx] >> 1) != (keys[idx - 1] >> 1)))
+                keep = sp_reduce_run<SEM, UNS>(keys, vals, idx, cnt, merge != 0, a.elem_bytes, v);
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int64_t pos = base + out + __popc(bal & ((1u << lane) - 1u));
+                a.ocol[pos] = (int)(keys[idx] >> 1);
+                a.oval[pos] = v;
+            }
+            out += __popc(bal);
+        }
+        if (lane == 0) a.rownnz[i] = out;
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) ev |= __shfl_xor_sync(0xffffffffu, ev, o);
+    if (lane == 0 && ev) atomicOr(a.flags, ev);
+}
+
+constexpr size_t SP_WARP_SMEM = (size_t)SP_WARPS * SP_WARP_CAP * 12 + SP_WARPS * 4;
+constexpr size_t SP_BLOCK_SMEM = (size_t)SP_BLOCK_CAP * 12 + 64;
+
+// One row per block for SP_WARP_CAP < candidates <= SP_BLOCK_CAP (rows from the big-row list).
+template <int SEM, bool UNS>
+__global__ void __launch_bounds__(SP_BLOCK_THREADS)
+sp_block_kernel(SpArgs a, int merge) {
+    extern __shared__ __align__(16) unsigned char sp_smem[];
+    long long *vals = reinterpret_cast<long long *>(sp_smem);
+    unsigned *keys = reinterpret_cast<unsigned *>(vals + SP_BLOCK_CAP);
+    __shared__ int scnt;
+    __shared__ int wsum[SP_BLOCK_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    unsigned ev = 0;
+    const int nbig = *a.big_count;
+    for (int b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const int64_t i = a.big_rows[b];
+        const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
+        if (c > SP_BLOCK_CAP) continue;              // the dense kernel takes it
+        if (tid == 0) scnt = 0;
+        __syncthreads();
+        sp_gather<SEM, UNS>(a, i, merge != 0, keys, vals, &scnt, tid, SP_BLOCK_THREADS, ev);
+        __syncthreads();
+        const int cnt = scnt;
+        int P = 1;
+        while (P < cnt) P <<= 1;
+        for (int idx = cnt + tid; idx < P; idx += SP_BLOCK_THREADS) keys[idx] = SP_PAD;
+        __syncthreads();
+        sp_bitonic(keys, vals, P, tid, SP_BLOCK_THREADS, BlockSync());
+        int64_t out = 0;
+        const int64_t base = a.cand_off[i];
+        for (int c0 = 0; c0 < cnt; c0 += SP_BLOCK_THREADS) {
+            const int idx = c0 + tid;
+            long long v = 0;
+            bool keep = false;
+            if (idx < cnt && (idx == 0 || (keys[idx] >> 1) != (keys[idx - 1] >> 1)))
+                keep = sp_reduce_run<SEM, UNS>(keys, vals, idx, cnt, merge != 0, a.elem_bytes, v);
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) wsum[w] = __popc(bal);
+            __syncthreads();
+            int before = 0, total = 0;
+            for (int q = 0; q < SP_BLOCK_THREADS / 32; ++q) {
+                before += q < w ? wsum[q] : 0;
+                total += wsum[q];
+            }
+            if (keep) {
+                const int64_t pos = base + out + before + __popc(bal & ((1u << lane) - 1u));
+                a.ocol[pos] = (int)(keys[idx] >> 1);
+                a.oval[pos] = v;
+            }
+            out += total;
+            __syncthreads();
+        }
+        if (tid == 0) a.rownnz[i] = out;
+        __syncthreads();
+    }
+    for (int o = 16; o > 0; o >>= 1) ev |= __shfl_xor_sync(0xffffffffu, ev, o);
+    if (lane == 0 && ev) atomicOr(a.flags, ev);
+}
+
+// Dense accumulator encoding for atomicMin: the (+) order becomes the unsigned (C core) or
+// signed (Cython) order of the key; an empty slot holds the largest key.
+template <int SEM>
+__device__ __forceinline__ unsigned long long sp_enc(long long v) {
+    if (SEM == SEM_CY32) return (unsigned long long)v;          // compared as signed below
+    return v == -1 ? 0ull : (unsigned long long)v;
+}
+template <int SEM>
+__device__ __forceinline__ long long sp_dec(unsigned long long k) {
+    if (SEM == SEM_CY32) return (long long)k;
+    return k == 0ull ? -1ll : (long long)k;
+}
+template <int SEM> __device__ __forceinline__ unsigned long long sp_empty() {
+    return SEM == SEM_CY32 ? (unsigned long long)LLONG_MAX : ~0ull;
+}
+
+// One row per block for rows beyond SP_BLOCK_CAP: a dense accumulator over all columns (one
+// scratch slot per block, left empty again after each row), read back in column order.
+template <int SEM, bool UNS>
+__global__ void __launch_bounds__(SP_BLOCK_THREADS)
+sp_dense_kernel(SpArgs a, int merge) {
+    __shared__ int wsum[SP_BLOCK_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t nc = a.n_cols, nwords = (nc + 31) / 32;
+    unsigned long long *dval = reinterpret_cast<unsigned long long *>(a.dense_val) + (int64_t)blockIdx.x * nc;
+    long long *drv = a.dense_val + (int64_t)SP_DENSE_BLOCKS * nc + (int64_t)blockIdx.x * nc;
+    unsigned *dmark = a.dense_mark + (int64_t)blockIdx.x * nwords;
+    unsigned ev = 0;
+    const int nbig = *a.big_count;
+    for (int b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const int64_t i = a.big_rows[b];
+        const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
+        if (c <= SP_BLOCK_CAP) continue;
+        if (merge && a.rp) {
+            for (int64_t e = a.rp[i] + tid; e < a.rp[i + 1]; e += SP_BLOCK_THREADS) {
+                const int j = a.rj[e];
+                drv[j] = sp_load(a.rx, e, a.elem_bytes, a.uns);
+                atomicOr(&dmark[j >> 5], 1u << (j & 31));
+            }
+        }
+        for (int64_t e = a.ap[i]; e < a.ap[i + 1]; ++e) {
+            const int k = a.aj[e];
+            const long long av = sp_load(a.ax, e, a.elem_bytes, a.uns);
+            for (int64_t f = a.bp[k] + tid; f < a.bp[k + 1]; f += SP_BLOCK_THREADS) {
+                const int j = a.bj[f];
+                if (a.upper && j < i) continue;
+                const long long p = sp_mul<SEM, UNS>(av, sp_load(a.bx, f, a.elem_bytes, a.uns), ev);
+                if (p == 0) continue;
+                if (j == i && p != -1 && p != 1) ev |= RBG_EV_CYCLE;
+                if (SEM == SEM_CY32) atomicMin(reinterpret_cast<long long *>(&dval[j]), (long long)p);
+                else atomicMin(&dval[j], sp_enc<SEM>(p));
+                atomicOr(&dmark[j >> 5], 1u << (j & 31));
+            }
+        }
+        __syncthreads();
+        int64_t out = 0;
+        const int64_t base = a.cand_off[i];
+        for (int64_t w0 = 0; w0 < nwords; w0 += SP_BLOCK_THREADS) {
+            const int64_t wi = w0 + tid;
+            unsigned bits = wi < nwords ? dmark[wi] : 0u;
+            // first pass: count this thread's outputs
+            int mine = 0;
+            for (unsigned bb = bits; bb; bb &= bb - 1) {
+                const int64_t j = wi * 32 + __ffs(bb) - 1;
+                const unsigned long long k = dval[j];
+                const long long s = k == sp_empty<SEM>() ? 0 : sp_dec<SEM>(k);
+                const long long r = merge ? drv[j] : 0;
+                long long v;
+                if (!merge) v = s == 0 ? 0 : ((SEM == SEM_CY32) ? s : sp_trunc(s, a.elem_bytes, UNS));
+                else {
+                    const long long s_t = s == 0 ? 0 : ((SEM == SEM_CY32) ? s : sp_trunc(s, a.elem_bytes, UNS));
+                    v = s == 0 ? r : (r != 0 ? sp_minabs(r, s_t, UNS) : s_t);
+                    v = (long long)(int)v;
+                }
+                mine += v != 0;
+            }
+            int incl = mine;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (lane == 31) wsum[w] = incl;
+            __syncthreads();
+            int before = incl - mine, total = 0;
+            for (int q = 0; q < SP_BLOCK_THREADS / 32; ++q) {
+                before += q < w ? wsum[q] : 0;
+                total += wsum[q];
+            }
+            // second pass: write in column order and leave the slot empty
+            int k2 = 0;
+            for (unsigned bb = bits; bb; bb &= bb - 1) {
+                const int64_t j = wi * 32 + __ffs(bb) - 1;
+                const unsigned long long k = dval[j];
+                const long long s = k == sp_empty<SEM>() ? 0 : sp_dec<SEM>(k);
+                const long long r = merge ? drv[j] : 0;
+                long long v;
+                if (!merge) v = s == 0 ? 0 : ((SEM == SEM_CY32) ? s : sp_trunc(s, a.elem_bytes, UNS));
+                else {
+                    const long long s_t = s == 0 ? 0 : ((SEM == SEM_CY32) ? s : sp_trunc(s, a.elem_bytes, UNS));
+                    v = s == 0 ? r : (r != 0 ? sp_minabs(r, s_t, UNS) : s_t);
+                    v = (long long)(int)v;
+                }
+                if (v != 0) {
+                    a.ocol[base + out + before + k2] = (int)j;
+                    a.oval[base + out + before + k2] = v;
+                    ++k2;
+                }
+                dval[j] = sp_empty<SEM>();
+                drv[j] = 0;
+            }
+            if (wi < nwords) dmark[wi] = 0;
+            out += total;
+            __syncthreads();
+        }
+        if (tid == 0) a.rownnz[i] = out;
+        __syncthreads();
+    }
+    for (int o = 16; o > 0; o >>= 1) ev |= __shfl_xor_sync(0xffffffffu, ev, o);
+    if (lane == 0 && ev) atomicOr(a.flags, ev);
+}
+
+template <int SEM>
+__global__ void sp_dense_init_kernel(long long *dense_val, unsigned *dense_mark, int64_t nc) {
+    const int64_t nwords = (nc + 31) / 32;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)SP_DENSE_BLOCKS * nc;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        reinterpret_cast<unsigned long long *>(dense_val)[e] = sp_empty<SEM>();
+        dense_val[(int64_t)SP_DENSE_BLOCKS * nc + e] = 0;
+        if (e < (int64_t)SP_DENSE_BLOCKS * nwords) dense_mark[e] = 0;
+    }
+}
+
+// Final CSR: row pointers from the scan of the row counts, entries gathered from the per-row
+// compacted output and stored in the storage type.
+__global__ void sp_gather_kernel(int64_t n_rows, const int64_t *cand_off, const int64_t *cptr,
+                                 const int *ocol, const long long *oval, int *cj, void *cx, int bytes) {
+    for (int64_t i = blockIdx.x; i < n_rows; i += gridDim.x) {
+        const int64_t src = cand_off[i], dst = cptr[i], cnt = cptr[i + 1] - dst;
+        for (int64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+            cj[dst + e] = ocol[src + e];
+            if (bytes == 8) reinterpret_cast<long long *>(cx)[dst + e] = oval[src + e];
+            else reinterpret_cast<int *>(cx)[dst + e] = (int)oval[src + e];
+        }
+    }
+}
+
+}  // namespace rbg
+
+using namespace rbg;
+
+namespace {
+
+struct Head {   // workspace that lives from rbg_spgemm_count to rbg_spgemm_gather
+    int64_t *cand_off;   // n+1
+    int *big_rows;       // n
+    int *counters;       // [0] big rows, [1] dense rows, [2] flags
+    void *scan_tmp;
+    size_t scan_bytes;
+};
+
+size_t scan_bytes(int64_t n) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (int64_t *)nullptr, (int64_t *)nullptr, (int)std::max<int64_t>(n + 1, 1));
+    return b;
+}
+
+size_t head_layout(int64_t n, unsigned char *base, Head *h) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return base ? base + at : nullptr; };
+    unsigned char *p;
+    p = take((size_t)(n + 1) * 8); if (h) h->cand_off = reinterpret_cast<int64_t *>(p);
+    p = take((size_t)std::max<int64_t>(n, 1) * 4); if (h) h->big_rows = reinterpret_cast<int *>(p);
+    p = take(64); if (h) h->counters = reinterpret_cast<int *>(p);
+    const size_t sb = scan_bytes(n);
+    p = take(sb); if (h) { h->scan_tmp = p; h->scan_bytes = sb; }
+    return o;
+}
+
+struct Tail {
+    int *ocol; long long *oval; int64_t *rownnz; int64_t *cptr;
+    long long *dense_val; unsigned *dense_mark;
+};
+
+size_t tail_layout(int64_t n, int64_t nc, int64_t total, int64_t dense, unsigned char *base, Tail *t) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return base ? base + at : nullptr; };
+    unsigned char *p;
+    p = take((size_t)std::max<int64_t>(total, 1) * 4); if (t) t->ocol = reinterpret_cast<int *>(p);
+    p = take((size_t)std::max<int64_t>(total, 1) * 8); if (t) t->oval = reinterpret_cast<long long *>(p);
+    p = take((size_t)(n + 1) * 8); if (t) t->rownnz = reinterpret_cast<int64_t *>(p);
+    p = take((size_t)(n + 1) * 8); if (t) t->cptr = reinterpret_cast<int64_t *>(p);
+    const int64_t nwords = (nc + 31) / 32;
+    p = take(dense > 0 ? (size_t)SP_DENSE_BLOCKS * nc * 16 : 8); if (t) t->dense_val = reinterpret_cast<long long *>(p);
+    p = take(dense > 0 ? (size_t)SP_DENSE_BLOCKS * nwords * 4 : 8); if (t) t->dense_mark = reinterpret_cast<unsigned *>(p);
+    return o;
+}
+
+bool csr_ok(const rbg_csr_t *m) {
+    return m && m->n_rows >= 0 && m->n_cols >= 0 && m->indptr && (m->n_cols < (1ll << 30));
+}
+
+void fill_args(SpArgs &a, const rbg_csr_t *A, const rbg_csr_t *B, const rbg_csr_t *R, int upper) {
+    memset(&a, 0, sizeof(a));
+    a.n_rows = A->n_rows; a.n_cols = B->n_cols;
+    a.ap = A->indptr; a.aj = A->indices; a.ax = A->data;
+    a.bp = B->indptr; a.bj = B->indices; a.bx = B->data;
+    if (R) { a.rp = R->indptr; a.rj = R->indices; a.rx = R->data; }
+    a.upper = upper;
+}
+
+int grid_of(int64_t work, int threads) { return grid_for(work, threads); }
+
+}  // namespace
+
+extern "C" int32_t rbg_spgemm_head_bytes(int64_t n_rows, int64_t *bytes) {
+    if (!bytes || n_rows < 0) return RBG_ERR_INVALID;
+    *bytes = (int64_t)head_layout(n_rows, nullptr, nullptr);
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_spgemm_tail_bytes(int64_t n_rows, int64_t n_cols, int64_t total_candidates,
+                                         int64_t dense_rows, int64_t *bytes) {
+    if (!bytes || n_rows < 0 || n_cols < 0 || total_candidates < 0 || dense_rows < 0) return RBG_ERR_INVALID;
+    *bytes = (int64_t)tail_layout(n_rows, n_cols, total_candidates, dense_rows, nullptr, nullptr);
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_spgemm_count(const rbg_csr_t *A, const rbg_csr_t *B, const rbg_csr_t *R, int32_t upper,
+                                    void *head, int64_t head_bytes, int64_t *total_candidates,
+                                    int64_t *dense_rows, rbg_stream_t stream) {
+    if (!csr_ok(A) || !csr_ok(B) || (R && !csr_ok(R)) || !head || !total_candidates || !dense_rows)
+        return RBG_ERR_INVALID;
+    if (A->n_cols != B->n_rows || (R && (R->n_rows != A->n_rows || R->n_cols != B->n_cols)))
+        return RBG_ERR_INVALID;
+    const int64_t n = A->n_rows;
+    if (head_bytes < (int64_t)head_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
+    Head h;
+    head_layout(n, reinterpret_cast<unsigned char *>(head), &h);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    SpArgs a;
+    fill_args(a, A, B, R, upper);
+    a.big_rows = h.big_rows;
+    a.big_count = h.counters;
+    RBG_CUDA_TRY(cudaMemsetAsync(h.counters, 0, 64, s));
+    note_launches(2);
+    sp_count_kernel<<<grid_of(n + 1, 256), 256, 0, s>>>(a, h.cand_off);
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(h.scan_tmp, h.scan_bytes, h.cand_off, h.cand_off, (int)(n + 1), s));
+    int64_t tot = 0;
+    int hc[2] = {0, 0};
+    RBG_CUDA_TRY(cudaMemcpyAsync(&tot, h.cand_off + n, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(hc, h.counters, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    const int64_t dense = hc[1];
+    *total_candidates = tot;
+    *dense_rows = dense;
+    return RBG_OK;
+}
+
+namespace {
+
+template <int SEM, bool UNS>
+int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)SP_WARP_SMEM));
+        RBG_CUDA_TRY(cudaFuncSetAttribute(sp_block_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)SP_BLOCK_SMEM));
+        configured = true;
+    }
+    const int64_t n = a.n_rows;
+    note_launches(2 + (dense > 0 ? 2 : 0));
+    sp_warp_kernel<SEM, UNS><<<grid_of((n + SP_WARPS - 1) / SP_WARPS, 1), SP_WARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
+    sp_block_kernel<SEM, UNS><<<grid_of(1 << 20, 1), SP_BLOCK_THREADS, SP_BLOCK_SMEM, s>>>(a, merge);
+    if (dense > 0) {
+        sp_dense_init_kernel<SEM><<<grid_of((int64_t)SP_DENSE_BLOCKS * nc, 256), 256, 0, s>>>(a.dense_val,
+                                                                                         a.dense_mark, nc);
+        sp_dense_kernel<SEM, UNS><<<SP_DENSE_BLOCKS, SP_BLOCK_THREADS, 0, s>>>(a, merge);
+    }
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t rbg_spgemm_numeric(int32_t sem, int32_t dtype, const rbg_csr_t *A, const rbg_csr_t *B,
+                                      const rbg_csr_t *R, int32_t upper, void *head, void *tail,
+                                      int64_t tail_bytes, int64_t total_candidates, int64_t dense_rows,
+                                      int64_t *nnz, uint32_t *flags, rbg_stream_t stream) {
+    if (!csr_ok(A) || !csr_ok(B) || (R && !csr_ok(R)) || !head || !tail || !nnz || !flags) return RBG_ERR_INVALID;
+    if (sem != RBG_SEM_C64 && sem != RBG_SEM_CY32) return RBG_ERR_INVALID;
+    if (sem == RBG_SEM_CY32 && dtype != RBG_DTYPE_INT32) return RBG_ERR_INVALID;
+    if (dtype != RBG_DTYPE_INT32 && dtype != RBG_DTYPE_INT64 && dtype != RBG_DTYPE_UINT32 &&
+        dtype != RBG_DTYPE_UINT64)
+        return RBG_ERR_INVALID;
+    const int64_t n = A->n_rows, nc = B->n_cols;
+    if (tail_bytes < (int64_t)tail_layout(n, nc, total_candidates, dense_rows, nullptr, nullptr))
+        return RBG_ERR_NOMEM;
+    Head h;
+    head_layout(n, reinterpret_cast<unsigned char *>(head), &h);
+    Tail t;
+    tail_layout(n, nc, total_candidates, dense_rows, reinterpret_cast<unsigned char *>(tail), &t);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    SpArgs a;
+    fill_args(a, A, B, R, upper);
+    a.elem_bytes = dtype_bytes(dtype);
+    a.uns = (dtype == RBG_DTYPE_UINT32 || dtype == RBG_DTYPE_UINT64);
+    a.cand_off = h.cand_off;
+    a.ocol = t.ocol; a.oval = t.oval; a.rownnz = t.rownnz;
+    a.dense_val = t.dense_val; a.dense_mark = t.dense_mark;
+    a.big_rows = h.big_rows; a.big_count = h.counters;
+    a.flags = reinterpret_cast<unsigned *>(h.counters + 2);
+    RBG_CUDA_TRY(cudaMemsetAsync(h.counters + 2, 0, 4, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(t.rownnz, 0, (size_t)(n + 1) * 8, s));
+    const int merge = R != nullptr;
+    int rc;
+    if (sem == RBG_SEM_CY32) rc = run_numeric<SEM_CY32, false>(a, merge, dense_rows, nc, s);
+    else if (a.uns) rc = run_numeric<SEM_C64, true>(a, merge, dense_rows, nc, s);
+    else rc = run_numeric<SEM_C64, false>(a, merge, dense_rows, nc, s);
+    if (rc) return rc;
+    size_t sb = h.scan_bytes;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(h.scan_tmp, sb, t.rownnz, t.cptr, (int)(n + 1), s));
+    int64_t tot = 0;
+    unsigned hf = 0;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&tot, t.cptr + n, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(&hf, h.counters + 2, 4, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    *nnz = tot;
+    *flags = hf;
+    return (hf & (RBG_EV_OVF_SIZE | RBG_EV_OVF_ONES | RBG_EV_HANG)) ? RBG_ERR_OVERFLOW : RBG_OK;
+}
+
+extern "C" int32_t rbg_spgemm_gather(int32_t dtype, int64_t n_rows, int64_t n_cols, const void *head,
+                                     const void *tail, int64_t total_candidates, int64_t dense_rows,
+                                     int64_t *indptr, int32_t *indices, void *data, rbg_stream_t stream) {
+    if (!head || !tail || !indptr || n_rows < 0 || dtype_bytes(dtype) < 4) return RBG_ERR_INVALID;
+    Head h;
+    head_layout(n_rows, const_cast<unsigned char *>(reinterpret_cast<const unsigned char *>(head)), &h);
+    Tail t;
+    tail_layout(n_rows, n_cols, total_candidates, dense_rows,
+                const_cast<unsigned char *>(reinterpret_cast<const unsigned char *>(tail)), &t);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    RBG_CUDA_TRY(cudaMemcpyAsync(indptr, t.cptr, (size_t)(n_rows + 1) * 8, cudaMemcpyDeviceToDevice, s));
+    if (n_rows > 0) {
+        note_launches(1);
+        sp_gather_kernel<<<grid_of(n_rows * 32, 32), 64, 0, s>>>(n_rows, h.cand_off, t.cptr, t.ocol, t.oval, indices,
+                                                                  data, dtype_bytes(dtype));
+        RBG_CUDA_TRY(cudaGetLastError());
+    }
+    return RBG_OK;
+}
+
+// ----------------------------------------------------------------------------- row merge
+// Z = X (+) Y cell by cell with the squaring step's magnitude rule (redblackgraph/gpu/
+// transitive_closure.py:77-156): the smaller |value| (X's on a tie), zero results dropped.
+// int32 values, rows sorted.  One thread merges one row's two sorted lists.
+namespace rbg {
+
+__device__ __forceinline__ int mg_pick(int x, int y) {
+    const unsigned ax = x < 0 ? 0u - (unsigned)x : (unsigned)x;
+    const unsigned ay = y < 0 ? 0u - (unsigned)y : (unsigned)y;
+    return ay < ax ? y : x;
+}
+
+template <bool FILL>
+__global__ void mg_kernel(int64_t n, const int64_t *xp, const int *xj, const int *xv, const int64_t *yp,
+                          const int *yj, const int *yv, int64_t *cnt, const int64_t *zp, int *zj, int *zv) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t a = xp[i], ae = xp[i + 1], b = yp[i], be = yp[i + 1];
+        int64_t out = FILL ? zp[i] : 0;
+        int64_t c = 0;
+        while (a < ae || b < be) {
+            int col, v;
+            if (b >= be || (a < ae && xj[a] < yj[b])) { col = xj[a]; v = xv[a]; ++a; }
+            else if (a >= ae || yj[b] < xj[a]) { col = yj[b]; v = yv[b]; ++b; }
+            else { col = xj[a]; v = mg_pick(xv[a], yv[b]); ++a; ++b; }
+            if (v == 0) continue;
+            if (FILL) { zj[out + c] = col; zv[out + c] = v; }
+            ++c;
+        }
+        if (!FILL) cnt[i] = c;
+    }
+}
+
+}  // namespace rbg
+
+extern "C" int32_t rbg_csr_merge_count(const rbg_csr_t *X, const rbg_csr_t *Y, void *head, int64_t head_bytes,
+                                       int64_t *nnz, rbg_stream_t stream) {
+    if (!csr_ok(X) || !csr_ok(Y) || !head || !nnz || X->n_rows != Y->n_rows || X->n_cols != Y->n_cols)
+        return RBG_ERR_INVALID;
+    const int64_t n = X->n_rows;
+    if (head_bytes < (int64_t)head_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
+    Head h;
+    head_layout(n, reinterpret_cast<unsigned char *>(head), &h);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    RBG_CUDA_TRY(cudaMemsetAsync(h.cand_off + n, 0, 8, s));
+    if (n > 0) {
+        note_launches(1);
+        mg_kernel<false><<<grid_of(n, 256), 256, 0, s>>>(n, X->indptr, X->indices, (const int *)X->data, Y->indptr,
+                                                         Y->indices, (const int *)Y->data, h.cand_off, nullptr,
+                                                         nullptr, nullptr);
+    }
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(h.scan_tmp, h.scan_bytes, h.cand_off, h.cand_off, (int)(n + 1), s));
+    int64_t tot = 0;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&tot, h.cand_off + n, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    *nnz = tot;
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, const void *head, int64_t *indptr,
+                                      int32_t *indices, int32_t *data, rbg_stream_t stream) {
+    if (!csr_ok(X) || !csr_ok(Y) || !head || !indptr) return RBG_ERR_INVALID;
+    const int64_t n = X->n_rows;
+    Head h;
+    head_layout(n, const_cast<unsigned char *>(reinterpret_cast<const unsigned char *>(head)), &h);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    RBG_CUDA_TRY(cudaMemcpyAsync(indptr, h.cand_off, (size_t)(n + 1) * 8, cudaMemcpyDeviceToDevice, s));
+    if (n > 0) {
+        note_launches(1);
+        mg_kernel<true><<<grid_of(n, 256), 256, 0, s>>>(n, X->indptr, X->indices, (const int *)X->data, Y->indptr,
+                                                        Y->indices, (const int *)Y->data, nullptr, h.cand_off,
+                                                        indices, data);
+    }
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}

@@ -4,8 +4,11 @@ from .transitive_closure import (
     transitive_closure,
     transitive_closure_floyd_warshall,
     transitive_closure_dijkstra,
+    transitive_closure_squaring,
+    transitive_closure_dag_sparse,
 )
 from .cycleerror import CycleError
 
 __all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
-           "transitive_closure_floyd_warshall", "transitive_closure_dijkstra", "CycleError"]
+           "transitive_closure_floyd_warshall", "transitive_closure_dijkstra",
+           "transitive_closure_squaring", "transitive_closure_dag_sparse", "CycleError"]

@@ -1,5 +1,7 @@
-"""Closure entry points of ``redblackgraph.sparse.csgraph`` (transitive_closure.py:17-82)."""
+"""Closure entry points of ``redblackgraph.sparse.csgraph`` (transitive_closure.py:17-574)."""
 from __future__ import annotations
+
+import numpy as np
 
 from ...types import TransitiveClosure
 from ._shortest_path import shortest_path
@@ -22,3 +24,83 @@ def transitive_closure_dijkstra(R) -> TransitiveClosure:
         if all((csr.indices[rows[i]:rows[i + 1]] >= i).all() for i in range(csr.shape[0])):
             return transitive_closure_floyd_warshall(R, assume_upper_triangular=True)
     return transitive_closure(R, method="D")
+
+
+# ------------------------------------------------------------------------- sparse closures
+def _is_upper(csr) -> bool:
+    rows = np.repeat(np.arange(csr.shape[0]), np.diff(csr.indptr))
+    return bool(np.all(csr.indices >= rows))
+
+
+def _is_lower(csr) -> bool:
+    rows = np.repeat(np.arange(csr.shape[0]), np.diff(csr.indptr))
+    return bool(np.all(csr.indices <= rows))
+
+
+def _as_csr(A):
+    import scipy.sparse as sp
+    if not sp.issparse(A):
+        return sp.csr_matrix(A)
+    return A.tocsr() if not isinstance(A, sp.csr_matrix) else A
+
+
+def _squaring(csr, max_iterations, cycle_error):
+    """R <- R (+) R^2 on the GPU until R is stable; returns (rb_matrix int32, max |value|)."""
+    import torch
+    from ...spgemm import DeviceCSR, spgemm, SEM_C64
+    from ... import _lib
+    from ..rbm import rb_matrix
+    a = csr.copy()
+    a.sort_indices()
+    a.sum_duplicates()
+    if a.dtype.kind not in "iu":
+        a = a.astype(np.int64)
+    if a.dtype.itemsize < 4:
+        a = a.astype(np.int32 if a.dtype.kind == "i" else np.uint32)
+    R = DeviceCSR.from_scipy(a)
+    for _ in range(max_iterations):
+        Rn, rc, flags = spgemm(R, R, R=R, sem=SEM_C64)
+        if cycle_error and (flags & _lib.EV_CYCLE):
+            from .cycleerror import CycleError
+            raise CycleError("Graph contains a cycle", vertex=-1)
+        if rc == _lib.RBG_ERR_OVERFLOW:
+            raise OverflowError("Avos product results in an overflow.")
+        if Rn.equal(R):
+            R = Rn
+            break
+        R = Rn
+    if R.data.dtype != torch.int32:
+        R = DeviceCSR(R.indptr, R.indices, R.data.to(torch.int32), R.shape)
+    mx_abs = int(R.data.abs().max().item()) if R.nnz else 0
+    mx = int(R.data.max().item()) if R.nnz else 0
+    out = R.to_scipy()
+    return rb_matrix((out.data, out.indices.astype(np.int32), out.indptr.astype(np.int32)),
+                     shape=out.shape), mx_abs, mx
+
+
+def transitive_closure_dag_sparse(A) -> TransitiveClosure:
+    """Closure of a DAG (redblackgraph/sparse/csgraph/transitive_closure.py:383-438): the
+    same closure computed by GPU squaring; diameter = MSB of the largest value
+    (_transitive_closure_dag.pyx:347-349); CycleError on a cycle."""
+    import scipy.sparse as sp
+    csr = _as_csr(A)
+    n = csr.shape[0]
+    if n == 0:
+        return TransitiveClosure(sp.csr_matrix((0, 0), dtype=np.int32), 0)
+    W, mx_abs, mx = _squaring(csr, 64, cycle_error=True)
+    return TransitiveClosure(W, (mx.bit_length() - 1) if mx > 1 else 0)
+
+
+def transitive_closure_squaring(A, max_iterations=64) -> TransitiveClosure:
+    """Closure by repeated squaring (transitive_closure.py:198-269): triangular inputs take the
+    DAG closure, others iterate R <- R (+) R^2 with the magnitude merge until stable."""
+    import scipy.sparse as sp
+    csr = _as_csr(A)
+    n = csr.shape[0]
+    if n == 0:
+        return TransitiveClosure(sp.csr_matrix((0, 0), dtype=np.int32), 0)
+    if _is_upper(csr) or _is_lower(csr):
+        return transitive_closure_dag_sparse(csr)
+    W, mx_abs, _ = _squaring(csr, max_iterations, cycle_error=False)
+    diameter = int(np.floor(np.log2(mx_abs))) if mx_abs > 1 else 0
+    return TransitiveClosure(W, diameter)
