@@ -1,14 +1,20 @@
 """Benchmark: AVOS transitive closure on GB300.
 
-Default workload (the batched dense closure): 4096 independent pedigree components with sizes
-log-uniform in [16, 4096], generation depth 1.5*log2(n), int32, closed in one batched run per
-step.  The metric is AVOS relaxations/s with the algorithmic count sum(n^3) per step (the
-reference's C warshall performs all n^3 relaxations of every component).
+Default workload (the batched dense closure): 4096 seeded pedigrees with sizes log-uniform in
+[16, 4096] and generation depth 1.5*log2(n), laid out as one block-diagonal forest (int32).
+Its connected components (a pedigree may hold isolated founders, so there are more components
+than pedigrees) are closed in one batched run per step.  The metric is AVOS relaxations/s with
+the algorithmic count sum(n^3) over the components (the reference's C warshall performs all n^3
+relaxations of every component).
+
+  value  batched closure with the dense blocks resident in HBM (CUDA events on the stream)
+  e2e    component_wise_closure on the forest in pinned host memory: CSR upload, component
+         split, densify, batched closure, compaction and download of the merged CSR per step
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Under torchrun (N > 1) every rank closes its own seeded set of 4096 components (weak scaling,
-no data-path collective); rank 0 prints one JSON line with the whole-job throughput.
+Under torchrun (N > 1) every rank closes its own seeded forest (weak scaling, no data-path
+collective); rank 0 prints one JSON line with the whole-job throughput.
 """
 from __future__ import annotations
 
@@ -44,16 +50,30 @@ def parse():
 
 
 def workload(rank: int):
+    """The 4096 seeded pedigrees as one block-diagonal forest, and its connected components
+    (numbered by least vertex, vertices ascending) found on the host by scipy."""
+    from scipy.sparse.csgraph import connected_components
     from redblackgraph_gb300 import synth
     sizes, seeds = synth.batch_components(COUNT, LO, HI, seed=SEED + 1000 * rank)
-    return sizes, seeds
+    forest, base = synth.batch_forest(sizes, seeds)
+    k, lab = connected_components(forest, directed=True, connection="weak")
+    order = np.argsort(lab, kind="stable")
+    csizes = np.bincount(lab, minlength=k).astype(np.int64)
+    cstart = np.concatenate([[0], np.cumsum(csizes)])
+    return dict(sizes=sizes, seeds=seeds, forest=forest, csizes=csizes, cstart=cstart, order=order)
 
 
-def config(l2_note: str):
-    return {"workload": "batched dense AVOS closure", "components": COUNT,
-            "n_range": [LO, HI], "sizes": "log-uniform", "generations": "max(2, round(1.5*log2 n))",
-            "parents": "father 2 / mother 3, p=0.9 each, uniform over earlier generations",
-            "storage": "int32 dense", "l2": l2_note}
+def config(l2_note: str, w=None):
+    c = {"workload": "batched dense AVOS closure", "pedigrees": COUNT,
+         "n_range": [LO, HI], "sizes": "log-uniform", "generations": "max(2, round(1.5*log2 n))",
+         "parents": "father 2 / mother 3, p=0.9 each, uniform over earlier generations",
+         "storage": "int32 dense", "l2": l2_note}
+    if w is not None:
+        c["components"] = int(w["csizes"].size)
+        c["vertices"] = int(w["forest"].shape[0])
+        c["components_note"] = ("connected components of the forest of the pedigrees (a pedigree "
+                                "can hold isolated founders); the work is their sum n^3")
+    return c
 
 
 # ------------------------------------------------------------------------------- clocks
@@ -112,31 +132,37 @@ def octave(n):
 
 def cpu_sample(sizes, budget_per_octave=CPU_SAMPLE_RELAX / 8):
     """Stratified sample: in every size octave [2^k, 2^(k+1)) the smallest components are taken
-    until their sum(n^3) reaches the octave budget (at least one per octave)."""
+    until their sum(n^3) reaches the octave budget or 64 are taken (at least one per octave)."""
     picked = []
     for k in sorted({octave(n) for n in sizes}):
         members = sorted((int(i) for i in np.flatnonzero([octave(n) == k for n in sizes])),
                          key=lambda i: int(sizes[i]))
-        acc = 0.0
+        acc, m = 0.0, 0
         for i in members:
-            if picked and acc > 0 and acc + float(sizes[i]) ** 3 > budget_per_octave:
+            if picked and acc > 0 and (acc + float(sizes[i]) ** 3 > budget_per_octave or m >= 64):
                 break
             picked.append(i)
             acc += float(sizes[i]) ** 3
+            m += 1
     return picked
 
 
-def cpu_closure_rate(sizes, seeds, idx, threads=None):
+def component_matrix(w, c):
+    """Dense int32 matrix of connected component c of the forest (vertices ascending)."""
+    v = w["order"][w["cstart"][c]:w["cstart"][c + 1]]
+    return w["forest"][v][:, v].toarray().astype(np.int32)
+
+
+def cpu_closure_rate(w, idx, threads=None):
     """Time the oracle's C restatement of the reference's warshall (the CPU baseline) on the
     sampled components, one component per host thread (ctypes releases the GIL), and
     extrapolate each size octave's sum(n^3) by that octave's measured per-core rate.
 
     Returns (relax/s of the whole workload on `threads` cores, wall seconds of the sample,
-    threads, oracle outputs by sample position, matrices)."""
+    threads, oracle outputs by sample position)."""
     from oracle import oracle as orc
-    from redblackgraph_gb300 import synth
-    mats = [synth.pedigree(int(sizes[i]), synth.generations_for(int(sizes[i])), int(seeds[i]),
-                           dtype=np.int32) for i in idx]
+    sizes = w["csizes"]
+    mats = [component_matrix(w, int(i)) for i in idx]
     threads = threads or os.cpu_count() or 1
     orc.lib()
 
@@ -162,18 +188,26 @@ def cpu_closure_rate(sizes, seeds, idx, threads=None):
         o = octave(n)
         t_single += float(n) ** 3 * (per_oct_t[o] / per_oct_w[o] if o in per_oct_w else overall)
     total = float((np.asarray(sizes, dtype=np.float64) ** 3).sum())
-    return total / (t_single / threads), wall, threads, outs, mats
+    return total / (t_single / threads), wall, threads, outs
 
 
 # ------------------------------------------------------------------------------- GPU side
-def build_device_batch(sizes, seeds, device):
+def build_device_batch(w, device):
+    """Split the forest into components and densify them with the library's own component
+    path (the same calls component_wise_closure makes); checks the split against the host's."""
     import torch
-    from redblackgraph_gb300 import synth
-    idx, val, offsets = synth.batch_edges(sizes, seeds)
-    total = int((sizes * sizes).sum())
-    buf = torch.zeros(total, dtype=torch.int32, device=device)
-    buf[torch.from_numpy(idx).to(device)] = torch.from_numpy(val.astype(np.int32)).to(device)
-    return buf, offsets
+    from redblackgraph_gb300.components import label_components, densify
+    from redblackgraph_gb300.device import to_device
+    f = w["forest"]
+    ip = to_device(f.indptr.astype(np.int64), device)
+    ij = to_device(f.indices.astype(np.int32), device)
+    iv = to_device(f.data.astype(np.int32), device)
+    comps = label_components(ip, ij, f.shape[0])
+    assert comps.count == w["csizes"].size and (comps.sizes == w["csizes"]).all(), \
+        "device component split differs from the host's"
+    blocks = densify(ip, ij, iv, comps)
+    torch.cuda.synchronize()
+    return blocks
 
 
 def int32_peak_ops(device_index: int, sm_max_mhz):
@@ -208,7 +242,7 @@ def profile_kernels(fn):
     return {names[k]: (ms[k], int(n[k])) for k in range(4)}
 
 
-def run_ours(args, rank, world):
+def run_ours(args, rank, world, w):
     import torch
     import torch.distributed as dist
     from redblackgraph_gb300 import _lib
@@ -216,13 +250,13 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     dev = torch.device("cuda", torch.cuda.current_device())
     L = _lib.load()
-    sizes, seeds = workload(rank)
+    blocks = build_device_batch(w, dev)
+    sizes, offsets, buf = blocks.sizes, blocks.offsets, blocks.flat
     work_per_step = float((sizes.astype(np.float64) ** 3).sum())
-    buf, offsets = build_device_batch(sizes, seeds, dev)
     out = torch.empty_like(buf)
 
     results = None
-    for _ in range(max(args.warmup, 3) if args.warmup >= 3 else 3):
+    for _ in range(max(args.warmup, 3)):
         out, results = fw_batch(buf, sizes, offsets, out=out)
     assert all(r.status == 0 for r in results), "closure reported an error"
     executed = float(sum(r.executed for r in results))
@@ -248,20 +282,71 @@ def run_ours(args, rank, world):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t = float(tt.item())
     clocks = clk.summary()
-    return dict(t=t, work=work_per_step, executed=executed, kprof=kprof, launches=launches,
-                clocks=clocks, sizes=sizes, seeds=seeds, out=out, offsets=offsets,
-                bytes=buf.numel() * 4)
+    res = dict(t=t, work=work_per_step, executed=executed, kprof=kprof, launches=launches,
+               clocks=clocks, out=out, offsets=offsets, bytes=buf.numel() * 4)
+    del buf, blocks
+    res["e2e"] = run_e2e(args, rank, world, w, dev, work_per_step)
+    return res
 
 
-def sample_parity(sizes, offsets, out, cpu_outs, idx, mats):
-    """The GPU closures of the CPU-sample components against the oracle's (bit-exact)."""
+def run_e2e(args, rank, world, w, dev, work_per_step):
+    """The same closure through the public API with host buffers: component_wise_closure on the
+    forest held in pinned host memory (H2D of the CSR, component split, densify, batched
+    closure, compaction, D2H of the merged CSR inside every timed step)."""
+    import torch
+    import torch.distributed as dist
+    import scipy.sparse as sp
+    from redblackgraph_gb300.sparse import component_wise_closure
+    f = w["forest"]
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory()
+        v = t.numpy().view(a.dtype)
+        v[:] = a
+        return t, v
+
+    keep = [pinned(np.ascontiguousarray(x)) for x in (f.data, f.indices, f.indptr)]
+    M = sp.csr_matrix(f.shape, dtype=np.int32)
+    M.data, M.indices, M.indptr = keep[0][1], keep[1][1], keep[2][1]   # the pinned arrays themselves
+    assert all(np.shares_memory(a, k[1]) for a, k in zip((M.data, M.indices, M.indptr), keep))
+    h2d = int(M.data.nbytes + M.indices.nbytes + M.indptr.nbytes)
+    steps = max(1, args.steps)
+    r = None
+    for _ in range(max(args.warmup, 3) if args.warmup > 0 else 3):
+        r = component_wise_closure(M)
+    stream = torch.cuda.current_stream()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        r = component_wise_closure(M)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    W = r.W
+    d2h = int(8 * (f.shape[0] + 1) + 8 * W.nnz)     # int64 row pointers, int32 indices and values
+    return dict(t=t, steps=steps, value=work_per_step * steps * world / t, h2d=h2d, d2h=d2h, W=W,
+                diameter=int(r.diameter))
+
+
+def sample_parity(w, offsets, out, cpu_outs, idx, W_e2e=None):
+    """The GPU closures of the CPU-sample components against the oracle's (bit-exact), both from
+    the batched run and from the public-API run."""
     from redblackgraph_gb300.device import to_host
     ok = True
     for k, i in enumerate(idx):
-        n, o = int(sizes[i]), int(offsets[i])
-        W = to_host(out[o:o + n * n]).reshape(n, n)
+        n, o = int(w["csizes"][i]), int(offsets[i])
         Wo = cpu_outs[k][0]
-        ok &= bool((W == Wo).all())
+        ok &= bool((to_host(out[o:o + n * n]).reshape(n, n) == Wo).all())
+        if W_e2e is not None:
+            v = w["order"][w["cstart"][i]:w["cstart"][i + 1]]
+            ok &= bool((W_e2e[v][:, v].toarray() == Wo).all())
     return ok
 
 
@@ -274,14 +359,15 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    r = run_ours(args, rank, world)
+    w = workload(rank)
+    r = run_ours(args, rank, world, w)
     total_work = r["work"] * args.steps * world
     value = total_work / r["t"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["t"] / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded pedigree components generated in-process",
-            "config": config(f"inputs larger than L2: {r['bytes'] / 1e9:.1f} GB resident per step"),
+            "config": config(f"inputs larger than L2: {r['bytes'] / 1e9:.1f} GB resident per step", w),
             "gpu_launches": int(r["launches"]), "clocks": r["clocks"]}
     # roofline of the dominant kernel (phase-3 tile kernel): int32 lane operations
     tms, tn = r["kprof"]["fw_tile_kernel"]
@@ -302,33 +388,38 @@ def main():
         ach = tile_relax_per_step * 2 / (tms / args.steps / 1e3) / 1e12
         line["roofline"]["achieved"] = ach
         line["roofline"]["frac"] = ach / (peak / 1e12)
+    e = r["e2e"]
+    line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                   "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["t"] / e["steps"] * 1e3,
+                   "api": "redblackgraph_gb300.sparse.component_wise_closure(forest CSR in pinned "
+                          "host memory) -> merged CSR on the host",
+                   "diameter": e["diameter"]}
     if rank == 0:
-        idx = cpu_sample(r["sizes"])
-        rate, tcpu, threads, outs, mats = cpu_closure_rate(r["sizes"], r["seeds"], idx)
+        idx = cpu_sample(w["csizes"])
+        rate, tcpu, threads, outs = cpu_closure_rate(w, idx)
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(idx)} of {COUNT} components (smallest of every size octave up to "
-                      f"{CPU_SAMPLE_RELAX / 8:.1e} relaxations per octave, sum n^3 = "
-                      f"{sum(int(r['sizes'][i]) ** 3 for i in idx):.3e}) closed in {tcpu:.1f} s "
+            "sample": f"{len(idx)} of {w['csizes'].size} components (smallest of every size octave up "
+                      f"to {CPU_SAMPLE_RELAX / 8:.1e} relaxations or 64 components per octave, sum "
+                      f"n^3 = {sum(int(w['csizes'][i]) ** 3 for i in idx):.3e}) closed in {tcpu:.1f} s "
                       "by the C restatement of the reference warshall, one component per host "
                       "thread; each octave's sum(n^3) extrapolated by its measured rate",
-            "sample_bit_exact_vs_gpu": sample_parity(r["sizes"], r["offsets"], r["out"], outs, idx, mats)}
-        line["e2e"] = None
+            "sample_bit_exact_vs_gpu": sample_parity(w, r["offsets"], r["out"], outs, idx, e["W"])}
         print(json.dumps(line))
 
 
 def main_reference(args, rank, world):
     if rank != 0:
         return
-    sizes, seeds = workload(0)
-    idx = cpu_sample(sizes)
-    work = float(sum(int(sizes[i]) ** 3 for i in idx))
+    w = workload(0)
+    idx = cpu_sample(w["csizes"])
+    work = float(sum(int(w["csizes"][i]) ** 3 for i in idx))
     rates, total_t = [], 0.0
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_closure_rate(sizes, seeds, idx[: max(1, len(idx) // 8)], threads)
+        cpu_closure_rate(w, idx[: max(1, len(idx) // 8)], threads)
     for _ in range(args.steps):
-        rate, t, threads, _, _ = cpu_closure_rate(sizes, seeds, idx, threads)
+        rate, t, threads, _ = cpu_closure_rate(w, idx, threads)
         rates.append(rate)
         total_t += t
     value = statistics.median(rates)
@@ -336,13 +427,13 @@ def main_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": total_t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded pedigree components generated in-process",
-            "config": config("CPU run"), "impl": "reference",
+            "config": config("CPU run", w), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{len(idx)} of {COUNT} components per step (smallest of "
-                                       f"every size octave, sum n^3 = {work:.3e}); C restatement "
-                                       "of the reference's warshall (core C gufunc), one "
-                                       "component per host thread, each octave extrapolated by "
-                                       "its measured rate"},
+                             "sample": f"{len(idx)} of {w['csizes'].size} components per step "
+                                       f"(smallest of every size octave, sum n^3 = {work:.3e}); C "
+                                       "restatement of the reference's warshall (core C gufunc), "
+                                       "one component per host thread, each octave extrapolated "
+                                       "by its measured rate"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

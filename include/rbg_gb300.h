@@ -248,6 +248,64 @@ int32_t rbg_avos_elementwise(int32_t op, int32_t dtype, int64_t n, const void *x
                              void *z, void *workspace, int64_t workspace_bytes, uint32_t *flags,
                              rbg_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Component-wise closure (redblackgraph/sparse/csgraph/transitive_closure.py:85-195): split a
+ * CSR graph (n vertices; int64 indptr, int32 indices, int32 values, all device buffers) into its
+ * connected components, densify each into the rbg_fw_batch layout, close them in one batch,
+ * and compact the closed blocks back into one CSR matrix with global indices.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Scratch bytes the rbg_cc_* calls need for an n-vertex graph (one workspace serves all). */
+int32_t rbg_cc_workspace_bytes(int64_t n, int64_t *bytes);
+
+/*
+ * Connected components with edges taken in both directions, numbered by their least vertex
+ * (replaces find_components_sparse, redblackgraph/sparse/csgraph/_components.pyx:86-177, and
+ * get_component_vertices, :326-344).  Outputs (device, caller-allocated):
+ *   label[n]          component of each vertex
+ *   sorted_vertex[n]  vertices grouped by component, ascending inside each component
+ *   local[n]          index of each vertex inside its component (extract_submatrix's renumbering,
+ *                     _components.pyx:180-252)
+ *   start[n + 1]      component c holds sorted_vertex[start[c] .. start[c + 1])
+ * and *ncomp (host).  The union-find loop is bounded (log2 n + 64 hooking passes); reaching
+ * the bound returns RBG_ERR_TIMEOUT.  Synchronises `stream`.
+ */
+int32_t rbg_cc_label(int64_t n, const int64_t *indptr, const int32_t *indices, void *workspace,
+                     int64_t workspace_bytes, int32_t *label, int32_t *sorted_vertex,
+                     int32_t *local, int64_t *start, int64_t *ncomp, rbg_stream_t stream);
+
+/*
+ * Zero `flat` (flat_elems int32) and scatter every stored value into its component's dense
+ * block: component c is the start[c+1]-start[c] square at element offset dense_off[c] (device
+ * array).  Replaces extract_submatrix + toarray (_components.pyx:180-252,
+ * transitive_closure.py:172-176).  Ordered on `stream`.
+ */
+int32_t rbg_cc_densify(int64_t n, const int64_t *indptr, const int32_t *indices,
+                       const int32_t *data, const int32_t *label, const int32_t *local,
+                       const int64_t *start, const int64_t *dense_off, int32_t *flat,
+                       int64_t flat_elems, rbg_stream_t stream);
+
+/*
+ * Count the nonzeros of the closed blocks per global row and scan them; *nnz (host) is the
+ * merged matrix's nnz.  When comp_max (device, ncomp int32) is not NULL it receives the largest
+ * value of each closed component, floored at 0 (the final-value diameter of the 'D' method,
+ * redblackgraph/sparse/csgraph/_shortest_path.pyx:842-845).  Synchronises `stream`.
+ */
+int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
+                             const int64_t *start, const int64_t *dense_off, const int32_t *flat,
+                             void *workspace, int64_t workspace_bytes, int64_t *nnz,
+                             int32_t *comp_max, rbg_stream_t stream);
+
+/*
+ * Write the merged CSR matrix (replaces merge_component_matrices, _components.pyx:254-324):
+ * indptr (n + 1, int64), indices (nnz, int32, ascending in each row), data (nnz, int32).  Uses
+ * the counts rbg_cc_compact_count left in `workspace`.  Ordered on `stream`.
+ */
+int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *local,
+                            const int64_t *start, const int64_t *dense_off, const int32_t *flat,
+                            const int32_t *sorted_vertex, const void *workspace, int64_t *indptr,
+                            int32_t *indices, int32_t *data, rbg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

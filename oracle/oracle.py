@@ -207,3 +207,66 @@ def rb_matmul_csr(a, b):
                             a.shape[0], b.shape[1])
     res = sp.csr_matrix((cx.astype(out_dtype), cj, cp), shape=(a.shape[0], b.shape[1]))
     return res, fl
+
+
+def components(indptr, indices, n: int) -> np.ndarray:
+    """Weakly connected components numbered by their least vertex (find_components_sparse,
+    redblackgraph/sparse/csgraph/_components.pyx:86-177: a DFS started from each unvisited
+    vertex in increasing order, following edges both ways).  Label propagation in numpy."""
+    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(np.asarray(indptr, dtype=np.int64)))
+    cols = np.asarray(indices, dtype=np.int64)
+    lab = np.arange(n, dtype=np.int64)
+    while True:
+        m = np.minimum(lab[rows], lab[cols])
+        new = lab.copy()
+        np.minimum.at(new, rows, m)
+        np.minimum.at(new, cols, m)
+        new = new[new]                          # pointer jumping
+        if (new == lab).all():
+            break
+        lab = new
+    roots = np.unique(lab)                      # ascending = ordered by least vertex
+    return np.searchsorted(roots, lab).astype(np.int64)
+
+
+def component_wise_closure(a, method: str = "auto", densify_threshold: int = 500):
+    """component_wise_closure (redblackgraph/sparse/csgraph/transitive_closure.py:85-195) with
+    each component closed by the Cython Floyd-Warshall restatement.
+
+    Returns ``(W csr int32, diameter, None)`` or ``(None, None, (component, info))`` for the first
+    component (by number) whose closure raises CycleError; ``info`` holds the local [kind, k, i, j].
+    A component takes the Floyd-Warshall diameter (running maximum) when the reference would
+    close it with floyd_warshall (:172-176) and MSB of its largest final value otherwise (:178-182,
+    _shortest_path.pyx:842-845); a single component takes "FW" only when asked (:151-158).
+    """
+    import scipy.sparse as sp
+    csr = sp.csr_matrix(a, copy=True)
+    csr.sum_duplicates()
+    csr.sort_indices()
+    n = csr.shape[0]
+    if n == 0:
+        return sp.csr_matrix((0, 0), dtype=np.int32), 0, None
+    lab = components(csr.indptr, csr.indices, n)
+    k = int(lab.max()) + 1
+    rows, cols, vals = [], [], []
+    diameter = 0
+    for c in range(k):
+        verts = np.flatnonzero(lab == c)
+        sub = csr[verts][:, verts].toarray().astype(np.int32)
+        W, d, st, info = fw_cython(sub)
+        if st != 0:
+            return None, None, (c, info)
+        fw = (method == "FW") if k == 1 else (len(verts) <= densify_threshold if method == "auto"
+                                              else method == "FW")
+        if not fw:
+            mx = int(W.max())
+            d = mx.bit_length() - 1 if mx > 1 else 0
+        diameter = max(diameter, d)
+        r, cc = np.nonzero(W)
+        rows.append(verts[r])
+        cols.append(verts[cc])
+        vals.append(W[r, cc])
+    W = sp.csr_matrix((np.concatenate(vals).astype(np.int32),
+                       (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+    W.sort_indices()
+    return W, diameter, None

@@ -91,6 +91,11 @@ SIGNATURES = [
     ("rbg_avos_matmul", _I32, [_I32, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
                                ctypes.POINTER(_U32), _P]),
     ("rbg_avos_elementwise", _I32, [_I32, _I32, _I64, _P, _P, _P, _P, _I64, ctypes.POINTER(_U32), _P]),
+    ("rbg_cc_workspace_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
+    ("rbg_cc_label", _I32, [_I64, _P, _P, _P, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64), _P]),
+    ("rbg_cc_densify", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _P]),
+    ("rbg_cc_compact_count", _I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P]),
+    ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
 ]
 
 _lib = None

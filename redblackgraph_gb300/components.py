@@ -1,0 +1,146 @@
+"""Component-wise closure on the GPU, at the device-tensor level.
+
+The graph (device CSR: int64 row pointers, int32 column indices, int32 values) is split into
+connected components by ``rbg_cc_label``, each component is scattered into its own dense block
+of one flat buffer (``rbg_cc_densify``), all blocks are closed by one ``rbg_fw_batch`` call in
+the Cython semantics, and the closed blocks are compacted back into one CSR matrix with global
+indices (``rbg_cc_compact_count`` / ``rbg_cc_compact_fill``).  Mirrors component_wise_closure,
+redblackgraph/sparse/csgraph/transitive_closure.py:85-195, whose per-component loop this batch
+replaces.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import default_workspace, stream_handle
+from .dense import fw_batch, raise_for_cython
+
+
+@dataclass
+class Components:
+    """Connected components of an n-vertex graph, on the device."""
+    n: int
+    count: int
+    label: torch.Tensor          # int32 [n]: component of each vertex (numbered by least vertex)
+    sorted_vertex: torch.Tensor  # int32 [n]: vertices grouped by component, ascending
+    local: torch.Tensor          # int32 [n]: index of each vertex inside its component
+    start: torch.Tensor          # int64 [n + 1]: component c is sorted_vertex[start[c]:start[c+1]]
+    workspace: torch.Tensor      # uint8 scratch shared by the rbg_cc_* calls
+    sizes: np.ndarray            # int64 [count] on the host
+
+
+@dataclass
+class DenseBlocks:
+    flat: torch.Tensor           # int32: every component's dense block, one after another
+    sizes: np.ndarray            # int64 [count]
+    offsets: np.ndarray          # int64 [count] element offsets into flat
+    dense_off: torch.Tensor      # the same offsets on the device
+
+
+def label_components(indptr: torch.Tensor, indices: torch.Tensor, n: int, stream=None) -> Components:
+    """Connected components with edges taken in both directions (_components.pyx:86-177)."""
+    dev = indptr.device
+    L = _lib.load()
+    nb = ctypes.c_int64(0)
+    _lib.check(L.rbg_cc_workspace_bytes(n, ctypes.byref(nb)), "cc_workspace_bytes")
+    ws = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=dev)
+    label = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    sv = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    local = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    start = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    nc = ctypes.c_int64(0)
+    idx_ptr = indices.data_ptr() if indices.numel() else indptr.data_ptr()
+    _lib.check(L.rbg_cc_label(n, indptr.data_ptr(), idx_ptr, ws.data_ptr(), ws.numel(), label.data_ptr(),
+                              sv.data_ptr(), local.data_ptr(), start.data_ptr(), ctypes.byref(nc),
+                              stream_handle(stream)), "cc_label")
+    count = nc.value
+    sizes = np.diff(start[:count + 1].cpu().numpy()) if count else np.zeros(0, np.int64)
+    return Components(n, count, label, sv, local, start, ws, sizes.astype(np.int64))
+
+
+def densify(indptr, indices, data, comps: Components, stream=None) -> DenseBlocks:
+    """Scatter the stored values into one dense block per component (zeros elsewhere)."""
+    sizes = comps.sizes
+    offsets = np.zeros_like(sizes)
+    if sizes.size > 1:
+        offsets[1:] = np.cumsum(sizes[:-1] * sizes[:-1])
+    total = int((sizes * sizes).sum())
+    dev = indptr.device
+    flat = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    dense_off = torch.from_numpy(offsets if offsets.size else np.zeros(1, np.int64)).to(dev)
+    L = _lib.load()
+    ip = indptr.data_ptr()
+    _lib.check(L.rbg_cc_densify(comps.n, ip, indices.data_ptr() if indices.numel() else ip,
+                                data.data_ptr() if data.numel() else ip, comps.label.data_ptr(),
+                                comps.local.data_ptr(), comps.start.data_ptr(), dense_off.data_ptr(),
+                                flat.data_ptr(), total, stream_handle(stream)), "cc_densify")
+    return DenseBlocks(flat, sizes, offsets, dense_off)
+
+
+def compact(comps: Components, blocks: DenseBlocks, want_max: bool = False, stream=None):
+    """Merge the closed blocks into one CSR matrix (_components.pyx:254-324).
+
+    Returns ``(indptr int64, indices int32, data int32, comp_max or None)``."""
+    dev = blocks.flat.device
+    L = _lib.load()
+    n, k = comps.n, comps.count
+    cmax = torch.empty(max(k, 1), dtype=torch.int32, device=dev) if want_max else None
+    nnz = ctypes.c_int64(0)
+    sh = stream_handle(stream)
+    args = (comps.label.data_ptr(), comps.local.data_ptr(), comps.start.data_ptr(),
+            blocks.dense_off.data_ptr(), blocks.flat.data_ptr())
+    _lib.check(L.rbg_cc_compact_count(n, k, *args, comps.workspace.data_ptr(), comps.workspace.numel(),
+                                      ctypes.byref(nnz), cmax.data_ptr() if cmax is not None else None, sh),
+               "cc_compact_count")
+    indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    indices = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
+    data = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
+    _lib.check(L.rbg_cc_compact_fill(n, *args, comps.sorted_vertex.data_ptr(), comps.workspace.data_ptr(),
+                                     indptr.data_ptr(), indices.data_ptr(), data.data_ptr(), sh),
+               "cc_compact_fill")
+    return indptr, indices[:nnz.value], data[:nnz.value], cmax
+
+
+def component_methods(sizes: np.ndarray, count: int, method: str, densify_threshold: int) -> np.ndarray:
+    """True where a component takes the Floyd-Warshall diameter, False for the 'D' one
+    (transitive_closure.py:151-187: a single component takes "FW" only when asked for; with
+    "auto" components up to ``densify_threshold`` vertices take "FW"; any other method string
+    runs the 'D' branch)."""
+    if count == 1:
+        return np.array([method == "FW"])
+    if method == "auto":
+        return sizes <= densify_threshold
+    return np.full(sizes.shape, method == "FW")
+
+
+def _msb(v: int) -> int:
+    return v.bit_length() - 1 if v > 1 else 0
+
+
+def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor, n: int,
+                             method: str = "auto", densify_threshold: int = 500, stream=None):
+    """Close every component of the device CSR graph.
+
+    Returns ``(indptr, indices, data, diameter, comps)``; raises CycleError for the first
+    component (by number) that holds a cycle, as the reference's per-component loop does.
+    """
+    comps = label_components(indptr, indices, n, stream)
+    blocks = densify(indptr, indices, data, comps, stream)
+    _, results = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat,
+                          mode=_lib.MODE_CYTHON, stream=stream)
+    for r in results:
+        raise_for_cython(r)
+    fw = component_methods(comps.sizes, comps.count, method, densify_threshold)
+    oi, oj, ov, cmax = compact(comps, blocks, want_max=not bool(fw.all()), stream=stream)
+    diameter = 0
+    if fw.any():
+        diameter = max(int(r.diameter) for r, f in zip(results, fw) if f)
+    if cmax is not None:
+        mx = cmax[:comps.count].cpu().numpy()
+        diameter = max(diameter, _msb(int(mx[~fw].max())))
+    return oi, oj, ov, diameter, comps

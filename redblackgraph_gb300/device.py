@@ -68,7 +68,7 @@ def to_device(a: np.ndarray, device: torch.device | None = None,
     device = device or require_cuda()
     a = np.ascontiguousarray(a)
     raw = torch.from_numpy(a.reshape(-1).view(np.uint8))
-    if a.nbytes >= (1 << 20):
+    if a.nbytes >= (1 << 20) and not raw.is_pinned():
         raw = raw.pin_memory()
     with torch.cuda.stream(stream) if stream is not None else _nullctx():
         d = raw.to(device, non_blocking=True)

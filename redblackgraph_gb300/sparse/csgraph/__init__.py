@@ -6,9 +6,11 @@ from .transitive_closure import (
     transitive_closure_dijkstra,
     transitive_closure_squaring,
     transitive_closure_dag_sparse,
+    component_wise_closure,
 )
 from .cycleerror import CycleError
 
 __all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
            "transitive_closure_floyd_warshall", "transitive_closure_dijkstra",
-           "transitive_closure_squaring", "transitive_closure_dag_sparse", "CycleError"]
+           "transitive_closure_squaring", "transitive_closure_dag_sparse", "component_wise_closure",
+           "CycleError"]

@@ -135,3 +135,25 @@ def batch_edges(sizes, seeds, p_parent: float = 0.9):
         idx.append(o + c * n + p)
         val.append(v)
     return np.concatenate(idx), np.concatenate(val), offsets
+
+
+def batch_forest(sizes, seeds, p_parent: float = 0.9):
+    """The pedigree components of ``batch_components`` laid out one after another as one sparse
+    forest (block diagonal CSR, int32 values).  Component i is ``pedigree_csr(sizes[i],
+    generations_for(sizes[i]), seeds[i])`` on vertices base[i] .. base[i] + sizes[i]."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    base = np.concatenate([[0], np.cumsum(sizes)])
+    rows, cols, vals = [], [], []
+    for n, s, b in zip(sizes, seeds, base[:-1]):
+        n = int(n)
+        colors, c, p, v = pedigree_edges(n, generations_for(n), int(s), p_parent)
+        ar = np.arange(n, dtype=np.int64)
+        rows += [b + ar, b + c]
+        cols += [b + ar, b + p]
+        vals += [colors, v]
+    N = int(base[-1])
+    m = sp.csr_matrix((np.concatenate(vals).astype(np.int32),
+                       (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+    m.sum_duplicates()
+    m.sort_indices()
+    return m, base

@@ -248,6 +248,43 @@ def main():
         arrays[key + "_W"] = np.asarray(res.W)
         index["dijkstra"].append({"key": key, "diameter": int(res.diameter)})
 
+    # ---------------------------------------------------------------- component-wise closure
+    index["components"] = []
+    for ci, (sizes, seed, method, thr, cyc) in enumerate([
+            ([30, 5, 80, 1, 45, 12], 31, "auto", 40, False),
+            ([30, 5, 80, 1, 45, 12], 31, "FW", 500, False),
+            ([30, 5, 80, 1, 45, 12], 31, "D", 500, False),
+            ([70], 32, "auto", 500, False),
+            ([70], 32, "FW", 500, False),
+            ([20, 35, 9], 33, "auto", 500, True)]):
+        blocks = [synth.pedigree_csr(n, max(2, n // 8), seed + j, dtype=np.int32)
+                  for j, n in enumerate(sizes)]
+        M = sp.block_diag(blocks, format="csr").astype(np.int32)
+        perm = np.random.default_rng(seed).permutation(M.shape[0])
+        M = sp.csr_matrix(M[perm][:, perm])
+        if cyc:                                   # a cycle inside the second component
+            M = M.tolil()
+            rows = np.flatnonzero(np.isin(perm, np.arange(20, 55)))
+            Mc = M[rows][:, rows].tocoo()
+            off = Mc.row != Mc.col
+            a, b = rows[Mc.row[off][0]], rows[Mc.col[off][0]]
+            M[b, a] = 2
+            M = M.tocsr()
+        M.sort_indices()
+        key = f"c{ci}"
+        arrays[key + "_indptr"], arrays[key + "_indices"], arrays[key + "_data"] = M.indptr, M.indices, M.data
+        rec = {"key": key, "n": int(M.shape[0]), "method": method, "threshold": thr}
+        try:
+            res = csgraph.component_wise_closure(M, method=method, densify_threshold=thr)
+            W = sp.csr_matrix(res.W)
+            W.sort_indices()
+            arrays[key + "_W_indptr"], arrays[key + "_W_indices"], arrays[key + "_W_data"] = W.indptr, W.indices, W.data
+            rec["diameter"] = int(res.diameter)
+        except Exception as e:
+            rec["error"] = exc_name(e)
+            rec["vertex"] = getattr(e, "vertex", None)
+        index["components"].append(rec)
+
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "index.json").write_text(json.dumps(index, indent=1))
     print(f"wrote {len(arrays)} arrays, {len(index['warshall'])} warshall cases")

@@ -1,0 +1,118 @@
+"""Component-wise closure on the GPU (component split, batched closure, merge) against the
+reference's golden answers and the oracle, bit-exact."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(a, b):
+    a, b = sp.csr_matrix(a), sp.csr_matrix(b)
+    a.sort_indices()
+    b.sort_indices()
+    return (a.shape == b.shape and a.nnz == b.nnz and (a.indptr == b.indptr).all()
+            and (a.indices == b.indices).all() and (a.data == b.data).all())
+
+
+def _shuffled_forest(sizes, seed, dtype=np.int32):
+    from redblackgraph_gb300 import synth
+    blocks = [synth.pedigree_csr(int(n), synth.generations_for(int(n)), seed + j, dtype=dtype)
+              for j, n in enumerate(sizes)]
+    M = sp.block_diag(blocks, format="csr")
+    perm = np.random.default_rng(seed).permutation(M.shape[0])
+    M = sp.csr_matrix(M[perm][:, perm])
+    M.sort_indices()
+    return M
+
+
+def test_golden_component_wise_closure(native, golden):
+    from redblackgraph_gb300.sparse import component_wise_closure, CycleError
+    arrays, index = golden
+    for rec in index["components"]:
+        k, n = rec["key"], rec["n"]
+        A = sp.csr_matrix((arrays[k + "_data"], arrays[k + "_indices"], arrays[k + "_indptr"]), shape=(n, n))
+        if "error" in rec:
+            with pytest.raises(CycleError) as ei:
+                component_wise_closure(A, rec["method"], rec["threshold"])
+            assert ei.value.vertex == rec["vertex"]
+            continue
+        r = component_wise_closure(A, method=rec["method"], densify_threshold=rec["threshold"])
+        E = sp.csr_matrix((arrays[k + "_W_data"], arrays[k + "_W_indices"], arrays[k + "_W_indptr"]),
+                          shape=(n, n))
+        assert _same(r.W, E), rec
+        assert r.W.dtype == np.int32 and r.W.has_sorted_indices
+        assert r.diameter == rec["diameter"], rec
+
+
+def test_labels_match_oracle(native):
+    import torch
+    from redblackgraph_gb300.components import label_components
+    from redblackgraph_gb300.device import to_device, to_host
+    M = _shuffled_forest([50, 1, 3, 400, 17, 2, 90, 1], seed=41)
+    n = M.shape[0]
+    c = label_components(to_device(M.indptr.astype(np.int64)), to_device(M.indices.astype(np.int32)), n)
+    lab = O.components(M.indptr, M.indices, n)
+    assert c.count == int(lab.max()) + 1
+    assert (to_host(c.label)[:n] == lab).all()
+    sv = to_host(c.sorted_vertex)[:n]
+    assert (sv == np.argsort(lab, kind="stable")).all()
+    st = to_host(c.start)[:c.count + 1]
+    assert (np.diff(st) == np.bincount(lab)).all()
+    loc = to_host(c.local)[:n]
+    assert (loc[sv] == np.arange(n) - st[lab[sv]]).all()
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("method,threshold", [("auto", 500), ("auto", 100), ("FW", 500), ("D", 500)])
+def test_forest_vs_oracle(native, method, threshold):
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.sparse import component_wise_closure
+    sizes = synth.component_sizes(40, 4, 700, seed=5)
+    M = _shuffled_forest(sizes, seed=7)
+    r = component_wise_closure(M, method=method, densify_threshold=threshold)
+    W, d, err = O.component_wise_closure(M, method, threshold)
+    assert err is None
+    assert _same(r.W, W)
+    assert r.diameter == d
+
+
+def test_single_component_and_edge_cases(native):
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.sparse import component_wise_closure
+    M = synth.pedigree_csr(300, 12, 9)
+    for method in ("auto", "FW", "D"):
+        r = component_wise_closure(M, method=method)
+        W, d, err = O.component_wise_closure(M, method, 500)
+        assert err is None and _same(r.W, W) and r.diameter == d
+    r = component_wise_closure(sp.csr_matrix((0, 0), dtype=np.int32))
+    assert r.W.shape == (0, 0) and r.diameter == 0
+    E = sp.csr_matrix((5, 5), dtype=np.int32)                  # no stored entries at all
+    r = component_wise_closure(E)
+    assert r.W.nnz == 0 and r.diameter == 0
+    # duplicate entries are summed (scipy's toarray in the reference), dense input accepted
+    D = sp.coo_matrix((np.array([1, -1, 1, 1, 1]), (np.array([0, 1, 0, 2, 2]), np.array([0, 1, 1, 2, 0]))),
+                      shape=(3, 3))
+    r = component_wise_closure(D)
+    W, d, err = O.component_wise_closure(D, "auto", 500)
+    assert _same(r.W, W) and r.diameter == d
+    r2 = component_wise_closure(D.toarray())
+    assert _same(r2.W, W)
+
+
+def test_cycle_in_a_later_component_raises(native):
+    from redblackgraph_gb300.sparse import component_wise_closure, CycleError
+    M = _shuffled_forest([30, 60, 25], seed=13).tolil()
+    lab = O.components(sp.csr_matrix(M).indptr, sp.csr_matrix(M).indices, M.shape[0])
+    verts = np.flatnonzero(lab == 1)
+    sub = sp.csr_matrix(M)[verts][:, verts].tocoo()
+    off = np.flatnonzero(sub.row != sub.col)[0]
+    M[verts[sub.col[off]], verts[sub.row[off]]] = 2            # close a two-vertex cycle
+    M = sp.csr_matrix(M)
+    _, _, err = O.component_wise_closure(M)
+    assert err is not None and err[0] == 1
+    with pytest.raises(CycleError) as ei:
+        component_wise_closure(M)
+    assert ei.value.vertex == int(err[1][2])

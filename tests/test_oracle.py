@@ -100,3 +100,22 @@ def test_warshall_triangular_equals_full_on_upper():
     W1, d1, s1, _ = O.warshall(A)
     W2, d2, s2, _ = O.warshall(A, triangular=True)
     assert (W1 == W2).all() and d1 == d2 and s1 == s2 == 0
+
+
+def test_oracle_component_wise_closure_vs_golden(golden):
+    """The component split, per-component closure, merge and diameter rule against the
+    reference's component_wise_closure on forests with shuffled vertices."""
+    import scipy.sparse as sp
+    arrays, index = golden
+    for rec in index["components"]:
+        k, n = rec["key"], rec["n"]
+        A = sp.csr_matrix((arrays[k + "_data"], arrays[k + "_indices"], arrays[k + "_indptr"]), shape=(n, n))
+        W, d, err = O.component_wise_closure(A, rec["method"], rec["threshold"])
+        if "error" in rec:
+            assert err is not None and rec["error"] == "CycleError"
+            assert int(err[1][2]) == rec["vertex"]      # the reference reports the local vertex
+            continue
+        E = sp.csr_matrix((arrays[k + "_W_data"], arrays[k + "_W_indices"], arrays[k + "_W_indptr"]),
+                          shape=(n, n))
+        assert d == rec["diameter"], rec
+        assert (W.indptr == E.indptr).all() and (W.indices == E.indices).all() and (W.data == E.data).all()
