@@ -46,7 +46,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    return ap.parse_args()
+    ap.add_argument("--count", type=int, default=COUNT,
+                    help="pedigrees in the forest (smaller values: profiling cases)")
+    ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
+    args = ap.parse_args()
+    globals()["COUNT"], globals()["HI"] = args.count, args.hi
+    return args
 
 
 def workload(rank: int):
