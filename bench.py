@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--count", type=int, default=COUNT,
                     help="pedigrees in the forest (smaller values: profiling cases)")
     ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
+    ap.add_argument("--serve", type=int, default=1, help="also run the serving workload (0: skip)")
+    ap.add_argument("--serve-count", type=int, default=0, help="requests in the serving stream")
     args = ap.parse_args()
     globals()["COUNT"], globals()["HI"] = args.count, args.hi
     return args
@@ -355,6 +357,57 @@ def sample_parity(w, offsets, out, cpu_outs, idx, W_e2e=None):
     return ok
 
 
+SERVE = dict(count=2000, rate=2000.0, lookup_fraction=0.5, lo=64, hi=16384, seed=11, warm=64,
+             budget=150 << 30)
+
+
+def serve_stats(st, reqs):
+    lat = st.latency_ms
+    return {"p50_ms": lat["all"]["p50"], "p99_ms": lat["all"]["p99"],
+            "closure_p50_ms": lat["closure"]["p50"], "closure_p99_ms": lat["closure"]["p99"],
+            "lookup_p50_ms": lat["lookup"]["p50"], "lookup_p99_ms": lat["lookup"]["p99"],
+            "throughput_req_s": len(reqs) / st.makespan_s,
+            "closure_relax_per_s": st.relaxations / st.makespan_s,
+            "makespan_s": st.makespan_s, "batches": st.batches, "max_batch": st.max_batch,
+            "lookup_launches": st.lookup_launches, "evictions": st.evictions, "reloads": st.reloads,
+            "peak_arena_gb": st.peak_arena_bytes / 1e9,
+            "errors": sum(1 for r in reqs if r.kind == "closure" and r.result[0] != 0)}
+
+
+def run_serving(count=None):
+    """The serving workload: Poisson arrivals of closure and lookup requests on resident graphs,
+    served with continuous batching and, for comparison, one request at a time."""
+    import torch
+    from redblackgraph_gb300.serving import GpuExecutor, Policy, Server, make_stream
+    cfg = dict(SERVE)
+    if count:
+        cfg["count"] = count
+    allreq = make_stream(cfg["count"], cfg["rate"], cfg["lookup_fraction"], cfg["lo"], cfg["hi"],
+                         cfg["seed"], warm=cfg["warm"])
+    warm, reqs = allreq[:cfg["warm"]], allreq[cfg["warm"]:]
+    ex = GpuExecutor(arena_bytes=cfg["budget"], slots=2)
+    ex.prepare(allreq)
+    out = {"workload": f"Poisson arrivals at {cfg['rate']:.0f} req/s, {cfg['count']} requests, "
+                       f"{int(cfg['lookup_fraction'] * 100)}% relationship lookups / "
+                       f"{100 - int(cfg['lookup_fraction'] * 100)}% closures, pedigrees log-uniform in "
+                       f"[{cfg['lo']}, {cfg['hi']}] (int32 up to 4096 vertices, int64 above), "
+                       f"{cfg['warm']} graphs closed and resident before the stream, "
+                       f"{cfg['budget'] >> 30} GiB resident-graph budget",
+           "latency": "arrival to completion on the host clock"}
+    for name, pol in (("batched", Policy(inflight=2)), ("unbatched", Policy.unbatched_baseline())):
+        for r in allreq:
+            r.done, r.result = float("nan"), None
+        srv = Server(ex, cfg["budget"], pol)
+        srv.run(warm)
+        torch.cuda.synchronize()
+        st = srv.run(reqs)
+        out[name] = serve_stats(st, reqs)
+    ex.close()
+    del ex
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", 0))
@@ -410,6 +463,12 @@ def main():
                       "by the C restatement of the reference warshall, one component per host "
                       "thread; each octave's sum(n^3) extrapolated by its measured rate",
             "sample_bit_exact_vs_gpu": sample_parity(w, r["offsets"], r["out"], outs, idx, e["W"])}
+    r.pop("out", None)
+    import torch
+    torch.cuda.empty_cache()
+    if args.serve:
+        line["serving"] = run_serving(args.serve_count)
+    if rank == 0:
         print(json.dumps(line))
 
 

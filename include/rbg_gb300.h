@@ -275,14 +275,18 @@ int32_t rbg_cc_label(int64_t n, const int64_t *indptr, const int32_t *indices, v
                      int32_t *local, int64_t *start, int64_t *ncomp, rbg_stream_t stream);
 
 /*
- * Zero `flat` (flat_elems int32) and scatter every stored value into its component's dense
- * block: component c is the start[c+1]-start[c] square at element offset dense_off[c] (device
- * array).  Replaces extract_submatrix + toarray (_components.pyx:180-252,
- * transitive_closure.py:172-176).  Ordered on `stream`.
+ * Write each component's dense block into `flat` (elements of `dtype`, RBG_DTYPE_INT32 or
+ * RBG_DTYPE_INT64): component c is the start[c+1]-start[c] square at element offset
+ * dense_off[c] (device array); its rows are zeroed and every stored int32 value
+ * (sign-extended for int64) is scattered in.  Replaces extract_submatrix + toarray
+ * (_components.pyx:180-252, transitive_closure.py:172-176).  Only the blocks are written, so
+ * they may sit anywhere in a larger buffer (flat_elems bounds them; a block past it is
+ * skipped).  Any grouping of the vertices into blocks works, not only connected components;
+ * entries joining two blocks are dropped.  Ordered on `stream`.
  */
-int32_t rbg_cc_densify(int64_t n, const int64_t *indptr, const int32_t *indices,
+int32_t rbg_cc_densify(int32_t dtype, int64_t n, const int64_t *indptr, const int32_t *indices,
                        const int32_t *data, const int32_t *label, const int32_t *local,
-                       const int64_t *start, const int64_t *dense_off, int32_t *flat,
+                       const int64_t *start, const int64_t *dense_off, void *flat,
                        int64_t flat_elems, rbg_stream_t stream);
 
 /*
@@ -305,6 +309,31 @@ int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *loca
                             const int64_t *start, const int64_t *dense_off, const int32_t *flat,
                             const int32_t *sorted_vertex, const void *workspace, int64_t *indptr,
                             int32_t *indices, int32_t *data, rbg_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Relationship lookups on resident closures (redblackgraph/reference/calc_relationship.py:54-71).
+ * ---------------------------------------------------------------------------------------- */
+typedef struct rbg_lookup_t {
+    const void *W;     /* device: closed matrix, row-major, leading dimension ld (elements) */
+    int64_t ld;
+    int64_t rows;      /* rows of W (u and v must be below) */
+    int64_t n;         /* row length (columns searched) */
+    int64_t u, v;      /* the two vertices (rows) */
+    int32_t dtype;     /* RBG_DTYPE_* of W */
+    int32_t reserved;
+} rbg_lookup_t;
+
+/*
+ * For every query (a device array of `count` rbg_lookup_t), the common ancestor of u and v:
+ * the first j minimising W[u][j] + W[v][j] over the j where both are non-zero, the sum wrapping
+ * in W's type as numpy scalar arithmetic does on the reference's rows.  out (device, 3 int64
+ * per query) receives j (-1: no relationship; -2: invalid query), W[u][j], W[v][j] (the value
+ * bits, to be read back in the matrix's dtype).  The relationship name is formed from the two
+ * values on the host (lookup_relationship, calc_relationship.py:23-51).  Ordered on `stream`,
+ * no synchronisation.
+ */
+int32_t rbg_relationship_lookup(int64_t count, const rbg_lookup_t *queries, int64_t *out,
+                                rbg_stream_t stream);
 
 #ifdef __cplusplus
 }

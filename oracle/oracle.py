@@ -270,3 +270,58 @@ def component_wise_closure(a, method: str = "auto", densify_threshold: int = 500
                        (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
     W.sort_indices()
     return W, diameter, None
+
+
+def _wrap(v: int, dtype) -> int:
+    """v reduced to the range of the integer dtype (two's complement wrap)."""
+    info = np.iinfo(dtype)
+    span = 1 << (8 * np.dtype(dtype).itemsize)
+    return (v - int(info.min)) % span + int(info.min)
+
+
+def calculate_relationship(a, b):
+    """calculate_relationship (redblackgraph/reference/calc_relationship.py:54-71) on two closure
+    rows given as numpy arrays: the first j minimising a[j] + b[j] over the j where both are
+    non-zero, the sum taken as numpy scalar arithmetic does (wrapping in the rows' dtype);
+    then the name from MSB of the two values (rbg_math.py:1-11, calc_relationship.py:23-51).
+    Returns (common ancestor, name)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    dt = np.result_type(a.dtype, b.dtype)
+    best, bj = None, -1
+    for j in range(a.size):
+        x, y = int(a[j]), int(b[j])
+        if x != 0 and y != 0:
+            s = _wrap(x + y, dt)
+            if best is None or s < best:
+                best, bj = s, j
+    if bj < 0:
+        return -1, "No Relationship"
+
+    def msb(x):
+        p = 0
+        while x > 1:
+            x >>= 1
+            p += 1
+        return p
+
+    da, db = msb(int(a[bj])), msb(int(b[bj]))
+    removal = abs(da - db)
+
+    def cousinth(g):
+        return {2: "1st cousin", 3: "2nd cousin", 4: "3rd cousin"}.get(g, f"{g - 1}th cousin")
+
+    if da == 0 or db == 0:
+        names = {1: "parent", 2: "grandparent", 3: "great grandparent"}
+        if removal in names:
+            return bj, names[removal]
+        gp = {4: "2nd", 5: "3rd"}.get(removal, f"{removal - 2}th")
+        return bj, f"{gp} great grandparent"
+    g = min(da, db)
+    if g == 1 and removal == 0:
+        return bj, "sibling"
+    if g == 1 and removal == 1:
+        return bj, "aunt/uncle"
+    if removal == 0:
+        return bj, cousinth(g)
+    return bj, f"{cousinth(g)} {removal} removed"

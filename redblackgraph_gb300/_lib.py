@@ -61,6 +61,13 @@ class RbgCsr(ctypes.Structure):
                 ("data", ctypes.c_void_p)]
 
 
+class RbgLookup(ctypes.Structure):
+    """rbg_lookup_t: one relationship query on a resident closed matrix."""
+    _fields_ = [("W", ctypes.c_void_p), ("ld", ctypes.c_int64), ("rows", ctypes.c_int64),
+                ("n", ctypes.c_int64), ("u", ctypes.c_int64), ("v", ctypes.c_int64),
+                ("dtype", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 # (name, restype, argtypes) of every exported entry point; include/rbg_gb300.h declares them
 _P = ctypes.c_void_p
 _I32, _U32, _I64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
@@ -93,9 +100,10 @@ SIGNATURES = [
     ("rbg_avos_elementwise", _I32, [_I32, _I32, _I64, _P, _P, _P, _P, _I64, ctypes.POINTER(_U32), _P]),
     ("rbg_cc_workspace_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
     ("rbg_cc_label", _I32, [_I64, _P, _P, _P, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64), _P]),
-    ("rbg_cc_densify", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _P]),
+    ("rbg_cc_densify", _I32, [_I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _P]),
     ("rbg_cc_compact_count", _I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P]),
     ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("rbg_relationship_lookup", _I32, [_I64, _P, _P, _P]),
 ]
 
 _lib = None

@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import default_workspace, stream_handle
+from .device import stream_handle
 from .dense import fw_batch, raise_for_cython
 
 
@@ -75,7 +75,7 @@ def densify(indptr, indices, data, comps: Components, stream=None) -> DenseBlock
     dense_off = torch.from_numpy(offsets if offsets.size else np.zeros(1, np.int64)).to(dev)
     L = _lib.load()
     ip = indptr.data_ptr()
-    _lib.check(L.rbg_cc_densify(comps.n, ip, indices.data_ptr() if indices.numel() else ip,
+    _lib.check(L.rbg_cc_densify(_lib.dtype_code(np.int32), comps.n, ip, indices.data_ptr() if indices.numel() else ip,
                                 data.data_ptr() if data.numel() else ip, comps.label.data_ptr(),
                                 comps.local.data_ptr(), comps.start.data_ptr(), dense_off.data_ptr(),
                                 flat.data_ptr(), total, stream_handle(stream)), "cc_densify")

@@ -84,17 +84,25 @@ __global__ void cc_local_kernel(int n, const int *sorted_label, const int *sorte
         local[sorted_vertex[p]] = (int)(p - start[sorted_label[p]]);
 }
 
-// scatter the stored entries into the per-component dense blocks (already zeroed)
+// one warp per vertex row: zero the row of its block, then scatter the row's stored entries
+// (__syncwarp orders the zeroing before the scatter).  Rows whose block would reach past
+// flat_elems are skipped.
+template <class T>
 __global__ void cc_densify_kernel(int64_t n, const int64_t *indptr, const int *indices, const int *data,
                                   const int *label, const int *local, const int64_t *start,
-                                  const int64_t *dense_off, int *flat) {
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+                                  const int64_t *dense_off, T *flat, int64_t flat_elems) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += warps) {
         const int c = label[u];
         const int64_t nc = start[c + 1] - start[c];
         const int64_t row = dense_off[c] + (int64_t)local[u] * nc;
-        for (int64_t e = indptr[u]; e < indptr[u + 1]; ++e) {
+        if (dense_off[c] < 0 || dense_off[c] + nc * nc > flat_elems) continue;
+        for (int64_t j = lane; j < nc; j += 32) flat[row + j] = (T)0;
+        __syncwarp();
+        for (int64_t e = indptr[u] + lane; e < indptr[u + 1]; e += 32) {
             const int v = indices[e];
-            if (v >= 0 && v < n) flat[row + local[v]] = data[e];
+            if (v >= 0 && v < n && label[v] == c) flat[row + local[v]] = (T)data[e];
         }
     }
 }
@@ -257,16 +265,22 @@ extern "C" int32_t rbg_cc_label(int64_t n, const int64_t *indptr, const int32_t 
     return RBG_OK;
 }
 
-extern "C" int32_t rbg_cc_densify(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
-                                  const int32_t *label, const int32_t *local, const int64_t *start,
-                                  const int64_t *dense_off, int32_t *flat, int64_t flat_elems, rbg_stream_t stream) {
+extern "C" int32_t rbg_cc_densify(int32_t dtype, int64_t n, const int64_t *indptr, const int32_t *indices,
+                                  const int32_t *data, const int32_t *label, const int32_t *local,
+                                  const int64_t *start, const int64_t *dense_off, void *flat, int64_t flat_elems,
+                                  rbg_stream_t stream) {
     if (n < 0 || !flat || flat_elems < 0) return RBG_ERR_INVALID;
+    if (dtype != RBG_DTYPE_INT32 && dtype != RBG_DTYPE_INT64) return RBG_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    RBG_CUDA_TRY(cudaMemsetAsync(flat, 0, (size_t)flat_elems * 4, s));
     if (n > 0) {
         note_launches(1);
-        cc_densify_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, indptr, indices, data, label, local, start, dense_off,
-                                                           flat);
+        const int g = grid_for(n * 32, 256);
+        if (dtype == RBG_DTYPE_INT64)
+            cc_densify_kernel<int64_t><<<g, 256, 0, s>>>(n, indptr, indices, data, label, local, start, dense_off,
+                                                          reinterpret_cast<int64_t *>(flat), flat_elems);
+        else
+            cc_densify_kernel<int32_t><<<g, 256, 0, s>>>(n, indptr, indices, data, label, local, start, dense_off,
+                                                          reinterpret_cast<int32_t *>(flat), flat_elems);
         RBG_CUDA_TRY(cudaGetLastError());
     }
     return RBG_OK;

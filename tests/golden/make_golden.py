@@ -285,6 +285,26 @@ def main():
             rec["vertex"] = getattr(e, "vertex", None)
         index["components"].append(rec)
 
+    # ---------------------------------------------------------------- relationship lookups
+    from redblackgraph.reference import calculate_relationship
+    index["relationship"] = []
+    for ci, (n, g, sd, dt) in enumerate([(120, 8, 41, np.int32), (90, 7, 42, np.uint32),
+                                         (200, 10, 43, np.int64)]):
+        A = synth.pedigree(n, g, sd, dtype=np.int64)
+        W, _, st, _ = O.warshall(A)
+        assert st == 0
+        W = W.astype(dt)                      # the red one -1 becomes the unsigned maximum
+        key = f"r{ci}"
+        arrays[key + "_W"] = W
+        rng = np.random.default_rng(sd)
+        pairs = rng.integers(0, n, size=(150, 2))
+        out = []
+        for u, v in pairs:
+            with np.errstate(over="ignore"):
+                rel = calculate_relationship(list(W[u]), list(W[v]))
+            out.append([int(u), int(v), int(rel.common_ancestor), rel.relationship])
+        index["relationship"].append({"key": key, "pairs": out})
+
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "index.json").write_text(json.dumps(index, indent=1))
     print(f"wrote {len(arrays)} arrays, {len(index['warshall'])} warshall cases")

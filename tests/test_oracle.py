@@ -119,3 +119,13 @@ def test_oracle_component_wise_closure_vs_golden(golden):
                           shape=(n, n))
         assert d == rec["diameter"], rec
         assert (W.indptr == E.indptr).all() and (W.indices == E.indices).all() and (W.data == E.data).all()
+
+
+def test_oracle_relationship_vs_golden(golden):
+    """Relationship lookups against the reference's calculate_relationship on closure rows
+    (numpy rows: sums wrap in the rows' dtype, as numpy scalar arithmetic does)."""
+    arrays, index = golden
+    for rec in index["relationship"]:
+        W = arrays[rec["key"] + "_W"]
+        for u, v, ca, name in rec["pairs"]:
+            assert O.calculate_relationship(W[u], W[v]) == (ca, name), (rec["key"], u, v)
