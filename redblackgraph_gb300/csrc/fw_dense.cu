@@ -95,13 +95,12 @@ static void timer_end(int kid, cudaEvent_t start, cudaStream_t s) {
 }
 
 int grid_for(int64_t work, int threads) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 152;
+    }();
     int64_t blocks = (work + threads - 1) / threads;
     int64_t cap = (int64_t)sms * 16;
     if (blocks > cap) blocks = cap;
@@ -823,12 +822,8 @@ template <typename T, typename U>
 static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws, cudaStream_t stream,
                           bool stop_after_convert, DevStatus *h_status) {
     typedef TileCfg<U> C;
-    static bool configured = false;
-    if (!configured) {
-        int rc = configure_kernels<U>();
-        if (rc) return rc;
-        configured = true;
-    }
+    static const int configured = configure_kernels<U>();   // once, thread-safe initialisation
+    if (configured) return configured;
     const int cnt = P.count;
     DevStatus *st = reinterpret_cast<DevStatus *>(ws + P.off_status);
     const FwComp *comps = reinterpret_cast<const FwComp *>(ws + P.off_comps);
@@ -846,13 +841,12 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     int2 *plist = reinterpret_cast<int2 *>(ws + P.off_plist);
     int2 *tlist = reinterpret_cast<int2 *>(ws + P.off_tlist);
     int *counters = reinterpret_cast<int *>(ws + P.off_counters);
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 152;
+    }();
     const int64_t persist = 2 * (int64_t)sms;   // two CTAs per SM for both persistent kernels
 
     RBG_CUDA_TRY(cudaMemsetAsync(occ, 0, std::max<size_t>(P.occ_bytes, 1), stream));

@@ -565,14 +565,14 @@ namespace {
 
 template <int SEM, bool UNS>
 int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
+    static const int configured = [] {      // once, thread-safe initialisation
         RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)SP_WARP_SMEM));
         RBG_CUDA_TRY(cudaFuncSetAttribute(sp_block_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)SP_BLOCK_SMEM));
-        configured = true;
-    }
+        return (int)RBG_OK;
+    }();
+    if (configured) return configured;
     const int64_t n = a.n_rows;
     note_launches(2 + (dense > 0 ? 2 : 0));
     sp_warp_kernel<SEM, UNS><<<grid_of((n + SP_WARPS - 1) / SP_WARPS, 1), SP_WARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
