@@ -147,8 +147,9 @@ struct FwComp {
     int64_t ld_in, ld_out;    // their leading dimensions
     int64_t work_off;         // lane offset of the np x np work matrix
     int64_t cp_off, rp_off;   // lane offsets of the snapshot panels (FW_B x np each, t-major)
-    int64_t any_off;          // int offset of the panel flags: one per 64-line group, column
-                              // panel then row panel (np / 64 each); 0 = all lines zero
+    int64_t any_off;          // offset (64-bit words) of the panel masks: per 64-line group,
+                              // column panel then row panel (np / 64 each, 0 = all lines
+                              // zero), then per line, column panel then row panel (np each)
     int64_t rb_index;         // round-buffer index
     int64_t occ_off;          // byte offset of the (np/64)^2 block-occupancy map (1 = nonzero)
     int32_t triangular, status_index;
@@ -254,20 +255,27 @@ fw_convert_kernel(const T *__restrict__ in_base, U *__restrict__ work_base,
 // kernel B: phase 3 over BM x BN tiles, register micro-tiles TM x TN, 256 threads
 // ------------------------------------------------------------------------------------------
 template <typename U, int BN> struct TileSmem {
-    U CPt[FW_B][FW_P];       // CPt[t][i] = d_{t-1}(i, t)
-    U RPm[FW_B][BN];         // 2^msb(d_{t-1}(t, j)) (0 for zero)
-    U RPl[FW_B][BN];         // d_{t-1}(t, j) - 2^msb   (inf for zero)
-    unsigned long long maskC[FW_P];   // bit t: CPt[t][i] valid
+    U CPt[FW_B][FW_P];       // CPt[q][i] = d_{t-1}(i, t) for the q-th active step t
+    U RPm[FW_B][BN];         // 2^msb(d_{t-1}(t, j)) (0 for zero), q-th active step
+    U RPl[FW_B][BN];         // d_{t-1}(t, j) - 2^msb   (inf for zero), q-th active step
+    unsigned long long maskC[FW_P];   // bit t: CP(i, t) valid
     unsigned long long maskR[BN];     // bit t: RP(t, j) valid
-    int msbR[FW_B];                   // max msb over valid RP(t, .) in this tile
-    int active[FW_B];
-    int nactive;
+    int active[FW_B];                 // active[q] = t
+    int qof[FW_B];                    // qof[t] = q (or -1)
     unsigned long long colAny, rowAny;
 };
 
+// Line masks and group masks of the panels (written by the panel kernel of this round):
+//   gm[0 .. nb)          column panel, per 64-row group: OR of its rows' masks (0 = no snapshots)
+//   gm[nb .. 2 nb)       row panel, per 64-column group
+//   gm[2 nb .. 2 nb + np)        column panel, per row i: bit t = CP(i, t) valid
+//   gm[2 nb + np .. 2 nb + 2 np) row panel, per column j: bit t = RP(t, j) valid
+// A line mask is meaningful only when its group mask is nonzero (groups with no nonzero line
+// skip the panel pass and leave their line masks and snapshots from an earlier round).
 template <typename U, int BN, int TM, int TN>
 __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t local, U *__restrict__ work_base,
-                                          const int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+                                          const unsigned long long *__restrict__ mask_base,
+                                          unsigned char *__restrict__ occ_base,
                                           const FwComp *__restrict__ comps, int64_t K0, int lbits,
                                           DevStatus *st_base) {
     typedef lane<U> L;
@@ -275,107 +283,102 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
     constexpr int TX = BN / TN;           // threads along columns
     constexpr int TY = BM / TM;           // threads along rows
     static_assert(TX * TY == FW_THREADS, "micro-tile layout must use 256 threads");
+    static_assert(BM % 32 == 0 && BN % 32 == 0, "mask reduction works on whole warps");
     constexpr int HN = TN / 2;            // each thread owns two column groups of HN
+    constexpr int PER = 16 / sizeof(U);
     const FwComp cmp = comps[ci];
     const int64_t np = cmp.np;
     U *work = work_base + cmp.work_off;
     const U *cpbuf = work_base + cmp.cp_off;
     const U *rpbuf = work_base + cmp.rp_off;
-    const int *anyCP = any_base + cmp.any_off;       // per 64-row group of the column panel
-    const int *anyRP = anyCP + np / FW_B;            // per 64-column group of the row panel
-    unsigned char *occ = occ_base + cmp.occ_off;
     const int nb = (int)(np / FW_B);
+    const unsigned long long *gmC = mask_base + cmp.any_off;
+    const unsigned long long *gmR = gmC + nb;
+    const unsigned long long *lmC = gmC + 2 * nb;
+    const unsigned long long *lmR = lmC + np;
+    unsigned char *occ = occ_base + cmp.occ_off;
     DevStatus *st = st_base + cmp.status_index;
     const int tJn = (int)(np / BN);
     const int tI = (int)(local / tJn), tJ = (int)(local % tJn);
-    constexpr int GC = BN / FW_B;                    // 64-column groups in this tile
-    const bool cg0 = anyCP[2 * tI] != 0, cg1 = anyCP[2 * tI + 1] != 0;
-    bool rg[GC];
-    bool anyr = false;
-#pragma unroll
-    for (int gq = 0; gq < GC; ++gq) { rg[gq] = anyRP[tJ * GC + gq] != 0; anyr |= rg[gq]; }
-    if (!(cg0 || cg1) || !anyr) return;   // an all-zero panel group wrote no snapshots
     const int64_t I0 = (int64_t)tI * BM, J0 = (int64_t)tJ * BN;
-    const int tid = threadIdx.x;
-    if (tid == 0) { S.colAny = 0; S.rowAny = 0; S.nactive = 0; }
+    const int tid = threadIdx.x, lane_id = tid & 31;
+    if (tid == 0) { S.colAny = 0; S.rowAny = 0; }
     __syncthreads();
 
-    // ---- stage the panel snapshots: batched 16-byte loads, then shared-memory stores
-    {
-        constexpr int PER = 16 / sizeof(U);
-        constexpr int NC = FW_B * BM / PER / FW_THREADS;      // column-panel vectors per thread
-        constexpr int NR = FW_B * BN / PER / FW_THREADS;      // row-panel vectors per thread
-        uint4 vc[NC], vr[NR];
-        const uint4 zero4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-#pragma unroll
-        for (int i = 0; i < NC; ++i) {
-            const int e = tid + i * FW_THREADS, t = e / (BM / PER), r = (e % (BM / PER)) * PER;
-            const bool live = (r < FW_B) ? cg0 : cg1;
-            vc[i] = live ? *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r) : zero4;
-        }
-#pragma unroll
-        for (int i = 0; i < NR; ++i) {
-            const int e = tid + i * FW_THREADS, t = e / (BN / PER), c = (e % (BN / PER)) * PER;
-            vr[i] = rg[c / FW_B] ? *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c) : zero4;
-        }
-#pragma unroll
-        for (int i = 0; i < NC; ++i) {
-            const int e = tid + i * FW_THREADS, t = e / (BM / PER), r = (e % (BM / PER)) * PER;
-            const U *w = reinterpret_cast<const U *>(&vc[i]);
-#pragma unroll
-            for (int k = 0; k < PER; ++k) S.CPt[t][r + k] = L::valid(w[k]) ? w[k] : L::inf;
-        }
-#pragma unroll
-        for (int i = 0; i < NR; ++i) {
-            const int e = tid + i * FW_THREADS, t = e / (BN / PER), c = (e % (BN / PER)) * PER;
-            const U *w = reinterpret_cast<const U *>(&vr[i]);
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                U m, low;
-                L::split(w[k], m, low);
-                S.RPm[t][c + k] = m;
-                S.RPl[t][c + k] = low;
-            }
-        }
-    }
-    __syncthreads();
-    for (int r = tid; r < BM; r += FW_THREADS) {
+    // ---- line masks of this tile's rows and columns; their ORs give the active steps
+    for (int e = tid; e < BM + BN; e += FW_THREADS) {
         unsigned long long m = 0;
-        for (int t = 0; t < FW_B; ++t) m |= (unsigned long long)L::valid(S.CPt[t][r]) << t;
-        S.maskC[r] = m;
-        if (m) atomicOr(&S.colAny, m);
-    }
-    for (int c = tid; c < BN; c += FW_THREADS) {
-        unsigned long long m = 0;
-        for (int t = 0; t < FW_B; ++t) m |= (unsigned long long)(S.RPm[t][c] != 0) << t;
-        S.maskR[c] = m;
-        if (m) atomicOr(&S.rowAny, m);
-    }
-    for (int t = tid; t < FW_B; t += FW_THREADS) {
-        int mr = -1000;
-        for (int c = 0; c < BN; ++c) {
-            U m = S.RPm[t][c];
-            if (m) mr = max(mr, msb_nz<U>(m));
+        if (e < BM) {
+            const int64_t i = I0 + e;
+            if (gmC[i / FW_B]) m = lmC[i];
+            S.maskC[e] = m;
+        } else {
+            const int64_t j = J0 + (e - BM);
+            if (gmR[j / FW_B]) m = lmR[j];
+            S.maskR[e - BM] = m;
         }
-        S.msbR[t] = mr;
+        const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)m);
+        const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(m >> 32));
+        if (lane_id == 0 && (lo | hi))
+            atomicOr(e < BM ? &S.colAny : &S.rowAny, ((unsigned long long)hi << 32) | lo);
     }
     __syncthreads();
     const unsigned long long act = S.colAny & S.rowAny;
     if (act == 0) return;   // uniform across the block
-    if (tid == 0) {
-        int na = 0;
-        unsigned long long a = act;
-        while (a) { int t = __ffsll((long long)a) - 1; S.active[na++] = t; a &= a - 1; }
-        S.nactive = na;
-    }
-    // risk: some computed product x (x) y with msb(x) + msb(y) >= lbits - 1
-    bool risk = false;
-    for (int e = tid; e < FW_B * BM; e += FW_THREADS) {
-        int t = e / BM, r = e % BM;
-        U x = S.CPt[t][r];
-        if (L::valid(x) && S.msbR[t] > -1 && msb_nz<U>(x) + S.msbR[t] >= lbits - 1) risk = true;
+    const int na = __popcll(act);
+    if (tid < FW_B) {
+        const bool on = (act >> tid) & 1ull;
+        const int q = __popcll(act & ((1ull << tid) - 1ull));
+        if (on) S.active[q] = tid;
+        S.qof[tid] = on ? q : -1;
     }
     __syncthreads();
+
+    // ---- stage the active steps' panel snapshots (dead 64-line groups read as zero)
+    {
+        const uint4 inf4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        const bool cg0 = gmC[I0 / FW_B] != 0, cg1 = gmC[I0 / FW_B + 1] != 0;
+        constexpr int VC = BM / PER, VR = BN / PER;      // vectors per staged row
+        for (int e = tid; e < na * VC; e += FW_THREADS) {
+            const int q = e / VC, r = (e % VC) * PER, t = S.active[q];
+            const bool live = (r < FW_B) ? cg0 : cg1;
+            const uint4 v = live ? *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r) : inf4;
+            const U *w = reinterpret_cast<const U *>(&v);
+#pragma unroll
+            for (int k = 0; k < PER; ++k) S.CPt[q][r + k] = L::valid(w[k]) ? w[k] : L::inf;
+        }
+        for (int e = tid; e < na * VR; e += FW_THREADS) {
+            const int q = e / VR, c = (e % VR) * PER, t = S.active[q];
+            const bool live = gmR[(J0 + c) / FW_B] != 0;
+            const uint4 v = live ? *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c) : inf4;
+            const U *w = reinterpret_cast<const U *>(&v);
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                U m, low;
+                L::split(w[k], m, low);
+                S.RPm[q][c + k] = m;
+                S.RPl[q][c + k] = low;
+            }
+        }
+    }
+    __syncthreads();
+    // risk: some computed product x (x) y with msb(x) + msb(y) >= lbits - 1, i.e. for some
+    // active step the largest column-panel MSB plus the largest row-panel MSB reaches it
+    bool risk = false;
+    for (int q = tid >> 5; q < na; q += FW_THREADS / 32) {
+        int mc = -1000, mr = -1000;
+        for (int r = lane_id; r < BM; r += 32) {
+            const U x = S.CPt[q][r];
+            if (L::valid(x)) mc = max(mc, msb_nz<U>(x));
+        }
+        for (int c = lane_id; c < BN; c += 32) {
+            const U m = S.RPm[q][c];
+            if (m) mr = max(mr, msb_nz<U>(m));
+        }
+        mc = __reduce_max_sync(0xffffffffu, mc);
+        mr = __reduce_max_sync(0xffffffffu, mr);
+        if (mc >= 0 && mr >= 0 && mc + mr >= lbits - 1) risk = true;
+    }
 
     // ---- accumulators
     const int ty = tid / TX, tx = tid % TX;
@@ -406,28 +409,26 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         }
     }
 
-    const int na = S.nactive;
     unsigned steps_done = 0;
     for (int q = 0; q < na; ++q) {
-        const int t = S.active[q];
         U x[TM], m[TN], l[TN];
         bool anyx = false;
 #pragma unroll
         for (int r = 0; r < TM; ++r) {
-            x[r] = S.CPt[t][r0 + r];
+            x[r] = S.CPt[q][r0 + r];
             anyx |= L::valid(x[r]);
         }
-        // the warp's 16 rows all zero at step t: every product is zero
+        // the warp's rows all zero at this step: every product is zero
         if (!__any_sync(0xffffffffu, anyx)) continue;
         ++steps_done;
 #pragma unroll
-        for (int c = 0; c < TN; ++c) { m[c] = S.RPm[t][cidx[c]]; l[c] = S.RPl[t][cidx[c]]; }
+        for (int c = 0; c < TN; ++c) { m[c] = S.RPm[q][cidx[c]]; l[c] = S.RPl[q][cidx[c]]; }
 #pragma unroll
         for (int r = 0; r < TM; ++r)
 #pragma unroll
             for (int c = 0; c < TN; ++c) acc[r][c] = umin(acc[r][c], x[r] * m[c] + l[c]);
     }
-    if ((tid & 31) == 0 && steps_done)
+    if (lane_id == 0 && steps_done)
         atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * TM * TN);
 
     // ---- write back, cycle test on the global diagonal, first values for the running max
@@ -440,8 +441,8 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         if (!((rowWork >> r) & 1u)) continue;
         const int64_t gi = I0 + r0 + r;
         U *row = work + gi * np + J0;
-#pragma unroll
         bool anyw = false;
+#pragma unroll
         for (int half = 0; half < 2; ++half) {
             uint4 v4;
             U *w = reinterpret_cast<U *>(&v4);
@@ -455,9 +456,9 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
                     if (valid) flags |= RBG_EV_CYCLE;
                     v = L::inf;   // the diagonal stays encoded zero
                 } else if (valid && ((wasInf >> (r * TN + c)) & 1ull)) {
-                    unsigned long long both = S.maskC[r0 + r] & S.maskR[cidx[c]];
-                    int kf = __ffsll((long long)both) - 1;
-                    U first = S.CPt[kf][r0 + r] * S.RPm[kf][cidx[c]] + S.RPl[kf][cidx[c]];
+                    const unsigned long long both = S.maskC[r0 + r] & S.maskR[cidx[c]];
+                    const int qf = S.qof[__ffsll((long long)both) - 1];
+                    const U first = S.CPt[qf][r0 + r] * S.RPm[qf][cidx[c]] + S.RPl[qf][cidx[c]];
                     if ((unsigned long long)first > mx) mx = (unsigned long long)first;
                 }
                 w[k] = L::valid(v) ? v : L::inf;
@@ -471,12 +472,13 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
     flush_status(st, mx, flags);
 }
 
-// Tile worklist: candidate tile (I, J) of this round is an item when a 64-row group of its
-// column panel and a 64-column group of its row panel hold a nonzero snapshot.
+// Tile worklist: candidate tile (I, J) of this round is an item when some step t has a nonzero
+// column-panel snapshot in one of its rows and a nonzero row-panel snapshot in one of its
+// columns (the OR of the 64-line group masks of both sides intersect).
 template <int BN>
 __global__ void fw_tile_list_kernel(const FwComp *__restrict__ comps, const int64_t *__restrict__ prefix,
-                                    int count, const int *__restrict__ any_base, int2 *__restrict__ list,
-                                    int *__restrict__ counters) {
+                                    int count, const unsigned long long *__restrict__ mask_base,
+                                    int2 *__restrict__ list, int *__restrict__ counters) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= prefix[count]) return;
     const int ci = fw_find(prefix, count, c);
@@ -484,20 +486,22 @@ __global__ void fw_tile_list_kernel(const FwComp *__restrict__ comps, const int6
     const int64_t local = c - prefix[ci];
     const int tJn = (int)(cmp.np / BN);
     const int tI = (int)(local / tJn), tJ = (int)(local % tJn);
-    const int *anyCP = any_base + cmp.any_off;
-    const int *anyRP = anyCP + cmp.np / FW_B;
+    const int nb = (int)(cmp.np / FW_B);
+    const unsigned long long *gmC = mask_base + cmp.any_off;
+    const unsigned long long *gmR = gmC + nb;
     constexpr int GC = BN / FW_B;
-    bool r = false;
+    unsigned long long r = 0;
 #pragma unroll
-    for (int gq = 0; gq < GC; ++gq) r |= anyRP[tJ * GC + gq] != 0;
-    if (!r || !(anyCP[2 * tI] | anyCP[2 * tI + 1])) return;
+    for (int gq = 0; gq < GC; ++gq) r |= gmR[tJ * GC + gq];
+    if ((r & (gmC[2 * tI] | gmC[2 * tI + 1])) == 0) return;
     const int slot = atomicAdd(&counters[CNT_TILE], 1);
     list[slot] = make_int2(ci, (int)local);
 }
 
 template <typename U, int BN, int TM, int TN>
 __global__ void __launch_bounds__(FW_THREADS, 2)
-fw_tile_kernel(U *__restrict__ work_base, const int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+fw_tile_kernel(U *__restrict__ work_base, const unsigned long long *__restrict__ any_base,
+               unsigned char *__restrict__ occ_base,
                const FwComp *__restrict__ comps, const int2 *__restrict__ list, int *__restrict__ counters,
                int64_t K0, int lbits, DevStatus *st_base) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -747,7 +751,7 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
         c.cp_off = lanes; lanes += (int64_t)FW_B * c.np;
         c.rp_off = lanes; lanes += (int64_t)FW_B * c.np;
         lanes = (int64_t)align_up((size_t)lanes, 64);
-        c.any_off = anys; anys += 2 * (c.np / FW_B);
+        c.any_off = anys; anys += 2 * (c.np / FW_B) + 2 * c.np;
         c.rb_index = k;
         c.occ_off = occs; occs += (c.np / FW_B) * (c.np / FW_B);
         c.triangular = triangular;
@@ -772,7 +776,7 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
     P.off_ppanel = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
     P.off_ptile = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
     P.off_rb = o; o = align_up(o + (size_t)count * (lane == 8 ? sizeof(RoundBuf<uint64_t>) : sizeof(RoundBuf<uint32_t>)), 256);
-    P.off_any = o; o = align_up(o + (size_t)anys * 4, 256);
+    P.off_any = o; o = align_up(o + (size_t)anys * 8, 256);
     P.off_occ = o; P.occ_bytes = (size_t)occs; o = align_up(o + (size_t)occs, 256);
     const int a0 = rounds > 0 ? P.active[0] : 0;
     P.off_plist = o; o = align_up(o + (size_t)std::max<int64_t>(P.pre_panel[(size_t)a0], 1) * 8, 256);
@@ -831,7 +835,7 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     const int64_t *ppanel = reinterpret_cast<const int64_t *>(ws + P.off_ppanel);
     const int64_t *ptile = reinterpret_cast<const int64_t *>(ws + P.off_ptile);
     RoundBuf<U> *rbs = reinterpret_cast<RoundBuf<U> *>(ws + P.off_rb);
-    int *any = reinterpret_cast<int *>(ws + P.off_any);
+    unsigned long long *any = reinterpret_cast<unsigned long long *>(ws + P.off_any);
     U *lanes = reinterpret_cast<U *>(ws + P.off_lanes);
     const int sbits = (int)sizeof(T) * 8;
     const int lbits = std::min<int>(sbits, (int)sizeof(U) * 8);

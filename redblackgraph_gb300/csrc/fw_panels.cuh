@@ -64,7 +64,7 @@ template <typename U> struct DiagSmem {
 // of the threads with h = t / 16.  One barrier per step: step t's writes go to slot t only.
 template <typename U>
 __global__ void __launch_bounds__(DG_THREADS)
-fw_diag_kernel(U *__restrict__ work_base, int *__restrict__ any_base, RoundBuf<U> *__restrict__ rbs,
+fw_diag_kernel(U *__restrict__ work_base, unsigned long long *__restrict__ any_base, RoundBuf<U> *__restrict__ rbs,
                const FwComp *__restrict__ comps, int *__restrict__ counters, int64_t K0, int lbits,
                DevStatus *st_base) {
     typedef lane<U> L;
@@ -176,7 +176,7 @@ template <typename U> struct PanelSmem {
     int msbCS[FW_B];
     int msbRS[FW_B];
     U Z[FW_B][PN_LINES];              // Z[t][line]: the line's step-t operand (its snapshot)
-    int any;
+    unsigned long long any;           // OR of the item's line masks
 };
 
 template <typename U> __device__ __forceinline__ U shfl_lane(U v, int src) {
@@ -191,7 +191,8 @@ template <typename U> __device__ __forceinline__ U shfl_lane(U v, int src) {
 // or column panel.
 template <typename U>
 __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U *__restrict__ work_base,
-                                           int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+                                           unsigned long long *__restrict__ any_base,
+                                           unsigned char *__restrict__ occ_base,
                                            const RoundBuf<U> *__restrict__ rbs,
                                            const FwComp *__restrict__ comps, int64_t K0, int lbits,
                                            DevStatus *st_base) {
@@ -203,8 +204,10 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     U *work = work_base + cmp.work_off;
     U *cpbuf = work_base + cmp.cp_off;
     U *rpbuf = work_base + cmp.rp_off;
-    int *anyCP = any_base + cmp.any_off;             // per 64-line group
-    int *anyRP = anyCP + np / FW_B;
+    unsigned long long *anyCP = any_base + cmp.any_off;   // group masks, per 64-line group
+    unsigned long long *anyRP = anyCP + np / FW_B;
+    unsigned long long *lineCP = anyRP + np / FW_B;        // line masks (bit t: snapshot valid)
+    unsigned long long *lineRP = lineCP + np;
     unsigned char *occ = occ_base + cmp.occ_off;     // (np/64)^2 block occupancy
     const int nb = (int)(np / FW_B);
     const RoundBuf<U> *rb = rbs + cmp.rb_index;
@@ -345,7 +348,8 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     }
     if ((tid & 31) == 0 && steps_done)
         atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * DG_ROWS);
-    if (seen) atomicOr(&S.any, 1);
+    if (h == 0) (rowPanel ? lineRP : lineCP)[g] = seen;
+    if (seen && h == 0) atomicOr(&S.any, seen);
     __syncthreads();
     if (tid == 0) (rowPanel ? anyRP : anyCP)[cta] = S.any;
     if (wrote) {
@@ -383,7 +387,8 @@ __global__ void fw_panel_list_kernel(const FwComp *__restrict__ comps, const int
 // Persistent panel kernel: CTAs pull items from the worklist until it is exhausted.
 template <typename U>
 __global__ void __launch_bounds__(PN_THREADS, 2)
-fw_panel_kernel(U *__restrict__ work_base, int *__restrict__ any_base, unsigned char *__restrict__ occ_base,
+fw_panel_kernel(U *__restrict__ work_base, unsigned long long *__restrict__ any_base,
+                unsigned char *__restrict__ occ_base,
                 const RoundBuf<U> *__restrict__ rbs, const FwComp *__restrict__ comps,
                 const int2 *__restrict__ list, int *__restrict__ counters, int64_t K0, int lbits,
                 DevStatus *st_base) {

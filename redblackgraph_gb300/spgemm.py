@@ -68,10 +68,13 @@ class DeviceCSR:
 
 
 def spgemm(A: DeviceCSR, B: DeviceCSR, R: DeviceCSR | None = None, upper: bool = False,
-           sem: int = SEM_C64, out_dtype=None, stream=None) -> tuple[DeviceCSR, int, int]:
+           sem: int = SEM_C64, out_dtype=None, stream=None, stats: dict | None = None
+           ) -> tuple[DeviceCSR, int, int]:
     """C = A (x) B (or the squaring step R (+) R^2 when R is given).
 
     Returns ``(C, status, flags)``; status is RBG_OK or RBG_ERR_OVERFLOW (C core semantics).
+    ``stats``, when given, receives the number of products (A entry x B row entry) and of rows
+    taking the dense accumulator.
     """
     if A.shape[1] != B.shape[0]:
         raise ValueError(f"Incompatible shapes: A is {A.shape}, B is {B.shape}.")
@@ -91,6 +94,9 @@ def spgemm(A: DeviceCSR, B: DeviceCSR, R: DeviceCSR | None = None, upper: bool =
                                   ctypes.byref(cr) if cr is not None else None, int(upper),
                                   head.data_ptr(), head.numel(), ctypes.byref(tot),
                                   ctypes.byref(dense), sh), "spgemm_count")
+    if stats is not None:
+        stats["products"] = tot.value - (R.nnz if R is not None else 0)
+        stats["dense_rows"] = dense.value
     tb = ctypes.c_int64(0)
     _lib.check(L.rbg_spgemm_tail_bytes(n, nc, tot.value, dense.value, ctypes.byref(tb)), "spgemm")
     tail = torch.empty(max(tb.value, 256), dtype=torch.uint8, device=dev)
