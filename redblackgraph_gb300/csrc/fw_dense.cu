@@ -271,7 +271,8 @@ template <typename U, int BN> struct TileSmem {
 //   gm[2 nb .. 2 nb + np)        column panel, per row i: bit t = CP(i, t) valid
 //   gm[2 nb + np .. 2 nb + 2 np) row panel, per column j: bit t = RP(t, j) valid
 // A line mask is meaningful only when its group mask is nonzero (groups with no nonzero line
-// skip the panel pass and leave their line masks and snapshots from an earlier round).
+// skip the panel pass and leave their line masks and snapshots from an earlier round), and a
+// group's snapshot row t is written only when bit t of its group mask is set.
 template <typename U, int BN, int TM, int TN>
 __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t local, U *__restrict__ work_base,
                                           const unsigned long long *__restrict__ mask_base,
@@ -337,11 +338,11 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
     // ---- stage the active steps' panel snapshots (dead 64-line groups read as zero)
     {
         const uint4 inf4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-        const bool cg0 = gmC[I0 / FW_B] != 0, cg1 = gmC[I0 / FW_B + 1] != 0;
+        const unsigned long long cg0 = gmC[I0 / FW_B], cg1 = gmC[I0 / FW_B + 1];
         constexpr int VC = BM / PER, VR = BN / PER;      // vectors per staged row
         for (int e = tid; e < na * VC; e += FW_THREADS) {
             const int q = e / VC, r = (e % VC) * PER, t = S.active[q];
-            const bool live = (r < FW_B) ? cg0 : cg1;
+            const bool live = (((r < FW_B) ? cg0 : cg1) >> t) & 1ull;
             const uint4 v = live ? *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r) : inf4;
             const U *w = reinterpret_cast<const U *>(&v);
 #pragma unroll
@@ -349,7 +350,7 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         }
         for (int e = tid; e < na * VR; e += FW_THREADS) {
             const int q = e / VR, c = (e % VR) * PER, t = S.active[q];
-            const bool live = gmR[(J0 + c) / FW_B] != 0;
+            const bool live = (gmR[(J0 + c) / FW_B] >> t) & 1ull;
             const uint4 v = live ? *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c) : inf4;
             const U *w = reinterpret_cast<const U *>(&v);
 #pragma unroll

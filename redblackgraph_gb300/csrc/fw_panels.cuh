@@ -277,48 +277,67 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     const int pc0 = Pad<U>::at(c0);
     const U *tabA = rowPanel ? &S.CS[0][pc0] : &S.RSm[0][pc0];
     const U *tabB = &S.RSl[0][pc0];
-    for (int T = 0; T < FW_B / DG_ROWS; ++T) {
-        // operands of step t are loaded one step ahead (registers double-buffered)
-        U xa[2][DG_ROWS], xb[2][DG_ROWS];
-        load16<U>(tabA + (T * DG_ROWS) * Pad<U>::LD, xa[0]);
-        if (!rowPanel) load16<U>(tabB + (T * DG_ROWS) * Pad<U>::LD, xb[0]);
+    bool changed = false;                             // some cell of this thread decreased
+    if (__all_sync(0xffffffffu, startInf == (1u << DG_ROWS) - 1u)) {
+        // the warp's 8 lines are all zero: they stay zero (a line only meets its own cells as
+        // step operands), so only their snapshots are written, as zeros
 #pragma unroll
-        for (int l = 0; l < DG_ROWS; ++l) {
-            const int t = T * DG_ROWS + l;
-            const int cur = l & 1, nxt = cur ^ 1;
-            if (l + 1 < DG_ROWS) {
-                load16<U>(tabA + (t + 1) * Pad<U>::LD, xa[nxt]);
-                if (!rowPanel) load16<U>(tabB + (t + 1) * Pad<U>::LD, xb[nxt]);
-            }
-            const U z = shfl_lane<U>(R[l], grp | T);  // P(t, j) or P(i, t): invariant at step t
-            const bool zv = L::valid(z);
-            seen |= (unsigned long long)zv << t;
-            if (h == 0) S.Z[t][tid >> 2] = z;
-            // a zero step operand makes every product of the step a zero: skip the step when
-            // it is zero for the whole warp (closures of family trees are sparse)
-            if (!__any_sync(0xffffffffu, zv)) continue;
-            ++steps_done;
-            if (rowPanel) {
-                U m, low;
-                L::split(z, m, low);
-                if (zv && S.msbCS[t] + msb_nz<U>(z) >= lbits - 1) risk = true;
+        for (int l = 0; l < DG_ROWS; ++l) S.Z[h * DG_ROWS + l][tid >> 2] = L::inf;
+    } else {
+        for (int T = 0; T < FW_B / DG_ROWS; ++T) {
 #pragma unroll
-                for (int r = 0; r < DG_ROWS; ++r) R[r] = umin(R[r], xa[cur][r] * m + low);
-            } else {
-                if (zv && msb_nz<U>(z) + S.msbRS[t] >= lbits - 1) risk = true;
+            for (int l = 0; l < DG_ROWS; ++l) {
+                const int t = T * DG_ROWS + l;
+                const U z = shfl_lane<U>(R[l], grp | T);  // P(t, j) or P(i, t): invariant at step t
+                const bool zv = L::valid(z);
+                seen |= (unsigned long long)zv << t;
+                if (h == 0) S.Z[t][tid >> 2] = z;
+                // a zero step operand makes every product of the step a zero: skip the step when
+                // it is zero for the whole warp (closures of family trees are sparse); operands
+                // are read only for the steps that run
+                if (!__any_sync(0xffffffffu, zv)) continue;
+                ++steps_done;
+                U xa[DG_ROWS];
+                load16<U>(tabA + t * Pad<U>::LD, xa);
+                if (rowPanel) {
+                    U m, low;
+                    L::split(z, m, low);
+                    if (zv && S.msbCS[t] + msb_nz<U>(z) >= lbits - 1) risk = true;
 #pragma unroll
-                for (int r = 0; r < DG_ROWS; ++r) R[r] = umin(R[r], z * xa[cur][r] + xb[cur][r]);
+                    for (int r = 0; r < DG_ROWS; ++r) {
+                        const U v = umin(R[r], xa[r] * m + low);
+                        changed |= v != R[r];
+                        R[r] = v;
+                    }
+                } else {
+                    U xb[DG_ROWS];
+                    load16<U>(tabB + t * Pad<U>::LD, xb);
+                    if (zv && msb_nz<U>(z) + S.msbRS[t] >= lbits - 1) risk = true;
+#pragma unroll
+                    for (int r = 0; r < DG_ROWS; ++r) {
+                        const U v = umin(R[r], z * xa[r] + xb[r]);
+                        changed |= v != R[r];
+                        R[r] = v;
+                    }
+                }
             }
         }
     }
-    __syncthreads();   // the snapshots (written by lane h == 0 of each group) are visible below
+    if (seen && h == 0) atomicOr(&S.any, seen);
+    __syncthreads();   // the snapshots (written by lane h == 0 of each group) and S.any are visible
+    const unsigned long long anyMask = S.any;
     {
-        U *dst = rowPanel ? rpbuf : cpbuf;            // t-major, coalesced over the CTA's lines
+        // t-major, coalesced over the CTA's lines; only the steps some line of this group has
+        // valid are written (the tile kernel reads a snapshot row only under its mask bit)
+        U *dst = rowPanel ? rpbuf : cpbuf;
         const int64_t base = (int64_t)cta * PN_LINES;
-        for (int e = tid; e < FW_B * PN_LINES; e += PN_THREADS)
-            dst[(int64_t)(e / PN_LINES) * np + base + e % PN_LINES] = S.Z[e / PN_LINES][e % PN_LINES];
+        for (int e = tid; e < FW_B * PN_LINES; e += PN_THREADS) {
+            const int t = e / PN_LINES;
+            if ((anyMask >> t) & 1ull) dst[(int64_t)t * np + base + e % PN_LINES] = S.Z[t][e % PN_LINES];
+        }
     }
-    // write back; the running maximum needs each newly valid cell's first valid product
+    // write back the cells that changed; the running maximum needs each newly valid cell's
+    // first valid product
     SU smx = 0;
     bool wrote = false;
 #pragma unroll
@@ -326,7 +345,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
         const U v = R[r];
         const bool vv = L::valid(v);
         const int c = c0 + r;
-        if (!inK) {
+        if (!inK && changed) {
             if (rowPanel) work[(K0 + c) * np + g] = vv ? v : L::inf;
             else rowp[r] = vv ? v : L::inf;
             wrote |= vv;
@@ -349,9 +368,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     if ((tid & 31) == 0 && steps_done)
         atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * DG_ROWS);
     if (h == 0) (rowPanel ? lineRP : lineCP)[g] = seen;
-    if (seen && h == 0) atomicOr(&S.any, seen);
-    __syncthreads();
-    if (tid == 0) (rowPanel ? anyRP : anyCP)[cta] = S.any;
+    if (tid == 0) (rowPanel ? anyRP : anyCP)[cta] = anyMask;
     if (wrote) {
         const int kb = (int)(K0 / FW_B);
         occ[rowPanel ? (int64_t)kb * nb + cta : (int64_t)cta * nb + kb] = 1;
