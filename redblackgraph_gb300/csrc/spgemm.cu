@@ -10,13 +10,15 @@
 //                    redblackgraph/gpu/transitive_closure.py:77-156 (R (+) R^2 taken per cell as
 //                    the value of smallest magnitude, R's value on a tie, zeros dropped)
 //
-// Design: one pass per output row, no global sort and no global hash.  The candidates of row i
-// (every product A[i,k] (x) B[k,j], plus R[i,.] for a squaring step) are gathered into shared
-// memory, sorted by column, and reduced: the (+) of the products of a column, then, for a
-// squaring step, the magnitude merge with R's entry.  Rows with at most 1024 candidates run
-// one per warp, up to 8192 one per block; longer rows use a dense per-block accumulator in the
-// workspace.  The output of every row is written compacted (columns ascending) at the row's
-// candidate offset; a scan of the row counts and a gather produce the final CSR.
+// Design: one pass per output row, no global sort and no global hash.  A warp takes a row,
+// walks its candidates (every product A[i,k] (x) B[k,j], plus R[i,.] for a squaring step) in
+// place and folds them into a shared-memory table keyed by column; the distinct columns are
+// sorted and reduced: the (+) of the products of a column, then, for a squaring step, the
+// magnitude merge with R's entry.  Rows with more distinct columns than the warp table holds
+// are redone one per block with a sort of their candidates; rows of more than 8192 candidates
+// use a dense per-block accumulator in the workspace.  The output of every row is written
+// compacted (columns ascending) at the row's candidate offset; a scan of the row counts and a
+// gather produce the final CSR.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 #include <string.h>
@@ -26,8 +28,6 @@
 
 namespace rbg {
 
-constexpr int SP_WARP_CAP = 1024;     // candidates per warp row
-constexpr int SP_WARPS = 4;           // warps per CTA in the warp kernel
 constexpr int SP_BLOCK_CAP = 8192;    // candidates per block row
 constexpr int SP_BLOCK_THREADS = 512;
 constexpr int SP_DENSE_BLOCKS = 8;    // concurrent dense-accumulator rows (one scratch slot each)
@@ -103,8 +103,10 @@ __global__ void sp_count_kernel(SpArgs a, int64_t *cand) {
         }
         if (a.rp) c += a.rp[i + 1] - a.rp[i];
         cand[i] = c;
-        if (c > SP_WARP_CAP) a.big_rows[atomicAdd(a.big_count, 1)] = (int)i;
-        if (c > SP_BLOCK_CAP) atomicAdd(a.big_count + 1, 1);
+        if (c > SP_BLOCK_CAP) {      // the dense kernel's rows
+            a.big_rows[atomicAdd(a.big_count, 1)] = (int)i;
+            atomicAdd(a.big_count + 1, 1);
+        }
     }
 }
 
@@ -193,60 +195,10 @@ __device__ __forceinline__ void sp_bitonic(unsigned *keys, long long *vals, int 
     }
 }
 
-// One row per warp (at most SP_WARP_CAP candidates), rows handed out by a grid-stride loop.
-template <int SEM, bool UNS>
-__global__ void __launch_bounds__(SP_WARPS * 32)
-sp_warp_kernel(SpArgs a, int merge) {
-    extern __shared__ __align__(16) unsigned char sp_smem[];
-    long long *svals = reinterpret_cast<long long *>(sp_smem);                      // [warps][cap]
-    unsigned *skeys = reinterpret_cast<unsigned *>(svals + SP_WARPS * SP_WARP_CAP);  // [warps][cap]
-    int *scnt = reinterpret_cast<int *>(skeys + SP_WARPS * SP_WARP_CAP);             // [warps]
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned *keys = skeys + w * SP_WARP_CAP;
-    long long *vals = svals + w * SP_WARP_CAP;
-    unsigned ev = 0;
-    const int64_t warps = (int64_t)gridDim.x * SP_WARPS;
-    for (int64_t i = (int64_t)blockIdx.x * SP_WARPS + w; i < a.n_rows; i += warps) {
-        const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
-        if (c > SP_WARP_CAP) continue;               // the block / dense kernels take it
-        if (lane == 0) scnt[w] = 0;
-        __syncwarp();
-        sp_gather<SEM, UNS>(a, i, merge != 0, keys, vals, &scnt[w], lane, 32, ev);
-        __syncwarp();
-        const int cnt = scnt[w];
-        int P = 1;
-        while (P < cnt) P <<= 1;
-        for (int idx = cnt + lane; idx < P; idx += 32) keys[idx] = SP_PAD;
-        __syncwarp();
-        sp_bitonic(keys, vals, P, lane, 32, WarpSync());
-        // heads of columns in ascending order, compacted with ballots
-        int64_t out = 0;
-        const int64_t base = a.cand_off[i];
-        for (int c0 = 0; c0 < cnt; c0 += 32) {
-            const int idx = c0 + lane;
-            long long v = 0;
-            bool keep = false;
-            if (idx < cnt && (idx == 0 || (keys[idx] >> 1) != (keys[idx - 1] >> 1)))
-                keep = sp_reduce_run<SEM, UNS>(keys, vals, idx, cnt, merge != 0, a.elem_bytes, v);
-            const unsigned bal = __ballot_sync(0xffffffffu, keep);
-            if (keep) {
-                const int64_t pos = base + out + __popc(bal & ((1u << lane) - 1u));
-                a.ocol[pos] = (int)(keys[idx] >> 1);
-                a.oval[pos] = v;
-            }
-            out += __popc(bal);
-        }
-        if (lane == 0) a.rownnz[i] = out;
-        __syncwarp();
-    }
-    for (int o = 16; o > 0; o >>= 1) ev |= __shfl_xor_sync(0xffffffffu, ev, o);
-    if (lane == 0 && ev) atomicOr(a.flags, ev);
-}
-
-constexpr size_t SP_WARP_SMEM = (size_t)SP_WARPS * SP_WARP_CAP * 12 + SP_WARPS * 4;
 constexpr size_t SP_BLOCK_SMEM = (size_t)SP_BLOCK_CAP * 12 + 64;
 
-// One row per block for SP_WARP_CAP < candidates <= SP_BLOCK_CAP (rows from the big-row list).
+// One row per block for the rows the warp kernel handed over (more distinct columns than its
+// table holds) with at most SP_BLOCK_CAP candidates: gather, bitonic sort, reduce.
 template <int SEM, bool UNS>
 __global__ void __launch_bounds__(SP_BLOCK_THREADS)
 sp_block_kernel(SpArgs a, int merge) {
@@ -317,6 +269,191 @@ __device__ __forceinline__ long long sp_dec(unsigned long long k) {
 }
 template <int SEM> __device__ __forceinline__ unsigned long long sp_empty() {
     return SEM == SEM_CY32 ? (unsigned long long)LLONG_MAX : ~0ull;
+}
+
+// ----------------------------------------------------------------------------- warp rows
+// One row per warp for rows of at most SP_BLOCK_CAP candidates.  The candidates are never
+// stored: the warp walks them in place -- the lanes take 32 entries (i, k) of A at a time, a
+// warp scan of nnz(B[k]) flattens their products into one index range, and every lane finds
+// the entry of its product by a shuffle binary search -- and folds each product into a small
+// open-addressing table in shared memory keyed by column (atomicMin on the order-encoded (+)).
+// A squaring step's own entries R[i, .] go into a second value per slot.  The table holds up to
+// SP_HASH_SLOTS distinct columns; a row with more goes to the block kernel instead.  The
+// distinct columns are then sorted (a bitonic sort of at most SP_HASH_SLOTS keys) and written
+// ascending.
+constexpr int SP_HASH_SLOTS = 256;
+constexpr int SP_HWARPS = 8;          // warps per CTA
+constexpr unsigned SP_NOKEY = 0xffffffffu;
+
+struct SpHashWarp {
+    unsigned key[SP_HASH_SLOTS];
+    unsigned long long val[SP_HASH_SLOTS];   // order-encoded (+) of the products
+    long long rv[SP_HASH_SLOTS];             // R's own entry (squaring step), 0 if none
+    unsigned long long list[SP_HASH_SLOTS];  // (column << 32 | slot) of the occupied slots
+};
+constexpr size_t SP_WARP_SMEM = sizeof(SpHashWarp) * SP_HWARPS;
+
+// Slot of column j (inserted if new); -1 when the table is full.
+__device__ __forceinline__ int sp_hash_slot(SpHashWarp &H, unsigned j, int mask) {
+    int h = (int)((j * 2654435761u) >> 8) & mask;
+    for (int probe = 0; probe <= mask; ++probe) {
+        const unsigned k = H.key[h];
+        if (k == j) return h;
+        if (k == SP_NOKEY) {
+            const unsigned old = atomicCAS(&H.key[h], SP_NOKEY, j);
+            if (old == SP_NOKEY || old == j) return h;
+        }
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+template <int SEM>
+__device__ __forceinline__ void sp_hash_fold(SpHashWarp &H, int slot, long long p) {
+    if (SEM == SEM_CY32) atomicMin(reinterpret_cast<long long *>(&H.val[slot]), p);
+    else atomicMin(&H.val[slot], sp_enc<SEM>(p));
+}
+
+template <int SEM, bool UNS>
+__global__ void __launch_bounds__(SP_HWARPS * 32)
+sp_warp_kernel(SpArgs a, int merge) {
+    extern __shared__ __align__(16) unsigned char sp_smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    SpHashWarp &H = reinterpret_cast<SpHashWarp *>(sp_smem)[w];
+    unsigned ev = 0;
+    const int64_t warps = (int64_t)gridDim.x * SP_HWARPS;
+    for (int64_t i = (int64_t)blockIdx.x * SP_HWARPS + w; i < a.n_rows; i += warps) {
+        const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
+        if (c > SP_BLOCK_CAP) continue;              // the dense kernel takes it
+        int S = 32;
+        while (S < c && S < SP_HASH_SLOTS) S <<= 1;
+        const int mask = S - 1;
+        for (int s = lane; s < S; s += 32) {
+            H.key[s] = SP_NOKEY;
+            H.val[s] = sp_empty<SEM>();
+            H.rv[s] = 0;
+        }
+        __syncwarp();
+        bool full = false;
+        if (merge && a.rp) {
+            for (int64_t e = a.rp[i] + lane; e < a.rp[i + 1]; e += 32) {
+                const int slot = sp_hash_slot(H, (unsigned)a.rj[e], mask);
+                if (slot < 0) full = true;
+                else H.rv[slot] = sp_load(a.rx, e, a.elem_bytes, a.uns);
+            }
+        }
+        for (int64_t e0 = a.ap[i]; e0 < a.ap[i + 1]; e0 += 32) {
+            const int64_t e = e0 + lane;
+            const bool in = e < a.ap[i + 1];
+            long long av = 0;
+            int64_t b0 = 0;
+            int len = 0;
+            if (in) {
+                const int k = a.aj[e];
+                av = sp_load(a.ax, e, a.elem_bytes, a.uns);
+                b0 = a.bp[k];
+                len = (int)(a.bp[k + 1] - b0);
+            }
+            int incl = len;                           // warp scan of the B-row lengths
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int excl = incl - len;
+            const int T = __shfl_sync(0xffffffffu, incl, 31);
+            for (int base = 0; base < T; base += 32) {
+                const int idx = base + lane;
+                int lo = 0;                          // last entry whose range starts at or before idx
+#pragma unroll
+                for (int st = 16; st > 0; st >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, excl, lo + st);
+                    if (v <= idx) lo += st;
+                }
+                const long long aq = __shfl_sync(0xffffffffu, av, lo);
+                const int64_t bq = __shfl_sync(0xffffffffu, b0, lo);
+                const int xq = __shfl_sync(0xffffffffu, excl, lo);
+                if (idx < T) {
+                    const int64_t f = bq + (idx - xq);
+                    const int j = a.bj[f];
+                    if (!(a.upper && j < i)) {
+                        const long long p = sp_mul<SEM, UNS>(aq, sp_load(a.bx, f, a.elem_bytes, a.uns), ev);
+                        if (p != 0) {                // a zero product adds nothing
+                            if (j == i && p != -1 && p != 1) ev |= RBG_EV_CYCLE;   // a vertex reaches itself
+                            const int slot = sp_hash_slot(H, (unsigned)j, mask);
+                            if (slot < 0) full = true;
+                            else sp_hash_fold<SEM>(H, slot, p);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (__any_sync(0xffffffffu, full)) {         // too many distinct columns: the block kernel
+            if (lane == 0) a.big_rows[atomicAdd(a.big_count, 1)] = (int)i;
+            __syncwarp();
+            continue;
+        }
+        // the occupied slots, compacted, then sorted by column
+        int nd = 0;
+        for (int s0 = 0; s0 < S; s0 += 32) {
+            const int s = s0 + lane;
+            const bool occ = H.key[s] != SP_NOKEY;   // S is a multiple of 32
+            const unsigned bal = __ballot_sync(0xffffffffu, occ);
+            if (occ) H.list[nd + __popc(bal & ((1u << lane) - 1u))] = ((unsigned long long)H.key[s] << 32) | (unsigned)s;
+            nd += __popc(bal);
+        }
+        int P = 1;
+        while (P < nd) P <<= 1;
+        for (int q = nd + lane; q < P; q += 32) H.list[q] = ~0ull;
+        __syncwarp();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int q = lane; q < P; q += 32) {
+                    const int qx = q ^ jj;
+                    if (qx > q) {
+                        const unsigned long long x = H.list[q], y = H.list[qx];
+                        if ((x > y) == ((q & k) == 0)) { H.list[q] = y; H.list[qx] = x; }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // values: the (+) of the products, then for a squaring step the magnitude merge with R
+        int64_t out = 0;
+        const int64_t base = a.cand_off[i];
+        for (int q0 = 0; q0 < nd; q0 += 32) {
+            const int q = q0 + lane;
+            long long v = 0;
+            unsigned col = 0;
+            if (q < nd) {
+                const unsigned long long e = H.list[q];
+                const int s = (int)(e & 0xffffffffu);
+                col = (unsigned)(e >> 32);
+                const unsigned long long kv = H.val[s];
+                const long long sv = kv == sp_empty<SEM>() ? 0 : sp_dec<SEM>(kv);
+                const long long s_t = sv == 0 ? 0 : ((SEM == SEM_CY32) ? sv : sp_trunc(sv, a.elem_bytes, UNS));
+                if (!merge) v = s_t;
+                else {
+                    const long long r = H.rv[s];
+                    v = sv == 0 ? r : (r != 0 ? sp_minabs(r, s_t, UNS) : s_t);
+                    v = (long long)(int)v;   // the merged matrix is int32 (transitive_closure.py:327)
+                }
+            }
+            const bool keep = v != 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int64_t pos = base + out + __popc(bal & ((1u << lane) - 1u));
+                a.ocol[pos] = (int)col;
+                a.oval[pos] = v;
+            }
+            out += __popc(bal);
+        }
+        if (lane == 0) a.rownnz[i] = out;
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) ev |= __shfl_xor_sync(0xffffffffu, ev, o);
+    if (lane == 0 && ev) atomicOr(a.flags, ev);
 }
 
 // One row per block for rows beyond SP_BLOCK_CAP: a dense accumulator over all columns (one
@@ -575,7 +712,7 @@ int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s)
     if (configured) return configured;
     const int64_t n = a.n_rows;
     note_launches(2 + (dense > 0 ? 2 : 0));
-    sp_warp_kernel<SEM, UNS><<<grid_of((n + SP_WARPS - 1) / SP_WARPS, 1), SP_WARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
+    sp_warp_kernel<SEM, UNS><<<grid_of((n + SP_HWARPS - 1) / SP_HWARPS, 1), SP_HWARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
     sp_block_kernel<SEM, UNS><<<grid_of(1 << 20, 1), SP_BLOCK_THREADS, SP_BLOCK_SMEM, s>>>(a, merge);
     if (dense > 0) {
         sp_dense_init_kernel<SEM><<<grid_of((int64_t)SP_DENSE_BLOCKS * nc, 256), 256, 0, s>>>(a.dense_val,
