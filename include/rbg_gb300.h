@@ -68,6 +68,9 @@ typedef void *rbg_stream_t; /* a cudaStream_t */
 #define RBG_MODE_TRIANGULAR 2u  /* assume_upper_triangular loop (_shortest_path.pyx:365) */
 #define RBG_MODE_FORCE_EXACT 4u /* always run the sequential-order kernel                */
 #define RBG_MODE_FORCE_WIDE 8u  /* 64-bit storage: skip the 32-bit lane attempt          */
+#define RBG_MODE_GRAPH 16u      /* rbg_fw_batch: record the launch sequence as a CUDA graph
+                                   and replay it on later calls with the same sizes,
+                                   offsets, buffers and workspace (small LRU cache)      */
 
 /* which kernel path produced a result */
 #define RBG_PATH_BLOCKED32 1

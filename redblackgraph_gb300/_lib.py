@@ -34,6 +34,7 @@ MODE_CYTHON = 1
 MODE_TRIANGULAR = 2
 MODE_FORCE_EXACT = 4
 MODE_FORCE_WIDE = 8
+MODE_GRAPH = 16
 
 PATH_BLOCKED32, PATH_BLOCKED64, PATH_EXACT = 1, 2, 3
 

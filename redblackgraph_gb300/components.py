@@ -132,7 +132,7 @@ def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: 
     comps = label_components(indptr, indices, n, stream)
     blocks = densify(indptr, indices, data, comps, stream)
     _, results = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat,
-                          mode=_lib.MODE_CYTHON, stream=stream)
+                          mode=_lib.MODE_CYTHON | _lib.MODE_GRAPH, stream=stream)
     for r in results:
         raise_for_cython(r)
     fw = component_methods(comps.sizes, comps.count, method, densify_threshold)

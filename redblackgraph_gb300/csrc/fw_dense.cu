@@ -63,7 +63,10 @@ __global__ void status_init_kernel(DevStatus *st, int count) {
 }
 
 static std::atomic<long long> g_launches(0);
-void note_launches(int64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+static thread_local int t_recording = 0;   // launches recorded into a graph are counted when it runs
+void note_launches(int64_t k) {
+    if (!t_recording) g_launches.fetch_add(k, std::memory_order_relaxed);
+}
 
 // Opt-in per-kernel timing: CUDA events recorded on the launching stream around each launch of
 // the blocked kernels (0 = tile, 1 = panel, 2 = diagonal, 3 = convert + finalize).
@@ -1041,6 +1044,96 @@ static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_
 // Batch: every component in one blocked run with 32-bit lanes; components that need another
 // path (64-bit lanes, exact order) are then closed one by one with the single-matrix path,
 // reusing the workspace.
+// ------------------------------------------------------------------------------------------
+// CUDA-graph replay of a batch's launch sequence (RBG_MODE_GRAPH)
+// ------------------------------------------------------------------------------------------
+// The blocked pass of a batch is a fixed sequence of ~5 launches per round whose grids depend
+// only on the plan.  With RBG_MODE_GRAPH the sequence is captured once into a CUDA graph,
+// keyed by everything it bakes in (types, sizes, offsets, buffers, workspace), and replayed by
+// later calls with the same key.  A small LRU cache holds the instantiated graphs.
+struct GraphKey {
+    int tbytes, ubytes, triangular;
+    const void *in;
+    void *out;
+    void *ws;
+    std::vector<int64_t> sizes, offsets;
+    bool operator==(const GraphKey &o) const {
+        return tbytes == o.tbytes && ubytes == o.ubytes && triangular == o.triangular && in == o.in &&
+               out == o.out && ws == o.ws && sizes == o.sizes && offsets == o.offsets;
+    }
+};
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec;
+    long long launches;
+    unsigned long long stamp;
+};
+static std::mutex g_graph_mu;
+static std::vector<GraphEntry> g_graphs;
+static unsigned long long g_graph_clock = 0;
+constexpr size_t GRAPH_CACHE = 8;
+
+// launches of one blocked pass (as launch_blocked counts them)
+static long long blocked_launches(const FwPlan &P) {
+    long long n = 3;
+    for (size_t r = 0; r < P.active.size(); ++r) {
+        const int a = P.active[r];
+        n += 1 + (P.pre_panel[(size_t)a] > 0 ? 2 : 0) + (P.pre_tile[(size_t)a] > 0 ? 2 : 0);
+    }
+    return n;
+}
+
+template <typename T, typename U>
+static int launch_blocked_graph(const FwPlan &P, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                                const T *in, T *out, unsigned char *ws, cudaStream_t stream, int triangular) {
+    if (g_timer.on) return launch_blocked<T, U>(P, in, out, ws, stream, false, nullptr);   // timed per kernel
+    GraphKey key{(int)sizeof(T), (int)sizeof(U), triangular, in, out, ws,
+                 std::vector<int64_t>(sizes, sizes + count), std::vector<int64_t>(offsets, offsets + count)};
+    {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        for (auto &e : g_graphs) {
+            if (e.key == key) {
+                e.stamp = ++g_graph_clock;
+                RBG_CUDA_TRY(cudaGraphLaunch(e.exec, stream));
+                note_launches(e.launches);
+                return RBG_OK;
+            }
+        }
+    }
+    // record on a private stream (the caller's may be the legacy default stream, which cannot be
+    // captured); nothing runs while recording, and the graph is launched on the caller's stream
+    static thread_local cudaStream_t cap = nullptr;
+    if (!cap) RBG_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    RBG_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    t_recording = 1;
+    const int rc = launch_blocked<T, U>(P, in, out, ws, cap, false, nullptr);
+    t_recording = 0;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cap, &graph);
+    if (rc || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc ? rc : RBG_ERR_CUDA;
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return RBG_ERR_CUDA;
+    RBG_CUDA_TRY(cudaGraphLaunch(exec, stream));
+    const long long nl = blocked_launches(P);
+    note_launches(nl);
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    if (g_graphs.size() >= GRAPH_CACHE) {
+        size_t old = 0;
+        for (size_t k = 1; k < g_graphs.size(); ++k)
+            if (g_graphs[k].stamp < g_graphs[old].stamp) old = k;
+        cudaDeviceSynchronize();   // the evicted graph may still run on another stream
+        cudaGraphExecDestroy(g_graphs[old].exec);
+        g_graphs.erase(g_graphs.begin() + (long)old);
+    }
+    g_graphs.push_back(GraphEntry{std::move(key), exec, nl, ++g_graph_clock});
+    return RBG_OK;
+}
+
 template <typename T>
 static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offsets, const T *in, T *out,
                       uint32_t mode, unsigned char *ws, rbg_result_t *results, cudaStream_t stream) {
@@ -1055,7 +1148,9 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
         build_plan(P, count, sizes, offsets, offsets, 4, triangular, TileCfg<uint32_t>::BN, (int)sizeof(T));
         int rc = upload_plan(P, ws, stream);
         if (rc) return rc;
-        rc = launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr);
+        rc = (mode & RBG_MODE_GRAPH)
+                 ? launch_blocked_graph<T, uint32_t>(P, count, sizes, offsets, in, out, ws, stream, triangular)
+                 : launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr);
         if (rc) return rc;
         std::vector<DevStatus> h((size_t)count);
         rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), h.data(), (int)count, stream);

@@ -64,3 +64,42 @@ def test_cython_batch(native):
     for A, W, r in zip(mats, Ws, res):
         Wo, do, so, _ = O.fw_cython(A)
         assert r.status == so == 0 and (W == Wo).all() and r.diameter == do
+
+
+def test_graph_replay_matches_direct_launches(native):
+    """RBG_MODE_GRAPH: the first call records the batch's launch sequence, later calls with the
+    same sizes, offsets and buffers replay it; results (values, diameters, fallbacks) equal the
+    direct launches, also after the input changes in place between replays."""
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.dense import fw_batch, pack
+    from redblackgraph_gb300.device import to_device, to_host
+    sizes, seeds = synth.batch_components(40, 3, 500, seed=9)
+    mats = [synth.pedigree(int(n), synth.generations_for(int(n)), int(s), dtype=np.int32)
+            for n, s in zip(sizes, seeds)]
+    cyc = np.array([[0, 2, 0], [0, 0, 3], [2, 0, 0]], dtype=np.int32)   # a cycle: reruns alone
+    mats.append(cyc)
+    flat, sz, off = pack(mats)
+    d = to_device(flat)
+    out = torch.empty_like(d)
+    ref, rres = fw_batch(d, sz, off, out=torch.empty_like(d))
+    ref = to_host(ref)
+    L = native
+    for rep in range(3):
+        l0 = L.rbg_launch_count()
+        _, res = fw_batch(d, sz, off, out=out, mode=_lib.MODE_GRAPH)
+        torch.cuda.synchronize()
+        assert L.rbg_launch_count() > l0                     # replays count their launches
+        assert (to_host(out) == ref).all()
+        assert [(r.status, r.diameter) for r in res] == [(r.status, r.diameter) for r in rres]
+    # new contents, same layout: the replay reads the new input
+    mats2 = [synth.pedigree(int(n), synth.generations_for(int(n)), int(s) + 1, dtype=np.int32)
+             for n, s in zip(sizes, seeds)] + [cyc]
+    flat2, _, _ = pack(mats2)
+    d.copy_(to_device(flat2))
+    _, res2 = fw_batch(d, sz, off, out=out, mode=_lib.MODE_GRAPH)
+    torch.cuda.synchronize()
+    h = to_host(out)
+    for A, o, n, r in zip(mats2[:-1], off, sz, res2):
+        Wo, do, so, _ = O.warshall(A)
+        assert (h[o:o + n * n].reshape(n, n) == Wo).all() and r.diameter == do
