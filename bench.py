@@ -266,7 +266,9 @@ def run_ours(args, rank, world, w):
     out = torch.empty_like(buf)
 
     results = None
-    mode = _lib.MODE_GRAPH          # the batch's launch sequence is replayed as a CUDA graph
+    # the first warm-up call tunes the tile shape of every round (closing the batch with both
+    # shapes); later calls replay the tuned launch sequence as a CUDA graph
+    mode = _lib.MODE_GRAPH | _lib.MODE_AUTOTUNE
     for _ in range(max(args.warmup, 3)):
         out, results = fw_batch(buf, sizes, offsets, out=out, mode=mode)
     assert all(r.status == 0 for r in results), "closure reported an error"
@@ -288,7 +290,7 @@ def run_ours(args, rank, world, w):
         dist.barrier()
     launches = L.rbg_launch_count() - launches0
     # per-kernel split from one more step with event timers between the launches (untimed)
-    kprof = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out))
+    kprof = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out, mode=mode))
     kprof = {k: (v[0] * args.steps, v[1] * args.steps) for k, v in kprof.items()}
     t = e0.elapsed_time(e1) / 1e3
     if world > 1:

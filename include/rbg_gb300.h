@@ -71,6 +71,10 @@ typedef void *rbg_stream_t; /* a cudaStream_t */
 #define RBG_MODE_GRAPH 16u      /* rbg_fw_batch: record the launch sequence as a CUDA graph
                                    and replay it on later calls with the same sizes,
                                    offsets, buffers and workspace (small LRU cache)      */
+#define RBG_MODE_TILE_NARROW 32u /* rbg_fw_batch: 128 x 64 phase-3 tiles in every round   */
+#define RBG_MODE_AUTOTUNE 64u   /* rbg_fw_batch: per-round tile shape chosen by timing both
+                                   shapes on the first call for a batch layout (the first
+                                   call closes the batch twice; not when in == out)      */
 
 /* which kernel path produced a result */
 #define RBG_PATH_BLOCKED32 1

@@ -35,6 +35,8 @@ MODE_TRIANGULAR = 2
 MODE_FORCE_EXACT = 4
 MODE_FORCE_WIDE = 8
 MODE_GRAPH = 16
+MODE_TILE_NARROW = 32
+MODE_AUTOTUNE = 64
 
 PATH_BLOCKED32, PATH_BLOCKED64, PATH_EXACT = 1, 2, 3
 

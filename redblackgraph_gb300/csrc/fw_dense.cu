@@ -503,7 +503,7 @@ __global__ void fw_tile_list_kernel(const FwComp *__restrict__ comps, const int6
 }
 
 template <typename U, int BN, int TM, int TN>
-__global__ void __launch_bounds__(FW_THREADS, 2)
+__global__ void __launch_bounds__(FW_THREADS, (TM * TN * sizeof(U) <= 128) ? 3 : 2)
 fw_tile_kernel(U *__restrict__ work_base, const unsigned long long *__restrict__ any_base,
                unsigned char *__restrict__ occ_base,
                const FwComp *__restrict__ comps, const int2 *__restrict__ list, int *__restrict__ counters,
@@ -712,9 +712,15 @@ static int run_exact(const T *in, int64_t ld_in, T *out, int64_t ld_out, int64_t
 // ------------------------------------------------------------------------------------------
 // host driver
 // ------------------------------------------------------------------------------------------
+// Phase-3 tile shapes: BM = 128 rows always; 32-bit lanes have a wide (128 columns, 8 x 8 cells
+// per thread) and a narrow (64 columns, 4 x 8 cells) shape, chosen per round (RBG_MODE_TILE_NARROW
+// or the autotuner); 64-bit lanes use 64 columns, 8 x 4 cells.
 template <typename U> struct TileCfg;
 template <> struct TileCfg<uint32_t> { static const int BN = 128, TM = 8, TN = 8; };
 template <> struct TileCfg<uint64_t> { static const int BN = 64, TM = 8, TN = 4; };
+template <typename U> struct TileNarrow;
+template <> struct TileNarrow<uint32_t> { static const int BN = 64, TM = 4, TN = 8; };
+template <> struct TileNarrow<uint64_t> { static const int BN = 64, TM = 8, TN = 4; };
 
 
 // Everything a (batched) blocked run needs on the host: the component table (sorted by size,
@@ -723,9 +729,9 @@ template <> struct TileCfg<uint64_t> { static const int BN = 64, TM = 8, TN = 4;
 struct FwPlan {
     int count = 0;
     std::vector<FwComp> comps;
-    std::vector<int64_t> pre_conv, pre_panel, pre_tile;
+    std::vector<int64_t> pre_conv, pre_panel, pre_tile, pre_tile_n;   // _n: narrow tiles
     std::vector<int> active;                // active[r] = components with n > 64 r
-    size_t off_status = 0, off_comps = 0, off_pconv = 0, off_ppanel = 0, off_ptile = 0;
+    size_t off_status = 0, off_comps = 0, off_pconv = 0, off_ppanel = 0, off_ptile = 0, off_ptile_n = 0;
     size_t off_rb = 0, off_any = 0, off_lanes = 0, off_exact = 0, total = 0;
     size_t off_occ = 0, occ_bytes = 0, off_plist = 0, off_tlist = 0, off_counters = 0;
 };
@@ -733,7 +739,7 @@ struct FwPlan {
 // sizes[i], in_off[i], out_off[i] of component i (input order); lane = bytes per lane word
 static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int64_t *in_off,
                        const int64_t *out_off, size_t lane, int triangular, int tile_bn,
-                       int elem_bytes) {
+                       int elem_bytes, int tile_bn_narrow = 64) {
     P.count = (int)count;
     std::vector<int> order((size_t)count);
     for (int64_t i = 0; i < count; ++i) order[(size_t)i] = (int)i;
@@ -742,6 +748,7 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
     P.pre_conv.assign((size_t)count + 1, 0);
     P.pre_panel.assign((size_t)count + 1, 0);
     P.pre_tile.assign((size_t)count + 1, 0);
+    P.pre_tile_n.assign((size_t)count + 1, 0);
     int64_t lanes = 0, anys = 0, maxn = 0, occs = 0;
     for (int64_t k = 0; k < count; ++k) {
         const int i = order[(size_t)k];
@@ -764,6 +771,8 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
         const bool big = c.n > FW_B;   // n <= 64: the diagonal tile is the whole matrix
         P.pre_panel[(size_t)k + 1] = P.pre_panel[(size_t)k] + (big ? 2 * (c.np / PN_LINES) : 0);
         P.pre_tile[(size_t)k + 1] = P.pre_tile[(size_t)k] + (big ? (c.np / tile_bn) * (c.np / FW_P) : 0);
+        P.pre_tile_n[(size_t)k + 1] =
+            P.pre_tile_n[(size_t)k] + (big ? (c.np / tile_bn_narrow) * (c.np / FW_P) : 0);
         maxn = std::max(maxn, c.n);
     }
     const int rounds = (int)((maxn + FW_B - 1) / FW_B);
@@ -779,12 +788,15 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
     P.off_pconv = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
     P.off_ppanel = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
     P.off_ptile = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
+    P.off_ptile_n = o; o = align_up(o + ((size_t)count + 1) * 8, 256);
     P.off_rb = o; o = align_up(o + (size_t)count * (lane == 8 ? sizeof(RoundBuf<uint64_t>) : sizeof(RoundBuf<uint32_t>)), 256);
     P.off_any = o; o = align_up(o + (size_t)anys * 8, 256);
     P.off_occ = o; P.occ_bytes = (size_t)occs; o = align_up(o + (size_t)occs, 256);
     const int a0 = rounds > 0 ? P.active[0] : 0;
     P.off_plist = o; o = align_up(o + (size_t)std::max<int64_t>(P.pre_panel[(size_t)a0], 1) * 8, 256);
-    P.off_tlist = o; o = align_up(o + (size_t)std::max<int64_t>(P.pre_tile[(size_t)a0], 1) * 8, 256);
+    P.off_tlist = o;
+    o = align_up(o + (size_t)std::max<int64_t>(std::max(P.pre_tile[(size_t)a0], P.pre_tile_n[(size_t)a0]), 1) * 8,
+                 256);
     P.off_counters = o; o = align_up(o + 64, 256);
     P.off_lanes = o; o = align_up(o + (size_t)lanes * lane, 256);
     P.off_exact = o; o = align_up(o + 3 * align_up((size_t)maxn, 32) * elem_bytes + 256, 256);
@@ -807,6 +819,10 @@ static int configure_kernels() {
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_tile_kernel<U, C::BN, C::TM, C::TN>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(TileSmem<U, C::BN>)));
+    typedef TileNarrow<U> N;
+    RBG_CUDA_TRY(cudaFuncSetAttribute(fw_tile_kernel<U, N::BN, N::TM, N::TN>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sizeof(TileSmem<U, N::BN>)));
     return RBG_OK;
 }
 
@@ -820,6 +836,8 @@ static int upload_plan(const FwPlan &P, unsigned char *ws, cudaStream_t stream) 
                                  cudaMemcpyHostToDevice, stream));
     RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ptile, P.pre_tile.data(), P.pre_tile.size() * 8,
                                  cudaMemcpyHostToDevice, stream));
+    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ptile_n, P.pre_tile_n.data(), P.pre_tile_n.size() * 8,
+                                 cudaMemcpyHostToDevice, stream));
     return RBG_OK;
 }
 
@@ -828,7 +846,8 @@ static int upload_plan(const FwPlan &P, unsigned char *ws, cudaStream_t stream) 
 // untouched in `out` by the finalization.
 template <typename T, typename U>
 static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws, cudaStream_t stream,
-                          bool stop_after_convert, DevStatus *h_status) {
+                          bool stop_after_convert, DevStatus *h_status, const unsigned char *shapes = nullptr,
+                          cudaEvent_t *round_events = nullptr) {
     typedef TileCfg<U> C;
     static const int configured = configure_kernels<U>();   // once, thread-safe initialisation
     if (configured) return configured;
@@ -838,6 +857,8 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     const int64_t *pconv = reinterpret_cast<const int64_t *>(ws + P.off_pconv);
     const int64_t *ppanel = reinterpret_cast<const int64_t *>(ws + P.off_ppanel);
     const int64_t *ptile = reinterpret_cast<const int64_t *>(ws + P.off_ptile);
+    const int64_t *ptile_n = reinterpret_cast<const int64_t *>(ws + P.off_ptile_n);
+    typedef TileNarrow<U> N;
     RoundBuf<U> *rbs = reinterpret_cast<RoundBuf<U> *>(ws + P.off_rb);
     unsigned long long *any = reinterpret_cast<unsigned long long *>(ws + P.off_any);
     U *lanes = reinterpret_cast<U *>(ws + P.off_lanes);
@@ -874,7 +895,8 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     for (size_t r = 0; r < P.active.size(); ++r) {
         const int a = P.active[r];
         const int64_t K0 = (int64_t)r * FW_B;
-        const int64_t np_ = P.pre_panel[(size_t)a], nt_ = P.pre_tile[(size_t)a];
+        const bool narrow = shapes && shapes[r];
+        const int64_t np_ = P.pre_panel[(size_t)a], nt_ = narrow ? P.pre_tile_n[(size_t)a] : P.pre_tile[(size_t)a];
         note_launches(1 + (np_ > 0 ? 2 : 0) + (nt_ > 0 ? 2 : 0));
         cudaEvent_t td = timer_begin(2, stream);
         fw_diag_kernel<U><<<a, DG_THREADS, sizeof(DiagSmem<U>), stream>>>(lanes, any, rbs, comps, counters,
@@ -888,15 +910,25 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
                                  stream>>>(lanes, any, occ, rbs, comps, plist, counters, K0, lbits, st);
             timer_end(1, t0, stream);
         }
+        if (round_events) RBG_CUDA_TRY(cudaEventRecord(round_events[2 * r], stream));
         if (nt_ > 0) {
             cudaEvent_t t0 = timer_begin(0, stream);
-            fw_tile_list_kernel<C::BN><<<(unsigned)((nt_ + 255) / 256), 256, 0, stream>>>(comps, ptile, a, any,
-                                                                                       tlist, counters);
-            fw_tile_kernel<U, C::BN, C::TM, C::TN><<<(unsigned)std::min<int64_t>(nt_, persist), FW_THREADS,
-                                                    sizeof(TileSmem<U, C::BN>), stream>>>(
-                lanes, any, occ, comps, tlist, counters, K0, lbits, st);
+            const unsigned tl = (unsigned)((nt_ + 255) / 256);
+            // persistent grids: as many CTAs as fit on the SMs (3 per SM for the narrow 32-bit shape)
+            const int per_sm = (N::TM * N::TN * (int)sizeof(U) <= 128) ? 3 : 2;
+            const unsigned tg = (unsigned)std::min<int64_t>(nt_, narrow ? (int64_t)per_sm * sms : persist);
+            if (narrow) {
+                fw_tile_list_kernel<N::BN><<<tl, 256, 0, stream>>>(comps, ptile_n, a, any, tlist, counters);
+                fw_tile_kernel<U, N::BN, N::TM, N::TN><<<tg, FW_THREADS, sizeof(TileSmem<U, N::BN>), stream>>>(
+                    lanes, any, occ, comps, tlist, counters, K0, lbits, st);
+            } else {
+                fw_tile_list_kernel<C::BN><<<tl, 256, 0, stream>>>(comps, ptile, a, any, tlist, counters);
+                fw_tile_kernel<U, C::BN, C::TM, C::TN><<<tg, FW_THREADS, sizeof(TileSmem<U, C::BN>), stream>>>(
+                    lanes, any, occ, comps, tlist, counters, K0, lbits, st);
+            }
             timer_end(0, t0, stream);
         }
+        if (round_events) RBG_CUDA_TRY(cudaEventRecord(round_events[2 * r + 1], stream));
     }
     RBG_CUDA_TRY(cudaGetLastError());
     note_launches(1);
@@ -1057,9 +1089,10 @@ struct GraphKey {
     void *out;
     void *ws;
     std::vector<int64_t> sizes, offsets;
+    std::vector<unsigned char> shapes;
     bool operator==(const GraphKey &o) const {
         return tbytes == o.tbytes && ubytes == o.ubytes && triangular == o.triangular && in == o.in &&
-               out == o.out && ws == o.ws && sizes == o.sizes && offsets == o.offsets;
+               out == o.out && ws == o.ws && sizes == o.sizes && offsets == o.offsets && shapes == o.shapes;
     }
 };
 struct GraphEntry {
@@ -1085,10 +1118,13 @@ static long long blocked_launches(const FwPlan &P) {
 
 template <typename T, typename U>
 static int launch_blocked_graph(const FwPlan &P, int64_t count, const int64_t *sizes, const int64_t *offsets,
-                                const T *in, T *out, unsigned char *ws, cudaStream_t stream, int triangular) {
-    if (g_timer.on) return launch_blocked<T, U>(P, in, out, ws, stream, false, nullptr);   // timed per kernel
+                                const T *in, T *out, unsigned char *ws, cudaStream_t stream, int triangular,
+                                const std::vector<unsigned char> &shapes) {
+    if (g_timer.on)   // timed per kernel: launched directly
+        return launch_blocked<T, U>(P, in, out, ws, stream, false, nullptr, shapes.data());
     GraphKey key{(int)sizeof(T), (int)sizeof(U), triangular, in, out, ws,
-                 std::vector<int64_t>(sizes, sizes + count), std::vector<int64_t>(offsets, offsets + count)};
+                 std::vector<int64_t>(sizes, sizes + count), std::vector<int64_t>(offsets, offsets + count),
+                 shapes};
     {
         std::lock_guard<std::mutex> lk(g_graph_mu);
         for (auto &e : g_graphs) {
@@ -1106,7 +1142,7 @@ static int launch_blocked_graph(const FwPlan &P, int64_t count, const int64_t *s
     if (!cap) RBG_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     RBG_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
     t_recording = 1;
-    const int rc = launch_blocked<T, U>(P, in, out, ws, cap, false, nullptr);
+    const int rc = launch_blocked<T, U>(P, in, out, ws, cap, false, nullptr, shapes.data());
     t_recording = 0;
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cap, &graph);
@@ -1134,6 +1170,61 @@ static int launch_blocked_graph(const FwPlan &P, int64_t count, const int64_t *s
     return RBG_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// autotuner (RBG_MODE_AUTOTUNE): the phase-3 tile shape of every round
+// ------------------------------------------------------------------------------------------
+// Round r of a batch runs the components larger than 64 r, so rounds stand for size classes.
+// The first call for a batch layout (keyed by the number of components active in each round)
+// closes the batch twice, with wide and with narrow tiles in every round, timing each round's
+// phase 3 with events; each round then keeps the faster shape, for every later call with that
+// key (in-process cache).  Both passes compute the full closure, so the call's results are those
+// of the second pass; a call whose input and output are the same buffer is not tuned.
+struct TuneEntry {
+    int tbytes, triangular;
+    std::vector<int> active;
+    std::vector<unsigned char> shapes;
+};
+static std::mutex g_tune_mu;
+static std::vector<TuneEntry> g_tune;
+
+static bool tune_lookup(int tbytes, int triangular, const std::vector<int> &active, std::vector<unsigned char> &shapes) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto &e : g_tune)
+        if (e.tbytes == tbytes && e.triangular == triangular && e.active == active) {
+            shapes = e.shapes;
+            return true;
+        }
+    return false;
+}
+
+template <typename T>
+static int tune_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws, cudaStream_t stream, int triangular,
+                        std::vector<unsigned char> &shapes) {
+    const size_t R = P.active.size();
+    std::vector<cudaEvent_t> ev(4 * R, nullptr);
+    for (auto &e : ev) RBG_CUDA_TRY(cudaEventCreate(&e));
+    std::vector<float> ms[2];
+    int rc = RBG_OK;
+    for (int shape = 0; shape < 2 && rc == RBG_OK; ++shape) {
+        std::vector<unsigned char> all(R, (unsigned char)shape);
+        rc = launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, all.data(), ev.data() + 2 * R * shape);
+    }
+    if (rc == RBG_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = RBG_ERR_CUDA;
+    if (rc == RBG_OK) {
+        shapes.assign(R, 0);
+        for (size_t r = 0; r < R; ++r) {
+            float w = 0.f, n = 0.f;
+            cudaEventElapsedTime(&w, ev[2 * r], ev[2 * r + 1]);
+            cudaEventElapsedTime(&n, ev[2 * R + 2 * r], ev[2 * R + 2 * r + 1]);
+            shapes[r] = n < 0.97f * w ? 1 : 0;   // narrow only when clearly faster
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune.push_back(TuneEntry{(int)sizeof(T), triangular, P.active, shapes});
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
 template <typename T>
 static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offsets, const T *in, T *out,
                       uint32_t mode, unsigned char *ws, rbg_result_t *results, cudaStream_t stream) {
@@ -1148,9 +1239,19 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
         build_plan(P, count, sizes, offsets, offsets, 4, triangular, TileCfg<uint32_t>::BN, (int)sizeof(T));
         int rc = upload_plan(P, ws, stream);
         if (rc) return rc;
-        rc = (mode & RBG_MODE_GRAPH)
-                 ? launch_blocked_graph<T, uint32_t>(P, count, sizes, offsets, in, out, ws, stream, triangular)
-                 : launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr);
+        std::vector<unsigned char> shapes(P.active.size(), (mode & RBG_MODE_TILE_NARROW) ? 1 : 0);
+        bool done = false;
+        if ((mode & RBG_MODE_AUTOTUNE) && !tune_lookup((int)sizeof(T), triangular, P.active, shapes) &&
+            (const void *)in != (const void *)out) {
+            rc = tune_blocked<T>(P, in, out, ws, stream, triangular, shapes);
+            if (rc) return rc;
+            done = true;
+        }
+        if (!done)
+            rc = (mode & RBG_MODE_GRAPH)
+                     ? launch_blocked_graph<T, uint32_t>(P, count, sizes, offsets, in, out, ws, stream, triangular,
+                                                         shapes)
+                     : launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, shapes.data());
         if (rc) return rc;
         std::vector<DevStatus> h((size_t)count);
         rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), h.data(), (int)count, stream);

@@ -103,3 +103,28 @@ def test_graph_replay_matches_direct_launches(native):
     for A, o, n, r in zip(mats2[:-1], off, sz, res2):
         Wo, do, so, _ = O.warshall(A)
         assert (h[o:o + n * n].reshape(n, n) == Wo).all() and r.diameter == do
+
+
+@pytest.mark.parametrize("mode_name", ["MODE_TILE_NARROW", "MODE_AUTOTUNE"])
+def test_tile_shapes_and_autotune_match_oracle(native, mode_name):
+    """The narrow phase-3 tile shape, and the autotuned per-round shapes (the first call tunes by
+    closing the batch with both shapes), give the oracle's results; a second call reuses the
+    tuned shapes."""
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.dense import fw_batch, pack
+    from redblackgraph_gb300.device import to_device, to_host
+    sizes, seeds = synth.batch_components(30, 3, 900, seed=11)
+    mats = [synth.pedigree(int(n), synth.generations_for(int(n)), int(s), dtype=np.int32)
+            for n, s in zip(sizes, seeds)]
+    flat, sz, off = pack(mats)
+    d = to_device(flat)
+    mode = getattr(_lib, mode_name)
+    for _ in range(2):
+        out, res = fw_batch(d, sz, off, out=torch.empty_like(d), mode=mode)
+        torch.cuda.synchronize()
+        h = to_host(out)
+        for A, o, n, r in zip(mats, off, sz, res):
+            Wo, do, so, _ = O.warshall(A)
+            assert r.status == so == 0
+            assert (h[o:o + n * n].reshape(n, n) == Wo).all() and r.diameter == do
