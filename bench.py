@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving workload (0: skip)")
     ap.add_argument("--serve-count", type=int, default=0, help="requests in the serving stream")
+    ap.add_argument("--only", choices=["spgemm", "single", "serve"], default=None,
+                    help="run one secondary workload alone and print its JSON (profiling cases)")
     ap.add_argument("--secondary", type=int, default=1,
                     help="also measure the per-component plain path, one n=8192 int64 closure and "
                          "the 2M-vertex squaring SpGEMM (0: skip)")
@@ -601,6 +603,13 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":
         return main_reference(args, rank, world)
+    if args.only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        fn = {"spgemm": run_spgemm_forest, "single": run_single_dense,
+              "serve": lambda: run_serving(args.serve_count)}[args.only]
+        print(json.dumps(fn()))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")

@@ -168,8 +168,7 @@ constexpr int PN_LINES = 64;                      // panel columns / rows per CT
 constexpr int PN_THREADS = PN_LINES * 4;
 
 template <typename U> struct PanelSmem {
-    U CS[FW_B][Pad<U>::LD];           // row panel:    cs[t][a]    (padded)
-    U RSm[FW_B][Pad<U>::LD];          // column panel: rsm[t][b]   (padded)
+    U TA[FW_B][Pad<U>::LD];           // row panel: cs[t][a]; column panel: rsm[t][b] (padded)
     U RSl[FW_B][Pad<U>::LD];          //               rsl[t][b]   (padded)
     unsigned long long maskCS[FW_B];
     unsigned long long maskRS[FW_B];
@@ -256,7 +255,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
             va[i] = ta[tid + i * PN_THREADS];
             if (!rowPanel) vb[i] = tb[tid + i * PN_THREADS];
         }
-        U *da = rowPanel ? &S.CS[0][0] : &S.RSm[0][0];
+        U *da = &S.TA[0][0];
         U *db = &S.RSl[0][0];
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
@@ -275,7 +274,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     __syncthreads();
 
     const int pc0 = Pad<U>::at(c0);
-    const U *tabA = rowPanel ? &S.CS[0][pc0] : &S.RSm[0][pc0];
+    const U *tabA = &S.TA[0][pc0];
     const U *tabB = &S.RSl[0][pc0];
     bool changed = false;                             // some cell of this thread decreased
     if (__all_sync(0xffffffffu, startInf == (1u << DG_ROWS) - 1u)) {
@@ -358,9 +357,9 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
             if (rowPanel) {
                 U m, low;
                 L::split(zf, m, low);
-                first = S.CS[tf][Pad<U>::at(c)] * m + low;
+                first = S.TA[tf][Pad<U>::at(c)] * m + low;
             } else {
-                first = zf * S.RSm[tf][Pad<U>::at(c)] + S.RSl[tf][Pad<U>::at(c)];
+                first = zf * S.TA[tf][Pad<U>::at(c)] + S.RSl[tf][Pad<U>::at(c)];
             }
             smx = max(smx, (SU)first);
         }
