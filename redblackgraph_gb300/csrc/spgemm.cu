@@ -41,8 +41,28 @@ constexpr int SEM_CY32 = 1;  // Cython semantics on int32 (the gpu module)
 template <int SEM, bool UNS>
 __device__ __forceinline__ long long sp_mul(long long a, long long b, unsigned &ev) {
     if (SEM == SEM_CY32) return (long long)cy_product((int32_t)a, (int32_t)b);
+    // both operands plain values (neither 0, 1, the red one nor, signed, negative): the bit
+    // splice with the C core's two overflow tests, without the identity and sign cases
+    const unsigned long long x = (unsigned long long)a, y = (unsigned long long)b;
+    const bool plain = UNS ? (x >= 2 && y >= 2 && ~x != 0 && ~y != 0) : (a >= 2 && b >= 2);
+    if (plain) {
+        const int bp = 63 - __clzll((long long)y), mx = 63 - __clzll((long long)x);
+        if (mx + bp >= 64) ev |= RBG_EV_OVF_SIZE;
+        const unsigned long long r = (x << bp) | (y ^ (1ull << bp));
+        if (~r == 0) ev |= RBG_EV_OVF_ONES;
+        return (long long)r;
+    }
     if (UNS) return (long long)avos_product<uint64_t>((uint64_t)a, (uint64_t)b, ev);
     return (long long)avos_product<int64_t>((int64_t)a, (int64_t)b, ev);
+}
+
+// a stored value widened to the 64-bit compute value (compile-time storage width)
+template <int BYTES, bool UNS>
+__device__ __forceinline__ long long sp_load_t(const void *x, int64_t i) {
+    if (BYTES == 8) return ((const long long *)x)[i];
+    const int v = ((const int *)x)[i];
+    if (UNS) return v == -1 ? -1ll : (long long)(unsigned)v;   // RED_ONE widens to all ones
+    return (long long)v;
 }
 template <int SEM, bool UNS>
 __device__ __forceinline__ long long sp_add(long long a, long long b) {
@@ -285,12 +305,18 @@ constexpr int SP_HASH_SLOTS = 256;
 constexpr int SP_HWARPS = 8;          // warps per CTA
 constexpr unsigned SP_NOKEY = 0xffffffffu;
 
+// The (+) of a column's products is a minimum in an order encoding (sp_enc); keys below the
+// 32-bit empty mark are folded with a native 32-bit shared atomicMin, larger ones (rare) with
+// a 64-bit one, and the two halves are combined when the row is written.
 struct SpHashWarp {
     unsigned key[SP_HASH_SLOTS];
-    unsigned long long val[SP_HASH_SLOTS];   // order-encoded (+) of the products
+    unsigned v32[SP_HASH_SLOTS];             // (+) of the products with small keys
+    unsigned long long v64[SP_HASH_SLOTS];   // (+) of the products with large keys
     long long rv[SP_HASH_SLOTS];             // R's own entry (squaring step), 0 if none
     unsigned long long list[SP_HASH_SLOTS];  // (column << 32 | slot) of the occupied slots
 };
+constexpr unsigned SP_E32 = 0xffffffffu;     // empty mark of v32 (C core encoding)
+constexpr int SP_E32S = 0x7fffffff;          // empty mark of v32 (Cython, signed)
 constexpr size_t SP_WARP_SMEM = sizeof(SpHashWarp) * SP_HWARPS;
 
 // Slot of column j (inserted if new); -1 when the table is full.
@@ -310,11 +336,69 @@ __device__ __forceinline__ int sp_hash_slot(SpHashWarp &H, unsigned j, int mask)
 
 template <int SEM>
 __device__ __forceinline__ void sp_hash_fold(SpHashWarp &H, int slot, long long p) {
-    if (SEM == SEM_CY32) atomicMin(reinterpret_cast<long long *>(&H.val[slot]), p);
-    else atomicMin(&H.val[slot], sp_enc<SEM>(p));
+    if (SEM == SEM_CY32) {
+        if (p < (long long)SP_E32S && p >= (long long)INT_MIN) {
+            int *v = reinterpret_cast<int *>(&H.v32[slot]);
+            if ((int)p < *v) atomicMin(v, (int)p);        // a larger value cannot lower the minimum
+        } else {
+            long long *v = reinterpret_cast<long long *>(&H.v64[slot]);
+            if (p < *v) atomicMin(v, p);
+        }
+    } else {
+        const unsigned long long e = sp_enc<SEM>(p);
+        if (e < (unsigned long long)SP_E32) {
+            if ((unsigned)e < H.v32[slot]) atomicMin(&H.v32[slot], (unsigned)e);
+        } else if (e < H.v64[slot]) {
+            atomicMin(&H.v64[slot], e);
+        }
+    }
 }
 
-template <int SEM, bool UNS>
+// the folded (+) of slot s (0 when no product landed there)
+template <int SEM>
+__device__ __forceinline__ long long sp_hash_value(const SpHashWarp &H, int s) {
+    if (SEM == SEM_CY32) {
+        const long long a = (int)H.v32[s] == SP_E32S ? LLONG_MAX : (long long)(int)H.v32[s];
+        const long long m = min(a, (long long)H.v64[s]);
+        return m == LLONG_MAX ? 0 : m;
+    }
+    const unsigned long long a = H.v32[s] == SP_E32 ? ~0ull : (unsigned long long)H.v32[s];
+    const unsigned long long m = min(a, H.v64[s]);
+    return m == sp_empty<SEM>() ? 0 : sp_dec<SEM>(m);
+}
+
+// Sort the first nd (<= 64) keys of list ascending in registers (shuffle bitonic network over 64
+// positions, two per lane, padded with the largest key); returns the two sorted keys of the lane.
+__device__ __forceinline__ void sp_sort64(unsigned long long *list, int nd, int lane) {
+    unsigned long long v[2];
+    v[0] = lane < nd ? list[lane] : ~0ull;
+    v[1] = lane + 32 < nd ? list[lane + 32] : ~0ull;
+#pragma unroll
+    for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j == 32) {                           // partners in the same lane
+                const unsigned long long lo = min(v[0], v[1]), hi = max(v[0], v[1]);
+                v[0] = lo;                           // k == 64: the whole sequence ascends
+                v[1] = hi;
+            } else {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int i = lane + 32 * h;
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, v[h], j);
+                    const bool up = (i & k) == 0, lower = (i & j) == 0;
+                    v[h] = (lower == up) ? min(v[h], o) : max(v[h], o);
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (lane < nd) list[lane] = v[0];
+    if (lane + 32 < nd) list[lane + 32] = v[1];
+    __syncwarp();
+}
+
+template <int SEM, bool UNS, int BYTES>
 __global__ void __launch_bounds__(SP_HWARPS * 32)
 sp_warp_kernel(SpArgs a, int merge) {
     extern __shared__ __align__(16) unsigned char sp_smem[];
@@ -330,7 +414,8 @@ sp_warp_kernel(SpArgs a, int merge) {
         const int mask = S - 1;
         for (int s = lane; s < S; s += 32) {
             H.key[s] = SP_NOKEY;
-            H.val[s] = sp_empty<SEM>();
+            H.v32[s] = SEM == SEM_CY32 ? (unsigned)SP_E32S : SP_E32;
+            H.v64[s] = sp_empty<SEM>();
             H.rv[s] = 0;
         }
         __syncwarp();
@@ -339,7 +424,7 @@ sp_warp_kernel(SpArgs a, int merge) {
             for (int64_t e = a.rp[i] + lane; e < a.rp[i + 1]; e += 32) {
                 const int slot = sp_hash_slot(H, (unsigned)a.rj[e], mask);
                 if (slot < 0) full = true;
-                else H.rv[slot] = sp_load(a.rx, e, a.elem_bytes, a.uns);
+                else H.rv[slot] = sp_load_t<BYTES, UNS>(a.rx, e);
             }
         }
         for (int64_t e0 = a.ap[i]; e0 < a.ap[i + 1]; e0 += 32) {
@@ -350,7 +435,7 @@ sp_warp_kernel(SpArgs a, int merge) {
             int len = 0;
             if (in) {
                 const int k = a.aj[e];
-                av = sp_load(a.ax, e, a.elem_bytes, a.uns);
+                av = sp_load_t<BYTES, UNS>(a.ax, e);
                 b0 = a.bp[k];
                 len = (int)(a.bp[k + 1] - b0);
             }
@@ -377,7 +462,7 @@ sp_warp_kernel(SpArgs a, int merge) {
                     const int64_t f = bq + (idx - xq);
                     const int j = a.bj[f];
                     if (!(a.upper && j < i)) {
-                        const long long p = sp_mul<SEM, UNS>(aq, sp_load(a.bx, f, a.elem_bytes, a.uns), ev);
+                        const long long p = sp_mul<SEM, UNS>(aq, sp_load_t<BYTES, UNS>(a.bx, f), ev);
                         if (p != 0) {                // a zero product adds nothing
                             if (j == i && p != -1 && p != 1) ev |= RBG_EV_CYCLE;   // a vertex reaches itself
                             const int slot = sp_hash_slot(H, (unsigned)j, mask);
@@ -405,6 +490,11 @@ sp_warp_kernel(SpArgs a, int merge) {
         }
         int P = 1;
         while (P < nd) P <<= 1;
+        if (nd <= 64) {
+            __syncwarp();
+            sp_sort64(H.list, nd, lane);
+            P = 0;                                   // sorted: skip the shared-memory network
+        }
         for (int q = nd + lane; q < P; q += 32) H.list[q] = ~0ull;
         __syncwarp();
         for (int k = 2; k <= P; k <<= 1) {
@@ -430,9 +520,8 @@ sp_warp_kernel(SpArgs a, int merge) {
                 const unsigned long long e = H.list[q];
                 const int s = (int)(e & 0xffffffffu);
                 col = (unsigned)(e >> 32);
-                const unsigned long long kv = H.val[s];
-                const long long sv = kv == sp_empty<SEM>() ? 0 : sp_dec<SEM>(kv);
-                const long long s_t = sv == 0 ? 0 : ((SEM == SEM_CY32) ? sv : sp_trunc(sv, a.elem_bytes, UNS));
+                const long long sv = sp_hash_value<SEM>(H, s);
+                const long long s_t = sv == 0 ? 0 : ((SEM == SEM_CY32) ? sv : sp_trunc(sv, BYTES, UNS));
                 if (!merge) v = s_t;
                 else {
                     const long long r = H.rv[s];
@@ -576,9 +665,11 @@ __global__ void sp_dense_init_kernel(long long *dense_val, unsigned *dense_mark,
 // compacted output and stored in the storage type.
 __global__ void sp_gather_kernel(int64_t n_rows, const int64_t *cand_off, const int64_t *cptr,
                                  const int *ocol, const long long *oval, int *cj, void *cx, int bytes) {
-    for (int64_t i = blockIdx.x; i < n_rows; i += gridDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_rows; i += warps) {
         const int64_t src = cand_off[i], dst = cptr[i], cnt = cptr[i + 1] - dst;
-        for (int64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+        for (int64_t e = lane; e < cnt; e += 32) {
             cj[dst + e] = ocol[src + e];
             if (bytes == 8) reinterpret_cast<long long *>(cx)[dst + e] = oval[src + e];
             else reinterpret_cast<int *>(cx)[dst + e] = (int)oval[src + e];
@@ -703,7 +794,9 @@ namespace {
 template <int SEM, bool UNS>
 int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s) {
     static const int configured = [] {      // once, thread-safe initialisation
-        RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)SP_WARP_SMEM));
+        RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)SP_WARP_SMEM));
         RBG_CUDA_TRY(cudaFuncSetAttribute(sp_block_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)SP_BLOCK_SMEM));
@@ -712,7 +805,9 @@ int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s)
     if (configured) return configured;
     const int64_t n = a.n_rows;
     note_launches(2 + (dense > 0 ? 2 : 0));
-    sp_warp_kernel<SEM, UNS><<<grid_of((n + SP_HWARPS - 1) / SP_HWARPS, 1), SP_HWARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
+    const int wg = grid_of((n + SP_HWARPS - 1) / SP_HWARPS, 1);
+    if (a.elem_bytes == 8) sp_warp_kernel<SEM, UNS, 8><<<wg, SP_HWARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
+    else sp_warp_kernel<SEM, UNS, 4><<<wg, SP_HWARPS * 32, SP_WARP_SMEM, s>>>(a, merge);
     sp_block_kernel<SEM, UNS><<<grid_of(1 << 20, 1), SP_BLOCK_THREADS, SP_BLOCK_SMEM, s>>>(a, merge);
     if (dense > 0) {
         sp_dense_init_kernel<SEM><<<grid_of((int64_t)SP_DENSE_BLOCKS * nc, 256), 256, 0, s>>>(a.dense_val,
@@ -785,7 +880,7 @@ extern "C" int32_t rbg_spgemm_gather(int32_t dtype, int64_t n_rows, int64_t n_co
     RBG_CUDA_TRY(cudaMemcpyAsync(indptr, t.cptr, (size_t)(n_rows + 1) * 8, cudaMemcpyDeviceToDevice, s));
     if (n_rows > 0) {
         note_launches(1);
-        sp_gather_kernel<<<grid_of(n_rows * 32, 32), 64, 0, s>>>(n_rows, h.cand_off, t.cptr, t.ocol, t.oval, indices,
+        sp_gather_kernel<<<grid_of(n_rows * 32, 256), 256, 0, s>>>(n_rows, h.cand_off, t.cptr, t.ocol, t.oval, indices,
                                                                   data, dtype_bytes(dtype));
         RBG_CUDA_TRY(cudaGetLastError());
     }
