@@ -301,7 +301,7 @@ template <int SEM> __device__ __forceinline__ unsigned long long sp_empty() {
 // SP_HASH_SLOTS distinct columns; a row with more goes to the block kernel instead.  The
 // distinct columns are then sorted (a bitonic sort of at most SP_HASH_SLOTS keys) and written
 // ascending.
-constexpr int SP_HASH_SLOTS = 256;
+constexpr int SP_HASH_SLOTS = 128;
 constexpr int SP_HWARPS = 8;          // warps per CTA
 constexpr unsigned SP_NOKEY = 0xffffffffu;
 
