@@ -272,9 +272,9 @@ def run_ours(args, rank, world, w):
     # shapes); later calls replay the tuned launch sequence as a CUDA graph
     mode = _lib.MODE_GRAPH | _lib.MODE_AUTOTUNE
     for _ in range(max(args.warmup, 3)):
-        out, results = fw_batch(buf, sizes, offsets, out=out, mode=mode)
-    assert all(r.status == 0 for r in results), "closure reported an error"
-    executed = float(sum(r.executed for r in results))
+        out, results = fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True)
+    assert (results["status"] == 0).all(), "closure reported an error"
+    executed = float(results["executed"].sum())
 
     stream = torch.cuda.current_stream()
     if world > 1:
@@ -285,14 +285,14 @@ def run_ours(args, rank, world, w):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            fw_batch(buf, sizes, offsets, out=out, mode=mode)
+            fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True)
         e1.record(stream)
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     launches = L.rbg_launch_count() - launches0
     # per-kernel split from one more step with event timers between the launches (untimed)
-    kprof = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out, mode=mode))
+    kprof = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True))
     kprof = {k: (v[0] * args.steps, v[1] * args.steps) for k, v in kprof.items()}
     t = e0.elapsed_time(e1) / 1e3
     if world > 1:

@@ -57,6 +57,12 @@ class RbgResult(ctypes.Structure):
     ]
 
 
+# the same record as a numpy structured dtype (results of a batch read without per-item objects)
+RESULT_DTYPE = np.dtype([("status", "<i4"), ("flags", "<u4"), ("diameter", "<i8"), ("k", "<i8"),
+                         ("i", "<i8"), ("j", "<i8"), ("path", "<i4"), ("reserved", "<i4"),
+                         ("executed", "<i8")])
+
+
 class RbgCsr(ctypes.Structure):
     """rbg_csr_t: a device CSR matrix (int64 row pointers, int32 indices, values)."""
     _fields_ = [("n_rows", ctypes.c_int64), ("n_cols", ctypes.c_int64),

@@ -131,15 +131,18 @@ def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: 
     """
     comps = label_components(indptr, indices, n, stream)
     blocks = densify(indptr, indices, data, comps, stream)
-    _, results = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat,
-                          mode=_lib.MODE_CYTHON | _lib.MODE_GRAPH, stream=stream)
-    for r in results:
+    _, res = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat,
+                      mode=_lib.MODE_CYTHON | _lib.MODE_GRAPH, stream=stream, as_array=True)
+    bad = np.flatnonzero(res["status"] != _lib.RBG_OK)
+    if bad.size:                                     # the first component (by number) raises
+        r = _lib.RbgResult()
+        ctypes.memmove(ctypes.addressof(r), res[bad[0]:bad[0] + 1].tobytes(), ctypes.sizeof(r))
         raise_for_cython(r)
     fw = component_methods(comps.sizes, comps.count, method, densify_threshold)
     oi, oj, ov, cmax = compact(comps, blocks, want_max=not bool(fw.all()), stream=stream)
     diameter = 0
     if fw.any():
-        diameter = max(int(r.diameter) for r, f in zip(results, fw) if f)
+        diameter = int(res["diameter"][fw].max())
     if cmax is not None:
         mx = cmax[:comps.count].cpu().numpy()
         diameter = max(diameter, _msb(int(mx[~fw].max())))

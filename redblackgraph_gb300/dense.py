@@ -92,11 +92,12 @@ def warshall_host(A: np.ndarray, mode: int = 0) -> tuple[np.ndarray, int, _lib.R
 
 
 def fw_batch(buf: torch.Tensor, sizes, offsets, out: torch.Tensor | None = None, mode: int = 0,
-             stream: torch.cuda.Stream | None = None) -> tuple[torch.Tensor, list]:
+             stream: torch.cuda.Stream | None = None, as_array: bool = False) -> tuple[torch.Tensor, list]:
     """Close many matrices packed in one flat device tensor ``buf``.
 
     Matrix i is ``sizes[i] x sizes[i]`` at element offset ``offsets[i]``.  Returns
-    ``(out, results)`` with one ``RbgResult`` per matrix.
+    ``(out, results)`` with one ``RbgResult`` per matrix, or with ``as_array`` a numpy
+    structured array of ``_lib.RESULT_DTYPE`` records (no per-matrix Python objects).
     """
     import numpy as np
     if not buf.is_cuda or buf.ndim != 1:
@@ -121,6 +122,8 @@ def fw_batch(buf: torch.Tensor, sizes, offsets, out: torch.Tensor | None = None,
                         out.data_ptr(), mode, ws.data_ptr(), ws.numel(), results,
                         stream_handle(stream))
     _lib.check(rc, "fw_batch")
+    if as_array:
+        return out, np.frombuffer(results, dtype=_lib.RESULT_DTYPE, count=count).copy()
     return out, [results[i] for i in range(count)]
 
 

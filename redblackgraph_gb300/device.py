@@ -75,6 +75,16 @@ def to_device(a: np.ndarray, device: torch.device | None = None,
     return d.view(torch_dtype(a.dtype)).reshape(a.shape)
 
 
+def to_host_pinned(t: torch.Tensor) -> np.ndarray:
+    """Copy a device tensor into page-locked host memory (a fast device-to-host copy); the
+    returned array keeps that memory alive."""
+    npdt = numpy_dtype(t.dtype)
+    src = t.contiguous().reshape(-1).view(torch.uint8)
+    dst = torch.empty(src.numel(), dtype=torch.uint8, pin_memory=True)
+    dst.copy_(src)
+    return dst.numpy().view(npdt).reshape(tuple(t.shape))
+
+
 def to_host(t: torch.Tensor) -> np.ndarray:
     npdt = numpy_dtype(t.dtype)
     raw = t.contiguous().reshape(-1).view(torch.uint8).cpu().numpy()

@@ -116,7 +116,7 @@ def component_wise_closure(A, method: str = "auto", densify_threshold: int = 500
     (the reference's DTYPE); W is a CSR matrix with int32 values and sorted rows.
     """
     import scipy.sparse as sp
-    from ...device import require_cuda, to_device, to_host
+    from ...device import require_cuda, to_device, to_host_pinned
     from ...components import component_closure_device
     csr = _as_csr(A)
     n = csr.shape[0]
@@ -133,5 +133,5 @@ def component_wise_closure(A, method: str = "auto", densify_threshold: int = 500
     ij = to_device(np.ascontiguousarray(csr.indices), dev).to(torch.int32)
     iv = to_device(np.ascontiguousarray(csr.data).astype(np.int32, copy=False), dev)
     oi, oj, ov, diameter, _ = component_closure_device(ip, ij, iv, n, method, densify_threshold)
-    W = sp.csr_matrix((to_host(ov), to_host(oj), to_host(oi)), shape=(n, n))
+    W = sp.csr_matrix((to_host_pinned(ov), to_host_pinned(oj), to_host_pinned(oi)), shape=(n, n))
     return TransitiveClosure(W, int(diameter))
