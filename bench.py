@@ -348,7 +348,7 @@ def run_e2e(args, rank, world, w, dev, work_per_step):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t = float(tt.item())
     W = r.W
-    d2h = int(8 * (f.shape[0] + 1) + 8 * W.nnz)     # int64 row pointers, int32 indices and values
+    d2h = int(W.indptr.nbytes + W.indices.nbytes + W.data.nbytes)   # the merged CSR as copied back
     return dict(t=t, steps=steps, value=work_per_step * steps * world / t, h2d=h2d, d2h=d2h, W=W,
                 diameter=int(r.diameter))
 

@@ -133,5 +133,7 @@ def component_wise_closure(A, method: str = "auto", densify_threshold: int = 500
     ij = to_device(np.ascontiguousarray(csr.indices), dev).to(torch.int32)
     iv = to_device(np.ascontiguousarray(csr.data).astype(np.int32, copy=False), dev)
     oi, oj, ov, diameter, _ = component_closure_device(ip, ij, iv, n, method, densify_threshold)
+    if ov.numel() < 2**31 - 1:   # int32 row pointers when they fit: scipy keeps the arrays as given
+        oi = oi.to(torch.int32)
     W = sp.csr_matrix((to_host_pinned(ov), to_host_pinned(oj), to_host_pinned(oi)), shape=(n, n))
     return TransitiveClosure(W, int(diameter))
