@@ -230,14 +230,13 @@ def int32_peak_ops(device_index: int, sm_max_mhz):
     return sms * 128 * mhz * 1e6, sms
 
 
-def tile_traffic_per_launch():
-    p = ROOT / "profiles" / "fw_tile_traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text()).get("bytes_per_launch")
-        except (ValueError, OSError):
-            return None
-    return None
+def phase_traffic():
+    """DRAM bytes per launch of the phase kernels, from the committed ncu capture summary."""
+    p = ROOT / "profiles" / "fw_phase_traffic.txt"
+    try:
+        return json.loads(p.read_text())
+    except (ValueError, OSError):
+        return None
 
 
 def profile_kernels(fn):
@@ -624,24 +623,33 @@ def main():
             "config": config(f"inputs larger than L2: {r['bytes'] / 1e9:.1f} GB resident per step", w),
             "gpu_launches": int(r["launches"]), "clocks": r["clocks"]}
     # roofline of the dominant kernel (phase-3 tile kernel): int32 lane operations
-    tms, tn = r["kprof"]["fw_tile_kernel"]
+    # roofline of the closure proper: the three phase kernels of every round (diagonal, panels,
+    # tiles) issue all executed relaxations; int32 lane operations against the nominal peak
+    kp = r["kprof"]
+    phase_ms = sum(kp[k][0] for k in ("fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel")) / args.steps
     peak, sms = int32_peak_ops(0, r["clocks"].get("sm_max_mhz"))
-    tile_relax_per_step = r["executed"]
+    tr = phase_traffic()
+    traffic = None
+    if tr:
+        traffic = sum(tr["bytes_per_launch"][k] * kp[k][1] / args.steps for k in tr["bytes_per_launch"] if k in kp)
     line["roofline"] = {
-        "bound": "int32_alu", "unit": "Tops/s",
+        "bound": "int32_alu", "unit": "Tops/s", "kernel": "fw_diag_kernel + fw_panel_kernel + fw_tile_kernel",
         "achieved": None, "peak": peak / 1e12, "frac": None,
-        "traffic": tile_traffic_per_launch(),
+        "traffic": traffic, "traffic_unit": "DRAM bytes per step of the three phase kernels "
+                                            "(per-launch bytes from profiles/fw_phase_traffic.txt x launches)",
         "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock",
         "ops_per_relaxation": 2,
-        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in r["kprof"].items()},
-        "kernel_launches_per_step": {k: v[1] / args.steps for k, v in r["kprof"].items()},
-        "executed_relaxations_per_step": tile_relax_per_step,
+        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kp.items()},
+        "kernel_launches_per_step": {k: v[1] / args.steps for k, v in kp.items()},
+        "executed_relaxations_per_step": r["executed"],
         "algorithmic_relaxations_per_step": r["work"],
     }
-    if tms > 0:
-        ach = tile_relax_per_step * 2 / (tms / args.steps / 1e3) / 1e12
+    if phase_ms > 0:
+        ach = r["executed"] * 2 / (phase_ms / 1e3) / 1e12
         line["roofline"]["achieved"] = ach
         line["roofline"]["frac"] = ach / (peak / 1e12)
+        if traffic:
+            line["roofline"]["dram_gb_s"] = traffic / (phase_ms / 1e3) / 1e9
     e = r["e2e"]
     line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                    "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["t"] / e["steps"] * 1e3,
