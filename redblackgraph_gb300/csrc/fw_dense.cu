@@ -311,14 +311,18 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
 
     // ---- line masks of this tile's rows and columns; their ORs give the active steps
     for (int e = tid; e < BM + BN; e += FW_THREADS) {
-        unsigned long long m = 0;
+        // the line mask and its group mask are loaded together; a line of a group without
+        // snapshots this round counts as zero
+        unsigned long long m;
         if (e < BM) {
             const int64_t i = I0 + e;
-            if (gmC[i / FW_B]) m = lmC[i];
+            const unsigned long long lm = lmC[i], gm = gmC[i / FW_B];
+            m = gm ? lm : 0ull;
             S.maskC[e] = m;
         } else {
             const int64_t j = J0 + (e - BM);
-            if (gmR[j / FW_B]) m = lmR[j];
+            const unsigned long long lm = lmR[j], gm = gmR[j / FW_B];
+            m = gm ? lm : 0ull;
             S.maskR[e - BM] = m;
         }
         const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)m);
@@ -337,6 +341,35 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         S.qof[tid] = on ? q : -1;
     }
     __syncthreads();
+
+    // ---- accumulators (loaded first, so that they are in flight with the staging loads)
+    const int ty = tid / TX, tx = tid % TX;
+    const int r0 = ty * TM;
+    int cidx[TN];
+#pragma unroll
+    for (int c = 0; c < TN; ++c) cidx[c] = (c < HN) ? tx * HN + c : BN / 2 + tx * HN + (c - HN);
+    U acc[TM][TN];
+    unsigned long long wasInf = 0;
+    unsigned rowWork = 0;   // bit r: row r0 + r has a nonzero operand at some active step
+#pragma unroll
+    for (int r = 0; r < TM; ++r) rowWork |= (unsigned)((S.maskC[r0 + r] & act) != 0) << r;
+    static_assert(HN * sizeof(U) == 16, "each column group is one 16-byte vector");
+#pragma unroll
+    for (int r = 0; r < TM; ++r) {
+        if (!((rowWork >> r) & 1u)) continue;       // cannot change: neither read nor written
+        const U *row = work + (I0 + r0 + r) * np + J0;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            uint4 v4 = *reinterpret_cast<const uint4 *>(row + cidx[half * HN]);
+            const U *w = reinterpret_cast<const U *>(&v4);
+#pragma unroll
+            for (int k = 0; k < HN; ++k) {
+                const int c = half * HN + k;
+                acc[r][c] = w[k];
+                wasInf |= (unsigned long long)(!L::valid(w[k])) << (r * TN + c);
+            }
+        }
+    }
 
     // ---- stage the active steps' panel snapshots (dead 64-line groups read as zero)
     {
@@ -382,35 +415,6 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         mc = __reduce_max_sync(0xffffffffu, mc);
         mr = __reduce_max_sync(0xffffffffu, mr);
         if (mc >= 0 && mr >= 0 && mc + mr >= lbits - 1) risk = true;
-    }
-
-    // ---- accumulators
-    const int ty = tid / TX, tx = tid % TX;
-    const int r0 = ty * TM;
-    int cidx[TN];
-#pragma unroll
-    for (int c = 0; c < TN; ++c) cidx[c] = (c < HN) ? tx * HN + c : BN / 2 + tx * HN + (c - HN);
-    U acc[TM][TN];
-    unsigned long long wasInf = 0;
-    unsigned rowWork = 0;   // bit r: row r0 + r has a nonzero operand at some active step
-#pragma unroll
-    for (int r = 0; r < TM; ++r) rowWork |= (unsigned)((S.maskC[r0 + r] & act) != 0) << r;
-    static_assert(HN * sizeof(U) == 16, "each column group is one 16-byte vector");
-#pragma unroll
-    for (int r = 0; r < TM; ++r) {
-        if (!((rowWork >> r) & 1u)) continue;       // cannot change: neither read nor written
-        const U *row = work + (I0 + r0 + r) * np + J0;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            uint4 v4 = *reinterpret_cast<const uint4 *>(row + cidx[half * HN]);
-            const U *w = reinterpret_cast<const U *>(&v4);
-#pragma unroll
-            for (int k = 0; k < HN; ++k) {
-                const int c = half * HN + k;
-                acc[r][c] = w[k];
-                wasInf |= (unsigned long long)(!L::valid(w[k])) << (r * TN + c);
-            }
-        }
     }
 
     unsigned steps_done = 0;

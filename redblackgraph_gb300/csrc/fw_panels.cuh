@@ -7,7 +7,7 @@
 //       rs(t, b) = d_{t-1}(t, b)   (row t as step t reads it), stored split as (2^msb, low)
 //   with per-step maxima of msb (for the exact top-bit test) and validity masks.
 // Phase 2 (fw_panel_kernel, 64 panel columns or rows per CTA): each panel column (row panel) or
-//   row (column panel) is held in registers by four lanes and runs its forward substitution
+//   row (column panel) is held in registers by PN_LANES lanes and runs its forward substitution
 //       P(a, j) <- P(a, j) (+) cs[t][a] (x) P(t, j)      (row panel, t = K0..K0+63)
 //       P(i, b) <- P(i, b) (+) P(i, t) (x) rs(t, b)      (column panel)
 //   storing the step-t operands P(t, j) / P(i, t) (the phase-3 snapshots) t-major.
@@ -160,12 +160,27 @@ fw_diag_kernel(U *__restrict__ work_base, unsigned long long *__restrict__ any_b
 }
 
 // ------------------------------------------------------------------------------ phase 2
-// Four lanes of a warp share one panel column (row panel) or row (column panel), 16 cells
-// each.  The step-t operand P(t, j) / P(i, t) lives in lane h = t / 16 of the group and is
-// broadcast with a shuffle, so the 64 steps need no barrier.  Steps run in fully unrolled
-// blocks of 16, keeping every register index static.
+// PN_LANES lanes of a warp share one panel column (row panel) or row (column panel),
+// PN_CELLS cells each.  The step-t operand P(t, j) / P(i, t) lives in lane h = t / PN_CELLS of
+// the group and is broadcast with a shuffle, so the 64 steps need no barrier.  Steps run in
+// fully unrolled blocks of PN_CELLS, keeping every register index static.
 constexpr int PN_LINES = 64;                      // panel columns / rows per CTA
-constexpr int PN_THREADS = PN_LINES * 4;
+constexpr int PN_CELLS = 16;                      // cells of a line held by one lane
+constexpr int PN_LANES = FW_B / PN_CELLS;         // lanes per line
+constexpr int PN_THREADS = PN_LINES * PN_LANES;
+
+// N consecutive lane words from 16-byte aligned memory
+template <typename U, int N> __device__ __forceinline__ void loadN(const U *p, U (&x)[N]) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+    constexpr int PER = 16 / sizeof(U);
+#pragma unroll
+    for (int i = 0; i < N / PER; ++i) {
+        uint4 v = q[i];
+        const U *w = reinterpret_cast<const U *>(&v);
+#pragma unroll
+        for (int k = 0; k < PER; ++k) x[i * PER + k] = w[k];
+    }
+}
 
 template <typename U> struct PanelSmem {
     U TA[FW_B][Pad<U>::LD];           // row panel: cs[t][a]; column panel: rsm[t][b] (padded)
@@ -216,38 +231,36 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     const int cta = rowPanel ? local : local - nct;
 
     const int lanei = tid & 31;
-    const int h = lanei & 3;                          // cells h*16 .. h*16+15 of the line
-    const int grp = lanei & ~3;                       // first lane of this line's group
-    const int64_t g = (int64_t)cta * PN_LINES + (tid >> 2);   // global column / row
+    const int h = lanei & (PN_LANES - 1);             // cells h*PN_CELLS .. of the line
+    const int grp = lanei & ~(PN_LANES - 1);          // first lane of this line's group
+    const int line = tid / PN_LANES;
+    const int64_t g = (int64_t)cta * PN_LINES + line; // global column / row
     const bool inK = g >= K0 && g < K0 + FW_B;        // the diagonal tile's own cells
-    const int c0 = h * DG_ROWS;
+    const int c0 = h * PN_CELLS;
+    constexpr unsigned ALL_INF = (1u << PN_CELLS) - 1u;
     bool risk = false;
     unsigned steps_done = 0;                          // steps this warp did not skip
     unsigned long long seen = 0;                      // bit t: the step-t operand is valid
     unsigned startInf = 0;                            // bit r: cell r was zero at round start
-    U R[DG_ROWS];
+    U R[PN_CELLS];
     U *rowp = work + g * np + K0 + c0;                // column panel: this thread's cells
     if (inK) {
 #pragma unroll
-        for (int r = 0; r < DG_ROWS; ++r) R[r] = L::inf;
+        for (int r = 0; r < PN_CELLS; ++r) R[r] = L::inf;
     } else if (rowPanel) {
 #pragma unroll
-        for (int r = 0; r < DG_ROWS; ++r) R[r] = work[(K0 + c0 + r) * np + g];
+        for (int r = 0; r < PN_CELLS; ++r) R[r] = work[(K0 + c0 + r) * np + g];
     } else {
-        load16<U>(rowp, R);   // 16-byte aligned: K0 and c0 are multiples of 16
+        loadN<U, PN_CELLS>(rowp, R);   // 16-byte aligned: K0 and c0 are multiples of 8 words
     }
 #pragma unroll
-    for (int r = 0; r < DG_ROWS; ++r) startInf |= (unsigned)(!L::valid(R[r])) << r;
-    // 64 lines that are all zero stay zero this round: no snapshots, no write-back, and the
-    // group flag stays 0 so the tile kernel reads none of them
-    if (!__syncthreads_or(startInf != (1u << DG_ROWS) - 1u)) return;
-
-    if (tid == 0) S.any = 0;
+    for (int r = 0; r < PN_CELLS; ++r) startInf |= (unsigned)(!L::valid(R[r])) << r;
+    // the pivot tables are loaded before the all-zero test so that both loads are in flight
+    // together (batched 16-byte loads; the shared-memory stores follow the test)
+    constexpr int PER = 16 / sizeof(U);
+    constexpr int NV = FW_B * FW_B / PER / PN_THREADS;   // vectors per table per thread
+    uint4 va[NV], vb[NV];
     {
-        // batched 16-byte loads first, then the shared-memory stores (no serial round trips)
-        constexpr int PER = 16 / sizeof(U);
-        constexpr int NV = FW_B * FW_B / PER / PN_THREADS;   // vectors per table per thread
-        uint4 va[NV], vb[NV];
         const uint4 *ta = reinterpret_cast<const uint4 *>(rowPanel ? &rb->cs[0][0] : &rb->rsm[0][0]);
         const uint4 *tb = reinterpret_cast<const uint4 *>(&rb->rsl[0][0]);
 #pragma unroll
@@ -255,6 +268,13 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
             va[i] = ta[tid + i * PN_THREADS];
             if (!rowPanel) vb[i] = tb[tid + i * PN_THREADS];
         }
+    }
+    // 64 lines that are all zero stay zero this round: no snapshots, no write-back, and the
+    // group flag stays 0 so the tile kernel reads none of them
+    if (!__syncthreads_or(startInf != ALL_INF)) return;
+
+    if (tid == 0) S.any = 0;
+    {
         U *da = &S.TA[0][0];
         U *db = &S.RSl[0][0];
 #pragma unroll
@@ -277,43 +297,43 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     const U *tabA = &S.TA[0][pc0];
     const U *tabB = &S.RSl[0][pc0];
     bool changed = false;                             // some cell of this thread decreased
-    if (__all_sync(0xffffffffu, startInf == (1u << DG_ROWS) - 1u)) {
-        // the warp's 8 lines are all zero: they stay zero (a line only meets its own cells as
+    if (__all_sync(0xffffffffu, startInf == ALL_INF)) {
+        // the warp's lines are all zero: they stay zero (a line only meets its own cells as
         // step operands), so only their snapshots are written, as zeros
 #pragma unroll
-        for (int l = 0; l < DG_ROWS; ++l) S.Z[h * DG_ROWS + l][tid >> 2] = L::inf;
+        for (int l = 0; l < PN_CELLS; ++l) S.Z[h * PN_CELLS + l][line] = L::inf;
     } else {
-        for (int T = 0; T < FW_B / DG_ROWS; ++T) {
+        for (int T = 0; T < PN_LANES; ++T) {
 #pragma unroll
-            for (int l = 0; l < DG_ROWS; ++l) {
-                const int t = T * DG_ROWS + l;
+            for (int l = 0; l < PN_CELLS; ++l) {
+                const int t = T * PN_CELLS + l;
                 const U z = shfl_lane<U>(R[l], grp | T);  // P(t, j) or P(i, t): invariant at step t
                 const bool zv = L::valid(z);
                 seen |= (unsigned long long)zv << t;
-                if (h == 0) S.Z[t][tid >> 2] = z;
+                if (h == 0) S.Z[t][line] = z;
                 // a zero step operand makes every product of the step a zero: skip the step when
                 // it is zero for the whole warp (closures of family trees are sparse); operands
                 // are read only for the steps that run
                 if (!__any_sync(0xffffffffu, zv)) continue;
                 ++steps_done;
-                U xa[DG_ROWS];
-                load16<U>(tabA + t * Pad<U>::LD, xa);
+                U xa[PN_CELLS];
+                loadN<U, PN_CELLS>(tabA + t * Pad<U>::LD, xa);
                 if (rowPanel) {
                     U m, low;
                     L::split(z, m, low);
                     if (zv && S.msbCS[t] + msb_nz<U>(z) >= lbits - 1) risk = true;
 #pragma unroll
-                    for (int r = 0; r < DG_ROWS; ++r) {
+                    for (int r = 0; r < PN_CELLS; ++r) {
                         const U v = umin(R[r], xa[r] * m + low);
                         changed |= v != R[r];
                         R[r] = v;
                     }
                 } else {
-                    U xb[DG_ROWS];
-                    load16<U>(tabB + t * Pad<U>::LD, xb);
+                    U xb[PN_CELLS];
+                    loadN<U, PN_CELLS>(tabB + t * Pad<U>::LD, xb);
                     if (zv && msb_nz<U>(z) + S.msbRS[t] >= lbits - 1) risk = true;
 #pragma unroll
-                    for (int r = 0; r < DG_ROWS; ++r) {
+                    for (int r = 0; r < PN_CELLS; ++r) {
                         const U v = umin(R[r], z * xa[r] + xb[r]);
                         changed |= v != R[r];
                         R[r] = v;
@@ -340,7 +360,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     SU smx = 0;
     bool wrote = false;
 #pragma unroll
-    for (int r = 0; r < DG_ROWS; ++r) {
+    for (int r = 0; r < PN_CELLS; ++r) {
         const U v = R[r];
         const bool vv = L::valid(v);
         const int c = c0 + r;
@@ -353,7 +373,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
             const unsigned long long both = seen & (rowPanel ? S.maskCS[c] : S.maskRS[c]);
             const int tf = __ffsll((long long)both) - 1;
             U first;
-            const U zf = S.Z[tf][tid >> 2];
+            const U zf = S.Z[tf][line];
             if (rowPanel) {
                 U m, low;
                 L::split(zf, m, low);
@@ -365,7 +385,7 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
         }
     }
     if ((tid & 31) == 0 && steps_done)
-        atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * DG_ROWS);
+        atomicAdd(&st->executed, (unsigned long long)steps_done * 32 * PN_CELLS);
     if (h == 0) (rowPanel ? lineRP : lineCP)[g] = seen;
     if (tid == 0) (rowPanel ? anyRP : anyCP)[cta] = anyMask;
     if (wrote) {
