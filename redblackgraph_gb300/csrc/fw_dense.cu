@@ -536,7 +536,8 @@ template <typename T, typename U>
 __global__ void __launch_bounds__(FW_THREADS)
 fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_base,
                    T *__restrict__ out_base, const FwComp *__restrict__ comps,
-                   const int64_t *__restrict__ prefix, int count, const DevStatus *st_base) {
+                   const int64_t *__restrict__ prefix, int count, const DevStatus *st_base,
+                   const unsigned char *__restrict__ occ_base) {
     const int ci = fw_find(prefix, count, blockIdx.x);
     const FwComp c = comps[ci];
     // a component that needs another path keeps its input untouched (it may be in place)
@@ -547,12 +548,18 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
     T *out = out_base + c.out_off;
     const int64_t n = c.n, np = c.np;
     const int64_t r0 = ((int64_t)blockIdx.x - prefix[ci]) * CONV_ROWS;
+    // a 64 x 64 block that never held a valid value is all zero: its lanes are not read
+    const unsigned char *occ = occ_base + c.occ_off;
+    const int64_t nb = np / FW_B;
     for (int64_t i = r0; i < r0 + CONV_ROWS && i < n; ++i) {
         const U *wrow = work + i * np;
+        const unsigned char *orow = occ + (i / FW_B) * nb;
         for (int64_t j = threadIdx.x; j < n; j += FW_THREADS) {
             T v;
             if (i == j || (c.triangular && i > j)) {
                 v = in[i * c.ld_in + j];
+            } else if (!orow[j / FW_B]) {
+                v = (T)0;
             } else {
                 const U w = wrow[j];
                 v = lane<U>::valid(w) ? (T)w : (T)0;
@@ -939,7 +946,7 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     {
         cudaEvent_t tf = timer_begin(3, stream);
         fw_finalize_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
-            in, lanes, out, comps, pconv, cnt, st);
+            in, lanes, out, comps, pconv, cnt, st, occ);
         timer_end(3, tf, stream);
     }
     RBG_CUDA_TRY(cudaGetLastError());

@@ -260,6 +260,14 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     constexpr int PER = 16 / sizeof(U);
     constexpr int NV = FW_B * FW_B / PER / PN_THREADS;   // vectors per table per thread
     uint4 va[NV], vb[NV];
+    unsigned long long mcs = 0, mrs = 0;
+    int bcs = 0, brs = 0;
+    if (tid < FW_B) {
+        mcs = rb->maskCS[tid];
+        mrs = rb->maskRS[tid];
+        bcs = rb->msbCS[tid];
+        brs = rb->msbRS[tid];
+    }
     {
         const uint4 *ta = reinterpret_cast<const uint4 *>(rowPanel ? &rb->cs[0][0] : &rb->rsm[0][0]);
         const uint4 *tb = reinterpret_cast<const uint4 *>(&rb->rsl[0][0]);
@@ -286,10 +294,10 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
         }
     }
     if (tid < FW_B) {
-        S.maskCS[tid] = rb->maskCS[tid];
-        S.maskRS[tid] = rb->maskRS[tid];
-        S.msbCS[tid] = rb->msbCS[tid];
-        S.msbRS[tid] = rb->msbRS[tid];
+        S.maskCS[tid] = mcs;
+        S.maskRS[tid] = mrs;
+        S.msbCS[tid] = bcs;
+        S.msbRS[tid] = brs;
     }
     __syncthreads();
 
