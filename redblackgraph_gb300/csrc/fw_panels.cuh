@@ -312,6 +312,21 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
         for (int l = 0; l < PN_CELLS; ++l) S.Z[h * PN_CELLS + l][line] = L::inf;
     } else {
         for (int T = 0; T < PN_LANES; ++T) {
+            // the step operands of block T are lane T's cells; if they are all zero for every
+            // line of the warp at the block's start, no step of the block updates anything (an
+            // update needs a valid step operand), so they stay zero: skip the block
+            bool mine = false;
+            if (h == T) {
+#pragma unroll
+                for (int r = 0; r < PN_CELLS; ++r) mine |= L::valid(R[r]);
+            }
+            if (!__any_sync(0xffffffffu, mine)) {
+                if (h == T) {
+#pragma unroll
+                    for (int l = 0; l < PN_CELLS; ++l) S.Z[T * PN_CELLS + l][line] = R[l];
+                }
+                continue;
+            }
 #pragma unroll
             for (int l = 0; l < PN_CELLS; ++l) {
                 const int t = T * PN_CELLS + l;
