@@ -199,14 +199,18 @@ fw_convert_kernel(const T *__restrict__ in_base, U *__restrict__ work_base,
     const unsigned long long llimit = 1ull << (lbits - 1);   // effective lane top bit
     unsigned flags = 0;
     unsigned long long mx = 0;
+    // one warp per row (CONV_ROWS = 8 warps): small components keep every lane busy
+    static_assert(CONV_ROWS * 32 == FW_THREADS, "one warp per converted row");
     const int64_t r0 = ((int64_t)blockIdx.x - prefix[ci]) * CONV_ROWS;
-    for (int64_t i = r0; i < r0 + CONV_ROWS && i < np; ++i) {
+    const int64_t i = r0 + (threadIdx.x >> 5);
+    const int lane_id = threadIdx.x & 31;
+    if (i < np) {
         // W(i, 0) for the k = 0 product of d_0 (row 0 / column 0 products are identities)
         const bool rowlive = i < n;
         const TU wi0 = (rowlive && i > 0 && !triangular) ? (TU)in[i * ld] : (TU)0;
         const bool xi = wi0 != 0 && wi0 != 1 && wi0 != tmax && (unsigned long long)wi0 < llimit;
         U *wrow = work + i * np;
-        for (int64_t j0 = (int64_t)threadIdx.x * 4; j0 < np; j0 += (int64_t)FW_THREADS * 4) {
+        for (int64_t j0 = (int64_t)lane_id * 4; j0 < np; j0 += 32 * 4) {
             U w4[4];
             bool live = false;
 #pragma unroll
@@ -551,10 +555,11 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
     // a 64 x 64 block that never held a valid value is all zero: its lanes are not read
     const unsigned char *occ = occ_base + c.occ_off;
     const int64_t nb = np / FW_B;
-    for (int64_t i = r0; i < r0 + CONV_ROWS && i < n; ++i) {
+    const int64_t i = r0 + (threadIdx.x >> 5);   // one warp per row
+    if (i < n) {
         const U *wrow = work + i * np;
         const unsigned char *orow = occ + (i / FW_B) * nb;
-        for (int64_t j = threadIdx.x; j < n; j += FW_THREADS) {
+        for (int64_t j = threadIdx.x & 31; j < n; j += 32) {
             T v;
             if (i == j || (c.triangular && i > j)) {
                 v = in[i * c.ld_in + j];
