@@ -256,6 +256,7 @@ def profile_kernels(fn):
 def run_ours(args, rank, world, w):
     import torch
     import torch.distributed as dist
+    from redblackgraph_gb300.sharding import max_over_ranks
     from redblackgraph_gb300 import _lib
     from redblackgraph_gb300.dense import fw_batch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
@@ -294,10 +295,7 @@ def run_ours(args, rank, world, w):
     kprof = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True))
     kprof = {k: (v[0] * args.steps, v[1] * args.steps) for k, v in kprof.items()}
     t = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(t, dev)          # the slowest rank's time (weak scaling)
     clocks = clk.summary()
     res = dict(t=t, work=work_per_step, executed=executed, kprof=kprof, launches=launches,
                clocks=clocks, out=out, offsets=offsets, bytes=buf.numel() * 4)
@@ -307,6 +305,7 @@ def run_ours(args, rank, world, w):
 
 
 def run_e2e(args, rank, world, w, dev, work_per_step):
+    from redblackgraph_gb300.sharding import max_over_ranks
     """The same closure through the public API with host buffers: component_wise_closure on the
     forest held in pinned host memory (H2D of the CSR, component split, densify, batched
     closure, compaction, D2H of the merged CSR inside every timed step)."""
@@ -342,10 +341,7 @@ def run_e2e(args, rank, world, w, dev, work_per_step):
     e1.record(stream)
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(t, dev)          # the slowest rank's time (weak scaling)
     W = r.W
     d2h = int(W.indptr.nbytes + W.indices.nbytes + W.data.nbytes)   # the merged CSR as copied back
     return dict(t=t, steps=steps, value=work_per_step * steps * world / t, h2d=h2d, d2h=d2h, W=W,
