@@ -227,6 +227,16 @@ int32_t rbg_csr_merge_count(const rbg_csr_t *X, const rbg_csr_t *Y, void *head, 
 int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, const void *head, int64_t *indptr,
                            int32_t *indices, int32_t *data, rbg_stream_t stream);
 
+/*
+ * Diameter source of the sparse DAG closure: the largest magnitude among the stored entries of A
+ * and the candidates A[v][w] (x) C[w][x] (w != v, x over row w of the closure C, Cython int32
+ * product), as redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:262-305 keeps it
+ * (candidates that lose the (+) included).  int32 values; `workspace` needs 8 bytes; *max_abs
+ * (host) receives the maximum.  Synchronises `stream`.
+ */
+int32_t rbg_dag_candidate_max(const rbg_csr_t *A, const rbg_csr_t *C, void *workspace,
+                              int64_t workspace_bytes, int64_t *max_abs, rbg_stream_t stream);
+
 /* Scratch bytes rbg_avos_matmul needs. */
 int32_t rbg_avos_matmul_workspace_bytes(int32_t dtype, int64_t m, int64_t q, int64_t p,
                                         int64_t *bytes);

@@ -325,3 +325,111 @@ def calculate_relationship(a, b):
     if removal == 0:
         return bj, cousinth(g)
     return bj, f"{cousinth(g)} {removal} removed"
+
+
+def _cy_msb(x: int) -> int:
+    p = 0
+    while x > 1:
+        x >>= 1
+        p += 1
+    return p
+
+
+def _i32(v: int) -> int:
+    v &= 0xffffffff
+    return v - (1 << 32) if v >= (1 << 31) else v
+
+
+def cy_product_py(lhs: int, rhs: int) -> int:
+    """The Cython avos_product on int32 (redblackgraph/sparse/csgraph/_rbg_math.pxi:33-87)."""
+    x, y = lhs & 0xffffffff, rhs & 0xffffffff
+    if x == 0 or y == 0:
+        return 0
+    if lhs == -1 and rhs == -1:
+        return -1
+    if lhs == 1 and rhs == 1:
+        return 1
+    if (lhs == -1 and rhs == 1) or (lhs == 1 and rhs == -1):
+        return 0
+    if lhs == -1:
+        x = 1
+    if rhs == -1:
+        return 0 if lhs & 1 else _i32(x)
+    if rhs == 1:
+        return _i32(x) if lhs & 1 else 0
+    bp = _cy_msb(_i32(y))
+    low = 0 if bp == 0 else (y & ((1 << bp) - 1))
+    return _i32(low | (x << bp))
+
+
+def cy_sum_py(x: int, y: int) -> int:
+    """The Cython avos_sum on int32 (_rbg_math.pxi:18-31): the non-zero minimum, signed."""
+    if x == 0:
+        return y
+    if y == 0:
+        return x
+    return x if x < y else y
+
+
+def dag_closure(a):
+    """transitive_closure_dag_sparse_cython (redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:
+    168-351), restated for small graphs: rows built parents first, each parent's closed row
+    multiplied in by the edge value, candidates folded with the Cython sum; the diameter is MSB of
+    the largest magnitude of any stored entry or candidate.  Returns ``(W csr int32, diameter)``;
+    raises ValueError on a cycle."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix(a)
+    A.sum_duplicates()
+    A.sort_indices()
+    n = A.shape[0]
+    ip, ij = A.indptr, A.indices
+    dv = np.asarray(A.data).astype(np.int64)
+    dv = np.array([_i32(int(v)) for v in dv], dtype=np.int64)
+    # parents first: Kahn's order on the edges v -> w (w != v)
+    deg = np.zeros(n, dtype=np.int64)
+    children = [[] for _ in range(n)]
+    for v in range(n):
+        for e in range(ip[v], ip[v + 1]):
+            w = int(ij[e])
+            if w != v:
+                deg[v] += 1
+                children[w].append(v)
+    order, ready = [], [v for v in range(n) if deg[v] == 0]
+    while ready:
+        w = ready.pop()
+        order.append(w)
+        for v in children[w]:
+            deg[v] -= 1
+            if deg[v] == 0:
+                ready.append(v)
+    if len(order) != n:
+        raise ValueError("graph contains a cycle")
+    rows = [None] * n
+    mx = 0
+    for v in order:
+        row = {}
+        for e in range(ip[v], ip[v + 1]):
+            w, val = int(ij[e]), int(dv[e])
+            row[w] = cy_sum_py(row[w], val) if w in row else val
+            mx = max(mx, abs(val) if val != -(1 << 31) else 0)
+        for e in range(ip[v], ip[v + 1]):
+            w, a_vw = int(ij[e]), int(dv[e])
+            if w == v:
+                continue
+            for x, c in rows[w].items():
+                p = cy_product_py(a_vw, c)
+                if p == 0:
+                    continue
+                row[x] = cy_sum_py(row[x], p) if x in row else p
+                mx = max(mx, abs(p) if p != -(1 << 31) else 0)
+        rows[v] = row
+    r_, c_, v_ = [], [], []
+    for v in range(n):
+        for x in sorted(rows[v]):
+            r_.append(v)
+            c_.append(x)
+            v_.append(rows[v][x])
+    W = sp.csr_matrix((np.array(v_, dtype=np.int32), (np.array(r_, dtype=np.int64), np.array(c_, dtype=np.int64))),
+                      shape=(n, n))
+    W.sort_indices()
+    return W, (_cy_msb(mx) if mx > 1 else 0)

@@ -962,3 +962,60 @@ extern "C" int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, co
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// Largest candidate of the DAG closure (the value its diameter is taken from)
+// ------------------------------------------------------------------------------------------
+// The reference's sparse DAG closure (redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:
+// 262-305) builds row v from each parent w != v as A[v][w] (x) C[w][x] over w's closed row and
+// keeps the largest magnitude of every such candidate, including those that lose the (+), and
+// of every stored entry of A.  Given the closure C, one warp per row of A recomputes the
+// candidates (Cython int32 product, magnitudes in int32) and keeps their maximum.
+namespace rbg {
+__global__ void dag_cand_max_kernel(int64_t n, const int64_t *ap, const int *aj, const int *ax,
+                                    const int64_t *cp, const int *cj, const int *cx,
+                                    unsigned long long *out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    int best = 0;
+    for (int64_t v = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < n; v += warps) {
+        for (int64_t e = ap[v]; e < ap[v + 1]; ++e) {
+            const int w = aj[e], a = ax[e];
+            if (lane == 0) {                      // the stored entry itself
+                const int m = a > 0 ? a : (int)(0u - (unsigned)a);
+                best = max(best, m);
+            }
+            if (w == (int)v || w < 0 || w >= n) continue;
+            for (int64_t f = cp[w] + lane; f < cp[w + 1]; f += 32) {
+                const int p = cy_product(a, cx[f]);
+                if (p == 0) continue;
+                const int m = p > 0 ? p : (int)(0u - (unsigned)p);   // int32 magnitude, as -val
+                best = max(best, m);
+            }
+        }
+    }
+    best = __reduce_max_sync(0xffffffffu, best);
+    if (lane == 0 && best > 0) atomicMax(out, (unsigned long long)best);
+}
+}  // namespace rbg
+
+extern "C" int32_t rbg_dag_candidate_max(const rbg_csr_t *A, const rbg_csr_t *C, void *workspace,
+                                         int64_t workspace_bytes, int64_t *max_abs, rbg_stream_t stream) {
+    if (!csr_ok(A) || !csr_ok(C) || !workspace || workspace_bytes < 8 || !max_abs) return RBG_ERR_INVALID;
+    if (A->n_rows != A->n_cols || C->n_rows != A->n_rows) return RBG_ERR_INVALID;
+    const int64_t n = A->n_rows;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long *d = reinterpret_cast<unsigned long long *>(workspace);
+    RBG_CUDA_TRY(cudaMemsetAsync(d, 0, 8, s));
+    if (n > 0) {
+        note_launches(1);
+        dag_cand_max_kernel<<<grid_of(n * 32, 256), 256, 0, s>>>(n, A->indptr, A->indices, (const int *)A->data,
+                                                                C->indptr, C->indices, (const int *)C->data, d);
+        RBG_CUDA_TRY(cudaGetLastError());
+    }
+    unsigned long long h = 0;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    *max_abs = (int64_t)h;
+    return RBG_OK;
+}

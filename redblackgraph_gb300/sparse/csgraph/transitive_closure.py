@@ -44,7 +44,7 @@ def _as_csr(A):
     return A.tocsr() if not isinstance(A, sp.csr_matrix) else A
 
 
-def _squaring(csr, max_iterations, cycle_error):
+def _squaring(csr, max_iterations, cycle_error, dag_candidates=False):
     """R <- R (+) R^2 on the GPU until R is stable; returns (rb_matrix int32, max |value|)."""
     import torch
     from ...spgemm import DeviceCSR, spgemm, SEM_C64
@@ -73,21 +73,43 @@ def _squaring(csr, max_iterations, cycle_error):
         R = DeviceCSR(R.indptr, R.indices, R.data.to(torch.int32), R.shape)
     mx_abs = int(R.data.abs().max().item()) if R.nnz else 0
     mx = int(R.data.max().item()) if R.nnz else 0
+    if dag_candidates:
+        mx = _dag_candidate_max(a, R)
     out = R.to_scipy()
     return rb_matrix((out.data, out.indices.astype(np.int32), out.indptr.astype(np.int32)),
                      shape=out.shape), mx_abs, mx
 
 
+def _dag_candidate_max(a, C):
+    """Largest magnitude among A's entries and the candidates A[v][w] (x) C[w][x] (w != v) that
+    the reference's DAG closure examines (_transitive_closure_dag.pyx:262-305)."""
+    import ctypes
+    import torch
+    from ...spgemm import DeviceCSR
+    from ... import _lib
+    from ...device import stream_handle
+    A = DeviceCSR.from_scipy(a, dtype=np.int32)
+    ws = torch.empty(256, dtype=torch.uint8, device=C.indptr.device)
+    out = ctypes.c_int64(0)
+    L = _lib.load()
+    ca, cc = A.cstruct(), C.cstruct()
+    _lib.check(L.rbg_dag_candidate_max(ctypes.byref(ca), ctypes.byref(cc), ws.data_ptr(), ws.numel(),
+                                       ctypes.byref(out), stream_handle()), "dag_candidate_max")
+    return int(out.value)
+
+
 def transitive_closure_dag_sparse(A) -> TransitiveClosure:
     """Closure of a DAG (redblackgraph/sparse/csgraph/transitive_closure.py:383-438): the
-    same closure computed by GPU squaring; diameter = MSB of the largest value
-    (_transitive_closure_dag.pyx:347-349); CycleError on a cycle."""
+    same closure computed by GPU squaring; the diameter is the reference's: MSB of the largest
+    magnitude among the input's entries and every candidate A[v][w] (x) C[w][x] its
+    parent-by-parent propagation examines, including candidates that lose the (+)
+    (_transitive_closure_dag.pyx:262-305, 347-349); CycleError on a cycle."""
     import scipy.sparse as sp
     csr = _as_csr(A)
     n = csr.shape[0]
     if n == 0:
         return TransitiveClosure(sp.csr_matrix((0, 0), dtype=np.int32), 0)
-    W, mx_abs, mx = _squaring(csr, 64, cycle_error=True)
+    W, mx_abs, mx = _squaring(csr, 64, cycle_error=True, dag_candidates=True)
     return TransitiveClosure(W, (mx.bit_length() - 1) if mx > 1 else 0)
 
 

@@ -305,6 +305,21 @@ def main():
             out.append([int(u), int(v), int(rel.common_ancestor), rel.relationship])
         index["relationship"].append({"key": key, "pairs": out})
 
+    # ---------------------------------------------------------------- sparse DAG closure
+    index["dag"] = []
+    for ci, seed in enumerate([0, 1, 2, 6]):
+        M = sp.csr_matrix(synth.forest(600, 12, seed, family=60, reach=3, dtype=np.int32))
+        M.sort_indices()
+        key = f"g{ci}"
+        arrays[key + "_indptr"], arrays[key + "_indices"], arrays[key + "_data"] = M.indptr, M.indices, M.data
+        res = csgraph.transitive_closure_dag_sparse(M)
+        W = sp.csr_matrix(res.W)
+        W.sort_indices()
+        arrays[key + "_W_indptr"], arrays[key + "_W_indices"], arrays[key + "_W_data"] = W.indptr, W.indices, W.data
+        mxf = int(np.abs(W.data).max())
+        index["dag"].append({"key": key, "n": int(M.shape[0]), "diameter": int(res.diameter),
+                             "final_max_msb": (mxf.bit_length() - 1) if mxf > 1 else 0})
+
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "index.json").write_text(json.dumps(index, indent=1))
     print(f"wrote {len(arrays)} arrays, {len(index['warshall'])} warshall cases")

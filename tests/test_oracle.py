@@ -129,3 +129,17 @@ def test_oracle_relationship_vs_golden(golden):
         W = arrays[rec["key"] + "_W"]
         for u, v, ca, name in rec["pairs"]:
             assert O.calculate_relationship(W[u], W[v]) == (ca, name), (rec["key"], u, v)
+
+
+def test_oracle_dag_closure_vs_golden(golden):
+    """The DAG-closure restatement (closure and its candidate-maximum diameter) against the
+    reference's transitive_closure_dag_sparse."""
+    import scipy.sparse as sp
+    arrays, index = golden
+    for rec in index["dag"]:
+        k, n = rec["key"], rec["n"]
+        A = sp.csr_matrix((arrays[k + "_data"], arrays[k + "_indices"], arrays[k + "_indptr"]), shape=(n, n))
+        E = sp.csr_matrix((arrays[k + "_W_data"], arrays[k + "_W_indices"], arrays[k + "_W_indptr"]), shape=(n, n))
+        W, d = O.dag_closure(A)
+        assert d == rec["diameter"]
+        assert (W != E).nnz == 0

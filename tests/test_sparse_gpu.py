@@ -103,8 +103,7 @@ def test_squaring_closures_match_dense_oracle(native):
     E = _dense_closure(A)
     r = transitive_closure_squaring(A)      # lower triangular: the DAG closure
     assert same(r.W, E)
-    mx = int(E.data.max())
-    assert r.diameter == (mx.bit_length() - 1)
+    assert r.diameter == O.dag_closure(A)[1]   # the DAG closure's candidate-maximum diameter
     r2 = transitive_closure_dag_sparse(A)
     assert same(r2.W, E) and r2.diameter == r.diameter
     # a DAG that is not triangular: permute the vertices
@@ -151,3 +150,19 @@ def test_golden_dijkstra_method(native, golden):
         r = transitive_closure(sp.csr_matrix(A), method="D")
         assert (np.asarray(r.W) == arrays[rec["key"] + "_W"]).all()
         assert r.diameter == rec["diameter"]
+
+
+def test_golden_dag_closure(native, golden):
+    """transitive_closure_dag_sparse against the reference: the closure and its diameter, which
+    counts candidates that lose the (+) (in two of these forests it exceeds MSB of the largest
+    final value)."""
+    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse, transitive_closure_squaring
+    arrays, index = golden
+    for rec in index["dag"]:
+        k, n = rec["key"], rec["n"]
+        A = sp.csr_matrix((arrays[k + "_data"], arrays[k + "_indices"], arrays[k + "_indptr"]), shape=(n, n))
+        E = sp.csr_matrix((arrays[k + "_W_data"], arrays[k + "_W_indices"], arrays[k + "_W_indptr"]), shape=(n, n))
+        for fn in (transitive_closure_dag_sparse, transitive_closure_squaring):
+            r = fn(A)
+            assert same(r.W, E), (k, fn.__name__)
+            assert r.diameter == rec["diameter"], (k, fn.__name__, r.diameter, rec["diameter"])
