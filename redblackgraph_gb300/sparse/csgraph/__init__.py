@@ -7,10 +7,16 @@ from .transitive_closure import (
     transitive_closure_squaring,
     transitive_closure_dag_sparse,
     component_wise_closure,
+    transitive_closure_adaptive,
+    find_components,
+    find_components_sparse,
+    get_component_vertices,
+    DensificationError,
 )
 from .cycleerror import CycleError
 
 __all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
            "transitive_closure_floyd_warshall", "transitive_closure_dijkstra",
            "transitive_closure_squaring", "transitive_closure_dag_sparse", "component_wise_closure",
-           "CycleError"]
+           "transitive_closure_adaptive", "find_components", "find_components_sparse",
+           "get_component_vertices", "DensificationError", "CycleError"]

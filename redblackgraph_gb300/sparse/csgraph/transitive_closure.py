@@ -159,3 +159,89 @@ def component_wise_closure(A, method: str = "auto", densify_threshold: int = 500
         oi = oi.to(torch.int32)
     W = sp.csr_matrix((to_host_pinned(ov), to_host_pinned(oj), to_host_pinned(oi)), shape=(n, n))
     return TransitiveClosure(W, int(diameter))
+
+
+# ------------------------------------------------------------------------- components, dispatch
+class DensificationError(Exception):
+    """Raised when an operation would densify (redblackgraph/sparse/csgraph/_density.py:14-25)."""
+
+    def __init__(self, message: str, density: float, threshold: float):
+        self.density = density
+        self.threshold = threshold
+        super().__init__(message)
+
+
+def find_components_sparse(A, q=None) -> np.ndarray:
+    """Connected components with edges taken both ways, numbered by least vertex, on the GPU
+    (redblackgraph/sparse/csgraph/_components.pyx:86-177).  Returns uint32 labels; fills ``q``
+    (component -> vertex count) when given."""
+    import torch
+    from ...device import require_cuda, to_device, to_host
+    from ...components import label_components
+    csr = _as_csr(A)
+    n = csr.shape[0]
+    if n == 0:
+        return np.zeros(0, dtype=np.uint32)
+    dev = require_cuda()
+    ip = to_device(np.ascontiguousarray(csr.indptr), dev).to(torch.int64)
+    ij = to_device(np.ascontiguousarray(csr.indices), dev).to(torch.int32)
+    comps = label_components(ip, ij, n)
+    if q is not None:
+        q.clear()
+        q.update({c: int(s) for c, s in enumerate(comps.sizes.tolist())})
+    return to_host(comps.label[:n]).astype(np.uint32)
+
+
+def find_components(A, q=None) -> np.ndarray:
+    """Components of a dense or sparse graph (_components.pyx:12-83, 86-177)."""
+    return find_components_sparse(A, q)
+
+
+def get_component_vertices(component_labels) -> dict:
+    """component id -> its vertices, ascending (_components.pyx:326-344)."""
+    lab = np.asarray(component_labels)
+    order = np.argsort(lab, kind="stable")
+    ids, starts = np.unique(lab[order], return_index=True)
+    bounds = list(starts) + [lab.size]
+    return {int(c): order[bounds[k]:bounds[k + 1]].astype(np.int32) for k, c in enumerate(ids)}
+
+
+def transitive_closure_adaptive(A, method: str = "auto", density_threshold: float = 0.1,
+                                component_threshold: int = 1, size_threshold: int = 1000,
+                                sparse_only: bool = False) -> TransitiveClosure:
+    """The reference's strategy selection (redblackgraph/sparse/csgraph/transitive_closure.py:
+    441-574) over the GPU closures: several components -> component_wise_closure; very sparse and
+    large -> the 'D' closure; triangular -> the DAG closure; otherwise Floyd-Warshall.
+    ``sparse_only`` runs the DAG closure and turns a cycle into DensificationError."""
+    import scipy.sparse as sp
+    from .cycleerror import CycleError
+    csr = _as_csr(A)
+    n = csr.shape[0]
+    if n == 0:
+        return TransitiveClosure(sp.csr_matrix((0, 0), dtype=np.int32), 0)
+    if sparse_only:
+        try:
+            return transitive_closure_dag_sparse(csr)
+        except CycleError as e:
+            raise DensificationError(f"sparse_only=True requires a DAG, but graph contains cycles: {e}",
+                                     density=1.0, threshold=0.0)
+    if method == "FW":
+        return transitive_closure(csr, method="FW")
+    if method == "D":
+        return transitive_closure(csr, method="D")
+    if method == "component":
+        return component_wise_closure(csr)
+    if method == "squaring":
+        return transitive_closure_squaring(csr)
+    if method == "dag_sparse":
+        return transitive_closure_dag_sparse(csr)
+    q = {}
+    find_components_sparse(csr, q)
+    if len(q) > component_threshold:
+        return component_wise_closure(csr)
+    density = csr.nnz / (n * n)
+    if density < density_threshold and n > size_threshold:
+        return transitive_closure(csr, method="D")
+    if _is_upper(csr) or _is_lower(csr):
+        return transitive_closure_dag_sparse(csr)
+    return transitive_closure(csr, method="FW")

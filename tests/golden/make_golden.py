@@ -320,6 +320,35 @@ def main():
         index["dag"].append({"key": key, "n": int(M.shape[0]), "diameter": int(res.diameter),
                              "final_max_msb": (mxf.bit_length() - 1) if mxf > 1 else 0})
 
+    # ---------------------------------------------------------------- adaptive dispatch, components
+    index["adaptive"] = []
+    perm_tri = synth.pedigree_csr(120, 8, 71)
+    p = np.random.default_rng(71).permutation(120)
+    cases = [("forest", sp.csr_matrix(sp.block_diag([synth.pedigree_csr(n, 5, 72 + j) for j, n in
+                                                         enumerate([30, 12, 50])]).astype(np.int32)), {}),
+             ("tri", sp.csr_matrix(synth.pedigree_csr(150, 9, 73)), {}),
+             ("perm", sp.csr_matrix(perm_tri[p][:, p]), {}),
+             ("perm_dag", sp.csr_matrix(perm_tri[p][:, p]), {"method": "dag_sparse"}),
+             ("sparse_only_cycle", sp.csr_matrix(np.array([[-1, 2, 0], [0, 1, 3], [2, 0, -1]], dtype=np.int32)),
+              {"sparse_only": True})]
+    for ci, (name, M, kw) in enumerate(cases):
+        key = f"ad{ci}"
+        M.sort_indices()
+        arrays[key + "_indptr"], arrays[key + "_indices"], arrays[key + "_data"] = M.indptr, M.indices, M.data
+        rec = {"key": key, "name": name, "n": int(M.shape[0]), "kwargs": kw}
+        q = {}
+        arrays[key + "_labels"] = np.asarray(csgraph.find_components_sparse(M, q)).astype(np.int64)
+        rec["q"] = {str(k): int(v) for k, v in q.items()}
+        try:
+            res = csgraph.transitive_closure_adaptive(M, **kw)
+            W = sp.csr_matrix(res.W)
+            W.sort_indices()
+            arrays[key + "_W_indptr"], arrays[key + "_W_indices"], arrays[key + "_W_data"] = W.indptr, W.indices, W.data
+            rec["diameter"] = int(res.diameter)
+        except Exception as e:
+            rec["error"] = exc_name(e)
+        index["adaptive"].append(rec)
+
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "index.json").write_text(json.dumps(index, indent=1))
     print(f"wrote {len(arrays)} arrays, {len(index['warshall'])} warshall cases")

@@ -116,3 +116,26 @@ def test_cycle_in_a_later_component_raises(native):
     with pytest.raises(CycleError) as ei:
         component_wise_closure(M)
     assert ei.value.vertex == int(err[1][2])
+
+
+def test_golden_adaptive_and_component_labels(native, golden):
+    """transitive_closure_adaptive (components / DAG / Floyd-Warshall dispatch, the sparse_only
+    error) and find_components_sparse against the reference."""
+    from redblackgraph_gb300.sparse import (transitive_closure_adaptive, find_components_sparse,
+                                            DensificationError)
+    arrays, index = golden
+    for rec in index["adaptive"]:
+        k, n = rec["key"], rec["n"]
+        A = sp.csr_matrix((arrays[k + "_data"], arrays[k + "_indices"], arrays[k + "_indptr"]), shape=(n, n))
+        q = {}
+        lab = find_components_sparse(A, q)
+        assert (lab.astype(np.int64) == arrays[k + "_labels"]).all(), rec["name"]
+        assert {str(c): v for c, v in q.items()} == rec["q"]
+        if "error" in rec:
+            with pytest.raises(DensificationError):
+                transitive_closure_adaptive(A, **rec["kwargs"])
+            continue
+        r = transitive_closure_adaptive(A, **rec["kwargs"])
+        E = sp.csr_matrix((arrays[k + "_W_data"], arrays[k + "_W_indices"], arrays[k + "_W_indptr"]), shape=(n, n))
+        assert _same(r.W, E), rec["name"]
+        assert r.diameter == rec["diameter"], rec["name"]
