@@ -237,6 +237,39 @@ int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, const void *h
 int32_t rbg_dag_candidate_max(const rbg_csr_t *A, const rbg_csr_t *C, void *workspace,
                               int64_t workspace_bytes, int64_t *max_abs, rbg_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Closure of a DAG by topological levels (replaces transitive_closure_dag_sparse_cython,
+ * redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:168-351, and the level-parallel
+ * transitive_closure_dag_gpu, redblackgraph/gpu/transitive_closure.py:474-652).
+ * ---------------------------------------------------------------------------------------- */
+
+/* Scratch bytes rbg_dag_closure needs for n vertices and nnz stored entries. */
+int32_t rbg_dag_workspace_bytes(int64_t n, int64_t nnz, int64_t *bytes);
+
+/*
+ * Row v of the closure = v's stored entries (+) A[v][w] (x) C[w][.] over v's parents w != v
+ * (Cython int32 product and sum), computed level by level into a caller-provided row pool
+ * (pool_cols / pool_vals, pool_capacity entries; row v at row_off[v], row_len[v] entries,
+ * columns ascending; row_off / row_len are device arrays of n).  A is CSR with int32 values.
+ * Returns RBG_OK with *nnz (host) = entries used and *max_abs = the largest magnitude of any
+ * stored entry or candidate (the reference's diameter source); RBG_ERR_CAPACITY when the pool
+ * is too small (*nnz = a size to retry with) or a row has more than 8192 distinct columns
+ * (*nnz = -1); RBG_ERR_CYCLE when the graph has a cycle.  *levels (host) = topological
+ * levels.  Synchronises `stream` (once per level).
+ */
+int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t workspace_bytes, int32_t *pool_cols,
+                        int32_t *pool_vals, int64_t pool_capacity, int64_t *row_off, int32_t *row_len,
+                        int64_t *nnz, int64_t *max_abs, int64_t *levels, rbg_stream_t stream);
+
+/* Scratch bytes rbg_dag_gather needs. */
+int32_t rbg_dag_gather_workspace_bytes(int64_t n, int64_t *bytes);
+
+/* The pooled rows of rbg_dag_closure as CSR: indptr (n + 1, int64), indices and data (int32).
+ * Ordered on `stream`. */
+int32_t rbg_dag_gather(int64_t n, const int32_t *pool_cols, const int32_t *pool_vals, const int64_t *row_off,
+                       const int32_t *row_len, void *workspace, int64_t workspace_bytes, int64_t *indptr,
+                       int32_t *indices, int32_t *data, rbg_stream_t stream);
+
 /* Scratch bytes rbg_avos_matmul needs. */
 int32_t rbg_avos_matmul_workspace_bytes(int32_t dtype, int64_t m, int64_t q, int64_t p,
                                         int64_t *bytes);

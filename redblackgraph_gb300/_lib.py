@@ -113,6 +113,11 @@ SIGNATURES = [
     ("rbg_cc_compact_count", _I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P]),
     ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("rbg_relationship_lookup", _I32, [_I64, _P, _P, _P]),
+    ("rbg_dag_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_dag_closure", _I32, [ctypes.POINTER(RbgCsr), _P, _I64, _P, _P, _I64, _P, _P, ctypes.POINTER(_I64),
+                               ctypes.POINTER(_I64), ctypes.POINTER(_I64), _P]),
+    ("rbg_dag_gather_workspace_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
+    ("rbg_dag_gather", _I32, [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
     ("rbg_dag_candidate_max", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _I64,
                                      ctypes.POINTER(_I64), _P]),
 ]

@@ -56,11 +56,17 @@ def sparse_equal_gpu(A: CSRMatrixGPU, B: CSRMatrixGPU) -> bool:
 
 
 def transitive_closure_dag_gpu(A: CSRMatrixGPU) -> Tuple[CSRMatrixGPU, int]:
-    """Closure of a DAG; the same closure as squaring, diameter = floor(log2(max |value| > 1))
-    (redblackgraph/gpu/transitive_closure.py:474-652)."""
+    """Closure of a DAG by topological levels (redblackgraph/gpu/transitive_closure.py:474-652),
+    with the level kernels of rbg_dag_closure; diameter = floor(log2(max |value| > 1)) of the
+    closure.  Rows too wide for the level kernels take the squaring closure instead."""
+    from ..dag import RowTooWide, dag_closure_device
     n = A.shape[0]
     if n == 0 or A.nnz == 0:
         return A.copy(), 0
-    R, _ = transitive_closure_gpu(A)
+    try:
+        C, _, _ = dag_closure_device(A.device_csr())
+        R = CSRMatrixGPU.from_device_csr(C, triangular=A.triangular)
+    except RowTooWide:
+        R, _ = transitive_closure_gpu(A)
     mv = _max_non_identity(R)
     return R, (int(np.floor(np.log2(mv))) if mv > 1 else 0)

@@ -100,16 +100,28 @@ def _dag_candidate_max(a, C):
 
 def transitive_closure_dag_sparse(A) -> TransitiveClosure:
     """Closure of a DAG (redblackgraph/sparse/csgraph/transitive_closure.py:383-438): the
-    same closure computed by GPU squaring; the diameter is the reference's: MSB of the largest
-    magnitude among the input's entries and every candidate A[v][w] (x) C[w][x] its
-    parent-by-parent propagation examines, including candidates that lose the (+)
+    reference's parent-by-parent propagation, run level by level on the GPU (rbg_dag_closure);
+    the diameter is the reference's: MSB of the largest magnitude among the input's entries and
+    every candidate A[v][w] (x) C[w][x], including candidates that lose the (+)
     (_transitive_closure_dag.pyx:262-305, 347-349); CycleError on a cycle."""
     import scipy.sparse as sp
+    from ...dag import RowTooWide, dag_closure_device
+    from ...spgemm import DeviceCSR
+    from ..rbm import rb_matrix
     csr = _as_csr(A)
     n = csr.shape[0]
     if n == 0:
         return TransitiveClosure(sp.csr_matrix((0, 0), dtype=np.int32), 0)
-    W, mx_abs, mx = _squaring(csr, 64, cycle_error=True, dag_candidates=True)
+    a = csr.copy()
+    a.sum_duplicates()
+    a.sort_indices()
+    try:   # by topological levels (the reference's algorithm, level-parallel)
+        C, mx, _ = dag_closure_device(DeviceCSR.from_scipy(a, dtype=np.int32))
+    except RowTooWide:   # rows past the level kernels' tables: the same closure by squaring
+        W, mx_abs, mx = _squaring(csr, 64, cycle_error=True, dag_candidates=True)
+        return TransitiveClosure(W, (mx.bit_length() - 1) if mx > 1 else 0)
+    out = C.to_scipy()
+    W = rb_matrix((out.data, out.indices.astype(np.int32), out.indptr.astype(np.int32)), shape=out.shape)
     return TransitiveClosure(W, (mx.bit_length() - 1) if mx > 1 else 0)
 
 

@@ -166,3 +166,75 @@ def test_golden_dag_closure(native, golden):
             r = fn(A)
             assert same(r.W, E), (k, fn.__name__)
             assert r.diameter == rec["diameter"], (k, fn.__name__, r.diameter, rec["diameter"])
+
+
+def _star(parents: int, grand: bool):
+    """Vertex 0 with `parents` parents (values 2/3), each with one parent of its own when `grand`:
+    row 0 of the closure holds 1 + parents (+ parents) columns."""
+    n = 1 + parents * (2 if grand else 1)
+    r, c, v = [], [], []
+    for i in range(n):
+        r.append(i); c.append(i); v.append(-1 if i % 2 else 1)
+    for i in range(1, parents + 1):
+        r.append(0); c.append(i); v.append(2 + (i & 1))
+        if grand:
+            r.append(i); c.append(parents + i); v.append(3 - (i & 1))
+    return sp.csr_matrix((np.array(v, dtype=np.int32), (np.array(r), np.array(c))), shape=(n, n))
+
+
+def test_dag_levels_vs_oracle(native):
+    """The level-parallel DAG closure (rbg_dag_closure) on permuted pedigree forests against the
+    oracle's parents-first closure: entries and the candidate-maximum diameter."""
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse
+    for seed, n, gens in ((5, 400, 10), (6, 900, 14), (7, 64, 3)):
+        A = synth.forest(n, gens, seed, family=50, reach=3, dtype=np.int32)
+        p = np.random.default_rng(seed).permutation(n)
+        A = sp.csr_matrix(A[p][:, p])
+        W, d = O.dag_closure(A)
+        r = transitive_closure_dag_sparse(A)
+        assert same(r.W, W) and r.diameter == d, seed
+
+
+def test_dag_block_tier_pool_retry_and_levels(native):
+    """Rows past the warp table (256 columns) go to the block tier; a pool too small is grown
+    and the call repeated; the level count is the longest parent chain + 1."""
+    import torch
+    from redblackgraph_gb300.dag import dag_closure_device
+    from redblackgraph_gb300.spgemm import DeviceCSR
+    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse
+    A = _star(300, True)
+    W, d = O.dag_closure(A)
+    assert sp.csr_matrix(W)[0].nnz == 601
+    r = transitive_closure_dag_sparse(A)
+    assert same(r.W, W) and r.diameter == d
+    C, mx, levels = dag_closure_device(DeviceCSR.from_scipy(A, dtype=np.int32, device="cuda"), pool_factor=0)
+    torch.cuda.synchronize()
+    assert same(C.to_scipy(), W) and levels == 3 and mx.bit_length() - 1 == d
+
+
+def test_dag_row_too_wide_takes_squaring(native):
+    """A row with more than 8192 columns is past the block table: RowTooWide from the level
+    closure, and transitive_closure_dag_sparse answers by squaring with the same result."""
+    from redblackgraph_gb300.dag import RowTooWide, dag_closure_device
+    from redblackgraph_gb300.spgemm import DeviceCSR
+    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse
+    A = _star(9000, False)
+    with pytest.raises(RowTooWide):
+        dag_closure_device(DeviceCSR.from_scipy(A, dtype=np.int32, device="cuda"))
+    W, d = O.dag_closure(A)
+    r = transitive_closure_dag_sparse(A)
+    assert same(r.W, W) and r.diameter == d
+
+
+def test_dag_cycle_below_a_dag(native):
+    """Vertices under a cycle are never placed in a level: CycleError, also from the gpu module."""
+    from redblackgraph_gb300.gpu import CSRMatrixGPU, transitive_closure_dag_gpu
+    from redblackgraph_gb300.sparse import CycleError, transitive_closure_dag_sparse
+    D = np.diag(np.array([-1, 1, -1, 1, -1], dtype=np.int32))
+    D[0, 1] = 2; D[1, 2] = 3; D[2, 1] = 2; D[3, 4] = 3
+    A = sp.csr_matrix(D)
+    with pytest.raises(CycleError):
+        transitive_closure_dag_sparse(A)
+    with pytest.raises(CycleError):
+        transitive_closure_dag_gpu(CSRMatrixGPU.from_cpu(A))
