@@ -516,11 +516,11 @@ def run_spgemm_forest(seed=7):
 def run_dag_forest(seed=7):
     """Closure of the same 2,000,000-vertex pedigree forest by topological levels (rbg_dag_closure
     then rbg_dag_gather: the reference's parents-first DAG closure with int32 values), timed with
-    CUDA events from the resident CSR to the resident closure CSR.  Algorithmic bytes: the count
-    and the fill pass each read the stored entries (8 nnz(A) + 16 n) and every candidate (8 per
-    parent-row entry, 12 per parent edge for its row position), the fill writes the pool (8 nnz(C))
-    and the gather reads it and writes the CSR (16 nnz(C) + 8 (n + 1)).  Checked entry for entry
-    against the squaring closure of the same forest."""
+    CUDA events from the resident CSR to the resident closure CSR.  Algorithmic bytes: A once
+    (12 nnz(A) + 8 (n + 1)), every candidate once (8 per parent-row entry, 12 per parent edge for
+    that row's position), the closure rows written to the pool (8 nnz(C)), then read and written
+    as the CSR (16 nnz(C) + 8 (n + 1)).  Checked entry for entry against the squaring closure of
+    the same forest."""
     import torch
     from redblackgraph_gb300 import synth
     from redblackgraph_gb300.dag import dag_closure_device
@@ -546,7 +546,7 @@ def run_dag_forest(seed=7):
     off = aj != rows
     cand = int(clen[aj[off]].sum())
     edges = int(off.sum())
-    b = 2.0 * (8 * A.nnz + 16 * n + 8 * cand + 12 * edges) + 8.0 * C.nnz + 16.0 * C.nnz + 8.0 * (n + 1)
+    b = 12.0 * A.nnz + 8.0 * (n + 1) + 8.0 * cand + 12.0 * edges + 24.0 * C.nnz + 8.0 * (n + 1)
     # the squaring closure of the same forest (int64), untimed, as the check
     R = DeviceCSR.from_scipy(A, dtype=np.int64)
     for _ in range(64):

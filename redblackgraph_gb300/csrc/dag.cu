@@ -6,30 +6,38 @@
 // (+) A[v][w] (x) C[w][.] over v's parents w != v, with the Cython int32 product and sum; the
 // diameter source is the largest magnitude of any stored entry or candidate.
 //
-// Design: the vertices are put in topological levels on the device (Kahn's algorithm, one launch
-// per level: a vertex joins the next level when its last parent is placed).  A level's rows only
-// read rows of earlier levels, so each level is one batch of independent rows: a count pass (one
-// warp per row folds its candidates into a shared-memory table keyed by column and counts the
-// distinct columns), a scan that places the rows in a caller-provided row pool, and a fill pass
-// that folds again and writes each row sorted.  Rows with more distinct columns than the warp
-// table holds are done by a 512-thread block with a larger table; a row wider than that makes the
-// call return RBG_ERR_CAPACITY with *nnz = -1.  A pool too small for the closure returns
-// RBG_ERR_CAPACITY with *nnz set to a larger size to retry with.  A cycle (vertices never placed)
-// returns RBG_ERR_CYCLE.
+// Design.  Vertices are put in topological levels on the device (Kahn's algorithm): a vertex
+// joins the next level when its last parent's row is done.  The kernel that discovers a vertex
+// also bounds its row (stored entries + the lengths of its parents' rows) and reserves that many
+// slots of a caller-provided row pool (one atomic per warp), so each level then needs a single
+// fill pass: one warp per row walks the row's candidates (a warp scan over the segments "stored
+// entry, then that parent's row" and a shuffle binary search give every lane its candidate), and
+//   - up to 64 candidates: sorts (column, value) keys in registers and keeps the first of each
+//     column (the signed minimum of the non-zero values, a stored zero when there is none);
+//   - up to 256: folds them into a per-warp shared-memory table and sorts the occupied slots;
+//   - more: the row goes to a 512-thread block with an 8192-slot table.
+// The host launches levels in chunks without waiting (every kernel reads its level's bounds from
+// device memory and exits at once on an empty level) and looks at the frontier once per chunk.
+// A pool too small marks the rows past its end as skipped; the call then returns
+// RBG_ERR_CAPACITY with *nnz = a larger pool to retry with.  A row with more distinct columns
+// than the block table returns RBG_ERR_CAPACITY with *nnz = -1.  Vertices never placed (on or
+// below a cycle) return RBG_ERR_CYCLE.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 #include <algorithm>
-#include <vector>
 #include "rbg_internal.cuh"
 
 namespace rbg {
 
-constexpr int DG_WSLOTS = 256;          // warp table slots (distinct columns of a row)
-constexpr int DG_WARPS = 8;             // warps per CTA
-constexpr int DG_BSLOTS = 8192;         // block table slots
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int DG_REG = 64;              // register path: candidates per row
+constexpr int DG_WSLOTS = 256;          // warp table slots (candidates per row)
+constexpr int DG_WARPS = 8;             // warps per CTA of the fill pass
+constexpr int DG_BSLOTS = 8192;         // block table slots (distinct columns)
 constexpr int DG_BTHREADS = 512;
 constexpr unsigned DG_NOKEY = 0xffffffffu;
 constexpr int DG_NOVAL = 0x7fffffff;    // (+) identity of the table (no non-zero candidate yet)
+constexpr unsigned long long DG_PAD = ~0ull;
 
 template <int SLOTS> struct DagTable {
     unsigned key[SLOTS];
@@ -37,6 +45,37 @@ template <int SLOTS> struct DagTable {
     unsigned char has[SLOTS];           // 1: some non-zero candidate landed here
     unsigned long long list[SLOTS];     // (column << 32 | slot) of the occupied slots
 };
+
+struct DagArgs {
+    int64_t n;
+    const int64_t *ap; const int *aj; const int *av;     // A (int32 values)
+    int *order; int *tail;                               // vertices by level; vertices placed
+    int64_t *lb;                                         // lb[L]: first position of level L in order
+    const int64_t *coff; const int *children; int *remaining;
+    int64_t *row_off; int *row_len; int *ubv;            // pool position, length, bound of each row
+    int *pcols; int *pvals; int64_t capacity;            // the row pool
+    unsigned long long *base;                            // pool slots reserved so far
+    int *wide; int *nwide; int64_t *wlb;                 // block-tier rows; wlb[L]: first of level L
+    unsigned long long *max_abs;
+    unsigned long long *total;                           // entries written
+    int *flags;                                          // 1: pool too small, 2: row past the block table
+    int *nlevels;
+};
+
+__device__ __forceinline__ int dag_abs(int v) { return v > 0 ? v : (int)(0u - (unsigned)v); }
+
+// (column, value) sort key: ascending keys put a column's signed-minimum non-zero value first and
+// a zero after every non-zero value.
+__device__ __forceinline__ unsigned long long dag_key(int col, int v) {
+    unsigned e = 0xffffffffu;
+    if (v != 0) e = ((unsigned)v ^ 0x80000000u) - (v > 0 ? 1u : 0u);
+    return ((unsigned long long)(unsigned)col << 32) | e;
+}
+__device__ __forceinline__ int dag_key_val(unsigned long long k) {
+    const unsigned e = (unsigned)k;
+    if (e == 0xffffffffu) return 0;
+    return e >= 0x80000000u ? (int)((e + 1u) ^ 0x80000000u) : (int)(e ^ 0x80000000u);
+}
 
 template <int SLOTS>
 __device__ __forceinline__ int dag_slot(DagTable<SLOTS> &H, unsigned j, int mask) {
@@ -53,8 +92,6 @@ __device__ __forceinline__ int dag_slot(DagTable<SLOTS> &H, unsigned j, int mask
     return -1;
 }
 
-__device__ __forceinline__ int dag_abs(int v) { return v > 0 ? v : (int)(0u - (unsigned)v); }
-
 // Fold candidate (column j, value p) into the table; returns false when the table is full.
 template <int SLOTS>
 __device__ __forceinline__ bool dag_fold(DagTable<SLOTS> &H, unsigned j, int p, int mask) {
@@ -67,47 +104,6 @@ __device__ __forceinline__ bool dag_fold(DagTable<SLOTS> &H, unsigned j, int p, 
     return true;
 }
 
-struct DagArgs {
-    int64_t n;
-    const int64_t *ap; const int *aj; const int *av;     // A (int32 values)
-    const int *order;                                   // vertices by level
-    int64_t *row_off; int *row_len;                     // pool position / length of each row
-    const int *pcols; const int *pvals;                 // the pool (rows of earlier levels)
-    int *wcols; int *wvals;                             // the pool, written by the fill pass
-    int64_t capacity;
-    int *lvl_len;                                       // count pass output (level order)
-    const int64_t *lvl_off;                             // fill pass input (level order)
-    int *wide; int *nwide;                              // rows for the block tier (level order)
-    unsigned long long *max_abs;
-    int *flags;                                         // [0] row wider than the block table
-};
-
-// The candidates of row v, folded by `nthreads` threads of the calling group (lane = rank in it).
-template <int SLOTS>
-__device__ __forceinline__ bool dag_gather(const DagArgs &a, int v, DagTable<SLOTS> &H, int mask, int lane,
-                                           int nthreads, int &best) {
-    bool ok = true;
-    for (int64_t e = a.ap[v] + lane; e < a.ap[v + 1]; e += nthreads) {   // the stored entries
-        const int w = a.aj[e], val = a.av[e];
-        best = max(best, dag_abs(val));
-        ok &= dag_fold(H, (unsigned)w, val, mask);
-    }
-    for (int64_t e = a.ap[v]; e < a.ap[v + 1]; ++e) {                   // each parent's closed row
-        const int w = a.aj[e];
-        if (w == v || w < 0 || w >= a.n) continue;
-        const int vw = a.av[e];
-        const int64_t o = a.row_off[w];
-        const int len = a.row_len[w];
-        for (int f = lane; f < len; f += nthreads) {
-            const int p = cy_product(vw, a.pvals[o + f]);
-            if (p == 0) continue;
-            best = max(best, dag_abs(p));
-            ok &= dag_fold(H, (unsigned)a.pcols[o + f], p, mask);
-        }
-    }
-    return ok;
-}
-
 template <int SLOTS>
 __device__ __forceinline__ void dag_clear(DagTable<SLOTS> &H, int S, int lane, int nthreads) {
     for (int s = lane; s < S; s += nthreads) {
@@ -117,182 +113,147 @@ __device__ __forceinline__ void dag_clear(DagTable<SLOTS> &H, int S, int lane, i
     }
 }
 
-// Count pass, one warp per row of the level (k = position in the level).
-__global__ void __launch_bounds__(DG_WARPS * 32) dag_count_kernel(DagArgs a, int64_t ls, int nl) {
-    extern __shared__ __align__(16) unsigned char dg_smem[];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    DagTable<DG_WSLOTS> &H = reinterpret_cast<DagTable<DG_WSLOTS> *>(dg_smem)[w];
-    int best = 0;
-    for (int k = blockIdx.x * DG_WARPS + w; k < nl; k += gridDim.x * DG_WARPS) {
-        const int v = a.order[ls + k];
-        dag_clear(H, DG_WSLOTS, lane, 32);
-        __syncwarp();
-        const bool ok = dag_gather(a, v, H, DG_WSLOTS - 1, lane, 32, best);
-        __syncwarp();
-        if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) a.wide[atomicAdd(a.nwide, 1)] = k;
-            continue;
+// ----------------------------------------------------------------------------- candidate walk
+// The candidates of row v, flattened: stored entry e of the row opens a segment of 1 + len(w)
+// positions (the entry itself, then A[v][w] (x) C[w][f] for f < len(w); len = 0 when w == v).
+// One chunk of up to 32 stored entries at a time: lane j holds chunk entry j.
+struct DagSeg {
+    int w, avw, len, excl;
+    int64_t off;
+};
+
+// Load chunk entry `lane` of row v (stored entries [e0, e1)) and scan the segment lengths;
+// returns the chunk's candidate count (all lanes).
+__device__ __forceinline__ int dag_seg_load(const DagArgs &a, int v, int64_t e0, int64_t e1, int lane, DagSeg &sg) {
+    const int64_t e = e0 + lane;
+    sg.w = -1; sg.avw = 0; sg.len = 0; sg.off = 0;
+    int cnt = 0;
+    if (e < e1) {
+        sg.w = a.aj[e];
+        sg.avw = a.av[e];
+        cnt = 1;
+        if (sg.w != v && sg.w >= 0 && sg.w < a.n) {
+            sg.len = a.row_len[sg.w];
+            sg.off = a.row_off[sg.w];
+            cnt += sg.len;
         }
-        int nd = 0;
-        for (int s0 = 0; s0 < DG_WSLOTS; s0 += 32)
-            nd += __popc(__ballot_sync(0xffffffffu, H.key[s0 + lane] != DG_NOKEY));
-        if (lane == 0) a.lvl_len[k] = nd;
-        __syncwarp();
     }
-    best = __reduce_max_sync(0xffffffffu, best);
-    if (lane == 0 && best > 0) atomicMax(a.max_abs, (unsigned long long)best);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    sg.excl = incl - cnt;
+    return __shfl_sync(FULL, incl, 31);
 }
 
-// Count pass for the wide rows, one block per row.
-__global__ void __launch_bounds__(DG_BTHREADS) dag_count_block_kernel(DagArgs a, int64_t ls) {
-    extern __shared__ __align__(16) unsigned char dg_smem[];
-    DagTable<DG_BSLOTS> &H = *reinterpret_cast<DagTable<DG_BSLOTS> *>(dg_smem);
-    __shared__ int s_cnt, s_ok;
-    const int nw = *a.nwide;
-    int best = 0;
-    for (int b = blockIdx.x; b < nw; b += gridDim.x) {
-        const int k = a.wide[b];
-        const int v = a.order[ls + k];
-        dag_clear(H, DG_BSLOTS, threadIdx.x, DG_BTHREADS);
-        if (threadIdx.x == 0) { s_cnt = 0; s_ok = 1; }
-        __syncthreads();
-        const bool ok = dag_gather(a, v, H, DG_BSLOTS - 1, threadIdx.x, DG_BTHREADS, best);
-        if (!ok) s_ok = 0;
-        __syncthreads();
-        int c = 0;
-        for (int s = threadIdx.x; s < DG_BSLOTS; s += DG_BTHREADS) c += H.key[s] != DG_NOKEY;
-        c = __reduce_add_sync(0xffffffffu, c);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&s_cnt, c);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            if (!s_ok) atomicOr(a.flags, 1);
-            a.lvl_len[k] = s_ok ? s_cnt : 0;
+// Candidate at chunk position idx (< the chunk's count when `in`): returns false for a zero
+// product (no candidate); else its column and value.  Every lane must call it (shuffles).
+__device__ __forceinline__ bool dag_candidate(const DagArgs &a, const DagSeg &sg, int idx, bool in, int &col,
+                                              int &val) {
+    int lo = 0;                                  // last segment starting at or before idx
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1) {
+        const int x = __shfl_sync(FULL, sg.excl, lo + st);
+        if (x <= idx) lo += st;
+    }
+    const int w = __shfl_sync(FULL, sg.w, lo);
+    const int avw = __shfl_sync(FULL, sg.avw, lo);
+    const int64_t off = __shfl_sync(FULL, sg.off, lo);
+    const int x0 = __shfl_sync(FULL, sg.excl, lo);
+    if (!in) return false;
+    const int f = idx - x0;
+    if (f == 0) {                                // the stored entry itself (a zero is kept)
+        col = w;
+        val = avw;
+        return true;
+    }
+    col = a.pcols[off + f - 1];
+    val = cy_product(avw, a.pvals[off + f - 1]);
+    return val != 0;
+}
+
+// ----------------------------------------------------------------------------- register sorts
+__device__ __forceinline__ unsigned long long dag_sort32(unsigned long long v, int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(FULL, v, j);
+            const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+            v = (lower == up) ? min(v, o) : max(v, o);
         }
-        __syncthreads();
     }
-    best = __reduce_max_sync(0xffffffffu, best);
-    if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(a.max_abs, (unsigned long long)best);
+    return v;
 }
 
-// Place the level's rows in the pool (base = rows placed so far, kept on the device).
-__global__ void dag_place_kernel(DagArgs a, int64_t ls, int nl, int64_t *base) {
-    const int64_t b = *base;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nl; k += gridDim.x * blockDim.x) {
-        const int v = a.order[ls + k];
-        a.row_off[v] = b + a.lvl_off[k];
-        a.row_len[v] = a.lvl_len[k];
-    }
-}
-
-__global__ void dag_advance_kernel(const int64_t *lvl_off, const int *lvl_len, int nl, int64_t *base) {
-    if (blockIdx.x == 0 && threadIdx.x == 0 && nl > 0) *base += lvl_off[nl - 1] + lvl_len[nl - 1];
-}
-
-// Write the occupied slots of a table as a sorted row at `dst` (warp: register sort for up to 64
-// columns, shared-memory bitonic otherwise).
-template <int SLOTS>
-__device__ __forceinline__ int dag_collect(DagTable<SLOTS> &H, int S, int lane, int nthreads) {
-    // compaction of the occupied slots into list (warp-synchronous when nthreads == 32)
-    __shared__ int s_nd;
-    int nd = 0;
-    if (nthreads == 32) {
-        for (int s0 = 0; s0 < S; s0 += 32) {
-            const int s = s0 + lane;
-            const bool occ = H.key[s] != DG_NOKEY;
-            const unsigned bal = __ballot_sync(0xffffffffu, occ);
-            if (occ) H.list[nd + __popc(bal & ((1u << lane) - 1u))] = ((unsigned long long)H.key[s] << 32) | (unsigned)s;
-            nd += __popc(bal);
-        }
-        __syncwarp();
-        return nd;
-    }
-    if (lane == 0) s_nd = 0;
-    __syncthreads();
-    for (int s = lane; s < S; s += nthreads)
-        if (H.key[s] != DG_NOKEY) H.list[atomicAdd(&s_nd, 1)] = ((unsigned long long)H.key[s] << 32) | (unsigned)s;
-    __syncthreads();
-    return s_nd;
-}
-
-template <int SLOTS, typename Sync>
-__device__ __forceinline__ void dag_sort(DagTable<SLOTS> &H, int nd, int lane, int nthreads, Sync sync) {
-    int P = 1;
-    while (P < nd) P <<= 1;
-    for (int q = nd + lane; q < P; q += nthreads) H.list[q] = ~0ull;
-    sync();
-    for (int k = 2; k <= P; k <<= 1) {
-        for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int q = lane; q < P; q += nthreads) {
-                const int qx = q ^ jj;
-                if (qx > q) {
-                    const unsigned long long x = H.list[q], y = H.list[qx];
-                    if ((x > y) == ((q & k) == 0)) { H.list[q] = y; H.list[qx] = x; }
+__device__ __forceinline__ void dag_sort64(unsigned long long (&v)[2], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j == 32) {
+                const unsigned long long lo = min(v[0], v[1]), hi = max(v[0], v[1]);
+                v[0] = lo;
+                v[1] = hi;
+            } else {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int i = lane + 32 * h;
+                    const unsigned long long o = __shfl_xor_sync(FULL, v[h], j);
+                    const bool up = (i & k) == 0, lower = (i & j) == 0;
+                    v[h] = (lower == up) ? min(v[h], o) : max(v[h], o);
                 }
             }
-            sync();
         }
     }
 }
 
-struct DgWarpSync { __device__ void operator()() const { __syncwarp(); } };
-struct DgBlockSync { __device__ void operator()() const { __syncthreads(); } };
-
-// Fill pass, one warp per (not wide) row.
-__global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int64_t ls, int nl) {
-    extern __shared__ __align__(16) unsigned char dg_smem[];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    DagTable<DG_WSLOTS> &H = reinterpret_cast<DagTable<DG_WSLOTS> *>(dg_smem)[w];
-    int best = 0;
-    for (int k = blockIdx.x * DG_WARPS + w; k < nl; k += gridDim.x * DG_WARPS) {
-        const int v = a.order[ls + k];
-        const int64_t o = a.row_off[v];
-        const int len = a.row_len[v];
-        if (len > DG_WSLOTS || o + len > a.capacity) continue;   // wide rows: block pass
-        dag_clear(H, DG_WSLOTS, lane, 32);
-        __syncwarp();
-        const bool ok = dag_gather(a, v, H, DG_WSLOTS - 1, lane, 32, best);
-        if (!__all_sync(0xffffffffu, ok)) continue;              // counted wide: block pass
-        const int nd = dag_collect(H, DG_WSLOTS, lane, 32);
-        dag_sort(H, nd, lane, 32, DgWarpSync());
-        for (int q = lane; q < nd; q += 32) {
-            const unsigned long long e = H.list[q];
-            const int s = (int)(e & 0xffffffffu);
-            a.wcols[o + q] = (int)(e >> 32);
-            a.wvals[o + q] = H.has[s] ? H.val[s] : 0;
+// ----------------------------------------------------------------------------- level discovery
+// Append the lanes' ready vertices to the order, bound their rows and reserve their pool slots.
+__device__ __forceinline__ void dag_append(const DagArgs &a, bool ready, int c, long long ub, int lane) {
+    const unsigned bal = __ballot_sync(FULL, ready);
+    if (!bal) return;
+    int pos0 = 0;
+    if (lane == 0) pos0 = atomicAdd(a.tail, __popc(bal));
+    pos0 = __shfl_sync(FULL, pos0, 0);
+    const long long x = ready ? ub : 0;
+    long long incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const long long tot = __shfl_sync(FULL, incl, 31);
+    unsigned long long b0 = 0;
+    if (lane == 0) b0 = atomicAdd(a.base, (unsigned long long)tot);
+    b0 = __shfl_sync(FULL, b0, 0);
+    if (ready) {
+        a.order[pos0 + __popc(bal & ((1u << lane) - 1u))] = c;
+        const long long off = (long long)b0 + incl - x;
+        a.ubv[c] = (int)min(x, (long long)INT_MAX);
+        if (off + x > a.capacity) {              // past the pool: skipped, the call asks for more
+            a.row_off[c] = -1;
+            a.row_len[c] = 0;
+            atomicOr(a.flags, 1);
+        } else {
+            a.row_off[c] = off;
+            if (x > DG_WSLOTS) a.wide[atomicAdd(a.nwide, 1)] = c;
         }
-        __syncwarp();
     }
 }
 
-// Fill pass for the wide rows, one block per row.
-__global__ void __launch_bounds__(DG_BTHREADS) dag_fill_block_kernel(DagArgs a, int64_t ls) {
-    extern __shared__ __align__(16) unsigned char dg_smem[];
-    DagTable<DG_BSLOTS> &H = *reinterpret_cast<DagTable<DG_BSLOTS> *>(dg_smem);
-    const int nw = *a.nwide;
-    int best = 0;
-    for (int b = blockIdx.x; b < nw; b += gridDim.x) {
-        const int k = a.wide[b];
-        const int v = a.order[ls + k];
-        const int64_t o = a.row_off[v];
-        const int len = a.row_len[v];
-        if (o + len > a.capacity) continue;                      // uniform across the block
-        dag_clear(H, DG_BSLOTS, threadIdx.x, DG_BTHREADS);
-        __syncthreads();
-        dag_gather(a, v, H, DG_BSLOTS - 1, threadIdx.x, DG_BTHREADS, best);
-        __syncthreads();
-        const int nd = dag_collect(H, DG_BSLOTS, threadIdx.x, DG_BTHREADS);
-        dag_sort(H, nd, threadIdx.x, DG_BTHREADS, DgBlockSync());
-        for (int q = threadIdx.x; q < nd; q += DG_BTHREADS) {
-            const unsigned long long e = H.list[q];
-            const int s = (int)(e & 0xffffffffu);
-            a.wcols[o + q] = (int)(e >> 32);
-            a.wvals[o + q] = H.has[s] ? H.val[s] : 0;
-        }
-        __syncthreads();
+// Upper bound of row c's length: its stored entries plus its parents' rows.
+__device__ __forceinline__ long long dag_bound(const DagArgs &a, int c) {
+    long long ub = 0;
+    for (int64_t q = a.ap[c]; q < a.ap[c + 1]; ++q) {
+        const int x = a.aj[q];
+        ub += 1 + ((x != c && x >= 0 && x < a.n) ? a.row_len[x] : 0);
     }
+    return ub;
 }
 
-// ----------------------------------------------------------------------------- levels (Kahn)
 __global__ void dag_indeg_kernel(int64_t n, const int64_t *ap, const int *aj, int *remaining, int *ccount) {
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         int c = 0;
@@ -317,31 +278,284 @@ __global__ void dag_children_kernel(int64_t n, const int64_t *ap, const int *aj,
     }
 }
 
-__global__ void dag_roots_kernel(int64_t n, const int *remaining, int *order, int *tail) {
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
-        if (remaining[v] == 0) order[atomicAdd(tail, 1)] = (int)v;
+// Level 0: the vertices without parents.
+__global__ void dag_roots_kernel(DagArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t v0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; v0 < a.n; v0 += warps * 32) {
+        const int64_t v = v0 + lane;
+        const bool ready = v < a.n && a.remaining[v] == 0;
+        dag_append(a, ready, (int)v, ready ? (long long)(a.ap[v + 1] - a.ap[v]) : 0, lane);
+    }
 }
 
-// place the children whose last parent is in [ls, le)
-__global__ void dag_level_kernel(const int *order, int64_t ls, int64_t le, const int64_t *coff,
-                                 const int *children, int *remaining, int *order_out, int *tail) {
-    for (int64_t k = ls + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < le;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const int w = order[k];
-        for (int64_t e = coff[w]; e < coff[w + 1]; ++e) {
-            const int c = children[e];
-            if (atomicSub(&remaining[c], 1) == 1) order_out[atomicAdd(tail, 1)] = c;
+// Level L + 1 from level L: every child edge of the level's vertices, flattened over the warp.
+__global__ void dag_discover_kernel(DagArgs a, int64_t L) {
+    const int lane = threadIdx.x & 31;
+    const int64_t s = a.lb[L], e = a.lb[L + 1];
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k0 = s + ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; k0 < e;
+         k0 += warps * 32) {
+        const int64_t k = k0 + lane;
+        int64_t c0 = 0;
+        int cnt = 0;
+        if (k < e) {
+            const int w = a.order[k];
+            c0 = a.coff[w];
+            cnt = (int)(a.coff[w + 1] - c0);
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int excl = incl - cnt;
+        const int T = __shfl_sync(FULL, incl, 31);
+        for (int b = 0; b < T; b += 32) {
+            const int idx = b + lane;
+            int lo = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const int x = __shfl_sync(FULL, excl, lo + st);
+                if (x <= idx) lo += st;
+            }
+            const int64_t cq = __shfl_sync(FULL, c0, lo);
+            const int xq = __shfl_sync(FULL, excl, lo);
+            bool ready = false;
+            int c = 0;
+            long long ub = 0;
+            if (idx < T) {
+                c = a.children[cq + (idx - xq)];
+                if (atomicSub(&a.remaining[c], 1) == 1) {
+                    ready = true;
+                    ub = dag_bound(a, c);
+                }
+            }
+            dag_append(a, ready, c, ub, lane);
         }
     }
 }
 
+// ----------------------------------------------------------------------------- fill passes
+// Write a warp's table (S slots) as a sorted row at pool position o; returns the row length.
+__device__ __forceinline__ int dag_table_row(const DagArgs &a, DagTable<DG_WSLOTS> &H, int S, int64_t o, int lane) {
+    int nd = 0;
+    for (int s0 = 0; s0 < S; s0 += 32) {
+        const int s = s0 + lane;
+        const bool occ = H.key[s] != DG_NOKEY;
+        const unsigned bal = __ballot_sync(FULL, occ);
+        if (occ) H.list[nd + __popc(bal & ((1u << lane) - 1u))] = ((unsigned long long)H.key[s] << 32) | (unsigned)s;
+        nd += __popc(bal);
+    }
+    __syncwarp();
+    int P = 32;
+    while (P < nd) P <<= 1;
+    for (int q = nd + lane; q < P; q += 32) H.list[q] = DG_PAD;
+    __syncwarp();
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int q = lane; q < P; q += 32) {
+                const int qx = q ^ jj;
+                if (qx > q) {
+                    const unsigned long long x = H.list[q], y = H.list[qx];
+                    if ((x > y) == ((q & k) == 0)) { H.list[q] = y; H.list[qx] = x; }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    for (int q = lane; q < nd; q += 32) {
+        const unsigned long long e = H.list[q];
+        const int s = (int)(e & 0xffffffffu);
+        a.pcols[o + q] = (int)(e >> 32);
+        a.pvals[o + q] = H.has[s] ? H.val[s] : 0;
+    }
+    __syncwarp();
+    return nd;
+}
+
+// One warp per row of level L (rows of up to 256 candidates).  Block 0 closes the level's range.
+__global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int64_t L) {
+    extern __shared__ __align__(16) unsigned char dg_smem[];
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    DagTable<DG_WSLOTS> &H = reinterpret_cast<DagTable<DG_WSLOTS> *>(dg_smem)[wi];
+    const int64_t s = a.lb[L], e = *a.tail;      // nothing appends to the order during the fill
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.lb[L + 1] = e;
+        if (e > s) atomicAdd(a.nlevels, 1);
+    }
+    int best = 0;
+    unsigned long long written = 0;
+    const int64_t warps = (int64_t)gridDim.x * DG_WARPS;
+    for (int64_t k = s + (int64_t)blockIdx.x * DG_WARPS + wi; k < e; k += warps) {
+        const int v = a.order[k];
+        const int64_t o = a.row_off[v];
+        const int ub = a.ubv[v];
+        if (o < 0 || ub > DG_WSLOTS) continue;   // skipped, or the block tier's
+        const int64_t e0 = a.ap[v], e1 = a.ap[v + 1];
+        int nd;
+        if (ub <= DG_REG && e1 - e0 <= 32) {
+            // register path: candidate idx sits in lane idx % 32, slot idx / 32
+            DagSeg sg;
+            const int T = dag_seg_load(a, v, e0, e1, lane, sg);
+            unsigned long long key[2] = {DG_PAD, DG_PAD};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (h * 32 < T) {
+                    int col = 0, val = 0;
+                    if (dag_candidate(a, sg, h * 32 + lane, h * 32 + lane < T, col, val)) {
+                        key[h] = dag_key(col, val);
+                        best = max(best, dag_abs(val));
+                    }
+                }
+            }
+            bool head[2];
+            if (T <= 32) {
+                key[0] = dag_sort32(key[0], lane);
+                const unsigned long long prev = __shfl_up_sync(FULL, key[0], 1);
+                head[0] = key[0] != DG_PAD && (lane == 0 || (prev >> 32) != (key[0] >> 32));
+                head[1] = false;
+            } else {
+                dag_sort64(key, lane);
+                const unsigned long long p0 = __shfl_up_sync(FULL, key[0], 1);
+                const unsigned long long p1 = __shfl_up_sync(FULL, key[1], 1);
+                const unsigned long long l31 = __shfl_sync(FULL, key[0], 31);
+                head[0] = key[0] != DG_PAD && (lane == 0 || (p0 >> 32) != (key[0] >> 32));
+                head[1] = key[1] != DG_PAD && ((lane == 0 ? l31 : p1) >> 32) != (key[1] >> 32);
+            }
+            const unsigned b0 = __ballot_sync(FULL, head[0]), b1 = __ballot_sync(FULL, head[1]);
+            const unsigned lt = (1u << lane) - 1u;
+            if (head[0]) {
+                const int r = __popc(b0 & lt);
+                a.pcols[o + r] = (int)(key[0] >> 32);
+                a.pvals[o + r] = dag_key_val(key[0]);
+            }
+            if (head[1]) {
+                const int r = __popc(b0) + __popc(b1 & lt);
+                a.pcols[o + r] = (int)(key[1] >> 32);
+                a.pvals[o + r] = dag_key_val(key[1]);
+            }
+            nd = __popc(b0) + __popc(b1);
+        } else {
+            // table path: ub >= distinct columns, so a table of ub slots never fills
+            int S = 32;
+            while (S < ub) S <<= 1;
+            dag_clear(H, S, lane, 32);
+            __syncwarp();
+            for (int64_t c0 = e0; c0 < e1; c0 += 32) {
+                DagSeg sg;
+                const int T = dag_seg_load(a, v, c0, e1, lane, sg);
+                for (int b = 0; b < T; b += 32) {
+                    int col = 0, val = 0;
+                    if (dag_candidate(a, sg, b + lane, b + lane < T, col, val)) {
+                        best = max(best, dag_abs(val));
+                        dag_fold(H, (unsigned)col, val, S - 1);
+                    }
+                }
+            }
+            __syncwarp();
+            nd = dag_table_row(a, H, S, o, lane);
+        }
+        if (lane == 0) {
+            a.row_len[v] = nd;
+            written += (unsigned long long)nd;
+        }
+    }
+    best = __reduce_max_sync(FULL, best);
+    if (lane == 0) {
+        if (best > 0) atomicMax(a.max_abs, (unsigned long long)best);
+        if (written) atomicAdd(a.total, written);
+    }
+}
+
+// One 512-thread block per row of level L with more than 256 candidates.
+__global__ void __launch_bounds__(DG_BTHREADS) dag_fill_block_kernel(DagArgs a, int64_t L) {
+    extern __shared__ __align__(16) unsigned char dg_smem[];
+    DagTable<DG_BSLOTS> &H = *reinterpret_cast<DagTable<DG_BSLOTS> *>(dg_smem);
+    __shared__ int s_nd, s_ok;
+    const int64_t s = a.wlb[L], e = *a.nwide;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.wlb[L + 1] = e;
+    int best = 0;
+    for (int64_t b = s + blockIdx.x; b < e; b += gridDim.x) {
+        const int v = a.wide[b];
+        const int64_t o = a.row_off[v];
+        dag_clear(H, DG_BSLOTS, threadIdx.x, DG_BTHREADS);
+        if (threadIdx.x == 0) { s_nd = 0; s_ok = 1; }
+        __syncthreads();
+        bool ok = true;
+        for (int64_t q = a.ap[v] + threadIdx.x; q < a.ap[v + 1]; q += DG_BTHREADS) {   // stored entries
+            const int val = a.av[q];
+            best = max(best, dag_abs(val));
+            ok &= dag_fold(H, (unsigned)a.aj[q], val, DG_BSLOTS - 1);
+        }
+        for (int64_t q = a.ap[v]; q < a.ap[v + 1]; ++q) {                              // parents' rows
+            const int w = a.aj[q];
+            if (w == v || w < 0 || w >= a.n) continue;
+            const int avw = a.av[q];
+            const int64_t po = a.row_off[w];
+            const int len = a.row_len[w];
+            for (int f = threadIdx.x; f < len; f += DG_BTHREADS) {
+                const int p = cy_product(avw, a.pvals[po + f]);
+                if (p == 0) continue;
+                best = max(best, dag_abs(p));
+                ok &= dag_fold(H, (unsigned)a.pcols[po + f], p, DG_BSLOTS - 1);
+            }
+        }
+        if (!ok) s_ok = 0;
+        __syncthreads();
+        if (!s_ok) {                             // more distinct columns than the table
+            if (threadIdx.x == 0) { atomicOr(a.flags, 2); a.row_len[v] = 0; }
+            __syncthreads();
+            continue;
+        }
+        for (int q = threadIdx.x; q < DG_BSLOTS; q += DG_BTHREADS)
+            if (H.key[q] != DG_NOKEY) H.list[atomicAdd(&s_nd, 1)] = ((unsigned long long)H.key[q] << 32) | (unsigned)q;
+        __syncthreads();
+        const int nd = s_nd;
+        int P = 1;
+        while (P < nd) P <<= 1;
+        for (int q = nd + threadIdx.x; q < P; q += DG_BTHREADS) H.list[q] = DG_PAD;
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int q = threadIdx.x; q < P; q += DG_BTHREADS) {
+                    const int qx = q ^ jj;
+                    if (qx > q) {
+                        const unsigned long long x = H.list[q], y = H.list[qx];
+                        if ((x > y) == ((q & k) == 0)) { H.list[q] = y; H.list[qx] = x; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int q = threadIdx.x; q < nd; q += DG_BTHREADS) {
+            const unsigned long long ek = H.list[q];
+            const int sl = (int)(ek & 0xffffffffu);
+            a.pcols[o + q] = (int)(ek >> 32);
+            a.pvals[o + q] = H.has[sl] ? H.val[sl] : 0;
+        }
+        if (threadIdx.x == 0) {
+            a.row_len[v] = nd;
+            atomicAdd(a.total, (unsigned long long)nd);
+        }
+        __syncthreads();
+    }
+    best = __reduce_max_sync(FULL, best);
+    if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(a.max_abs, (unsigned long long)best);
+}
+
+// ----------------------------------------------------------------------------- pool -> CSR
+// Eight lanes per row.
 __global__ void dag_gather_rows_kernel(int64_t n, const int64_t *row_off, const int *pcols, const int *pvals,
                                        const int64_t *indptr, int *cj, int *cx) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t v = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < n; v += warps) {
-        const int64_t src = row_off[v], dst = indptr[v], len = indptr[v + 1] - dst;
-        for (int64_t e = lane; e < len; e += 32) {
+    const int sub = threadIdx.x & 7;
+    const int64_t groups = (int64_t)gridDim.x * (blockDim.x >> 3);
+    for (int64_t v = (int64_t)blockIdx.x * (blockDim.x >> 3) + (threadIdx.x >> 3); v < n; v += groups) {
+        const int64_t dst = indptr[v], len = indptr[v + 1] - dst;
+        if (len == 0) continue;
+        const int64_t src = row_off[v];
+        for (int64_t e = sub; e < len; e += 8) {
             cj[dst + e] = pcols[src + e];
             cx[dst + e] = pvals[src + e];
         }
@@ -360,41 +574,54 @@ using namespace rbg;
 namespace {
 
 struct DagWs {
-    int *remaining, *ccount, *cursor, *children, *order, *tail, *lvl_len, *wide, *nwide, *flags;
-    int64_t *coff, *lvl_off, *base;
-    unsigned long long *max_abs;
+    int *remaining, *ccount, *cursor, *children, *order, *ubv, *wide;
+    int *tail, *nwide, *flags, *nlevels;
+    int64_t *coff, *lb, *wlb;
+    unsigned long long *base, *max_abs, *total;
     void *tmp;
     size_t tmp_bytes;
 };
 
 size_t dag_tmp_bytes(int64_t n) {
-    size_t a = 0, b = 0, c = 0;
-    const int m = (int)std::max<int64_t>(n + 1, 1);
-    cub::DeviceScan::ExclusiveSum(nullptr, a, (int *)nullptr, (int64_t *)nullptr, m);
-    cub::DeviceScan::ExclusiveSum(nullptr, b, (int64_t *)nullptr, (int64_t *)nullptr, m);
-    cub::DeviceScan::ExclusiveSum(nullptr, c, (int *)nullptr, (int64_t *)nullptr, m);
-    return std::max(a, std::max(b, c));
+    size_t a = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, a, (int *)nullptr, (int64_t *)nullptr, (int)std::max<int64_t>(n + 1, 1));
+    return a;
 }
 
 size_t dag_layout(int64_t n, int64_t nnz, unsigned char *base, DagWs *w) {
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return base ? base + at : nullptr; };
-    const size_t ni = (size_t)(n + 1) * 4, nl = (size_t)(n + 1) * 8;
+    const size_t ni = (size_t)(n + 1) * 4, nl = (size_t)(n + 2) * 8;
     unsigned char *p;
     p = take(ni); if (w) w->remaining = (int *)p;
     p = take(ni); if (w) w->ccount = (int *)p;
     p = take(ni); if (w) w->cursor = (int *)p;
     p = take((size_t)std::max<int64_t>(nnz, 1) * 4); if (w) w->children = (int *)p;
     p = take(ni); if (w) w->order = (int *)p;
-    p = take(ni); if (w) w->lvl_len = (int *)p;
+    p = take(ni); if (w) w->ubv = (int *)p;
     p = take(ni); if (w) w->wide = (int *)p;
-    p = take(64); if (w) { w->tail = (int *)p; w->nwide = (int *)p + 1; w->flags = (int *)p + 2; }
     p = take(nl); if (w) w->coff = (int64_t *)p;
-    p = take(nl); if (w) w->lvl_off = (int64_t *)p;
-    p = take(64); if (w) { w->base = (int64_t *)p; w->max_abs = (unsigned long long *)((int64_t *)p + 1); }
+    p = take(nl); if (w) w->lb = (int64_t *)p;
+    p = take(nl); if (w) w->wlb = (int64_t *)p;
+    // counters, zeroed together: tail, nwide, flags, nlevels, then base, max_abs, total
+    p = take(64);
+    if (w) {
+        w->tail = (int *)p; w->nwide = (int *)p + 1; w->flags = (int *)p + 2; w->nlevels = (int *)p + 3;
+        w->base = (unsigned long long *)(p + 16); w->max_abs = w->base + 1; w->total = w->base + 2;
+    }
     const size_t tb = dag_tmp_bytes(n);
     p = take(tb); if (w) { w->tmp = p; w->tmp_bytes = tb; }
     return o;
+}
+
+int sm_count() {
+    static const int sms = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 152;
+    }();
+    return sms;
 }
 
 }  // namespace
@@ -414,6 +641,7 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
     const int64_t n = A->n_rows;
     *nnz = 0; *max_abs = 0; *levels = 0;
     if (n == 0) return RBG_OK;
+    if (n >= (1ll << 31) - 1) return RBG_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int64_t annz = 0;
     RBG_CUDA_TRY(cudaMemcpyAsync(&annz, A->indptr + n, 8, cudaMemcpyDeviceToHost, s));
@@ -421,87 +649,74 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
     if (workspace_bytes < (int64_t)dag_layout(n, annz, nullptr, nullptr)) return RBG_ERR_NOMEM;
     DagWs w;
     dag_layout(n, annz, reinterpret_cast<unsigned char *>(workspace), &w);
-    const int *aj = reinterpret_cast<const int *>(A->indices);
-    const int *av = reinterpret_cast<const int *>(A->data);
-    const int g = grid_for(n, 256);
-    // ---- levels
-    RBG_CUDA_TRY(cudaMemsetAsync(w.ccount, 0, (size_t)(n + 1) * 4, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.cursor, 0, (size_t)(n + 1) * 4, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.tail, 0, 64, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.base, 0, 64, s));
-    note_launches(2);
-    dag_indeg_kernel<<<g, 256, 0, s>>>(n, A->indptr, aj, w.remaining, w.ccount);
-    size_t tb = w.tmp_bytes;
-    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.ccount, w.coff, (int)(n + 1), s));
-    dag_children_kernel<<<g, 256, 0, s>>>(n, A->indptr, aj, w.coff, w.cursor, w.children);
-    note_launches(1);
-    dag_roots_kernel<<<g, 256, 0, s>>>(n, w.remaining, w.order, w.tail);
-    std::vector<int64_t> bounds{0};
-    int tail = 0;
-    RBG_CUDA_TRY(cudaMemcpyAsync(&tail, w.tail, 4, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    while (tail > bounds.back()) {
-        const int64_t ls = bounds.back(), le = tail;
-        bounds.push_back(le);
-        note_launches(1);
-        dag_level_kernel<<<grid_for(le - ls, 256), 256, 0, s>>>(w.order, ls, le, w.coff, w.children, w.remaining,
-                                                                w.order, w.tail);
-        RBG_CUDA_TRY(cudaMemcpyAsync(&tail, w.tail, 4, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    }
-    *levels = (int64_t)bounds.size() - 1;
-    if (tail < n) return RBG_ERR_CYCLE;          // vertices on (or below) a cycle were never placed
-    // ---- rows, level by level
     static const int configured = [] {
-        RBG_CUDA_TRY(cudaFuncSetAttribute(dag_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(sizeof(DagTable<DG_WSLOTS>) * DG_WARPS)));
         RBG_CUDA_TRY(cudaFuncSetAttribute(dag_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(sizeof(DagTable<DG_WSLOTS>) * DG_WARPS)));
-        RBG_CUDA_TRY(cudaFuncSetAttribute(dag_count_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sizeof(DagTable<DG_BSLOTS>)));
         RBG_CUDA_TRY(cudaFuncSetAttribute(dag_fill_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)sizeof(DagTable<DG_BSLOTS>)));
         return (int)RBG_OK;
     }();
     if (configured) return configured;
     DagArgs a;
-    a.n = n; a.ap = A->indptr; a.aj = aj; a.av = av; a.order = w.order;
-    a.row_off = row_off; a.row_len = row_len;
-    a.pcols = pool_cols; a.pvals = pool_vals; a.wcols = pool_cols; a.wvals = pool_vals;
-    a.capacity = pool_capacity; a.lvl_len = w.lvl_len; a.lvl_off = w.lvl_off;
-    a.wide = w.wide; a.nwide = w.nwide; a.max_abs = w.max_abs; a.flags = w.flags;
+    a.n = n; a.ap = A->indptr; a.aj = reinterpret_cast<const int *>(A->indices);
+    a.av = reinterpret_cast<const int *>(A->data);
+    a.order = w.order; a.tail = w.tail; a.lb = w.lb;
+    a.coff = w.coff; a.children = w.children; a.remaining = w.remaining;
+    a.row_off = row_off; a.row_len = row_len; a.ubv = w.ubv;
+    a.pcols = pool_cols; a.pvals = pool_vals; a.capacity = pool_capacity;
+    a.base = w.base; a.wide = w.wide; a.nwide = w.nwide; a.wlb = w.wlb;
+    a.max_abs = w.max_abs; a.total = w.total; a.flags = w.flags; a.nlevels = w.nlevels;
+    const int g = grid_for(n, 256);
+    const int sms = sm_count();
+    // ---- parents -> children lists and level 0
+    RBG_CUDA_TRY(cudaMemsetAsync(w.ccount, 0, (size_t)(n + 1) * 4, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.cursor, 0, (size_t)(n + 1) * 4, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.tail, 0, 64, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.lb, 0, 8, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.wlb, 0, 8, s));
+    note_launches(4);
+    dag_indeg_kernel<<<g, 256, 0, s>>>(n, A->indptr, a.aj, w.remaining, w.ccount);
+    size_t tb = w.tmp_bytes;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.ccount, w.coff, (int)(n + 1), s));
+    dag_children_kernel<<<g, 256, 0, s>>>(n, A->indptr, a.aj, w.coff, w.cursor, w.children);
+    dag_roots_kernel<<<grid_for(n, 256), 256, 0, s>>>(a);
+    // ---- levels, launched in chunks; every kernel reads its level's bounds on the device
     const size_t wsm = sizeof(DagTable<DG_WSLOTS>) * DG_WARPS, bsm = sizeof(DagTable<DG_BSLOTS>);
-    int64_t placed = 0;
-    for (size_t L = 0; L + 1 < bounds.size(); ++L) {
-        const int64_t ls = bounds[L];
-        const int nl = (int)(bounds[L + 1] - ls);
-        RBG_CUDA_TRY(cudaMemsetAsync(w.nwide, 0, 4, s));
-        note_launches(6);
-        const int cg = grid_for((int64_t)nl * 32, DG_WARPS * 32);
-        dag_count_kernel<<<cg, DG_WARPS * 32, wsm, s>>>(a, ls, nl);
-        dag_count_block_kernel<<<grid_for(304, 1), DG_BTHREADS, bsm, s>>>(a, ls);   // wide rows are rare
-        tb = w.tmp_bytes;
-        RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.lvl_len, w.lvl_off, nl, s));
-        dag_place_kernel<<<grid_for(nl, 256), 256, 0, s>>>(a, ls, nl, w.base);
-        dag_advance_kernel<<<1, 32, 0, s>>>(w.lvl_off, w.lvl_len, nl, w.base);
-        int fl[3] = {0, 0, 0};
-        RBG_CUDA_TRY(cudaMemcpyAsync(&placed, w.base, 8, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaMemcpyAsync(fl, w.tail, 12, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaStreamSynchronize(s));
-        if (fl[2]) { *nnz = -1; return RBG_ERR_CAPACITY; }          // a row wider than the block table
-        if (placed > pool_capacity) {                               // rows of later levels need these
-            *nnz = std::max<int64_t>(2 * pool_capacity, placed + placed / 2 + 1024);
-            return RBG_ERR_CAPACITY;
+    const int fill_grid = sms * 6, disc_grid = sms * 8, block_grid = sms;
+    int64_t L = 0, chunk = 8;
+    while (true) {
+        const int64_t Lend = std::min<int64_t>(L + chunk, n);
+        for (; L < Lend; ++L) {
+            note_launches(3);
+            dag_fill_kernel<<<fill_grid, DG_WARPS * 32, wsm, s>>>(a, L);
+            dag_fill_block_kernel<<<block_grid, DG_BTHREADS, bsm, s>>>(a, L);
+            dag_discover_kernel<<<disc_grid, 256, 0, s>>>(a, L);
         }
-        dag_fill_kernel<<<cg, DG_WARPS * 32, wsm, s>>>(a, ls, nl);
-        dag_fill_block_kernel<<<grid_for(304, 1), DG_BTHREADS, bsm, s>>>(a, ls);
         RBG_CUDA_TRY(cudaGetLastError());
+        // level L is empty when the order has not grown past its start (written by fill(L - 1))
+        int tail = 0;
+        int64_t start = 0;
+        RBG_CUDA_TRY(cudaMemcpyAsync(&tail, w.tail, 4, cudaMemcpyDeviceToHost, s));
+        RBG_CUDA_TRY(cudaMemcpyAsync(&start, w.lb + L, 8, cudaMemcpyDeviceToHost, s));
+        RBG_CUDA_TRY(cudaStreamSynchronize(s));
+        if ((int64_t)tail <= start || L >= n) break;
+        chunk *= 2;
     }
-    unsigned long long mx = 0;
-    RBG_CUDA_TRY(cudaMemcpyAsync(&mx, w.max_abs, 8, cudaMemcpyDeviceToHost, s));
+    int cnt[4] = {0, 0, 0, 0};
+    unsigned long long tot[3] = {0, 0, 0};
+    RBG_CUDA_TRY(cudaMemcpyAsync(cnt, w.tail, 16, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(tot, w.base, 24, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    *nnz = placed;
-    *max_abs = (int64_t)mx;
+    *levels = cnt[3];
+    if (cnt[0] < n) return RBG_ERR_CYCLE;        // vertices on (or below) a cycle were never placed
+    if (cnt[2] & 2) { *nnz = -1; return RBG_ERR_CAPACITY; }
+    if (cnt[2] & 1) {
+        const int64_t reserved = (int64_t)tot[0];
+        *nnz = std::max<int64_t>(2 * pool_capacity, reserved + reserved / 2 + 1024);
+        return RBG_ERR_CAPACITY;
+    }
+    *nnz = (int64_t)tot[2];
+    *max_abs = (int64_t)tot[1];
     return RBG_OK;
 }
 
@@ -521,8 +736,8 @@ extern "C" int32_t rbg_dag_gather(int64_t n, const int32_t *pool_cols, const int
     dag_len64_kernel<<<grid_for(n + 1, 256), 256, 0, s>>>(n, row_len, len64);
     RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, len64, indptr, (int)(n + 1), s));
     if (n > 0)
-        dag_gather_rows_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(n, row_off, pool_cols, pool_vals, indptr,
-                                                                     indices, data);
+        dag_gather_rows_kernel<<<grid_for(n * 8, 256), 256, 0, s>>>(n, row_off, pool_cols, pool_vals, indptr,
+                                                                    indices, data);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }

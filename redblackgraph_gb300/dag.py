@@ -3,8 +3,9 @@
 The reference's sparse DAG closure (redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:
 168-351) builds every vertex's row from its parents' closed rows; here all rows of one
 topological level are built at once on the device.  The closure rows land in a row pool whose
-size is not known in advance: the pool starts at a multiple of nnz(A) and grows (the call is
-repeated) when the library reports it too small.
+size is not known in advance (each row reserves its bound: stored entries plus its parents' row
+lengths): the pool starts at a multiple of nnz(A) and grows (the call is repeated) when the
+library reports it too small.
 """
 from __future__ import annotations
 
@@ -22,7 +23,7 @@ class RowTooWide(RuntimeError):
     """A closure row has more distinct columns than the level kernels hold (8192)."""
 
 
-def dag_closure_device(A: DeviceCSR, stream=None, pool_factor: int = 12):
+def dag_closure_device(A: DeviceCSR, stream=None, pool_factor: int = 16):
     """Closure of the DAG ``A`` (int32 values).  Returns ``(C, max_abs, levels)``: the closure as
     a DeviceCSR (int64 row pointers, int32 indices and values, rows sorted), the largest magnitude
     among A's entries and all candidates (the reference's diameter source) and the number of
