@@ -10,10 +10,13 @@
 // joins the next level when its last parent's row is done.  The kernel that discovers a vertex
 // also bounds its row (stored entries + the lengths of its parents' rows) and reserves that many
 // slots of a caller-provided row pool (one atomic per warp), so each level then needs a single
-// fill pass: one warp per row walks the row's candidates (a warp scan over the segments "stored
-// entry, then that parent's row" and a shuffle binary search give every lane its candidate), and
-//   - up to 64 candidates: sorts (column, value) keys in registers and keeps the first of each
-//     column (the signed minimum of the non-zero values, a stored zero when there is none);
+// fill pass: one warp per row walks the row's candidates (a warp scan over the segment lengths and
+// a shuffle binary search give every lane its candidate), and
+//   - up to 128 candidates: orders (column, value) keys in registers and keeps the first of each
+//     column (the signed minimum of the non-zero values, a stored zero when there is none), by
+//     bitonic merges of the row's sorted runs (stored entries, each parent's row) when there are
+//     few runs, else by a bitonic sort (up to 64); rows of up to 8 (16) candidates take 8 (16)
+//     lanes each, so a warp fills four (two) at once;
 //   - up to 256: folds them into a per-warp shared-memory table and sorts the occupied slots;
 //   - more: the row goes to a 512-thread block with an 8192-slot table.
 // The host launches levels in chunks without waiting (every kernel reads its level's bounds from
@@ -30,7 +33,6 @@
 namespace rbg {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int DG_REG = 64;              // register path: candidates per row
 constexpr int DG_WSLOTS = 256;          // warp table slots (candidates per row)
 constexpr int DG_WARPS = 8;             // warps per CTA of the fill pass
 constexpr int DG_BSLOTS = 8192;         // block table slots (distinct columns)
@@ -46,13 +48,22 @@ template <int SLOTS> struct DagTable {
     unsigned long long list[SLOTS];     // (column << 32 | slot) of the occupied slots
 };
 
+// The row at one position of the order, written when the vertex is discovered so that the fill
+// pass starts from one coalesced record.
+struct __align__(16) DagRec {
+    long long off;                                       // pool position (-1: skipped)
+    long long e0;                                        // first stored entry
+    int v, ub, na, pad;
+};
+constexpr int DG_DESC_LEN_BITS = 24;
+
 struct DagArgs {
     int64_t n;
     const int64_t *ap; const int *aj; const int *av;     // A (int32 values)
     int *order; int *tail;                               // vertices by level; vertices placed
     int64_t *lb;                                         // lb[L]: first position of level L in order
     const int64_t *coff; const int *children; int *remaining;
-    int64_t *row_off; int *row_len; int *ubv;            // pool position, length, bound of each row
+    int64_t *row_off; int *row_len;                      // pool position and length of each row
     int *pcols; int *pvals; int64_t capacity;            // the row pool
     unsigned long long *base;                            // pool slots reserved so far
     int *wide; int *nwide; int64_t *wlb;                 // block-tier rows; wlb[L]: first of level L
@@ -60,7 +71,10 @@ struct DagArgs {
     unsigned long long *total;                           // entries written
     int *flags;                                          // 1: pool too small, 2: row past the block table
     int *nlevels;
+    DagRec *rec;                                         // per order position: the row to fill
+    unsigned long long *desc;                            // per stored entry: parent row (offset << 24 | length)
 };
+
 
 __device__ __forceinline__ int dag_abs(int v) { return v > 0 ? v : (int)(0u - (unsigned)v); }
 
@@ -114,54 +128,55 @@ __device__ __forceinline__ void dag_clear(DagTable<SLOTS> &H, int S, int lane, i
 }
 
 // ----------------------------------------------------------------------------- candidate walk
-// The candidates of row v, flattened: stored entry e of the row opens a segment of 1 + len(w)
+// The candidates of a row, flattened: stored entry e of the row opens a segment of 1 + len(w)
 // positions (the entry itself, then A[v][w] (x) C[w][f] for f < len(w); len = 0 when w == v).
-// One chunk of up to 32 stored entries at a time: lane j holds chunk entry j.
+// A group of G lanes (G = 8, 16 or 32; lane gl of the group) walks one row, one chunk of up to
+// G stored entries at a time: lane gl holds chunk entry gl.
 struct DagSeg {
     int w, avw, len, excl;
     int64_t off;
 };
 
-// Load chunk entry `lane` of row v (stored entries [e0, e1)) and scan the segment lengths;
-// returns the chunk's candidate count (all lanes).
-__device__ __forceinline__ int dag_seg_load(const DagArgs &a, int v, int64_t e0, int64_t e1, int lane, DagSeg &sg) {
-    const int64_t e = e0 + lane;
+// Load chunk entry gl of a row (stored entries [e0, e1)) and scan the segment lengths over the
+// group; returns the chunk's candidate count (all lanes of the group).
+template <int G>
+__device__ __forceinline__ int dag_seg_load(const DagArgs &a, int64_t e0, int64_t e1, int gl, DagSeg &sg) {
+    const int64_t e = e0 + gl;
     sg.w = -1; sg.avw = 0; sg.len = 0; sg.off = 0;
     int cnt = 0;
     if (e < e1) {
         sg.w = a.aj[e];
         sg.avw = a.av[e];
-        cnt = 1;
-        if (sg.w != v && sg.w >= 0 && sg.w < a.n) {
-            sg.len = a.row_len[sg.w];
-            sg.off = a.row_off[sg.w];
-            cnt += sg.len;
-        }
+        const unsigned long long d = a.desc[e];  // zero for the diagonal and invalid columns
+        sg.len = (int)(d & ((1ull << DG_DESC_LEN_BITS) - 1));
+        sg.off = (int64_t)(d >> DG_DESC_LEN_BITS);
+        cnt = 1 + sg.len;
     }
     int incl = cnt;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
+    for (int o = 1; o < G; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o, G);
+        if (gl >= o) incl += t;
     }
     sg.excl = incl - cnt;
-    return __shfl_sync(FULL, incl, 31);
+    return __shfl_sync(FULL, incl, G - 1, G);
 }
 
 // Candidate at chunk position idx (< the chunk's count when `in`): returns false for a zero
 // product (no candidate); else its column and value.  Every lane must call it (shuffles).
+template <int G>
 __device__ __forceinline__ bool dag_candidate(const DagArgs &a, const DagSeg &sg, int idx, bool in, int &col,
                                               int &val) {
     int lo = 0;                                  // last segment starting at or before idx
 #pragma unroll
-    for (int st = 16; st > 0; st >>= 1) {
-        const int x = __shfl_sync(FULL, sg.excl, lo + st);
+    for (int st = G / 2; st > 0; st >>= 1) {
+        const int x = __shfl_sync(FULL, sg.excl, lo + st, G);
         if (x <= idx) lo += st;
     }
-    const int w = __shfl_sync(FULL, sg.w, lo);
-    const int avw = __shfl_sync(FULL, sg.avw, lo);
-    const int64_t off = __shfl_sync(FULL, sg.off, lo);
-    const int x0 = __shfl_sync(FULL, sg.excl, lo);
+    const int w = __shfl_sync(FULL, sg.w, lo, G);
+    const int avw = __shfl_sync(FULL, sg.avw, lo, G);
+    const int64_t off = __shfl_sync(FULL, sg.off, lo, G);
+    const int x0 = __shfl_sync(FULL, sg.excl, lo, G);
     if (!in) return false;
     const int f = idx - x0;
     if (f == 0) {                                // the stored entry itself (a zero is kept)
@@ -175,33 +190,29 @@ __device__ __forceinline__ bool dag_candidate(const DagArgs &a, const DagSeg &sg
 }
 
 // ----------------------------------------------------------------------------- register sorts
-__device__ __forceinline__ unsigned long long dag_sort32(unsigned long long v, int lane) {
+// Bitonic sort of G * H keys held H per lane of a G-lane group (element i = gl + G h).
+template <int G, int H>
+__device__ __forceinline__ void dag_sort(unsigned long long (&v)[H], int gl) {
 #pragma unroll
-    for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const unsigned long long o = __shfl_xor_sync(FULL, v, j);
-            const bool up = (lane & k) == 0, lower = (lane & j) == 0;
-            v = (lower == up) ? min(v, o) : max(v, o);
-        }
-    }
-    return v;
-}
-
-__device__ __forceinline__ void dag_sort64(unsigned long long (&v)[2], int lane) {
-#pragma unroll
-    for (int k = 2; k <= 64; k <<= 1) {
+    for (int k = 2; k <= G * H; k <<= 1) {
 #pragma unroll
         for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j == 32) {
-                const unsigned long long lo = min(v[0], v[1]), hi = max(v[0], v[1]);
-                v[0] = lo;
-                v[1] = hi;
+            if (j >= G) {                        // partners in the same lane
+                const int hj = j / G;
+#pragma unroll
+                for (int h = 0; h < H; ++h) {
+                    if (h & hj) continue;
+                    const bool up = ((gl + G * h) & k) == 0;
+                    const unsigned long long x = v[h], y = v[h | hj];
+                    const unsigned long long lo = min(x, y), hi = max(x, y);
+                    v[h] = up ? lo : hi;
+                    v[h | hj] = up ? hi : lo;
+                }
             } else {
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int i = lane + 32 * h;
-                    const unsigned long long o = __shfl_xor_sync(FULL, v[h], j);
+                for (int h = 0; h < H; ++h) {
+                    const int i = gl + G * h;
+                    const unsigned long long o = __shfl_xor_sync(FULL, v[h], j, G);
                     const bool up = (i & k) == 0, lower = (i & j) == 0;
                     v[h] = (lower == up) ? min(v[h], o) : max(v[h], o);
                 }
@@ -210,9 +221,161 @@ __device__ __forceinline__ void dag_sort64(unsigned long long (&v)[2], int lane)
     }
 }
 
+// One row per G-lane group (group g = lane / G) of at most G H candidates from at most G stored
+// entries: keys sorted in registers, the first key of every column written at the row's pool
+// position.  Every lane calls it; a group with act == false has no row.  Returns the row length.
+template <int G, int H>
+__device__ __forceinline__ int dag_group_row(const DagArgs &a, bool act, const DagRec &r, int lane, int &best) {
+    const int gl = lane & (G - 1);
+    DagSeg sg;
+    const int T = dag_seg_load<G>(a, r.e0, act ? r.e0 + r.na : r.e0, gl, sg);
+    unsigned long long key[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+        key[h] = DG_PAD;
+        int col = 0, val = 0;
+        if (dag_candidate<G>(a, sg, h * G + gl, h * G + gl < T, col, val)) {
+            key[h] = dag_key(col, val);
+            best = max(best, dag_abs(val));
+        }
+    }
+    dag_sort<G, H>(key, gl);
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned gm = G == 32 ? FULL : ((1u << G) - 1u) << (lane & ~(G - 1));
+    int nd = 0;
+    unsigned long long carry = DG_PAD;            // the group's last key of the previous register
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+        const unsigned long long up1 = __shfl_up_sync(FULL, key[h], 1, G);
+        const unsigned long long prev = gl == 0 ? carry : up1;
+        const bool head = key[h] != DG_PAD && ((gl == 0 && h == 0) || (prev >> 32) != (key[h] >> 32));
+        const unsigned bal = __ballot_sync(FULL, head) & gm;
+        if (head) {
+            const int q = nd + __popc(bal & lt);
+            a.pcols[r.off + q] = (int)(key[h] >> 32);
+            a.pvals[r.off + q] = dag_key_val(key[h]);
+        }
+        nd += __popc(bal);
+        carry = __shfl_sync(FULL, key[h], G - 1, G);
+    }
+    return nd;
+}
+
+// ----------------------------------------------------------------------------- merge of sorted runs
+// A row's candidates are sorted runs: its stored entries (ascending columns) and each parent's
+// closed row times the edge value (ascending columns).  With merge keys (column, zero-product
+// flag, value code) a run stays sorted with its zero products in place.  The stored run goes to
+// the front of a window of G H positions; each parent run then goes, descending, to the end of
+// the window, which makes the window bitonic, and one bitonic merge (log2(G H) steps) sorts it.
+// After the last merge the first key of a column carries the column's value, or the flag when
+// the column has no candidate.
+__device__ __forceinline__ unsigned long long dag_mkey(int col, int v) {
+    unsigned e = 0xffffffffu;
+    if (v != 0) e = ((unsigned)v ^ 0x80000000u) - (v > 0 ? 1u : 0u);
+    return ((unsigned long long)(unsigned)col << 33) | e;
+}
+__device__ __forceinline__ unsigned long long dag_mkey_drop(int col) {
+    return ((unsigned long long)(unsigned)col << 33) | (1ull << 32) | 0xffffffffull;
+}
+
+template <int G, int H>
+__device__ __forceinline__ void dag_merge_asc(unsigned long long (&v)[H], int gl) {
+#pragma unroll
+    for (int j = G * H / 2; j > 0; j >>= 1) {
+        if (j >= G) {
+            const int hj = j / G;
+#pragma unroll
+            for (int h = 0; h < H; ++h) {
+                if (h & hj) continue;
+                const unsigned long long x = v[h], y = v[h | hj];
+                v[h] = min(x, y);
+                v[h | hj] = max(x, y);
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < H; ++h) {
+                const unsigned long long o = __shfl_xor_sync(FULL, v[h], j, G);
+                v[h] = (gl & j) == 0 ? min(v[h], o) : max(v[h], o);
+            }
+        }
+    }
+}
+
+__host__ __device__ constexpr int dag_log2(int x) { return x <= 1 ? 0 : 1 + dag_log2(x / 2); }
+
+// One row per G-lane group, as dag_group_row, by merges of sorted runs.  Returns -1 (nothing
+// written) when the warp should sort instead: a stored run that does not ascend strictly, more
+// stored entries than lanes, or so many parent runs that the merges cost more than a sort.
+template <int G, int H>
+__device__ __forceinline__ int dag_group_row_runs(const DagArgs &a, bool act, const DagRec &r, int lane, int &best) {
+    constexpr int P2 = G * H, LG = dag_log2(G * H);
+    const int gl = lane & (G - 1);
+    const bool has = act && gl < r.na;
+    int w = -1, avw = 0, len = 0;
+    int64_t off = 0;
+    if (has) {
+        w = a.aj[r.e0 + gl];
+        avw = a.av[r.e0 + gl];
+        const unsigned long long d = a.desc[r.e0 + gl];
+        len = (int)(d & ((1ull << DG_DESC_LEN_BITS) - 1));
+        off = (int64_t)(d >> DG_DESC_LEN_BITS);
+    }
+    const int wn = __shfl_down_sync(FULL, w, 1, G);
+    const bool bad = (act && r.na > G) || (has && gl + 1 < r.na && wn <= w);
+    const int runs = __popc(__ballot_sync(FULL, len > 0) & (G == 32 ? FULL : ((1u << G) - 1u) << (lane & ~(G - 1))));
+    const int maxruns = __reduce_max_sync(FULL, (unsigned)runs);
+    if (__any_sync(FULL, bad) || maxruns * LG >= LG * (LG + 1) / 2) return -1;
+    unsigned long long key[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) key[h] = DG_PAD;
+    if (has) {                                   // the stored run: positions [0, na)
+        key[0] = dag_mkey(w, avw);
+        best = max(best, dag_abs(avw));
+    }
+    const int nam = __reduce_max_sync(FULL, act ? (unsigned)r.na : 0u);
+    for (int j = 0; j < nam; ++j) {
+        const int lj = __shfl_sync(FULL, len, j, G);
+        if (!__any_sync(FULL, lj > 0)) continue;
+        const int64_t oj = __shfl_sync(FULL, off, j, G);
+        const int vj = __shfl_sync(FULL, avw, j, G);
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const int p = gl + G * h;
+            if (p >= P2 - lj) {                  // element P2 - 1 - p of the run, descending
+                const int64_t f = oj + (P2 - 1 - p);
+                const int col = a.pcols[f];
+                const int pv = cy_product(vj, a.pvals[f]);
+                key[h] = pv != 0 ? dag_mkey(col, pv) : dag_mkey_drop(col);
+                best = max(best, pv != 0 ? dag_abs(pv) : 0);
+            }
+        }
+        dag_merge_asc<G, H>(key, gl);
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned gm = G == 32 ? FULL : ((1u << G) - 1u) << (lane & ~(G - 1));
+    int nd = 0;
+    unsigned long long carry = DG_PAD;
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+        const unsigned long long up1 = __shfl_up_sync(FULL, key[h], 1, G);
+        const unsigned long long prev = gl == 0 ? carry : up1;
+        const bool head = key[h] != DG_PAD && !((key[h] >> 32) & 1ull) &&
+                          ((gl == 0 && h == 0) || (prev >> 33) != (key[h] >> 33));
+        const unsigned bal = __ballot_sync(FULL, head) & gm;
+        if (head) {
+            const int q = nd + __popc(bal & lt);
+            a.pcols[r.off + q] = (int)(key[h] >> 33);
+            a.pvals[r.off + q] = dag_key_val(key[h]);
+        }
+        nd += __popc(bal);
+        carry = __shfl_sync(FULL, key[h], G - 1, G);
+    }
+    return nd;
+}
+
 // ----------------------------------------------------------------------------- level discovery
 // Append the lanes' ready vertices to the order, bound their rows and reserve their pool slots.
-__device__ __forceinline__ void dag_append(const DagArgs &a, bool ready, int c, long long ub, int lane) {
+__device__ __forceinline__ void dag_append(const DagArgs &a, bool ready, int c, long long ub, int64_t e0, int lane) {
     const unsigned bal = __ballot_sync(FULL, ready);
     if (!bal) return;
     int pos0 = 0;
@@ -230,26 +393,44 @@ __device__ __forceinline__ void dag_append(const DagArgs &a, bool ready, int c, 
     if (lane == 0) b0 = atomicAdd(a.base, (unsigned long long)tot);
     b0 = __shfl_sync(FULL, b0, 0);
     if (ready) {
-        a.order[pos0 + __popc(bal & ((1u << lane) - 1u))] = c;
-        const long long off = (long long)b0 + incl - x;
-        a.ubv[c] = (int)min(x, (long long)INT_MAX);
+        const int pos = pos0 + __popc(bal & ((1u << lane) - 1u));
+        a.order[pos] = c;
+        long long off = (long long)b0 + incl - x;
         if (off + x > a.capacity) {              // past the pool: skipped, the call asks for more
-            a.row_off[c] = -1;
+            off = -1;
             a.row_len[c] = 0;
             atomicOr(a.flags, 1);
-        } else {
-            a.row_off[c] = off;
-            if (x > DG_WSLOTS) a.wide[atomicAdd(a.nwide, 1)] = c;
+        } else if (x > DG_WSLOTS) {
+            a.wide[atomicAdd(a.nwide, 1)] = c;
         }
+        a.row_off[c] = off;
+        DagRec r;
+        r.off = off;
+        r.e0 = e0;
+        r.v = c;
+        r.ub = (int)min(x, (long long)INT_MAX);
+        r.na = (int)(a.ap[c + 1] - e0);
+        r.pad = 0;
+        a.rec[pos] = r;
     }
 }
 
-// Upper bound of row c's length: its stored entries plus its parents' rows.
-__device__ __forceinline__ long long dag_bound(const DagArgs &a, int c) {
+// Upper bound of row c's length (its stored entries plus its parents' rows, all done); records
+// each stored entry's parent row for the fill pass.
+__device__ __forceinline__ long long dag_bound(const DagArgs &a, int c, int64_t &e0) {
     long long ub = 0;
-    for (int64_t q = a.ap[c]; q < a.ap[c + 1]; ++q) {
+    e0 = a.ap[c];
+    for (int64_t q = e0; q < a.ap[c + 1]; ++q) {
         const int x = a.aj[q];
-        ub += 1 + ((x != c && x >= 0 && x < a.n) ? a.row_len[x] : 0);
+        unsigned long long d = 0;
+        if (x != c && x >= 0 && x < a.n) {
+            const int len = a.row_len[x];
+            const int64_t off = a.row_off[x];
+            ub += len;
+            if (len > 0) d = ((unsigned long long)off << DG_DESC_LEN_BITS) | (unsigned long long)len;
+        }
+        a.desc[q] = d;
+        ub += 1;
     }
     return ub;
 }
@@ -285,7 +466,9 @@ __global__ void dag_roots_kernel(DagArgs a) {
     for (int64_t v0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; v0 < a.n; v0 += warps * 32) {
         const int64_t v = v0 + lane;
         const bool ready = v < a.n && a.remaining[v] == 0;
-        dag_append(a, ready, (int)v, ready ? (long long)(a.ap[v + 1] - a.ap[v]) : 0, lane);
+        int64_t e0 = 0;
+        const long long ub = ready ? dag_bound(a, (int)v, e0) : 0;
+        dag_append(a, ready, (int)v, ub, e0, lane);
     }
 }
 
@@ -325,20 +508,22 @@ __global__ void dag_discover_kernel(DagArgs a, int64_t L) {
             bool ready = false;
             int c = 0;
             long long ub = 0;
+            int64_t e0 = 0;
             if (idx < T) {
                 c = a.children[cq + (idx - xq)];
                 if (atomicSub(&a.remaining[c], 1) == 1) {
                     ready = true;
-                    ub = dag_bound(a, c);
+                    ub = dag_bound(a, c, e0);
                 }
             }
-            dag_append(a, ready, c, ub, lane);
+            dag_append(a, ready, c, ub, e0, lane);
         }
     }
 }
 
 // ----------------------------------------------------------------------------- fill passes
 // Write a warp's table (S slots) as a sorted row at pool position o; returns the row length.
+// Up to 64 distinct columns sort in registers, more in shared memory.
 __device__ __forceinline__ int dag_table_row(const DagArgs &a, DagTable<DG_WSLOTS> &H, int S, int64_t o, int lane) {
     int nd = 0;
     for (int s0 = 0; s0 < S; s0 += 32) {
@@ -349,6 +534,23 @@ __device__ __forceinline__ int dag_table_row(const DagArgs &a, DagTable<DG_WSLOT
         nd += __popc(bal);
     }
     __syncwarp();
+    if (nd <= 64) {
+        unsigned long long v[2];
+        v[0] = lane < nd ? H.list[lane] : DG_PAD;
+        v[1] = lane + 32 < nd ? H.list[lane + 32] : DG_PAD;
+        dag_sort<32, 2>(v, lane);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = lane + 32 * h;
+            if (q < nd) {
+                const int sl = (int)(v[h] & 0xffffffffu);
+                a.pcols[o + q] = (int)(v[h] >> 32);
+                a.pvals[o + q] = H.has[sl] ? H.val[sl] : 0;
+            }
+        }
+        __syncwarp();
+        return nd;
+    }
     int P = 32;
     while (P < nd) P <<= 1;
     for (int q = nd + lane; q < P; q += 32) H.list[q] = DG_PAD;
@@ -375,7 +577,44 @@ __device__ __forceinline__ int dag_table_row(const DagArgs &a, DagTable<DG_WSLOT
     return nd;
 }
 
-// One warp per row of level L (rows of up to 256 candidates).  Block 0 closes the level's range.
+// A row of up to 256 candidates through the warp's table (ub >= distinct columns, so a table of
+// ub slots never fills).  Returns the row length.
+__device__ __noinline__ int dag_table_fill(const DagArgs &a, DagTable<DG_WSLOTS> &H, const DagRec &r, int lane,
+                                              int &best) {
+    int S = 32;
+    while (S < r.ub) S <<= 1;
+    dag_clear(H, S, lane, 32);
+    __syncwarp();
+    for (int64_t c0 = r.e0; c0 < r.e0 + r.na; c0 += 32) {
+        DagSeg sg;
+        const int T = dag_seg_load<32>(a, c0, r.e0 + r.na, lane, sg);
+        for (int b = 0; b < T; b += 32) {
+            int col = 0, val = 0;
+            if (dag_candidate<32>(a, sg, b + lane, b + lane < T, col, val)) {
+                best = max(best, dag_abs(val));
+                dag_fold(H, (unsigned)col, val, S - 1);
+            }
+        }
+    }
+    __syncwarp();
+    return dag_table_row(a, H, S, r.off, lane);
+}
+
+__device__ __forceinline__ DagRec dag_shfl_rec(const DagRec &r, int src) {
+    DagRec o;
+    o.off = __shfl_sync(FULL, r.off, src);
+    o.e0 = __shfl_sync(FULL, r.e0, src);
+    o.v = __shfl_sync(FULL, r.v, src);
+    o.ub = __shfl_sync(FULL, r.ub, src);
+    o.na = __shfl_sync(FULL, r.na, src);
+    o.pad = 0;
+    return o;
+}
+
+// Level L's rows of up to 256 candidates, four consecutive rows per warp at a time: four rows of
+// at most 8 candidates fill together (8 lanes each), rows of at most 16 two at a time, larger
+// rows one after the other with the whole warp.  Lanes 8i..8i+7 hold row i's record; the next
+// four records are read before the current rows are filled.  Block 0 closes the level's range.
 __global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int64_t L) {
     extern __shared__ __align__(16) unsigned char dg_smem[];
     const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -388,81 +627,69 @@ __global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int6
     int best = 0;
     unsigned long long written = 0;
     const int64_t warps = (int64_t)gridDim.x * DG_WARPS;
-    for (int64_t k = s + (int64_t)blockIdx.x * DG_WARPS + wi; k < e; k += warps) {
-        const int v = a.order[k];
-        const int64_t o = a.row_off[v];
-        const int ub = a.ubv[v];
-        if (o < 0 || ub > DG_WSLOTS) continue;   // skipped, or the block tier's
-        const int64_t e0 = a.ap[v], e1 = a.ap[v + 1];
-        int nd;
-        if (ub <= DG_REG && e1 - e0 <= 32) {
-            // register path: candidate idx sits in lane idx % 32, slot idx / 32
-            DagSeg sg;
-            const int T = dag_seg_load(a, v, e0, e1, lane, sg);
-            unsigned long long key[2] = {DG_PAD, DG_PAD};
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (h * 32 < T) {
-                    int col = 0, val = 0;
-                    if (dag_candidate(a, sg, h * 32 + lane, h * 32 + lane < T, col, val)) {
-                        key[h] = dag_key(col, val);
-                        best = max(best, dag_abs(val));
-                    }
+    const int64_t nq = (e - s + 3) >> 2;
+    const int sub = lane >> 3;
+    int64_t q = (int64_t)blockIdx.x * DG_WARPS + wi;
+    DagRec cur;
+    bool cv = false;
+    if (q < nq && s + 4 * q + sub < e) {
+        cur = a.rec[s + 4 * q + sub];
+        cv = true;
+    }
+    for (; q < nq; q += warps) {
+        DagRec nxt;
+        bool nv = false;
+        const int64_t kn = s + 4 * (q + warps) + sub;
+        if (q + warps < nq && kn < e) {
+            nxt = a.rec[kn];
+            nv = true;
+        }
+        const bool act = cv && cur.off >= 0 && cur.ub <= DG_WSLOTS;   // else skipped, or the block tier's
+        const int tm = __reduce_max_sync(FULL, act ? cur.ub : 0);
+        if (tm <= 8) {
+            const int nd = dag_group_row<8, 1>(a, act, cur, lane, best);
+            if ((lane & 7) == 0 && act) {
+                a.row_len[cur.v] = nd;
+                written += (unsigned long long)nd;
+            }
+        } else if (tm <= 16) {
+            for (int p = 0; p < 2; ++p) {
+                const int src = (2 * p + (lane >> 4)) * 8;
+                const DagRec r = dag_shfl_rec(cur, src);
+                const bool ra = __shfl_sync(FULL, (int)act, src) != 0;
+                const int nd = dag_group_row<16, 1>(a, ra, r, lane, best);
+                if ((lane & 15) == 0 && ra) {
+                    a.row_len[r.v] = nd;
+                    written += (unsigned long long)nd;
                 }
             }
-            bool head[2];
-            if (T <= 32) {
-                key[0] = dag_sort32(key[0], lane);
-                const unsigned long long prev = __shfl_up_sync(FULL, key[0], 1);
-                head[0] = key[0] != DG_PAD && (lane == 0 || (prev >> 32) != (key[0] >> 32));
-                head[1] = false;
-            } else {
-                dag_sort64(key, lane);
-                const unsigned long long p0 = __shfl_up_sync(FULL, key[0], 1);
-                const unsigned long long p1 = __shfl_up_sync(FULL, key[1], 1);
-                const unsigned long long l31 = __shfl_sync(FULL, key[0], 31);
-                head[0] = key[0] != DG_PAD && (lane == 0 || (p0 >> 32) != (key[0] >> 32));
-                head[1] = key[1] != DG_PAD && ((lane == 0 ? l31 : p1) >> 32) != (key[1] >> 32);
-            }
-            const unsigned b0 = __ballot_sync(FULL, head[0]), b1 = __ballot_sync(FULL, head[1]);
-            const unsigned lt = (1u << lane) - 1u;
-            if (head[0]) {
-                const int r = __popc(b0 & lt);
-                a.pcols[o + r] = (int)(key[0] >> 32);
-                a.pvals[o + r] = dag_key_val(key[0]);
-            }
-            if (head[1]) {
-                const int r = __popc(b0) + __popc(b1 & lt);
-                a.pcols[o + r] = (int)(key[1] >> 32);
-                a.pvals[o + r] = dag_key_val(key[1]);
-            }
-            nd = __popc(b0) + __popc(b1);
         } else {
-            // table path: ub >= distinct columns, so a table of ub slots never fills
-            int S = 32;
-            while (S < ub) S <<= 1;
-            dag_clear(H, S, lane, 32);
-            __syncwarp();
-            for (int64_t c0 = e0; c0 < e1; c0 += 32) {
-                DagSeg sg;
-                const int T = dag_seg_load(a, v, c0, e1, lane, sg);
-                for (int b = 0; b < T; b += 32) {
-                    int col = 0, val = 0;
-                    if (dag_candidate(a, sg, b + lane, b + lane < T, col, val)) {
-                        best = max(best, dag_abs(val));
-                        dag_fold(H, (unsigned)col, val, S - 1);
-                    }
+            for (int i = 0; i < 4; ++i) {
+                const DagRec r = dag_shfl_rec(cur, 8 * i);
+                if (__shfl_sync(FULL, (int)act, 8 * i) == 0) continue;
+                int nd = -1;
+                if (r.ub <= 32) {
+                    nd = dag_group_row_runs<32, 1>(a, true, r, lane, best);
+                    if (nd < 0) nd = dag_group_row<32, 1>(a, true, r, lane, best);
+                } else if (r.ub <= 64 && r.na <= 32) {
+                    nd = dag_group_row_runs<32, 2>(a, true, r, lane, best);
+                    if (nd < 0) nd = dag_group_row<32, 2>(a, true, r, lane, best);
+                } else if (r.ub <= 128 && r.na <= 32) {
+                    nd = dag_group_row_runs<32, 4>(a, true, r, lane, best);
+                }
+                if (nd < 0) nd = dag_table_fill(a, H, r, lane, best);
+                if (lane == 0) {
+                    a.row_len[r.v] = nd;
+                    written += (unsigned long long)nd;
                 }
             }
-            __syncwarp();
-            nd = dag_table_row(a, H, S, o, lane);
         }
-        if (lane == 0) {
-            a.row_len[v] = nd;
-            written += (unsigned long long)nd;
-        }
+        cur = nxt;
+        cv = nv;
     }
     best = __reduce_max_sync(FULL, best);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) written += __shfl_xor_sync(FULL, written, o);   // group leaders' counts
     if (lane == 0) {
         if (best > 0) atomicMax(a.max_abs, (unsigned long long)best);
         if (written) atomicAdd(a.total, written);
@@ -574,10 +801,11 @@ using namespace rbg;
 namespace {
 
 struct DagWs {
-    int *remaining, *ccount, *cursor, *children, *order, *ubv, *wide;
+    int *remaining, *ccount, *cursor, *children, *order, *wide;
     int *tail, *nwide, *flags, *nlevels;
     int64_t *coff, *lb, *wlb;
-    unsigned long long *base, *max_abs, *total;
+    unsigned long long *base, *max_abs, *total, *desc;
+    DagRec *rec;
     void *tmp;
     size_t tmp_bytes;
 };
@@ -598,7 +826,8 @@ size_t dag_layout(int64_t n, int64_t nnz, unsigned char *base, DagWs *w) {
     p = take(ni); if (w) w->cursor = (int *)p;
     p = take((size_t)std::max<int64_t>(nnz, 1) * 4); if (w) w->children = (int *)p;
     p = take(ni); if (w) w->order = (int *)p;
-    p = take(ni); if (w) w->ubv = (int *)p;
+    p = take((size_t)(n + 1) * sizeof(DagRec)); if (w) w->rec = (DagRec *)p;
+    p = take((size_t)std::max<int64_t>(nnz, 1) * 8); if (w) w->desc = (unsigned long long *)p;
     p = take(ni); if (w) w->wide = (int *)p;
     p = take(nl); if (w) w->coff = (int64_t *)p;
     p = take(nl); if (w) w->lb = (int64_t *)p;
@@ -662,7 +891,7 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
     a.av = reinterpret_cast<const int *>(A->data);
     a.order = w.order; a.tail = w.tail; a.lb = w.lb;
     a.coff = w.coff; a.children = w.children; a.remaining = w.remaining;
-    a.row_off = row_off; a.row_len = row_len; a.ubv = w.ubv;
+    a.row_off = row_off; a.row_len = row_len; a.rec = w.rec; a.desc = w.desc;
     a.pcols = pool_cols; a.pvals = pool_vals; a.capacity = pool_capacity;
     a.base = w.base; a.wide = w.wide; a.nwide = w.nwide; a.wlb = w.wlb;
     a.max_abs = w.max_abs; a.total = w.total; a.flags = w.flags; a.nlevels = w.nlevels;
@@ -682,8 +911,15 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
     dag_roots_kernel<<<grid_for(n, 256), 256, 0, s>>>(a);
     // ---- levels, launched in chunks; every kernel reads its level's bounds on the device
     const size_t wsm = sizeof(DagTable<DG_WSLOTS>) * DG_WARPS, bsm = sizeof(DagTable<DG_BSLOTS>);
-    const int fill_grid = sms * 6, disc_grid = sms * 8, block_grid = sms;
-    int64_t L = 0, chunk = 8;
+    static const int fill_per_sm = [wsm] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, dag_fill_kernel, DG_WARPS * 32, wsm) != cudaSuccess || b < 1)
+            b = 4;
+        return b;
+    }();
+    const int fill_grid = sms * fill_per_sm, disc_grid = sms * 8, block_grid = sms;
+    const int64_t chunk = 8;
+    int64_t L = 0;
     while (true) {
         const int64_t Lend = std::min<int64_t>(L + chunk, n);
         for (; L < Lend; ++L) {
@@ -700,7 +936,6 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
         RBG_CUDA_TRY(cudaMemcpyAsync(&start, w.lb + L, 8, cudaMemcpyDeviceToHost, s));
         RBG_CUDA_TRY(cudaStreamSynchronize(s));
         if ((int64_t)tail <= start || L >= n) break;
-        chunk *= 2;
     }
     int cnt[4] = {0, 0, 0, 0};
     unsigned long long tot[3] = {0, 0, 0};

@@ -238,3 +238,28 @@ def test_dag_cycle_below_a_dag(native):
         transitive_closure_dag_sparse(A)
     with pytest.raises(CycleError):
         transitive_closure_dag_gpu(CSRMatrixGPU.from_cpu(A))
+
+
+def test_dag_explicit_zeros_and_deep_rows(native):
+    """Stored zeros stay in the closure (a zero product adds nothing), rows of 33-256 candidates
+    take the merge of sorted runs; both against the oracle's parents-first closure."""
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse
+    A = sp.lil_matrix(synth.forest(1500, 20, 11, family=40, reach=3, dtype=np.int32))
+    n = A.shape[0]
+    rng = np.random.default_rng(3)
+    roots = [v for v in range(n) if A[v].nnz == 1]
+    for v in rng.choice(n, size=40, replace=False):
+        w = int(rng.choice(roots))
+        if w != v and A[v, w] == 0:
+            A[v, w] = 1          # placeholder, set to an explicit zero below
+    A = sp.csr_matrix(A)
+    A.data[A.data == 1] = np.where(A.indices[A.data == 1] == np.repeat(np.arange(n), np.diff(A.indptr))[A.data == 1],
+                                   1, 0)
+    assert (A.data == 0).sum() > 0
+    W, d = O.dag_closure(A)
+    r = transitive_closure_dag_sparse(A)
+    assert same(r.W, W) and r.diameter == d
+    assert (sp.csr_matrix(W).data == 0).sum() > 0
+    lens = np.diff(sp.csr_matrix(W).indptr)
+    assert lens.max() > 32
