@@ -255,7 +255,7 @@ int32_t rbg_dag_workspace_bytes(int64_t n, int64_t nnz, int64_t *bytes);
  * stored entry or candidate (the reference's diameter source); RBG_ERR_CAPACITY when the pool
  * is too small (*nnz = a size to retry with) or a row has more than 8192 distinct columns
  * (*nnz = -1); RBG_ERR_CYCLE when the graph has a cycle.  *levels (host) = topological
- * levels.  Synchronises `stream` (once per level).
+ * levels.  Synchronises `stream` once per eight levels.
  */
 int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t workspace_bytes, int32_t *pool_cols,
                         int32_t *pool_vals, int64_t pool_capacity, int64_t *row_off, int32_t *row_len,
