@@ -385,6 +385,53 @@ typedef struct rbg_lookup_t {
 int32_t rbg_relationship_lookup(int64_t count, const rbg_lookup_t *queries, int64_t *out,
                                 rbg_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Relational composition: the closure of a closed graph after adding one vertex or one edge,
+ * without recomputing the closure (replaces the C core gufuncs vertex_relational_composition
+ * and edge_relational_composition, redblackgraph/core/src/redblackgraph/
+ * relational_composition.c.in:72-262, and with RBG_MODE_CYTHON their Cython counterparts,
+ * redblackgraph/sparse/csgraph/_relational_composition.pyx:10-113, int32 only).
+ * ---------------------------------------------------------------------------------------- */
+typedef struct rbg_compose_result {
+    int32_t status;   /* RBG_OK; RBG_ERR_OVERFLOW (a product overflowed, or would make the
+                         reference's MSB loop run forever: RBG_EV_HANG in `event`);
+                         RBG_ERR_CYCLE (vertex composition: the new vertex closes a cycle)    */
+    uint32_t flags;   /* RBG_EV_* over every product                                        */
+    uint32_t event;   /* RBG_EV_* of the deciding product (RBG_ERR_OVERFLOW)                */
+    int32_t reserved;
+    int64_t step;     /* reference loop of the deciding event: 1 (u (x) R), 2 (R (x) v; edge:
+                         the update), 3 (the cycle check), 4 (vertex update); -1 when OK     */
+    int64_t i, j;     /* its row and column (step 3: i = the vertex index k)                */
+    int64_t lhs, rhs; /* its operands (step 3: u_k, v_k), value bits widened from the type  */
+    int64_t updated;  /* entries in the updated rectangle                                   */
+} rbg_compose_result_t;
+
+/* Scratch bytes rbg_vertex_compose / rbg_edge_compose need for an n x n closure. */
+int32_t rbg_compose_workspace_bytes(int32_t dtype, int64_t n, int64_t *bytes);
+
+/*
+ * R_lambda = the closure of closed R (n x n, leading dimension ldr, `dtype`) with a new vertex:
+ * u (its row, n values), v (its column, n values), colour `color`.  out is (n + 1) x (n + 1)
+ * with leading dimension ldo >= n + 1; out == R (same ld) updates in place, touching only the
+ * rows reaching the new vertex x the columns it reaches, plus row and column n (the buffer must
+ * have n + 1 rows).  res->status is what the reference raises: OverflowError for
+ * RBG_ERR_OVERFLOW, ValueError ("would result in a cycle", index res->i, values res->lhs /
+ * res->rhs) for RBG_ERR_CYCLE.  Synchronises `stream`.
+ */
+int32_t rbg_vertex_compose(int32_t dtype, int64_t n, const void *R, int64_t ldr, const void *u, const void *v,
+                           int64_t color, void *out, int64_t ldo, uint32_t mode, void *workspace,
+                           int64_t workspace_bytes, rbg_compose_result_t *res, rbg_stream_t stream);
+
+/*
+ * R' = the closure of closed R (n x n) with the edge alpha -> beta of value `relationship`: row
+ * alpha becomes (row alpha with column beta replaced) (x) R, and every row reaching alpha takes
+ * the update.  out (n x n, ldo) may be R (in place).  The caller checks R[beta][alpha] == 0
+ * first (a cycle), as the reference's Python layer does.  Synchronises `stream`.
+ */
+int32_t rbg_edge_compose(int32_t dtype, int64_t n, const void *R, int64_t ldr, int64_t alpha, int64_t beta,
+                         int64_t relationship, void *out, int64_t ldo, uint32_t mode, void *workspace,
+                         int64_t workspace_bytes, rbg_compose_result_t *res, rbg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

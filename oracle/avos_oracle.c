@@ -16,6 +16,9 @@
  *                            -- redblackgraph/core/src/redblackgraph/redblack.c.src:554-594
  *   - the sparse SpGEMM pass 1 / pass 2 behind rb_matrix @
  *                            -- redblackgraph/sparse/sparsetools/rbm_math.h:14-222
+ *   - vertex and edge relational composition, C core and Cython
+ *                            -- redblackgraph/core/src/redblackgraph/relational_composition.c.in:47-262
+ *                               redblackgraph/sparse/csgraph/_relational_composition.pyx:10-113
  *
  * Error events.  The C core reports errors through PyErr_Format and keeps looping, so the
  * exception Python finally raises is the LAST one set.  The oracle records, in loop order,
@@ -314,3 +317,157 @@ int64_t orc_spgemm_pass1(int64_t n_row, int64_t n_col, const int64_t *ap, const 
 
 DEFINE_SPGEMM2(i64, int64_t, uint64_t)
 DEFINE_SPGEMM2(u64, uint64_t, uint64_t)
+
+/* ------------------------------------------------------------------------------------
+ * Relational composition, C core semantics (relational_composition.c.in:47-262), in the
+ * reference's loop order.  info[0] = status (0, RBG_ERR_OVERFLOW, RBG_ERR_CYCLE), info[1] =
+ * flags over every product, info[2] = step of the deciding event (1, 2, 3 = cycle check, 4),
+ * info[3], info[4] = its row and column (cycle: the index k), info[5], info[6] = its operands
+ * (cycle: u_k, v_k), info[7] = its event bits.  A product on which the reference's MSB would
+ * never return stops the run there (RBG_EV_HANG), as in orc_warshall.
+ * ------------------------------------------------------------------------------------ */
+#define COMP_EVENT(STEP, I, J, A, B, EV)                                                     \
+    do {                                                                                     \
+        flags |= (EV);                                                                       \
+        if ((EV) & RBG_EV_HANG) {                                                            \
+            info[0] = RBG_ERR_OVERFLOW; info[1] = flags; info[2] = (STEP); info[3] = (I);    \
+            info[4] = (J); info[5] = (int64_t)(A); info[6] = (int64_t)(B); info[7] = (EV);   \
+            return RBG_ERR_OVERFLOW;                                                         \
+        }                                                                                    \
+        last = RBG_ERR_OVERFLOW; ls = (STEP); li = (I); lj = (J);                            \
+        la = (int64_t)(A); lb = (int64_t)(B); lev = (EV);                                    \
+    } while (0)
+
+#define DEFINE_COMPOSE(NAME, T, U)                                                           \
+    int orc_vertex_comp_##NAME(int64_t n, const T *R, const T *u, const T *v, T color, T *out, \
+                               int64_t *info) {                                              \
+        int last = 0; unsigned flags = 0, lev = 0;                                           \
+        int64_t ls = -1, li = -1, lj = -1, la = 0, lb = 0;                                   \
+        const int64_t m1 = n + 1;                                                            \
+        for (int64_t p = 0; p < n; p++) {          /* step 1: out[n][p] = u (x) R[:, p] */   \
+            T r = 0;                                                                         \
+            for (int64_t i = 0; i < n; i++) {                                                \
+                unsigned ev = 0;                                                             \
+                T pr = (T)NAME##_product(u[i], R[i * n + p], &ev);                           \
+                if (ev) COMP_EVENT(1, i, p, u[i], R[i * n + p], ev);                         \
+                r = NAME##_sum(r, pr);                                                       \
+            }                                                                                \
+            out[n * m1 + p] = r;                                                             \
+        }                                                                                    \
+        out[n * m1 + n] = color;                                                             \
+        for (int64_t m = 0; m < n; m++) {          /* step 2: out[m][n] = R[m, :] (x) v */   \
+            T r = 0;                                                                         \
+            for (int64_t j = 0; j < n; j++) {                                                \
+                unsigned ev = 0;                                                             \
+                T pr = (T)NAME##_product(R[m * n + j], v[j], &ev);                           \
+                if (ev) COMP_EVENT(2, m, j, R[m * n + j], v[j], ev);                         \
+                r = NAME##_sum(r, pr);                                                       \
+            }                                                                                \
+            out[m * m1 + n] = r;                                                             \
+        }                                                                                    \
+        for (int64_t k = 0; k < n; k++)           /* step 3: the cycle check */              \
+            if (out[k * m1 + n] != 0 && out[n * m1 + k] != 0) {                              \
+                info[0] = RBG_ERR_CYCLE; info[1] = flags; info[2] = 3; info[3] = k;          \
+                info[4] = n; info[5] = (int64_t)out[n * m1 + k];                             \
+                info[6] = (int64_t)out[k * m1 + n]; info[7] = 0;                             \
+                return RBG_ERR_CYCLE;                                                        \
+            }                                                                                \
+        for (int64_t m = 0; m < n; m++)            /* step 4: R (+) vc (x) uc */             \
+            for (int64_t p = 0; p < n; p++) {                                                \
+                unsigned ev = 0;                                                             \
+                T a = out[m * m1 + n], b = out[n * m1 + p];                                  \
+                T pr = (T)NAME##_product(a, b, &ev);                                         \
+                if (ev) COMP_EVENT(4, m, p, a, b, ev);                                       \
+                out[m * m1 + p] = NAME##_sum(R[m * n + p], pr);                              \
+            }                                                                                \
+        info[0] = last; info[1] = flags; info[2] = ls; info[3] = li; info[4] = lj;           \
+        info[5] = la; info[6] = lb; info[7] = lev;                                           \
+        return last;                                                                         \
+    }                                                                                        \
+    /* edge: loop indices compared in the storage type, as the C core does */               \
+    int orc_edge_comp_##NAME(int64_t n, const T *R, int64_t alpha, int64_t beta, T np, T *out,  \
+                             int64_t *info) {                                                \
+        int last = 0; unsigned flags = 0, lev = 0;                                           \
+        int64_t ls = -1, li = -1, lj = -1, la = 0, lb = 0;                                   \
+        memcpy(out, R, (size_t)(n * n) * sizeof(T));                                         \
+        for (int64_t p = 0; p < n; p++) {          /* step 1: row alpha */                   \
+            T r = 0;                                                                         \
+            for (int64_t i = 0; i < n; i++) {                                                \
+                T lhs = R[alpha * n + i];                                                    \
+                if (np != 0 && (T)i == (T)beta) lhs = np;                                    \
+                unsigned ev = 0;                                                             \
+                T pr = (T)NAME##_product(lhs, R[i * n + p], &ev);                            \
+                if (ev) COMP_EVENT(1, i, p, lhs, R[i * n + p], ev);                          \
+                r = NAME##_sum(r, pr);                                                       \
+            }                                                                                \
+            out[alpha * n + p] = r;                                                          \
+        }                                                                                    \
+        for (int64_t m = 0; m < n; m++) {          /* step 2: the other rows */              \
+            if ((T)m == (T)alpha) continue;                                                  \
+            T lhs = R[m * n + alpha];                                                        \
+            for (int64_t p = 0; p < n; p++) {                                                \
+                T a = out[alpha * n + p];                                                    \
+                if (a != 0) {                                                                \
+                    unsigned ev = 0;                                                         \
+                    T pr = (T)NAME##_product(lhs, a, &ev);                                   \
+                    if (ev) COMP_EVENT(2, m, p, lhs, a, ev);                                 \
+                    out[m * n + p] = NAME##_sum(R[m * n + p], pr);                           \
+                } else {                                                                     \
+                    out[m * n + p] = R[m * n + p];                                           \
+                }                                                                            \
+            }                                                                                \
+        }                                                                                    \
+        info[0] = last; info[1] = flags; info[2] = ls; info[3] = li; info[4] = lj;           \
+        info[5] = la; info[6] = lb; info[7] = lev;                                           \
+        return last;                                                                         \
+    }
+
+DEFINE_COMPOSE(i8, int8_t, uint8_t)
+DEFINE_COMPOSE(u8, uint8_t, uint8_t)
+DEFINE_COMPOSE(i16, int16_t, uint16_t)
+DEFINE_COMPOSE(u16, uint16_t, uint16_t)
+DEFINE_COMPOSE(i32, int32_t, uint32_t)
+DEFINE_COMPOSE(u32, uint32_t, uint32_t)
+DEFINE_COMPOSE(i64, int64_t, uint64_t)
+DEFINE_COMPOSE(u64, uint64_t, uint64_t)
+
+/* Cython relational composition (_relational_composition.pyx:10-113), int32, no events. */
+void orc_vertex_comp_cy(int64_t n, const int32_t *A, const int32_t *u, const int32_t *v, int32_t color,
+                        int32_t *out) {
+    const int64_t m1 = n + 1;
+    int32_t *ul = (int32_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(int32_t));
+    int32_t *vl = (int32_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(int32_t));
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++) {
+            ul[i] = cy_sum(ul[i], cy_product(u[j], A[j * n + i]));
+            vl[i] = cy_sum(vl[i], cy_product(A[i * n + j], v[j]));
+        }
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++)
+            out[i * m1 + j] = ul[j] != 0 ? cy_sum(cy_product(vl[i], ul[j]), A[i * n + j]) : A[i * n + j];
+    for (int64_t i = 0; i < n; i++) {
+        out[i * m1 + n] = vl[i];
+        out[n * m1 + i] = ul[i];
+    }
+    out[n * m1 + n] = color;
+    free(ul);
+    free(vl);
+}
+
+void orc_edge_comp_cy(int64_t n, const int32_t *R, int64_t alpha, int64_t beta, int32_t rel, int32_t *out) {
+    int32_t *A = (int32_t *)malloc((size_t)(n * n) * sizeof(int32_t));
+    int32_t *ul = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    memcpy(A, R, (size_t)(n * n) * sizeof(int32_t));
+    A[alpha * n + beta] = rel;                     /* the Cython code edits R in place */
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++)
+            ul[i] = cy_sum(ul[i], cy_product(A[alpha * n + j], A[j * n + i]));
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++) {
+            if (i == alpha) out[i * n + j] = ul[j];
+            else if (ul[j] != 0) out[i * n + j] = cy_sum(cy_product(A[i * n + alpha], ul[j]), A[i * n + j]);
+            else out[i * n + j] = A[i * n + j];
+        }
+    free(A);
+    free(ul);
+}

@@ -76,6 +76,16 @@ def _declare(L):
     L.orc_cy_product.argtypes = [ctypes.c_int32, ctypes.c_int32]
     L.orc_cy_sum.restype = ctypes.c_int32
     L.orc_cy_sum.argtypes = [ctypes.c_int32, ctypes.c_int32]
+    for s in _SUFFIX.values():
+        T = _CTYPE[s]
+        getattr(L, f"orc_vertex_comp_{s}").restype = ctypes.c_int
+        getattr(L, f"orc_vertex_comp_{s}").argtypes = [i64, p, p, p, T, p, p]
+        getattr(L, f"orc_edge_comp_{s}").restype = ctypes.c_int
+        getattr(L, f"orc_edge_comp_{s}").argtypes = [i64, p, i64, i64, T, p, p]
+    L.orc_vertex_comp_cy.restype = None
+    L.orc_vertex_comp_cy.argtypes = [i64, p, p, p, ctypes.c_int32, p]
+    L.orc_edge_comp_cy.restype = None
+    L.orc_edge_comp_cy.argtypes = [i64, p, i64, i64, ctypes.c_int32, p]
     L.orc_spgemm_pass1.restype = i64
     L.orc_spgemm_pass1.argtypes = [i64, i64, p, p, p, p, p]
     for s in ("i64", "u64"):
@@ -433,3 +443,54 @@ def dag_closure(a):
                       shape=(n, n))
     W.sort_indices()
     return W, (_cy_msb(mx) if mx > 1 else 0)
+
+
+# ----------------------------------------------------------------------------- composition
+def vertex_compose(R, u, v, color):
+    """C core vertex relational composition (relational_composition.c.in:166-262) in the
+    reference's loop order.  Returns ``(out, info)``; info = [status, flags, step, i, j, lhs,
+    rhs, event] of the deciding event (status 0 when none)."""
+    R = np.ascontiguousarray(R)
+    dt = R.dtype
+    n = R.shape[0]
+    u = np.ascontiguousarray(np.asarray(u).reshape(-1), dtype=dt)
+    v = np.ascontiguousarray(np.asarray(v).reshape(-1), dtype=dt)
+    out = np.zeros((n + 1, n + 1), dtype=dt)
+    info = np.zeros(8, dtype=np.int64)
+    s = suffix(dt)
+    c = _CTYPE[s](int(np.array(color).astype(dt))).value
+    getattr(lib(), f"orc_vertex_comp_{s}")(n, _ptr(R), _ptr(u), _ptr(v), c, _ptr(out), _ptr(info))
+    return out, info
+
+
+def edge_compose(R, alpha, beta, relationship):
+    """C core edge relational composition (relational_composition.c.in:72-139)."""
+    R = np.ascontiguousarray(R)
+    dt = R.dtype
+    n = R.shape[0]
+    out = np.zeros((n, n), dtype=dt)
+    info = np.zeros(8, dtype=np.int64)
+    s = suffix(dt)
+    r = _CTYPE[s](int(np.array(relationship).astype(dt))).value
+    getattr(lib(), f"orc_edge_comp_{s}")(n, _ptr(R), int(alpha), int(beta), r, _ptr(out), _ptr(info))
+    return out, info
+
+
+def vertex_compose_cy(R, u, v, color):
+    """Cython vertex_relational_composition (_relational_composition.pyx:10-64), int32."""
+    R = np.ascontiguousarray(R, dtype=np.int32)
+    n = R.shape[0]
+    u = np.ascontiguousarray(np.asarray(u).reshape(-1), dtype=np.int32)
+    v = np.ascontiguousarray(np.asarray(v).reshape(-1), dtype=np.int32)
+    out = np.zeros((n + 1, n + 1), dtype=np.int32)
+    lib().orc_vertex_comp_cy(n, _ptr(R), _ptr(u), _ptr(v), int(np.int32(color)), _ptr(out))
+    return out
+
+
+def edge_compose_cy(R, alpha, beta, relationship):
+    """Cython edge_relational_composition (_relational_composition.pyx:67-113), int32."""
+    R = np.ascontiguousarray(R, dtype=np.int32)
+    n = R.shape[0]
+    out = np.zeros((n, n), dtype=np.int32)
+    lib().orc_edge_comp_cy(n, _ptr(R), int(alpha), int(beta), int(np.int32(relationship)), _ptr(out))
+    return out

@@ -77,6 +77,14 @@ class RbgLookup(ctypes.Structure):
                 ("dtype", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class RbgComposeResult(ctypes.Structure):
+    """rbg_compose_result_t: outcome of a relational composition."""
+    _fields_ = [("status", ctypes.c_int32), ("flags", ctypes.c_uint32), ("event", ctypes.c_uint32),
+                ("reserved", ctypes.c_int32), ("step", ctypes.c_int64), ("i", ctypes.c_int64),
+                ("j", ctypes.c_int64), ("lhs", ctypes.c_int64), ("rhs", ctypes.c_int64),
+                ("updated", ctypes.c_int64)]
+
+
 # (name, restype, argtypes) of every exported entry point; include/rbg_gb300.h declares them
 _P = ctypes.c_void_p
 _I32, _U32, _I64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
@@ -120,6 +128,11 @@ SIGNATURES = [
     ("rbg_dag_gather", _I32, [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
     ("rbg_dag_candidate_max", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _I64,
                                      ctypes.POINTER(_I64), _P]),
+    ("rbg_compose_workspace_bytes", _I32, [_I32, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_vertex_compose", _I32, [_I32, _I64, _P, _I64, _P, _P, _I64, _P, _I64, _U32, _P, _I64,
+                                  ctypes.POINTER(RbgComposeResult), _P]),
+    ("rbg_edge_compose", _I32, [_I32, _I64, _P, _I64, _I64, _I64, _I64, _P, _I64, _U32, _P, _I64,
+                                ctypes.POINTER(RbgComposeResult), _P]),
 ]
 
 _lib = None

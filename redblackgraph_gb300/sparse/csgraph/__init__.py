@@ -14,9 +14,11 @@ from .transitive_closure import (
     DensificationError,
 )
 from .cycleerror import CycleError
+from ._relational_composition import vertex_relational_composition, edge_relational_composition
 
 __all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
            "transitive_closure_floyd_warshall", "transitive_closure_dijkstra",
            "transitive_closure_squaring", "transitive_closure_dag_sparse", "component_wise_closure",
            "transitive_closure_adaptive", "find_components", "find_components_sparse",
-           "get_component_vertices", "DensificationError", "CycleError"]
+           "get_component_vertices", "DensificationError", "CycleError",
+           "vertex_relational_composition", "edge_relational_composition"]

@@ -68,6 +68,95 @@ def ref_warshall_isolated(A):
         return out[1], None, None
 
 
+_CHILD_COMPOSE = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from oracle import refimport
+refimport.load()
+import redblackgraph.core as core
+from redblackgraph.core.redblack import array as rb_array
+z = np.load(sys.argv[2])
+try:
+    if str(z["kind"]) == "vertex":
+        out = core.vertex_relational_composition(z["u"], rb_array(z["R"]), z["v"], int(z["c"]))
+    else:
+        out = core.edge_relational_composition(rb_array(z["R"]), int(z["alpha"]), int(z["beta"]), int(z["rel"]))
+    np.save(sys.argv[3], np.asarray(out))
+    print("OK")
+except Exception as e:
+    print("EXC", type(e).__name__)
+"""
+
+
+def ref_compose_isolated(**kw):
+    """The reference's C core composition in a child process (errors are raised from a gufunc
+    loop, which can take the interpreter down)."""
+    import subprocess
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "a.npz", Path(td) / "w.npy"
+        np.savez(fin, **kw)
+        r = subprocess.run([sys.executable, "-c", _CHILD_COMPOSE, str(ROOT), str(fin), str(fout)],
+                           capture_output=True, text=True, timeout=120)
+        out = r.stdout.strip().split()
+        if r.returncode != 0 or not out:
+            return "crash", None
+        if out[0] == "OK":
+            return "ok", np.load(fout)
+        return out[1], None
+
+
+def compose_cases():
+    """(name, kind, R, args) for relational composition: the reference's own test graphs, and
+    closed pedigrees with a new vertex (parents u, children v) or a new edge."""
+    cases = []
+    A5 = np.array([[-1, 2, 3, 4, 0], [0, -1, 0, 2, 0], [0, 0, 1, 0, 0], [0, 0, 0, -1, 0], [2, 4, 5, 8, 1]])
+    cases.append(("sibling", "vertex", A5, dict(u=np.array([2, 0, 0, 0, 0]), v=np.zeros(5, np.int64), c=-1)))
+    R5 = np.array([[-1, 0, 3, 0, 0], [0, -1, 0, 2, 0], [0, 0, 1, 0, 0], [0, 0, 0, -1, 0], [2, 0, 5, 0, 1]])
+    cases.append(("edge5", "edge", R5, dict(alpha=0, beta=1, rel=2)))
+    cases.append(("edge5_zero_rel", "edge", R5, dict(alpha=0, beta=1, rel=0)))
+    rng = np.random.default_rng(5)
+    for n, g, seed in [(30, 5, 1), (60, 7, 2), (90, 9, 3)]:
+        P = synth.pedigree(n, g, seed, dtype=np.int64)
+        W, _, st, _ = O.warshall(P)
+        assert st == 0
+        anc = lambda x: set(np.nonzero(W[x])[0])  # noqa: E731
+        for t in range(3):
+            f, m = rng.choice(n, size=2, replace=False)
+            u = np.zeros(n, np.int64)
+            u[f], u[m] = 2, 3
+            up = anc(f) | anc(m)
+            kids = [k for k in rng.choice(n, size=4, replace=False) if k not in up and not (set(np.nonzero(W[:, k])[0]) & up)]
+            v = np.zeros(n, np.int64)
+            for k in kids[:2]:
+                v[k] = 2 if k % 2 else 3
+            cases.append((f"ped{n}_v{t}", "vertex", W, dict(u=u, v=v, c=-1 if t % 2 else 1)))
+            # a cycle: a child that is also an ancestor of the parents
+            if t == 0:
+                vc = v.copy()
+                vc[f] = 2
+                cases.append((f"ped{n}_cycle", "vertex", W, dict(u=u, v=vc, c=1)))
+        for t in range(3):
+            while True:
+                a, b = rng.choice(n, size=2, replace=False)
+                if W[b, a] == 0 and W[a, b] == 0:
+                    break
+            cases.append((f"ped{n}_e{t}", "edge", W, dict(alpha=int(a), beta=int(b), rel=int(2 + t % 2))))
+    # overflow: deep chains in narrow types
+    for depth in (6, 8):
+        nn = depth + 1
+        C = np.zeros((nn, nn), np.int64)
+        np.fill_diagonal(C, [(-1 if i % 2 == 0 else 1) for i in range(nn)])
+        for i in range(nn - 1):
+            C[i + 1, i] = 2 if i % 2 == 0 else 3
+        W, _, st, _ = O.warshall(C)
+        u = np.zeros(nn, np.int64)
+        u[0] = 2
+        cases.append((f"chain{depth}_v", "vertex", W, dict(u=u, v=np.eye(nn, dtype=np.int64)[nn - 1] * 3, c=1)))
+        cases.append((f"chain{depth}_e", "edge", W, dict(alpha=nn - 1, beta=0, rel=2)))
+    return cases
+
+
 def main():
     rbg = refimport.load()
     import redblackgraph.core as core
@@ -348,6 +437,48 @@ def main():
         except Exception as e:
             rec["error"] = exc_name(e)
         index["adaptive"].append(rec)
+
+    # ---------------------------------------------------------------- relational composition
+    index["compose"] = []
+    ci = 0
+    for name, kind, R, args in compose_cases():
+        for dt in ([np.int32] if name.startswith("ped9") else DTYPES):
+            if kind == "edge" and np.iinfo(dt).max < R.shape[0]:
+                continue
+            Rt = R.astype(dt)
+            key = f"rc{ci}"
+            ci += 1
+            arrays[key + "_R"] = Rt
+            rec = {"key": key, "name": name, "kind": kind, "dtype": np.dtype(dt).name}
+            if kind == "vertex":
+                u, v = args["u"].astype(dt), args["v"].astype(dt)
+                arrays[key + "_u"], arrays[key + "_v"] = u, v
+                rec["c"] = int(args["c"])
+                _, info = O.vertex_compose(Rt, u, v, rec["c"])
+                kw = dict(kind="vertex", R=Rt, u=u, v=v, c=rec["c"])
+            else:
+                rec.update(alpha=args["alpha"], beta=args["beta"], rel=args["rel"])
+                _, info = O.edge_compose(Rt, args["alpha"], args["beta"], args["rel"])
+                kw = dict(kind="edge", R=Rt, alpha=args["alpha"], beta=args["beta"], rel=args["rel"])
+            if info[0] and (info[7] & O.EV_HANG):
+                rec["hang"] = True               # the reference would not return
+            else:
+                st, out = ref_compose_isolated(**kw)
+                if st == "ok":
+                    arrays[key + "_out"] = out.astype(dt)
+                else:
+                    rec["error"] = st
+            # the Cython functions (int32 only, no cycle check, silent wrap)
+            if dt == np.int32 and R.shape[0] < 100:
+                try:
+                    if kind == "vertex":
+                        cy = csgraph.vertex_relational_composition(u.copy(), Rt.copy(), v.copy(), rec["c"])
+                    else:
+                        cy = csgraph.edge_relational_composition(Rt.copy(), args["alpha"], args["beta"], args["rel"])
+                    arrays[key + "_cy"] = np.asarray(cy)
+                except Exception as e:  # noqa: BLE001
+                    rec["cy_error"] = exc_name(e)
+            index["compose"].append(rec)
 
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "index.json").write_text(json.dumps(index, indent=1))

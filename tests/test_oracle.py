@@ -143,3 +143,35 @@ def test_oracle_dag_closure_vs_golden(golden):
         W, d = O.dag_closure(A)
         assert d == rec["diameter"]
         assert (W != E).nnz == 0
+
+
+def test_oracle_relational_composition_vs_golden(golden):
+    """The composition restatements (C core, every storage type; Cython, int32) against the
+    reference's core and csgraph functions.  Where the reference's gufunc raised (or took the
+    interpreter down raising from its loop), the oracle reports the error; where its MSB loop
+    would not return, the oracle says so."""
+    import numpy as np
+    arrays, index = golden
+    assert len(index["compose"]) > 100
+    for rec in index["compose"]:
+        k = rec["key"]
+        R = arrays[k + "_R"]
+        if rec["kind"] == "vertex":
+            out, info = O.vertex_compose(R, arrays[k + "_u"], arrays[k + "_v"], rec["c"])
+        else:
+            out, info = O.edge_compose(R, rec["alpha"], rec["beta"], rec["rel"])
+        if rec.get("hang"):
+            assert info[0] == 1 and info[7] & O.EV_HANG, rec
+        elif "error" in rec:
+            assert info[0] != 0, rec
+            if rec["error"] == "OverflowError":
+                assert info[0] == 1, rec
+        else:
+            assert info[0] == 0, rec
+            assert (out == arrays[k + "_out"]).all(), rec
+        if k + "_cy" in arrays.files:
+            if rec["kind"] == "vertex":
+                cy = O.vertex_compose_cy(R, arrays[k + "_u"], arrays[k + "_v"], rec["c"])
+            else:
+                cy = O.edge_compose_cy(R, rec["alpha"], rec["beta"], rec["rel"])
+            assert (cy == arrays[k + "_cy"]).all(), rec
