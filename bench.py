@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving workload (0: skip)")
     ap.add_argument("--serve-count", type=int, default=0, help="requests in the serving stream")
-    ap.add_argument("--only", choices=["spgemm", "dag", "single", "serve"], default=None,
+    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve"], default=None,
                     help="run one secondary workload alone and print its JSON (profiling cases)")
     ap.add_argument("--secondary", type=int, default=1,
                     help="also measure the per-component plain path, one n=8192 int64 closure and "
@@ -440,6 +440,95 @@ def run_single_dense(n=8192, generations=30, seed=1, steps=5):
                                        f"pedigree in {tc:.1f} s; n^3 extrapolation"}}
 
 
+def run_compose(n=8192, family=128, ops=16, seed=11):
+    """Incremental closure updates (relational composition) on one resident closed forest of
+    n=8192 vertices in families of 128 (int32), against closing the graph again: `ops` edge
+    compositions in place, each joining the founder of an untouched family to a deep vertex of
+    another (every descendant of the founder gains that vertex's ancestors), then `ops` vertex
+    compositions growing the buffer in place (a new vertex with two parents in one family and an
+    untouched family's founder as its child).  Per-operation host wall time (the call synchronises)
+    and entries rewritten; the first edge and the first vertex composition are checked against
+    the oracle's restatement of the C core gufuncs on the full matrix."""
+    import torch
+    from oracle import oracle as orc
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.composition import edge_compose_device, vertex_compose_device
+    from redblackgraph_gb300.dense import fw_dense
+    from redblackgraph_gb300.device import to_device
+    A = synth.forest(n, 12, seed, family=family, reach=3, dtype=np.int32).toarray()
+    d = to_device(A)
+    W = torch.empty_like(d)
+    for _ in range(3):
+        fw_dense(d, out=W)
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    _, res = fw_dense(d, out=W)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_close = e0.elapsed_time(e1)
+    Wh = W.cpu().numpy()
+    fams = n // family
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(fams)
+    diag = np.diag(Wh)
+    buf = torch.zeros((n + ops, n + ops), dtype=torch.int32, device="cuda")
+    buf[:n, :n] = W
+    R = buf[:n, :n]
+    first_ok = []
+    edge_ms, edge_upd, vert_ms, vert_upd = [], [], [], []
+    # edges: founder of family X (position 0) gains a deep vertex of family Y as a parent
+    for t in range(ops):
+        X, Y = int(order[2 * t]), int(order[2 * t + 1])
+        a = X * family
+        b = Y * family + family - 1 - int(rng.integers(0, 8))
+        rel = 2 if diag[b] == -1 else 3
+        if t == 0:
+            exp, info = orc.edge_compose(Wh, a, b, rel)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, res = edge_compose_device(R, a, b, rel, out=R)
+        edge_ms.append((time.perf_counter() - t0) * 1e3)
+        edge_upd.append(int(res.updated))
+        if t == 0:
+            first_ok.append(bool(info[0] == 0 and res.status == 0 and (R.cpu().numpy() == exp).all()))
+    # vertices: parents in family X (two deep vertices), child = founder of untouched family Z
+    base = 2 * ops
+    for t in range(ops):
+        m = n + t
+        X, Z = int(order[base + 2 * t]), int(order[base + 2 * t + 1])
+        f = X * family + family - 1
+        while diag[f] != -1:
+            f -= 1
+        mo = X * family + family - 1
+        while diag[mo] != 1:
+            mo -= 1
+        c = Z * family
+        color = -1 if t % 2 == 0 else 1
+        u = torch.zeros(m, dtype=torch.int32, device="cuda")
+        v = torch.zeros(m, dtype=torch.int32, device="cuda")
+        u[f], u[mo] = 2, 3
+        v[c] = 2 if color == -1 else 3
+        if t == 0:
+            Rh = buf[:m, :m].cpu().numpy()
+            exp, info = orc.vertex_compose(Rh, u.cpu().numpy(), v.cpu().numpy(), color)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, res = vertex_compose_device(buf, u, v, color, out=buf, n=m)
+        vert_ms.append((time.perf_counter() - t0) * 1e3)
+        vert_upd.append(int(res.updated))
+        if t == 0:
+            first_ok.append(bool(info[0] == 0 and res.status == 0 and (buf[:m + 1, :m + 1].cpu().numpy() == exp).all()))
+    return {"workload": f"closed forest, n={n}, families of {family}, int32; {ops} edge and {ops} vertex "
+                        "compositions in place",
+            "recompute_closure_ms": t_close,
+            "edge_ms_median": statistics.median(edge_ms), "edge_updated_median": statistics.median(edge_upd),
+            "vertex_ms_median": statistics.median(vert_ms), "vertex_updated_median": statistics.median(vert_upd),
+            "edge_vs_recompute": t_close / statistics.median(edge_ms),
+            "first_ops_bit_exact_vs_oracle": all(first_ok)}
+
+
 def generations_for_small(m):
     from redblackgraph_gb300 import synth
     return synth.generations_for(m)
@@ -653,7 +742,8 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        fn = {"spgemm": run_spgemm_forest, "dag": run_dag_forest, "single": run_single_dense,
+        fn = {"spgemm": run_spgemm_forest, "dag": run_dag_forest, "compose": run_compose,
+              "single": run_single_dense,
               "serve": lambda: run_serving(args.serve_count)}[args.only]
         print(json.dumps(fn()))
         return
@@ -725,6 +815,7 @@ def main():
         line["single_graph"] = run_single_dense()
         line["spgemm_squaring"] = run_spgemm_forest()
         line["dag_levels"] = run_dag_forest()
+        line["relational_composition"] = run_compose()
     if args.serve:
         line["serving"] = run_serving(args.serve_count)
     if rank == 0:
