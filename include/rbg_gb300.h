@@ -432,6 +432,56 @@ int32_t rbg_edge_compose(int32_t dtype, int64_t n, const void *R, int64_t ldr, i
                          int64_t relationship, void *out, int64_t ldo, uint32_t mode, void *workspace,
                          int64_t workspace_bytes, rbg_compose_result_t *res, rbg_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Orderings of closed graphs (replace _ordering.pyx:15-177, _permutation.pyx:11-205 and
+ * _topological_sort.pyx:30-265 of redblackgraph/sparse/csgraph).  int32 values, int32 indices.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Per vertex: anc = sum of the Cython MSB of the row's non-zero values, maxrel = the largest
+ * value in the vertex's column (starting from 0), diag = the diagonal value (the row's last
+ * diagonal entry, 0 when none).  Device arrays of n.  Ordered on `stream`. */
+int32_t rbg_ordering_metrics_csr(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
+                                 int64_t *anc, int32_t *maxrel, int32_t *diag, rbg_stream_t stream);
+int32_t rbg_ordering_metrics_dense(int64_t n, const int32_t *A, int64_t lda, int64_t *anc, int32_t *maxrel,
+                                   int32_t *diag, rbg_stream_t stream);
+
+int32_t rbg_canonical_permutation_workspace_bytes(int64_t n, int64_t *bytes);
+
+/* The canonical permutation perm (perm[new] = old): vertices sorted by (size of their component
+ * descending, component id ascending, anc descending, maxrel ascending, diag descending, vertex
+ * id ascending).  label[v] = component of v, comp_start[c + 1] - comp_start[c] = its size
+ * (rbg_cc_label's outputs).  Ordered on `stream`. */
+int32_t rbg_canonical_permutation(int64_t n, const int32_t *label, const int64_t *comp_start, const int64_t *anc,
+                                  const int32_t *maxrel, const int32_t *diag, int32_t *perm, void *workspace,
+                                  int64_t workspace_bytes, rbg_stream_t stream);
+
+/* B[i][j] = A[perm[i]][perm[j]] (upper != 0: only j >= i, zeros below).  A != B. */
+int32_t rbg_permute_dense(int32_t dtype, int64_t n, const void *A, int64_t lda, const int32_t *perm, void *B,
+                          int64_t ldb, int32_t upper, rbg_stream_t stream);
+
+int32_t rbg_permute_csr_workspace_bytes(int64_t n, int64_t nnz, int64_t *bytes);
+/* Row i of the result = row perm[i] of A with columns mapped through the inverse permutation
+ * (upper != 0 keeps new columns >= i), columns ascending.  count writes indptr_out (n + 1) and
+ * *nnz_out (host); fill writes indices and data (int32).  Same workspace for both calls. */
+int32_t rbg_permute_csr_count(const rbg_csr_t *A, const int32_t *perm, int32_t upper, int64_t *indptr_out,
+                              void *workspace, int64_t workspace_bytes, int64_t *nnz_out, rbg_stream_t stream);
+int32_t rbg_permute_csr_fill(const rbg_csr_t *A, const int32_t *perm, int32_t upper, const int64_t *indptr_out,
+                             int32_t *indices_out, int32_t *data_out, void *workspace, int64_t workspace_bytes,
+                             rbg_stream_t stream);
+
+int32_t rbg_topological_workspace_bytes(int64_t n, int64_t nnz, int64_t *bytes);
+/* A topological permutation (perm[new] = old) after which every stored entry (v, w), w != v,
+ * lies above the diagonal: vertices by Kahn level, deepest first, vertex id ascending within a
+ * level.  *levels = number of levels.  RBG_ERR_CYCLE with *cycle_vertex = a vertex on a cycle.
+ * Synchronises `stream`. */
+int32_t rbg_topological_order(const rbg_csr_t *A, void *workspace, int64_t workspace_bytes, int32_t *perm,
+                              int64_t *levels, int64_t *cycle_vertex, rbg_stream_t stream);
+
+/* *result = 1 when no stored entry lies below the diagonal (strict: on or below).  workspace >=
+ * 4 bytes.  Synchronises `stream`. */
+int32_t rbg_is_upper_triangular_csr(const rbg_csr_t *A, int32_t strict, int32_t *result, void *workspace,
+                                    int64_t workspace_bytes, rbg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

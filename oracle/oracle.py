@@ -494,3 +494,88 @@ def edge_compose_cy(R, alpha, beta, relationship):
     out = np.zeros((n, n), dtype=np.int32)
     lib().orc_edge_comp_cy(n, _ptr(R), int(alpha), int(beta), int(np.int32(relationship)), _ptr(out))
     return out
+
+
+# ----------------------------------------------------------------------------- orderings
+def ordering_metrics(A):
+    """Per vertex (ancestor count, column maximum, diagonal) as _get_permutation /
+    _compute_ordering_metrics_sparse compute them (_ordering.pyx:15-39, 101-149)."""
+    import scipy.sparse as sp
+    if sp.issparse(A):
+        csr = sp.csr_matrix(A)
+        n = csr.shape[0]
+        anc = np.zeros(n, np.int64)
+        mx = np.zeros(n, np.int64)
+        dg = np.zeros(n, np.int64)
+        for i in range(n):
+            for e in range(csr.indptr[i], csr.indptr[i + 1]):
+                c, v = int(csr.indices[e]), int(np.int32(csr.data[e]))
+                if v != 0:
+                    anc[i] += _cy_msb(v)
+                    mx[c] = max(mx[c], v)
+                if c == i:
+                    dg[i] = v
+        return anc, mx, dg
+    a = np.asarray(A).astype(np.int64)
+    n = a.shape[0]
+    anc = np.array([sum(_cy_msb(int(v)) for v in a[i] if v != 0) for i in range(n)], np.int64)
+    mx = np.array([max([0] + [int(v) for v in a[:, i] if v != 0]) for i in range(n)], np.int64)
+    return anc, mx, np.diag(a).copy()
+
+
+def canonical_permutation(A, q, ids):
+    """The canonical order's sort (_ordering.pyx:37-38, 92-97)."""
+    anc, mx, dg = ordering_metrics(A)
+    ids = np.asarray(ids)
+    return sorted(range(len(ids)), key=lambda x: (-q[int(ids[x])], int(ids[x]), -anc[x], mx[x], -dg[x], x))
+
+
+def permute_dense(A, p, upper=False):
+    """B[i][j] = A[p[i]][p[j]], j >= i when triangular (_permutation.pyx:48-63)."""
+    a = np.asarray(A)
+    n = a.shape[0]
+    B = np.zeros((n, n), np.int32)
+    for i in range(n):
+        for j in range(i if upper else 0, n):
+            B[i, j] = a[p[i], p[j]]
+    return B
+
+
+def topological_sort_dfs(A):
+    """The reference's iterative depth-first topological sort (_topological_sort.pyx:30-181):
+    reverse post-order from every unvisited vertex in order, neighbours in CSR order, diagonal
+    skipped; ValueError on a back edge."""
+    import scipy.sparse as sp
+    csr = sp.csr_matrix(A)
+    n = csr.shape[0]
+    ip, ij = csr.indptr, csr.indices
+    color = [0] * n
+    order = [0] * n
+    at = n - 1
+    for s in range(n):
+        if color[s]:
+            continue
+        stack = [[s, ip[s]]]
+        color[s] = 1
+        while stack:
+            v, idx = stack[-1]
+            pushed = False
+            while idx < ip[v + 1]:
+                w = int(ij[idx])
+                idx += 1
+                if w == v:
+                    continue
+                if color[w] == 0:
+                    stack[-1][1] = idx
+                    stack.append([w, ip[w]])
+                    color[w] = 1
+                    pushed = True
+                    break
+                if color[w] == 1:
+                    raise ValueError(f"cycle at {w}")
+            if not pushed:
+                color[v] = 2
+                order[at] = v
+                at -= 1
+                stack.pop()
+    return np.array(order, np.int32)

@@ -133,6 +133,18 @@ SIGNATURES = [
                                   ctypes.POINTER(RbgComposeResult), _P]),
     ("rbg_edge_compose", _I32, [_I32, _I64, _P, _I64, _I64, _I64, _I64, _P, _I64, _U32, _P, _I64,
                                 ctypes.POINTER(RbgComposeResult), _P]),
+    ("rbg_ordering_metrics_csr", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P]),
+    ("rbg_ordering_metrics_dense", _I32, [_I64, _P, _I64, _P, _P, _P, _P]),
+    ("rbg_canonical_permutation_workspace_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
+    ("rbg_canonical_permutation", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _P]),
+    ("rbg_permute_dense", _I32, [_I32, _I64, _P, _I64, _P, _P, _I64, _I32, _P]),
+    ("rbg_permute_csr_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_permute_csr_count", _I32, [ctypes.POINTER(RbgCsr), _P, _I32, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
+    ("rbg_permute_csr_fill", _I32, [ctypes.POINTER(RbgCsr), _P, _I32, _P, _P, _P, _P, _I64, _P]),
+    ("rbg_topological_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_topological_order", _I32, [ctypes.POINTER(RbgCsr), _P, _I64, _P, ctypes.POINTER(_I64),
+                                     ctypes.POINTER(_I64), _P]),
+    ("rbg_is_upper_triangular_csr", _I32, [ctypes.POINTER(RbgCsr), _I32, ctypes.POINTER(_I32), _P, _I64, _P]),
 ]
 
 _lib = None

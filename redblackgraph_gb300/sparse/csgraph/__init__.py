@@ -15,10 +15,14 @@ from .transitive_closure import (
 )
 from .cycleerror import CycleError
 from ._relational_composition import vertex_relational_composition, edge_relational_composition
+from ._ordering import (avos_canonical_ordering, _get_permutation, _get_permutation_sparse, permute,
+                        permute_sparse, topological_sort, topological_ordering, is_upper_triangular)
 
 __all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
            "transitive_closure_floyd_warshall", "transitive_closure_dijkstra",
            "transitive_closure_squaring", "transitive_closure_dag_sparse", "component_wise_closure",
            "transitive_closure_adaptive", "find_components", "find_components_sparse",
            "get_component_vertices", "DensificationError", "CycleError",
-           "vertex_relational_composition", "edge_relational_composition"]
+           "vertex_relational_composition", "edge_relational_composition",
+           "avos_canonical_ordering", "_get_permutation", "_get_permutation_sparse", "permute", "permute_sparse",
+           "topological_sort", "topological_ordering", "is_upper_triangular"]

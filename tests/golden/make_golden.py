@@ -480,6 +480,42 @@ def main():
                     rec["cy_error"] = exc_name(e)
             index["compose"].append(rec)
 
+    # ---------------------------------------------------------------- orderings
+    index["ordering"] = []
+    import scipy.sparse as sp2
+    rng2 = np.random.default_rng(17)
+    for oi, (sizes, seed) in enumerate([((20, 35, 12, 35, 1, 1), 3), ((60, 60, 9), 4), ((150,), 5),
+                                        ((7, 7, 7, 3, 3, 40), 6)]):
+        blocks = []
+        for j, m in enumerate(sizes):
+            P = synth.pedigree(m, max(2, int(np.log2(m + 1)) + 1), seed * 31 + j, dtype=np.int64)
+            W, _, st, _ = O.warshall(P)
+            blocks.append(W)
+        from scipy.linalg import block_diag
+        M = block_diag(*blocks).astype(np.int32)
+        p = rng2.permutation(M.shape[0])
+        M = np.ascontiguousarray(M[p][:, p])             # interleave the components
+        key = f"ord{oi}"
+        arrays[key + "_A"] = M
+        dense = csgraph.avos_canonical_ordering(rb_array(M))
+        arrays[key + "_perm_dense"] = np.asarray(dense.label_permutation, np.int32)
+        arrays[key + "_B_dense"] = np.asarray(dense.A)
+        S = sp2.csr_matrix(M)
+        sparse = csgraph.avos_canonical_ordering(S)
+        arrays[key + "_perm_sparse"] = np.asarray(sparse.label_permutation, np.int32)
+        Bs = sp2.csr_matrix(sparse.A)
+        arrays[key + "_B_indptr"], arrays[key + "_B_indices"], arrays[key + "_B_data"] = Bs.indptr, Bs.indices, Bs.data
+        rp = rng2.permutation(M.shape[0]).astype(np.int32)
+        arrays[key + "_rp"] = rp
+        arrays[key + "_permute_full"] = np.asarray(csgraph.permute(M, rp))
+        arrays[key + "_permute_upper"] = np.asarray(csgraph.permute(M, rp, assume_upper_triangular=True))
+        Pu = sp2.csr_matrix(csgraph.permute_sparse(S, rp, assume_upper_triangular=True))
+        arrays[key + "_ps_indptr"], arrays[key + "_ps_indices"], arrays[key + "_ps_data"] = Pu.indptr, Pu.indices, Pu.data
+        arrays[key + "_topo"] = np.asarray(csgraph.topological_sort(S), np.int32)
+        index["ordering"].append({"key": key, "n": int(M.shape[0]),
+                                  "q_dense": {str(k): int(v) for k, v in dense.components.items()},
+                                  "q_sparse": {str(k): int(v) for k, v in sparse.components.items()}})
+
     np.savez_compressed(HERE / "golden.npz", **arrays)
     (HERE / "index.json").write_text(json.dumps(index, indent=1))
     print(f"wrote {len(arrays)} arrays, {len(index['warshall'])} warshall cases")

@@ -175,3 +175,29 @@ def test_oracle_relational_composition_vs_golden(golden):
             else:
                 cy = O.edge_compose_cy(R, rec["alpha"], rec["beta"], rec["rel"])
             assert (cy == arrays[k + "_cy"]).all(), rec
+
+
+def test_oracle_orderings_vs_golden(golden):
+    """The ordering restatements (canonical sort keys, dense and sparse permutation, the
+    depth-first topological sort) against the reference's outputs."""
+    import numpy as np
+    import scipy.sparse as sp
+    arrays, index = golden
+    for rec in index["ordering"]:
+        k = rec["key"]
+        M = arrays[k + "_A"]
+        q = {int(c): v for c, v in rec["q_dense"].items()}
+        # component labels: numbered by least vertex, edges both ways
+        from scipy.sparse.csgraph import connected_components
+        _, lab = connected_components(sp.csr_matrix(M != 0), directed=True, connection="weak")
+        first = {}
+        ids = np.array([first.setdefault(c, len(first)) for c in lab])
+        assert {c: int((ids == c).sum()) for c in set(ids.tolist())} == q
+        p = O.canonical_permutation(M, q, ids)
+        assert (np.array(p) == arrays[k + "_perm_dense"]).all()
+        assert (np.array(O.canonical_permutation(sp.csr_matrix(M), q, ids)) == arrays[k + "_perm_sparse"]).all()
+        assert (O.permute_dense(M, p) == arrays[k + "_B_dense"]).all()
+        rp = arrays[k + "_rp"]
+        assert (O.permute_dense(M, rp) == arrays[k + "_permute_full"]).all()
+        assert (O.permute_dense(M, rp, upper=True) == arrays[k + "_permute_upper"]).all()
+        assert (O.topological_sort_dfs(sp.csr_matrix(M)) == arrays[k + "_topo"]).all()
