@@ -482,6 +482,17 @@ int32_t rbg_topological_order(const rbg_csr_t *A, void *workspace, int64_t works
 int32_t rbg_is_upper_triangular_csr(const rbg_csr_t *A, int32_t strict, int32_t *result, void *workspace,
                                     int64_t workspace_bytes, rbg_stream_t stream);
 
+/* Row/column remap of an int32 CSR (replaces extract_submatrix and merge_component_matrices,
+ * redblackgraph/sparse/csgraph/_components.pyx:178-323): output row row_map[k] (-1: dropped)
+ * receives input row k, its columns mapped through col_map (-1: dropped), columns ascending;
+ * each output row receives at most one input row.  Writes indptr_out (n_out + 1) and *nnz_out;
+ * RBG_ERR_CAPACITY when *nnz_out > capacity (indices/data untouched: call again with room).
+ * Synchronises `stream`. */
+int32_t rbg_csr_remap_workspace_bytes(int64_t n_out, int64_t nnz, int64_t *bytes);
+int32_t rbg_csr_remap(const rbg_csr_t *A, const int32_t *row_map, const int32_t *col_map, int64_t n_out,
+                      int64_t *indptr_out, int32_t *indices_out, int32_t *data_out, int64_t capacity, void *workspace,
+                      int64_t workspace_bytes, int64_t *nnz_out, rbg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -145,6 +145,9 @@ SIGNATURES = [
     ("rbg_topological_order", _I32, [ctypes.POINTER(RbgCsr), _P, _I64, _P, ctypes.POINTER(_I64),
                                      ctypes.POINTER(_I64), _P]),
     ("rbg_is_upper_triangular_csr", _I32, [ctypes.POINTER(RbgCsr), _I32, ctypes.POINTER(_I32), _P, _I64, _P]),
+    ("rbg_csr_remap_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_csr_remap", _I32, [ctypes.POINTER(RbgCsr), _P, _P, _I64, _P, _P, _P, _I64, _P, _I64,
+                             ctypes.POINTER(_I64), _P]),
 ]
 
 _lib = None

@@ -615,3 +615,114 @@ extern "C" int32_t rbg_is_upper_triangular_csr(const rbg_csr_t *A, int32_t stric
     *result = h ? 0 : 1;
     return RBG_OK;
 }
+
+// ---------------------------------------------------------------------------- row/column remap
+// Output row row_map[k] (-1: dropped) receives input row k with its columns mapped through
+// col_map (-1: dropped), columns ascending: extract_submatrix and merge_component_matrices
+// (redblackgraph/sparse/csgraph/_components.pyx:178-323).  Each output row receives at most one
+// input row.
+namespace rbg {
+namespace {
+__global__ void remap_count_kernel(int64_t n_in, const int64_t *ip, const int32_t *ij, const int32_t *row_map,
+                                   const int32_t *col_map, int64_t *cnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < n_in; k += warps) {
+        const int32_t r = row_map[k];
+        if (r < 0) continue;
+        long long c = 0;
+        for (int64_t e = ip[k] + lane; e < ip[k + 1]; e += 32) c += col_map[ij[e]] >= 0 ? 1 : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) cnt[r] = c;
+    }
+}
+
+__global__ void remap_fill_kernel(int64_t n_in, const int64_t *ip, const int32_t *ij, const int32_t *x,
+                                  const int32_t *row_map, const int32_t *col_map, const int64_t *op, int32_t *oj,
+                                  int32_t *ox) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < n_in; k += warps) {
+        const int32_t r = row_map[k];
+        if (r < 0) continue;
+        int64_t base = op[r];
+        for (int64_t e0 = ip[k]; e0 < ip[k + 1]; e0 += 32) {
+            const int64_t e = e0 + lane;
+            int32_t c = -1;
+            if (e < ip[k + 1]) c = col_map[ij[e]];
+            const unsigned bal = __ballot_sync(0xffffffffu, c >= 0);
+            if (c >= 0) {
+                const int64_t q = base + __popc(bal & ((1u << lane) - 1u));
+                oj[q] = c;
+                ox[q] = x[e];
+            }
+            base += __popc(bal);
+        }
+    }
+}
+
+size_t remap_tmp_bytes(int64_t n_out, int64_t nnz) {
+    size_t scan = 0, seg = 0;
+    const size_t m = (size_t)std::max<int64_t>(n_out, 1), z = (size_t)std::max<int64_t>(nnz, 1);
+    cub::DeviceScan::ExclusiveSum(nullptr, scan, (int64_t *)nullptr, (int64_t *)nullptr, (int)(m + 1));
+    cub::DeviceSegmentedSort::SortPairs(nullptr, seg, (int32_t *)nullptr, (int32_t *)nullptr, (int32_t *)nullptr,
+                                        (int32_t *)nullptr, (int64_t)z, (int64_t)m, (int64_t *)nullptr,
+                                        (int64_t *)nullptr);
+    return std::max(scan, seg);
+}
+}  // namespace
+}  // namespace rbg
+
+extern "C" int32_t rbg_csr_remap_workspace_bytes(int64_t n_out, int64_t nnz, int64_t *bytes) {
+    if (!bytes || n_out < 0 || nnz < 0) return RBG_ERR_INVALID;
+    const size_t m = (size_t)std::max<int64_t>(n_out, 1), z = (size_t)std::max<int64_t>(nnz, 1);
+    *bytes = (int64_t)(align_up((m + 1) * 8, 256) + 2 * align_up(z * 4, 256) + align_up(remap_tmp_bytes(n_out, nnz), 256));
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_csr_remap(const rbg_csr_t *A, const int32_t *row_map, const int32_t *col_map, int64_t n_out,
+                                 int64_t *indptr_out, int32_t *indices_out, int32_t *data_out, int64_t capacity,
+                                 void *workspace, int64_t workspace_bytes, int64_t *nnz_out, rbg_stream_t stream) {
+    if (!A || !row_map || !col_map || !indptr_out || !nnz_out || A->n_rows < 0 || n_out < 0) return RBG_ERR_INVALID;
+    const int64_t n_in = A->n_rows;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int64_t annz = 0;
+    if (n_in > 0) {
+        RBG_CUDA_TRY(cudaMemcpyAsync(&annz, A->indptr + n_in, 8, cudaMemcpyDeviceToHost, s));
+        RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    int64_t need = 0;
+    rbg_csr_remap_workspace_bytes(n_out, annz, &need);
+    if (!workspace || workspace_bytes < need) return RBG_ERR_NOMEM;
+    unsigned char *w = reinterpret_cast<unsigned char *>(workspace);
+    const size_t m = (size_t)std::max<int64_t>(n_out, 1), z = (size_t)std::max<int64_t>(annz, 1);
+    int64_t *cnt = reinterpret_cast<int64_t *>(w);
+    int32_t *kj = reinterpret_cast<int32_t *>(w + align_up((m + 1) * 8, 256));
+    int32_t *kx = reinterpret_cast<int32_t *>(w + align_up((m + 1) * 8, 256) + align_up(z * 4, 256));
+    void *tmp = w + align_up((m + 1) * 8, 256) + 2 * align_up(z * 4, 256);
+    size_t tb = remap_tmp_bytes(n_out, annz);
+    RBG_CUDA_TRY(cudaMemsetAsync(cnt, 0, (m + 1) * 8, s));
+    if (n_in > 0) {
+        note_launches(1);
+        remap_count_kernel<<<grid_for(n_in * 32, 256), 256, 0, s>>>(n_in, A->indptr, A->indices, row_map, col_map,
+                                                                     cnt);
+    }
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, cnt, indptr_out, (int)(n_out + 1), s));
+    int64_t total = 0;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&total, indptr_out + n_out, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    *nnz_out = total;
+    if (total > capacity) return RBG_ERR_CAPACITY;
+    if (total == 0) return RBG_OK;
+    if (!indices_out || !data_out) return RBG_ERR_INVALID;
+    note_launches(1);
+    remap_fill_kernel<<<grid_for(n_in * 32, 256), 256, 0, s>>>(n_in, A->indptr, A->indices,
+                                                                reinterpret_cast<const int32_t *>(A->data), row_map,
+                                                                col_map, indptr_out, kj, kx);
+    tb = remap_tmp_bytes(n_out, annz);
+    RBG_CUDA_TRY(cub::DeviceSegmentedSort::SortPairs(tmp, tb, kj, indices_out, kx, data_out, total, n_out, indptr_out,
+                                                     indptr_out + 1, s));
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}

@@ -15,6 +15,7 @@ from .transitive_closure import (
 )
 from .cycleerror import CycleError
 from ._relational_composition import vertex_relational_composition, edge_relational_composition
+from ._components import extract_submatrix, merge_component_matrices
 from ._ordering import (avos_canonical_ordering, _get_permutation, _get_permutation_sparse, permute,
                         permute_sparse, topological_sort, topological_ordering, is_upper_triangular)
 
@@ -25,4 +26,5 @@ __all__ = ["shortest_path", "floyd_warshall", "transitive_closure",
            "get_component_vertices", "DensificationError", "CycleError",
            "vertex_relational_composition", "edge_relational_composition",
            "avos_canonical_ordering", "_get_permutation", "_get_permutation_sparse", "permute", "permute_sparse",
-           "topological_sort", "topological_ordering", "is_upper_triangular"]
+           "topological_sort", "topological_ordering", "is_upper_triangular", "extract_submatrix",
+           "merge_component_matrices"]

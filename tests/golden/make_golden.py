@@ -512,7 +512,21 @@ def main():
         Pu = sp2.csr_matrix(csgraph.permute_sparse(S, rp, assume_upper_triangular=True))
         arrays[key + "_ps_indptr"], arrays[key + "_ps_indices"], arrays[key + "_ps_data"] = Pu.indptr, Pu.indices, Pu.data
         arrays[key + "_topo"] = np.asarray(csgraph.topological_sort(S), np.int32)
-        index["ordering"].append({"key": key, "n": int(M.shape[0]),
+        # extract every component, then merge them back
+        q2 = {}
+        lab = csgraph.find_components_sparse(S, q2)
+        parts = []
+        for c, verts in sorted(csgraph.get_component_vertices(lab).items()):
+            sub, mp = csgraph.extract_submatrix(S, verts)
+            sub = sp2.csr_matrix(sub)
+            arrays[f"{key}_sub{c}_indptr"], arrays[f"{key}_sub{c}_indices"], arrays[f"{key}_sub{c}_data"] = (
+                sub.indptr, sub.indices, sub.data)
+            arrays[f"{key}_sub{c}_map"] = np.asarray(mp, np.int32)
+            parts.append((sub, mp))
+        Mg = sp2.csr_matrix(csgraph.merge_component_matrices(parts, M.shape[0]))
+        arrays[key + "_merged_indptr"], arrays[key + "_merged_indices"], arrays[key + "_merged_data"] = (
+            Mg.indptr, Mg.indices, Mg.data)
+        index["ordering"].append({"key": key, "n": int(M.shape[0]), "ncomp": len(parts),
                                   "q_dense": {str(k): int(v) for k, v in dense.components.items()},
                                   "q_sparse": {str(k): int(v) for k, v in sparse.components.items()}})
 

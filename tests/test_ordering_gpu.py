@@ -81,3 +81,28 @@ def test_topological_sort_properties(native):
     assert csgraph.is_upper_triangular(U) and not csgraph.is_upper_triangular(U.T)
     assert not csgraph.is_upper_triangular(U, strict=True)
     assert csgraph.is_upper_triangular(np.triu(U, 1), strict=True)
+
+
+def test_golden_extract_and_merge(native, golden):
+    """extract_submatrix of every component and merge_component_matrices back, against the
+    reference's outputs."""
+    from redblackgraph_gb300.sparse import csgraph
+    arrays, index = golden
+    for rec in index["ordering"]:
+        k = rec["key"]
+        S = sp.csr_matrix(arrays[k + "_A"])
+        lab = csgraph.find_components_sparse(S)
+        parts = []
+        for c, verts in sorted(csgraph.get_component_vertices(lab).items()):
+            sub, mp = csgraph.extract_submatrix(S, verts)
+            exp = sp.csr_matrix((arrays[f"{k}_sub{c}_data"], arrays[f"{k}_sub{c}_indices"],
+                                 arrays[f"{k}_sub{c}_indptr"]), shape=sub.shape)
+            assert (sub != exp).nnz == 0 and sub.nnz == exp.nnz and sub.dtype == np.int32
+            assert (mp == arrays[f"{k}_sub{c}_map"]).all()
+            parts.append((sub, mp))
+        assert len(parts) == rec["ncomp"]
+        merged = csgraph.merge_component_matrices(parts, S.shape[0])
+        exp = sp.csr_matrix((arrays[k + "_merged_data"], arrays[k + "_merged_indices"], arrays[k + "_merged_indptr"]),
+                            shape=S.shape)
+        assert (merged != exp).nnz == 0 and merged.nnz == exp.nnz
+        assert (merged != S).nnz == 0
