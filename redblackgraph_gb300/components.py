@@ -132,7 +132,8 @@ def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: 
     comps = label_components(indptr, indices, n, stream)
     blocks = densify(indptr, indices, data, comps, stream)
     _, res = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat,
-                      mode=_lib.MODE_CYTHON | _lib.MODE_GRAPH, stream=stream, as_array=True)
+                      mode=_lib.MODE_CYTHON | _lib.MODE_GRAPH | _lib.MODE_AUTOTUNE, stream=stream,
+                      as_array=True)
     bad = np.flatnonzero(res["status"] != _lib.RBG_OK)
     if bad.size:                                     # the first component (by number) raises
         r = _lib.RbgResult()

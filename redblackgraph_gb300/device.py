@@ -85,6 +85,24 @@ def to_host_pinned(t: torch.Tensor) -> np.ndarray:
     return dst.numpy().view(npdt).reshape(tuple(t.shape))
 
 
+def csr_from_parts(data: np.ndarray, indices: np.ndarray, indptr: np.ndarray, shape, canonical: bool = True,
+                   cls=None):
+    """A scipy CSR matrix over these host arrays as they are: the library's outputs are already
+    valid CSR (sorted rows, no duplicates), so the constructor's checks and copies are skipped.
+    The index arrays share one dtype (int32 when the entries fit, else int64).  ``cls`` is a
+    csr_matrix subclass to build (default csr_matrix)."""
+    import scipy.sparse as sp
+    idx = np.int32 if indptr.size == 0 or int(indptr[-1]) < 2**31 - 1 else np.int64
+    m = (cls or sp.csr_matrix)(tuple(shape), dtype=data.dtype)
+    m.data = data
+    m.indices = indices if indices.dtype == idx else indices.astype(idx)
+    m.indptr = indptr if indptr.dtype == idx else indptr.astype(idx)
+    if canonical:
+        m.has_sorted_indices = True
+        m.has_canonical_format = True
+    return m
+
+
 def to_host(t: torch.Tensor) -> np.ndarray:
     npdt = numpy_dtype(t.dtype)
     raw = t.contiguous().reshape(-1).view(torch.uint8).cpu().numpy()

@@ -66,9 +66,7 @@ class CSRMatrixGPU:
                    validate=validate)
 
     def to_cpu(self):
-        import scipy.sparse as sp
-        return sp.csr_matrix((to_host(self.data), to_host(self.indices), to_host(self.indptr)),
-                             shape=self.shape)
+        return self.device_csr().to_scipy()
 
     def device_csr(self) -> DeviceCSR:
         return DeviceCSR(self.indptr, self.indices, self.data, self.shape)

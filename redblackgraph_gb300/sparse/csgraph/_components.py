@@ -9,7 +9,7 @@ import numpy as np
 import torch
 
 from ... import _lib
-from ...device import require_cuda, to_device, to_host
+from ...device import csr_from_parts, require_cuda, to_device, to_host
 from ...spgemm import DeviceCSR
 
 __all__ = ["extract_submatrix", "merge_component_matrices"]
@@ -34,7 +34,7 @@ def _remap(csr, row_map: np.ndarray, col_map: np.ndarray, n_out: int):
     _lib.check(L.rbg_csr_remap(ctypes.byref(ca), rm.data_ptr(), cm.data_ptr(), n_out, ip.data_ptr(), oj.data_ptr(),
                                ox.data_ptr(), cap, ws.data_ptr(), ws.numel(), ctypes.byref(nnz), 0), "csr_remap")
     m = int(nnz.value)
-    return sp.csr_matrix((to_host(ox[:m]), to_host(oj[:m]), to_host(ip).astype(np.int32)), shape=(n_out, n_out))
+    return csr_from_parts(to_host(ox[:m]), to_host(oj[:m]), to_host(ip), (n_out, n_out))
 
 
 def extract_submatrix(A, vertices):

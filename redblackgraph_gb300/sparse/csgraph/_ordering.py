@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from ... import _lib
-from ...device import require_cuda, to_device, to_host
+from ...device import csr_from_parts, require_cuda, to_device, to_host
 from ...spgemm import DeviceCSR
 from ...types import Ordering
 from .cycleerror import CycleError
@@ -167,7 +167,7 @@ def permute_sparse(A, p, assume_upper_triangular=False):
     ox = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
     _lib.check(L.rbg_permute_csr_fill(ctypes.byref(ca), dp.data_ptr(), upper, ip.data_ptr(), oj.data_ptr(),
                                       ox.data_ptr(), ws.data_ptr(), ws.numel(), 0), "permute_csr")
-    return sp.csr_matrix((to_host(ox[:m]), to_host(oj[:m]), to_host(ip).astype(np.int32)), shape=(n, n))
+    return csr_from_parts(to_host(ox[:m]), to_host(oj[:m]), to_host(ip), (n, n))
 
 
 def topological_sort(A) -> np.ndarray:

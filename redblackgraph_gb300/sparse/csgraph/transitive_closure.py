@@ -75,9 +75,7 @@ def _squaring(csr, max_iterations, cycle_error, dag_candidates=False):
     mx = int(R.data.max().item()) if R.nnz else 0
     if dag_candidates:
         mx = _dag_candidate_max(a, R)
-    out = R.to_scipy()
-    return rb_matrix((out.data, out.indices.astype(np.int32), out.indptr.astype(np.int32)),
-                     shape=out.shape), mx_abs, mx
+    return R.to_scipy(cls=rb_matrix), mx_abs, mx
 
 
 def _dag_candidate_max(a, C):
@@ -120,9 +118,7 @@ def transitive_closure_dag_sparse(A) -> TransitiveClosure:
     except RowTooWide:   # rows past the level kernels' tables: the same closure by squaring
         W, mx_abs, mx = _squaring(csr, 64, cycle_error=True, dag_candidates=True)
         return TransitiveClosure(W, (mx.bit_length() - 1) if mx > 1 else 0)
-    out = C.to_scipy()
-    W = rb_matrix((out.data, out.indices.astype(np.int32), out.indptr.astype(np.int32)), shape=out.shape)
-    return TransitiveClosure(W, (mx.bit_length() - 1) if mx > 1 else 0)
+    return TransitiveClosure(C.to_scipy(cls=rb_matrix), (mx.bit_length() - 1) if mx > 1 else 0)
 
 
 def transitive_closure_squaring(A, max_iterations=64) -> TransitiveClosure:
@@ -150,7 +146,7 @@ def component_wise_closure(A, method: str = "auto", densify_threshold: int = 500
     (the reference's DTYPE); W is a CSR matrix with int32 values and sorted rows.
     """
     import scipy.sparse as sp
-    from ...device import require_cuda, to_device, to_host_pinned
+    from ...device import csr_from_parts, require_cuda, to_device, to_host_pinned
     from ...components import component_closure_device
     csr = _as_csr(A)
     n = csr.shape[0]
@@ -169,7 +165,7 @@ def component_wise_closure(A, method: str = "auto", densify_threshold: int = 500
     oi, oj, ov, diameter, _ = component_closure_device(ip, ij, iv, n, method, densify_threshold)
     if ov.numel() < 2**31 - 1:   # int32 row pointers when they fit: scipy keeps the arrays as given
         oi = oi.to(torch.int32)
-    W = sp.csr_matrix((to_host_pinned(ov), to_host_pinned(oj), to_host_pinned(oi)), shape=(n, n))
+    W = csr_from_parts(to_host_pinned(ov), to_host_pinned(oj), to_host_pinned(oi), (n, n))
     return TransitiveClosure(W, int(diameter))
 
 

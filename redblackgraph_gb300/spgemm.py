@@ -51,10 +51,11 @@ class DeviceCSR:
                    to_device(np.ascontiguousarray(m.indices, dtype=np.int32), dev),
                    to_device(data, dev), tuple(m.shape))
 
-    def to_scipy(self):
-        import scipy.sparse as sp
-        return sp.csr_matrix((to_host(self.data), to_host(self.indices), to_host(self.indptr)),
-                             shape=self.shape)
+    def to_scipy(self, cls=None):
+        """The matrix on the host (rows as stored; no constructor copies)."""
+        from .device import csr_from_parts
+        return csr_from_parts(to_host(self.data), to_host(self.indices), to_host(self.indptr), self.shape,
+                              canonical=False, cls=cls)
 
     def equal(self, other: "DeviceCSR") -> bool:
         """Same pattern and values (compared as values, whatever the two dtypes)."""
