@@ -339,26 +339,32 @@ int32_t rbg_cc_densify(int32_t dtype, int64_t n, const int64_t *indptr, const in
                        const int64_t *start, const int64_t *dense_off, void *flat,
                        int64_t flat_elems, rbg_stream_t stream);
 
+/* 64-bit words of the optional chunk mask of rbg_cc_compact_count / _fill for a batch of
+ * flat_elems dense elements. */
+int32_t rbg_cc_chunk_mask_words(int64_t n, int64_t ncomp, int64_t flat_elems, int64_t *words);
+
 /*
  * Count the nonzeros of the closed blocks per global row and scan them; *nnz (host) is the
  * merged matrix's nnz.  When comp_max (device, ncomp int32) is not NULL it receives the largest
  * value of each closed component, floored at 0 (the final-value diameter of the 'D' method,
- * redblackgraph/sparse/csgraph/_shortest_path.pyx:842-845).  Synchronises `stream`.
+ * redblackgraph/sparse/csgraph/_shortest_path.pyx:842-845).  When chunk_mask (device,
+ * rbg_cc_chunk_mask_words words) is not NULL it records which 32-column chunks of every row
+ * hold a nonzero, and rbg_cc_compact_fill then reads only those.  Synchronises `stream`.
  */
 int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
                              const int64_t *start, const int64_t *dense_off, const int32_t *flat,
                              void *workspace, int64_t workspace_bytes, int64_t *nnz,
-                             int32_t *comp_max, rbg_stream_t stream);
+                             int32_t *comp_max, uint64_t *chunk_mask, rbg_stream_t stream);
 
 /*
  * Write the merged CSR matrix (replaces merge_component_matrices, _components.pyx:254-324):
  * indptr (n + 1, int64), indices (nnz, int32, ascending in each row), data (nnz, int32).  Uses
- * the counts rbg_cc_compact_count left in `workspace`.  Ordered on `stream`.
+ * the counts (and the chunk mask, when not NULL) rbg_cc_compact_count left.  Ordered on `stream`.
  */
 int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *local,
                             const int64_t *start, const int64_t *dense_off, const int32_t *flat,
                             const int32_t *sorted_vertex, const void *workspace, int64_t *indptr,
-                            int32_t *indices, int32_t *data, rbg_stream_t stream);
+                            int32_t *indices, int32_t *data, const uint64_t *chunk_mask, rbg_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Relationship lookups on resident closures (redblackgraph/reference/calc_relationship.py:54-71).

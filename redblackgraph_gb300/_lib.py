@@ -118,8 +118,9 @@ SIGNATURES = [
     ("rbg_cc_workspace_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
     ("rbg_cc_label", _I32, [_I64, _P, _P, _P, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64), _P]),
     ("rbg_cc_densify", _I32, [_I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _P]),
-    ("rbg_cc_compact_count", _I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P]),
-    ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("rbg_cc_chunk_mask_words", _I32, [_I64, _I64, _I64, ctypes.POINTER(_I64)]),
+    ("rbg_cc_compact_count", _I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P, _P]),
+    ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("rbg_relationship_lookup", _I32, [_I64, _P, _P, _P]),
     ("rbg_dag_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),
     ("rbg_dag_closure", _I32, [ctypes.POINTER(RbgCsr), _P, _I64, _P, _P, _I64, _P, _P, ctypes.POINTER(_I64),

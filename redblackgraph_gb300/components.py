@@ -94,14 +94,18 @@ def compact(comps: Components, blocks: DenseBlocks, want_max: bool = False, stre
     sh = stream_handle(stream)
     args = (comps.label.data_ptr(), comps.local.data_ptr(), comps.start.data_ptr(),
             blocks.dense_off.data_ptr(), blocks.flat.data_ptr())
+    mw = ctypes.c_int64(0)
+    _lib.check(L.rbg_cc_chunk_mask_words(n, k, blocks.flat.numel(), ctypes.byref(mw)), "cc_chunk_mask_words")
+    mask = torch.empty(max(mw.value, 1), dtype=torch.int64, device=dev)   # which 32-column chunks hold values
     _lib.check(L.rbg_cc_compact_count(n, k, *args, comps.workspace.data_ptr(), comps.workspace.numel(),
-                                      ctypes.byref(nnz), cmax.data_ptr() if cmax is not None else None, sh),
+                                      ctypes.byref(nnz), cmax.data_ptr() if cmax is not None else None,
+                                      mask.data_ptr(), sh),
                "cc_compact_count")
     indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
     indices = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
     data = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
     _lib.check(L.rbg_cc_compact_fill(n, *args, comps.sorted_vertex.data_ptr(), comps.workspace.data_ptr(),
-                                     indptr.data_ptr(), indices.data_ptr(), data.data_ptr(), sh),
+                                     indptr.data_ptr(), indices.data_ptr(), data.data_ptr(), mask.data_ptr(), sh),
                "cc_compact_fill")
     return indptr, indices[:nnz.value], data[:nnz.value], cmax
 

@@ -109,25 +109,50 @@ __global__ void cc_densify_kernel(int64_t n, const int64_t *indptr, const int *i
 
 // nonzeros of each closed row (warp per global row); optionally the largest value of each
 // component (signed, floored at 0), which the final-value diameter needs
+// Chunk masks: bit b of a row's mask words says whether columns [32 b, 32 b + 32) of the closed
+// row hold a nonzero, so the fill reads only those chunks.  Component c keeps its rows' words
+// (ceil(nc / 2048) each) from word ceil(dense_off[c] / 2048) + start[c] + c on.
+__device__ __forceinline__ int64_t cc_mask_base(int c, const int64_t *start, const int64_t *dense_off) {
+    return (dense_off[c] + 2047) / 2048 + start[c] + c;
+}
+
 __global__ void cc_rowcount_kernel(int64_t n, const int *label, const int *local, const int64_t *start,
-                                   const int64_t *dense_off, const int *flat, int64_t *cnt, int *comp_max) {
+                                   const int64_t *dense_off, const int *flat, int64_t *cnt, int *comp_max,
+                                   unsigned long long *mask) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += warps) {
         const int c = label[u];
         const int64_t nc = start[c + 1] - start[c];
         const int *row = flat + dense_off[c] + (int64_t)local[u] * nc;
+        const int64_t words = (nc + 2047) / 2048;
+        unsigned long long *mrow = mask ? mask + cc_mask_base(c, start, dense_off) + (int64_t)local[u] * words : nullptr;
         int64_t k = 0;
         int mx = 0;
-        for (int64_t j = lane; j < nc; j += 32) {
-            const int v = row[j];
-            k += v != 0;
-            mx = max(mx, v);
+        unsigned long long word = 0;
+        for (int64_t j0 = 0; j0 < nc; j0 += 256) {     // eight chunks of 32 columns in flight
+            int v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int64_t j = j0 + 32 * q + lane;
+                v[q] = j < nc ? row[j] : 0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int64_t c0 = j0 + 32 * q;
+                if (c0 >= nc) break;                    // uniform
+                mx = max(mx, v[q]);
+                const unsigned bal = __ballot_sync(0xffffffffu, v[q] != 0);
+                k += __popc(bal);
+                const int64_t chunk = c0 >> 5;
+                if (bal) word |= 1ull << (chunk & 63);
+                if (mrow && ((chunk & 63) == 63 || c0 + 32 >= nc)) {
+                    if (lane == 0) mrow[chunk >> 6] = word;
+                    word = 0;
+                }
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            k += __shfl_xor_sync(0xffffffffu, k, o);
-            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        }
+        mx = __reduce_max_sync(0xffffffffu, mx);
         if (lane == 0) {
             cnt[u] = k;
             if (comp_max && mx > 0) atomicMax(comp_max + c, mx);
@@ -138,7 +163,7 @@ __global__ void cc_rowcount_kernel(int64_t n, const int *label, const int *local
 // write each closed row with global column indices (ascending: local order is vertex order)
 __global__ void cc_fill_kernel(int64_t n, const int *label, const int *local, const int64_t *start,
                                const int64_t *dense_off, const int *flat, const int *sorted_vertex,
-                               const int64_t *outptr, int *oj, int *ov) {
+                               const int64_t *outptr, int *oj, int *ov, const unsigned long long *mask) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += warps) {
@@ -146,6 +171,27 @@ __global__ void cc_fill_kernel(int64_t n, const int *label, const int *local, co
         const int64_t s = start[c], nc = start[c + 1] - s;
         const int *row = flat + dense_off[c] + (int64_t)local[u] * nc;
         int64_t out = outptr[u];
+        if (mask) {
+            const int64_t words = (nc + 2047) / 2048;
+            const unsigned long long *mrow = mask + cc_mask_base(c, start, dense_off) + (int64_t)local[u] * words;
+            for (int64_t wi = 0; wi < words; ++wi) {
+                unsigned long long word = mrow[wi];
+                while (word) {
+                    const int b = __ffsll((long long)word) - 1;
+                    word &= word - 1;
+                    const int64_t j = (wi * 64 + b) * 32 + lane;
+                    const int v = j < nc ? row[j] : 0;
+                    const unsigned bal = __ballot_sync(0xffffffffu, v != 0);
+                    if (v != 0) {
+                        const int64_t pos = out + __popc(bal & ((1u << lane) - 1u));
+                        oj[pos] = sorted_vertex[s + j];
+                        ov[pos] = v;
+                    }
+                    out += __popc(bal);
+                }
+            }
+            continue;
+        }
         for (int64_t j0 = 0; j0 < nc; j0 += 32) {
             const int64_t j = j0 + lane;
             const int v = j < nc ? row[j] : 0;
@@ -286,10 +332,16 @@ extern "C" int32_t rbg_cc_densify(int32_t dtype, int64_t n, const int64_t *indpt
     return RBG_OK;
 }
 
+extern "C" int32_t rbg_cc_chunk_mask_words(int64_t n, int64_t ncomp, int64_t flat_elems, int64_t *words) {
+    if (!words || n < 0 || ncomp < 0 || flat_elems < 0) return RBG_ERR_INVALID;
+    *words = (flat_elems + 2047) / 2048 + n + 2 * ncomp + 2;
+    return RBG_OK;
+}
+
 extern "C" int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
                                         const int64_t *start, const int64_t *dense_off, const int32_t *flat,
                                         void *workspace, int64_t workspace_bytes, int64_t *nnz,
-                                        int32_t *comp_max, rbg_stream_t stream) {
+                                        int32_t *comp_max, uint64_t *chunk_mask, rbg_stream_t stream) {
     if (n < 0 || ncomp < 0 || ncomp > n || !workspace || !nnz) return RBG_ERR_INVALID;
     if (workspace_bytes < (int64_t)cc_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
     CcWs w;
@@ -300,7 +352,8 @@ extern "C" int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t 
     if (n > 0) {
         note_launches(1);
         cc_rowcount_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(n, label, local, start, dense_off, flat, w.cnt,
-                                                                 comp_max);
+                                                                 comp_max,
+                                                                 reinterpret_cast<unsigned long long *>(chunk_mask));
     }
     size_t tb = w.tmp_bytes;
     RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.cnt, w.cnt, (int)(n + 1), s));
@@ -314,7 +367,7 @@ extern "C" int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t 
 extern "C" int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *local, const int64_t *start,
                                        const int64_t *dense_off, const int32_t *flat, const int32_t *sorted_vertex,
                                        const void *workspace, int64_t *indptr, int32_t *indices, int32_t *data,
-                                       rbg_stream_t stream) {
+                                       const uint64_t *chunk_mask, rbg_stream_t stream) {
     if (n < 0 || !workspace || !indptr) return RBG_ERR_INVALID;
     CcWs w;
     cc_layout(n, const_cast<unsigned char *>(reinterpret_cast<const unsigned char *>(workspace)), &w);
@@ -323,7 +376,8 @@ extern "C" int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const in
     if (n > 0) {
         note_launches(1);
         cc_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(n, label, local, start, dense_off, flat, sorted_vertex,
-                                                             w.cnt, indices, data);
+                                                             w.cnt, indices, data,
+                                                             reinterpret_cast<const unsigned long long *>(chunk_mask));
         RBG_CUDA_TRY(cudaGetLastError());
     }
     return RBG_OK;

@@ -559,17 +559,26 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
     if (i < n) {
         const U *wrow = work + i * np;
         const unsigned char *orow = occ + (i / FW_B) * nb;
-        for (int64_t j = threadIdx.x & 31; j < n; j += 32) {
-            T v;
-            if (i == j || (c.triangular && i > j)) {
-                v = in[i * c.ld_in + j];
-            } else if (!orow[j / FW_B]) {
-                v = (T)0;
-            } else {
-                const U w = wrow[j];
-                v = lane<U>::valid(w) ? (T)w : (T)0;
+        // four columns per lane in flight: 128 columns per warp and step
+        for (int64_t j0 = threadIdx.x & 31; j0 < n; j0 += 128) {
+            T v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t j = j0 + 32 * q;
+                v[q] = (T)0;
+                if (j >= n) continue;
+                if (i == j || (c.triangular && i > j)) {
+                    v[q] = in[i * c.ld_in + j];
+                } else if (orow[j / FW_B]) {
+                    const U w = wrow[j];
+                    v[q] = lane<U>::valid(w) ? (T)w : (T)0;
+                }
             }
-            out[i * c.ld_out + j] = v;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t j = j0 + 32 * q;
+                if (j < n) out[i * c.ld_out + j] = v[q];
+            }
         }
     }
 }
