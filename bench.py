@@ -696,7 +696,9 @@ def serve_stats(st, reqs):
             "makespan_s": st.makespan_s, "batches": st.batches, "max_batch": st.max_batch,
             "lookup_launches": st.lookup_launches, "evictions": st.evictions, "reloads": st.reloads,
             "peak_arena_gb": st.peak_arena_bytes / 1e9,
-            "errors": sum(1 for r in reqs if r.kind == "closure" and r.result[0] != 0)}
+            "errors": sum(1 for r in reqs if r.kind == "closure" and r.result[0] != 0),
+            **({"mutations": st.mutations, "mutation_p50_ms": lat["mutation"]["p50"],
+                "mutation_p99_ms": lat["mutation"]["p99"]} if st.mutations else {})}
 
 
 def run_serving(count=None):
@@ -727,6 +729,16 @@ def run_serving(count=None):
         torch.cuda.synchronize()
         st = srv.run(reqs)
         out[name] = serve_stats(st, reqs)
+    # the same stream with a fifth of the lookups turned into mutations (links and new vertices
+    # applied to the resident closures by relational composition)
+    mreq = make_stream(cfg["count"], cfg["rate"], cfg["lookup_fraction"], cfg["lo"], cfg["hi"],
+                       cfg["seed"], warm=cfg["warm"], mutation_fraction=0.2)
+    mwarm, mreqs = mreq[:cfg["warm"]], mreq[cfg["warm"]:]
+    srv = Server(ex, cfg["budget"], Policy(inflight=2))
+    srv.run(mwarm)
+    torch.cuda.synchronize()
+    st = srv.run(mreqs)
+    out["batched_with_mutations"] = serve_stats(st, mreqs)
     ex.close()
     del ex
     torch.cuda.empty_cache()

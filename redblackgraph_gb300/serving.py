@@ -15,6 +15,13 @@ vertices of a graph closed earlier.  The server
 * runs up to ``inflight`` closure batches at once, each on its own CUDA stream and host worker,
   while the main loop keeps admitting; lookups on closed graphs go out in batches on a further
   stream (``rbg_relationship_lookup``), overlapping the closures on the device;
+* applies *mutations* of resident closed graphs without closing them again: a *link* request
+  adds the relationship u -> v (value ``rel``) to a graph (``rbg_edge_compose``, in place), an
+  *add* request adds a new vertex with parents u and v and colour ``rel`` (``rbg_vertex_compose``
+  into an (n+1) x (n+1) extent, the old extent released when it completes).  Mutations and
+  lookups leave one queue in arrival order on one stream, so a lookup sees exactly the mutations
+  that arrived before it.  A mutated graph is no longer evicted (its mutations cannot be
+  regenerated from its seed);
 * records each request's latency (arrival to completion) for p50/p99 reporting.
 
 The same server with ``Policy.unbatched_baseline()`` handles one request at a time with one
@@ -40,15 +47,17 @@ ALIGN = 256
 @dataclass
 class Request:
     rid: int
-    kind: str                       # "closure" or "lookup"
+    kind: str                       # "closure", "lookup", "link" or "add"
     arrival: float                  # seconds after the start of the stream
     n: int = 0                      # closure: vertices
     seed: int = 0                   # closure: pedigree seed
-    target: int = -1                # lookup: rid of the closure request whose graph it reads
-    u: int = 0
+    target: int = -1                # lookup / link / add: rid of the closure request of its graph
+    u: int = 0                      # lookup: the two vertices; link: u -> v; add: the parents
     v: int = 0
+    rel: int = 0                    # link: relationship value (2 or 3); add: colour (-1 or 1)
     done: float = math.nan          # completion, seconds after the start
-    result: object = None           # closure: (status, diameter); lookup: Relationship
+    result: object = None           # closure: (status, diameter); lookup: Relationship;
+                                    # link / add: status (0, or the RBG_ERR_* the change would raise)
 
     @property
     def latency(self) -> float:
@@ -61,12 +70,15 @@ def storage_dtype(n: int):
 
 
 def make_stream(count: int, rate: float, lookup_fraction: float, lo: int, hi: int, seed: int,
-                warm: int = 0) -> list[Request]:
+                warm: int = 0, mutation_fraction: float = 0.0) -> list[Request]:
     """Seeded request stream: ``warm`` closure requests at time 0 (closed before measuring),
     then ``count`` requests with exponential inter-arrival times of mean 1/rate.  Sizes are
     log-uniform in [lo, hi]; a lookup reads two distinct vertices of a graph whose closure
-    request arrived before it."""
+    request arrived before it.  A ``mutation_fraction`` of the non-closure requests are
+    mutations of such a graph, half links between two of its vertices, half new vertices with
+    two of its vertices as parents."""
     rng = np.random.default_rng(seed)
+    mrng = np.random.default_rng(seed + 7_777_777)   # the mutation draws leave the base stream as it is
     reqs: list[Request] = []
     closures: list[int] = []
     for k in range(warm):
@@ -80,7 +92,13 @@ def make_stream(count: int, rate: float, lookup_fraction: float, lo: int, hi: in
             g = closures[int(rng.integers(len(closures)))]
             n = reqs[g].n
             u, v = (int(x) for x in rng.choice(n, size=2, replace=False))
-            reqs.append(Request(k, "lookup", t, target=g, u=u, v=v))
+            if mutation_fraction > 0 and mrng.random() < mutation_fraction:
+                if mrng.random() < 0.5:
+                    reqs.append(Request(k, "link", t, target=g, u=u, v=v, rel=int(2 + mrng.integers(2))))
+                else:
+                    reqs.append(Request(k, "add", t, target=g, u=u, v=v, rel=int(-1 if mrng.random() < 0.5 else 1)))
+            else:
+                reqs.append(Request(k, "lookup", t, target=g, u=u, v=v))
         else:
             n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
             reqs.append(Request(k, "closure", t, n=n, seed=int(rng.integers(2**31 - 1))))
@@ -156,6 +174,7 @@ class Resident:
     pins: int = 0                   # queued lookups that need this graph
     status: int = 0
     diameter: int = 0
+    mutated: bool = False           # changed by a link / add: never evicted
 
 
 class GraphStore:
@@ -177,8 +196,7 @@ class GraphStore:
             raise MemoryError(f"a {n}-vertex graph does not fit in the memory budget")
         off = self.arena.alloc(nbytes)
         if off is None:
-            victims = sorted((g for g in self.graphs.values() if g.state == "closed" and g.pins == 0),
-                             key=lambda g: g.last_use)
+            victims = self._victims()
             for g in victims:
                 self.evict(g.gid)
                 off = self.arena.alloc(nbytes)
@@ -189,6 +207,34 @@ class GraphStore:
         r = Resident(gid, n, np.dtype(dtype), off, nbytes, last_use=now)
         self.graphs[gid] = r
         return r
+
+    def _victims(self, keep: int = -1):
+        return sorted((g for g in self.graphs.values()
+                       if g.state == "closed" and g.pins == 0 and not g.mutated and g.gid != keep),
+                      key=lambda g: g.last_use)
+
+    def grow(self, gid: int, n: int, now: float):
+        """A new extent for graph gid at n x n (its dtype), evicting other LRU graphs as needed;
+        returns its offset, or None when it cannot fit now.  The caller moves the graph and then
+        calls ``moved``."""
+        g = self.graphs[gid]
+        nbytes = n * n * g.dtype.itemsize
+        if Arena.round(nbytes) > self.arena.capacity:
+            raise MemoryError(f"a {n}-vertex graph does not fit in the memory budget")
+        off = self.arena.alloc(nbytes)
+        if off is None:
+            for v in self._victims(keep=gid):
+                self.evict(v.gid)
+                off = self.arena.alloc(nbytes)
+                if off is not None:
+                    break
+        return off
+
+    def moved(self, gid: int, n: int, offset: int, now: float) -> None:
+        """Graph gid now lives at `offset` with n vertices; its old extent is released."""
+        g = self.graphs[gid]
+        self.arena.release(g.offset, g.nbytes)
+        g.n, g.offset, g.nbytes, g.last_use = n, offset, n * n * g.dtype.itemsize, now
 
     def evict(self, gid: int) -> None:
         g = self.graphs.pop(gid)
@@ -223,6 +269,7 @@ class ServeStats:
     requests: int = 0
     closures: int = 0
     lookups: int = 0
+    mutations: int = 0
     batches: int = 0
     lookup_launches: int = 0
     max_batch: int = 0
@@ -270,7 +317,8 @@ class Server:
         waiting: dict[int, list[Request]] = {}       # gid -> lookups waiting for its closure
         ready: deque[Request] = deque()
         inflight: list = []                          # (future, jobs)
-        lookup_inflight = None                       # (future, lookups)
+        lookup_inflight = None                       # (future, lookups or [mutation], new extent)
+        mutation_next = False                        # a mutation waits: it goes before more lookups
         st = ServeStats(requests=len(requests))
         remaining = len(requests)
         t0 = clock()
@@ -288,7 +336,10 @@ class Server:
                     st.closures += 1
                     enqueue_closure(r.rid, r)
                     continue
-                st.lookups += 1
+                if r.kind == "lookup":
+                    st.lookups += 1
+                else:
+                    st.mutations += 1
                 self._pin(r.target)
                 g = self.store.get(r.target)
                 if g is not None and g.state == "closed":
@@ -314,24 +365,66 @@ class Server:
                     ready.extend(waiting.pop(job.gid, []))
                 progressed = True
             if lookup_inflight is not None and lookup_inflight[0].done():
-                fut, lks = lookup_inflight
-                rels, t_done = fut.result()
-                for r, rel in zip(lks, rels):
-                    r.done, r.result = t_done, rel
+                fut, lks, new_off = lookup_inflight
+                out, t_done = fut.result()
+                if lks[0].kind == "lookup":
+                    for r, rel in zip(lks, out):
+                        r.done, r.result = t_done, rel
+                        g = self.store.get(r.target)
+                        if g is not None:
+                            g.last_use = t_done
+                        self._unpin(r.target)
+                        remaining -= 1
+                else:                                   # one mutation
+                    r = lks[0]
                     g = self.store.get(r.target)
-                    if g is not None:
-                        g.last_use = t_done
+                    if r.kind == "add" and out == 0:
+                        self.store.moved(r.target, g.n + 1, new_off, t_done)
+                    elif r.kind == "add":
+                        self.store.arena.release(new_off, (g.n + 1) * (g.n + 1) * g.dtype.itemsize)
+                    g.mutated |= out == 0
+                    g.last_use = t_done
+                    r.done, r.result = t_done, out
                     self._unpin(r.target)
                     remaining -= 1
                 lookup_inflight = None
                 progressed = True
-            # ---- lookups on closed graphs
+            # ---- lookups and mutations on closed graphs, one stream: a lookup never passes a
+            # mutation of its own graph that arrived before it; lookups of other graphs do, and
+            # a pending mutation goes out after at most one lookup batch
             if lookup_inflight is None and ready:
-                lks = [ready.popleft() for _ in range(min(P.lookup_batch, len(ready)))]
-                items = [(self.store.get(r.target), r.u, r.v) for r in lks]
-                lookup_inflight = (self.ex.lookups_async(items, t0), lks)
-                st.lookup_launches += 1
-                progressed = True
+                lks, blocked, first_mut = [], set(), None
+                if not (mutation_next and any(r.kind != "lookup" for r in ready)):
+                    for r in ready:
+                        if r.kind != "lookup":
+                            blocked.add(r.target)
+                            first_mut = r if first_mut is None else first_mut
+                        elif r.target not in blocked:
+                            lks.append(r)
+                            if len(lks) == P.lookup_batch:
+                                break
+                if lks:
+                    taken = set(id(r) for r in lks)
+                    ready = deque(r for r in ready if id(r) not in taken)
+                    items = [(self.store.get(r.target), r.u, r.v) for r in lks]
+                    lookup_inflight = (self.ex.lookups_async(items, t0), lks, None)
+                    st.lookup_launches += 1
+                    mutation_next = True
+                    progressed = True
+                else:
+                    r = next(x for x in ready if x.kind != "lookup")
+                    g = self.store.get(r.target)
+                    new_off = None
+                    if r.kind == "add":
+                        new_off = self.store.grow(r.target, g.n + 1, t)
+                        st.peak_arena_bytes = max(st.peak_arena_bytes, self.store.arena.used)
+                    if r.kind == "link" or new_off is not None:
+                        ready.remove(r)
+                        lookup_inflight = (self.ex.mutate_async(g, r, new_off, t0), [r], new_off)
+                        mutation_next = False
+                        progressed = True
+                    elif not inflight:
+                        raise MemoryError("serving stalled: a grown graph does not fit in the budget")
             # ---- closure batches
             while len(inflight) < P.inflight and closure_q:
                 jobs, cells = [], 0
@@ -367,6 +460,9 @@ class Server:
             "closure": percentiles([r.latency * 1e3 for r in requests if r.kind == "closure"]),
             "lookup": percentiles([r.latency * 1e3 for r in requests if r.kind == "lookup"]),
         }
+        if st.mutations:
+            st.latency_ms["mutation"] = percentiles([r.latency * 1e3 for r in requests
+                                                     if r.kind in ("link", "add")])
         return st
 
 
@@ -515,6 +611,32 @@ class GpuExecutor:
             d = to_device(np.frombuffer(table, dtype=np.uint8).copy(), self.device, self.lstream)
             raw = lookup_table(d, len(items), self.lstream)
         return decode(raw, dts), time.perf_counter() - t0
+
+    # -- mutations (on the lookup stream, so they keep their order with the lookups)
+    def mutate_async(self, g: Resident, req: Request, new_off, t0):
+        return self.pool.submit(self._mutate, g.offset, g.n, g.dtype, req, new_off, t0)
+
+    def _mutate(self, off, n, dtype, req, new_off, t0):
+        from .composition import edge_compose_device, vertex_compose_device
+        from .device import torch_dtype
+        torch, lib = self.torch, self.lib
+        td = torch_dtype(dtype)
+        R = self.buf[off:off + n * n * dtype.itemsize].view(td).view(n, n)
+        with torch.cuda.stream(self.lstream):
+            if req.kind == "link":
+                # the reference's wrapper refuses a link against an existing path (a cycle)
+                if int(R[req.v, req.u].item()) != 0:
+                    return lib.RBG_ERR_CYCLE, time.perf_counter() - t0
+                _, res = edge_compose_device(R, req.u, req.v, req.rel, out=R, stream=self.lstream)
+            else:
+                m = n + 1
+                new = self.buf[new_off:new_off + m * m * dtype.itemsize].view(td).view(m, m)
+                u = torch.zeros(n, dtype=td, device=self.device)
+                u[req.u], u[req.v] = 2, 3           # father, mother
+                v = torch.zeros(n, dtype=td, device=self.device)
+                _, res = vertex_compose_device(R, u, v, req.rel, out=new, stream=self.lstream)
+            self.lstream.synchronize()
+        return int(res.status), time.perf_counter() - t0
 
     def close(self):
         self.pool.shutdown(wait=True)

@@ -81,6 +81,7 @@ class FakeExecutor:
         self.batches = []
         self.lookups = []
         self.resident_at_launch = []
+        self.log = []
 
     @staticmethod
     def _done(value):
@@ -97,7 +98,15 @@ class FakeExecutor:
         for g, u, v in items:
             assert g is not None and g.state == "closed"
         self.lookups.append([(g.gid, u, v) for g, u, v in items])
-        return self._done(([("rel", g.gid, u, v) for g, u, v in items], time.perf_counter() - t0))
+        self.log.extend(("lookup", g.gid) for g, _, _ in items)
+        return self._done(([("rel", g.gid, u, v, g.n) for g, u, v in items], time.perf_counter() - t0))
+
+    def mutate_async(self, g, req, new_off, t0):
+        assert g.state == "closed"
+        if req.kind == "add":
+            assert new_off is not None and new_off != g.offset
+        self.log.append((req.kind, g.gid))
+        return self._done((0, time.perf_counter() - t0))
 
 
 def test_server_completes_everything_in_order():
@@ -108,7 +117,7 @@ def test_server_completes_everything_in_order():
     by = {r.rid: r for r in reqs}
     for r in reqs:
         if r.kind == "lookup":
-            assert r.result == ("rel", r.target, r.u, r.v)
+            assert r.result[:4] == ("rel", r.target, r.u, r.v)
             assert r.done >= by[r.target].done
         else:
             assert r.result == (0, r.n % 7)
@@ -141,8 +150,45 @@ def test_server_budget_eviction_and_reload():
     srv = Server(ex, cap)
     st = srv.run(reqs)
     assert st.evictions >= 3 and st.reloads == 1
-    assert reqs[-1].result == ("rel", 0, 1, 2)
+    assert reqs[-1].result[:4] == ("rel", 0, 1, 2)
     for snap in ex.resident_at_launch:            # extents stay inside the arena
         for gid, off, nb in snap:
             assert off + nb <= cap
     assert srv.store.arena.used <= srv.store.arena.capacity
+
+
+def test_server_mutations_in_order_and_growth():
+    """Links and vertex additions leave the lookup queue in arrival order (a lookup after an
+    add sees the grown graph), an add moves the graph to a larger extent and frees the old one,
+    and mutated graphs are not evicted."""
+    reqs = make_stream(400, 20000.0, 0.6, 16, 200, seed=3, warm=5, mutation_fraction=0.3)
+    kinds = {r.kind for r in reqs}
+    assert {"link", "add", "lookup", "closure"} <= kinds
+    ex = FakeExecutor()
+    srv = Server(ex, 1 << 30)
+    srv.run(reqs[:5])
+    st = srv.run(reqs[5:])
+    assert st.mutations == sum(r.kind in ("link", "add") for r in reqs[5:])
+    assert all(np.isfinite(r.done) for r in reqs)
+    # per graph, mutations and lookups were issued in arrival order
+    issued = [e for e in ex.log]
+    for gid in {r.target for r in reqs if r.kind != "closure"}:
+        want = [(r.kind, gid) for r in sorted(reqs, key=lambda r: (r.arrival, r.rid))
+                if r.kind != "closure" and r.target == gid]
+        assert [e for e in issued if e[1] == gid] == want
+    # a lookup answers on the graph as grown by the adds that arrived before it
+    grown = {}
+    for r in sorted(reqs, key=lambda r: (r.arrival, r.rid)):
+        if r.kind == "closure":
+            grown[r.rid] = r.n
+        elif r.kind == "add":
+            grown[r.target] += 1
+        elif r.kind == "lookup":
+            assert r.result[4] == grown[r.target], r
+    for gid, n in grown.items():
+        g = srv.store.get(gid)
+        if g is not None:
+            assert g.n == n and g.nbytes == n * n * g.dtype.itemsize
+    assert srv.store.arena.used <= srv.store.arena.capacity
+    mutated = [g for g in srv.store.graphs.values() if g.mutated]
+    assert mutated and all(g.gid in srv.store.graphs for g in mutated)

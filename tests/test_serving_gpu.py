@@ -95,3 +95,50 @@ def test_unbatched_baseline_and_eviction(native):
             W = ex.kept[r.target]
             assert (r.result.common_ancestor, r.result.relationship) == O.calculate_relationship(W[r.u], W[r.v])
     ex.close()
+
+
+def test_served_mutations_match_sequential_oracle(native):
+    """Links and vertex additions served among lookups: every lookup answers on the graph as
+    changed by the mutations that arrived before it, and the resident closures end equal to the
+    oracle's compositions applied one after another in arrival order (a link against an
+    existing path is refused with the cycle status and changes nothing)."""
+    from redblackgraph_gb300 import _lib
+    from redblackgraph_gb300.serving import GpuExecutor, Policy, Server, make_stream
+    allreq = make_stream(300, 5000.0, 0.7, 24, 400, seed=21, warm=8, mutation_fraction=0.35)
+    warm, reqs = allreq[:8], allreq[8:]
+    cap = 256 << 20
+    ex = GpuExecutor(arena_bytes=cap, slots=2, keep=True)
+    ex.prepare(allreq)
+    srv = Server(ex, cap, Policy(inflight=2, max_batch=32))
+    srv.run(warm)
+    st = srv.run(reqs)
+    assert st.mutations > 20
+    state = {}
+    for r in sorted(allreq, key=lambda r: (r.arrival, r.rid)):
+        if r.kind == "closure":
+            state[r.rid] = ex.kept[r.rid].copy()       # closed alone: checked by the test above
+            continue
+        W = state[r.target]
+        if r.kind == "lookup":
+            assert (r.result.common_ancestor, r.result.relationship) == O.calculate_relationship(W[r.u], W[r.v])
+        elif r.kind == "link":
+            if W[r.v, r.u] != 0:
+                assert r.result == _lib.RBG_ERR_CYCLE, r
+                continue
+            out, info = O.edge_compose(W, r.u, r.v, r.rel)
+            assert r.result == int(info[0]), r
+            if info[0] == 0:
+                state[r.target] = out
+        else:
+            n = W.shape[0]
+            u = np.zeros(n, W.dtype)
+            u[r.u], u[r.v] = 2, 3
+            out, info = O.vertex_compose(W, u, np.zeros(n, W.dtype), r.rel)
+            assert r.result == int(info[0]), r
+            if info[0] == 0:
+                state[r.target] = out
+    for gid, W in state.items():
+        g = srv.store.get(gid)
+        if g is not None and g.state == "closed":
+            assert (ex.view(g).cpu().numpy() == W).all(), gid
+    ex.close()
