@@ -213,6 +213,20 @@ fw_convert_kernel(const T *__restrict__ in_base, U *__restrict__ work_base,
         for (int64_t j0 = (int64_t)lane_id * 4; j0 < np; j0 += 32 * 4) {
             U w4[4];
             bool live = false;
+            if (rowlive && !xi && j0 + 4 <= n && (i < j0 || i >= j0 + 4)) {
+                // fast path: four off-diagonal zeros (the common case) encode as zeros and add
+                // nothing to the running maximum (no W(i, 0) (x) W(0, j) term on this row)
+                const TU a = (TU)in[i * ld + j0], b = (TU)in[i * ld + j0 + 1];
+                const TU c2 = (TU)in[i * ld + j0 + 2], d = (TU)in[i * ld + j0 + 3];
+                if ((a | b | c2 | d) == 0) {
+                    const U inf = L::inf;
+                    w4[0] = w4[1] = w4[2] = w4[3] = inf;
+                    *reinterpret_cast<uint4 *>(wrow + j0) = *reinterpret_cast<const uint4 *>(w4);
+                    if (sizeof(U) == 8)
+                        *reinterpret_cast<uint4 *>(wrow + j0 + 2) = *reinterpret_cast<const uint4 *>(w4 + 2);
+                    continue;
+                }
+            }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int64_t j = j0 + k;
