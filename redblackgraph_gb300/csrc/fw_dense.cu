@@ -534,15 +534,20 @@ fw_tile_kernel(U *__restrict__ work_base, const unsigned long long *__restrict__
     TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
     __shared__ int s_item;
     const int total = counters[CNT_TILE];
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_TILE], 1);
-        __syncthreads();
-        const int i = s_item;
-        __syncthreads();
-        if (i >= total) break;
+    if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_TILE], 1);
+    __syncthreads();
+    int i = s_item;
+    while (i < total) {
+        // the next item is claimed now and published after this one: the claim's round trip
+        // overlaps the item.  tile_item's first barrier comes before its first shared-memory
+        // write, so one barrier per item keeps the items apart.
+        int nxt = 0;
+        if (threadIdx.x == 0) nxt = atomicAdd(&counters[CUR_TILE], 1);
         const int2 e = list[i];
         tile_item<U, BN, TM, TN>(S, e.x, e.y, work_base, any_base, occ_base, comps, K0, lbits, st_base);
+        if (threadIdx.x == 0) s_item = nxt;
         __syncthreads();
+        i = s_item;
     }
 }
 

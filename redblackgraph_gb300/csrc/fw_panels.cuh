@@ -455,14 +455,18 @@ fw_panel_kernel(U *__restrict__ work_base, unsigned long long *__restrict__ any_
     PanelSmem<U> &S = *reinterpret_cast<PanelSmem<U> *>(smem_raw);
     __shared__ int s_item;
     const int total = counters[CNT_PANEL];
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_PANEL], 1);
-        __syncthreads();
-        const int i = s_item;
-        __syncthreads();
-        if (i >= total) break;
+    if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_PANEL], 1);
+    __syncthreads();
+    int i = s_item;
+    while (i < total) {
+        // the next item is claimed now and published after this one (its round trip overlaps
+        // the item); panel_item's first barrier precedes its first shared-memory write
+        int nxt = 0;
+        if (threadIdx.x == 0) nxt = atomicAdd(&counters[CUR_PANEL], 1);
         const int2 e = list[i];
         panel_item<U>(S, e.x, e.y, work_base, any_base, occ_base, rbs, comps, K0, lbits, st_base);
+        if (threadIdx.x == 0) s_item = nxt;
         __syncthreads();
+        i = s_item;
     }
 }
