@@ -393,12 +393,24 @@ class Server:
             # mutation of its own graph that arrived before it; lookups of other graphs do, and
             # a pending mutation goes out after at most one lookup batch
             if lookup_inflight is None and ready:
-                lks, blocked, first_mut = [], set(), None
-                if not (mutation_next and any(r.kind != "lookup" for r in ready)):
+                mut = None
+                if mutation_next:
+                    # the oldest mutation with no earlier lookup of its graph still queued
+                    before = set()
+                    for r in ready:
+                        if r.kind == "lookup":
+                            before.add(r.target)
+                        elif r.target not in before:
+                            mut = r
+                            break
+                        else:
+                            before.add(r.target)
+                lks = []
+                if mut is None:
+                    blocked = set()
                     for r in ready:
                         if r.kind != "lookup":
                             blocked.add(r.target)
-                            first_mut = r if first_mut is None else first_mut
                         elif r.target not in blocked:
                             lks.append(r)
                             if len(lks) == P.lookup_batch:
@@ -412,7 +424,8 @@ class Server:
                     mutation_next = True
                     progressed = True
                 else:
-                    r = next(x for x in ready if x.kind != "lookup")
+                    # no lookup can go: the head of the queue is a mutation
+                    r = mut if mut is not None else ready[0]
                     g = self.store.get(r.target)
                     new_off = None
                     if r.kind == "add":

@@ -161,3 +161,23 @@ def test_errors(native):
     a, b = [(i, j) for i in range(60) for j in range(60) if i != j and W[i, j] != 0][0]
     with pytest.raises(ValueError, match="cycle"):
         core.edge_relational_composition(core.array(W), b, a, 2)
+
+
+def test_edges_of_the_domain(native):
+    """An empty closure grows to one vertex; an unknown vertex index is refused; unsigned and
+    narrow storage types keep the C core's wrap-around of -1."""
+    import redblackgraph_gb300.core as core
+    from redblackgraph_gb300.composition import vertex_compose_host, edge_compose_host
+    out = vertex_compose_host(np.zeros(0, np.int32), np.zeros((0, 0), np.int32), np.zeros(0, np.int32), -1)
+    assert out.shape == (1, 1) and out[0, 0] == -1
+    W = _closed_pedigree(40, 5, 9, np.int32)
+    with pytest.raises(Exception):
+        edge_compose_host(W, 40, 1, 2)
+    for dt in (np.uint8, np.uint16, np.uint32, np.uint64):
+        Wt = _closed_pedigree(20, 4, 2, np.int64).astype(dt)
+        u = np.zeros(20, dt)
+        u[3] = 2
+        exp, info = O.vertex_compose(Wt, u, np.zeros(20, dt), -1)
+        if info[0] == 0:
+            got = core.vertex_relational_composition(u, core.array(Wt), np.zeros(20, dt), -1)
+            assert got.dtype == dt and (np.asarray(got) == exp).all()

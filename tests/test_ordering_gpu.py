@@ -106,3 +106,19 @@ def test_golden_extract_and_merge(native, golden):
                             shape=S.shape)
         assert (merged != exp).nnz == 0 and merged.nnz == exp.nnz
         assert (merged != S).nnz == 0
+
+
+def test_orderings_on_tiny_graphs(native):
+    """Empty and one-vertex graphs, a graph of isolated vertices (every component of size 1)."""
+    from redblackgraph_gb300.sparse import csgraph
+    e = sp.csr_matrix((0, 0), dtype=np.int32)
+    assert len(csgraph.topological_sort(e)) == 0 and csgraph.is_upper_triangular(e)
+    one = sp.csr_matrix(np.array([[-1]], np.int32))
+    o = csgraph.avos_canonical_ordering(one)
+    assert list(o.label_permutation) == [0] and o.components == {0: 1}
+    iso = np.diag(np.array([1, -1, 1, -1, -1], np.int32))
+    o = csgraph.avos_canonical_ordering(sp.csr_matrix(iso))
+    q = {c: 1 for c in range(5)}
+    assert list(o.label_permutation) == O.canonical_permutation(iso, q, np.arange(5))
+    d = csgraph.avos_canonical_ordering(iso)
+    assert list(d.label_permutation) == list(o.label_permutation)

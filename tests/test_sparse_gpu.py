@@ -263,3 +263,12 @@ def test_dag_explicit_zeros_and_deep_rows(native):
     assert (sp.csr_matrix(W).data == 0).sum() > 0
     lens = np.diff(sp.csr_matrix(W).indptr)
     assert lens.max() > 32
+
+
+def test_dag_closure_tiny(native):
+    """One vertex, and a graph of isolated vertices: the closure is the input."""
+    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse
+    for M in (np.array([[1]]), np.diag([-1, 1, 1, -1])):
+        A = sp.csr_matrix(M.astype(np.int32))
+        r = transitive_closure_dag_sparse(A)
+        assert same(r.W, A) and r.diameter == 0
