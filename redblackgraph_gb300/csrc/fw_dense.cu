@@ -578,26 +578,29 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
     if (i < n) {
         const U *wrow = work + i * np;
         const unsigned char *orow = occ + (i / FW_B) * nb;
-        // four columns per lane in flight: 128 columns per warp and step
-        for (int64_t j0 = threadIdx.x & 31; j0 < n; j0 += 128) {
+        // four consecutive columns per lane (one 16-byte lane vector, one 64-column block):
+        // 128 columns per warp and step
+        constexpr int PER = 16 / sizeof(U);
+        for (int64_t j0 = (int64_t)(threadIdx.x & 31) * 4; j0 < n; j0 += 128) {
             T v[4];
+            U w[4];
+            const bool occupied = orow[j0 / FW_B] != 0;
+            if (occupied) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int64_t j = j0 + 32 * q;
-                v[q] = (T)0;
+                for (int k = 0; k < 4; k += PER)
+                    *reinterpret_cast<uint4 *>(w + k) = *reinterpret_cast<const uint4 *>(wrow + j0 + k);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int64_t j = j0 + k;
+                v[k] = (T)0;
                 if (j >= n) continue;
-                if (i == j || (c.triangular && i > j)) {
-                    v[q] = in[i * c.ld_in + j];
-                } else if (orow[j / FW_B]) {
-                    const U w = wrow[j];
-                    v[q] = lane<U>::valid(w) ? (T)w : (T)0;
-                }
+                if (i == j || (c.triangular && i > j)) v[k] = in[i * c.ld_in + j];
+                else if (occupied) v[k] = lane<U>::valid(w[k]) ? (T)w[k] : (T)0;
             }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int64_t j = j0 + 32 * q;
-                if (j < n) out[i * c.ld_out + j] = v[q];
-            }
+            for (int k = 0; k < 4; ++k)
+                if (j0 + k < n) out[i * c.ld_out + j0 + k] = v[k];
         }
     }
 }
