@@ -162,6 +162,38 @@ int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const i
                      const void *in, void *out, uint32_t mode, void *workspace,
                      int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream);
 
+/*
+ * Row statistics rbg_fw_batch_rows records while it writes the closed matrices, so that a
+ * caller merging them into one CSR matrix (rbg_cc_compact_scan + rbg_cc_compact_fill) need
+ * not read them again.  Device arrays:
+ *   row_base   [count]: matrix c's row i is output row row_id[row_base[c] + i], or
+ *              row_base[c] + i when row_id is NULL
+ *   row_count  nonzero values of every output row
+ *   chunk_mask (NULL: none) 32-column chunks of every row that hold a nonzero, in the layout of
+ *              rbg_cc_compact_count: ceil(sizes[c] / 2048) words per row, matrix c's rows from
+ *              word ceil(offsets[c] / 2048) + row_base[c] + c
+ *   comp_max   (NULL: none) [count] largest value of each matrix, by atomic max over values
+ *              > 0: the caller zeroes it
+ */
+typedef struct rbg_row_stats {
+    const int64_t *row_base;
+    const int32_t *row_id;
+    int64_t *row_count;
+    uint64_t *chunk_mask;
+    int32_t *comp_max;
+} rbg_row_stats_t;
+
+/*
+ * rbg_fw_batch (RBG_DTYPE_INT32 only) that also records `stats` for every matrix whose result
+ * comes from the 32-bit blocked pass (results[c].path == RBG_PATH_BLOCKED32 and status
+ * RBG_OK); the rows of any other matrix are left unwritten.  Replaces the second read of the
+ * closed blocks by merge_component_matrices' row counting (_components.pyx:254-290).
+ */
+int32_t rbg_fw_batch_rows(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                          const void *in, void *out, uint32_t mode, void *workspace,
+                          int64_t workspace_bytes, const rbg_row_stats_t *stats, rbg_result_t *results,
+                          rbg_stream_t stream);
+
 /* ---------------------------------------------------------------------- sparse product */
 
 /* A CSR matrix in device memory: int64 row pointers, int32 column indices (sorted, no
@@ -355,6 +387,14 @@ int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t *label, con
                              const int64_t *start, const int64_t *dense_off, const int32_t *flat,
                              void *workspace, int64_t workspace_bytes, int64_t *nnz,
                              int32_t *comp_max, uint64_t *chunk_mask, rbg_stream_t stream);
+
+/*
+ * rbg_cc_compact_count for counts already known (row_count, device, n int64: the
+ * rbg_fw_batch_rows statistics): scans them into the workspace for rbg_cc_compact_fill;
+ * *nnz (host) is the merged matrix's nnz.  Synchronises `stream`.
+ */
+int32_t rbg_cc_compact_scan(int64_t n, const int64_t *row_count, void *workspace, int64_t workspace_bytes,
+                            int64_t *nnz, rbg_stream_t stream);
 
 /*
  * Write the merged CSR matrix (replaces merge_component_matrices, _components.pyx:254-324):

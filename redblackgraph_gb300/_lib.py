@@ -85,6 +85,12 @@ class RbgComposeResult(ctypes.Structure):
                 ("updated", ctypes.c_int64)]
 
 
+class RbgRowStats(ctypes.Structure):
+    """rbg_row_stats_t: where rbg_fw_batch_rows records per-row statistics (device pointers)."""
+    _fields_ = [("row_base", ctypes.c_void_p), ("row_id", ctypes.c_void_p), ("row_count", ctypes.c_void_p),
+                ("chunk_mask", ctypes.c_void_p), ("comp_max", ctypes.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported entry point; include/rbg_gb300.h declares them
 _P = ctypes.c_void_p
 _I32, _U32, _I64 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64
@@ -100,6 +106,7 @@ SIGNATURES = [
                                     ctypes.POINTER(RbgResult), _P]),
     ("rbg_fw_batch_workspace_bytes", _I32, [_I32, _I64, _P, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_batch", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, _P, _P]),
+    ("rbg_fw_batch_rows", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, ctypes.POINTER(RbgRowStats), _P, _P]),
     ("rbg_spgemm_head_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
     ("rbg_spgemm_count", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr),
                                 _I32, _P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _P]),
@@ -120,6 +127,7 @@ SIGNATURES = [
     ("rbg_cc_densify", _I32, [_I32, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _P]),
     ("rbg_cc_chunk_mask_words", _I32, [_I64, _I64, _I64, ctypes.POINTER(_I64)]),
     ("rbg_cc_compact_count", _I32, [_I64, _I64, _P, _P, _P, _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P, _P]),
+    ("rbg_cc_compact_scan", _I32, [_I64, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
     ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("rbg_relationship_lookup", _I32, [_I64, _P, _P, _P]),
     ("rbg_dag_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),

@@ -4,7 +4,8 @@ The graph (device CSR: int64 row pointers, int32 column indices, int32 values) i
 connected components by ``rbg_cc_label``, each component is scattered into its own dense block
 of one flat buffer (``rbg_cc_densify``), all blocks are closed by one ``rbg_fw_batch`` call in
 the Cython semantics, and the closed blocks are compacted back into one CSR matrix with global
-indices (``rbg_cc_compact_count`` / ``rbg_cc_compact_fill``).  Mirrors component_wise_closure,
+indices (``rbg_cc_compact_scan`` of the row counts the closure recorded, or
+``rbg_cc_compact_count``, then ``rbg_cc_compact_fill``).  Mirrors component_wise_closure,
 redblackgraph/sparse/csgraph/transitive_closure.py:85-195, whose per-component loop this batch
 replaces.
 """
@@ -82,25 +83,39 @@ def densify(indptr, indices, data, comps: Components, stream=None) -> DenseBlock
     return DenseBlocks(flat, sizes, offsets, dense_off)
 
 
-def compact(comps: Components, blocks: DenseBlocks, want_max: bool = False, stream=None):
+def chunk_mask_buffer(comps: Components, blocks: DenseBlocks) -> torch.Tensor:
+    """Device words for the per-row 32-column chunk masks of the closed blocks."""
+    mw = ctypes.c_int64(0)
+    _lib.check(_lib.load().rbg_cc_chunk_mask_words(comps.n, comps.count, blocks.flat.numel(), ctypes.byref(mw)),
+               "cc_chunk_mask_words")
+    return torch.empty(max(mw.value, 1), dtype=torch.int64, device=blocks.flat.device)
+
+
+def compact(comps: Components, blocks: DenseBlocks, want_max: bool = False, stream=None,
+            counted: tuple | None = None):
     """Merge the closed blocks into one CSR matrix (_components.pyx:254-324).
 
-    Returns ``(indptr int64, indices int32, data int32, comp_max or None)``."""
+    ``counted = (row_count, mask, comp_max)``: the per-row statistics the closure recorded
+    (rbg_fw_batch_rows); the blocks are then read once, by the fill.  Returns
+    ``(indptr int64, indices int32, data int32, comp_max or None)``."""
     dev = blocks.flat.device
     L = _lib.load()
     n, k = comps.n, comps.count
-    cmax = torch.empty(max(k, 1), dtype=torch.int32, device=dev) if want_max else None
     nnz = ctypes.c_int64(0)
     sh = stream_handle(stream)
     args = (comps.label.data_ptr(), comps.local.data_ptr(), comps.start.data_ptr(),
             blocks.dense_off.data_ptr(), blocks.flat.data_ptr())
-    mw = ctypes.c_int64(0)
-    _lib.check(L.rbg_cc_chunk_mask_words(n, k, blocks.flat.numel(), ctypes.byref(mw)), "cc_chunk_mask_words")
-    mask = torch.empty(max(mw.value, 1), dtype=torch.int64, device=dev)   # which 32-column chunks hold values
-    _lib.check(L.rbg_cc_compact_count(n, k, *args, comps.workspace.data_ptr(), comps.workspace.numel(),
-                                      ctypes.byref(nnz), cmax.data_ptr() if cmax is not None else None,
-                                      mask.data_ptr(), sh),
-               "cc_compact_count")
+    if counted is not None:
+        row_count, mask, cmax = counted
+        _lib.check(L.rbg_cc_compact_scan(n, row_count.data_ptr(), comps.workspace.data_ptr(),
+                                         comps.workspace.numel(), ctypes.byref(nnz), sh), "cc_compact_scan")
+    else:
+        cmax = torch.empty(max(k, 1), dtype=torch.int32, device=dev) if want_max else None
+        mask = chunk_mask_buffer(comps, blocks)     # which 32-column chunks hold values
+        _lib.check(L.rbg_cc_compact_count(n, k, *args, comps.workspace.data_ptr(), comps.workspace.numel(),
+                                          ctypes.byref(nnz), cmax.data_ptr() if cmax is not None else None,
+                                          mask.data_ptr(), sh),
+                   "cc_compact_count")
     indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
     indices = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
     data = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
@@ -135,16 +150,25 @@ def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: 
     """
     comps = label_components(indptr, indices, n, stream)
     blocks = densify(indptr, indices, data, comps, stream)
+    fw = component_methods(comps.sizes, comps.count, method, densify_threshold)
+    # the closure's finalization counts every row while it writes it (one read of the blocks less)
+    dev = blocks.flat.device
+    row_count = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
+    mask = chunk_mask_buffer(comps, blocks)
+    cmax = None if fw.all() else torch.zeros(max(comps.count, 1), dtype=torch.int32, device=dev)
+    stats = _lib.RbgRowStats(comps.start.data_ptr(), comps.sorted_vertex.data_ptr(), row_count.data_ptr(),
+                             mask.data_ptr(), cmax.data_ptr() if cmax is not None else None)
     _, res = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat,
                       mode=_lib.MODE_CYTHON | _lib.MODE_GRAPH | _lib.MODE_AUTOTUNE, stream=stream,
-                      as_array=True)
+                      as_array=True, row_stats=stats)
     bad = np.flatnonzero(res["status"] != _lib.RBG_OK)
     if bad.size:                                     # the first component (by number) raises
         r = _lib.RbgResult()
         ctypes.memmove(ctypes.addressof(r), res[bad[0]:bad[0] + 1].tobytes(), ctypes.sizeof(r))
         raise_for_cython(r)
-    fw = component_methods(comps.sizes, comps.count, method, densify_threshold)
-    oi, oj, ov, cmax = compact(comps, blocks, want_max=not bool(fw.all()), stream=stream)
+    # components closed on another path have no recorded statistics: count every row again
+    counted = (row_count, mask, cmax) if bool((res["path"] == _lib.PATH_BLOCKED32).all()) else None
+    oi, oj, ov, cmax = compact(comps, blocks, want_max=not bool(fw.all()), stream=stream, counted=counted)
     diameter = 0
     if fw.any():
         diameter = int(res["diameter"][fw].max())

@@ -364,6 +364,24 @@ extern "C" int32_t rbg_cc_compact_count(int64_t n, int64_t ncomp, const int32_t 
     return RBG_OK;
 }
 
+extern "C" int32_t rbg_cc_compact_scan(int64_t n, const int64_t *row_count, void *workspace,
+                                       int64_t workspace_bytes, int64_t *nnz, rbg_stream_t stream) {
+    if (n < 0 || !workspace || !nnz || (n > 0 && !row_count)) return RBG_ERR_INVALID;
+    if (workspace_bytes < (int64_t)cc_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
+    CcWs w;
+    cc_layout(n, reinterpret_cast<unsigned char *>(workspace), &w);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (n > 0) RBG_CUDA_TRY(cudaMemcpyAsync(w.cnt, row_count, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.cnt + n, 0, 8, s));
+    size_t tb = w.tmp_bytes;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.cnt, w.cnt, (int)(n + 1), s));
+    int64_t tot = 0;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&tot, w.cnt + n, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    *nnz = tot;
+    return RBG_OK;
+}
+
 extern "C" int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *local, const int64_t *start,
                                        const int64_t *dense_off, const int32_t *flat, const int32_t *sorted_vertex,
                                        const void *workspace, int64_t *indptr, int32_t *indices, int32_t *data,

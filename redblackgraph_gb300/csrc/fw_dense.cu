@@ -158,6 +158,24 @@ struct FwComp {
     int32_t triangular, status_index;
 };
 
+// Row statistics the finalization can record while it writes the result (rbg_fw_batch_rows,
+// storage int32): the nonzero count of every output row, which 32-column chunks of it hold a
+// nonzero, and each component's largest value.  Component c's row i is output row
+// row_id[row_base[c] + i] (row_base[c] + i when row_id is null); the chunk masks follow the
+// layout of the compaction (ceil(n / 2048) words per row, component c's rows from word
+// ceil(in_off / 2048) + row_base[c] + c).  row_count null: nothing is recorded.
+struct RowStats {
+    const int64_t *row_base = nullptr;
+    const int32_t *row_id = nullptr;
+    int64_t *row_count = nullptr;
+    unsigned long long *chunk_mask = nullptr;
+    int32_t *comp_max = nullptr;
+    bool operator==(const RowStats &o) const {
+        return row_base == o.row_base && row_id == o.row_id && row_count == o.row_count &&
+               chunk_mask == o.chunk_mask && comp_max == o.comp_max;
+    }
+};
+
 __device__ __forceinline__ int fw_find(const int64_t *__restrict__ prefix, int count, int64_t cta) {
     int lo = 0, hi = count - 1;
     while (lo < hi) {
@@ -560,7 +578,7 @@ __global__ void __launch_bounds__(FW_THREADS)
 fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_base,
                    T *__restrict__ out_base, const FwComp *__restrict__ comps,
                    const int64_t *__restrict__ prefix, int count, const DevStatus *st_base,
-                   const unsigned char *__restrict__ occ_base) {
+                   const unsigned char *__restrict__ occ_base, RowStats rs) {
     const int ci = fw_find(prefix, count, blockIdx.x);
     const FwComp c = comps[ci];
     // a component that needs another path keeps its input untouched (it may be in place)
@@ -574,17 +592,27 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
     // a 64 x 64 block that never held a valid value is all zero: its lanes are not read
     const unsigned char *occ = occ_base + c.occ_off;
     const int64_t nb = np / FW_B;
-    const int64_t i = r0 + (threadIdx.x >> 5);   // one warp per row
+    const int64_t i = r0 + (threadIdx.x >> 5);   // one warp per row (warp-uniform)
+    const int lane_id = threadIdx.x & 31;
     if (i < n) {
         const U *wrow = work + i * np;
         const unsigned char *orow = occ + (i / FW_B) * nb;
+        const bool stats = rs.row_count != nullptr;
+        unsigned long long *mrow = nullptr;
+        if (stats && rs.chunk_mask)
+            mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[c.status_index] + c.status_index +
+                   i * ((n + 2047) / 2048);
+        int nnz = 0;
+        long long mx = 0;
+        unsigned long long word = 0;
         // four consecutive columns per lane (one 16-byte lane vector, one 64-column block):
         // 128 columns per warp and step
         constexpr int PER = 16 / sizeof(U);
-        for (int64_t j0 = (int64_t)(threadIdx.x & 31) * 4; j0 < n; j0 += 128) {
+        for (int64_t b = 0; b < n; b += 128) {
+            const int64_t j0 = b + lane_id * 4;
             T v[4];
             U w[4];
-            const bool occupied = orow[j0 / FW_B] != 0;
+            const bool occupied = j0 < n && orow[j0 / FW_B] != 0;
             if (occupied) {
 #pragma unroll
                 for (int k = 0; k < 4; k += PER)
@@ -601,6 +629,37 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 if (j0 + k < n) out[i * c.ld_out + j0 + k] = v[k];
+            if (stats) {
+                int here = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    here += v[k] != (T)0;
+                    mx = max(mx, (long long)v[k]);
+                }
+                nnz += here;
+                // chunk 4s + q (s = b / 128) is columns held by lanes 8q .. 8q + 7
+                const unsigned bal = __ballot_sync(0xffffffffu, here != 0);
+                unsigned q4 = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if ((bal >> (8 * q)) & 0xffu) q4 |= 1u << q;
+                const int64_t s = b >> 7;
+                word |= (unsigned long long)q4 << (4 * (s & 15));
+                if ((s & 15) == 15 || b + 128 >= n) {
+                    if (mrow && lane_id == 0) mrow[s >> 4] = word;
+                    word = 0;
+                }
+            }
+        }
+        if (stats) {
+            nnz = __reduce_add_sync(0xffffffffu, nnz);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane_id == 0) {
+                const int64_t at = rs.row_base[c.status_index] + i;
+                rs.row_count[rs.row_id ? (int64_t)rs.row_id[at] : at] = nnz;
+                if (rs.comp_max && mx > 0) atomicMax(rs.comp_max + c.status_index, (int)mx);
+            }
         }
     }
 }
@@ -894,7 +953,7 @@ static int upload_plan(const FwPlan &P, unsigned char *ws, cudaStream_t stream) 
 template <typename T, typename U>
 static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws, cudaStream_t stream,
                           bool stop_after_convert, DevStatus *h_status, const unsigned char *shapes = nullptr,
-                          cudaEvent_t *round_events = nullptr) {
+                          cudaEvent_t *round_events = nullptr, const RowStats &rs = RowStats()) {
     typedef TileCfg<U> C;
     static const int configured = configure_kernels<U>();   // once, thread-safe initialisation
     if (configured) return configured;
@@ -982,7 +1041,7 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     {
         cudaEvent_t tf = timer_begin(3, stream);
         fw_finalize_kernel<T, U><<<(unsigned)P.pre_conv[cnt], FW_THREADS, 0, stream>>>(
-            in, lanes, out, comps, pconv, cnt, st, occ);
+            in, lanes, out, comps, pconv, cnt, st, occ, rs);
         timer_end(3, tf, stream);
     }
     RBG_CUDA_TRY(cudaGetLastError());
@@ -1137,9 +1196,11 @@ struct GraphKey {
     void *ws;
     std::vector<int64_t> sizes, offsets;
     std::vector<unsigned char> shapes;
+    RowStats rs;
     bool operator==(const GraphKey &o) const {
         return tbytes == o.tbytes && ubytes == o.ubytes && triangular == o.triangular && in == o.in &&
-               out == o.out && ws == o.ws && sizes == o.sizes && offsets == o.offsets && shapes == o.shapes;
+               out == o.out && ws == o.ws && sizes == o.sizes && offsets == o.offsets && shapes == o.shapes &&
+               rs == o.rs;
     }
 };
 struct GraphEntry {
@@ -1166,12 +1227,12 @@ static long long blocked_launches(const FwPlan &P) {
 template <typename T, typename U>
 static int launch_blocked_graph(const FwPlan &P, int64_t count, const int64_t *sizes, const int64_t *offsets,
                                 const T *in, T *out, unsigned char *ws, cudaStream_t stream, int triangular,
-                                const std::vector<unsigned char> &shapes) {
+                                const std::vector<unsigned char> &shapes, const RowStats &rs) {
     if (g_timer.on)   // timed per kernel: launched directly
-        return launch_blocked<T, U>(P, in, out, ws, stream, false, nullptr, shapes.data());
+        return launch_blocked<T, U>(P, in, out, ws, stream, false, nullptr, shapes.data(), nullptr, rs);
     GraphKey key{(int)sizeof(T), (int)sizeof(U), triangular, in, out, ws,
                  std::vector<int64_t>(sizes, sizes + count), std::vector<int64_t>(offsets, offsets + count),
-                 shapes};
+                 shapes, rs};
     {
         std::lock_guard<std::mutex> lk(g_graph_mu);
         for (auto &e : g_graphs) {
@@ -1189,7 +1250,7 @@ static int launch_blocked_graph(const FwPlan &P, int64_t count, const int64_t *s
     if (!cap) RBG_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     RBG_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
     t_recording = 1;
-    const int rc = launch_blocked<T, U>(P, in, out, ws, cap, false, nullptr, shapes.data());
+    const int rc = launch_blocked<T, U>(P, in, out, ws, cap, false, nullptr, shapes.data(), nullptr, rs);
     t_recording = 0;
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cap, &graph);
@@ -1246,7 +1307,7 @@ static bool tune_lookup(int tbytes, int triangular, const std::vector<int> &acti
 
 template <typename T>
 static int tune_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws, cudaStream_t stream, int triangular,
-                        std::vector<unsigned char> &shapes) {
+                        std::vector<unsigned char> &shapes, const RowStats &rs) {
     const size_t R = P.active.size();
     std::vector<cudaEvent_t> ev(4 * R, nullptr);
     for (auto &e : ev) RBG_CUDA_TRY(cudaEventCreate(&e));
@@ -1254,7 +1315,8 @@ static int tune_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws,
     int rc = RBG_OK;
     for (int shape = 0; shape < 2 && rc == RBG_OK; ++shape) {
         std::vector<unsigned char> all(R, (unsigned char)shape);
-        rc = launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, all.data(), ev.data() + 2 * R * shape);
+        rc = launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, all.data(), ev.data() + 2 * R * shape,
+                                         rs);
     }
     if (rc == RBG_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = RBG_ERR_CUDA;
     if (rc == RBG_OK) {
@@ -1274,7 +1336,8 @@ static int tune_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws,
 
 template <typename T>
 static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offsets, const T *in, T *out,
-                      uint32_t mode, unsigned char *ws, rbg_result_t *results, cudaStream_t stream) {
+                      uint32_t mode, unsigned char *ws, rbg_result_t *results, cudaStream_t stream,
+                      const RowStats &rs = RowStats()) {
     const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
     for (int64_t i = 0; i < count; ++i) {
         memset(&results[i], 0, sizeof(rbg_result_t));
@@ -1290,15 +1353,16 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
         bool done = false;
         if ((mode & RBG_MODE_AUTOTUNE) && !tune_lookup((int)sizeof(T), triangular, P.active, shapes) &&
             (const void *)in != (const void *)out) {
-            rc = tune_blocked<T>(P, in, out, ws, stream, triangular, shapes);
+            rc = tune_blocked<T>(P, in, out, ws, stream, triangular, shapes, rs);
             if (rc) return rc;
             done = true;
         }
         if (!done)
             rc = (mode & RBG_MODE_GRAPH)
                      ? launch_blocked_graph<T, uint32_t>(P, count, sizes, offsets, in, out, ws, stream, triangular,
-                                                         shapes)
-                     : launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, shapes.data());
+                                                         shapes, rs)
+                     : launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, shapes.data(), nullptr,
+                                                   rs);
         if (rc) return rc;
         std::vector<DevStatus> h((size_t)count);
         rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), h.data(), (int)count, stream);
@@ -1461,9 +1525,9 @@ extern "C" int32_t rbg_fw_batch_workspace_bytes(int32_t dtype, int64_t count, co
     return RBG_OK;
 }
 
-extern "C" int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
-                                const void *in, void *out, uint32_t mode, void *workspace,
-                                int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream) {
+static int32_t fw_batch_entry(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                              const void *in, void *out, uint32_t mode, void *workspace, int64_t workspace_bytes,
+                              rbg_result_t *results, rbg_stream_t stream, const RowStats &rs) {
     if (count < 0 || (count > 0 && (!sizes || !offsets || !in || !out || !workspace || !results)))
         return RBG_ERR_INVALID;
     if (dtype_bytes(dtype) == 0) return RBG_ERR_INVALID;
@@ -1477,6 +1541,28 @@ extern "C" int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *siz
     int rc = RBG_ERR_INVALID;
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_batch_t<T>(count, sizes, offsets, reinterpret_cast<const T *>(in), reinterpret_cast<T *>(out),
-                           mode, ws, results, s));
+                           mode, ws, results, s, rs));
     return rc;
+}
+
+extern "C" int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                                const void *in, void *out, uint32_t mode, void *workspace,
+                                int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream) {
+    return fw_batch_entry(dtype, count, sizes, offsets, in, out, mode, workspace, workspace_bytes, results, stream,
+                          RowStats());
+}
+
+extern "C" int32_t rbg_fw_batch_rows(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
+                                     const void *in, void *out, uint32_t mode, void *workspace,
+                                     int64_t workspace_bytes, const rbg_row_stats_t *stats, rbg_result_t *results,
+                                     rbg_stream_t stream) {
+    if (!stats || !stats->row_base || !stats->row_count || dtype != RBG_DTYPE_INT32) return RBG_ERR_INVALID;
+    RowStats rs;
+    rs.row_base = stats->row_base;
+    rs.row_id = stats->row_id;
+    rs.row_count = stats->row_count;
+    rs.chunk_mask = reinterpret_cast<unsigned long long *>(stats->chunk_mask);
+    rs.comp_max = stats->comp_max;
+    return fw_batch_entry(dtype, count, sizes, offsets, in, out, mode, workspace, workspace_bytes, results, stream,
+                          rs);
 }

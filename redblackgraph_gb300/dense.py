@@ -92,12 +92,15 @@ def warshall_host(A: np.ndarray, mode: int = 0) -> tuple[np.ndarray, int, _lib.R
 
 
 def fw_batch(buf: torch.Tensor, sizes, offsets, out: torch.Tensor | None = None, mode: int = 0,
-             stream: torch.cuda.Stream | None = None, as_array: bool = False) -> tuple[torch.Tensor, list]:
+             stream: torch.cuda.Stream | None = None, as_array: bool = False,
+             row_stats: "_lib.RbgRowStats | None" = None) -> tuple[torch.Tensor, list]:
     """Close many matrices packed in one flat device tensor ``buf``.
 
     Matrix i is ``sizes[i] x sizes[i]`` at element offset ``offsets[i]``.  Returns
     ``(out, results)`` with one ``RbgResult`` per matrix, or with ``as_array`` a numpy
     structured array of ``_lib.RESULT_DTYPE`` records (no per-matrix Python objects).
+    With ``row_stats`` (int32 only) the finalization also records the per-row statistics of
+    ``rbg_fw_batch_rows`` for every matrix closed by the 32-bit blocked pass.
     """
     import numpy as np
     if not buf.is_cuda or buf.ndim != 1:
@@ -118,9 +121,14 @@ def fw_batch(buf: torch.Tensor, sizes, offsets, out: torch.Tensor | None = None,
                                               ctypes.byref(nbytes)), "fw_batch")
     ws = default_workspace().get(nbytes.value, buf.device)
     results = (_lib.RbgResult * max(count, 1))()
-    rc = L.rbg_fw_batch(code, count, sizes.ctypes.data, offsets.ctypes.data, buf.data_ptr(),
-                        out.data_ptr(), mode, ws.data_ptr(), ws.numel(), results,
-                        stream_handle(stream))
+    if row_stats is not None:
+        rc = L.rbg_fw_batch_rows(code, count, sizes.ctypes.data, offsets.ctypes.data, buf.data_ptr(),
+                                 out.data_ptr(), mode, ws.data_ptr(), ws.numel(), ctypes.byref(row_stats),
+                                 results, stream_handle(stream))
+    else:
+        rc = L.rbg_fw_batch(code, count, sizes.ctypes.data, offsets.ctypes.data, buf.data_ptr(),
+                            out.data_ptr(), mode, ws.data_ptr(), ws.numel(), results,
+                            stream_handle(stream))
     _lib.check(rc, "fw_batch")
     if as_array:
         return out, np.frombuffer(results, dtype=_lib.RESULT_DTYPE, count=count).copy()

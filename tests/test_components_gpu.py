@@ -139,3 +139,73 @@ def test_golden_adaptive_and_component_labels(native, golden):
         E = sp.csr_matrix((arrays[k + "_W_data"], arrays[k + "_W_indices"], arrays[k + "_W_indptr"]), shape=(n, n))
         assert _same(r.W, E), rec["name"]
         assert r.diameter == rec["diameter"], rec["name"]
+
+
+def test_recorded_row_statistics_equal_the_counting_pass(native):
+    """rbg_fw_batch_rows records, while it finalises, the row counts, chunk masks and component
+    maxima that rbg_cc_compact_count would read back from the closed blocks."""
+    import ctypes
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.components import label_components, densify, compact, chunk_mask_buffer
+    from redblackgraph_gb300.dense import fw_batch
+    from redblackgraph_gb300.device import to_device
+    sizes = synth.component_sizes(30, 4, 2300, seed=11)      # rows past 2048 columns: two mask words
+    M = _shuffled_forest(sizes, seed=13)
+    n = M.shape[0]
+    ip, ix, dv = (to_device(M.indptr.astype(np.int64)), to_device(M.indices.astype(np.int32)),
+                  to_device(M.data.astype(np.int32)))
+    comps = label_components(ip, ix, n)
+    blocks = densify(ip, ix, dv, comps)
+    ref = blocks.flat.clone()
+    row_count = torch.full((n,), -7, dtype=torch.int64, device="cuda")
+    mask = chunk_mask_buffer(comps, blocks)
+    cmax = torch.zeros(comps.count, dtype=torch.int32, device="cuda")
+    stats = _lib.RbgRowStats(comps.start.data_ptr(), comps.sorted_vertex.data_ptr(), row_count.data_ptr(),
+                             mask.data_ptr(), cmax.data_ptr())
+    mode = _lib.MODE_CYTHON | _lib.MODE_GRAPH
+    _, res = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat, mode=mode, as_array=True,
+                      row_stats=stats)
+    assert (res["status"] == 0).all() and (res["path"] == _lib.PATH_BLOCKED32).all()
+    _, res2 = fw_batch(ref, blocks.sizes, blocks.offsets, out=ref, mode=mode, as_array=True)
+    assert torch.equal(ref, blocks.flat)
+    # the counting pass over the same closed blocks
+    oi, oj, ov, cm = compact(comps, blocks, want_max=True)
+    cnt = np.diff(oi.cpu().numpy())
+    assert (row_count.cpu().numpy() == cnt).all()
+    assert (cmax.cpu().numpy() == cm[:comps.count].cpu().numpy()).all()
+    # the merged matrix from the recorded statistics is the same matrix
+    oi2, oj2, ov2, _ = compact(comps, blocks, counted=(row_count, mask, cmax))
+    assert torch.equal(oi, oi2) and torch.equal(oj, oj2) and torch.equal(ov, ov2)
+    # the recorded rows after a second call are replayed from the CUDA graph: same counts
+    row_count.fill_(-7)
+    fw_batch(ref, blocks.sizes, blocks.offsets, out=ref, mode=mode, as_array=True, row_stats=stats)
+    assert (row_count.cpu().numpy() == cnt).all()
+    # the call refuses what it cannot record
+    bad = _lib.RbgRowStats(comps.start.data_ptr(), None, None, None, None)
+    with pytest.raises(Exception):
+        fw_batch(ref, blocks.sizes, blocks.offsets, out=ref, mode=mode, row_stats=bad)
+    del ctypes
+
+
+def test_component_on_another_path_is_counted_again(native):
+    """A component whose products leave the 32-bit lanes is closed on the exact path and has no
+    recorded statistics: the merge counts every row again and the result equals the oracle's."""
+    from redblackgraph_gb300.sparse import component_wise_closure
+    sizes = [60, 5, 200]
+    M = _shuffled_forest(sizes, seed=17).tolil()
+    # a chain of three vertices whose values overflow 32 bits when composed (Cython semantics wrap)
+    n0 = M.shape[0]
+    M.resize((n0 + 3, n0 + 3))
+    M[n0, n0] = -1
+    M[n0 + 1, n0 + 1] = 1
+    M[n0 + 2, n0 + 2] = -1
+    M[n0, n0 + 1] = 1 << 20
+    M[n0 + 1, n0 + 2] = 1 << 20
+    M = sp.csr_matrix(M, dtype=np.int32)
+    M.sort_indices()
+    r = component_wise_closure(M)
+    W, d, err = O.component_wise_closure(M)
+    assert err is None
+    assert _same(r.W, W)
+    assert r.diameter == d
