@@ -246,11 +246,12 @@ def profile_kernels(fn):
     L = _lib.load()
     L.rbg_profile_begin()
     fn()
-    ms = (ctypes.c_double * 4)()
-    n = (ctypes.c_int64 * 4)()
-    _lib.check(L.rbg_profile_end(ms, n), "profile")
-    names = ["fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel", "convert/finalize"]
-    return {names[k]: (ms[k], int(n[k])) for k in range(4)}
+    ms = (ctypes.c_double * 8)()
+    n = (ctypes.c_int64 * 8)()
+    _lib.check(L.rbg_profile_end_slots(ms, n, 8), "profile")
+    names = ["fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel", "convert/finalize",
+             "tri_scan_kernel", "dag_closure", "tri_stats_kernel", "tri_write_kernel"]
+    return {names[k]: (ms[k], int(n[k])) for k in range(8)}
 
 
 def run_ours(args, rank, world, w):

@@ -75,11 +75,15 @@ typedef void *rbg_stream_t; /* a cudaStream_t */
 #define RBG_MODE_AUTOTUNE 64u   /* rbg_fw_batch: per-round tile shape chosen by timing both
                                    shapes on the first call for a batch layout (the first
                                    call closes the batch twice; not when in == out)      */
+#define RBG_MODE_NO_DAG 128u    /* rbg_fw_batch: no DAG path; every matrix takes the blocked
+                                   (or exact) kernels                                     */
 
 /* which kernel path produced a result */
 #define RBG_PATH_BLOCKED32 1
 #define RBG_PATH_BLOCKED64 2
 #define RBG_PATH_EXACT 3
+#define RBG_PATH_DAG 4   /* rbg_fw_batch: int32 matrix whose off-diagonal entries all lie on
+                            one side of the diagonal, closed by the DAG closure by levels   */
 
 typedef struct rbg_result {
     int32_t status;   /* RBG_OK or RBG_ERR_*                                         */
@@ -105,6 +109,10 @@ int32_t rbg_profile_begin(void);
 /* Stop timing; ms[k] and launches[k] (k = 0 tile, 1 panel, 2 diagonal, 3 convert/finalize)
  * receive the summed kernel time and launch count since rbg_profile_begin. */
 int32_t rbg_profile_end(double *ms, int64_t *launches);
+
+/* rbg_profile_end for the first `slots` (1..8) timer slots: 0-3 as above, then the DAG path of
+ * rbg_fw_batch: 4 scan, 5 closure by levels (with its CSR), 6 statistics, 7 write. */
+int32_t rbg_profile_end_slots(double *ms, int64_t *launches, int32_t slots);
 
 /* Scratch bytes rbg_fw_dense needs for an n x n matrix of `dtype` under `mode`. */
 int32_t rbg_fw_dense_workspace_bytes(int32_t dtype, int64_t n, uint32_t mode, int64_t *bytes);
@@ -161,6 +169,17 @@ int32_t rbg_fw_batch_workspace_bytes(int32_t dtype, int64_t count, const int64_t
 int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const int64_t *offsets,
                      const void *in, void *out, uint32_t mode, void *workspace,
                      int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream);
+/*
+ * DAG path (RBG_DTYPE_INT32, unless RBG_MODE_NO_DAG, RBG_MODE_TRIANGULAR, RBG_MODE_FORCE_EXACT
+ * or RBG_MODE_FORCE_WIDE is given): a matrix whose off-diagonal entries all lie below (or all
+ * above) the diagonal, in the clean regime (off-diagonal values 0 or >= 2, diagonal in
+ * {-1, 0, 1}) and of at most 8192 rows, is closed through the DAG closure by levels: with its
+ * vertices in a topological order the sequential loop's step k only pushes row k into the
+ * rows of k's children (below) or pulls k's parents into the rows that reach k (above), so the
+ * values are the DAG recurrence's and the diameter comes from each cell's first product in
+ * step order.  A product that may reach the top bit sends the matrix to the blocked kernels.
+ * The path allocates its scratch (device memory kept by the library between calls).
+ */
 
 /*
  * Row statistics rbg_fw_batch_rows records while it writes the closed matrices, so that a

@@ -37,8 +37,9 @@ MODE_FORCE_WIDE = 8
 MODE_GRAPH = 16
 MODE_TILE_NARROW = 32
 MODE_AUTOTUNE = 64
+MODE_NO_DAG = 128
 
-PATH_BLOCKED32, PATH_BLOCKED64, PATH_EXACT = 1, 2, 3
+PATH_BLOCKED32, PATH_BLOCKED64, PATH_EXACT, PATH_DAG = 1, 2, 3, 4
 
 NOALLOC_MAX_N = 1024   # include/rbg_gb300.h RBG_NOALLOC_MAX_N
 
@@ -99,6 +100,7 @@ SIGNATURES = [
     ("rbg_launch_count", _I64, []),
     ("rbg_profile_begin", _I32, []),
     ("rbg_profile_end", _I32, [_P, _P]),
+    ("rbg_profile_end_slots", _I32, [_P, _P, _I32]),
     ("rbg_fw_dense_workspace_bytes", _I32, [_I32, _I64, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_dense", _I32, [_I32, _I64, _P, _I64, _P, _I64, _U32, _P, _I64,
                             ctypes.POINTER(RbgResult), _P]),

@@ -167,7 +167,8 @@ def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: 
         ctypes.memmove(ctypes.addressof(r), res[bad[0]:bad[0] + 1].tobytes(), ctypes.sizeof(r))
         raise_for_cython(r)
     # components closed on another path have no recorded statistics: count every row again
-    counted = (row_count, mask, cmax) if bool((res["path"] == _lib.PATH_BLOCKED32).all()) else None
+    recorded = (res["path"] == _lib.PATH_BLOCKED32) | (res["path"] == _lib.PATH_DAG)
+    counted = (row_count, mask, cmax) if bool(recorded.all()) else None
     oi, oj, ov, cmax = compact(comps, blocks, want_max=not bool(fw.all()), stream=stream, counted=counted)
     diameter = 0
     if fw.any():

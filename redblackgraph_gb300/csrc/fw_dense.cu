@@ -38,6 +38,7 @@
 #include <vector>
 #include <atomic>
 #include <mutex>
+#include <type_traits>
 #include "rbg_internal.cuh"
 
 namespace rbg {
@@ -72,7 +73,7 @@ void note_launches(int64_t k) {
 // the blocked kernels (0 = tile, 1 = panel, 2 = diagonal, 3 = convert + finalize).
 struct KernelTimer {
     bool on = false;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[4];
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[TIMER_SLOTS];
     std::vector<cudaEvent_t> pool;
     cudaEvent_t get() {
         if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
@@ -83,19 +84,20 @@ struct KernelTimer {
 };
 static KernelTimer g_timer;
 
-static cudaEvent_t timer_begin(int kid, cudaStream_t s) {
+cudaEvent_t timer_begin(int kid, cudaStream_t s) {
     (void)kid;
     if (!g_timer.on) return nullptr;
     cudaEvent_t e = g_timer.get();
     cudaEventRecord(e, s);
     return e;
 }
-static void timer_end(int kid, cudaEvent_t start, cudaStream_t s) {
+void timer_end(int kid, cudaEvent_t start, cudaStream_t s) {
     if (!g_timer.on || !start) return;
     cudaEvent_t e = g_timer.get();
     cudaEventRecord(e, s);
     g_timer.pending[kid].push_back({start, e});
 }
+bool timer_on() { return g_timer.on; }
 
 int grid_for(int64_t work, int threads) {
     static const int sms = [] {
@@ -156,24 +158,7 @@ struct FwComp {
     int64_t rb_index;         // round-buffer index
     int64_t occ_off;          // byte offset of the (np/64)^2 block-occupancy map (1 = nonzero)
     int32_t triangular, status_index;
-};
-
-// Row statistics the finalization can record while it writes the result (rbg_fw_batch_rows,
-// storage int32): the nonzero count of every output row, which 32-column chunks of it hold a
-// nonzero, and each component's largest value.  Component c's row i is output row
-// row_id[row_base[c] + i] (row_base[c] + i when row_id is null); the chunk masks follow the
-// layout of the compaction (ceil(n / 2048) words per row, component c's rows from word
-// ceil(in_off / 2048) + row_base[c] + c).  row_count null: nothing is recorded.
-struct RowStats {
-    const int64_t *row_base = nullptr;
-    const int32_t *row_id = nullptr;
-    int64_t *row_count = nullptr;
-    unsigned long long *chunk_mask = nullptr;
-    int32_t *comp_max = nullptr;
-    bool operator==(const RowStats &o) const {
-        return row_base == o.row_base && row_id == o.row_id && row_count == o.row_count &&
-               chunk_mask == o.chunk_mask && comp_max == o.comp_max;
-    }
+    int32_t orig, pad_;       // index in the caller's batch (row statistics)
 };
 
 __device__ __forceinline__ int fw_find(const int64_t *__restrict__ prefix, int count, int64_t cta) {
@@ -600,7 +585,7 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
         const bool stats = rs.row_count != nullptr;
         unsigned long long *mrow = nullptr;
         if (stats && rs.chunk_mask)
-            mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[c.status_index] + c.status_index +
+            mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[c.orig] + c.orig +
                    i * ((n + 2047) / 2048);
         int nnz = 0;
         long long mx = 0;
@@ -656,9 +641,9 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             if (lane_id == 0) {
-                const int64_t at = rs.row_base[c.status_index] + i;
+                const int64_t at = rs.row_base[c.orig] + i;
                 rs.row_count[rs.row_id ? (int64_t)rs.row_id[at] : at] = nnz;
-                if (rs.comp_max && mx > 0) atomicMax(rs.comp_max + c.status_index, (int)mx);
+                if (rs.comp_max && mx > 0) atomicMax(rs.comp_max + c.orig, (int)mx);
             }
         }
     }
@@ -845,7 +830,7 @@ struct FwPlan {
 // sizes[i], in_off[i], out_off[i] of component i (input order); lane = bytes per lane word
 static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int64_t *in_off,
                        const int64_t *out_off, size_t lane, int triangular, int tile_bn,
-                       int elem_bytes, int tile_bn_narrow = 64) {
+                       int elem_bytes, int tile_bn_narrow = 64, const int64_t *orig = nullptr) {
     P.count = (int)count;
     std::vector<int> order((size_t)count);
     for (int64_t i = 0; i < count; ++i) order[(size_t)i] = (int)i;
@@ -873,6 +858,7 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
         c.occ_off = occs; occs += (c.np / FW_B) * (c.np / FW_B);
         c.triangular = triangular;
         c.status_index = i;
+        c.orig = orig ? (int32_t)orig[i] : i;
         P.pre_conv[(size_t)k + 1] = P.pre_conv[(size_t)k] + (c.np + CONV_ROWS - 1) / CONV_ROWS;
         const bool big = c.n > FW_B;   // n <= 64: the diagonal tile is the whole matrix
         P.pre_panel[(size_t)k + 1] = P.pre_panel[(size_t)k] + (big ? 2 * (c.np / PN_LINES) : 0);
@@ -1343,10 +1329,34 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
         memset(&results[i], 0, sizeof(rbg_result_t));
         results[i].k = results[i].i = results[i].j = -1;
     }
-    std::vector<char> redo((size_t)count, 1);
+    // matrices numbered in a topological order take the DAG path; the rest form a sub-batch
+    std::vector<char> closed((size_t)count, 0);
+    if (std::is_same<T, int32_t>::value &&
+        !(mode & (RBG_MODE_NO_DAG | RBG_MODE_TRIANGULAR | RBG_MODE_FORCE_EXACT | RBG_MODE_FORCE_WIDE))) {
+        const int rc = tri_batch(count, sizes, offsets, reinterpret_cast<const int32_t *>(in),
+                                 reinterpret_cast<int32_t *>(out), results, closed.data(), stream, rs);
+        if (rc) return rc;
+    }
+    std::vector<int64_t> idx;
+    for (int64_t i = 0; i < count; ++i)
+        if (!closed[(size_t)i]) idx.push_back(i);
+    if (idx.empty()) return RBG_OK;
+    const bool whole = (int64_t)idx.size() == count;
+    std::vector<int64_t> sub_sizes, sub_offsets;
+    if (!whole) {
+        for (int64_t i : idx) {
+            sub_sizes.push_back(sizes[i]);
+            sub_offsets.push_back(offsets[i]);
+        }
+    }
+    const int64_t cnt = (int64_t)idx.size();
+    const int64_t *sz = whole ? sizes : sub_sizes.data();
+    const int64_t *of = whole ? offsets : sub_offsets.data();
+    std::vector<char> redo((size_t)cnt, 1);
     if (!(mode & (RBG_MODE_FORCE_EXACT | RBG_MODE_FORCE_WIDE))) {
         FwPlan P;
-        build_plan(P, count, sizes, offsets, offsets, 4, triangular, TileCfg<uint32_t>::BN, (int)sizeof(T));
+        build_plan(P, cnt, sz, of, of, 4, triangular, TileCfg<uint32_t>::BN, (int)sizeof(T), 64,
+                   whole ? nullptr : idx.data());
         int rc = upload_plan(P, ws, stream);
         if (rc) return rc;
         std::vector<unsigned char> shapes(P.active.size(), (mode & RBG_MODE_TILE_NARROW) ? 1 : 0);
@@ -1359,23 +1369,23 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
         }
         if (!done)
             rc = (mode & RBG_MODE_GRAPH)
-                     ? launch_blocked_graph<T, uint32_t>(P, count, sizes, offsets, in, out, ws, stream, triangular,
-                                                         shapes, rs)
+                     ? launch_blocked_graph<T, uint32_t>(P, cnt, sz, of, in, out, ws, stream, triangular, shapes, rs)
                      : launch_blocked<T, uint32_t>(P, in, out, ws, stream, false, nullptr, shapes.data(), nullptr,
                                                    rs);
         if (rc) return rc;
-        std::vector<DevStatus> h((size_t)count);
-        rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), h.data(), (int)count, stream);
+        std::vector<DevStatus> h((size_t)cnt);
+        rc = read_status(reinterpret_cast<DevStatus *>(ws + P.off_status), h.data(), (int)cnt, stream);
         if (rc) return rc;
-        for (int64_t i = 0; i < count; ++i) {
-            if (!(h[(size_t)i].flags & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_WIDE | RBG_EV_RISK))) {
-                result_from_blocked(h[(size_t)i], RBG_PATH_BLOCKED32, &results[i]);
-                redo[(size_t)i] = 0;
+        for (int64_t k = 0; k < cnt; ++k) {
+            if (!(h[(size_t)k].flags & (RBG_EV_UNCLEAN | RBG_EV_CYCLE | RBG_EV_WIDE | RBG_EV_RISK))) {
+                result_from_blocked(h[(size_t)k], RBG_PATH_BLOCKED32, &results[idx[(size_t)k]]);
+                redo[(size_t)k] = 0;
             }
         }
     }
-    for (int64_t i = 0; i < count; ++i) {
-        if (!redo[(size_t)i] || sizes[i] == 0) continue;
+    for (int64_t k = 0; k < cnt; ++k) {
+        const int64_t i = idx[(size_t)k];
+        if (!redo[(size_t)k] || sizes[i] == 0) continue;
         int rc = fw_dense_t<T>(sizes[i], in + offsets[i], sizes[i], out + offsets[i], sizes[i], mode, ws,
                                &results[i], stream);
         if (rc) return rc;
@@ -1401,9 +1411,17 @@ extern "C" int32_t rbg_profile_begin(void) {
 }
 
 extern "C" int32_t rbg_profile_end(double *ms, int64_t *launches) {
-    if (!ms || !launches) return RBG_ERR_INVALID;
+    return rbg_profile_end_slots(ms, launches, 4);
+}
+
+extern "C" int32_t rbg_profile_end_slots(double *ms, int64_t *launches, int32_t slots) {
+    if (!ms || !launches || slots < 1 || slots > TIMER_SLOTS) return RBG_ERR_INVALID;
     g_timer.on = false;
-    for (int k = 0; k < 4; ++k) {
+    for (int k = slots; k < TIMER_SLOTS; ++k) {   // slots not asked for are dropped
+        for (auto &pr : g_timer.pending[k]) { g_timer.pool.push_back(pr.first); g_timer.pool.push_back(pr.second); }
+        g_timer.pending[k].clear();
+    }
+    for (int k = 0; k < slots; ++k) {
         double tot = 0.0;
         for (auto &pr : g_timer.pending[k]) {
             float t = 0.f;

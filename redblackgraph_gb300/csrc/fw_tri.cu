@@ -1,0 +1,530 @@
+// fw_tri.cu -- dense closure of matrices numbered in a topological order, by the DAG closure.
+//
+// The reference's warshall (redblackgraph/core/src/redblackgraph/warshall.c.in:88-106) runs the
+// sequential loop  for k, i, j: W(i, j) = W(i, j) (+) W(i, k) (x) W(k, j)  over the whole matrix.
+// When every off-diagonal entry lies below the diagonal (an edge i -> k only for k < i, as in a
+// pedigree whose vertices are numbered oldest first), a path from i to k passes only vertices
+// numbered above k, none of which an earlier step has used: before step k, W(i, k) is still the
+// input A(i, k), while row k is already final (every path from k descends through vertices
+// below k).  Step k therefore adds A(i, k) (x) C(k, .) to the rows of k's children, and the
+// closure is the DAG recurrence  C(i, .) = A(i, .) (+) sum over parents k of A(i, k) (x) C(k, .)
+// that rbg_dag_closure computes level by level.  Above the diagonal (edges to higher numbers)
+// it is the mirror image: before step k, W(i, k) = C(i, k) and W(k, j) = A(k, j).
+//
+// In the clean regime (off-diagonal values 0 or >= 2, diagonal in {-1, 0, 1}) products with the
+// diagonal change nothing and a cell only decreases once it holds a value, so the largest value
+// the loop ever writes -- the diameter's source -- is, per cell, its first value: A(i, j), else
+// the product of the first step that reaches the cell.  Below the diagonal that is the smallest
+// parent k of i with j in C(k); above it, the smallest k in C(i) with j a parent of k.  A
+// product whose most significant bit may reach the top bit of the 32-bit value sends the
+// matrix to the blocked kernels (which report the reference's overflow or wrap), as does
+// anything outside the clean regime, a row of more than TRI_CAP entries or n > 8192.
+//
+// Pipeline (one call): scan the dense rows (clean-regime test, which side of the diagonal, up
+// to TRI_CAP off-diagonal entries per row) -> CSR of the candidate matrices with batch-global
+// row numbers -> rbg_dag_closure -> per-row statistics (largest product MSB, largest first-value
+// MSB) -> dense rows of the accepted matrices written from the closure rows.
+#include <cuda_runtime.h>
+#include <cub/cub.cuh>
+#include <string.h>
+#include <algorithm>
+#include <mutex>
+#include <vector>
+#include "rbg_internal.cuh"
+
+namespace rbg {
+namespace {
+
+constexpr int TRI_ROWS = 8;                  // rows per CTA, one warp each
+constexpr int TRI_THREADS = 32 * TRI_ROWS;
+constexpr int TRI_CAP = 16;                  // off-diagonal entries per row the scan keeps
+constexpr int64_t TRI_MAX_N = 8192;          // rows of a matrix on this path (bitmap size)
+constexpr int TRI_BM_WORDS = (int)(TRI_MAX_N / 32);
+constexpr unsigned TF_UNCLEAN = 1u, TF_BELOW = 2u, TF_ABOVE = 4u, TF_WIDE = 8u;
+constexpr int KIND_NONE = 0, KIND_BELOW = 1, KIND_ABOVE = 2;
+constexpr int TRI_TOP = 31;                  // lbits - 1 for 32-bit values
+
+struct TriComp {
+    int64_t n, in_off, out_off, row_base;    // row_base: first batch-global row
+};
+
+__device__ __forceinline__ int tri_find(const int64_t *__restrict__ prefix, int count, int64_t cta) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= cta) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// MSB of an off-diagonal value; a value no clean product yields (zero, or negative after a
+// wrap) counts as reaching the top bit
+__device__ __forceinline__ int tri_msb(int32_t v) { return v > 0 ? msb_u32((uint32_t)v) : 99; }
+
+// One warp per row: clean-regime test, side of the diagonal, the row's off-diagonal entries in
+// column order into its TRI_CAP slots (the count may exceed TRI_CAP: then only flagged).
+__global__ void __launch_bounds__(TRI_THREADS)
+tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comps, const int64_t *__restrict__ pre,
+                int count, int32_t *__restrict__ slot_col, int32_t *__restrict__ slot_val,
+                int32_t *__restrict__ row_cnt, int32_t *__restrict__ row_comp, unsigned *__restrict__ cflags) {
+    const int ci = tri_find(pre, count, blockIdx.x);
+    const TriComp c = comps[ci];
+    const int64_t i = ((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS + (threadIdx.x >> 5);
+    if (i >= c.n) return;                    // warp-uniform
+    const int lane = threadIdx.x & 31;
+    const int32_t *row = in + c.in_off + i * c.n;
+    const int64_t g = c.row_base + i;
+    unsigned flags = 0;
+    int cnt = 0;
+    for (int64_t b = 0; b < c.n; b += 128) {
+        const int64_t j0 = b + lane * 4;
+        int32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = j0 + k < c.n ? row[j0 + k] : 0;
+        int c4 = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t j = j0 + k;
+            if (j == i) {
+                if (!(v[k] == 0 || v[k] == 1 || v[k] == -1)) flags |= TF_UNCLEAN;
+                v[k] = 0;                    // the diagonal is not an edge
+            } else if (v[k] != 0) {
+                if (v[k] == 1 || v[k] < 0) flags |= TF_UNCLEAN;
+                flags |= j < i ? TF_BELOW : TF_ABOVE;
+                ++c4;
+            }
+        }
+        if (!__any_sync(0xffffffffu, c4 != 0)) continue;
+        int x = c4;                          // inclusive prefix over the lanes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        int pos = cnt + x - c4;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (v[k] != 0) {
+                if (pos < TRI_CAP) {
+                    slot_col[g * TRI_CAP + pos] = (int32_t)(j0 + k);
+                    slot_val[g * TRI_CAP + pos] = v[k];
+                }
+                ++pos;
+            }
+        }
+        cnt += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (cnt > TRI_CAP) flags |= TF_WIDE;
+    flags = __reduce_or_sync(0xffffffffu, flags);
+    if (lane == 0) {
+        row_cnt[g] = cnt;
+        row_comp[g] = ci;
+        if (flags) atomicOr(cflags + ci, flags);
+    }
+}
+
+// entries of each row in the CSR of the candidate matrices (rows of other matrices empty)
+__global__ void tri_count_kernel(int64_t R, const int32_t *__restrict__ row_cnt, const int32_t *__restrict__ row_comp,
+                                 const int32_t *__restrict__ ckind, int64_t *__restrict__ cnt64) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < R; g += (int64_t)gridDim.x * blockDim.x)
+        cnt64[g] = ckind[row_comp[g]] != KIND_NONE ? row_cnt[g] : 0;
+}
+
+__global__ void tri_csr_fill_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                                    const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
+                                    const int32_t *__restrict__ slot_col, const int32_t *__restrict__ slot_val,
+                                    int32_t *__restrict__ a_col, int32_t *__restrict__ a_val) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < R; g += (int64_t)gridDim.x * blockDim.x) {
+        const int ci = row_comp[g];
+        if (ckind[ci] == KIND_NONE) continue;
+        const int32_t base = (int32_t)comps[ci].row_base;
+        const int64_t o = indptr[g];
+        const int m = (int)(indptr[g + 1] - o);
+        for (int p = 0; p < m; ++p) {
+            a_col[o + p] = base + slot_col[g * TRI_CAP + p];
+            a_val[o + p] = slot_val[g * TRI_CAP + p];
+        }
+    }
+}
+
+// One warp per row of a candidate matrix: the largest MSB of every product the sequential loop
+// performs on the row (and, above the diagonal, of the DAG recurrence's own candidates) and the
+// largest MSB of the row's first values.  A per-warp bitmap of the matrix's columns marks the
+// cells that already hold a value.
+__global__ void __launch_bounds__(TRI_THREADS)
+tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                 const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
+                 const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
+                 const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
+                 const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, int *__restrict__ cam,
+                 int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
+    __shared__ unsigned bm_all[TRI_ROWS][TRI_BM_WORDS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned *bm = bm_all[w];
+    const int64_t warps = (int64_t)gridDim.x * TRI_ROWS;
+    for (int64_t g = (int64_t)blockIdx.x * TRI_ROWS + w; g < R; g += warps) {
+        const int ci = row_comp[g];
+        const int kind = ckind[ci];
+        if (kind == KIND_NONE) continue;     // warp-uniform
+        const int32_t base = (int32_t)comps[ci].row_base;
+        const int words = (int)((comps[ci].n + 31) >> 5);
+        for (int q = lane; q < words; q += 32) bm[q] = 0;
+        __syncwarp();
+        const int64_t a0 = indptr[g];
+        const int alen = (int)(indptr[g + 1] - a0);
+        int am = -1, fm = -1;
+        unsigned long long prods = 0;
+        for (int p = lane; p < alen; p += 32) {      // the row's own values are written first
+            const int j = a_col[a0 + p] - base;
+            atomicOr(&bm[j >> 5], 1u << (j & 31));
+            fm = max(fm, tri_msb(a_val[a0 + p]));
+        }
+        __syncwarp();
+        // below: steps k over the parents, ascending, each adding A(i, k) (x) C(k, .).  Above:
+        // the same products are the recurrence's candidates (their MSB bounds the closure values)
+        for (int p = 0; p < alen; ++p) {
+            const int32_t kg = a_col[a0 + p];
+            const int mk = tri_msb(a_val[a0 + p]);
+            const int64_t c0 = row_off[kg];
+            const int clen = row_len[kg];
+            for (int q = lane; q < clen; q += 32) {
+                const int pm = mk + tri_msb(p_val[c0 + q]);
+                am = max(am, pm);
+                if (kind == KIND_BELOW) {
+                    const int j = p_col[c0 + q] - base;
+                    const unsigned bit = 1u << (j & 31);
+                    if (!(bm[j >> 5] & bit)) {
+                        fm = max(fm, pm);
+                        atomicOr(&bm[j >> 5], bit);
+                    }
+                }
+            }
+            if (kind == KIND_BELOW && lane == 0) prods += (unsigned long long)clen;
+            __syncwarp();
+        }
+        if (kind == KIND_ABOVE) {
+            // steps k over C(i), ascending, each adding C(i, k) (x) A(k, .)
+            const int64_t c0 = row_off[g];
+            const int clen = row_len[g];
+            for (int q = 0; q < clen; ++q) {
+                const int32_t kg = p_col[c0 + q];
+                const int mk = tri_msb(p_val[c0 + q]);
+                const int64_t k0 = indptr[kg];
+                const int klen = (int)(indptr[kg + 1] - k0);
+                for (int r = lane; r < klen; r += 32) {
+                    const int j = a_col[k0 + r] - base;
+                    const int pm = mk + tri_msb(a_val[k0 + r]);
+                    am = max(am, pm);
+                    const unsigned bit = 1u << (j & 31);
+                    if (!(bm[j >> 5] & bit)) {
+                        fm = max(fm, pm);
+                        atomicOr(&bm[j >> 5], bit);
+                    }
+                }
+                if (lane == 0) prods += (unsigned long long)klen;
+                __syncwarp();
+            }
+        }
+        am = __reduce_max_sync(0xffffffffu, am);
+        fm = __reduce_max_sync(0xffffffffu, fm);
+        if (lane == 0) {
+            if (am >= 0) atomicMax(cam + ci, am);
+            if (fm >= 0) atomicMax(cfm + ci, fm);
+            if (prods) atomicAdd(cprod + ci, prods);
+        }
+        __syncwarp();                        // the next row clears the bitmap
+    }
+}
+
+// One warp per row of an accepted matrix: the dense row from its closure row (every cell when
+// out != in; in place only the closure's entries, the other cells already hold the result),
+// and the row statistics when asked for.
+__global__ void __launch_bounds__(TRI_THREADS)
+tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
+                 const int64_t *__restrict__ pre, int count, const unsigned char *__restrict__ cfinal,
+                 const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
+                 const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, RowStats rs) {
+    const int ci = tri_find(pre, count, blockIdx.x);
+    if (!cfinal[ci]) return;                 // block-uniform
+    const TriComp c = comps[ci];
+    const int64_t i = ((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS + (threadIdx.x >> 5);
+    if (i >= c.n) return;                    // warp-uniform
+    const int lane = threadIdx.x & 31;
+    const int64_t n = c.n, g = c.row_base + i;
+    const int32_t *rin = in + c.in_off + i * n;
+    int32_t *rout = out + c.out_off + i * n;
+    const int32_t diag = rin[i];
+    if (rin != rout) {
+        for (int64_t b = 0; b < n; b += 128) {
+            const int64_t j0 = b + lane * 4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (j0 + k < n) rout[j0 + k] = j0 + k == i ? diag : 0;
+        }
+        __syncwarp();                        // the zeros land before the closure's values
+    }
+    const int64_t c0 = row_off[g];
+    const int clen = row_len[g];
+    const int32_t base = (int32_t)c.row_base;
+    unsigned long long wd[4] = {0ull, 0ull, 0ull, 0ull};   // chunk masks (n <= 8192: <= 4 words)
+    int mx = 0;
+    for (int q = lane; q < clen; q += 32) {
+        const int j = p_col[c0 + q] - base;
+        const int32_t v = p_val[c0 + q];
+        rout[j] = v;
+        mx = max(mx, v);
+        const int chunk = j >> 5;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if ((chunk >> 6) == t) wd[t] |= 1ull << (chunk & 63);
+    }
+    if (rs.row_count) {
+        if (lane == 0 && diag != 0) {
+            const int chunk = (int)(i >> 5);
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if ((chunk >> 6) == t) wd[t] |= 1ull << (chunk & 63);
+            mx = max(mx, diag);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)wd[t]);
+            const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(wd[t] >> 32));
+            wd[t] = ((unsigned long long)hi << 32) | lo;
+        }
+        mx = __reduce_max_sync(0xffffffffu, mx);
+        if (lane == 0) {
+            const int64_t at = rs.row_base[ci] + i;
+            rs.row_count[rs.row_id ? (int64_t)rs.row_id[at] : at] = clen + (diag != 0 ? 1 : 0);
+            if (rs.chunk_mask) {
+                const int64_t words = (n + 2047) / 2048;
+                unsigned long long *mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[ci] + ci + i * words;
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (t < words) mrow[t] = wd[t];
+            }
+            if (rs.comp_max && mx > 0) atomicMax(rs.comp_max + ci, mx);
+        }
+    }
+}
+
+// Device scratch kept between calls (grown when a batch needs more; one call at a time).
+struct TriScratch {
+    unsigned char *p = nullptr;
+    size_t cap = 0;
+};
+std::mutex g_tri_mu;
+TriScratch g_tri_a, g_tri_b;
+
+int tri_reserve(TriScratch &s, size_t bytes, cudaStream_t st) {
+    if (bytes <= s.cap) return RBG_OK;
+    RBG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (s.p) cudaFree(s.p);
+    s.p = nullptr;
+    s.cap = 0;
+    const size_t want = bytes + bytes / 4;
+    RBG_CUDA_TRY(cudaMalloc(reinterpret_cast<void **>(&s.p), want));
+    s.cap = want;
+    return RBG_OK;
+}
+
+struct Carve {
+    unsigned char *p;
+    size_t off = 0;
+    template <typename X> X *take(size_t n) {
+        off = align_up(off, 256);
+        X *r = reinterpret_cast<X *>(p + off);
+        off += n * sizeof(X);
+        return r;
+    }
+};
+
+}  // namespace
+
+int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const int32_t *in, int32_t *out,
+              rbg_result_t *results, char *closed, cudaStream_t s, const RowStats &rs) {
+    if (count <= 0 || count > INT32_MAX) return RBG_OK;
+    std::vector<TriComp> hc((size_t)count);
+    std::vector<int64_t> pre((size_t)count + 1, 0);
+    int64_t R = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const int64_t n = (sizes[i] > 0 && sizes[i] <= TRI_MAX_N) ? sizes[i] : 0;
+        hc[(size_t)i] = TriComp{n, offsets[i], offsets[i], R};
+        R += n;
+        pre[(size_t)i + 1] = pre[(size_t)i] + (n + TRI_ROWS - 1) / TRI_ROWS;
+    }
+    if (R == 0 || R > INT32_MAX) return RBG_OK;
+    std::lock_guard<std::mutex> lk(g_tri_mu);
+    size_t scan_tmp = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (int64_t *)nullptr, (int64_t *)nullptr, (int)(R + 1));
+    const size_t C = (size_t)count, NR = (size_t)R;
+    auto layout = [&](Carve &cv, TriComp *&dc, int64_t *&dpre, unsigned *&cflags, int32_t *&ckind,
+                      unsigned char *&cfinal, int *&cam, int *&cfm, unsigned long long *&cprod, int32_t *&row_cnt,
+                      int32_t *&row_comp, int32_t *&slot_col, int32_t *&slot_val, int64_t *&indptr, void *&tmp,
+                      int32_t *&a_col, int32_t *&a_val) {
+        dc = cv.take<TriComp>(C);
+        dpre = cv.take<int64_t>(C + 1);
+        cflags = cv.take<unsigned>(C);
+        ckind = cv.take<int32_t>(C);
+        cfinal = cv.take<unsigned char>(C);
+        cam = cv.take<int>(C);
+        cfm = cv.take<int>(C);
+        cprod = cv.take<unsigned long long>(C);
+        row_cnt = cv.take<int32_t>(NR);
+        row_comp = cv.take<int32_t>(NR);
+        slot_col = cv.take<int32_t>(NR * TRI_CAP);
+        slot_val = cv.take<int32_t>(NR * TRI_CAP);
+        indptr = cv.take<int64_t>(NR + 1);
+        tmp = cv.take<unsigned char>(scan_tmp);
+        a_col = cv.take<int32_t>(NR * TRI_CAP);
+        a_val = cv.take<int32_t>(NR * TRI_CAP);
+    };
+    TriComp *dc;
+    int64_t *dpre, *indptr;
+    unsigned *cflags;
+    int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val;
+    unsigned char *cfinal;
+    int *cam, *cfm;
+    unsigned long long *cprod;
+    void *tmp;
+    {
+        Carve dry{nullptr};
+        layout(dry, dc, dpre, cflags, ckind, cfinal, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr,
+               tmp, a_col, a_val);
+        const int rc = tri_reserve(g_tri_a, dry.off + 256, s);
+        if (rc) return rc;
+    }
+    Carve cv{g_tri_a.p};
+    layout(cv, dc, dpre, cflags, ckind, cfinal, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr, tmp,
+           a_col, a_val);
+    RBG_CUDA_TRY(cudaMemcpyAsync(dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(cflags, 0, C * 4, s));
+
+    // 1. scan
+    {
+        cudaEvent_t t = timer_begin(4, s);
+        note_launches(1);
+        tri_scan_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, dc, dpre, (int)count, slot_col, slot_val,
+                                                                 row_cnt, row_comp, cflags);
+        RBG_CUDA_TRY(cudaGetLastError());
+        timer_end(4, t, s);
+    }
+    std::vector<unsigned> hf(C);
+    RBG_CUDA_TRY(cudaMemcpyAsync(hf.data(), cflags, C * 4, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<int32_t> kind(C, KIND_NONE);
+    int64_t candidates = 0;
+    for (size_t i = 0; i < C; ++i) {
+        const unsigned f = hf[i];
+        if (hc[i].n == 0 || (f & (TF_UNCLEAN | TF_WIDE)) || ((f & TF_BELOW) && (f & TF_ABOVE))) continue;
+        kind[i] = (f & TF_ABOVE) ? KIND_ABOVE : KIND_BELOW;
+        ++candidates;
+    }
+    if (candidates == 0) return RBG_OK;
+    RBG_CUDA_TRY(cudaMemcpyAsync(ckind, kind.data(), C * 4, cudaMemcpyHostToDevice, s));
+
+    // 2. CSR of the candidates and their closure by levels
+    cudaEvent_t tdag = timer_begin(5, s);
+    note_launches(2);
+    tri_count_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, row_cnt, row_comp, ckind, indptr);
+    RBG_CUDA_TRY(cudaMemsetAsync(indptr + R, 0, 8, s));
+    size_t tb = scan_tmp;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, indptr, indptr, (int)(R + 1), s));
+    int64_t nnz_a = 0;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&nnz_a, indptr + R, 8, cudaMemcpyDeviceToHost, s));
+    tri_csr_fill_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, row_comp, ckind, dc, indptr, slot_col, slot_val, a_col,
+                                                        a_val);
+    RBG_CUDA_TRY(cudaGetLastError());
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    rbg_csr_t A{R, R, indptr, a_col, a_val};
+    int64_t dws = 0;
+    int rc = rbg_dag_workspace_bytes(R, nnz_a, &dws);
+    if (rc) return rc;
+    int64_t pool = std::max<int64_t>(16 * nnz_a + R, 1024);
+    int32_t *p_col = nullptr, *p_val = nullptr, *row_len = nullptr;
+    int64_t *row_off = nullptr;
+    int64_t used = 0;
+    for (int attempt = 0;; ++attempt) {
+        Carve dry{nullptr};
+        dry.take<unsigned char>((size_t)dws);
+        dry.take<int32_t>((size_t)pool);
+        dry.take<int32_t>((size_t)pool);
+        dry.take<int64_t>(NR);
+        dry.take<int32_t>(NR);
+        rc = tri_reserve(g_tri_b, dry.off + 256, s);
+        if (rc) return rc;
+        Carve cb{g_tri_b.p};
+        void *dw = cb.take<unsigned char>((size_t)dws);
+        p_col = cb.take<int32_t>((size_t)pool);
+        p_val = cb.take<int32_t>((size_t)pool);
+        row_off = cb.take<int64_t>(NR);
+        row_len = cb.take<int32_t>(NR);
+        int64_t mx = 0, levels = 0;
+        used = 0;
+        rc = rbg_dag_closure(&A, dw, dws, p_col, p_val, pool, row_off, row_len, &used, &mx, &levels,
+                             reinterpret_cast<rbg_stream_t>(s));
+        if (rc == RBG_ERR_CAPACITY && used > pool && attempt < 4) {
+            pool = used;
+            continue;
+        }
+        break;
+    }
+    timer_end(5, tdag, s);
+    if (rc == RBG_ERR_CAPACITY || rc == RBG_ERR_CYCLE) return RBG_OK;   // the blocked kernels decide
+    if (rc) return rc;
+
+    // 3. statistics
+    {
+        cudaEvent_t t = timer_begin(6, s);
+        RBG_CUDA_TRY(cudaMemsetAsync(cam, 0xff, C * 4, s));
+        RBG_CUDA_TRY(cudaMemsetAsync(cfm, 0xff, C * 4, s));
+        RBG_CUDA_TRY(cudaMemsetAsync(cprod, 0, C * 8, s));
+        note_launches(1);
+        tri_stats_kernel<<<grid_for(R * 32, TRI_THREADS), TRI_THREADS, 0, s>>>(
+            R, row_comp, ckind, dc, indptr, a_col, a_val, row_off, row_len, p_col, p_val, cam, cfm, cprod);
+        RBG_CUDA_TRY(cudaGetLastError());
+        timer_end(6, t, s);
+    }
+    std::vector<int> ham(C), hfm(C);
+    std::vector<unsigned long long> hprod(C);
+    RBG_CUDA_TRY(cudaMemcpyAsync(ham.data(), cam, C * 4, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(hfm.data(), cfm, C * 4, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(hprod.data(), cprod, C * 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<unsigned char> fin(C, 0);
+    int64_t accepted = 0;
+    for (size_t i = 0; i < C; ++i) {
+        if (kind[i] == KIND_NONE || ham[i] >= TRI_TOP) continue;
+        fin[i] = 1;
+        ++accepted;
+    }
+    if (accepted == 0) return RBG_OK;
+    RBG_CUDA_TRY(cudaMemcpyAsync(cfinal, fin.data(), C, cudaMemcpyHostToDevice, s));
+
+    // 4. dense rows
+    {
+        cudaEvent_t t = timer_begin(7, s);
+        note_launches(1);
+        tri_write_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, out, dc, dpre, (int)count, cfinal, row_off,
+                                                                  row_len, p_col, p_val, rs);
+        RBG_CUDA_TRY(cudaGetLastError());
+        timer_end(7, t, s);
+    }
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < C; ++i) {
+        if (!fin[i]) continue;
+        closed[i] = 1;
+        rbg_result_t &r = results[i];
+        r.status = RBG_OK;
+        r.flags = 0;
+        r.diameter = hfm[i] > 0 ? hfm[i] : 0;
+        r.k = r.i = r.j = -1;
+        r.path = RBG_PATH_DAG;
+        r.executed = (int64_t)hprod[i];
+    }
+    return RBG_OK;
+}
+
+}  // namespace rbg

@@ -41,6 +41,40 @@ int grid_for(int64_t work, int threads);
 // running count of kernel launches issued by this library (rbg_launch_count)
 void note_launches(int64_t k);
 
+// Benchmark timer (rbg_profile_begin / rbg_profile_end_slots): CUDA events around the kernels
+// of each slot, recorded on the launching stream while the timer is on.  Slots: 0 phase-3
+// tiles, 1 panels, 2 diagonal tiles, 3 convert + finalize, 4 DAG path scan, 5 DAG path
+// closure by levels (with its CSR), 6 DAG path statistics, 7 DAG path write.
+constexpr int TIMER_SLOTS = 8;
+cudaEvent_t timer_begin(int slot, cudaStream_t s);
+void timer_end(int slot, cudaEvent_t start, cudaStream_t s);
+bool timer_on();
+
+// Row statistics the closure can record while it writes the result (rbg_fw_batch_rows,
+// storage int32): the nonzero count of every output row, which 32-column chunks of it hold a
+// nonzero, and each component's largest value.  Component c's row i is output row
+// row_id[row_base[c] + i] (row_base[c] + i when row_id is null); the chunk masks follow the
+// layout of the compaction (ceil(n / 2048) words per row, component c's rows from word
+// ceil(offset_c / 2048) + row_base[c] + c).  row_count null: nothing is recorded.
+struct RowStats {
+    const int64_t *row_base = nullptr;
+    const int32_t *row_id = nullptr;
+    int64_t *row_count = nullptr;
+    unsigned long long *chunk_mask = nullptr;
+    int32_t *comp_max = nullptr;
+    bool operator==(const RowStats &o) const {
+        return row_base == o.row_base && row_id == o.row_id && row_count == o.row_count &&
+               chunk_mask == o.chunk_mask && comp_max == o.comp_max;
+    }
+};
+
+// fw_tri.cu: the components of an int32 batch whose off-diagonal entries all lie on one side of
+// the diagonal (vertices numbered in a topological order) and are in the clean regime, closed
+// through the DAG closure by levels; sets closed[i] and results[i] for each of them and leaves
+// every other component untouched.
+int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const int32_t *in, int32_t *out,
+              rbg_result_t *results, char *closed, cudaStream_t stream, const RowStats &rs);
+
 template <typename T> struct dtype_of;
 template <> struct dtype_of<int8_t> { static const int value = RBG_DTYPE_INT8; };
 template <> struct dtype_of<uint8_t> { static const int value = RBG_DTYPE_UINT8; };

@@ -128,3 +128,79 @@ def test_tile_shapes_and_autotune_match_oracle(native, mode_name):
             Wo, do, so, _ = O.warshall(A)
             assert r.status == so == 0
             assert (h[o:o + n * n].reshape(n, n) == Wo).all() and r.diameter == do
+
+
+def _random_dag(rng, n, density, above=False, vmax=8):
+    """Random DAG numbered in a topological order: entries below the diagonal (or, reversed,
+    above it) with values in [2, vmax), diagonal in {-1, 0, 1}."""
+    A = np.zeros((n, n), np.int64)
+    low = np.tril(rng.random((n, n)) < density, -1)
+    A[low] = rng.integers(2, vmax, size=int(low.sum()))
+    np.fill_diagonal(A, rng.choice([-1, 0, 1], size=n))
+    return A[::-1, ::-1].copy() if above else A
+
+
+@pytest.mark.parametrize("in_place", [False, True])
+def test_dag_path_vs_oracle(native, in_place):
+    """int32 matrices numbered in a topological order (entries all below, or all above, the
+    diagonal) take the DAG path; values, diameters (each cell's first value) and errors equal
+    the oracle's sequential loop, in both semantics."""
+    from redblackgraph_gb300 import synth, _lib
+    rng = np.random.default_rng(7)
+    mats = [_random_dag(rng, int(rng.integers(1, 90)), rng.uniform(0.02, 0.4), above=t % 2 == 1).astype(np.int32)
+            for t in range(60)]
+    mats += [synth.pedigree(n, synth.generations_for(n), n, dtype=np.int32) for n in (300, 700, 1500)]
+    mats += [synth.pedigree(500, 12, 9, dtype=np.int32)[::-1, ::-1].copy()]   # pedigree above the diagonal
+    for mode, oracle in ((0, O.warshall), (_lib.MODE_CYTHON, O.fw_cython)):
+        Ws, res = run_batch(mats, mode=mode, in_place=in_place)
+        dag = 0
+        for A, W, r in zip(mats, Ws, res):
+            Wo, do, so, _ = oracle(A)
+            assert r.status == so
+            if so == 0:
+                assert (W == Wo).all() and r.diameter == do
+            dag += r.path == _lib.PATH_DAG
+        assert dag >= 40                     # deep random DAGs may reach the top bit: blocked path
+
+
+def test_dag_path_mixed_batch_and_opt_out(native):
+    """A batch mixing DAG-path matrices with ones that must take the blocked kernels (entries
+    on both sides, unclean, a cycle, rows of more than 16 entries, values that reach the top
+    bit): every result is the oracle's and lands at its own index; RBG_MODE_NO_DAG gives the
+    same results on the blocked path."""
+    from redblackgraph_gb300 import synth, _lib
+    rng = np.random.default_rng(11)
+    ped = synth.pedigree(200, 9, 3, dtype=np.int64)
+    p = rng.permutation(200)
+    both = ped[p][:, p]                                              # both sides of the diagonal
+    unclean = ped.copy()
+    unclean[150, 3] = -7
+    cyc = synth.pedigree(120, 8, 4, dtype=np.int64)
+    Wc, _, _, _ = O.warshall(cyc)
+    v, u = max(zip(*np.nonzero(np.tril(Wc, -1))), key=lambda t: t[0] - t[1])
+    cyc[u, v] = 2
+    wide = _random_dag(rng, 80, 0.05)
+    wide[70, :40] = rng.integers(2, 4, size=40)                      # a row of 40 parents
+    deep = np.zeros((40, 40), np.int64)
+    np.fill_diagonal(deep, 1)
+    for i in range(1, 40):
+        deep[i, i - 1] = 3                                           # a chain: products past 31 bits
+    mats = [ped, both, _random_dag(rng, 50, 0.1), unclean, cyc, wide, synth.pedigree(64, 6, 8), deep,
+            synth.pedigree(90, 7, 5)[::-1, ::-1]]
+    mats = [m.astype(np.int32) for m in mats]
+    Ws, res = run_batch(mats)
+    for A, W, r in zip(mats, Ws, res):
+        Wo, do, so, _ = O.warshall(A)
+        assert r.status == so
+        if so == 0:
+            assert (W == Wo).all() and r.diameter == do
+    paths = [r.path for r in res]
+    dag, blk = _lib.PATH_DAG, _lib.PATH_BLOCKED32
+    assert [paths[k] for k in (0, 1, 2, 3, 5, 6, 7, 8)] == [dag, blk, dag, _lib.PATH_EXACT, blk, dag,
+                                                           paths[7], dag], paths
+    assert res[4].status == _lib.RBG_ERR_CYCLE and paths[7] != dag
+    Ws2, res2 = run_batch(mats, mode=_lib.MODE_NO_DAG)
+    for W, W2, r, r2 in zip(Ws, Ws2, res, res2):
+        assert r2.status == r.status and r2.path != _lib.PATH_DAG
+        if r.status == 0:
+            assert (W == W2).all() and r.diameter == r2.diameter
