@@ -230,6 +230,17 @@ def int32_peak_ops(device_index: int, sm_max_mhz):
     return sms * 128 * mhz * 1e6, sms
 
 
+def scan_traffic(algorithmic_bytes):
+    """DRAM bytes of one full-size scan launch: the committed ncu capture of a smaller batch,
+    scaled by dense cells (the scan's traffic grows with the cells it reads and writes)."""
+    p = ROOT / "profiles" / "tri_scan_kernel_traffic.txt"
+    try:
+        d = json.loads(p.read_text())
+        return d["dram_bytes_per_launch"] * algorithmic_bytes / d["algorithmic_bytes_per_launch"]
+    except (ValueError, OSError, KeyError, ZeroDivisionError):
+        return None
+
+
 def phase_traffic():
     """DRAM bytes per launch of the phase kernels, from the committed ncu capture summary."""
     p = ROOT / "profiles" / "fw_phase_traffic.txt"
@@ -298,11 +309,36 @@ def run_ours(args, rank, world, w):
     t = e0.elapsed_time(e1) / 1e3
     t = max_over_ranks(t, dev)          # the slowest rank's time (weak scaling)
     clocks = clk.summary()
+    paths = {int(p): int((results["path"] == p).sum()) for p in np.unique(results["path"])}
     res = dict(t=t, work=work_per_step, executed=executed, kprof=kprof, launches=launches,
-               clocks=clocks, out=out, offsets=offsets, bytes=buf.numel() * 4)
+               clocks=clocks, out=out, offsets=offsets, bytes=buf.numel() * 4,
+               cells=float((sizes.astype(np.float64) ** 2).sum()), paths=paths)
+    if args.secondary:
+        res["blocked"] = run_blocked(args, buf, sizes, offsets, out, mode | _lib.MODE_NO_DAG)
     del buf, blocks
     res["e2e"] = run_e2e(args, rank, world, w, dev, work_per_step)
     return res
+
+
+def run_blocked(args, buf, sizes, offsets, out, mode):
+    """The same resident batch on the blocked kernels only (RBG_MODE_NO_DAG): the path every
+    matrix takes when its vertices are not numbered in a topological order."""
+    import torch
+    from redblackgraph_gb300.dense import fw_batch
+    for _ in range(3):
+        _, res = fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True)
+    assert (res["status"] == 0).all()
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / args.steps
+    kp = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True))
+    return dict(t=t, executed=float(res["executed"].sum()), kprof=kp)
 
 
 def run_e2e(args, rank, world, w, dev, work_per_step):
@@ -773,34 +809,54 @@ def main():
             "data": "synthetic: seeded pedigree components generated in-process",
             "config": config(f"inputs larger than L2: {r['bytes'] / 1e9:.1f} GB resident per step", w),
             "gpu_launches": int(r["launches"]), "clocks": r["clocks"]}
-    # roofline of the dominant kernel (phase-3 tile kernel): int32 lane operations
-    # roofline of the closure proper: the three phase kernels of every round (diagonal, panels,
-    # tiles) issue all executed relaxations; int32 lane operations against the nominal peak
+    # roofline of the dominant kernel: on the DAG path (every component here is numbered oldest
+    # first) the scan reads every input cell and writes every output cell's zero or diagonal
     kp = r["kprof"]
-    phase_ms = sum(kp[k][0] for k in ("fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel")) / args.steps
-    peak, sms = int32_peak_ops(0, r["clocks"].get("sm_max_mhz"))
-    tr = phase_traffic()
-    traffic = None
-    if tr:
-        traffic = sum(tr["bytes_per_launch"][k] * kp[k][1] / args.steps for k in tr["bytes_per_launch"] if k in kp)
+    per = {k: v[0] / args.steps for k, v in kp.items()}
+    scan_ms = per["tri_scan_kernel"]
+    hbm = hbm_peak_gbs()
+    scan_bytes = r["cells"] * 4 * 2
+    line["paths"] = {{1: "blocked32", 2: "blocked64", 3: "exact", 4: "dag"}.get(k, str(k)): v
+                     for k, v in r["paths"].items()}
     line["roofline"] = {
-        "bound": "int32_alu", "unit": "Tops/s", "kernel": "fw_diag_kernel + fw_panel_kernel + fw_tile_kernel",
-        "achieved": None, "peak": peak / 1e12, "frac": None,
-        "traffic": traffic, "traffic_unit": "DRAM bytes per step of the three phase kernels "
-                                            "(per-launch bytes from profiles/fw_phase_traffic.txt x launches)",
-        "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock",
-        "ops_per_relaxation": 2,
-        "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kp.items()},
+        "bound": "hbm", "unit": "GB/s", "kernel": "tri_scan_kernel",
+        "achieved": scan_bytes / (scan_ms / 1e3) / 1e9 if scan_ms > 0 else None, "peak": hbm,
+        "frac": scan_bytes / (scan_ms / 1e3) / 1e9 / hbm if scan_ms > 0 else None,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
+        "algorithmic_bytes_per_launch": scan_bytes,
+        "algorithmic_bytes_note": "every input cell read and every output cell written once (4 + 4 bytes "
+                                  "per cell of the sum n^2 dense cells); the slot writes are < 0.1%",
+        "traffic": scan_traffic(scan_bytes),
+        "traffic_unit": "DRAM bytes per launch (ncu capture of a smaller batch scaled by dense cells, "
+                        "profiles/tri_scan_kernel_traffic.txt)",
+        "kernel_ms_per_step": per,
         "kernel_launches_per_step": {k: v[1] / args.steps for k, v in kp.items()},
-        "executed_relaxations_per_step": r["executed"],
+        "step_hbm_gb_s": scan_bytes / (r["t"] / args.steps) / 1e9,
+        "executed_products_per_step": r["executed"],
         "algorithmic_relaxations_per_step": r["work"],
     }
-    if phase_ms > 0:
-        ach = r["executed"] * 2 / (phase_ms / 1e3) / 1e12
-        line["roofline"]["achieved"] = ach
-        line["roofline"]["frac"] = ach / (peak / 1e12)
-        if traffic:
-            line["roofline"]["dram_gb_s"] = traffic / (phase_ms / 1e3) / 1e9
+    if "blocked" in r:
+        b = r["blocked"]
+        bk = b["kprof"]
+        phase_ms = sum(bk[k][0] for k in ("fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel"))
+        peak, sms = int32_peak_ops(0, r["clocks"].get("sm_max_mhz"))
+        ach = b["executed"] * 2 / (phase_ms / 1e3) / 1e12 if phase_ms > 0 else None
+        tr = phase_traffic()
+        traffic = sum(tr["bytes_per_launch"][k] * bk[k][1] for k in tr["bytes_per_launch"] if k in bk) if tr else None
+        line["blocked_kernels_same_batch"] = {
+            "value": r["work"] / b["t"], "unit": UNIT, "ms_per_step": b["t"] * 1e3,
+            "how": "rbg_fw_batch with RBG_MODE_NO_DAG on the same resident blocks: snapshot-exact blocked "
+                   "Floyd-Warshall for every component (the path of matrices not numbered in a "
+                   "topological order)",
+            "roofline": {"bound": "int32_alu", "unit": "Tops/s", "achieved": ach, "peak": peak / 1e12,
+                         "frac": ach / (peak / 1e12) if ach else None,
+                         "kernel": "fw_diag_kernel + fw_panel_kernel + fw_tile_kernel",
+                         "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock",
+                         "ops_per_relaxation": 2, "executed_relaxations_per_step": b["executed"],
+                         "traffic": traffic,
+                         "traffic_unit": "DRAM bytes per step of the three phase kernels (per-launch bytes "
+                                         "from profiles/fw_phase_traffic.txt x launches)"},
+            "kernel_ms_per_step": {k: v[0] for k, v in bk.items() if v[1]}}
     e = r["e2e"]
     line["e2e"] = {"value": e["value"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                    "d2h_bytes_per_step": e["d2h"], "ms_per_step": e["t"] / e["steps"] * 1e3,

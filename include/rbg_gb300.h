@@ -426,6 +426,51 @@ int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *loca
                             int32_t *indices, int32_t *data, const uint64_t *chunk_mask, rbg_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Component-wise closure straight from the CSR graph (no dense blocks) when every component is
+ * numbered in a topological order (its off-diagonal entries all below, or all above, the
+ * diagonal) and in the clean regime: the DAG path of rbg_fw_batch applied to the graph.  The
+ * sequence is rbg_cc_dag_classify -> rbg_cc_dag_edges -> rbg_dag_closure / rbg_dag_gather on
+ * the edges -> rbg_cc_dag_stats -> rbg_cc_dag_merge_count / _fill; values and diameters are
+ * those of merge_component_matrices over the reference's per-component closures
+ * (redblackgraph/sparse/csgraph/transitive_closure.py:85-195).  Components come from
+ * rbg_cc_label; `workspace` is its workspace.
+ * ---------------------------------------------------------------------------------------- */
+
+/* comp_flags[c] (device, ncomp): bit 0 outside the clean regime, bit 1 an entry below the
+ * diagonal, bit 2 an entry above it; diag (device, n): each row's diagonal value (0 when not
+ * stored); edge_ptr (device, n + 1): row pointers of the off-diagonal nonzeros, *edges (host)
+ * their number.  Synchronises `stream`. */
+int32_t rbg_cc_dag_classify(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
+                            const int32_t *sorted_vertex, const int64_t *start, int64_t ncomp,
+                            void *workspace, int64_t workspace_bytes, uint32_t *comp_flags, int32_t *diag,
+                            int64_t *edge_ptr, int64_t *edges, rbg_stream_t stream);
+
+/* The off-diagonal nonzeros (columns ascending) at edge_ptr.  Ordered on `stream`. */
+int32_t rbg_cc_dag_edges(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
+                         const int64_t *edge_ptr, int32_t *edge_col, int32_t *edge_val, rbg_stream_t stream);
+
+/* Per component c (comp_kind[c]: 1 entries below the diagonal, 2 above, 0 skip): top_msb[c] =
+ * the largest MSB of the products the sequential loop performs (a component with top_msb >= 31
+ * may overflow and must take the dense path), first_msb[c] = the largest MSB of any cell's
+ * first value (the Floyd-Warshall diameter; -1 when there is none), comp_max[c] = the largest
+ * final value, floored at 0 (the 'D' method's diameter source).  `edges` and `closure` are
+ * device CSR matrices of n rows (int32 values).  Ordered on `stream`. */
+int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
+                         const int64_t *start, const int32_t *comp_kind, const rbg_csr_t *edges,
+                         const rbg_csr_t *closure, const int32_t *diag, int32_t *top_msb,
+                         int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream);
+
+/* Row pointers (device, n + 1) of the merged matrix: each closure row plus its diagonal value
+ * when nonzero; *nnz (host) its size.  Synchronises `stream`. */
+int32_t rbg_cc_dag_merge_count(int64_t n, const int64_t *closure_ptr, const int32_t *diag, void *workspace,
+                               int64_t workspace_bytes, int64_t *out_indptr, int64_t *nnz, rbg_stream_t stream);
+
+/* The merged matrix's columns (ascending) and values.  Ordered on `stream`. */
+int32_t rbg_cc_dag_merge_fill(int64_t n, const rbg_csr_t *closure, const int32_t *diag,
+                              const int64_t *out_indptr, int32_t *out_indices, int32_t *out_data,
+                              rbg_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
  * Relationship lookups on resident closures (redblackgraph/reference/calc_relationship.py:54-71).
  * ---------------------------------------------------------------------------------------- */
 typedef struct rbg_lookup_t {

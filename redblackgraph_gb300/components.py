@@ -1,5 +1,9 @@
 """Component-wise closure on the GPU, at the device-tensor level.
 
+When every component is numbered in a topological order and clean, the closure is taken
+straight from the CSR graph (``dag_component_closure``: the DAG recurrence per component, the
+Floyd-Warshall diameter from each cell's first value).  Otherwise:
+
 The graph (device CSR: int64 row pointers, int32 column indices, int32 values) is split into
 connected components by ``rbg_cc_label``, each component is scattered into its own dense block
 of one flat buffer (``rbg_cc_densify``), all blocks are closed by one ``rbg_fw_batch`` call in
@@ -141,6 +145,76 @@ def _msb(v: int) -> int:
     return v.bit_length() - 1 if v > 1 else 0
 
 
+DAG_MAX_N = 8192          # rows of a component the DAG path takes (include/rbg_gb300.h)
+_UNCLEAN, _BELOW, _ABOVE = 1, 2, 4
+
+
+def dag_component_closure(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor, n: int,
+                          comps: Components, method: str, densify_threshold: int, stream=None):
+    """Component-wise closure straight from the CSR graph when every component is numbered in a
+    topological order (entries all below, or all above, the diagonal), clean and at most 8192
+    vertices: closure rows by the DAG recurrence, Floyd-Warshall diameters from each cell's first
+    value, the diagonal put back (rbg_cc_dag_*).  Returns ``(indptr, indices, data, diameter)``,
+    or None when some component needs the dense path (or a product may reach the top bit)."""
+    from .dag import RowTooWide, dag_closure_device
+    from .spgemm import DeviceCSR
+    k = comps.count
+    if k == 0 or int(comps.sizes.max()) > DAG_MAX_N:
+        return None
+    L = _lib.load()
+    dev = indptr.device
+    sh = stream_handle(stream)
+    ws = comps.workspace
+    ip = indptr.data_ptr()
+    ij = indices.data_ptr() if indices.numel() else ip
+    iv = data.data_ptr() if data.numel() else ip
+    flags = torch.empty(k, dtype=torch.int32, device=dev)
+    diag = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    eptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    ne = ctypes.c_int64(0)
+    _lib.check(L.rbg_cc_dag_classify(n, ip, ij, iv, comps.sorted_vertex.data_ptr(), comps.start.data_ptr(), k,
+                                     ws.data_ptr(), ws.numel(), flags.data_ptr(), diag.data_ptr(), eptr.data_ptr(),
+                                     ctypes.byref(ne), sh), "cc_dag_classify")
+    f = flags.cpu().numpy()
+    if ((f & _UNCLEAN) != 0).any() or (((f & _BELOW) != 0) & ((f & _ABOVE) != 0)).any():
+        return None
+    kind = torch.from_numpy(np.where(f & _ABOVE, 2, 1).astype(np.int32)).to(dev)
+    ecol = torch.empty(max(ne.value, 1), dtype=torch.int32, device=dev)
+    evals = torch.empty(max(ne.value, 1), dtype=torch.int32, device=dev)
+    _lib.check(L.rbg_cc_dag_edges(n, ip, ij, iv, eptr.data_ptr(), ecol.data_ptr(), evals.data_ptr(), sh),
+               "cc_dag_edges")
+    E = DeviceCSR(eptr, ecol[:ne.value], evals[:ne.value], (n, n))
+    try:
+        C, _, _ = dag_closure_device(E, stream)
+    except RowTooWide:
+        return None
+    top = torch.empty(k, dtype=torch.int32, device=dev)
+    first = torch.empty(k, dtype=torch.int32, device=dev)
+    cmax = torch.empty(k, dtype=torch.int32, device=dev)
+    ec, cc = E.cstruct(), C.cstruct()
+    _lib.check(L.rbg_cc_dag_stats(n, k, comps.label.data_ptr(), comps.local.data_ptr(), comps.start.data_ptr(),
+                                  kind.data_ptr(), ctypes.byref(ec), ctypes.byref(cc), diag.data_ptr(),
+                                  top.data_ptr(), first.data_ptr(), cmax.data_ptr(), sh), "cc_dag_stats")
+    st = torch.stack([top, first, cmax]).cpu().numpy()
+    if (st[0] >= 31).any():
+        return None
+    oi = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    nnz = ctypes.c_int64(0)
+    _lib.check(L.rbg_cc_dag_merge_count(n, C.indptr.data_ptr(), diag.data_ptr(), ws.data_ptr(), ws.numel(),
+                                        oi.data_ptr(), ctypes.byref(nnz), sh), "cc_dag_merge_count")
+    oj = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
+    ov = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
+    _lib.check(L.rbg_cc_dag_merge_fill(n, ctypes.byref(cc), diag.data_ptr(), oi.data_ptr(), oj.data_ptr(),
+                                       ov.data_ptr(), sh), "cc_dag_merge_fill")
+    fw = component_methods(comps.sizes, k, method, densify_threshold)
+    diameter = 0
+    if fw.any():
+        diameter = max(0, int(st[1][fw].max()))
+    if (~fw).any():
+        diameter = max(diameter, _msb(int(st[2][~fw].max())))
+    return oi, oj[:nnz.value], ov[:nnz.value], diameter
+
+
 def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor, n: int,
                              method: str = "auto", densify_threshold: int = 500, stream=None):
     """Close every component of the device CSR graph.
@@ -149,6 +223,9 @@ def component_closure_device(indptr: torch.Tensor, indices: torch.Tensor, data: 
     component (by number) that holds a cycle, as the reference's per-component loop does.
     """
     comps = label_components(indptr, indices, n, stream)
+    got = dag_component_closure(indptr, indices, data, n, comps, method, densify_threshold, stream)
+    if got is not None:
+        return (*got, comps)
     blocks = densify(indptr, indices, data, comps, stream)
     fw = component_methods(comps.sizes, comps.count, method, densify_threshold)
     # the closure's finalization counts every row while it writes it (one read of the blocks less)

@@ -18,6 +18,7 @@
 #include <cub/cub.cuh>
 #include <algorithm>
 #include "rbg_internal.cuh"
+#include "dag_rows.cuh"
 
 namespace rbg {
 
@@ -398,5 +399,237 @@ extern "C" int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const in
                                                              reinterpret_cast<const unsigned long long *>(chunk_mask));
         RBG_CUDA_TRY(cudaGetLastError());
     }
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Component-wise closure straight from the CSR graph, for graphs whose components are all
+// numbered in a topological order and in the clean regime: the DAG path of the batched dense
+// closure (fw_tri.cu) without dense blocks.  Each component's closure is the DAG recurrence
+// (rbg_dag_closure over the off-diagonal entries), its Floyd-Warshall diameter comes from each
+// cell's first value (dag_rows.cuh), and the merged matrix is the closure rows with the
+// diagonal put back.
+// ------------------------------------------------------------------------------------------
+namespace rbg {
+
+constexpr unsigned CCD_UNCLEAN = 1u, CCD_BELOW = 2u, CCD_ABOVE = 4u;
+constexpr int CCD_WARPS = 8;
+
+// one warp per component: its rows' diagonal values and off-diagonal nonzero counts, and the
+// component's flags (clean regime, side of the diagonal)
+__global__ void cc_dag_classify_kernel(int64_t ncomp, const int64_t *__restrict__ indptr,
+                                       const int32_t *__restrict__ indices, const int32_t *__restrict__ data,
+                                       const int32_t *__restrict__ sorted_vertex, const int64_t *__restrict__ start,
+                                       unsigned *__restrict__ comp_flags, int32_t *__restrict__ diag,
+                                       int64_t *__restrict__ cnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < ncomp; c += warps) {
+        unsigned f = 0;
+        for (int64_t r = start[c] + lane; r < start[c + 1]; r += 32) {
+            const int64_t u = sorted_vertex[r];
+            int32_t d = 0;
+            int64_t k = 0;
+            for (int64_t e = indptr[u]; e < indptr[u + 1]; ++e) {
+                const int32_t v = data[e];
+                const int64_t col = indices[e];
+                if (col == u) {
+                    d = v;
+                    if (!(v == 0 || v == 1 || v == -1)) f |= CCD_UNCLEAN;
+                } else if (v != 0) {
+                    if (v == 1 || v < 0) f |= CCD_UNCLEAN;
+                    f |= col < u ? CCD_BELOW : CCD_ABOVE;
+                    ++k;
+                }
+            }
+            diag[u] = d;
+            cnt[u] = k;
+        }
+        f = __reduce_or_sync(0xffffffffu, f);
+        if (lane == 0) comp_flags[c] = f;
+    }
+}
+
+// the off-diagonal nonzeros of every row, in column order
+__global__ void cc_dag_edges_kernel(int64_t n, const int64_t *__restrict__ indptr, const int32_t *__restrict__ indices,
+                                    const int32_t *__restrict__ data, const int64_t *__restrict__ edge_ptr,
+                                    int32_t *__restrict__ edge_col, int32_t *__restrict__ edge_val) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        int64_t o = edge_ptr[u];
+        for (int64_t e = indptr[u]; e < indptr[u + 1]; ++e) {
+            const int32_t v = data[e];
+            if (indices[e] != u && v != 0) {
+                edge_col[o] = indices[e];
+                edge_val[o] = v;
+                ++o;
+            }
+        }
+    }
+}
+
+// one warp per vertex: the row statistics of dag_rows.cuh and the row's largest final value,
+// reduced per component
+__global__ void __launch_bounds__(32 * CCD_WARPS)
+cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t *__restrict__ local,
+                    const int64_t *__restrict__ start, const int32_t *__restrict__ comp_kind,
+                    const int64_t *__restrict__ eptr, const int32_t *__restrict__ ecol, const int32_t *__restrict__ eval,
+                    const int64_t *__restrict__ cptr, const int32_t *__restrict__ ccol, const int32_t *__restrict__ cval,
+                    const int32_t *__restrict__ diag, int *__restrict__ top, int *__restrict__ first,
+                    int *__restrict__ cmax) {
+    __shared__ unsigned bm_all[CCD_WARPS][DAG_MAX_N / 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * CCD_WARPS;
+    for (int64_t u = (int64_t)blockIdx.x * CCD_WARPS + w; u < n; u += warps) {
+        const int c = label[u];
+        const int kind = comp_kind[c];
+        if (kind == DAG_KIND_NONE) continue;         // warp-uniform
+        const int words = (int)((start[c + 1] - start[c] + 31) >> 5);
+        int am = -1, fm = -1;
+        unsigned long long prods = 0;
+        dag_row_stats(bm_all[w], words, kind, u, eptr, ecol, eval,
+                      [&](int64_t r, int64_t &off, int &len) { off = cptr[r]; len = (int)(cptr[r + 1] - off); },
+                      ccol, cval, [&](int32_t col) { return local[col]; }, lane, am, fm, prods);
+        int mx = 0;
+        for (int64_t q = cptr[u] + lane; q < cptr[u + 1]; q += 32) mx = max(mx, cval[q]);
+        if (lane == 0) mx = max(mx, diag[u]);
+        am = __reduce_max_sync(0xffffffffu, am);
+        fm = __reduce_max_sync(0xffffffffu, fm);
+        mx = __reduce_max_sync(0xffffffffu, mx);
+        if (lane == 0) {
+            if (am >= 0) atomicMax(top + c, am);
+            if (fm >= 0) atomicMax(first + c, fm);
+            if (mx > 0) atomicMax(cmax + c, mx);
+        }
+    }
+}
+
+__global__ void cc_dag_merge_count_kernel(int64_t n, const int64_t *__restrict__ cptr, const int32_t *__restrict__ diag,
+                                          int64_t *__restrict__ cnt) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
+        cnt[u] = (cptr[u + 1] - cptr[u]) + (diag[u] != 0 ? 1 : 0);
+}
+
+// one warp per vertex: the closure row with the diagonal value put in its place
+__global__ void cc_dag_merge_fill_kernel(int64_t n, const int64_t *__restrict__ cptr, const int32_t *__restrict__ ccol,
+                                         const int32_t *__restrict__ cval, const int32_t *__restrict__ diag,
+                                         const int64_t *__restrict__ optr, int32_t *__restrict__ ocol,
+                                         int32_t *__restrict__ oval) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += warps) {
+        const int64_t c0 = cptr[u], c1 = cptr[u + 1], o = optr[u];
+        const int32_t d = diag[u];
+        int below = 0;                                  // closure entries left of the diagonal
+        for (int64_t q = c0 + lane; q < c1; q += 32) below += ccol[q] < u;
+        below = __reduce_add_sync(0xffffffffu, below);
+        const int shift = d != 0 ? 1 : 0;
+        if (lane == 0 && d != 0) {
+            ocol[o + below] = (int32_t)u;
+            oval[o + below] = d;
+        }
+        for (int64_t q = c0 + lane; q < c1; q += 32) {
+            const int32_t col = ccol[q];
+            const int64_t at = o + (q - c0) + (col > u ? shift : 0);
+            ocol[at] = col;
+            oval[at] = cval[q];
+        }
+    }
+}
+
+}  // namespace rbg
+
+extern "C" int32_t rbg_cc_dag_classify(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
+                                       const int32_t *sorted_vertex, const int64_t *start, int64_t ncomp,
+                                       void *workspace, int64_t workspace_bytes, uint32_t *comp_flags,
+                                       int32_t *diag, int64_t *edge_ptr, int64_t *edges, rbg_stream_t stream) {
+    if (n < 0 || ncomp < 0 || ncomp > n || !workspace || !edges || (n > 0 && (!indptr || !sorted_vertex || !start ||
+                                                                              !comp_flags || !diag || !edge_ptr)))
+        return RBG_ERR_INVALID;
+    if (workspace_bytes < (int64_t)cc_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
+    CcWs w;
+    cc_layout(n, reinterpret_cast<unsigned char *>(workspace), &w);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    *edges = 0;
+    if (n == 0) return RBG_OK;
+    note_launches(1);
+    cc_dag_classify_kernel<<<grid_for(ncomp * 32, 256), 256, 0, s>>>(ncomp, indptr, indices, data, sorted_vertex,
+                                                                     start, comp_flags, diag, edge_ptr);
+    RBG_CUDA_TRY(cudaGetLastError());
+    RBG_CUDA_TRY(cudaMemsetAsync(edge_ptr + n, 0, 8, s));
+    size_t tb = w.tmp_bytes;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, edge_ptr, edge_ptr, (int)(n + 1), s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(edges, edge_ptr + n, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_cc_dag_edges(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
+                                    const int64_t *edge_ptr, int32_t *edge_col, int32_t *edge_val,
+                                    rbg_stream_t stream) {
+    if (n < 0 || (n > 0 && (!indptr || !edge_ptr))) return RBG_ERR_INVALID;
+    if (n == 0) return RBG_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    note_launches(1);
+    cc_dag_edges_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, indptr, indices, data, edge_ptr, edge_col, edge_val);
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
+                                    const int64_t *start, const int32_t *comp_kind, const rbg_csr_t *edges,
+                                    const rbg_csr_t *closure, const int32_t *diag, int32_t *top_msb,
+                                    int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream) {
+    if (n < 0 || ncomp < 0 || !edges || !closure || (ncomp > 0 && (!top_msb || !first_msb || !comp_max)))
+        return RBG_ERR_INVALID;
+    if (edges->n_rows != n || closure->n_rows != n) return RBG_ERR_INVALID;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (ncomp > 0) {
+        RBG_CUDA_TRY(cudaMemsetAsync(top_msb, 0xff, (size_t)ncomp * 4, s));
+        RBG_CUDA_TRY(cudaMemsetAsync(first_msb, 0xff, (size_t)ncomp * 4, s));
+        RBG_CUDA_TRY(cudaMemsetAsync(comp_max, 0, (size_t)ncomp * 4, s));
+    }
+    if (n == 0) return RBG_OK;
+    note_launches(1);
+    cc_dag_stats_kernel<<<grid_for(n * 32, 32 * CCD_WARPS), 32 * CCD_WARPS, 0, s>>>(
+        n, label, local, start, comp_kind, edges->indptr, edges->indices, static_cast<const int32_t *>(edges->data),
+        closure->indptr, closure->indices, static_cast<const int32_t *>(closure->data), diag, top_msb, first_msb,
+        comp_max);
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_cc_dag_merge_count(int64_t n, const int64_t *closure_ptr, const int32_t *diag, void *workspace,
+                                          int64_t workspace_bytes, int64_t *out_indptr, int64_t *nnz,
+                                          rbg_stream_t stream) {
+    if (n < 0 || !workspace || !nnz || !out_indptr || (n > 0 && (!closure_ptr || !diag))) return RBG_ERR_INVALID;
+    if (workspace_bytes < (int64_t)cc_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
+    CcWs w;
+    cc_layout(n, reinterpret_cast<unsigned char *>(workspace), &w);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (n > 0) {
+        note_launches(1);
+        cc_dag_merge_count_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, closure_ptr, diag, out_indptr);
+        RBG_CUDA_TRY(cudaGetLastError());
+    }
+    RBG_CUDA_TRY(cudaMemsetAsync(out_indptr + n, 0, 8, s));
+    size_t tb = w.tmp_bytes;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, out_indptr, out_indptr, (int)(n + 1), s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(nnz, out_indptr + n, 8, cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_cc_dag_merge_fill(int64_t n, const rbg_csr_t *closure, const int32_t *diag,
+                                         const int64_t *out_indptr, int32_t *out_indices, int32_t *out_data,
+                                         rbg_stream_t stream) {
+    if (n < 0 || !closure || (n > 0 && (!diag || !out_indptr))) return RBG_ERR_INVALID;
+    if (closure->n_rows != n) return RBG_ERR_INVALID;
+    if (n == 0) return RBG_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    note_launches(1);
+    cc_dag_merge_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(
+        n, closure->indptr, closure->indices, static_cast<const int32_t *>(closure->data), diag, out_indptr,
+        out_indices, out_data);
+    RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }

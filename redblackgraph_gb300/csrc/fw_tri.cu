@@ -21,9 +21,10 @@
 // anything outside the clean regime, a row of more than TRI_CAP entries or n > 8192.
 //
 // Pipeline (one call): scan the dense rows (clean-regime test, which side of the diagonal, up
-// to TRI_CAP off-diagonal entries per row) -> CSR of the candidate matrices with batch-global
-// row numbers -> rbg_dag_closure -> per-row statistics (largest product MSB, largest first-value
-// MSB) -> dense rows of the accepted matrices written from the closure rows.
+// to TRI_CAP off-diagonal entries per row; the output's zeros and diagonal written in the same
+// pass) -> CSR of the candidate matrices with batch-global row numbers -> rbg_dag_closure ->
+// per-row statistics (largest product MSB, largest first-value MSB) -> the closure rows'
+// entries scattered into the dense rows of the accepted matrices.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 #include <string.h>
@@ -31,6 +32,7 @@
 #include <mutex>
 #include <vector>
 #include "rbg_internal.cuh"
+#include "dag_rows.cuh"
 
 namespace rbg {
 namespace {
@@ -38,11 +40,11 @@ namespace {
 constexpr int TRI_ROWS = 8;                  // rows per CTA, one warp each
 constexpr int TRI_THREADS = 32 * TRI_ROWS;
 constexpr int TRI_CAP = 16;                  // off-diagonal entries per row the scan keeps
-constexpr int64_t TRI_MAX_N = 8192;          // rows of a matrix on this path (bitmap size)
+constexpr int64_t TRI_MAX_N = DAG_MAX_N;     // rows of a matrix on this path (bitmap size)
 constexpr int TRI_BM_WORDS = (int)(TRI_MAX_N / 32);
 constexpr unsigned TF_UNCLEAN = 1u, TF_BELOW = 2u, TF_ABOVE = 4u, TF_WIDE = 8u;
-constexpr int KIND_NONE = 0, KIND_BELOW = 1, KIND_ABOVE = 2;
-constexpr int TRI_TOP = 31;                  // lbits - 1 for 32-bit values
+constexpr int KIND_NONE = DAG_KIND_NONE, KIND_BELOW = DAG_KIND_BELOW, KIND_ABOVE = DAG_KIND_ABOVE;
+constexpr int TRI_TOP = DAG_TOP_MSB;         // lbits - 1 for 32-bit values
 
 struct TriComp {
     int64_t n, in_off, out_off, row_base;    // row_base: first batch-global row
@@ -58,62 +60,115 @@ __device__ __forceinline__ int tri_find(const int64_t *__restrict__ prefix, int 
     return lo;
 }
 
-// MSB of an off-diagonal value; a value no clean product yields (zero, or negative after a
-// wrap) counts as reaching the top bit
-__device__ __forceinline__ int tri_msb(int32_t v) { return v > 0 ? msb_u32((uint32_t)v) : 99; }
+// Off-diagonal entries of four consecutive columns j0 .. j0 + 3 held by each lane (m of them
+// valid): clean-regime flags, and the nonzeros appended to the row's slots in column order.
+__device__ __forceinline__ void tri_take(int32_t (&v)[4], int64_t j0, int m, int64_t i, int lane, int64_t g,
+                                         int32_t *__restrict__ slot_col, int32_t *__restrict__ slot_val,
+                                         unsigned &flags, int &cnt) {
+    int c4 = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int64_t j = j0 + k;
+        if (k >= m) {
+            v[k] = 0;
+        } else if (j == i) {
+            if (!(v[k] == 0 || v[k] == 1 || v[k] == -1)) flags |= TF_UNCLEAN;
+            v[k] = 0;                        // the diagonal is not an edge
+        } else if (v[k] != 0) {
+            if (v[k] == 1 || v[k] < 0) flags |= TF_UNCLEAN;
+            flags |= j < i ? TF_BELOW : TF_ABOVE;
+            ++c4;
+        }
+    }
+    if (!__any_sync(0xffffffffu, c4 != 0)) return;
+    int x = c4;                              // inclusive prefix over the lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    int pos = cnt + x - c4;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (v[k] != 0) {
+            if (pos < TRI_CAP) {
+                slot_col[g * TRI_CAP + pos] = (int32_t)(j0 + k);
+                slot_val[g * TRI_CAP + pos] = v[k];
+            }
+            ++pos;
+        }
+    }
+    cnt += __shfl_sync(0xffffffffu, x, 31);
+}
 
 // One warp per row: clean-regime test, side of the diagonal, the row's off-diagonal entries in
-// column order into its TRI_CAP slots (the count may exceed TRI_CAP: then only flagged).
+// column order into its TRI_CAP slots (the count may exceed TRI_CAP: then only flagged).  The
+// row is read as 16-byte vectors from its first 16-byte boundary (scalar head and tail).  When
+// the output is another buffer, the row's zeros and diagonal are written there in the same
+// pass (a matrix that then leaves this path has its output rewritten by the blocked kernels).
 __global__ void __launch_bounds__(TRI_THREADS)
-tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comps, const int64_t *__restrict__ pre,
-                int count, int32_t *__restrict__ slot_col, int32_t *__restrict__ slot_val,
-                int32_t *__restrict__ row_cnt, int32_t *__restrict__ row_comp, unsigned *__restrict__ cflags) {
+tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
+                const int64_t *__restrict__ pre, int count, int32_t *__restrict__ slot_col,
+                int32_t *__restrict__ slot_val, int32_t *__restrict__ row_cnt, int32_t *__restrict__ row_comp,
+                unsigned *__restrict__ cflags) {
     const int ci = tri_find(pre, count, blockIdx.x);
     const TriComp c = comps[ci];
     const int64_t i = ((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS + (threadIdx.x >> 5);
     if (i >= c.n) return;                    // warp-uniform
     const int lane = threadIdx.x & 31;
-    const int32_t *row = in + c.in_off + i * c.n;
-    const int64_t g = c.row_base + i;
+    const int64_t n = c.n, g = c.row_base + i;
+    const int32_t *row = in + c.in_off + i * n;
+    int32_t *orow = in == out ? nullptr : out + c.out_off + i * n;
+    const int64_t lead = (int64_t)((16 - ((uintptr_t)row & 15)) & 15) / 4;   // to the first boundary
+    const int head = (int)(lead < n ? lead : n);
+    const int64_t nv = (n - head) / 4;       // 16-byte vectors after the head
+    const int tail = (int)(n - head - 4 * nv);
+    const bool ovec = orow && (((uintptr_t)orow - (uintptr_t)row) & 15) == 0;
     unsigned flags = 0;
     int cnt = 0;
-    for (int64_t b = 0; b < c.n; b += 128) {
-        const int64_t j0 = b + lane * 4;
-        int32_t v[4];
+    int32_t v[4];
+    // head: columns 0 .. head - 1, one per lane
+    if (head) {
+        v[0] = lane < head ? row[lane] : 0;
+        if (orow && lane < head) orow[lane] = lane == i ? v[0] : 0;
+        tri_take(v, lane, lane < head ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
+    }
+    // four 16-byte vectors per lane in flight: vectors s0 + 32 u + lane (u = 0..3), taken in
+    // column order (u ascending)
+    for (int64_t s0 = 0; s0 < nv; s0 += 128) {
+        int4 x[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) v[k] = j0 + k < c.n ? row[j0 + k] : 0;
-        int c4 = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int64_t j = j0 + k;
-            if (j == i) {
-                if (!(v[k] == 0 || v[k] == 1 || v[k] == -1)) flags |= TF_UNCLEAN;
-                v[k] = 0;                    // the diagonal is not an edge
-            } else if (v[k] != 0) {
-                if (v[k] == 1 || v[k] < 0) flags |= TF_UNCLEAN;
-                flags |= j < i ? TF_BELOW : TF_ABOVE;
-                ++c4;
-            }
+        for (int u = 0; u < 4; ++u) {
+            const int64_t q = s0 + 32 * u + lane;
+            if (q < nv) x[u] = *reinterpret_cast<const int4 *>(row + head + 4 * q);
+            else x[u] = make_int4(0, 0, 0, 0);
         }
-        if (!__any_sync(0xffffffffu, c4 != 0)) continue;
-        int x = c4;                          // inclusive prefix over the lanes
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        int pos = cnt + x - c4;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (v[k] != 0) {
-                if (pos < TRI_CAP) {
-                    slot_col[g * TRI_CAP + pos] = (int32_t)(j0 + k);
-                    slot_val[g * TRI_CAP + pos] = v[k];
+        for (int u = 0; u < 4; ++u) {
+            const int64_t q = s0 + 32 * u + lane;
+            const int64_t j0 = head + 4 * q;
+            v[0] = x[u].x; v[1] = x[u].y; v[2] = x[u].z; v[3] = x[u].w;
+            if (orow && q < nv) {
+                int4 z = make_int4(0, 0, 0, 0);
+                if (i >= j0 && i < j0 + 4) {
+                    const int d = (int)(i - j0);
+                    if (d == 0) z.x = v[0]; else if (d == 1) z.y = v[1]; else if (d == 2) z.z = v[2]; else z.w = v[3];
                 }
-                ++pos;
+                if (ovec) {
+                    *reinterpret_cast<int4 *>(orow + j0) = z;
+                } else {
+                    orow[j0] = z.x; orow[j0 + 1] = z.y; orow[j0 + 2] = z.z; orow[j0 + 3] = z.w;
+                }
             }
+            if (s0 + 32 * u < nv)            // warp-uniform: some lane holds a vector
+                tri_take(v, j0, q < nv ? 4 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
         }
-        cnt += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (tail) {
+        const int64_t j = head + 4 * nv + lane;
+        v[0] = lane < tail ? row[j] : 0;
+        if (orow && lane < tail) orow[j] = j == i ? v[0] : 0;
+        tri_take(v, j, lane < tail ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
     }
     if (cnt > TRI_CAP) flags |= TF_WIDE;
     flags = __reduce_or_sync(0xffffffffu, flags);
@@ -148,10 +203,8 @@ __global__ void tri_csr_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
     }
 }
 
-// One warp per row of a candidate matrix: the largest MSB of every product the sequential loop
-// performs on the row (and, above the diagonal, of the DAG recurrence's own candidates) and the
-// largest MSB of the row's first values.  A per-warp bitmap of the matrix's columns marks the
-// cells that already hold a value.
+// One warp per row of a candidate matrix: the row statistics of dag_rows.cuh, reduced per
+// matrix (largest product MSB, largest first-value MSB, products).
 __global__ void __launch_bounds__(TRI_THREADS)
 tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                  const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
@@ -161,7 +214,6 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
                  int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
     __shared__ unsigned bm_all[TRI_ROWS][TRI_BM_WORDS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned *bm = bm_all[w];
     const int64_t warps = (int64_t)gridDim.x * TRI_ROWS;
     for (int64_t g = (int64_t)blockIdx.x * TRI_ROWS + w; g < R; g += warps) {
         const int ci = row_comp[g];
@@ -169,63 +221,11 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
         if (kind == KIND_NONE) continue;     // warp-uniform
         const int32_t base = (int32_t)comps[ci].row_base;
         const int words = (int)((comps[ci].n + 31) >> 5);
-        for (int q = lane; q < words; q += 32) bm[q] = 0;
-        __syncwarp();
-        const int64_t a0 = indptr[g];
-        const int alen = (int)(indptr[g + 1] - a0);
         int am = -1, fm = -1;
         unsigned long long prods = 0;
-        for (int p = lane; p < alen; p += 32) {      // the row's own values are written first
-            const int j = a_col[a0 + p] - base;
-            atomicOr(&bm[j >> 5], 1u << (j & 31));
-            fm = max(fm, tri_msb(a_val[a0 + p]));
-        }
-        __syncwarp();
-        // below: steps k over the parents, ascending, each adding A(i, k) (x) C(k, .).  Above:
-        // the same products are the recurrence's candidates (their MSB bounds the closure values)
-        for (int p = 0; p < alen; ++p) {
-            const int32_t kg = a_col[a0 + p];
-            const int mk = tri_msb(a_val[a0 + p]);
-            const int64_t c0 = row_off[kg];
-            const int clen = row_len[kg];
-            for (int q = lane; q < clen; q += 32) {
-                const int pm = mk + tri_msb(p_val[c0 + q]);
-                am = max(am, pm);
-                if (kind == KIND_BELOW) {
-                    const int j = p_col[c0 + q] - base;
-                    const unsigned bit = 1u << (j & 31);
-                    if (!(bm[j >> 5] & bit)) {
-                        fm = max(fm, pm);
-                        atomicOr(&bm[j >> 5], bit);
-                    }
-                }
-            }
-            if (kind == KIND_BELOW && lane == 0) prods += (unsigned long long)clen;
-            __syncwarp();
-        }
-        if (kind == KIND_ABOVE) {
-            // steps k over C(i), ascending, each adding C(i, k) (x) A(k, .)
-            const int64_t c0 = row_off[g];
-            const int clen = row_len[g];
-            for (int q = 0; q < clen; ++q) {
-                const int32_t kg = p_col[c0 + q];
-                const int mk = tri_msb(p_val[c0 + q]);
-                const int64_t k0 = indptr[kg];
-                const int klen = (int)(indptr[kg + 1] - k0);
-                for (int r = lane; r < klen; r += 32) {
-                    const int j = a_col[k0 + r] - base;
-                    const int pm = mk + tri_msb(a_val[k0 + r]);
-                    am = max(am, pm);
-                    const unsigned bit = 1u << (j & 31);
-                    if (!(bm[j >> 5] & bit)) {
-                        fm = max(fm, pm);
-                        atomicOr(&bm[j >> 5], bit);
-                    }
-                }
-                if (lane == 0) prods += (unsigned long long)klen;
-                __syncwarp();
-            }
-        }
+        dag_row_stats(bm_all[w], words, kind, g, indptr, a_col, a_val,
+                      [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; },
+                      p_col, p_val, [&](int32_t col) { return col - base; }, lane, am, fm, prods);
         am = __reduce_max_sync(0xffffffffu, am);
         fm = __reduce_max_sync(0xffffffffu, fm);
         if (lane == 0) {
@@ -233,13 +233,12 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
             if (fm >= 0) atomicMax(cfm + ci, fm);
             if (prods) atomicAdd(cprod + ci, prods);
         }
-        __syncwarp();                        // the next row clears the bitmap
     }
 }
 
-// One warp per row of an accepted matrix: the dense row from its closure row (every cell when
-// out != in; in place only the closure's entries, the other cells already hold the result),
-// and the row statistics when asked for.
+// One warp per row of an accepted matrix: the closure row's entries into the dense row (its
+// other cells already hold the result: zeros and the diagonal, in place or written by the
+// scan), and the row statistics when asked for.
 __global__ void __launch_bounds__(TRI_THREADS)
 tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
                  const int64_t *__restrict__ pre, int count, const unsigned char *__restrict__ cfinal,
@@ -255,44 +254,38 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
     const int32_t *rin = in + c.in_off + i * n;
     int32_t *rout = out + c.out_off + i * n;
     const int32_t diag = rin[i];
-    if (rin != rout) {
-        for (int64_t b = 0; b < n; b += 128) {
-            const int64_t j0 = b + lane * 4;
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (j0 + k < n) rout[j0 + k] = j0 + k == i ? diag : 0;
-        }
-        __syncwarp();                        // the zeros land before the closure's values
-    }
     const int64_t c0 = row_off[g];
     const int clen = row_len[g];
     const int32_t base = (int32_t)c.row_base;
-    unsigned long long wd[4] = {0ull, 0ull, 0ull, 0ull};   // chunk masks (n <= 8192: <= 4 words)
+    // chunk masks of the row (n <= 8192: at most four 64-bit words), held in registers
+    unsigned long long w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+    auto mark = [&](int chunk) {
+        const unsigned long long bit = 1ull << (chunk & 63);
+        const int t = chunk >> 6;
+        w0 |= t == 0 ? bit : 0ull;
+        w1 |= t == 1 ? bit : 0ull;
+        w2 |= t == 2 ? bit : 0ull;
+        w3 |= t == 3 ? bit : 0ull;
+    };
     int mx = 0;
     for (int q = lane; q < clen; q += 32) {
         const int j = p_col[c0 + q] - base;
         const int32_t v = p_val[c0 + q];
         rout[j] = v;
         mx = max(mx, v);
-        const int chunk = j >> 5;
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-            if ((chunk >> 6) == t) wd[t] |= 1ull << (chunk & 63);
+        mark(j >> 5);
     }
     if (rs.row_count) {
         if (lane == 0 && diag != 0) {
-            const int chunk = (int)(i >> 5);
-#pragma unroll
-            for (int t = 0; t < 4; ++t)
-                if ((chunk >> 6) == t) wd[t] |= 1ull << (chunk & 63);
+            mark((int)(i >> 5));
             mx = max(mx, diag);
         }
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)wd[t]);
-            const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(wd[t] >> 32));
-            wd[t] = ((unsigned long long)hi << 32) | lo;
-        }
+        auto orw = [](unsigned long long x) {
+            const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)x);
+            const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(x >> 32));
+            return ((unsigned long long)hi << 32) | lo;
+        };
+        const unsigned long long wd[4] = {orw(w0), orw(w1), orw(w2), orw(w3)};
         mx = __reduce_max_sync(0xffffffffu, mx);
         if (lane == 0) {
             const int64_t at = rs.row_base[ci] + i;
@@ -406,8 +399,8 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
     {
         cudaEvent_t t = timer_begin(4, s);
         note_launches(1);
-        tri_scan_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, dc, dpre, (int)count, slot_col, slot_val,
-                                                                 row_cnt, row_comp, cflags);
+        tri_scan_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, out, dc, dpre, (int)count, slot_col,
+                                                                 slot_val, row_cnt, row_comp, cflags);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(4, t, s);
     }

@@ -221,3 +221,44 @@ def test_component_on_another_path_is_counted_again(native):
     assert err is None
     assert _same(r.W, W)
     assert r.diameter == d
+
+
+@pytest.mark.parametrize("reverse", [False, True])
+def test_csr_dag_path_vs_oracle(native, reverse):
+    """Components numbered in a topological order (oldest first, or reversed: entries above the
+    diagonal) are closed straight from the CSR graph; results and diameters of every method
+    equal the oracle's.  One component in another order sends the graph to the dense path."""
+    import torch
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.components import label_components, dag_component_closure
+    from redblackgraph_gb300.device import to_device
+    from redblackgraph_gb300.sparse import component_wise_closure
+    sizes = synth.component_sizes(50, 1, 900, seed=21)
+    M = _shuffled_forest(sizes, seed=23, shuffle=False)
+    n = M.shape[0]
+    if reverse:
+        p = np.arange(n)[::-1]
+        M = sp.csr_matrix(M[p][:, p])
+        M.sort_indices()
+    dev = lambda a, t: to_device(np.ascontiguousarray(a).astype(t))  # noqa: E731
+    ip, ix, dv = dev(M.indptr, np.int64), dev(M.indices, np.int32), dev(M.data, np.int32)
+    comps = label_components(ip, ix, n)
+    assert dag_component_closure(ip, ix, dv, n, comps, "auto", 500) is not None
+    for method, thr in (("auto", 500), ("auto", 60), ("FW", 500), ("D", 500)):
+        r = component_wise_closure(M, method=method, densify_threshold=thr)
+        W, d, err = O.component_wise_closure(M, method, thr)
+        assert err is None and _same(r.W, W) and r.diameter == d, (method, thr)
+        assert r.W.has_sorted_indices
+    # one component renumbered at random: the whole graph takes the dense path, same answers
+    big = int(np.argmax(sizes))
+    lo = int(np.sum(sizes[:big])) if not reverse else n - int(np.sum(sizes[:big + 1]))
+    q = np.arange(n)
+    q[lo:lo + int(sizes[big])] = lo + np.random.default_rng(3).permutation(int(sizes[big]))
+    S = sp.csr_matrix(M[q][:, q])
+    S.sort_indices()
+    sip, six, sdv = dev(S.indptr, np.int64), dev(S.indices, np.int32), dev(S.data, np.int32)
+    assert dag_component_closure(sip, six, sdv, n, label_components(sip, six, n), "auto", 500) is None
+    r = component_wise_closure(S)
+    W, d, err = O.component_wise_closure(S)
+    assert err is None and _same(r.W, W) and r.diameter == d
+    torch.cuda.synchronize()
