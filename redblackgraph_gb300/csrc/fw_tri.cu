@@ -179,6 +179,19 @@ tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const
     }
 }
 
+// which matrices are candidates, from the scan's flags (decided on the device: no host round
+// trip before the CSR is built)
+__global__ void tri_kind_kernel(int count, const TriComp *__restrict__ comps, const unsigned *__restrict__ cflags,
+                                int32_t *__restrict__ ckind) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const unsigned f = cflags[i];
+        int k = KIND_NONE;
+        if (comps[i].n > 0 && !(f & (TF_UNCLEAN | TF_WIDE)) && !((f & TF_BELOW) && (f & TF_ABOVE)))
+            k = (f & TF_ABOVE) ? KIND_ABOVE : KIND_BELOW;
+        ckind[i] = k;
+    }
+}
+
 // entries of each row in the CSR of the candidate matrices (rows of other matrices empty)
 __global__ void tri_count_kernel(int64_t R, const int32_t *__restrict__ row_cnt, const int32_t *__restrict__ row_comp,
                                  const int32_t *__restrict__ ckind, int64_t *__restrict__ cnt64) {
@@ -241,11 +254,12 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
 // scan), and the row statistics when asked for.
 __global__ void __launch_bounds__(TRI_THREADS)
 tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
-                 const int64_t *__restrict__ pre, int count, const unsigned char *__restrict__ cfinal,
+                 const int64_t *__restrict__ pre, int count, const int32_t *__restrict__ ckind,
+                 const int *__restrict__ cam,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, RowStats rs) {
     const int ci = tri_find(pre, count, blockIdx.x);
-    if (!cfinal[ci]) return;                 // block-uniform
+    if (ckind[ci] == KIND_NONE || cam[ci] >= TRI_TOP) return;   // not accepted (block-uniform)
     const TriComp c = comps[ci];
     const int64_t i = ((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS + (threadIdx.x >> 5);
     if (i >= c.n) return;                    // warp-uniform
@@ -353,14 +367,13 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
     cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (int64_t *)nullptr, (int64_t *)nullptr, (int)(R + 1));
     const size_t C = (size_t)count, NR = (size_t)R;
     auto layout = [&](Carve &cv, TriComp *&dc, int64_t *&dpre, unsigned *&cflags, int32_t *&ckind,
-                      unsigned char *&cfinal, int *&cam, int *&cfm, unsigned long long *&cprod, int32_t *&row_cnt,
+                      int *&cam, int *&cfm, unsigned long long *&cprod, int32_t *&row_cnt,
                       int32_t *&row_comp, int32_t *&slot_col, int32_t *&slot_val, int64_t *&indptr, void *&tmp,
                       int32_t *&a_col, int32_t *&a_val) {
         dc = cv.take<TriComp>(C);
         dpre = cv.take<int64_t>(C + 1);
         cflags = cv.take<unsigned>(C);
         ckind = cv.take<int32_t>(C);
-        cfinal = cv.take<unsigned char>(C);
         cam = cv.take<int>(C);
         cfm = cv.take<int>(C);
         cprod = cv.take<unsigned long long>(C);
@@ -377,19 +390,18 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
     int64_t *dpre, *indptr;
     unsigned *cflags;
     int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val;
-    unsigned char *cfinal;
     int *cam, *cfm;
     unsigned long long *cprod;
     void *tmp;
     {
         Carve dry{nullptr};
-        layout(dry, dc, dpre, cflags, ckind, cfinal, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr,
+        layout(dry, dc, dpre, cflags, ckind, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr,
                tmp, a_col, a_val);
         const int rc = tri_reserve(g_tri_a, dry.off + 256, s);
         if (rc) return rc;
     }
     Carve cv{g_tri_a.p};
-    layout(cv, dc, dpre, cflags, ckind, cfinal, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr, tmp,
+    layout(cv, dc, dpre, cflags, ckind, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr, tmp,
            a_col, a_val);
     RBG_CUDA_TRY(cudaMemcpyAsync(dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
     RBG_CUDA_TRY(cudaMemcpyAsync(dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
@@ -404,23 +416,11 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(4, t, s);
     }
-    std::vector<unsigned> hf(C);
-    RBG_CUDA_TRY(cudaMemcpyAsync(hf.data(), cflags, C * 4, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    std::vector<int32_t> kind(C, KIND_NONE);
-    int64_t candidates = 0;
-    for (size_t i = 0; i < C; ++i) {
-        const unsigned f = hf[i];
-        if (hc[i].n == 0 || (f & (TF_UNCLEAN | TF_WIDE)) || ((f & TF_BELOW) && (f & TF_ABOVE))) continue;
-        kind[i] = (f & TF_ABOVE) ? KIND_ABOVE : KIND_BELOW;
-        ++candidates;
-    }
-    if (candidates == 0) return RBG_OK;
-    RBG_CUDA_TRY(cudaMemcpyAsync(ckind, kind.data(), C * 4, cudaMemcpyHostToDevice, s));
-
     // 2. CSR of the candidates and their closure by levels
     cudaEvent_t tdag = timer_begin(5, s);
-    note_launches(2);
+    note_launches(3);
+    tri_kind_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>((int)count, dc, cflags,
+                                                                                          ckind);
     tri_count_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, row_cnt, row_comp, ckind, indptr);
     RBG_CUDA_TRY(cudaMemsetAsync(indptr + R, 0, 8, s));
     size_t tb = scan_tmp;
@@ -430,7 +430,15 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
     tri_csr_fill_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, row_comp, ckind, dc, indptr, slot_col, slot_val, a_col,
                                                         a_val);
     RBG_CUDA_TRY(cudaGetLastError());
+    std::vector<int32_t> kind(C);
+    RBG_CUDA_TRY(cudaMemcpyAsync(kind.data(), ckind, C * 4, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    int64_t candidates = 0;
+    for (size_t i = 0; i < C; ++i) candidates += kind[i] != KIND_NONE;
+    if (candidates == 0) {
+        timer_end(5, tdag, s);
+        return RBG_OK;
+    }
     rbg_csr_t A{R, R, indptr, a_col, a_val};
     int64_t dws = 0;
     int rc = rbg_dag_workspace_bytes(R, nnz_a, &dws);
@@ -480,34 +488,23 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(6, t, s);
     }
+    // 4. dense rows of the accepted matrices (decided on the device from the statistics)
+    {
+        cudaEvent_t t = timer_begin(7, s);
+        note_launches(1);
+        tri_write_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, out, dc, dpre, (int)count, ckind, cam,
+                                                                  row_off, row_len, p_col, p_val, rs);
+        RBG_CUDA_TRY(cudaGetLastError());
+        timer_end(7, t, s);
+    }
     std::vector<int> ham(C), hfm(C);
     std::vector<unsigned long long> hprod(C);
     RBG_CUDA_TRY(cudaMemcpyAsync(ham.data(), cam, C * 4, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaMemcpyAsync(hfm.data(), cfm, C * 4, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaMemcpyAsync(hprod.data(), cprod, C * 8, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    std::vector<unsigned char> fin(C, 0);
-    int64_t accepted = 0;
     for (size_t i = 0; i < C; ++i) {
         if (kind[i] == KIND_NONE || ham[i] >= TRI_TOP) continue;
-        fin[i] = 1;
-        ++accepted;
-    }
-    if (accepted == 0) return RBG_OK;
-    RBG_CUDA_TRY(cudaMemcpyAsync(cfinal, fin.data(), C, cudaMemcpyHostToDevice, s));
-
-    // 4. dense rows
-    {
-        cudaEvent_t t = timer_begin(7, s);
-        note_launches(1);
-        tri_write_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, out, dc, dpre, (int)count, cfinal, row_off,
-                                                                  row_len, p_col, p_val, rs);
-        RBG_CUDA_TRY(cudaGetLastError());
-        timer_end(7, t, s);
-    }
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    for (size_t i = 0; i < C; ++i) {
-        if (!fin[i]) continue;
         closed[i] = 1;
         rbg_result_t &r = results[i];
         r.status = RBG_OK;
