@@ -62,13 +62,14 @@ __device__ __forceinline__ int tri_find(const int64_t *__restrict__ prefix, int 
 
 // Off-diagonal entries of four consecutive columns j0 .. j0 + 3 held by each lane (m of them
 // valid): clean-regime flags, and the nonzeros appended to the row's slots in column order.
-__device__ __forceinline__ void tri_take(int32_t (&v)[4], int64_t j0, int m, int64_t i, int lane, int64_t g,
+// Column numbers fit 32 bits (n <= 8192 on this path).
+__device__ __forceinline__ void tri_take(int32_t (&v)[4], int j0, int m, int i, int lane, int64_t g,
                                          int32_t *__restrict__ slot_col, int32_t *__restrict__ slot_val,
                                          unsigned &flags, int &cnt) {
     int c4 = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int64_t j = j0 + k;
+        const int j = j0 + k;
         if (k >= m) {
             v[k] = 0;
         } else if (j == i) {
@@ -92,7 +93,7 @@ __device__ __forceinline__ void tri_take(int32_t (&v)[4], int64_t j0, int m, int
     for (int k = 0; k < 4; ++k) {
         if (v[k] != 0) {
             if (pos < TRI_CAP) {
-                slot_col[g * TRI_CAP + pos] = (int32_t)(j0 + k);
+                slot_col[g * TRI_CAP + pos] = j0 + k;
                 slot_val[g * TRI_CAP + pos] = v[k];
             }
             ++pos;
@@ -103,69 +104,68 @@ __device__ __forceinline__ void tri_take(int32_t (&v)[4], int64_t j0, int m, int
 
 // One warp per row: clean-regime test, side of the diagonal, the row's off-diagonal entries in
 // column order into its TRI_CAP slots (the count may exceed TRI_CAP: then only flagged).  The
-// row is read as 16-byte vectors from its first 16-byte boundary (scalar head and tail).  When
-// the output is another buffer, the row's zeros and diagonal are written there in the same
-// pass (a matrix that then leaves this path has its output rewritten by the blocked kernels).
-__global__ void __launch_bounds__(TRI_THREADS)
+// row is read as 16-byte vectors from its first 16-byte boundary (scalar head and tail), four
+// vectors per lane in flight; a vector of zeros (the common case) costs one vote.  When the
+// output is another buffer, the row's zeros and diagonal are written there in the same pass (a
+// matrix that then leaves this path has its output rewritten by the blocked kernels).
+__global__ void __launch_bounds__(TRI_THREADS, 5)
 tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
                 const int64_t *__restrict__ pre, int count, int32_t *__restrict__ slot_col,
                 int32_t *__restrict__ slot_val, int32_t *__restrict__ row_cnt, int32_t *__restrict__ row_comp,
                 unsigned *__restrict__ cflags) {
     const int ci = tri_find(pre, count, blockIdx.x);
     const TriComp c = comps[ci];
-    const int64_t i = ((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS + (threadIdx.x >> 5);
+    const int i = (int)(((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS) + (threadIdx.x >> 5);
     if (i >= c.n) return;                    // warp-uniform
     const int lane = threadIdx.x & 31;
-    const int64_t n = c.n, g = c.row_base + i;
-    const int32_t *row = in + c.in_off + i * n;
-    int32_t *orow = in == out ? nullptr : out + c.out_off + i * n;
-    const int64_t lead = (int64_t)((16 - ((uintptr_t)row & 15)) & 15) / 4;   // to the first boundary
-    const int head = (int)(lead < n ? lead : n);
-    const int64_t nv = (n - head) / 4;       // 16-byte vectors after the head
-    const int tail = (int)(n - head - 4 * nv);
+    const int n = (int)c.n;
+    const int64_t g = c.row_base + i;
+    const int32_t *row = in + c.in_off + (int64_t)i * n;
+    int32_t *orow = in == out ? nullptr : out + c.out_off + (int64_t)i * n;
+    const int lead = (int)(((16 - ((uintptr_t)row & 15)) & 15) / 4);   // to the first boundary
+    const int head = lead < n ? lead : n;
+    const int nv = (n - head) / 4;           // 16-byte vectors after the head
+    const int tail = n - head - 4 * nv;
     const bool ovec = orow && (((uintptr_t)orow - (uintptr_t)row) & 15) == 0;
     unsigned flags = 0;
     int cnt = 0;
     int32_t v[4];
-    // head: columns 0 .. head - 1, one per lane
-    if (head) {
+    if (head) {                              // columns 0 .. head - 1, one per lane
         v[0] = lane < head ? row[lane] : 0;
         if (orow && lane < head) orow[lane] = lane == i ? v[0] : 0;
         tri_take(v, lane, lane < head ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
     }
-    // four 16-byte vectors per lane in flight: vectors s0 + 32 u + lane (u = 0..3), taken in
-    // column order (u ascending)
-    for (int64_t s0 = 0; s0 < nv; s0 += 128) {
+    // vectors s0 + 32 u + lane (u = 0..3), taken in column order (u ascending)
+    for (int s0 = 0; s0 < nv; s0 += 128) {
         int4 x[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int64_t q = s0 + 32 * u + lane;
-            if (q < nv) x[u] = *reinterpret_cast<const int4 *>(row + head + 4 * q);
-            else x[u] = make_int4(0, 0, 0, 0);
+            const int q = s0 + 32 * u + lane;
+            x[u] = q < nv ? *reinterpret_cast<const int4 *>(row + head + 4 * q) : make_int4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int64_t q = s0 + 32 * u + lane;
-            const int64_t j0 = head + 4 * q;
-            v[0] = x[u].x; v[1] = x[u].y; v[2] = x[u].z; v[3] = x[u].w;
+            const int q = s0 + 32 * u + lane;
+            const int j0 = head + 4 * q;
+            const unsigned dd = (unsigned)(i - j0);          // < 4: the diagonal is in this vector
             if (orow && q < nv) {
-                int4 z = make_int4(0, 0, 0, 0);
-                if (i >= j0 && i < j0 + 4) {
-                    const int d = (int)(i - j0);
-                    if (d == 0) z.x = v[0]; else if (d == 1) z.y = v[1]; else if (d == 2) z.z = v[2]; else z.w = v[3];
-                }
+                const int4 z = make_int4(dd == 0 ? x[u].x : 0, dd == 1 ? x[u].y : 0, dd == 2 ? x[u].z : 0,
+                                         dd == 3 ? x[u].w : 0);
                 if (ovec) {
                     *reinterpret_cast<int4 *>(orow + j0) = z;
                 } else {
                     orow[j0] = z.x; orow[j0 + 1] = z.y; orow[j0 + 2] = z.z; orow[j0 + 3] = z.w;
                 }
             }
-            if (s0 + 32 * u < nv)            // warp-uniform: some lane holds a vector
+            // all-zero vectors (a zero diagonal included) leave nothing to take
+            if (__any_sync(0xffffffffu, (x[u].x | x[u].y | x[u].z | x[u].w) != 0)) {
+                v[0] = x[u].x; v[1] = x[u].y; v[2] = x[u].z; v[3] = x[u].w;
                 tri_take(v, j0, q < nv ? 4 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
+            }
         }
     }
     if (tail) {
-        const int64_t j = head + 4 * nv + lane;
+        const int j = head + 4 * nv + lane;
         v[0] = lane < tail ? row[j] : 0;
         if (orow && lane < tail) orow[j] = j == i ? v[0] : 0;
         tri_take(v, j, lane < tail ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
