@@ -469,7 +469,7 @@ __global__ void cc_dag_edges_kernel(int64_t n, const int64_t *__restrict__ indpt
 
 // one warp per vertex: the row statistics of dag_rows.cuh and the row's largest final value,
 // reduced per component
-__global__ void __launch_bounds__(32 * CCD_WARPS)
+__global__ void __launch_bounds__(32 * CCD_WARPS, 8)
 cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t *__restrict__ local,
                     const int64_t *__restrict__ start, const int32_t *__restrict__ comp_kind,
                     const int64_t *__restrict__ eptr, const int32_t *__restrict__ ecol, const int32_t *__restrict__ eval,

@@ -218,7 +218,7 @@ __global__ void tri_csr_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
 
 // One warp per row of a candidate matrix: the row statistics of dag_rows.cuh, reduced per
 // matrix (largest product MSB, largest first-value MSB, products).
-__global__ void __launch_bounds__(TRI_THREADS)
+__global__ void __launch_bounds__(TRI_THREADS, 8)
 tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                  const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
                  const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
