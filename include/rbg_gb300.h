@@ -456,7 +456,8 @@ int32_t rbg_cc_dag_edges(int64_t n, const int64_t *indptr, const int32_t *indice
  * final value, floored at 0 (the 'D' method's diameter source).  `edges` and `closure` are
  * device CSR matrices of n rows (int32 values).  Ordered on `stream`. */
 int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
-                         const int64_t *start, const int32_t *comp_kind, const rbg_csr_t *edges,
+                         const int64_t *start, const int32_t *sorted_vertex, const int32_t *comp_kind,
+                         const rbg_csr_t *edges,
                          const rbg_csr_t *closure, const int32_t *diag, int32_t *top_msb,
                          int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream);
 

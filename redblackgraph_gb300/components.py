@@ -193,7 +193,7 @@ def dag_component_closure(indptr: torch.Tensor, indices: torch.Tensor, data: tor
     cmax = torch.empty(k, dtype=torch.int32, device=dev)
     ec, cc = E.cstruct(), C.cstruct()
     _lib.check(L.rbg_cc_dag_stats(n, k, comps.label.data_ptr(), comps.local.data_ptr(), comps.start.data_ptr(),
-                                  kind.data_ptr(), ctypes.byref(ec), ctypes.byref(cc), diag.data_ptr(),
+                                  comps.sorted_vertex.data_ptr(), kind.data_ptr(), ctypes.byref(ec), ctypes.byref(cc), diag.data_ptr(),
                                   top.data_ptr(), first.data_ptr(), cmax.data_ptr(), sh), "cc_dag_stats")
     st = torch.stack([top, first, cmax]).cpu().numpy()
     if (st[0] >= 31).any():

@@ -471,7 +471,8 @@ __global__ void cc_dag_edges_kernel(int64_t n, const int64_t *__restrict__ indpt
 // reduced per component
 __global__ void __launch_bounds__(32 * CCD_WARPS, 8)
 cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t *__restrict__ local,
-                    const int64_t *__restrict__ start, const int32_t *__restrict__ comp_kind,
+                    const int64_t *__restrict__ start, const int32_t *__restrict__ sorted_vertex,
+                    const int32_t *__restrict__ comp_kind,
                     const int64_t *__restrict__ eptr, const int32_t *__restrict__ ecol, const int32_t *__restrict__ eval,
                     const int64_t *__restrict__ cptr, const int32_t *__restrict__ ccol, const int32_t *__restrict__ cval,
                     const int32_t *__restrict__ diag, int *__restrict__ top, int *__restrict__ first,
@@ -483,12 +484,18 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
         const int c = label[u];
         const int kind = comp_kind[c];
         if (kind == DAG_KIND_NONE) continue;         // warp-uniform
-        const int words = (int)((start[c + 1] - start[c] + 31) >> 5);
+        // a component whose vertices span fewer than DAG_MAX_N numbers indexes its bitmap by
+        // vertex - lowest vertex (no gather); otherwise by its local index
+        const int lo = sorted_vertex[start[c]], hi = sorted_vertex[start[c + 1] - 1];
         int am = -1, fm = -1;
         unsigned long long prods = 0;
-        dag_row_stats(bm_all[w], words, kind, u, eptr, ecol, eval,
-                      [&](int64_t r, int64_t &off, int &len) { off = cptr[r]; len = (int)(cptr[r + 1] - off); },
-                      ccol, cval, [&](int32_t col) { return local[col]; }, lane, am, fm, prods);
+        auto crow = [&](int64_t r, int64_t &off, int &len) { off = cptr[r]; len = (int)(cptr[r + 1] - off); };
+        if (hi - lo < DAG_MAX_N)
+            dag_row_stats(bm_all[w], (hi - lo + 32) >> 5, kind, u, eptr, ecol, eval, crow, ccol, cval,
+                          [&](int32_t col) { return col - lo; }, lane, am, fm, prods);
+        else
+            dag_row_stats(bm_all[w], (int)((start[c + 1] - start[c] + 31) >> 5), kind, u, eptr, ecol, eval, crow,
+                          ccol, cval, [&](int32_t col) { return local[col]; }, lane, am, fm, prods);
         int mx = 0;
         for (int64_t q = cptr[u] + lane; q < cptr[u + 1]; q += 32) mx = max(mx, cval[q]);
         if (lane == 0) mx = max(mx, diag[u]);
@@ -576,7 +583,8 @@ extern "C" int32_t rbg_cc_dag_edges(int64_t n, const int64_t *indptr, const int3
 }
 
 extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
-                                    const int64_t *start, const int32_t *comp_kind, const rbg_csr_t *edges,
+                                    const int64_t *start, const int32_t *sorted_vertex, const int32_t *comp_kind,
+                                    const rbg_csr_t *edges,
                                     const rbg_csr_t *closure, const int32_t *diag, int32_t *top_msb,
                                     int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream) {
     if (n < 0 || ncomp < 0 || !edges || !closure || (ncomp > 0 && (!top_msb || !first_msb || !comp_max)))
@@ -591,7 +599,7 @@ extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *lab
     if (n == 0) return RBG_OK;
     note_launches(1);
     cc_dag_stats_kernel<<<grid_for(n * 32, 32 * CCD_WARPS), 32 * CCD_WARPS, 0, s>>>(
-        n, label, local, start, comp_kind, edges->indptr, edges->indices, static_cast<const int32_t *>(edges->data),
+        n, label, local, start, sorted_vertex, comp_kind, edges->indptr, edges->indices, static_cast<const int32_t *>(edges->data),
         closure->indptr, closure->indices, static_cast<const int32_t *>(closure->data), diag, top_msb, first_msb,
         comp_max);
     RBG_CUDA_TRY(cudaGetLastError());

@@ -21,10 +21,9 @@
 // anything outside the clean regime, a row of more than TRI_CAP entries or n > 8192.
 //
 // Pipeline (one call): scan the dense rows (clean-regime test, which side of the diagonal, up
-// to TRI_CAP off-diagonal entries per row; the output's zeros and diagonal written in the same
-// pass) -> CSR of the candidate matrices with batch-global row numbers -> rbg_dag_closure ->
-// per-row statistics (largest product MSB, largest first-value MSB) -> the closure rows'
-// entries scattered into the dense rows of the accepted matrices.
+// to TRI_CAP off-diagonal entries per row) -> CSR of the candidate matrices with batch-global
+// row numbers -> rbg_dag_closure -> per-row statistics (largest product MSB, largest
+// first-value MSB) -> the dense rows of the accepted matrices written from the closure rows.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 #include <string.h>
@@ -105,11 +104,9 @@ __device__ __forceinline__ void tri_take(int32_t (&v)[4], int j0, int m, int i, 
 // One warp per row: clean-regime test, side of the diagonal, the row's off-diagonal entries in
 // column order into its TRI_CAP slots (the count may exceed TRI_CAP: then only flagged).  The
 // row is read as 16-byte vectors from its first 16-byte boundary (scalar head and tail), four
-// vectors per lane in flight; a vector of zeros (the common case) costs one vote.  When the
-// output is another buffer, the row's zeros and diagonal are written there in the same pass (a
-// matrix that then leaves this path has its output rewritten by the blocked kernels).
+// vectors per lane in flight; a vector of zeros (the common case) costs one vote.
 __global__ void __launch_bounds__(TRI_THREADS, 5)
-tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
+tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comps,
                 const int64_t *__restrict__ pre, int count, int32_t *__restrict__ slot_col,
                 int32_t *__restrict__ slot_val, int32_t *__restrict__ row_cnt, int32_t *__restrict__ row_comp,
                 unsigned *__restrict__ cflags) {
@@ -121,18 +118,15 @@ tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const
     const int n = (int)c.n;
     const int64_t g = c.row_base + i;
     const int32_t *row = in + c.in_off + (int64_t)i * n;
-    int32_t *orow = in == out ? nullptr : out + c.out_off + (int64_t)i * n;
     const int lead = (int)(((16 - ((uintptr_t)row & 15)) & 15) / 4);   // to the first boundary
     const int head = lead < n ? lead : n;
     const int nv = (n - head) / 4;           // 16-byte vectors after the head
     const int tail = n - head - 4 * nv;
-    const bool ovec = orow && (((uintptr_t)orow - (uintptr_t)row) & 15) == 0;
     unsigned flags = 0;
     int cnt = 0;
     int32_t v[4];
     if (head) {                              // columns 0 .. head - 1, one per lane
         v[0] = lane < head ? row[lane] : 0;
-        if (orow && lane < head) orow[lane] = lane == i ? v[0] : 0;
         tri_take(v, lane, lane < head ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
     }
     // vectors s0 + 32 u + lane (u = 0..3), taken in column order (u ascending)
@@ -147,16 +141,6 @@ tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const
         for (int u = 0; u < 4; ++u) {
             const int q = s0 + 32 * u + lane;
             const int j0 = head + 4 * q;
-            const unsigned dd = (unsigned)(i - j0);          // < 4: the diagonal is in this vector
-            if (orow && q < nv) {
-                const int4 z = make_int4(dd == 0 ? x[u].x : 0, dd == 1 ? x[u].y : 0, dd == 2 ? x[u].z : 0,
-                                         dd == 3 ? x[u].w : 0);
-                if (ovec) {
-                    *reinterpret_cast<int4 *>(orow + j0) = z;
-                } else {
-                    orow[j0] = z.x; orow[j0 + 1] = z.y; orow[j0 + 2] = z.z; orow[j0 + 3] = z.w;
-                }
-            }
             // all-zero vectors (a zero diagonal included) leave nothing to take
             if (__any_sync(0xffffffffu, (x[u].x | x[u].y | x[u].z | x[u].w) != 0)) {
                 v[0] = x[u].x; v[1] = x[u].y; v[2] = x[u].z; v[3] = x[u].w;
@@ -167,7 +151,6 @@ tri_scan_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const
     if (tail) {
         const int j = head + 4 * nv + lane;
         v[0] = lane < tail ? row[j] : 0;
-        if (orow && lane < tail) orow[j] = j == i ? v[0] : 0;
         tri_take(v, j, lane < tail ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
     }
     if (cnt > TRI_CAP) flags |= TF_WIDE;
@@ -249,24 +232,30 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
     }
 }
 
-// One warp per row of an accepted matrix: the closure row's entries into the dense row (its
-// other cells already hold the result: zeros and the diagonal, in place or written by the
-// scan), and the row statistics when asked for.
+constexpr int TRI_SEG = 512;                 // columns per shared-memory segment of a row
+
+// One warp per row of an accepted matrix.  Out of place, the whole dense row is written in
+// segments of TRI_SEG columns built in shared memory (zeros, the closure row's entries, the
+// diagonal) and stored as full 16-byte vectors on the row's 16-byte grid, so no DRAM line is
+// written partially; in place, only the closure's entries (the other cells already hold the
+// result).  The row statistics are recorded when asked for.
 __global__ void __launch_bounds__(TRI_THREADS)
 tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
                  const int64_t *__restrict__ pre, int count, const int32_t *__restrict__ ckind,
                  const int *__restrict__ cam,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, RowStats rs) {
+    __shared__ __align__(16) int32_t seg_all[TRI_ROWS][TRI_SEG];
     const int ci = tri_find(pre, count, blockIdx.x);
     if (ckind[ci] == KIND_NONE || cam[ci] >= TRI_TOP) return;   // not accepted (block-uniform)
     const TriComp c = comps[ci];
-    const int64_t i = ((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS + (threadIdx.x >> 5);
+    const int i = (int)(((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS) + (threadIdx.x >> 5);
     if (i >= c.n) return;                    // warp-uniform
     const int lane = threadIdx.x & 31;
-    const int64_t n = c.n, g = c.row_base + i;
-    const int32_t *rin = in + c.in_off + i * n;
-    int32_t *rout = out + c.out_off + i * n;
+    const int n = (int)c.n;
+    const int64_t g = c.row_base + i;
+    const int32_t *rin = in + c.in_off + (int64_t)i * n;
+    int32_t *rout = out + c.out_off + (int64_t)i * n;
     const int32_t diag = rin[i];
     const int64_t c0 = row_off[g];
     const int clen = row_len[g];
@@ -282,16 +271,62 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
         w3 |= t == 3 ? bit : 0ull;
     };
     int mx = 0;
-    for (int q = lane; q < clen; q += 32) {
-        const int j = p_col[c0 + q] - base;
-        const int32_t v = p_val[c0 + q];
-        rout[j] = v;
-        mx = max(mx, v);
-        mark(j >> 5);
+    if (rin == rout) {
+        for (int q = lane; q < clen; q += 32) {
+            const int j = p_col[c0 + q] - base;
+            const int32_t v = p_val[c0 + q];
+            rout[j] = v;
+            mx = max(mx, v);
+            mark(j >> 5);
+        }
+    } else {
+        int32_t *seg = seg_all[threadIdx.x >> 5];
+        // column j sits at j' = j + shift on the 16-byte grid; segment s0 holds j' in [s0, s0 + TRI_SEG)
+        const int shift = (int)(((uintptr_t)rout & 15) >> 2);
+        int e = 0;                           // first closure entry not yet placed (warp-uniform)
+        for (int s0 = 0; s0 < n + shift; s0 += TRI_SEG) {
+            for (int t = lane; t < TRI_SEG / 4; t += 32) reinterpret_cast<int4 *>(seg)[t] = make_int4(0, 0, 0, 0);
+            __syncwarp();
+            const int lim = s0 + TRI_SEG - shift;        // entries with j < lim belong to this segment
+            for (;;) {                                   // batches of 32 entries, ascending
+                const int q = e + lane;
+                int j = INT_MAX;
+                int32_t v = 0;
+                if (q < clen) {
+                    j = p_col[c0 + q] - base;
+                    v = p_val[c0 + q];
+                }
+                const bool here = j < lim;
+                if (here) {
+                    seg[j + shift - s0] = v;
+                    mx = max(mx, v);
+                    mark(j >> 5);
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, here);
+                e += __popc(bal);
+                if (bal != 0xffffffffu) break;
+            }
+            if (lane == 0 && i + shift >= s0 && i + shift < s0 + TRI_SEG) seg[i + shift - s0] = diag;
+            __syncwarp();
+            for (int t = lane; t < TRI_SEG / 4; t += 32) {
+                const int j0 = s0 + 4 * t - shift;
+                if (j0 >= n) break;
+                const int4 z = reinterpret_cast<const int4 *>(seg)[t];
+                if (j0 >= 0 && j0 + 4 <= n) {
+                    *reinterpret_cast<int4 *>(rout + j0) = z;
+                } else {                                 // the row's ragged ends
+                    const int zz[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (j0 + k >= 0 && j0 + k < n) rout[j0 + k] = zz[k];
+                }
+            }
+            __syncwarp();                                // before the next segment is zeroed
+        }
     }
     if (rs.row_count) {
         if (lane == 0 && diag != 0) {
-            mark((int)(i >> 5));
+            mark(i >> 5);
             mx = max(mx, diag);
         }
         auto orw = [](unsigned long long x) {
@@ -306,7 +341,8 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
             rs.row_count[rs.row_id ? (int64_t)rs.row_id[at] : at] = clen + (diag != 0 ? 1 : 0);
             if (rs.chunk_mask) {
                 const int64_t words = (n + 2047) / 2048;
-                unsigned long long *mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[ci] + ci + i * words;
+                unsigned long long *mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[ci] + ci +
+                                           (int64_t)i * words;
 #pragma unroll
                 for (int t = 0; t < 4; ++t)
                     if (t < words) mrow[t] = wd[t];
@@ -411,8 +447,8 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
     {
         cudaEvent_t t = timer_begin(4, s);
         note_launches(1);
-        tri_scan_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, out, dc, dpre, (int)count, slot_col,
-                                                                 slot_val, row_cnt, row_comp, cflags);
+        tri_scan_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, dc, dpre, (int)count, slot_col, slot_val,
+                                                                 row_cnt, row_comp, cflags);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(4, t, s);
     }
