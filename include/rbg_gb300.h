@@ -178,8 +178,13 @@ int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const i
  * rows of k's children (below) or pulls k's parents into the rows that reach k (above), so the
  * values are the DAG recurrence's and the diameter comes from each cell's first product in
  * step order.  A product that may reach the top bit sends the matrix to the blocked kernels.
- * The path allocates its scratch (device memory kept by the library between calls).
+ * The path allocates its scratch (device memory kept by the library between calls, released by
+ * rbg_release_scratch).
  */
+
+/* Free the device scratch the DAG path of rbg_fw_batch keeps between calls (waits for the
+ * device first).  The next call allocates it again. */
+int32_t rbg_release_scratch(void);
 
 /*
  * Row statistics rbg_fw_batch_rows records while it writes the closed matrices, so that a

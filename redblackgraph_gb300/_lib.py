@@ -108,6 +108,7 @@ SIGNATURES = [
                                     ctypes.POINTER(RbgResult), _P]),
     ("rbg_fw_batch_workspace_bytes", _I32, [_I32, _I64, _P, _U32, ctypes.POINTER(_I64)]),
     ("rbg_fw_batch", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, _P, _P]),
+    ("rbg_release_scratch", _I32, []),
     ("rbg_fw_batch_rows", _I32, [_I32, _I64, _P, _P, _P, _P, _U32, _P, _I64, ctypes.POINTER(RbgRowStats), _P, _P]),
     ("rbg_spgemm_head_bytes", _I32, [_I64, ctypes.POINTER(_I64)]),
     ("rbg_spgemm_count", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr),

@@ -554,3 +554,16 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
 }
 
 }  // namespace rbg
+
+extern "C" int32_t rbg_release_scratch(void) {
+    std::lock_guard<std::mutex> lk(rbg::g_tri_mu);
+    for (rbg::TriScratch *t : {&rbg::g_tri_a, &rbg::g_tri_b}) {
+        if (t->p) {
+            RBG_CUDA_TRY(cudaDeviceSynchronize());
+            RBG_CUDA_TRY(cudaFree(t->p));
+        }
+        t->p = nullptr;
+        t->cap = 0;
+    }
+    return RBG_OK;
+}

@@ -204,3 +204,17 @@ def test_dag_path_mixed_batch_and_opt_out(native):
         assert r2.status == r.status and r2.path != _lib.PATH_DAG
         if r.status == 0:
             assert (W == W2).all() and r.diameter == r2.diameter
+
+
+def test_dag_path_scratch_release(native):
+    """rbg_release_scratch frees the DAG path's device scratch; the next call allocates it again
+    and gives the same results."""
+    from redblackgraph_gb300 import synth, _lib
+    mats = [synth.pedigree(n, 9, n, dtype=np.int32) for n in (40, 300, 900)]
+    Ws, res = run_batch(mats)
+    assert all(r.path == _lib.PATH_DAG for r in res)
+    _lib.check(_lib.load().rbg_release_scratch(), "release_scratch")
+    _lib.check(_lib.load().rbg_release_scratch(), "release_scratch")     # twice is harmless
+    Ws2, res2 = run_batch(mats)
+    for W, W2, r, r2 in zip(Ws, Ws2, res, res2):
+        assert (W == W2).all() and r.diameter == r2.diameter and r2.path == _lib.PATH_DAG
