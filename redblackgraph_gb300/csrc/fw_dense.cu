@@ -1524,7 +1524,36 @@ extern "C" int32_t rbg_fw_dense_noalloc(int32_t dtype, int64_t n, const void *in
     return rc;
 }
 
+// Workspace sizes of recent batch layouts: a batch closed again (every step of a benchmark, a
+// serving arena) skips building its plan twice per call just to size the workspace.
+struct WsEntry {
+    int32_t dtype;
+    int triangular;
+    std::vector<int64_t> sizes;
+    size_t bytes;
+};
+static std::mutex g_ws_mu;
+static std::vector<WsEntry> g_ws_cache;
+
+static size_t batch_workspace_uncached(int32_t dtype, int64_t count, const int64_t *sizes, uint32_t mode);
+
 static size_t batch_workspace(int32_t dtype, int64_t count, const int64_t *sizes, uint32_t mode) {
+    const int tri = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
+    {
+        std::lock_guard<std::mutex> lk(g_ws_mu);
+        for (const auto &e : g_ws_cache)
+            if (e.dtype == dtype && e.triangular == tri && (int64_t)e.sizes.size() == count &&
+                (count == 0 || memcmp(e.sizes.data(), sizes, (size_t)count * 8) == 0))
+                return e.bytes;
+    }
+    const size_t b = batch_workspace_uncached(dtype, count, sizes, mode);
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    if (g_ws_cache.size() >= 4) g_ws_cache.erase(g_ws_cache.begin());
+    g_ws_cache.push_back(WsEntry{dtype, tri, std::vector<int64_t>(sizes, sizes + count), b});
+    return b;
+}
+
+static size_t batch_workspace_uncached(int32_t dtype, int64_t count, const int64_t *sizes, uint32_t mode) {
     std::vector<int64_t> off((size_t)count, 0);
     FwPlan P;
     build_plan(P, count, sizes, off.data(), off.data(), 4, (mode & RBG_MODE_TRIANGULAR) ? 1 : 0,

@@ -359,6 +359,9 @@ struct TriScratch {
 };
 std::mutex g_tri_mu;
 TriScratch g_tri_a, g_tri_b;
+// the matrix table and CTA prefix last uploaded into g_tri_a (a batch closed again skips the copy)
+std::vector<TriComp> g_tri_last_comps;
+const unsigned char *g_tri_last_buf = nullptr;
 
 int tri_reserve(TriScratch &s, size_t bytes, cudaStream_t st) {
     if (bytes <= s.cap) return RBG_OK;
@@ -366,6 +369,7 @@ int tri_reserve(TriScratch &s, size_t bytes, cudaStream_t st) {
     if (s.p) cudaFree(s.p);
     s.p = nullptr;
     s.cap = 0;
+    g_tri_last_buf = nullptr;
     const size_t want = bytes + bytes / 4;
     RBG_CUDA_TRY(cudaMalloc(reinterpret_cast<void **>(&s.p), want));
     s.cap = want;
@@ -439,8 +443,14 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const
     Carve cv{g_tri_a.p};
     layout(cv, dc, dpre, cflags, ckind, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr, tmp,
            a_col, a_val);
-    RBG_CUDA_TRY(cudaMemcpyAsync(dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
-    RBG_CUDA_TRY(cudaMemcpyAsync(dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
+    const bool same = g_tri_last_buf == g_tri_a.p && g_tri_last_comps.size() == C &&
+                      memcmp(g_tri_last_comps.data(), hc.data(), C * sizeof(TriComp)) == 0;
+    if (!same) {
+        RBG_CUDA_TRY(cudaMemcpyAsync(dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
+        RBG_CUDA_TRY(cudaMemcpyAsync(dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
+        g_tri_last_comps = hc;
+        g_tri_last_buf = g_tri_a.p;
+    }
     RBG_CUDA_TRY(cudaMemsetAsync(cflags, 0, C * 4, s));
 
     // 1. scan
@@ -565,5 +575,6 @@ extern "C" int32_t rbg_release_scratch(void) {
         t->p = nullptr;
         t->cap = 0;
     }
+    rbg::g_tri_last_buf = nullptr;
     return RBG_OK;
 }
