@@ -1,0 +1,78 @@
+"""The rule behind the DAG path, checked on the CPU against the oracle's sequential loop.
+
+For a matrix whose off-diagonal entries all lie below (or all above) the diagonal, the
+sequential Floyd-Warshall loop equals the DAG recurrence, and its diameter (the largest value
+ever written) is the largest first value of any cell: A(i, j), else the product of the first step
+that reaches the cell (below: the smallest parent k of i with j in C(k); above: the smallest k in
+C(i) with j a parent of k).  This restates that rule in plain Python (the GPU kernels implement
+it in fw_tri.cu / dag_rows.cuh) and compares it with the oracle on random DAGs, a third of which
+have a diameter above their final values' MSB."""
+import numpy as np
+
+from oracle import oracle as O
+
+
+def _msb(x):
+    return int(x).bit_length() - 1
+
+
+def _prod(x, y):
+    b = _msb(y)
+    return (x << b) | (y & ((1 << b) - 1))
+
+
+def _dag_rule(A):
+    n = A.shape[0]
+    par = {i: [j for j in range(n) if j != i and A[i, j] != 0] for i in range(n)}
+    above = any(j > i for i in range(n) for j in par[i])
+    C = {}
+    for i in (range(n - 1, -1, -1) if above else range(n)):
+        row = {j: int(A[i, j]) for j in par[i]}
+        for k in par[i]:
+            for j, v in C[k].items():
+                p = _prod(int(A[i, k]), v)
+                row[j] = min(row.get(j, p), p)
+        C[i] = row
+    top, first = -1, -1
+    for i in range(n):
+        seen = set(par[i])
+        first = max([first] + [_msb(A[i, j]) for j in par[i]])
+        for k in par[i]:                     # the recurrence's own candidates
+            for v in C[k].values():
+                top = max(top, _msb(A[i, k]) + _msb(v))
+        steps = ([(k, C[k].items(), _msb(A[i, k]), True) for k in par[i]] if not above else
+                 [(k, [(j, int(A[k, j])) for j in par[k]], _msb(C[i][k]), False) for k in sorted(C[i])])
+        for k, items, mk, _ in steps:
+            for j, v in sorted(items):
+                pm = mk + _msb(v)
+                top = max(top, pm)
+                if j not in seen:
+                    first = max(first, pm)
+                    seen.add(j)
+    W = A.copy()
+    for i in range(n):
+        for j, v in C[i].items():
+            W[i, j] = v
+    return W, max(first, 0), top
+
+
+def test_dag_rule_matches_the_sequential_loop():
+    rng = np.random.default_rng(1)
+    checked = differs = 0
+    for t in range(240):
+        n = int(rng.integers(1, 32))
+        A = np.zeros((n, n), np.int64)
+        low = np.tril(rng.random((n, n)) < rng.uniform(0.02, 0.5), -1)
+        A[low] = rng.integers(2, 8, size=int(low.sum()))
+        np.fill_diagonal(A, rng.choice([-1, 0, 1], size=n))
+        if t % 2:
+            A = A[::-1, ::-1].copy()
+        W, d, top = _dag_rule(A)
+        if top >= 31:                        # the GPU path hands these to the blocked kernels
+            continue
+        Wo, do, so, _ = O.warshall(A.astype(np.int32))
+        assert so == 0 and (W == Wo).all() and d == do, t
+        checked += 1
+        final = _msb(W[W > 1].max()) if (W > 1).any() else 0
+        differs += d != final
+    assert checked > 200 and differs > 30
