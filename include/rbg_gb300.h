@@ -434,8 +434,8 @@ int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *loca
  * Component-wise closure straight from the CSR graph (no dense blocks) when every component is
  * numbered in a topological order (its off-diagonal entries all below, or all above, the
  * diagonal) and in the clean regime: the DAG path of rbg_fw_batch applied to the graph.  The
- * sequence is rbg_cc_dag_classify -> rbg_cc_dag_edges -> rbg_dag_closure / rbg_dag_gather on
- * the edges -> rbg_cc_dag_stats -> rbg_cc_dag_merge_count / _fill; values and diameters are
+ * sequence is rbg_cc_dag_classify -> rbg_cc_dag_edges -> rbg_dag_closure on the edges (its row
+ * pool is read as it is) -> rbg_cc_dag_stats -> rbg_cc_dag_merge_count / _fill; values and diameters are
  * those of merge_component_matrices over the reference's per-component closures
  * (redblackgraph/sparse/csgraph/transitive_closure.py:85-195).  Components come from
  * rbg_cc_label; `workspace` is its workspace.
@@ -458,21 +458,23 @@ int32_t rbg_cc_dag_edges(int64_t n, const int64_t *indptr, const int32_t *indice
  * the largest MSB of the products the sequential loop performs (a component with top_msb >= 31
  * may overflow and must take the dense path), first_msb[c] = the largest MSB of any cell's
  * first value (the Floyd-Warshall diameter; -1 when there is none), comp_max[c] = the largest
- * final value, floored at 0 (the 'D' method's diameter source).  `edges` and `closure` are
- * device CSR matrices of n rows (int32 values).  Ordered on `stream`. */
+ * final value, floored at 0 (the 'D' method's diameter source).  `edges` is a device CSR matrix
+ * of n rows (int32 values); the closure rows are rbg_dag_closure's row pool as it left it
+ * (row_off, row_len, pool_cols, pool_vals).  Ordered on `stream`. */
 int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
                          const int64_t *start, const int32_t *sorted_vertex, const int32_t *comp_kind,
-                         const rbg_csr_t *edges,
-                         const rbg_csr_t *closure, const int32_t *diag, int32_t *top_msb,
-                         int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream);
+                         const rbg_csr_t *edges, const int64_t *row_off, const int32_t *row_len,
+                         const int32_t *pool_cols, const int32_t *pool_vals, const int32_t *diag,
+                         int32_t *top_msb, int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream);
 
-/* Row pointers (device, n + 1) of the merged matrix: each closure row plus its diagonal value
- * when nonzero; *nnz (host) its size.  Synchronises `stream`. */
-int32_t rbg_cc_dag_merge_count(int64_t n, const int64_t *closure_ptr, const int32_t *diag, void *workspace,
+/* Row pointers (device, n + 1) of the merged matrix: each closure row (row_len from the row
+ * pool) plus its diagonal value when nonzero; *nnz (host) its size.  Synchronises `stream`. */
+int32_t rbg_cc_dag_merge_count(int64_t n, const int32_t *row_len, const int32_t *diag, void *workspace,
                                int64_t workspace_bytes, int64_t *out_indptr, int64_t *nnz, rbg_stream_t stream);
 
-/* The merged matrix's columns (ascending) and values.  Ordered on `stream`. */
-int32_t rbg_cc_dag_merge_fill(int64_t n, const rbg_csr_t *closure, const int32_t *diag,
+/* The merged matrix's columns (ascending) and values, from the row pool.  Ordered on `stream`. */
+int32_t rbg_cc_dag_merge_fill(int64_t n, const int64_t *row_off, const int32_t *row_len,
+                              const int32_t *pool_cols, const int32_t *pool_vals, const int32_t *diag,
                               const int64_t *out_indptr, int32_t *out_indices, int32_t *out_data,
                               rbg_stream_t stream);
 

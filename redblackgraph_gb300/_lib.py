@@ -133,10 +133,10 @@ SIGNATURES = [
     ("rbg_cc_compact_scan", _I32, [_I64, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
     ("rbg_cc_dag_classify", _I32, [_I64, _P, _P, _P, _P, _P, _I64, _P, _I64, _P, _P, _P, ctypes.POINTER(_I64), _P]),
     ("rbg_cc_dag_edges", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P]),
-    ("rbg_cc_dag_stats", _I32, [_I64, _I64, _P, _P, _P, _P, _P, ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr),
-                                _P, _P, _P, _P, _P]),
+    ("rbg_cc_dag_stats", _I32, [_I64, _I64, _P, _P, _P, _P, _P, ctypes.POINTER(RbgCsr), _P, _P, _P, _P, _P,
+                                _P, _P, _P, _P]),
     ("rbg_cc_dag_merge_count", _I32, [_I64, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), _P]),
-    ("rbg_cc_dag_merge_fill", _I32, [_I64, ctypes.POINTER(RbgCsr), _P, _P, _P, _P, _P]),
+    ("rbg_cc_dag_merge_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("rbg_cc_compact_fill", _I32, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("rbg_relationship_lookup", _I32, [_I64, _P, _P, _P]),
     ("rbg_dag_workspace_bytes", _I32, [_I64, _I64, ctypes.POINTER(_I64)]),

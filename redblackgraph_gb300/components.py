@@ -185,27 +185,29 @@ def dag_component_closure(indptr: torch.Tensor, indices: torch.Tensor, data: tor
                "cc_dag_edges")
     E = DeviceCSR(eptr, ecol[:ne.value], evals[:ne.value], (n, n))
     try:
-        C, _, _ = dag_closure_device(E, stream)
+        C, _, _ = dag_closure_device(E, stream, gather=False)    # the row pool, read in place
     except RowTooWide:
         return None
     top = torch.empty(k, dtype=torch.int32, device=dev)
     first = torch.empty(k, dtype=torch.int32, device=dev)
     cmax = torch.empty(k, dtype=torch.int32, device=dev)
-    ec, cc = E.cstruct(), C.cstruct()
+    ec = E.cstruct()
+    pool = (C.row_off.data_ptr(), C.row_len.data_ptr(), C.cols.data_ptr(), C.vals.data_ptr())
     _lib.check(L.rbg_cc_dag_stats(n, k, comps.label.data_ptr(), comps.local.data_ptr(), comps.start.data_ptr(),
-                                  comps.sorted_vertex.data_ptr(), kind.data_ptr(), ctypes.byref(ec), ctypes.byref(cc), diag.data_ptr(),
-                                  top.data_ptr(), first.data_ptr(), cmax.data_ptr(), sh), "cc_dag_stats")
+                                  comps.sorted_vertex.data_ptr(), kind.data_ptr(), ctypes.byref(ec), *pool,
+                                  diag.data_ptr(), top.data_ptr(), first.data_ptr(), cmax.data_ptr(), sh),
+               "cc_dag_stats")
     st = torch.stack([top, first, cmax]).cpu().numpy()
     if (st[0] >= 31).any():
         return None
     oi = torch.empty(n + 1, dtype=torch.int64, device=dev)
     nnz = ctypes.c_int64(0)
-    _lib.check(L.rbg_cc_dag_merge_count(n, C.indptr.data_ptr(), diag.data_ptr(), ws.data_ptr(), ws.numel(),
+    _lib.check(L.rbg_cc_dag_merge_count(n, C.row_len.data_ptr(), diag.data_ptr(), ws.data_ptr(), ws.numel(),
                                         oi.data_ptr(), ctypes.byref(nnz), sh), "cc_dag_merge_count")
     oj = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
     ov = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
-    _lib.check(L.rbg_cc_dag_merge_fill(n, ctypes.byref(cc), diag.data_ptr(), oi.data_ptr(), oj.data_ptr(),
-                                       ov.data_ptr(), sh), "cc_dag_merge_fill")
+    _lib.check(L.rbg_cc_dag_merge_fill(n, *pool, diag.data_ptr(), oi.data_ptr(), oj.data_ptr(), ov.data_ptr(), sh),
+               "cc_dag_merge_fill")
     fw = component_methods(comps.sizes, k, method, densify_threshold)
     diameter = 0
     if fw.any():

@@ -474,7 +474,8 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
                     const int64_t *__restrict__ start, const int32_t *__restrict__ sorted_vertex,
                     const int32_t *__restrict__ comp_kind,
                     const int64_t *__restrict__ eptr, const int32_t *__restrict__ ecol, const int32_t *__restrict__ eval,
-                    const int64_t *__restrict__ cptr, const int32_t *__restrict__ ccol, const int32_t *__restrict__ cval,
+                    const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
+                    const int32_t *__restrict__ ccol, const int32_t *__restrict__ cval,
                     const int32_t *__restrict__ diag, int *__restrict__ top, int *__restrict__ first,
                     int *__restrict__ cmax) {
     __shared__ unsigned bm_all[CCD_WARPS][DAG_MAX_N / 32];
@@ -489,7 +490,7 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
         const int lo = sorted_vertex[start[c]], hi = sorted_vertex[start[c + 1] - 1];
         int am = -1, fm = -1;
         unsigned long long prods = 0;
-        auto crow = [&](int64_t r, int64_t &off, int &len) { off = cptr[r]; len = (int)(cptr[r + 1] - off); };
+        auto crow = [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; };
         if (hi - lo < DAG_MAX_N)
             dag_row_stats(bm_all[w], (hi - lo + 32) >> 5, kind, u, eptr, ecol, eval, crow, ccol, cval,
                           [&](int32_t col) { return col - lo; }, lane, am, fm, prods);
@@ -497,7 +498,7 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
             dag_row_stats(bm_all[w], (int)((start[c + 1] - start[c] + 31) >> 5), kind, u, eptr, ecol, eval, crow,
                           ccol, cval, [&](int32_t col) { return local[col]; }, lane, am, fm, prods);
         int mx = 0;
-        for (int64_t q = cptr[u] + lane; q < cptr[u + 1]; q += 32) mx = max(mx, cval[q]);
+        for (int64_t q = row_off[u] + lane; q < row_off[u] + row_len[u]; q += 32) mx = max(mx, cval[q]);
         if (lane == 0) mx = max(mx, diag[u]);
         am = __reduce_max_sync(0xffffffffu, am);
         fm = __reduce_max_sync(0xffffffffu, fm);
@@ -510,21 +511,22 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
     }
 }
 
-__global__ void cc_dag_merge_count_kernel(int64_t n, const int64_t *__restrict__ cptr, const int32_t *__restrict__ diag,
+__global__ void cc_dag_merge_count_kernel(int64_t n, const int32_t *__restrict__ row_len, const int32_t *__restrict__ diag,
                                           int64_t *__restrict__ cnt) {
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
-        cnt[u] = (cptr[u + 1] - cptr[u]) + (diag[u] != 0 ? 1 : 0);
+        cnt[u] = row_len[u] + (diag[u] != 0 ? 1 : 0);
 }
 
 // one warp per vertex: the closure row with the diagonal value put in its place
-__global__ void cc_dag_merge_fill_kernel(int64_t n, const int64_t *__restrict__ cptr, const int32_t *__restrict__ ccol,
+__global__ void cc_dag_merge_fill_kernel(int64_t n, const int64_t *__restrict__ row_off,
+                                         const int32_t *__restrict__ row_len, const int32_t *__restrict__ ccol,
                                          const int32_t *__restrict__ cval, const int32_t *__restrict__ diag,
                                          const int64_t *__restrict__ optr, int32_t *__restrict__ ocol,
                                          int32_t *__restrict__ oval) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += warps) {
-        const int64_t c0 = cptr[u], c1 = cptr[u + 1], o = optr[u];
+        const int64_t c0 = row_off[u], c1 = c0 + row_len[u], o = optr[u];
         const int32_t d = diag[u];
         int below = 0;                                  // closure entries left of the diagonal
         for (int64_t q = c0 + lane; q < c1; q += 32) below += ccol[q] < u;
@@ -584,12 +586,12 @@ extern "C" int32_t rbg_cc_dag_edges(int64_t n, const int64_t *indptr, const int3
 
 extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *label, const int32_t *local,
                                     const int64_t *start, const int32_t *sorted_vertex, const int32_t *comp_kind,
-                                    const rbg_csr_t *edges,
-                                    const rbg_csr_t *closure, const int32_t *diag, int32_t *top_msb,
-                                    int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream) {
-    if (n < 0 || ncomp < 0 || !edges || !closure || (ncomp > 0 && (!top_msb || !first_msb || !comp_max)))
+                                    const rbg_csr_t *edges, const int64_t *row_off, const int32_t *row_len,
+                                    const int32_t *pool_cols, const int32_t *pool_vals, const int32_t *diag,
+                                    int32_t *top_msb, int32_t *first_msb, int32_t *comp_max, rbg_stream_t stream) {
+    if (n < 0 || ncomp < 0 || !edges || (ncomp > 0 && (!top_msb || !first_msb || !comp_max)))
         return RBG_ERR_INVALID;
-    if (edges->n_rows != n || closure->n_rows != n) return RBG_ERR_INVALID;
+    if (edges->n_rows != n || (n > 0 && (!row_off || !row_len))) return RBG_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (ncomp > 0) {
         RBG_CUDA_TRY(cudaMemsetAsync(top_msb, 0xff, (size_t)ncomp * 4, s));
@@ -600,23 +602,22 @@ extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *lab
     note_launches(1);
     cc_dag_stats_kernel<<<grid_for(n * 32, 32 * CCD_WARPS), 32 * CCD_WARPS, 0, s>>>(
         n, label, local, start, sorted_vertex, comp_kind, edges->indptr, edges->indices, static_cast<const int32_t *>(edges->data),
-        closure->indptr, closure->indices, static_cast<const int32_t *>(closure->data), diag, top_msb, first_msb,
-        comp_max);
+        row_off, row_len, pool_cols, pool_vals, diag, top_msb, first_msb, comp_max);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }
 
-extern "C" int32_t rbg_cc_dag_merge_count(int64_t n, const int64_t *closure_ptr, const int32_t *diag, void *workspace,
+extern "C" int32_t rbg_cc_dag_merge_count(int64_t n, const int32_t *row_len, const int32_t *diag, void *workspace,
                                           int64_t workspace_bytes, int64_t *out_indptr, int64_t *nnz,
                                           rbg_stream_t stream) {
-    if (n < 0 || !workspace || !nnz || !out_indptr || (n > 0 && (!closure_ptr || !diag))) return RBG_ERR_INVALID;
+    if (n < 0 || !workspace || !nnz || !out_indptr || (n > 0 && (!row_len || !diag))) return RBG_ERR_INVALID;
     if (workspace_bytes < (int64_t)cc_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
     CcWs w;
     cc_layout(n, reinterpret_cast<unsigned char *>(workspace), &w);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (n > 0) {
         note_launches(1);
-        cc_dag_merge_count_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, closure_ptr, diag, out_indptr);
+        cc_dag_merge_count_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, row_len, diag, out_indptr);
         RBG_CUDA_TRY(cudaGetLastError());
     }
     RBG_CUDA_TRY(cudaMemsetAsync(out_indptr + n, 0, 8, s));
@@ -627,17 +628,16 @@ extern "C" int32_t rbg_cc_dag_merge_count(int64_t n, const int64_t *closure_ptr,
     return RBG_OK;
 }
 
-extern "C" int32_t rbg_cc_dag_merge_fill(int64_t n, const rbg_csr_t *closure, const int32_t *diag,
+extern "C" int32_t rbg_cc_dag_merge_fill(int64_t n, const int64_t *row_off, const int32_t *row_len,
+                                         const int32_t *pool_cols, const int32_t *pool_vals, const int32_t *diag,
                                          const int64_t *out_indptr, int32_t *out_indices, int32_t *out_data,
                                          rbg_stream_t stream) {
-    if (n < 0 || !closure || (n > 0 && (!diag || !out_indptr))) return RBG_ERR_INVALID;
-    if (closure->n_rows != n) return RBG_ERR_INVALID;
+    if (n < 0 || (n > 0 && (!row_off || !row_len || !diag || !out_indptr))) return RBG_ERR_INVALID;
     if (n == 0) return RBG_OK;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     note_launches(1);
-    cc_dag_merge_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(
-        n, closure->indptr, closure->indices, static_cast<const int32_t *>(closure->data), diag, out_indptr,
-        out_indices, out_data);
+    cc_dag_merge_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(n, row_off, row_len, pool_cols, pool_vals, diag,
+                                                                   out_indptr, out_indices, out_data);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }

@@ -10,6 +10,7 @@ library reports it too small.
 from __future__ import annotations
 
 import ctypes
+from dataclasses import dataclass
 
 import numpy as np
 import torch
@@ -23,11 +24,23 @@ class RowTooWide(RuntimeError):
     """A closure row has more distinct columns than the level kernels hold (8192)."""
 
 
-def dag_closure_device(A: DeviceCSR, stream=None, pool_factor: int = 16):
+@dataclass
+class DagRows:
+    """The closure's rows as rbg_dag_closure leaves them in its row pool: row v is
+    cols[row_off[v]:row_off[v] + row_len[v]] (columns ascending) with its values in vals."""
+    cols: torch.Tensor
+    vals: torch.Tensor
+    row_off: torch.Tensor      # int64 [n]
+    row_len: torch.Tensor      # int32 [n]
+    nnz: int
+
+
+def dag_closure_device(A: DeviceCSR, stream=None, pool_factor: int = 16, gather: bool = True):
     """Closure of the DAG ``A`` (int32 values).  Returns ``(C, max_abs, levels)``: the closure as
-    a DeviceCSR (int64 row pointers, int32 indices and values, rows sorted), the largest magnitude
-    among A's entries and all candidates (the reference's diameter source) and the number of
-    topological levels.  Raises CycleError on a cycle and RowTooWide for rows past 8192 columns."""
+    a DeviceCSR (int64 row pointers, int32 indices and values, rows sorted) -- or, with
+    ``gather=False``, as the row pool itself (``DagRows``) -- the largest magnitude among A's
+    entries and all candidates (the reference's diameter source) and the number of topological
+    levels.  Raises CycleError on a cycle and RowTooWide for rows past 8192 columns."""
     from .dense import CycleError
     if A.data.dtype != torch.int32:
         raise TypeError("the DAG closure takes int32 values")
@@ -64,6 +77,8 @@ def dag_closure_device(A: DeviceCSR, stream=None, pool_factor: int = 16):
         _lib.check(rc, "dag_closure")
         break
     total = int(nnz.value)
+    if not gather:
+        return DagRows(cols, vals, row_off, row_len, total), int(mx.value), int(lv.value)
     gb = ctypes.c_int64(0)
     _lib.check(L.rbg_dag_gather_workspace_bytes(n, ctypes.byref(gb)), "dag_gather")
     gws = torch.empty(max(gb.value, 256), dtype=torch.uint8, device=dev)
