@@ -356,6 +356,7 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
 struct TriScratch {
     unsigned char *p = nullptr;
     size_t cap = 0;
+    int device = -1;                         // the device the buffer lives on
 };
 std::mutex g_tri_mu;
 TriScratch g_tri_a, g_tri_b;
@@ -363,16 +364,27 @@ TriScratch g_tri_a, g_tri_b;
 std::vector<TriComp> g_tri_last_comps;
 const unsigned char *g_tri_last_buf = nullptr;
 
+// A buffer on another device than the calling thread's current one is freed and allocated
+// again on the current device (a process may drive several GPUs, one at a time per call).
 int tri_reserve(TriScratch &s, size_t bytes, cudaStream_t st) {
-    if (bytes <= s.cap) return RBG_OK;
+    int dev = 0;
+    RBG_CUDA_TRY(cudaGetDevice(&dev));
+    if (bytes <= s.cap && dev == s.device) return RBG_OK;
     RBG_CUDA_TRY(cudaStreamSynchronize(st));
-    if (s.p) cudaFree(s.p);
+    if (s.p) {                               // freed on its own device, after its work
+        if (s.device != dev) RBG_CUDA_TRY(cudaSetDevice(s.device));
+        RBG_CUDA_TRY(cudaDeviceSynchronize());
+        cudaFree(s.p);
+        if (s.device != dev) RBG_CUDA_TRY(cudaSetDevice(dev));
+    }
     s.p = nullptr;
     s.cap = 0;
+    s.device = -1;
     g_tri_last_buf = nullptr;
     const size_t want = bytes + bytes / 4;
     RBG_CUDA_TRY(cudaMalloc(reinterpret_cast<void **>(&s.p), want));
     s.cap = want;
+    s.device = dev;
     return RBG_OK;
 }
 
@@ -569,11 +581,16 @@ extern "C" int32_t rbg_release_scratch(void) {
     std::lock_guard<std::mutex> lk(rbg::g_tri_mu);
     for (rbg::TriScratch *t : {&rbg::g_tri_a, &rbg::g_tri_b}) {
         if (t->p) {
+            int cur = 0;
+            RBG_CUDA_TRY(cudaGetDevice(&cur));
+            if (t->device != cur) RBG_CUDA_TRY(cudaSetDevice(t->device));
             RBG_CUDA_TRY(cudaDeviceSynchronize());
             RBG_CUDA_TRY(cudaFree(t->p));
+            if (t->device != cur) RBG_CUDA_TRY(cudaSetDevice(cur));
         }
         t->p = nullptr;
         t->cap = 0;
+        t->device = -1;
     }
     rbg::g_tri_last_buf = nullptr;
     return RBG_OK;
