@@ -3,9 +3,10 @@
  *
  * One shared library, librbg_gb300.so, exports every entry point below.  Conventions:
  *   - plain pointers and sizes only; device buffers are owned by the caller;
- *   - the library never allocates device memory behind the caller's back: every entry
- *     point that needs scratch takes a caller-provided `workspace` whose size the matching
- *     *_workspace_bytes query returns;
+ *   - every entry point that needs scratch takes a caller-provided `workspace` whose size
+ *     the matching *_workspace_bytes query returns; the one exception is the DAG path of
+ *     rbg_fw_batch (its scratch depends on the closure's size), which keeps library-owned
+ *     device memory between calls (rbg_release_scratch frees it, RBG_MODE_NO_DAG avoids it);
  *   - each call is ordered on the caller's CUDA stream (`stream`, a cudaStream_t; 0 is the
  *     legacy default stream); calls that report a status synchronise that stream before
  *     they return;
@@ -16,6 +17,9 @@
  *   AVOS algebra       redblackgraph/core/src/redblackgraph/rbg_math.c.in:30-121
  *   dense closure      redblackgraph/core/src/redblackgraph/warshall.c.in:51-135
  *                      redblackgraph/sparse/csgraph/_shortest_path.pyx:213-389
+ *   component closure  redblackgraph/sparse/csgraph/transitive_closure.py:85-195,
+ *                      redblackgraph/sparse/csgraph/_components.pyx:86-344
+ *   DAG closure        redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:168-351
  *   dense product      redblackgraph/core/src/redblackgraph/redblack.c.src:554-594
  *   sparse product     redblackgraph/sparse/sparsetools/rbm_math.h:117-222,
  *                      redblackgraph/gpu/spgemm.py:32-119
