@@ -7,9 +7,10 @@ than pedigrees) are closed in one batched run per step.  The metric is AVOS rela
 the algorithmic count sum(n^3) over the components (the reference's C warshall performs all n^3
 relaxations of every component).
 
-  value  batched closure with the dense blocks resident in HBM (CUDA events on the stream)
+  value  batched closure with the dense blocks resident in HBM (CUDA events on the stream);
+         every component is numbered oldest first, so the batch takes the DAG path
   e2e    component_wise_closure on the forest in pinned host memory: CSR upload, component
-         split, densify, batched closure, compaction and download of the merged CSR per step
+         split, the closure straight from the CSR graph and download of the merged CSR per step
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -343,10 +344,11 @@ def run_blocked(args, buf, sizes, offsets, out, mode):
 
 
 def run_e2e(args, rank, world, w, dev, work_per_step):
-    from redblackgraph_gb300.sharding import max_over_ranks
     """The same closure through the public API with host buffers: component_wise_closure on the
-    forest held in pinned host memory (H2D of the CSR, component split, densify, batched
-    closure, compaction, D2H of the merged CSR inside every timed step)."""
+    forest held in pinned host memory (H2D of the CSR, component split, the closure straight
+    from the CSR graph -- or, for components not numbered in a topological order, densify,
+    batched closure and compaction -- and D2H of the merged CSR inside every timed step)."""
+    from redblackgraph_gb300.sharding import max_over_ranks
     import torch
     import torch.distributed as dist
     import scipy.sparse as sp
