@@ -315,7 +315,7 @@ def run_ours(args, rank, world, w):
     res = dict(t=t, work=work_per_step, executed=executed, kprof=kprof, launches=launches,
                clocks=clocks, out=out, offsets=offsets, bytes=buf.numel() * 4,
                cells=float((sizes.astype(np.float64) ** 2).sum()), paths=paths)
-    if args.secondary:
+    if args.secondary and rank == 0:
         res["blocked"] = run_blocked(args, buf, sizes, offsets, out, mode | _lib.MODE_NO_DAG)
     del buf, blocks
     res["e2e"] = run_e2e(args, rank, world, w, dev, work_per_step)
