@@ -32,3 +32,29 @@ def test_workspace_queries_without_gpu(native):
     assert n.value >= 1024 * 1024 * 4
     assert native.rbg_fw_dense_workspace_bytes(99, 10, 0, ctypes.byref(n)) == _lib.RBG_ERR_INVALID
     assert native.rbg_version() > 0
+
+
+def test_batch_workspace_sizes_are_stable(native):
+    """rbg_fw_batch_workspace_bytes (host only) gives the same size for a layout asked again (the
+    answer is cached per layout), distinguishes layouts, dtypes and the triangular mode, and grows
+    with the batch."""
+    import numpy as np
+
+    def size(sizes, dtype=4, mode=0):
+        s = np.ascontiguousarray(sizes, dtype=np.int64)
+        b = ctypes.c_int64(0)
+        assert native.rbg_fw_batch_workspace_bytes(dtype, s.size, s.ctypes.data, mode, ctypes.byref(b)) == 0
+        return b.value
+
+    a = [16, 300, 4096, 17, 1]
+    first = size(a)
+    assert all(size(a) == first for _ in range(3))
+    assert size(a + [200]) > first
+    assert size(a, dtype=6) != first                 # 64-bit storage: other lane buffers
+    for k in range(6):                               # more layouts than the cache holds
+        size([64 * (k + 1)] * 3)
+    assert size(a) == first
+    assert size([]) >= 0
+    bad = np.array([-1], np.int64)
+    out = ctypes.c_int64(0)
+    assert native.rbg_fw_batch_workspace_bytes(4, 1, bad.ctypes.data, 0, ctypes.byref(out)) != 0
