@@ -76,3 +76,33 @@ def test_dag_rule_matches_the_sequential_loop():
         final = _msb(W[W > 1].max()) if (W > 1).any() else 0
         differs += d != final
     assert checked > 200 and differs > 30
+
+
+def test_dag_rule_matches_the_reference_itself():
+    """The same rule against the reference's own C warshall (where the reference is mounted and
+    built: not on the GPU host)."""
+    import pytest
+    from oracle import refimport
+    if not refimport.available():
+        pytest.skip("reference not available here")
+    refimport.load()
+    import redblackgraph.core as core
+    from redblackgraph.core.redblack import array as rb_array
+    rng = np.random.default_rng(7)
+    checked = 0
+    for t in range(60):
+        n = int(rng.integers(2, 28))
+        A = np.zeros((n, n), np.int64)
+        low = np.tril(rng.random((n, n)) < rng.uniform(0.05, 0.4), -1)
+        A[low] = rng.integers(2, 8, size=int(low.sum()))
+        np.fill_diagonal(A, rng.choice([-1, 1], size=n))
+        if t % 2:
+            A = A[::-1, ::-1].copy()
+        W, d, top = _dag_rule(A)
+        if top >= 31:
+            continue
+        A32 = A.astype(np.int32)
+        Wr, dr = core.warshall(np.stack([A32, A32]).view(rb_array))
+        assert (np.asarray(Wr[0]) == W).all() and int(np.asarray(dr).reshape(-1)[0]) == d, t
+        checked += 1
+    assert checked > 40
