@@ -106,3 +106,67 @@ def test_dag_rule_matches_the_reference_itself():
         assert (np.asarray(Wr[0]) == W).all() and int(np.asarray(dr).reshape(-1)[0]) == d, t
         checked += 1
     assert checked > 40
+
+
+def _replay_on_pattern(A):
+    """The sequential loop replayed only on the final closure's pattern (reachability), with the
+    evolving values: for step k, the rows whose final pattern holds column k, merged with row k's
+    current non-zeros.  Returns (W, diameter, largest product MSB)."""
+    n = A.shape[0]
+    reach = [set(j for j in range(n) if j != i and A[i, j] != 0) for i in range(n)]
+    changed = True
+    while changed:                                    # the pattern: plain reachability
+        changed = False
+        for i in range(n):
+            new = set().union(*(reach[k] for k in reach[i])) - reach[i] - {i} if reach[i] else set()
+            if new:
+                reach[i] |= new
+                changed = True
+    col = [[i for i in range(n) if k in reach[i]] for k in range(n)]
+    cur = {i: {j: int(A[i, j]) for j in reach[i] if A[i, j] != 0} for i in range(n)}
+    first = max([_msb(v) for i in range(n) for v in cur[i].values()] + [-1])
+    top = -1
+    for k in range(n):
+        rowk = list(cur[k].items())
+        for i in col[k]:
+            x = cur[i].get(k, 0)
+            if x == 0:
+                continue
+            for j, y in rowk:
+                if j == i:
+                    continue
+                p = _prod(x, y)
+                top = max(top, _msb(p))
+                old = cur[i].get(j, 0)
+                if old == 0:
+                    first = max(first, _msb(p))
+                    cur[i][j] = p
+                else:
+                    cur[i][j] = min(old, p)
+    W = A.copy()
+    for i in range(n):
+        for j, v in cur[i].items():
+            W[i, j] = v
+    return W, max(first, 0), top
+
+
+def test_replay_on_the_pattern_matches_in_any_numbering():
+    """For components numbered in any order (the plan for the ones the DAG path does not take):
+    the loop replayed on the final pattern gives the oracle's values and diameter."""
+    rng = np.random.default_rng(3)
+    checked = 0
+    for t in range(120):
+        n = int(rng.integers(2, 26))
+        A = np.zeros((n, n), np.int64)
+        low = np.tril(rng.random((n, n)) < rng.uniform(0.05, 0.4), -1)
+        A[low] = rng.integers(2, 8, size=int(low.sum()))
+        np.fill_diagonal(A, rng.choice([-1, 0, 1], size=n))
+        p = rng.permutation(n)
+        A = A[p][:, p]                                # any numbering
+        W, d, top = _replay_on_pattern(A)
+        if top >= 31:
+            continue
+        Wo, do, so, _ = O.warshall(A.astype(np.int32))
+        assert so == 0 and (W == Wo).all() and d == do, t
+        checked += 1
+    assert checked > 80
