@@ -4,9 +4,8 @@
  * One shared library, librbg_gb300.so, exports every entry point below.  Conventions:
  *   - plain pointers and sizes only; device buffers are owned by the caller;
  *   - every entry point that needs scratch takes a caller-provided `workspace` whose size
- *     the matching *_workspace_bytes query returns; the one exception is the DAG path of
- *     rbg_fw_batch (its scratch depends on the closure's size), which keeps library-owned
- *     device memory between calls (rbg_release_scratch frees it, RBG_MODE_NO_DAG avoids it);
+ *     the matching *_workspace_bytes query returns; no entry point allocates device memory
+ *     behind the caller (rbg_fw_dense_noalloc uses a fixed array compiled into the library);
  *   - each call is ordered on the caller's CUDA stream (`stream`, a cudaStream_t; 0 is the
  *     legacy default stream); calls that report a status synchronise that stream before
  *     they return;
@@ -72,22 +71,24 @@ typedef void *rbg_stream_t; /* a cudaStream_t */
 #define RBG_MODE_TRIANGULAR 2u  /* assume_upper_triangular loop (_shortest_path.pyx:365) */
 #define RBG_MODE_FORCE_EXACT 4u /* always run the sequential-order kernel                */
 #define RBG_MODE_FORCE_WIDE 8u  /* 64-bit storage: skip the 32-bit lane attempt          */
-#define RBG_MODE_GRAPH 16u      /* rbg_fw_batch: record the launch sequence as a CUDA graph
-                                   and replay it on later calls with the same sizes,
-                                   offsets, buffers and workspace (small LRU cache)      */
+#define RBG_MODE_GRAPH 16u      /* rbg_fw_batch, rbg_fw_dense: record the launch sequence as
+                                   a CUDA graph and replay it on later calls with the same
+                                   sizes, offsets, buffers and workspace (small LRU cache);
+                                   the DAG path's level loop is a while node the device ends,
+                                   so a call is one graph launch and one read of results   */
 #define RBG_MODE_TILE_NARROW 32u /* rbg_fw_batch: 128 x 64 phase-3 tiles in every round   */
 #define RBG_MODE_AUTOTUNE 64u   /* rbg_fw_batch: per-round tile shape chosen by timing both
                                    shapes on the first call for a batch layout (the first
                                    call closes the batch twice; not when in == out)      */
-#define RBG_MODE_NO_DAG 128u    /* rbg_fw_batch: no DAG path; every matrix takes the blocked
-                                   (or exact) kernels                                     */
+#define RBG_MODE_NO_DAG 128u    /* rbg_fw_batch, rbg_fw_dense: no DAG path; every matrix
+                                   takes the blocked (or exact) kernels                   */
 
 /* which kernel path produced a result */
 #define RBG_PATH_BLOCKED32 1
 #define RBG_PATH_BLOCKED64 2
 #define RBG_PATH_EXACT 3
-#define RBG_PATH_DAG 4   /* rbg_fw_batch: int32 matrix whose off-diagonal entries all lie on
-                            one side of the diagonal, closed by the DAG closure by levels   */
+#define RBG_PATH_DAG 4   /* int32 / int64 matrix whose off-diagonal entries all lie on one
+                            side of the diagonal, closed by the DAG closure by levels       */
 
 typedef struct rbg_result {
     int32_t status;   /* RBG_OK or RBG_ERR_*                                         */
@@ -147,9 +148,11 @@ int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_t ld_in, vo
  * scratch is a 12 MiB array in the library's device image, which every GPU that loads the
  * library holds until the process exits.  n must be at most RBG_NOALLOC_MAX_N, otherwise the
  * call returns RBG_ERR_CAPACITY without touching the GPU.  The first call on a device looks up
- * the array's device address; make that first call before any stream capture.  All calls
- * share the one array: calls that overlap on the GPU race on it and must be serialised by the
- * caller.  Synchronises `stream`.
+ * the array's device address; make that first call before any stream capture (later calls
+ * look it up again, so the address stays right after cudaDeviceReset).  All calls share the
+ * one array: calls that overlap on the GPU race on it and must be serialised by the caller.
+ * RBG_MODE_GRAPH is ignored here (instantiating a graph may take driver memory).
+ * Synchronises `stream`.
  */
 int32_t rbg_fw_dense_noalloc(int32_t dtype, int64_t n, const void *in, int64_t ld_in, void *out,
                              int64_t ld_out, uint32_t mode, rbg_result_t *result,
@@ -174,20 +177,22 @@ int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const i
                      const void *in, void *out, uint32_t mode, void *workspace,
                      int64_t workspace_bytes, rbg_result_t *results, rbg_stream_t stream);
 /*
- * DAG path (RBG_DTYPE_INT32, unless RBG_MODE_NO_DAG, RBG_MODE_TRIANGULAR, RBG_MODE_FORCE_EXACT
- * or RBG_MODE_FORCE_WIDE is given): a matrix whose off-diagonal entries all lie below (or all
- * above) the diagonal, in the clean regime (off-diagonal values 0 or >= 2, diagonal in
- * {-1, 0, 1}) and of at most 8192 rows, is closed through the DAG closure by levels: with its
- * vertices in a topological order the sequential loop's step k only pushes row k into the
- * rows of k's children (below) or pulls k's parents into the rows that reach k (above), so the
- * values are the DAG recurrence's and the diameter comes from each cell's first product in
- * step order.  A product that may reach the top bit sends the matrix to the blocked kernels.
- * The path allocates its scratch (device memory kept by the library between calls, released by
- * rbg_release_scratch).
+ * DAG path of rbg_fw_batch and rbg_fw_dense (RBG_DTYPE_INT32 and RBG_DTYPE_INT64, unless
+ * RBG_MODE_NO_DAG, RBG_MODE_TRIANGULAR, RBG_MODE_FORCE_EXACT or RBG_MODE_FORCE_WIDE is given): a
+ * matrix whose off-diagonal entries all lie below (or all above) the diagonal, in the clean
+ * regime (off-diagonal values 0 or in [2, 2^31), diagonal in {-1, 0, 1}) and of at most 8192
+ * rows, is closed through the DAG closure by levels: with its vertices in a topological order
+ * the sequential loop's step k only pushes row k into the rows of k's children (below) or pulls
+ * k's parents into the rows that reach k (above), so the values are the DAG recurrence's and
+ * the diameter comes from each cell's first product in step order.  A product that may reach
+ * bit 31 sends the matrix to the blocked kernels.  The path's scratch (row slots, the
+ * candidates' CSR, the closure's row pool) is carved from `workspace`; a closure that does not
+ * fit leaves its matrices to the blocked kernels.  Every accept / reject decision is made on
+ * the device and the results are read back once per call.
  */
 
-/* Free the device scratch the DAG path of rbg_fw_batch keeps between calls (waits for the
- * device first).  The next call allocates it again. */
+/* Destroy the CUDA graphs RBG_MODE_GRAPH keeps for the DAG path (waits for the device first);
+ * the next call in that mode records again.  No reference counterpart. */
 int32_t rbg_release_scratch(void);
 
 /*

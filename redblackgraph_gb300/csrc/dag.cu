@@ -472,8 +472,16 @@ __global__ void dag_roots_kernel(DagArgs a) {
     }
 }
 
+// The level a kernel works on: L itself, or L levels past the device-resident level counter *Lp
+// (the level loop run as a CUDA-graph while node); false past the last possible level.
+__device__ __forceinline__ bool dag_level(const DagArgs &a, int64_t &L, const int64_t *Lp) {
+    if (Lp) L += *Lp;
+    return L < a.n;
+}
+
 // Level L + 1 from level L: every child edge of the level's vertices, flattened over the warp.
-__global__ void dag_discover_kernel(DagArgs a, int64_t L) {
+__global__ void dag_discover_kernel(DagArgs a, int64_t L, const int64_t *Lp) {
+    if (!dag_level(a, L, Lp)) return;
     const int lane = threadIdx.x & 31;
     const int64_t s = a.lb[L], e = a.lb[L + 1];
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -615,7 +623,8 @@ __device__ __forceinline__ DagRec dag_shfl_rec(const DagRec &r, int src) {
 // at most 8 candidates fill together (8 lanes each), rows of at most 16 two at a time, larger
 // rows one after the other with the whole warp.  Lanes 8i..8i+7 hold row i's record; the next
 // four records are read before the current rows are filled.  Block 0 closes the level's range.
-__global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int64_t L) {
+__global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int64_t L, const int64_t *Lp) {
+    if (!dag_level(a, L, Lp)) return;
     extern __shared__ __align__(16) unsigned char dg_smem[];
     const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
     DagTable<DG_WSLOTS> &H = reinterpret_cast<DagTable<DG_WSLOTS> *>(dg_smem)[wi];
@@ -697,7 +706,8 @@ __global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int6
 }
 
 // One 512-thread block per row of level L with more than 256 candidates.
-__global__ void __launch_bounds__(DG_BTHREADS) dag_fill_block_kernel(DagArgs a, int64_t L) {
+__global__ void __launch_bounds__(DG_BTHREADS) dag_fill_block_kernel(DagArgs a, int64_t L, const int64_t *Lp) {
+    if (!dag_level(a, L, Lp)) return;
     extern __shared__ __align__(16) unsigned char dg_smem[];
     DagTable<DG_BSLOTS> &H = *reinterpret_cast<DagTable<DG_BSLOTS> *>(dg_smem);
     __shared__ int s_nd, s_ok;
@@ -794,6 +804,15 @@ __global__ void dag_len64_kernel(int64_t n, const int *row_len, int64_t *len64) 
         len64[v] = v < n ? row_len[v] : 0;
 }
 
+// One iteration of the graph's level loop has run DAG_GRAPH_CHUNK levels from *Lp: advance the
+// counter and keep looping while the next level holds a vertex (fill(L - 1) wrote lb[L]).
+__global__ void dag_advance_kernel(DagArgs a, int64_t *Lp, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0) return;
+    const int64_t L = *Lp + DAG_GRAPH_CHUNK;
+    *Lp = L;
+    cudaGraphSetConditional(h, (L < a.n && (int64_t)*a.tail > a.lb[L]) ? 1u : 0u);
+}
+
 }  // namespace rbg
 
 using namespace rbg;
@@ -802,10 +821,10 @@ namespace {
 
 struct DagWs {
     int *remaining, *ccount, *cursor, *children, *order, *wide;
-    int *tail, *nwide, *flags, *nlevels;
     int64_t *coff, *lb, *wlb;
-    unsigned long long *base, *max_abs, *total, *desc;
+    DagCounters *cnt;
     DagRec *rec;
+    unsigned long long *desc;
     void *tmp;
     size_t tmp_bytes;
 };
@@ -832,28 +851,180 @@ size_t dag_layout(int64_t n, int64_t nnz, unsigned char *base, DagWs *w) {
     p = take(nl); if (w) w->coff = (int64_t *)p;
     p = take(nl); if (w) w->lb = (int64_t *)p;
     p = take(nl); if (w) w->wlb = (int64_t *)p;
-    // counters, zeroed together: tail, nwide, flags, nlevels, then base, max_abs, total
-    p = take(64);
-    if (w) {
-        w->tail = (int *)p; w->nwide = (int *)p + 1; w->flags = (int *)p + 2; w->nlevels = (int *)p + 3;
-        w->base = (unsigned long long *)(p + 16); w->max_abs = w->base + 1; w->total = w->base + 2;
-    }
+    p = take(sizeof(DagCounters)); if (w) w->cnt = (DagCounters *)p;   // zeroed together
     const size_t tb = dag_tmp_bytes(n);
     p = take(tb); if (w) { w->tmp = p; w->tmp_bytes = tb; }
     return o;
 }
 
-int sm_count() {
-    static const int sms = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        return v > 0 ? v : 152;
-    }();
-    return sms;
+PerDeviceOnce g_dag_configured;
+
+int dag_configure() {
+    return g_dag_configured.run([] {
+        RBG_CUDA_TRY(cudaFuncSetAttribute(dag_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(sizeof(DagTable<DG_WSLOTS>) * DG_WARPS)));
+        RBG_CUDA_TRY(cudaFuncSetAttribute(dag_fill_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)sizeof(DagTable<DG_BSLOTS>)));
+        return (int)RBG_OK;
+    });
+}
+
+DagArgs dag_args(int64_t n, const rbg_csr_t *A, const DagWs &w, int32_t *pool_cols, int32_t *pool_vals,
+                 int64_t pool_capacity, int64_t *row_off, int32_t *row_len) {
+    DagArgs a;
+    a.n = n; a.ap = A->indptr; a.aj = reinterpret_cast<const int *>(A->indices);
+    a.av = reinterpret_cast<const int *>(A->data);
+    a.order = w.order; a.tail = &w.cnt->placed; a.lb = w.lb;
+    a.coff = w.coff; a.children = w.children; a.remaining = w.remaining;
+    a.row_off = row_off; a.row_len = row_len; a.rec = w.rec; a.desc = w.desc;
+    a.pcols = pool_cols; a.pvals = pool_vals; a.capacity = pool_capacity;
+    a.base = &w.cnt->reserved; a.wide = w.wide; a.nwide = &w.cnt->nwide; a.wlb = w.wlb;
+    a.max_abs = &w.cnt->max_abs; a.total = &w.cnt->total; a.flags = &w.cnt->flags; a.nlevels = &w.cnt->nlevels;
+    return a;
+}
+
+// parents -> children lists and level 0
+int dag_front(const DagArgs &a, const DagWs &w, cudaStream_t s) {
+    const int64_t n = a.n;
+    const int g = grid_for(n, 256);
+    RBG_CUDA_TRY(cudaMemsetAsync(w.ccount, 0, (size_t)(n + 1) * 4, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.cursor, 0, (size_t)(n + 1) * 4, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.cnt, 0, sizeof(DagCounters), s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.lb, 0, 8, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(w.wlb, 0, 8, s));
+    note_launches(4);
+    dag_indeg_kernel<<<g, 256, 0, s>>>(n, a.ap, a.aj, w.remaining, w.ccount);
+    size_t tb = w.tmp_bytes;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.ccount, w.coff, (int)(n + 1), s));
+    dag_children_kernel<<<g, 256, 0, s>>>(n, a.ap, a.aj, w.coff, w.cursor, w.children);
+    dag_roots_kernel<<<g, 256, 0, s>>>(a);
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+struct LevelLaunch {
+    int fill_grid, disc_grid, block_grid;
+    size_t wsm, bsm;
+};
+
+LevelLaunch level_launch() {
+    LevelLaunch l;
+    l.wsm = sizeof(DagTable<DG_WSLOTS>) * DG_WARPS;
+    l.bsm = sizeof(DagTable<DG_BSLOTS>);
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, dag_fill_kernel, DG_WARPS * 32, l.wsm) != cudaSuccess || b < 1)
+        b = 4;
+    const int sms = sm_count();
+    l.fill_grid = sms * b;
+    l.disc_grid = sms * 8;
+    l.block_grid = sms;
+    return l;
+}
+
+void launch_level(const DagArgs &a, const LevelLaunch &l, int64_t L, const int64_t *Lp, cudaStream_t s) {
+    dag_fill_kernel<<<l.fill_grid, DG_WARPS * 32, l.wsm, s>>>(a, L, Lp);
+    dag_fill_block_kernel<<<l.block_grid, DG_BTHREADS, l.bsm, s>>>(a, L, Lp);
+    dag_discover_kernel<<<l.disc_grid, 256, 0, s>>>(a, L, Lp);
+}
+
+// Levels launched in chunks of 8 without waiting (every kernel reads its level's bounds from
+// device memory and exits at once on an empty level); the host looks at the frontier once per
+// chunk.
+int dag_levels_host(const DagArgs &a, const DagWs &w, cudaStream_t s, int64_t *launches) {
+    const LevelLaunch l = level_launch();
+    const int64_t chunk = 8;
+    int64_t L = 0;
+    while (true) {
+        const int64_t Lend = std::min<int64_t>(L + chunk, a.n);
+        for (; L < Lend; ++L) {
+            note_launches(3);
+            *launches += 3;
+            launch_level(a, l, L, nullptr, s);
+        }
+        RBG_CUDA_TRY(cudaGetLastError());
+        // level L is empty when the order has not grown past its start (written by fill(L - 1))
+        int tail = 0;
+        int64_t start = 0;
+        RBG_CUDA_TRY(cudaMemcpyAsync(&tail, &w.cnt->placed, 4, cudaMemcpyDeviceToHost, s));
+        RBG_CUDA_TRY(cudaMemcpyAsync(&start, w.lb + L, 8, cudaMemcpyDeviceToHost, s));
+        RBG_CUDA_TRY(cudaStreamSynchronize(s));
+        if ((int64_t)tail <= start || L >= a.n) break;
+    }
+    return RBG_OK;
+}
+
+// The level loop inside the graph being captured on `s`: a while node whose body runs
+// DAG_GRAPH_CHUNK levels from the device-resident counter and then lets dag_advance_kernel
+// decide whether to go on.  Nothing is read back by the host.
+int dag_levels_graph(const DagArgs &a, const DagWs &w, cudaStream_t s) {
+    const LevelLaunch l = level_launch();
+    int64_t *Lp = reinterpret_cast<int64_t *>(&w.cnt->level);
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    RBG_CUDA_TRY(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps));
+    if (st != cudaStreamCaptureStatusActive || !g) return RBG_ERR_INVALID;
+    cudaGraphConditionalHandle h;
+    RBG_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    RBG_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    // the body is recorded from a second stream captured into it
+    static thread_local cudaStream_t side = nullptr;
+    if (!side) RBG_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    RBG_CUDA_TRY(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    for (int t = 0; t < DAG_GRAPH_CHUNK; ++t) launch_level(a, l, t, Lp, side);
+    dag_advance_kernel<<<1, 32, 0, side>>>(a, Lp, h);
+    const cudaError_t le = cudaGetLastError();
+    cudaGraph_t got = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(side, &got);
+    if (le != cudaSuccess || ee != cudaSuccess) return RBG_ERR_CUDA;
+    RBG_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return RBG_OK;
 }
 
 }  // namespace
+
+namespace rbg {
+
+int sm_count() {
+    static int sms[PerDeviceOnce::kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= PerDeviceOnce::kMaxDevices) return 152;
+    if (sms[dev] <= 0) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev] = v > 0 ? v : 152;   // every thread writes the same value
+    }
+    return sms[dev];
+}
+
+size_t dag_workspace_for(int64_t n, int64_t nnz_bound) { return dag_layout(n, nnz_bound, nullptr, nullptr); }
+
+int dag_enqueue(const rbg_csr_t *A, int64_t nnz_bound, void *workspace, int32_t *pool_cols, int32_t *pool_vals,
+                int64_t pool_capacity, int64_t *row_off, int32_t *row_len, cudaStream_t s, bool captured,
+                DagCounters **counters, int64_t *launches) {
+    const int64_t n = A->n_rows;
+    DagWs w;
+    dag_layout(n, nnz_bound, reinterpret_cast<unsigned char *>(workspace), &w);
+    *counters = w.cnt;
+    int rc = dag_configure();
+    if (rc) return rc;
+    const DagArgs a = dag_args(n, A, w, pool_cols, pool_vals, pool_capacity, row_off, row_len);
+    rc = dag_front(a, w, s);
+    if (rc) return rc;
+    *launches += 4;
+    if (n == 0) return RBG_OK;
+    return captured ? dag_levels_graph(a, w, s) : dag_levels_host(a, w, s, launches);
+}
+
+}  // namespace rbg
 
 extern "C" int32_t rbg_dag_workspace_bytes(int64_t n, int64_t nnz, int64_t *bytes) {
     if (!bytes || n < 0 || nnz < 0 || n >= (1ll << 31) - 1) return RBG_ERR_INVALID;
@@ -876,82 +1047,24 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
     RBG_CUDA_TRY(cudaMemcpyAsync(&annz, A->indptr + n, 8, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
     if (workspace_bytes < (int64_t)dag_layout(n, annz, nullptr, nullptr)) return RBG_ERR_NOMEM;
-    DagWs w;
-    dag_layout(n, annz, reinterpret_cast<unsigned char *>(workspace), &w);
-    static const int configured = [] {
-        RBG_CUDA_TRY(cudaFuncSetAttribute(dag_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(sizeof(DagTable<DG_WSLOTS>) * DG_WARPS)));
-        RBG_CUDA_TRY(cudaFuncSetAttribute(dag_fill_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sizeof(DagTable<DG_BSLOTS>)));
-        return (int)RBG_OK;
-    }();
-    if (configured) return configured;
-    DagArgs a;
-    a.n = n; a.ap = A->indptr; a.aj = reinterpret_cast<const int *>(A->indices);
-    a.av = reinterpret_cast<const int *>(A->data);
-    a.order = w.order; a.tail = w.tail; a.lb = w.lb;
-    a.coff = w.coff; a.children = w.children; a.remaining = w.remaining;
-    a.row_off = row_off; a.row_len = row_len; a.rec = w.rec; a.desc = w.desc;
-    a.pcols = pool_cols; a.pvals = pool_vals; a.capacity = pool_capacity;
-    a.base = w.base; a.wide = w.wide; a.nwide = w.nwide; a.wlb = w.wlb;
-    a.max_abs = w.max_abs; a.total = w.total; a.flags = w.flags; a.nlevels = w.nlevels;
-    const int g = grid_for(n, 256);
-    const int sms = sm_count();
-    // ---- parents -> children lists and level 0
-    RBG_CUDA_TRY(cudaMemsetAsync(w.ccount, 0, (size_t)(n + 1) * 4, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.cursor, 0, (size_t)(n + 1) * 4, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.tail, 0, 64, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.lb, 0, 8, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(w.wlb, 0, 8, s));
-    note_launches(4);
-    dag_indeg_kernel<<<g, 256, 0, s>>>(n, A->indptr, a.aj, w.remaining, w.ccount);
-    size_t tb = w.tmp_bytes;
-    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w.tmp, tb, w.ccount, w.coff, (int)(n + 1), s));
-    dag_children_kernel<<<g, 256, 0, s>>>(n, A->indptr, a.aj, w.coff, w.cursor, w.children);
-    dag_roots_kernel<<<grid_for(n, 256), 256, 0, s>>>(a);
-    // ---- levels, launched in chunks; every kernel reads its level's bounds on the device
-    const size_t wsm = sizeof(DagTable<DG_WSLOTS>) * DG_WARPS, bsm = sizeof(DagTable<DG_BSLOTS>);
-    static const int fill_per_sm = [wsm] {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, dag_fill_kernel, DG_WARPS * 32, wsm) != cudaSuccess || b < 1)
-            b = 4;
-        return b;
-    }();
-    const int fill_grid = sms * fill_per_sm, disc_grid = sms * 8, block_grid = sms;
-    const int64_t chunk = 8;
-    int64_t L = 0;
-    while (true) {
-        const int64_t Lend = std::min<int64_t>(L + chunk, n);
-        for (; L < Lend; ++L) {
-            note_launches(3);
-            dag_fill_kernel<<<fill_grid, DG_WARPS * 32, wsm, s>>>(a, L);
-            dag_fill_block_kernel<<<block_grid, DG_BTHREADS, bsm, s>>>(a, L);
-            dag_discover_kernel<<<disc_grid, 256, 0, s>>>(a, L);
-        }
-        RBG_CUDA_TRY(cudaGetLastError());
-        // level L is empty when the order has not grown past its start (written by fill(L - 1))
-        int tail = 0;
-        int64_t start = 0;
-        RBG_CUDA_TRY(cudaMemcpyAsync(&tail, w.tail, 4, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaMemcpyAsync(&start, w.lb + L, 8, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaStreamSynchronize(s));
-        if ((int64_t)tail <= start || L >= n) break;
-    }
-    int cnt[4] = {0, 0, 0, 0};
-    unsigned long long tot[3] = {0, 0, 0};
-    RBG_CUDA_TRY(cudaMemcpyAsync(cnt, w.tail, 16, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaMemcpyAsync(tot, w.base, 24, cudaMemcpyDeviceToHost, s));
+    DagCounters *dc = nullptr;
+    int64_t launched = 0;
+    int rc = dag_enqueue(A, annz, workspace, pool_cols, pool_vals, pool_capacity, row_off, row_len, s, false, &dc,
+                         &launched);
+    if (rc) return rc;
+    DagCounters c;
+    RBG_CUDA_TRY(cudaMemcpyAsync(&c, dc, sizeof(c), cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    *levels = cnt[3];
-    if (cnt[0] < n) return RBG_ERR_CYCLE;        // vertices on (or below) a cycle were never placed
-    if (cnt[2] & 2) { *nnz = -1; return RBG_ERR_CAPACITY; }
-    if (cnt[2] & 1) {
-        const int64_t reserved = (int64_t)tot[0];
+    *levels = c.nlevels;
+    if (c.placed < n) return RBG_ERR_CYCLE;      // vertices on (or below) a cycle were never placed
+    if (c.flags & 2) { *nnz = -1; return RBG_ERR_CAPACITY; }
+    if (c.flags & 1) {
+        const int64_t reserved = (int64_t)c.reserved;
         *nnz = std::max<int64_t>(2 * pool_capacity, reserved + reserved / 2 + 1024);
         return RBG_ERR_CAPACITY;
     }
-    *nnz = (int64_t)tot[2];
-    *max_abs = (int64_t)tot[1];
+    *nnz = (int64_t)c.total;
+    *max_abs = (int64_t)c.max_abs;
     return RBG_OK;
 }
 

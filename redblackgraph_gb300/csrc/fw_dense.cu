@@ -68,6 +68,7 @@ static thread_local int t_recording = 0;   // launches recorded into a graph are
 void note_launches(int64_t k) {
     if (!t_recording) g_launches.fetch_add(k, std::memory_order_relaxed);
 }
+void launch_recording(bool on) { t_recording = on ? 1 : 0; }
 
 // Opt-in per-kernel timing: CUDA events recorded on the launching stream around each launch of
 // the blocked kernels (0 = tile, 1 = panel, 2 = diagonal, 3 = convert + finalize).
@@ -100,12 +101,7 @@ void timer_end(int kid, cudaEvent_t start, cudaStream_t s) {
 bool timer_on() { return g_timer.on; }
 
 int grid_for(int64_t work, int threads) {
-    static const int sms = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        return v > 0 ? v : 152;
-    }();
+    const int sms = sm_count();
     int64_t blocks = (work + threads - 1) / threads;
     int64_t cap = (int64_t)sms * 16;
     if (blocks > cap) blocks = cap;
@@ -903,6 +899,8 @@ static int read_status(DevStatus *d, DevStatus *h, int count, cudaStream_t strea
 
 template <typename U>
 static int configure_kernels() {
+    static PerDeviceOnce once;   // one per lane type, for every device
+    return once.run([] {
     typedef TileCfg<U> C;
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(PanelSmem<U>)));
@@ -915,7 +913,8 @@ static int configure_kernels() {
     RBG_CUDA_TRY(cudaFuncSetAttribute(fw_tile_kernel<U, N::BN, N::TM, N::TN>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sizeof(TileSmem<U, N::BN>)));
-    return RBG_OK;
+    return (int)RBG_OK;
+    });
 }
 
 // Upload the plan's tables into the workspace.
@@ -941,7 +940,7 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
                           bool stop_after_convert, DevStatus *h_status, const unsigned char *shapes = nullptr,
                           cudaEvent_t *round_events = nullptr, const RowStats &rs = RowStats()) {
     typedef TileCfg<U> C;
-    static const int configured = configure_kernels<U>();   // once, thread-safe initialisation
+    const int configured = configure_kernels<U>();   // once per device
     if (configured) return configured;
     const int cnt = P.count;
     DevStatus *st = reinterpret_cast<DevStatus *>(ws + P.off_status);
@@ -962,12 +961,7 @@ static int launch_blocked(const FwPlan &P, const T *in, T *out, unsigned char *w
     int2 *plist = reinterpret_cast<int2 *>(ws + P.off_plist);
     int2 *tlist = reinterpret_cast<int2 *>(ws + P.off_tlist);
     int *counters = reinterpret_cast<int *>(ws + P.off_counters);
-    static const int sms = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        return v > 0 ? v : 152;
-    }();
+    const int sms = sm_count();
     const int64_t persist = 2 * (int64_t)sms;   // two CTAs per SM for both persistent kernels
 
     RBG_CUDA_TRY(cudaMemsetAsync(occ, 0, std::max<size_t>(P.occ_bytes, 1), stream));
@@ -1114,15 +1108,31 @@ static void result_from_blocked(const DevStatus &h, int path, rbg_result_t *res)
     res->path = path;
 }
 
-// Single matrix: 32-bit lanes, then 64-bit lanes when 64-bit values need them, then the exact
-// sequential-order kernel for anything outside the clean regime, cycles and top-bit products.
+// Modes under which a matrix numbered in a topological order may take the DAG path.
+static bool dag_path_allowed(uint32_t mode) {
+    return !(mode & (RBG_MODE_NO_DAG | RBG_MODE_TRIANGULAR | RBG_MODE_FORCE_EXACT | RBG_MODE_FORCE_WIDE));
+}
+
+// Single matrix: the DAG path for int32 / int64 matrices numbered in a topological order, else
+// 32-bit lanes, then 64-bit lanes when 64-bit values need them, then the exact sequential-order
+// kernel for anything outside the clean regime, cycles and top-bit products.
 template <typename T>
 static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_out, uint32_t mode,
-                      unsigned char *ws, rbg_result_t *res, cudaStream_t stream) {
+                      unsigned char *ws, size_t ws_bytes, bool try_dag, rbg_result_t *res, cudaStream_t stream) {
     const bool cython = (mode & RBG_MODE_CYTHON) != 0;
     const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
     memset(res, 0, sizeof(*res));
     res->k = res->i = res->j = -1;
+    if constexpr (std::is_same<T, int32_t>::value || std::is_same<T, int64_t>::value) {
+        if (try_dag && dag_path_allowed(mode)) {
+            const int64_t zero = 0;
+            char closed = 0;
+            const int rc = tri_batch<T>(1, &n, &zero, &zero, ld_in, ld_out, in, out, res, &closed, ws, ws_bytes, mode,
+                                        stream, RowStats());
+            if (rc) return rc;
+            if (closed) return RBG_OK;
+        }
+    }
     DevStatus h;
     FwPlan P;
     single_plan<uint32_t>(P, n, ld_in, ld_out, triangular, (int)sizeof(T));
@@ -1322,7 +1332,7 @@ static int tune_blocked(const FwPlan &P, const T *in, T *out, unsigned char *ws,
 
 template <typename T>
 static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offsets, const T *in, T *out,
-                      uint32_t mode, unsigned char *ws, rbg_result_t *results, cudaStream_t stream,
+                      uint32_t mode, unsigned char *ws, size_t ws_bytes, rbg_result_t *results, cudaStream_t stream,
                       const RowStats &rs = RowStats()) {
     const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
     for (int64_t i = 0; i < count; ++i) {
@@ -1331,11 +1341,12 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
     }
     // matrices numbered in a topological order take the DAG path; the rest form a sub-batch
     std::vector<char> closed((size_t)count, 0);
-    if (std::is_same<T, int32_t>::value &&
-        !(mode & (RBG_MODE_NO_DAG | RBG_MODE_TRIANGULAR | RBG_MODE_FORCE_EXACT | RBG_MODE_FORCE_WIDE))) {
-        const int rc = tri_batch(count, sizes, offsets, reinterpret_cast<const int32_t *>(in),
-                                 reinterpret_cast<int32_t *>(out), results, closed.data(), stream, rs);
-        if (rc) return rc;
+    if constexpr (std::is_same<T, int32_t>::value || std::is_same<T, int64_t>::value) {
+        if (dag_path_allowed(mode)) {
+            const int rc = tri_batch<T>(count, sizes, offsets, offsets, 0, 0, in, out, results, closed.data(), ws,
+                                        ws_bytes, mode, stream, rs);
+            if (rc) return rc;
+        }
     }
     std::vector<int64_t> idx;
     for (int64_t i = 0; i < count; ++i)
@@ -1387,7 +1398,7 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
         const int64_t i = idx[(size_t)k];
         if (!redo[(size_t)k] || sizes[i] == 0) continue;
         int rc = fw_dense_t<T>(sizes[i], in + offsets[i], sizes[i], out + offsets[i], sizes[i], mode, ws,
-                               &results[i], stream);
+                               ws_bytes, false, &results[i], stream);
         if (rc) return rc;
     }
     return RBG_OK;
@@ -1462,7 +1473,7 @@ extern "C" int32_t rbg_fw_dense(int32_t dtype, int64_t n, const void *in, int64_
     int rc = RBG_ERR_INVALID;
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out),
-                           ld_out, mode, ws, result, s));
+                           ld_out, mode, ws, (size_t)workspace_bytes, true, result, s));
     return rc;
 }
 
@@ -1486,13 +1497,18 @@ static void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // the array's device address
 
 // Device address of the scratch array on the current device.  In host code the array's name is
 // only a host-side stand-in, so the address is asked of the runtime once per device (with that
-// device current) and cached; this first call must come before any stream capture.
-static int noalloc_scratch(void **ptr) {
+// device current) and cached; this first call must come before any stream capture.  Outside a
+// capture every call asks again and replaces a cached address that changed (the module is
+// loaded afresh after cudaDeviceReset), so a reset never leaves a dangling address behind.
+static int noalloc_scratch(cudaStream_t s, void **ptr) {
     int dev = 0;
     RBG_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return RBG_ERR_INVALID;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    RBG_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone || !g_noalloc_ptr[dev]) {
+        if (cs != cudaStreamCaptureStatusNone) return RBG_ERR_INVALID;   // set-up inside a capture
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) return RBG_ERR_CUDA;
@@ -1513,14 +1529,16 @@ extern "C" int32_t rbg_fw_dense_noalloc(int32_t dtype, int64_t n, const void *in
     if (n > RBG_NOALLOC_MAX_N || single_workspace(n, dtype) > (size_t)RBG_NOALLOC_SCRATCH_BYTES)
         return RBG_ERR_CAPACITY;   // beyond what the fixed scratch array holds
     if (n == 0) return RBG_OK;
-    void *ws = nullptr;
-    int rc = noalloc_scratch(&ws);
-    if (rc) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    void *ws = nullptr;
+    int rc = noalloc_scratch(s, &ws);
+    if (rc) return rc;
+    mode &= ~RBG_MODE_GRAPH;   // instantiating a graph may take driver memory
     rc = RBG_ERR_INVALID;
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out), ld_out,
-                           mode, reinterpret_cast<unsigned char *>(ws), result, s));
+                           mode, reinterpret_cast<unsigned char *>(ws), (size_t)RBG_NOALLOC_SCRATCH_BYTES, true,
+                           result, s));
     return rc;
 }
 
@@ -1588,7 +1606,7 @@ static int32_t fw_batch_entry(int32_t dtype, int64_t count, const int64_t *sizes
     int rc = RBG_ERR_INVALID;
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_batch_t<T>(count, sizes, offsets, reinterpret_cast<const T *>(in), reinterpret_cast<T *>(out),
-                           mode, ws, results, s, rs));
+                           mode, ws, (size_t)workspace_bytes, results, s, rs));
     return rc;
 }
 

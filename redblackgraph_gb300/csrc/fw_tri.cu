@@ -8,22 +8,27 @@
 // input A(i, k), while row k is already final (every path from k descends through vertices
 // below k).  Step k therefore adds A(i, k) (x) C(k, .) to the rows of k's children, and the
 // closure is the DAG recurrence  C(i, .) = A(i, .) (+) sum over parents k of A(i, k) (x) C(k, .)
-// that rbg_dag_closure computes level by level.  Above the diagonal (edges to higher numbers)
-// it is the mirror image: before step k, W(i, k) = C(i, k) and W(k, j) = A(k, j).
+// that the closure by levels computes.  Above the diagonal (edges to higher numbers) it is the
+// mirror image: before step k, W(i, k) = C(i, k) and W(k, j) = A(k, j).
 //
 // In the clean regime (off-diagonal values 0 or >= 2, diagonal in {-1, 0, 1}) products with the
 // diagonal change nothing and a cell only decreases once it holds a value, so the largest value
 // the loop ever writes -- the diameter's source -- is, per cell, its first value: A(i, j), else
 // the product of the first step that reaches the cell.  Below the diagonal that is the smallest
 // parent k of i with j in C(k); above it, the smallest k in C(i) with j a parent of k.  A
-// product whose most significant bit may reach the top bit of the 32-bit value sends the
-// matrix to the blocked kernels (which report the reference's overflow or wrap), as does
-// anything outside the clean regime, a row of more than TRI_CAP entries or n > 8192.
+// product whose most significant bit may reach bit 31 sends the matrix to the blocked kernels
+// (which report the reference's overflow or wrap for 32-bit storage, and carry 64-bit values
+// exactly), as does anything outside the clean regime or the 32-bit value range, a row of more
+// than TRI_CAP entries or n > 8192.  For 64-bit storage no product below bit 31 can overflow, so
+// the values, the diameter and the absence of errors are the reference's as well.
 //
-// Pipeline (one call): scan the dense rows (clean-regime test, which side of the diagonal, up
-// to TRI_CAP off-diagonal entries per row) -> CSR of the candidate matrices with batch-global
-// row numbers -> rbg_dag_closure -> per-row statistics (largest product MSB, largest
-// first-value MSB) -> the dense rows of the accepted matrices written from the closure rows.
+// Pipeline (one call, every decision on the device): scan the dense rows (clean-regime test,
+// which side of the diagonal, up to TRI_CAP off-diagonal entries per row) -> CSR of the
+// candidate matrices with batch-global row numbers -> closure by levels -> per-row statistics
+// (largest product MSB, largest first-value MSB) -> the dense rows of the accepted matrices
+// written from the closure rows -> one result record per matrix, read back once.  Scratch is
+// carved from the caller's workspace; with RBG_MODE_GRAPH the sequence, level loop included (a
+// while node the device ends), is one CUDA graph replayed for the same layout.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 #include <string.h>
@@ -43,10 +48,16 @@ constexpr int64_t TRI_MAX_N = DAG_MAX_N;     // rows of a matrix on this path (b
 constexpr int TRI_BM_WORDS = (int)(TRI_MAX_N / 32);
 constexpr unsigned TF_UNCLEAN = 1u, TF_BELOW = 2u, TF_ABOVE = 4u, TF_WIDE = 8u;
 constexpr int KIND_NONE = DAG_KIND_NONE, KIND_BELOW = DAG_KIND_BELOW, KIND_ABOVE = DAG_KIND_ABOVE;
-constexpr int TRI_TOP = DAG_TOP_MSB;         // lbits - 1 for 32-bit values
+constexpr int TRI_TOP = DAG_TOP_MSB;         // products reaching bit 31 leave the path
 
 struct TriComp {
     int64_t n, in_off, out_off, row_base;    // row_base: first batch-global row
+};
+
+// Result of one matrix, written on the device and read back once per call.
+struct TriOut {
+    int32_t accepted, diameter;
+    unsigned long long executed;
 };
 
 __device__ __forceinline__ int tri_find(const int64_t *__restrict__ prefix, int count, int64_t cta) {
@@ -59,15 +70,30 @@ __device__ __forceinline__ int tri_find(const int64_t *__restrict__ prefix, int 
     return lo;
 }
 
-// Off-diagonal entries of four consecutive columns j0 .. j0 + 3 held by each lane (m of them
+// A 16-byte vector of the storage type, unpacked.
+template <typename T> struct TriVec {
+    static constexpr int E = 16 / (int)sizeof(T);
+    __device__ __forceinline__ static void split(const int4 &x, T (&v)[E]) {
+        static_assert(sizeof(T) == 4 || sizeof(T) == 8, "int32 or int64 storage");
+        if constexpr (sizeof(T) == 4) {
+            v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+        } else {
+            v[0] = (T)(((unsigned long long)(unsigned)x.y << 32) | (unsigned)x.x);
+            v[1] = (T)(((unsigned long long)(unsigned)x.w << 32) | (unsigned)x.z);
+        }
+    }
+};
+
+// Off-diagonal entries of E consecutive columns j0 .. j0 + E - 1 held by each lane (m of them
 // valid): clean-regime flags, and the nonzeros appended to the row's slots in column order.
-// Column numbers fit 32 bits (n <= 8192 on this path).
-__device__ __forceinline__ void tri_take(int32_t (&v)[4], int j0, int m, int i, int lane, int64_t g,
+// Column numbers fit 32 bits (n <= 8192 on this path); values outside [2, 2^31) are unclean.
+template <typename T, int E>
+__device__ __forceinline__ void tri_take(T (&v)[E], int j0, int m, int i, int lane, int64_t g,
                                          int32_t *__restrict__ slot_col, int32_t *__restrict__ slot_val,
                                          unsigned &flags, int &cnt) {
     int c4 = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < E; ++k) {
         const int j = j0 + k;
         if (k >= m) {
             v[k] = 0;
@@ -75,7 +101,8 @@ __device__ __forceinline__ void tri_take(int32_t (&v)[4], int j0, int m, int i, 
             if (!(v[k] == 0 || v[k] == 1 || v[k] == -1)) flags |= TF_UNCLEAN;
             v[k] = 0;                        // the diagonal is not an edge
         } else if (v[k] != 0) {
-            if (v[k] == 1 || v[k] < 0) flags |= TF_UNCLEAN;
+            if (v[k] == 1 || v[k] < 0 || (sizeof(T) == 8 && (long long)v[k] > (long long)INT32_MAX))
+                flags |= TF_UNCLEAN;
             flags |= j < i ? TF_BELOW : TF_ABOVE;
             ++c4;
         }
@@ -89,11 +116,11 @@ __device__ __forceinline__ void tri_take(int32_t (&v)[4], int j0, int m, int i, 
     }
     int pos = cnt + x - c4;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < E; ++k) {
         if (v[k] != 0) {
             if (pos < TRI_CAP) {
                 slot_col[g * TRI_CAP + pos] = j0 + k;
-                slot_val[g * TRI_CAP + pos] = v[k];
+                slot_val[g * TRI_CAP + pos] = (int32_t)v[k];
             }
             ++pos;
         }
@@ -105,11 +132,13 @@ __device__ __forceinline__ void tri_take(int32_t (&v)[4], int j0, int m, int i, 
 // column order into its TRI_CAP slots (the count may exceed TRI_CAP: then only flagged).  The
 // row is read as 16-byte vectors from its first 16-byte boundary (scalar head and tail), four
 // vectors per lane in flight; a vector of zeros (the common case) costs one vote.
+template <typename T>
 __global__ void __launch_bounds__(TRI_THREADS, 5)
-tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comps,
+tri_scan_kernel(const T *__restrict__ in, int64_t ld_in, const TriComp *__restrict__ comps,
                 const int64_t *__restrict__ pre, int count, int32_t *__restrict__ slot_col,
                 int32_t *__restrict__ slot_val, int32_t *__restrict__ row_cnt, int32_t *__restrict__ row_comp,
                 unsigned *__restrict__ cflags) {
+    constexpr int E = TriVec<T>::E;
     const int ci = tri_find(pre, count, blockIdx.x);
     const TriComp c = comps[ci];
     const int i = (int)(((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS) + (threadIdx.x >> 5);
@@ -117,17 +146,17 @@ tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comp
     const int lane = threadIdx.x & 31;
     const int n = (int)c.n;
     const int64_t g = c.row_base + i;
-    const int32_t *row = in + c.in_off + (int64_t)i * n;
-    const int lead = (int)(((16 - ((uintptr_t)row & 15)) & 15) / 4);   // to the first boundary
+    const T *row = in + c.in_off + (int64_t)i * (ld_in ? ld_in : c.n);
+    const int lead = (int)(((16 - ((uintptr_t)row & 15)) & 15) / sizeof(T));   // to the first boundary
     const int head = lead < n ? lead : n;
-    const int nv = (n - head) / 4;           // 16-byte vectors after the head
-    const int tail = n - head - 4 * nv;
+    const int nv = (n - head) / E;           // 16-byte vectors after the head
+    const int tail = n - head - E * nv;
     unsigned flags = 0;
     int cnt = 0;
-    int32_t v[4];
+    T v1[1];
     if (head) {                              // columns 0 .. head - 1, one per lane
-        v[0] = lane < head ? row[lane] : 0;
-        tri_take(v, lane, lane < head ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
+        v1[0] = lane < head ? row[lane] : (T)0;
+        tri_take<T, 1>(v1, lane, lane < head ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
     }
     // vectors s0 + 32 u + lane (u = 0..3), taken in column order (u ascending)
     for (int s0 = 0; s0 < nv; s0 += 128) {
@@ -135,23 +164,24 @@ tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comp
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int q = s0 + 32 * u + lane;
-            x[u] = q < nv ? *reinterpret_cast<const int4 *>(row + head + 4 * q) : make_int4(0, 0, 0, 0);
+            x[u] = q < nv ? *reinterpret_cast<const int4 *>(row + head + E * q) : make_int4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int q = s0 + 32 * u + lane;
-            const int j0 = head + 4 * q;
+            const int j0 = head + E * q;
             // all-zero vectors (a zero diagonal included) leave nothing to take
             if (__any_sync(0xffffffffu, (x[u].x | x[u].y | x[u].z | x[u].w) != 0)) {
-                v[0] = x[u].x; v[1] = x[u].y; v[2] = x[u].z; v[3] = x[u].w;
-                tri_take(v, j0, q < nv ? 4 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
+                T v[E];
+                TriVec<T>::split(x[u], v);
+                tri_take<T, E>(v, j0, q < nv ? E : 0, i, lane, g, slot_col, slot_val, flags, cnt);
             }
         }
     }
     if (tail) {
-        const int j = head + 4 * nv + lane;
-        v[0] = lane < tail ? row[j] : 0;
-        tri_take(v, j, lane < tail ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
+        const int j = head + E * nv + lane;
+        v1[0] = lane < tail ? row[j] : (T)0;
+        tri_take<T, 1>(v1, j, lane < tail ? 1 : 0, i, lane, g, slot_col, slot_val, flags, cnt);
     }
     if (cnt > TRI_CAP) flags |= TF_WIDE;
     flags = __reduce_or_sync(0xffffffffu, flags);
@@ -162,24 +192,27 @@ tri_scan_kernel(const int32_t *__restrict__ in, const TriComp *__restrict__ comp
     }
 }
 
-// which matrices are candidates, from the scan's flags (decided on the device: no host round
-// trip before the CSR is built)
+// Per matrix: candidate kind from the scan's flags, and the statistics' starting values.
 __global__ void tri_kind_kernel(int count, const TriComp *__restrict__ comps, const unsigned *__restrict__ cflags,
-                                int32_t *__restrict__ ckind) {
+                                int32_t *__restrict__ ckind, int *__restrict__ cam, int *__restrict__ cfm,
+                                unsigned long long *__restrict__ cprod) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const unsigned f = cflags[i];
         int k = KIND_NONE;
         if (comps[i].n > 0 && !(f & (TF_UNCLEAN | TF_WIDE)) && !((f & TF_BELOW) && (f & TF_ABOVE)))
             k = (f & TF_ABOVE) ? KIND_ABOVE : KIND_BELOW;
         ckind[i] = k;
+        cam[i] = -1;
+        cfm[i] = -1;
+        cprod[i] = 0;
     }
 }
 
 // entries of each row in the CSR of the candidate matrices (rows of other matrices empty)
 __global__ void tri_count_kernel(int64_t R, const int32_t *__restrict__ row_cnt, const int32_t *__restrict__ row_comp,
                                  const int32_t *__restrict__ ckind, int64_t *__restrict__ cnt64) {
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < R; g += (int64_t)gridDim.x * blockDim.x)
-        cnt64[g] = ckind[row_comp[g]] != KIND_NONE ? row_cnt[g] : 0;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g <= R; g += (int64_t)gridDim.x * blockDim.x)
+        cnt64[g] = g < R && ckind[row_comp[g]] != KIND_NONE ? row_cnt[g] : 0;
 }
 
 __global__ void tri_csr_fill_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
@@ -199,6 +232,12 @@ __global__ void tri_csr_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
     }
 }
 
+// The closure by levels left every candidate row in the pool (no pool overflow, every vertex
+// placed); otherwise nothing of this call's DAG path is used.
+__device__ __forceinline__ bool tri_dag_ok(const DagCounters *dc, int64_t R) {
+    return !(dc->flags & 3) && (int64_t)dc->placed >= R;
+}
+
 // One warp per row of a candidate matrix: the row statistics of dag_rows.cuh, reduced per
 // matrix (largest product MSB, largest first-value MSB, products).
 __global__ void __launch_bounds__(TRI_THREADS, 8)
@@ -206,9 +245,10 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
                  const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
                  const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
-                 const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, int *__restrict__ cam,
-                 int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
+                 const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, const DagCounters *dc,
+                 int *__restrict__ cam, int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
     __shared__ unsigned bm_all[TRI_ROWS][TRI_BM_WORDS];
+    if (!tri_dag_ok(dc, R)) return;          // block-uniform
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * TRI_ROWS;
     for (int64_t g = (int64_t)blockIdx.x * TRI_ROWS + w; g < R; g += warps) {
@@ -232,31 +272,37 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
     }
 }
 
-constexpr int TRI_SEG = 512;                 // columns per shared-memory segment of a row
+__device__ __forceinline__ bool tri_accepted(int ci, const int32_t *ckind, const int *cam, const DagCounters *dc,
+                                             int64_t R) {
+    return ckind[ci] != KIND_NONE && cam[ci] < TRI_TOP && tri_dag_ok(dc, R);
+}
 
 // One warp per row of an accepted matrix.  Out of place, the whole dense row is written in
-// segments of TRI_SEG columns built in shared memory (zeros, the closure row's entries, the
+// segments of SEG columns (2 KB) built in shared memory (zeros, the closure row's entries, the
 // diagonal) and stored as full 16-byte vectors on the row's 16-byte grid, so no DRAM line is
 // written partially; in place, only the closure's entries (the other cells already hold the
-// result).  The row statistics are recorded when asked for.
+// result).  The row statistics are recorded when asked for (32-bit storage).
+template <typename T>
 __global__ void __launch_bounds__(TRI_THREADS)
-tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, const TriComp *__restrict__ comps,
-                 const int64_t *__restrict__ pre, int count, const int32_t *__restrict__ ckind,
-                 const int *__restrict__ cam,
+tri_write_kernel(const T *__restrict__ in, int64_t ld_in, T *__restrict__ out, int64_t ld_out,
+                 const TriComp *__restrict__ comps, const int64_t *__restrict__ pre, int count,
+                 const int32_t *__restrict__ ckind, const int *__restrict__ cam, const DagCounters *dc, int64_t R,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, RowStats rs) {
-    __shared__ __align__(16) int32_t seg_all[TRI_ROWS][TRI_SEG];
+    constexpr int SEG = 2048 / (int)sizeof(T);
+    constexpr int E = TriVec<T>::E;
+    __shared__ __align__(16) T seg_all[TRI_ROWS][SEG];
     const int ci = tri_find(pre, count, blockIdx.x);
-    if (ckind[ci] == KIND_NONE || cam[ci] >= TRI_TOP) return;   // not accepted (block-uniform)
+    if (!tri_accepted(ci, ckind, cam, dc, R)) return;   // block-uniform
     const TriComp c = comps[ci];
     const int i = (int)(((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS) + (threadIdx.x >> 5);
     if (i >= c.n) return;                    // warp-uniform
     const int lane = threadIdx.x & 31;
     const int n = (int)c.n;
     const int64_t g = c.row_base + i;
-    const int32_t *rin = in + c.in_off + (int64_t)i * n;
-    int32_t *rout = out + c.out_off + (int64_t)i * n;
-    const int32_t diag = rin[i];
+    const T *rin = in + c.in_off + (int64_t)i * (ld_in ? ld_in : c.n);
+    T *rout = out + c.out_off + (int64_t)i * (ld_out ? ld_out : c.n);
+    const T diag = rin[i];
     const int64_t c0 = row_off[g];
     const int clen = row_len[g];
     const int32_t base = (int32_t)c.row_base;
@@ -275,19 +321,19 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
         for (int q = lane; q < clen; q += 32) {
             const int j = p_col[c0 + q] - base;
             const int32_t v = p_val[c0 + q];
-            rout[j] = v;
+            rout[j] = (T)v;
             mx = max(mx, v);
             mark(j >> 5);
         }
     } else {
-        int32_t *seg = seg_all[threadIdx.x >> 5];
-        // column j sits at j' = j + shift on the 16-byte grid; segment s0 holds j' in [s0, s0 + TRI_SEG)
-        const int shift = (int)(((uintptr_t)rout & 15) >> 2);
+        T *seg = seg_all[threadIdx.x >> 5];
+        // column j sits at j' = j + shift on the 16-byte grid; segment s0 holds j' in [s0, s0 + SEG)
+        const int shift = (int)(((uintptr_t)rout & 15) / sizeof(T));
         int e = 0;                           // first closure entry not yet placed (warp-uniform)
-        for (int s0 = 0; s0 < n + shift; s0 += TRI_SEG) {
-            for (int t = lane; t < TRI_SEG / 4; t += 32) reinterpret_cast<int4 *>(seg)[t] = make_int4(0, 0, 0, 0);
+        for (int s0 = 0; s0 < n + shift; s0 += SEG) {
+            for (int t = lane; t < SEG / E; t += 32) reinterpret_cast<int4 *>(seg)[t] = make_int4(0, 0, 0, 0);
             __syncwarp();
-            const int lim = s0 + TRI_SEG - shift;        // entries with j < lim belong to this segment
+            const int lim = s0 + SEG - shift;            // entries with j < lim belong to this segment
             for (;;) {                                   // batches of 32 entries, ascending
                 const int q = e + lane;
                 int j = INT_MAX;
@@ -298,7 +344,7 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
                 }
                 const bool here = j < lim;
                 if (here) {
-                    seg[j + shift - s0] = v;
+                    seg[j + shift - s0] = (T)v;
                     mx = max(mx, v);
                     mark(j >> 5);
                 }
@@ -306,86 +352,65 @@ tri_write_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, cons
                 e += __popc(bal);
                 if (bal != 0xffffffffu) break;
             }
-            if (lane == 0 && i + shift >= s0 && i + shift < s0 + TRI_SEG) seg[i + shift - s0] = diag;
+            if (lane == 0 && i + shift >= s0 && i + shift < s0 + SEG) seg[i + shift - s0] = diag;
             __syncwarp();
-            for (int t = lane; t < TRI_SEG / 4; t += 32) {
-                const int j0 = s0 + 4 * t - shift;
+            for (int t = lane; t < SEG / E; t += 32) {
+                const int j0 = s0 + E * t - shift;
                 if (j0 >= n) break;
                 const int4 z = reinterpret_cast<const int4 *>(seg)[t];
-                if (j0 >= 0 && j0 + 4 <= n) {
+                if (j0 >= 0 && j0 + E <= n) {
                     *reinterpret_cast<int4 *>(rout + j0) = z;
                 } else {                                 // the row's ragged ends
-                    const int zz[4] = {z.x, z.y, z.z, z.w};
+                    T zz[E];
+                    TriVec<T>::split(z, zz);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
+                    for (int k = 0; k < E; ++k)
                         if (j0 + k >= 0 && j0 + k < n) rout[j0 + k] = zz[k];
                 }
             }
             __syncwarp();                                // before the next segment is zeroed
         }
     }
-    if (rs.row_count) {
-        if (lane == 0 && diag != 0) {
-            mark(i >> 5);
-            mx = max(mx, diag);
-        }
-        auto orw = [](unsigned long long x) {
-            const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)x);
-            const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(x >> 32));
-            return ((unsigned long long)hi << 32) | lo;
-        };
-        const unsigned long long wd[4] = {orw(w0), orw(w1), orw(w2), orw(w3)};
-        mx = __reduce_max_sync(0xffffffffu, mx);
-        if (lane == 0) {
-            const int64_t at = rs.row_base[ci] + i;
-            rs.row_count[rs.row_id ? (int64_t)rs.row_id[at] : at] = clen + (diag != 0 ? 1 : 0);
-            if (rs.chunk_mask) {
-                const int64_t words = (n + 2047) / 2048;
-                unsigned long long *mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[ci] + ci +
-                                           (int64_t)i * words;
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    if (t < words) mrow[t] = wd[t];
+    if constexpr (sizeof(T) == 4) {
+        if (rs.row_count) {
+            if (lane == 0 && diag != 0) {
+                mark(i >> 5);
+                mx = max(mx, (int)diag);
             }
-            if (rs.comp_max && mx > 0) atomicMax(rs.comp_max + ci, mx);
+            auto orw = [](unsigned long long x) {
+                const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)x);
+                const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(x >> 32));
+                return ((unsigned long long)hi << 32) | lo;
+            };
+            const unsigned long long wd[4] = {orw(w0), orw(w1), orw(w2), orw(w3)};
+            mx = __reduce_max_sync(0xffffffffu, mx);
+            if (lane == 0) {
+                const int64_t at = rs.row_base[ci] + i;
+                rs.row_count[rs.row_id ? (int64_t)rs.row_id[at] : at] = clen + (diag != 0 ? 1 : 0);
+                if (rs.chunk_mask) {
+                    const int64_t words = (n + 2047) / 2048;
+                    unsigned long long *mrow = rs.chunk_mask + (c.in_off + 2047) / 2048 + rs.row_base[ci] + ci +
+                                               (int64_t)i * words;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                        if (t < words) mrow[t] = wd[t];
+                }
+                if (rs.comp_max && mx > 0) atomicMax(rs.comp_max + ci, mx);
+            }
         }
     }
 }
 
-// Device scratch kept between calls (grown when a batch needs more; one call at a time).
-struct TriScratch {
-    unsigned char *p = nullptr;
-    size_t cap = 0;
-    int device = -1;                         // the device the buffer lives on
-};
-std::mutex g_tri_mu;
-TriScratch g_tri_a, g_tri_b;
-// the matrix table and CTA prefix last uploaded into g_tri_a (a batch closed again skips the copy)
-std::vector<TriComp> g_tri_last_comps;
-const unsigned char *g_tri_last_buf = nullptr;
-
-// A buffer on another device than the calling thread's current one is freed and allocated
-// again on the current device (a process may drive several GPUs, one at a time per call).
-int tri_reserve(TriScratch &s, size_t bytes, cudaStream_t st) {
-    int dev = 0;
-    RBG_CUDA_TRY(cudaGetDevice(&dev));
-    if (bytes <= s.cap && dev == s.device) return RBG_OK;
-    RBG_CUDA_TRY(cudaStreamSynchronize(st));
-    if (s.p) {                               // freed on its own device, after its work
-        if (s.device != dev) RBG_CUDA_TRY(cudaSetDevice(s.device));
-        RBG_CUDA_TRY(cudaDeviceSynchronize());
-        cudaFree(s.p);
-        if (s.device != dev) RBG_CUDA_TRY(cudaSetDevice(dev));
+__global__ void tri_result_kernel(int count, const int32_t *__restrict__ ckind, const int *__restrict__ cam,
+                                  const int *__restrict__ cfm, const unsigned long long *__restrict__ cprod,
+                                  const DagCounters *dc, int64_t R, TriOut *__restrict__ res) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        TriOut o;
+        o.accepted = tri_accepted(i, ckind, cam, dc, R) ? 1 : 0;
+        o.diameter = cfm[i] > 0 ? cfm[i] : 0;
+        o.executed = cprod[i];
+        res[i] = o;
     }
-    s.p = nullptr;
-    s.cap = 0;
-    s.device = -1;
-    g_tri_last_buf = nullptr;
-    const size_t want = bytes + bytes / 4;
-    RBG_CUDA_TRY(cudaMalloc(reinterpret_cast<void **>(&s.p), want));
-    s.cap = want;
-    s.device = dev;
-    return RBG_OK;
 }
 
 struct Carve {
@@ -393,205 +418,280 @@ struct Carve {
     size_t off = 0;
     template <typename X> X *take(size_t n) {
         off = align_up(off, 256);
-        X *r = reinterpret_cast<X *>(p + off);
+        X *r = p ? reinterpret_cast<X *>(p + off) : nullptr;
         off += n * sizeof(X);
         return r;
     }
 };
 
-}  // namespace
-
-int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const int32_t *in, int32_t *out,
-              rbg_result_t *results, char *closed, cudaStream_t s, const RowStats &rs) {
-    if (count <= 0 || count > INT32_MAX) return RBG_OK;
-    std::vector<TriComp> hc((size_t)count);
-    std::vector<int64_t> pre((size_t)count + 1, 0);
-    int64_t R = 0;
-    for (int64_t i = 0; i < count; ++i) {
-        const int64_t n = (sizes[i] > 0 && sizes[i] <= TRI_MAX_N) ? sizes[i] : 0;
-        hc[(size_t)i] = TriComp{n, offsets[i], offsets[i], R};
-        R += n;
-        pre[(size_t)i + 1] = pre[(size_t)i] + (n + TRI_ROWS - 1) / TRI_ROWS;
-    }
-    if (R == 0 || R > INT32_MAX) return RBG_OK;
-    std::lock_guard<std::mutex> lk(g_tri_mu);
-    size_t scan_tmp = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (int64_t *)nullptr, (int64_t *)nullptr, (int)(R + 1));
-    const size_t C = (size_t)count, NR = (size_t)R;
-    auto layout = [&](Carve &cv, TriComp *&dc, int64_t *&dpre, unsigned *&cflags, int32_t *&ckind,
-                      int *&cam, int *&cfm, unsigned long long *&cprod, int32_t *&row_cnt,
-                      int32_t *&row_comp, int32_t *&slot_col, int32_t *&slot_val, int64_t *&indptr, void *&tmp,
-                      int32_t *&a_col, int32_t *&a_val) {
-        dc = cv.take<TriComp>(C);
-        dpre = cv.take<int64_t>(C + 1);
-        cflags = cv.take<unsigned>(C);
-        ckind = cv.take<int32_t>(C);
-        cam = cv.take<int>(C);
-        cfm = cv.take<int>(C);
-        cprod = cv.take<unsigned long long>(C);
-        row_cnt = cv.take<int32_t>(NR);
-        row_comp = cv.take<int32_t>(NR);
-        slot_col = cv.take<int32_t>(NR * TRI_CAP);
-        slot_val = cv.take<int32_t>(NR * TRI_CAP);
-        indptr = cv.take<int64_t>(NR + 1);
-        tmp = cv.take<unsigned char>(scan_tmp);
-        a_col = cv.take<int32_t>(NR * TRI_CAP);
-        a_val = cv.take<int32_t>(NR * TRI_CAP);
-    };
+// The scratch of one call, carved from the caller's workspace: the matrix table, per-matrix
+// flags and statistics, the scan's row slots, the candidates' CSR, the closure's workspace and
+// row index, and the row pool in whatever remains.
+struct TriLayout {
     TriComp *dc;
-    int64_t *dpre, *indptr;
+    int64_t *dpre, *indptr, *row_off;
     unsigned *cflags;
-    int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val;
+    int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val, *row_len, *p_col, *p_val;
     int *cam, *cfm;
     unsigned long long *cprod;
-    void *tmp;
-    {
-        Carve dry{nullptr};
-        layout(dry, dc, dpre, cflags, ckind, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr,
-               tmp, a_col, a_val);
-        const int rc = tri_reserve(g_tri_a, dry.off + 256, s);
-        if (rc) return rc;
-    }
-    Carve cv{g_tri_a.p};
-    layout(cv, dc, dpre, cflags, ckind, cam, cfm, cprod, row_cnt, row_comp, slot_col, slot_val, indptr, tmp,
-           a_col, a_val);
-    const bool same = g_tri_last_buf == g_tri_a.p && g_tri_last_comps.size() == C &&
-                      memcmp(g_tri_last_comps.data(), hc.data(), C * sizeof(TriComp)) == 0;
-    if (!same) {
-        RBG_CUDA_TRY(cudaMemcpyAsync(dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
-        RBG_CUDA_TRY(cudaMemcpyAsync(dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
-        g_tri_last_comps = hc;
-        g_tri_last_buf = g_tri_a.p;
-    }
-    RBG_CUDA_TRY(cudaMemsetAsync(cflags, 0, C * 4, s));
+    TriOut *res;
+    void *tmp, *dag_ws;
+    size_t scan_tmp;
+    int64_t pool;
+    size_t fixed;                            // bytes before the pool
+};
 
+void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLayout &L) {
+    Carve cv{base};
+    L.scan_tmp = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, L.scan_tmp, (int64_t *)nullptr, (int64_t *)nullptr, (int)(NR + 1));
+    L.dc = cv.take<TriComp>(C);
+    L.dpre = cv.take<int64_t>(C + 1);
+    L.cflags = cv.take<unsigned>(C);
+    L.ckind = cv.take<int32_t>(C);
+    L.cam = cv.take<int>(C);
+    L.cfm = cv.take<int>(C);
+    L.cprod = cv.take<unsigned long long>(C);
+    L.res = cv.take<TriOut>(C);
+    L.row_cnt = cv.take<int32_t>(NR);
+    L.row_comp = cv.take<int32_t>(NR);
+    L.slot_col = cv.take<int32_t>(NR * TRI_CAP);
+    L.slot_val = cv.take<int32_t>(NR * TRI_CAP);
+    L.indptr = cv.take<int64_t>(NR + 1);
+    L.tmp = cv.take<unsigned char>(L.scan_tmp);
+    L.a_col = cv.take<int32_t>(NR * TRI_CAP);
+    L.a_val = cv.take<int32_t>(NR * TRI_CAP);
+    L.dag_ws = cv.take<unsigned char>(dag_workspace_for((int64_t)NR, (int64_t)(NR * TRI_CAP)));
+    L.row_off = cv.take<int64_t>(NR);
+    L.row_len = cv.take<int32_t>(NR);
+    L.fixed = align_up(cv.off, 256);
+    const size_t rest = ws_bytes > L.fixed + 256 ? ws_bytes - L.fixed - 256 : 0;
+    L.pool = (int64_t)(rest / 8 / 64 * 64);  // column and value halves
+    L.p_col = base ? reinterpret_cast<int32_t *>(base + L.fixed) : nullptr;
+    L.p_val = base ? reinterpret_cast<int32_t *>(base + align_up(L.fixed + (size_t)L.pool * 4, 256)) : nullptr;
+}
+
+struct TriShape {
+    int64_t count, R, ctas;
+    int64_t ld_in, ld_out;
+};
+
+// Every launch of the DAG path, in stream order, with no host synchronisation when `captured`
+// (the level loop then is a while node).  Returns the number of kernel launches issued.
+template <typename T>
+int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cudaStream_t s, bool captured,
+                const RowStats &rs, DagCounters **dcount, int64_t *launches) {
+    const int64_t R = sh.R;
+    const int count = (int)sh.count;
+    RBG_CUDA_TRY(cudaMemsetAsync(L.cflags, 0, (size_t)count * 4, s));
     // 1. scan
     {
         cudaEvent_t t = timer_begin(4, s);
         note_launches(1);
-        tri_scan_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, dc, dpre, (int)count, slot_col, slot_val,
-                                                                 row_cnt, row_comp, cflags);
+        tri_scan_kernel<T><<<(unsigned)sh.ctas, TRI_THREADS, 0, s>>>(in, sh.ld_in, L.dc, L.dpre, count, L.slot_col,
+                                                                     L.slot_val, L.row_cnt, L.row_comp, L.cflags);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(4, t, s);
     }
     // 2. CSR of the candidates and their closure by levels
     cudaEvent_t tdag = timer_begin(5, s);
-    note_launches(3);
-    tri_kind_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>((int)count, dc, cflags,
-                                                                                          ckind);
-    tri_count_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, row_cnt, row_comp, ckind, indptr);
-    RBG_CUDA_TRY(cudaMemsetAsync(indptr + R, 0, 8, s));
-    size_t tb = scan_tmp;
-    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(tmp, tb, indptr, indptr, (int)(R + 1), s));
-    int64_t nnz_a = 0;
-    RBG_CUDA_TRY(cudaMemcpyAsync(&nnz_a, indptr + R, 8, cudaMemcpyDeviceToHost, s));
-    tri_csr_fill_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, row_comp, ckind, dc, indptr, slot_col, slot_val, a_col,
-                                                        a_val);
+    note_launches(4);
+    tri_kind_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>(count, L.dc, L.cflags,
+                                                                                          L.ckind, L.cam, L.cfm,
+                                                                                          L.cprod);
+    tri_count_kernel<<<grid_for(R + 1, 256), 256, 0, s>>>(R, L.row_cnt, L.row_comp, L.ckind, L.indptr);
+    size_t tb = L.scan_tmp;
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb, L.indptr, L.indptr, (int)(R + 1), s));
+    tri_csr_fill_kernel<<<grid_for(R, 256), 256, 0, s>>>(R, L.row_comp, L.ckind, L.dc, L.indptr, L.slot_col,
+                                                        L.slot_val, L.a_col, L.a_val);
     RBG_CUDA_TRY(cudaGetLastError());
-    std::vector<int32_t> kind(C);
-    RBG_CUDA_TRY(cudaMemcpyAsync(kind.data(), ckind, C * 4, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
-    int64_t candidates = 0;
-    for (size_t i = 0; i < C; ++i) candidates += kind[i] != KIND_NONE;
-    if (candidates == 0) {
-        timer_end(5, tdag, s);
-        return RBG_OK;
-    }
-    rbg_csr_t A{R, R, indptr, a_col, a_val};
-    int64_t dws = 0;
-    int rc = rbg_dag_workspace_bytes(R, nnz_a, &dws);
+    *launches += 5;
+    rbg_csr_t A{R, R, L.indptr, L.a_col, L.a_val};
+    int rc = dag_enqueue(&A, R * TRI_CAP, L.dag_ws, L.p_col, L.p_val, L.pool, L.row_off, L.row_len, s, captured,
+                         dcount, launches);
     if (rc) return rc;
-    int64_t pool = std::max<int64_t>(16 * nnz_a + R, 1024);
-    int32_t *p_col = nullptr, *p_val = nullptr, *row_len = nullptr;
-    int64_t *row_off = nullptr;
-    int64_t used = 0;
-    for (int attempt = 0;; ++attempt) {
-        Carve dry{nullptr};
-        dry.take<unsigned char>((size_t)dws);
-        dry.take<int32_t>((size_t)pool);
-        dry.take<int32_t>((size_t)pool);
-        dry.take<int64_t>(NR);
-        dry.take<int32_t>(NR);
-        rc = tri_reserve(g_tri_b, dry.off + 256, s);
-        if (rc) return rc;
-        Carve cb{g_tri_b.p};
-        void *dw = cb.take<unsigned char>((size_t)dws);
-        p_col = cb.take<int32_t>((size_t)pool);
-        p_val = cb.take<int32_t>((size_t)pool);
-        row_off = cb.take<int64_t>(NR);
-        row_len = cb.take<int32_t>(NR);
-        int64_t mx = 0, levels = 0;
-        used = 0;
-        rc = rbg_dag_closure(&A, dw, dws, p_col, p_val, pool, row_off, row_len, &used, &mx, &levels,
-                             reinterpret_cast<rbg_stream_t>(s));
-        if (rc == RBG_ERR_CAPACITY && used > pool && attempt < 4) {
-            pool = used;
-            continue;
-        }
-        break;
-    }
     timer_end(5, tdag, s);
-    if (rc == RBG_ERR_CAPACITY || rc == RBG_ERR_CYCLE) return RBG_OK;   // the blocked kernels decide
-    if (rc) return rc;
-
     // 3. statistics
     {
         cudaEvent_t t = timer_begin(6, s);
-        RBG_CUDA_TRY(cudaMemsetAsync(cam, 0xff, C * 4, s));
-        RBG_CUDA_TRY(cudaMemsetAsync(cfm, 0xff, C * 4, s));
-        RBG_CUDA_TRY(cudaMemsetAsync(cprod, 0, C * 8, s));
         note_launches(1);
         tri_stats_kernel<<<grid_for(R * 32, TRI_THREADS), TRI_THREADS, 0, s>>>(
-            R, row_comp, ckind, dc, indptr, a_col, a_val, row_off, row_len, p_col, p_val, cam, cfm, cprod);
+            R, L.row_comp, L.ckind, L.dc, L.indptr, L.a_col, L.a_val, L.row_off, L.row_len, L.p_col, L.p_val, *dcount,
+            L.cam, L.cfm, L.cprod);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(6, t, s);
     }
     // 4. dense rows of the accepted matrices (decided on the device from the statistics)
     {
         cudaEvent_t t = timer_begin(7, s);
-        note_launches(1);
-        tri_write_kernel<<<(unsigned)pre[C], TRI_THREADS, 0, s>>>(in, out, dc, dpre, (int)count, ckind, cam,
-                                                                  row_off, row_len, p_col, p_val, rs);
+        note_launches(2);
+        tri_write_kernel<T><<<(unsigned)sh.ctas, TRI_THREADS, 0, s>>>(in, sh.ld_in, out, sh.ld_out, L.dc, L.dpre,
+                                                                      count, L.ckind, L.cam, *dcount, R, L.row_off,
+                                                                      L.row_len, L.p_col, L.p_val, rs);
+        tri_result_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>(
+            count, L.ckind, L.cam, L.cfm, L.cprod, *dcount, R, L.res);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(7, t, s);
     }
-    std::vector<int> ham(C), hfm(C);
-    std::vector<unsigned long long> hprod(C);
-    RBG_CUDA_TRY(cudaMemcpyAsync(ham.data(), cam, C * 4, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaMemcpyAsync(hfm.data(), cfm, C * 4, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaMemcpyAsync(hprod.data(), cprod, C * 8, cudaMemcpyDeviceToHost, s));
+    *launches += 3;
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// RBG_MODE_GRAPH: the whole sequence recorded once per layout and replayed
+// ------------------------------------------------------------------------------------------
+struct TriGraphKey {
+    int device, tbytes;
+    const void *in;
+    void *out;
+    unsigned char *ws;
+    size_t ws_bytes;
+    int64_t ld_in, ld_out;
+    std::vector<int64_t> sizes, in_off, out_off;
+    RowStats rs;
+    bool operator==(const TriGraphKey &o) const {
+        return device == o.device && tbytes == o.tbytes && in == o.in && out == o.out && ws == o.ws &&
+               ws_bytes == o.ws_bytes && ld_in == o.ld_in && ld_out == o.ld_out && sizes == o.sizes &&
+               in_off == o.in_off && out_off == o.out_off && rs == o.rs;
+    }
+};
+struct TriGraph {
+    TriGraphKey key;
+    cudaGraphExec_t exec;
+    DagCounters *dcount;
+    int64_t launches;                        // outside the level loop
+    unsigned long long stamp;
+};
+std::mutex g_tri_graph_mu;
+std::vector<TriGraph> g_tri_graphs;
+unsigned long long g_tri_clock = 0;
+constexpr size_t TRI_GRAPH_CACHE = 8;
+
+// Record the sequence into a graph on a private stream (the caller's may be the legacy default
+// stream, which cannot be captured); nothing runs while recording.
+template <typename T>
+int tri_record(const TriShape &sh, const TriLayout &L, const T *in, T *out, const RowStats &rs, TriGraph &g) {
+    static thread_local cudaStream_t cap = nullptr;
+    if (!cap) RBG_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    RBG_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    launch_recording(true);
+    int64_t launches = 0;
+    const int rc = tri_enqueue<T>(sh, L, in, out, cap, true, rs, &g.dcount, &launches);
+    launch_recording(false);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cap, &graph);
+    if (rc || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc ? rc : RBG_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return RBG_ERR_CUDA;
+    g.launches = launches;
+    return RBG_OK;
+}
+
+}  // namespace
+
+template <typename T>
+int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const int64_t *out_off, int64_t ld_in,
+              int64_t ld_out, const T *in, T *out, rbg_result_t *results, char *closed, unsigned char *ws,
+              size_t ws_bytes, uint32_t mode, cudaStream_t s, const RowStats &rs) {
+    if (count <= 0 || count > INT32_MAX || !ws) return RBG_OK;
+    std::vector<TriComp> hc((size_t)count);
+    std::vector<int64_t> pre((size_t)count + 1, 0);
+    int64_t R = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const int64_t n = (sizes[i] > 0 && sizes[i] <= TRI_MAX_N) ? sizes[i] : 0;
+        hc[(size_t)i] = TriComp{n, in_off[i], out_off[i], R};
+        R += n;
+        pre[(size_t)i + 1] = pre[(size_t)i] + (n + TRI_ROWS - 1) / TRI_ROWS;
+    }
+    if (R == 0 || R * TRI_CAP > INT32_MAX) return RBG_OK;
+    const size_t C = (size_t)count, NR = (size_t)R;
+    TriLayout L;
+    tri_layout(nullptr, ws_bytes, C, NR, L);
+    if (L.pool < 4 * R) return RBG_OK;       // no room for a closure: the other paths decide
+    tri_layout(ws, ws_bytes, C, NR, L);
+    const TriShape sh{count, R, pre[C], ld_in, ld_out};
+    RBG_CUDA_TRY(cudaMemcpyAsync(L.dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(L.dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
+
+    DagCounters *dcount = nullptr;
+    int64_t fixed_launches = -1;             // >= 0: a graph ran; its level loop is counted below
+    if ((mode & RBG_MODE_GRAPH) && !timer_on()) {
+        int dev = 0;
+        RBG_CUDA_TRY(cudaGetDevice(&dev));
+        TriGraphKey key{dev, (int)sizeof(T), in, out, ws, ws_bytes, ld_in, ld_out,
+                        std::vector<int64_t>(sizes, sizes + count), std::vector<int64_t>(in_off, in_off + count),
+                        std::vector<int64_t>(out_off, out_off + count), rs};
+        std::lock_guard<std::mutex> lk(g_tri_graph_mu);
+        TriGraph *hit = nullptr;
+        for (auto &e : g_tri_graphs)
+            if (e.key == key) hit = &e;
+        if (!hit) {
+            TriGraph g;
+            g.key = std::move(key);
+            const int rc = tri_record<T>(sh, L, in, out, rs, g);
+            if (rc) return rc;
+            if (g_tri_graphs.size() >= TRI_GRAPH_CACHE) {
+                size_t old = 0;
+                for (size_t k = 1; k < g_tri_graphs.size(); ++k)
+                    if (g_tri_graphs[k].stamp < g_tri_graphs[old].stamp) old = k;
+                RBG_CUDA_TRY(cudaDeviceSynchronize());   // the evicted graph may still run on another stream
+                cudaGraphExecDestroy(g_tri_graphs[old].exec);
+                g_tri_graphs.erase(g_tri_graphs.begin() + (long)old);
+            }
+            g_tri_graphs.push_back(std::move(g));
+            hit = &g_tri_graphs.back();
+        }
+        hit->stamp = ++g_tri_clock;
+        RBG_CUDA_TRY(cudaGraphLaunch(hit->exec, s));
+        dcount = hit->dcount;
+        fixed_launches = hit->launches;
+    } else {
+        int64_t launches = 0;
+        const int rc = tri_enqueue<T>(sh, L, in, out, s, false, rs, &dcount, &launches);
+        if (rc) return rc;
+    }
+    std::vector<TriOut> h(C);
+    DagCounters hd;
+    RBG_CUDA_TRY(cudaMemcpyAsync(h.data(), L.res, C * sizeof(TriOut), cudaMemcpyDeviceToHost, s));
+    RBG_CUDA_TRY(cudaMemcpyAsync(&hd, dcount, sizeof(hd), cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (fixed_launches >= 0) {
+        const int64_t iters = std::max<int64_t>(1, (hd.nlevels + DAG_GRAPH_CHUNK - 1) / DAG_GRAPH_CHUNK);
+        note_launches(fixed_launches + iters * (3 * DAG_GRAPH_CHUNK + 1));
+    }
     for (size_t i = 0; i < C; ++i) {
-        if (kind[i] == KIND_NONE || ham[i] >= TRI_TOP) continue;
+        if (!h[i].accepted) continue;
         closed[i] = 1;
         rbg_result_t &r = results[i];
         r.status = RBG_OK;
         r.flags = 0;
-        r.diameter = hfm[i] > 0 ? hfm[i] : 0;
+        r.diameter = h[i].diameter;
         r.k = r.i = r.j = -1;
         r.path = RBG_PATH_DAG;
-        r.executed = (int64_t)hprod[i];
+        r.executed = (int64_t)h[i].executed;
     }
     return RBG_OK;
 }
 
+template int tri_batch<int32_t>(int64_t, const int64_t *, const int64_t *, const int64_t *, int64_t, int64_t,
+                                const int32_t *, int32_t *, rbg_result_t *, char *, unsigned char *, size_t, uint32_t,
+                                cudaStream_t, const RowStats &);
+template int tri_batch<int64_t>(int64_t, const int64_t *, const int64_t *, const int64_t *, int64_t, int64_t,
+                                const int64_t *, int64_t *, rbg_result_t *, char *, unsigned char *, size_t, uint32_t,
+                                cudaStream_t, const RowStats &);
+
 }  // namespace rbg
 
+// Frees the DAG path's cached CUDA graphs (device memory is never held by this library outside
+// rbg_fw_dense_noalloc's fixed array).
 extern "C" int32_t rbg_release_scratch(void) {
-    std::lock_guard<std::mutex> lk(rbg::g_tri_mu);
-    for (rbg::TriScratch *t : {&rbg::g_tri_a, &rbg::g_tri_b}) {
-        if (t->p) {
-            int cur = 0;
-            RBG_CUDA_TRY(cudaGetDevice(&cur));
-            if (t->device != cur) RBG_CUDA_TRY(cudaSetDevice(t->device));
-            RBG_CUDA_TRY(cudaDeviceSynchronize());
-            RBG_CUDA_TRY(cudaFree(t->p));
-            if (t->device != cur) RBG_CUDA_TRY(cudaSetDevice(cur));
-        }
-        t->p = nullptr;
-        t->cap = 0;
-        t->device = -1;
-    }
-    rbg::g_tri_last_buf = nullptr;
+    std::lock_guard<std::mutex> lk(rbg::g_tri_graph_mu);
+    if (!rbg::g_tri_graphs.empty()) RBG_CUDA_TRY(cudaDeviceSynchronize());
+    for (auto &g : rbg::g_tri_graphs) cudaGraphExecDestroy(g.exec);
+    rbg::g_tri_graphs.clear();
     return RBG_OK;
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <limits.h>
+#include <mutex>
 #include "avos.cuh"
 #include "../../include/rbg_gb300.h"
 
@@ -38,8 +39,38 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // grid size for grid-stride loops: a multiple of the SM count
 int grid_for(int64_t work, int threads);
 
-// running count of kernel launches issued by this library (rbg_launch_count)
+// SM count of the current device
+int sm_count();
+
+// Kernel attributes set with cudaFuncSetAttribute (dynamic shared memory above 48 KB) belong to
+// the context of the device that was current, so a process driving several GPUs sets them once
+// per device: run() calls `configure` the first time it sees the current device and returns that
+// status on every later call on the device.
+class PerDeviceOnce {
+public:
+    template <typename F> int run(F &&configure) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return RBG_ERR_CUDA;
+        if (dev < 0 || dev >= kMaxDevices) return RBG_ERR_INVALID;
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!done_[dev]) {
+            rc_[dev] = configure();
+            done_[dev] = true;
+        }
+        return rc_[dev];
+    }
+    static constexpr int kMaxDevices = 64;
+
+private:
+    std::mutex mu_;
+    bool done_[kMaxDevices] = {};
+    int rc_[kMaxDevices] = {};
+};
+
+// running count of kernel launches issued by this library (rbg_launch_count); while a graph is
+// being recorded (launch_recording(true)) launches are counted when the graph runs instead
 void note_launches(int64_t k);
+void launch_recording(bool on);
 
 // Benchmark timer (rbg_profile_begin / rbg_profile_end_slots): CUDA events around the kernels
 // of each slot, recorded on the launching stream while the timer is on.  Slots: 0 phase-3
@@ -68,12 +99,34 @@ struct RowStats {
     }
 };
 
-// fw_tri.cu: the components of an int32 batch whose off-diagonal entries all lie on one side of
-// the diagonal (vertices numbered in a topological order) and are in the clean regime, closed
-// through the DAG closure by levels; sets closed[i] and results[i] for each of them and leaves
-// every other component untouched.
-int tri_batch(int64_t count, const int64_t *sizes, const int64_t *offsets, const int32_t *in, int32_t *out,
-              rbg_result_t *results, char *closed, cudaStream_t stream, const RowStats &rs);
+// dag.cu: the closure by levels as an enqueue-only sequence for callers inside this library.
+// The workspace is laid out for at most `nnz_bound` stored entries of A, so nothing is read back
+// before the levels.  With `captured` the stream is being captured into a CUDA graph and the
+// level loop becomes a while node that the device ends when a level comes out empty (no host
+// synchronisation at all); otherwise the host looks at the frontier once per chunk of levels.
+// The device counters (DagCounters) are left in the workspace for the caller to read later.
+struct DagCounters {
+    int placed, nwide, flags, nlevels;       // flags: 1 pool too small, 2 row past the block table
+    unsigned long long reserved, max_abs, total;
+    long long level;                         // the graph loop's level counter
+};
+size_t dag_workspace_for(int64_t n, int64_t nnz_bound);
+int dag_enqueue(const rbg_csr_t *A, int64_t nnz_bound, void *workspace, int32_t *pool_cols, int32_t *pool_vals,
+                int64_t pool_capacity, int64_t *row_off, int32_t *row_len, cudaStream_t s, bool captured,
+                DagCounters **counters, int64_t *launches);
+constexpr int DAG_GRAPH_CHUNK = 4;           // levels per iteration of the graph's while node
+
+// fw_tri.cu: the components of an int32 or int64 batch whose off-diagonal entries all lie on one
+// side of the diagonal (vertices numbered in a topological order) and are in the clean regime,
+// closed through the DAG closure by levels; sets closed[i] and results[i] for each of them and
+// leaves every other component untouched.  Scratch comes from the caller's workspace (`ws`,
+// `ws_bytes`); a workspace too small for a closure leaves its components to the other paths.
+// ld_in / ld_out are the row strides of every block (0: each block's own n).  With
+// RBG_MODE_GRAPH in `mode` the whole sequence is replayed from a cached CUDA graph.
+template <typename T>
+int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const int64_t *out_off, int64_t ld_in,
+              int64_t ld_out, const T *in, T *out, rbg_result_t *results, char *closed, unsigned char *ws,
+              size_t ws_bytes, uint32_t mode, cudaStream_t stream, const RowStats &rs);
 
 template <typename T> struct dtype_of;
 template <> struct dtype_of<int8_t> { static const int value = RBG_DTYPE_INT8; };

@@ -54,11 +54,17 @@ class Workspace:
             return self._buf
 
 
-_default_ws = Workspace()
+_default_ws = threading.local()
 
 
 def default_workspace() -> Workspace:
-    return _default_ws
+    """The calling thread's workspace.  Every closure call synchronises its stream before it
+    returns, so one thread's calls never overlap on the GPU; calls from different threads (each
+    on its own stream) get different buffers and can run at the same time."""
+    ws = getattr(_default_ws, "ws", None)
+    if ws is None:
+        ws = _default_ws.ws = Workspace()
+    return ws
 
 
 def to_device(a: np.ndarray, device: torch.device | None = None,

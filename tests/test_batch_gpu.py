@@ -66,10 +66,13 @@ def test_cython_batch(native):
         assert r.status == so == 0 and (W == Wo).all() and r.diameter == do
 
 
-def test_graph_replay_matches_direct_launches(native):
-    """RBG_MODE_GRAPH: the first call records the batch's launch sequence, later calls with the
-    same sizes, offsets and buffers replay it; results (values, diameters, fallbacks) equal the
-    direct launches, also after the input changes in place between replays."""
+@pytest.mark.parametrize("extra", ["dag", "blocked"])
+def test_graph_replay_matches_direct_launches(native, extra):
+    """RBG_MODE_GRAPH: the first call records the batch's launch sequence (the DAG path with its
+    level loop as a device-driven while node, or with RBG_MODE_NO_DAG the blocked kernels), later
+    calls with the same sizes, offsets and buffers replay it; results (values, diameters,
+    fallbacks) equal the direct launches, also after the input changes in place between
+    replays."""
     import torch
     from redblackgraph_gb300 import synth, _lib
     from redblackgraph_gb300.dense import fw_batch, pack
@@ -82,12 +85,13 @@ def test_graph_replay_matches_direct_launches(native):
     flat, sz, off = pack(mats)
     d = to_device(flat)
     out = torch.empty_like(d)
-    ref, rres = fw_batch(d, sz, off, out=torch.empty_like(d))
+    base = _lib.MODE_NO_DAG if extra == "blocked" else 0
+    ref, rres = fw_batch(d, sz, off, out=torch.empty_like(d), mode=base)
     ref = to_host(ref)
     L = native
     for rep in range(3):
         l0 = L.rbg_launch_count()
-        _, res = fw_batch(d, sz, off, out=out, mode=_lib.MODE_GRAPH)
+        _, res = fw_batch(d, sz, off, out=out, mode=_lib.MODE_GRAPH | base)
         torch.cuda.synchronize()
         assert L.rbg_launch_count() > l0                     # replays count their launches
         assert (to_host(out) == ref).all()
@@ -97,7 +101,7 @@ def test_graph_replay_matches_direct_launches(native):
              for n, s in zip(sizes, seeds)] + [cyc]
     flat2, _, _ = pack(mats2)
     d.copy_(to_device(flat2))
-    _, res2 = fw_batch(d, sz, off, out=out, mode=_lib.MODE_GRAPH)
+    _, res2 = fw_batch(d, sz, off, out=out, mode=_lib.MODE_GRAPH | base)
     torch.cuda.synchronize()
     h = to_host(out)
     for A, o, n, r in zip(mats2[:-1], off, sz, res2):
@@ -119,7 +123,7 @@ def test_tile_shapes_and_autotune_match_oracle(native, mode_name):
             for n, s in zip(sizes, seeds)]
     flat, sz, off = pack(mats)
     d = to_device(flat)
-    mode = getattr(_lib, mode_name)
+    mode = getattr(_lib, mode_name) | _lib.MODE_NO_DAG   # the blocked kernels are the subject
     for _ in range(2):
         out, res = fw_batch(d, sz, off, out=torch.empty_like(d), mode=mode)
         torch.cuda.synchronize()
@@ -140,18 +144,20 @@ def _random_dag(rng, n, density, above=False, vmax=8):
     return A[::-1, ::-1].copy() if above else A
 
 
+@pytest.mark.parametrize("dtype", [np.int32, np.int64])
 @pytest.mark.parametrize("in_place", [False, True])
-def test_dag_path_vs_oracle(native, in_place):
-    """int32 matrices numbered in a topological order (entries all below, or all above, the
-    diagonal) take the DAG path; values, diameters (each cell's first value) and errors equal
-    the oracle's sequential loop, in both semantics."""
+def test_dag_path_vs_oracle(native, in_place, dtype):
+    """int32 and int64 matrices numbered in a topological order (entries all below, or all
+    above, the diagonal) take the DAG path; values, diameters (each cell's first value) and
+    errors equal the oracle's sequential loop, in both semantics (Cython: int32 only)."""
     from redblackgraph_gb300 import synth, _lib
     rng = np.random.default_rng(7)
-    mats = [_random_dag(rng, int(rng.integers(1, 90)), rng.uniform(0.02, 0.4), above=t % 2 == 1).astype(np.int32)
+    mats = [_random_dag(rng, int(rng.integers(1, 90)), rng.uniform(0.02, 0.4), above=t % 2 == 1).astype(dtype)
             for t in range(60)]
-    mats += [synth.pedigree(n, synth.generations_for(n), n, dtype=np.int32) for n in (300, 700, 1500)]
-    mats += [synth.pedigree(500, 12, 9, dtype=np.int32)[::-1, ::-1].copy()]   # pedigree above the diagonal
-    for mode, oracle in ((0, O.warshall), (_lib.MODE_CYTHON, O.fw_cython)):
+    mats += [synth.pedigree(n, synth.generations_for(n), n, dtype=dtype) for n in (300, 700, 1500)]
+    mats += [synth.pedigree(500, 12, 9, dtype=dtype)[::-1, ::-1].copy()]   # pedigree above the diagonal
+    semantics = ((0, O.warshall), (_lib.MODE_CYTHON, O.fw_cython)) if dtype == np.int32 else ((0, O.warshall),)
+    for mode, oracle in semantics:
         Ws, res = run_batch(mats, mode=mode, in_place=in_place)
         dag = 0
         for A, W, r in zip(mats, Ws, res):
@@ -206,15 +212,36 @@ def test_dag_path_mixed_batch_and_opt_out(native):
             assert (W == W2).all() and r.diameter == r2.diameter
 
 
-def test_dag_path_scratch_release(native):
-    """rbg_release_scratch frees the DAG path's device scratch; the next call allocates it again
+def test_dag_path_graph_release(native):
+    """rbg_release_scratch frees the DAG path's cached CUDA graphs; the next call records again
     and gives the same results."""
     from redblackgraph_gb300 import synth, _lib
     mats = [synth.pedigree(n, 9, n, dtype=np.int32) for n in (40, 300, 900)]
-    Ws, res = run_batch(mats)
+    Ws, res = run_batch(mats, mode=_lib.MODE_GRAPH)
     assert all(r.path == _lib.PATH_DAG for r in res)
     _lib.check(_lib.load().rbg_release_scratch(), "release_scratch")
     _lib.check(_lib.load().rbg_release_scratch(), "release_scratch")     # twice is harmless
-    Ws2, res2 = run_batch(mats)
+    Ws2, res2 = run_batch(mats, mode=_lib.MODE_GRAPH)
     for W, W2, r, r2 in zip(Ws, Ws2, res, res2):
         assert (W == W2).all() and r.diameter == r2.diameter and r2.path == _lib.PATH_DAG
+
+
+def test_dag_path_int64_mixed_batch(native):
+    """int64 storage: pedigrees take the DAG path; values past 31 bits (in the input or in a
+    product) send their matrix to the blocked kernels with 64-bit lanes; every result is the
+    oracle's."""
+    from redblackgraph_gb300 import synth, _lib
+    ped = synth.pedigree(400, 14, 21, dtype=np.int64)
+    big_in = ped.copy()
+    big_in[399, 0] = 1 << 40                                         # an input value past 31 bits
+    deep = np.zeros((45, 45), np.int64)
+    np.fill_diagonal(deep, -1)
+    for i in range(1, 45):
+        deep[i, i - 1] = 2                                           # products reach bit 44
+    mats = [ped, big_in, deep, synth.pedigree(64, 6, 8, dtype=np.int64)[::-1, ::-1].copy()]
+    Ws, res = run_batch(mats)
+    for A, W, r in zip(mats, Ws, res):
+        Wo, do, so, _ = O.warshall(A)
+        assert r.status == so == 0
+        assert (W == Wo).all() and r.diameter == do
+    assert [r.path for r in res] == [_lib.PATH_DAG, _lib.PATH_BLOCKED64, _lib.PATH_BLOCKED64, _lib.PATH_DAG]

@@ -87,12 +87,70 @@ def test_unclean_random_triu_exact_path(native, seed):
 
 
 def test_forced_exact_equals_blocked(native):
+    """The same pedigree on the DAG path (the default for a matrix numbered oldest first), on
+    the blocked kernels (RBG_MODE_NO_DAG) and on the exact sequential-order kernel."""
     from redblackgraph_gb300 import synth, _lib
     A = synth.pedigree(333, 15, 5, dtype=np.int32)
-    W1, r1 = gpu_close(A)
+    W0, r0 = gpu_close(A)
+    W1, r1 = gpu_close(A, mode=_lib.MODE_NO_DAG)
     W2, r2 = gpu_close(A, mode=_lib.MODE_FORCE_EXACT)
-    assert r1.path == _lib.PATH_BLOCKED32 and r2.path == _lib.PATH_EXACT
-    assert (W1 == W2).all() and r1.diameter == r2.diameter
+    assert r0.path == _lib.PATH_DAG and r1.path == _lib.PATH_BLOCKED32 and r2.path == _lib.PATH_EXACT
+    assert (W0 == W1).all() and (W1 == W2).all() and r0.diameter == r1.diameter == r2.diameter
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64])
+@pytest.mark.parametrize("above", [False, True])
+def test_single_matrix_dag_path(native, dtype, above):
+    """rbg_fw_dense takes the DAG path for an int32 or int64 matrix numbered in a topological
+    order (entries below the diagonal, or above it), out of place, in place and into rows with a
+    longer stride; values, diameter and status are the oracle's sequential loop's."""
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.dense import fw_dense
+    from redblackgraph_gb300.device import to_device, to_host
+    for n, gens in ((1, 1), (7, 3), (300, 12), (1025, 15), (2000, 30)):
+        A = synth.pedigree(n, gens, seed=n + 3, dtype=dtype)
+        if above:
+            A = A[::-1, ::-1].copy()
+        Wo, do, so, _ = O.warshall(A)
+        assert so == 0
+        W, res = gpu_close(A)
+        assert res.path == _lib.PATH_DAG and res.status == 0, (n, res.path)
+        assert (W == Wo).all() and res.diameter == do
+        d = to_device(A)
+        _, ri = fw_dense(d, out=d)                        # in place
+        assert ri.path == _lib.PATH_DAG and (to_host(d) == Wo).all() and ri.diameter == do
+        big = torch.full((n, n + 5), 77, dtype=d.dtype, device=d.device)
+        view = big[:, 2:n + 2]                            # rows 16-byte misaligned, stride n + 5
+        _, rv = fw_dense(to_device(A), out=view)
+        torch.cuda.synchronize()
+        hb = big.cpu().numpy()
+        assert rv.path == _lib.PATH_DAG and (hb[:, 2:n + 2] == Wo).all()
+        assert (hb[:, :2] == 77).all() and (hb[:, n + 2:] == 77).all()   # nothing outside the view
+
+
+def test_single_matrix_dag_path_graph_mode(native):
+    """RBG_MODE_GRAPH on a single matrix: recorded once (level loop as a device-driven while
+    node), replayed on later calls; every call equals the direct launches and the oracle, also
+    after the input changes in place."""
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.dense import fw_dense
+    from redblackgraph_gb300.device import to_device, to_host
+    A = synth.pedigree(1500, 25, 4, dtype=np.int64)
+    Wo, do, so, _ = O.warshall(A)
+    d = to_device(A)
+    out = torch.empty_like(d)
+    for _ in range(3):
+        _, r = fw_dense(d, out=out, mode=_lib.MODE_GRAPH)
+        torch.cuda.synchronize()
+        assert r.path == _lib.PATH_DAG and (to_host(out) == Wo).all() and r.diameter == do
+    B = synth.pedigree(1500, 25, 5, dtype=np.int64)
+    Wb, db, _, _ = O.warshall(B)
+    d.copy_(to_device(B))
+    _, r = fw_dense(d, out=out, mode=_lib.MODE_GRAPH)
+    torch.cuda.synchronize()
+    assert r.path == _lib.PATH_DAG and (to_host(out) == Wb).all() and r.diameter == db
 
 
 def test_wide_lanes_int64(native):

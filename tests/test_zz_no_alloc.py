@@ -60,6 +60,50 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(native):
         assert (to_host(d) == A).all()          # the input is left untouched
 
 
+def _wide_int64():
+    """A pedigree whose int64 closure values pass 2^31 without overflowing 64 bits (64-bit lanes
+    of the blocked kernels)."""
+    from redblackgraph_gb300 import synth
+    A = synth.pedigree(200, 10, 9, dtype=np.int64)
+    return np.where(A > 1, A << 8, A)
+
+
+def _unclean_int32(n):
+    """Random upper-triangular values 0..3 (value 1 off the diagonal): the exact kernel."""
+    rs = np.random.RandomState(5)
+    A = np.triu(rs.randint(0, 4, size=(n, n)), k=1)
+    np.fill_diagonal(A, rs.choice([-1, 1], size=n))
+    return A.astype(np.int32)
+
+
+def test_noalloc_every_path_inside_its_array(native):
+    """The fixed array also holds the scratch of the other paths a closure can take: the DAG
+    path, the blocked kernels with 64-bit lanes and the exact sequential-order kernel (with its
+    status block).  Each case runs twice in a row and equals the workspace entry point, path
+    included."""
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.device import to_device, to_host
+    L = native
+    cases = [(synth.pedigree(900, 15, 3, dtype=np.int32), _lib.PATH_DAG),
+             (_wide_int64(), _lib.PATH_BLOCKED64),
+             (_unclean_int32(300), _lib.PATH_EXACT),
+             (synth.pedigree(_lib.NOALLOC_MAX_N, 20, 4, dtype=np.int64), _lib.PATH_DAG)]
+    for A, path in cases:
+        d = to_device(A)
+        ref_out = torch.empty_like(d)
+        ref = _close_with_workspace(L, _lib, d, ref_out)
+        assert ref.path == path
+        for _ in range(2):
+            out = torch.full_like(d, 5)
+            res = _close_without_workspace(L, _lib, d, out)
+            torch.cuda.synchronize()
+            assert (res.status, res.diameter, res.path) == (ref.status, ref.diameter, ref.path)
+            assert (res.k, res.i, res.j) == (ref.k, ref.i, ref.j)
+            if ref.status == _lib.RBG_OK:
+                assert (to_host(out) == to_host(ref_out)).all()
+
+
 def test_noalloc_refuses_sizes_beyond_its_array(native):
     import torch
     from redblackgraph_gb300 import _lib
