@@ -39,6 +39,9 @@ COUNT, LO, HI, SEED = 4096, 16, 4096, 3
 CPU_SAMPLE_RELAX = 6.0e10        # bounded CPU sample: ~10-30 s of C warshall on the host cores
 METRIC = "avos_relaxations_per_s"
 UNIT = "relax/s"
+# int32 operations per dense AVOS relaxation in the ALU roofline (shift, and, or for the product,
+# min for the sum); the blocked kernels execute 2 (IMAD + IMNMX) after their lane encoding
+OPS_PER_RELAXATION = 4
 
 
 def parse():
@@ -76,11 +79,11 @@ def workload(rank: int):
     return dict(sizes=sizes, seeds=seeds, forest=forest, csizes=csizes, cstart=cstart, order=order)
 
 
-def config(l2_note: str, w=None):
+def config(w=None):
     c = {"workload": "batched dense AVOS closure", "pedigrees": COUNT,
          "n_range": [LO, HI], "sizes": "log-uniform", "generations": "max(2, round(1.5*log2 n))",
          "parents": "father 2 / mother 3, p=0.9 each, uniform over earlier generations",
-         "storage": "int32 dense", "l2": l2_note}
+         "storage": "int32 dense"}
     if w is not None:
         c["components"] = int(w["csizes"].size)
         c["vertices"] = int(w["forest"].shape[0])
@@ -436,33 +439,64 @@ def run_plain(w):
             "how": "rbg_fw_dense once per component over the same 16,761 blocks, one timed pass"}
 
 
+def fullsize_fixture(name):
+    """The digest helpers and the reference's digests of one bench input (tests/golden/
+    fullsize.json, made by running the reference's own CPU code on that input)."""
+    import importlib.util
+    gold = ROOT / "tests" / "golden"
+    spec = importlib.util.spec_from_file_location("make_fullsize", gold / "make_fullsize.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    try:
+        fx = json.loads((gold / "fullsize.json").read_text()).get(name)
+    except (OSError, ValueError):
+        fx = None
+    return mk, fx
+
+
 def run_single_dense(n=8192, generations=30, seed=1, steps=5):
-    """One dense closure of a single n=8192, 30-generation pedigree with int64 entries, checked
-    against the sparse squaring closure of the same graph (a different kernel family)."""
+    """One dense closure of a single n=8192, 30-generation pedigree with int64 entries (what
+    rb.array(A).transitive_closure() runs), on the DAG path (the pedigree is numbered oldest
+    first; RBG_MODE_GRAPH: one graph launch per call) and on the blocked kernels
+    (RBG_MODE_NO_DAG), each checked against the digest and diameter of the reference's own
+    warshall on the same input."""
     import torch
-    import scipy.sparse as sp
     from oracle import oracle as orc
     from redblackgraph_gb300 import _lib, synth
     from redblackgraph_gb300.dense import fw_dense
     from redblackgraph_gb300.device import to_device, to_host
-    from redblackgraph_gb300.sparse import transitive_closure_dag_sparse
     A = synth.pedigree(n, generations, seed, dtype=np.int64)
+    mk, fx = fullsize_fixture("dense8192")
+    input_ok = bool(fx) and mk.dense_digest(A) == fx["input_sha256"]
     d = to_device(A)
     out = torch.empty_like(d)
-    for _ in range(3):
-        _, res = fw_dense(d, out=out)
     stream = torch.cuda.current_stream()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps):
-        _, res = fw_dense(d, out=out)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3 / steps
-    W = to_host(out)
-    S = transitive_closure_dag_sparse(sp.csr_matrix(A))
-    same = bool(((sp.csr_matrix(W) != sp.csr_matrix(S.W.astype(np.int64))).nnz == 0))
+
+    def timed(mode):
+        for _ in range(3):
+            _, res = fw_dense(d, out=out, mode=mode)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            _, res = fw_dense(d, out=out, mode=mode)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / steps
+        kp = profile_kernels(lambda: fw_dense(d, out=out, mode=mode))
+        W = to_host(out)
+        exact = bool(input_ok and mk.dense_digest(W) == fx["closure_sha256"] and res.diameter == fx["diameter"])
+        return t, res, {k: v for k, v in kp.items() if v[1]}, exact
+
+    t_dag, r_dag, kp_dag, ok_dag = timed(_lib.MODE_GRAPH)
+    t_blk, r_blk, kp_blk, ok_blk = timed(_lib.MODE_NO_DAG)
+    hbm = hbm_peak_gbs()
+    io_bytes = 16.0 * n * n                     # every int64 cell read once and written once
+    hbm_ms = sum(kp_dag[k][0] for k in ("tri_scan_kernel", "tri_write_kernel") if k in kp_dag)
+    ach = io_bytes / (hbm_ms / 1e3) / 1e9 if hbm_ms else None
+    phase_ms = sum(kp_blk[k][0] for k in ("fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel") if k in kp_blk)
+    peak, sms = int32_peak_ops(0, None)
+    alu = r_blk.executed * OPS_PER_RELAXATION / (phase_ms / 1e3) / 1e12 if phase_ms else None
     # CPU: the C restatement of the reference warshall at n=1024 (int64), extrapolated by n^3
     m = 1024
     B = synth.pedigree(m, generations_for_small(m), seed, dtype=np.int64)
@@ -472,9 +506,28 @@ def run_single_dense(n=8192, generations=30, seed=1, steps=5):
     tc = time.perf_counter() - t0
     cpu_rate = m ** 3 / tc
     return {"workload": f"one pedigree, n={n}, {generations} generations, int64 entries",
-            "value": n ** 3 / t, "unit": UNIT, "ms": t * 1e3, "path": int(res.path),
-            "diameter": int(res.diameter), "status": int(res.status),
-            "matches_sparse_squaring_closure": same,
+            "value": n ** 3 / t_dag, "unit": UNIT, "ms": t_dag * 1e3, "path": int(r_dag.path),
+            "diameter": int(r_dag.diameter), "status": int(r_dag.status),
+            "bit_exact_vs_reference_fixture": ok_dag,
+            "roofline": {"bound": "hbm", "unit": "GB/s", "kernel": "tri_scan_kernel + tri_write_kernel",
+                         "achieved": ach, "peak": hbm, "frac": ach / hbm if ach else None,
+                         "algorithmic_bytes_per_launch": io_bytes,
+                         "step_gb_s": io_bytes / t_dag / 1e9, "step_frac": io_bytes / t_dag / 1e9 / hbm,
+                         "kernel_ms": {k: v[0] for k, v in kp_dag.items()},
+                         "note": "the closure by levels and the statistics (latency-bound) take the "
+                                 "rest of the step"},
+            "blocked_kernels": {"value": n ** 3 / t_blk, "unit": UNIT, "ms": t_blk * 1e3,
+                                "path": int(r_blk.path), "bit_exact_vs_reference_fixture": ok_blk,
+                                "roofline": {"bound": "int32_alu", "unit": "Tops/s", "achieved": alu,
+                                             "peak": peak / 1e12, "frac": alu / (peak / 1e12) if alu else None,
+                                             "kernel": "fw_diag_kernel + fw_panel_kernel + fw_tile_kernel",
+                                             "ops_per_relaxation": OPS_PER_RELAXATION,
+                                             "executed_relaxations": int(r_blk.executed),
+                                             "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock"},
+                                "kernel_ms": {k: v[0] for k, v in kp_blk.items()}},
+            "reference_full_run_s": fx.get("reference_seconds") if fx else None,
+            "reference_full_run_note": "the reference's compiled C warshall on the whole input, one x86 "
+                                       "core of the build container (tests/golden/make_fullsize.py)",
             "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": f"C restatement of the reference warshall, one n={m} int64 "
                                        f"pedigree in {tc:.1f} s; n^3 extrapolation"}}
@@ -609,6 +662,9 @@ def run_spgemm_forest(seed=7):
     rec = []
     R, iters = closure(rec)
     torch.cuda.synchronize()
+    mk, fx = fullsize_fixture("forest2m")
+    fixed_point_ok = bool(fx) and mk.csr_digest(A) == fx["input_sha256"] and \
+        mk.csr_digest(R.to_scipy()) == fx["closure_sha256"]
     peak = hbm_peak_gbs()
     rows, tb, tms = [], 0.0, 0.0
     for e0, e1, nnz_a, nnz_c, prods in rec:
@@ -637,6 +693,9 @@ def run_spgemm_forest(seed=7):
             "roofline": {"bound": "hbm", "achieved": tb / (tms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": tb / (tms / 1e3) / 1e9 / peak, "peak_source": "measured copy bandwidth"},
             "first_squaring_bit_exact_vs_oracle": same,
+            "bit_exact_vs_reference_fixture": fixed_point_ok,
+            "fixture_note": "the squaring's fixed point against the digest of the reference's Cython DAG "
+                            "closure of the same forest (tests/golden/fullsize.json)",
             "cpu_baseline": {"first_product_s": tcpu, "gpu_first_squaring_ms": rows[0]["ms"],
                              "cores": 1, "kind": "port",
                              "sample": "C restatement of rb_matrix @ (pass 1/2) on A @ A"}}
@@ -648,12 +707,12 @@ def run_dag_forest(seed=7):
     CUDA events from the resident CSR to the resident closure CSR.  Algorithmic bytes: A once
     (12 nnz(A) + 8 (n + 1)), every candidate once (8 per parent-row entry, 12 per parent edge for
     that row's position), the closure rows written to the pool (8 nnz(C)), then read and written
-    as the CSR (16 nnz(C) + 8 (n + 1)).  Checked entry for entry against the squaring closure of
-    the same forest."""
+    as the CSR (16 nnz(C) + 8 (n + 1)).  Checked against the digest and diameter of the
+    reference's Cython DAG closure of the same forest."""
     import torch
     from redblackgraph_gb300 import synth
     from redblackgraph_gb300.dag import dag_closure_device
-    from redblackgraph_gb300.spgemm import DeviceCSR, SEM_C64, spgemm
+    from redblackgraph_gb300.spgemm import DeviceCSR
     A = synth.forest(2_000_000, 25, seed, family=64, reach=3, p_parent=0.97, dtype=np.int32)
     n = A.shape[0]
     D = DeviceCSR.from_scipy(A)
@@ -676,22 +735,20 @@ def run_dag_forest(seed=7):
     cand = int(clen[aj[off]].sum())
     edges = int(off.sum())
     b = 12.0 * A.nnz + 8.0 * (n + 1) + 8.0 * cand + 12.0 * edges + 24.0 * C.nnz + 8.0 * (n + 1)
-    # the squaring closure of the same forest (int64), untimed, as the check
-    R = DeviceCSR.from_scipy(A, dtype=np.int64)
-    for _ in range(64):
-        Rn, rc, _ = spgemm(R, R, R=R, sem=SEM_C64)
-        if rc != 0 or Rn.equal(R):
-            break
-        R = Rn
-    same = bool(C.equal(Rn))
+    diameter = (mx.bit_length() - 1) if mx > 1 else 0
+    mk, fx = fullsize_fixture("forest2m")
+    same = bool(fx) and mk.csr_digest(A) == fx["input_sha256"] and \
+        mk.csr_digest(C.to_scipy()) == fx["closure_sha256"] and diameter == fx["diameter"]
     peak = hbm_peak_gbs()
     return {"workload": f"pedigree forest, n={n}, 25 generations, nnz(A)={A.nnz}, int32 values",
             "ms": ms, "runs_ms": [round(t, 3) for t in times], "levels": levels, "nnz_closure": int(C.nnz),
-            "candidates": cand, "diameter": (mx.bit_length() - 1) if mx > 1 else 0,
+            "candidates": cand, "diameter": diameter,
             "algorithmic_gb": b / 1e9, "gb_s": b / (ms / 1e3) / 1e9,
             "roofline": {"bound": "hbm", "achieved": b / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": b / (ms / 1e3) / 1e9 / peak, "peak_source": "measured copy bandwidth"},
-            "bit_exact_vs_squaring_closure": same}
+            "bit_exact_vs_reference_fixture": same,
+            "fixture_note": "closure and diameter against the digest of the reference's Cython DAG closure "
+                            "of the same forest (tests/golden/fullsize.json)"}
 
 
 def _merge_minabs_host(X, Y):
@@ -810,7 +867,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": r["t"] / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded pedigree components generated in-process",
-            "config": config(f"inputs larger than L2: {r['bytes'] / 1e9:.1f} GB resident per step", w),
+            "config": config(w), "l2": f"inputs larger than L2: {r['bytes'] / 1e9:.1f} GB resident per step",
             "gpu_launches": int(r["launches"]), "clocks": r["clocks"]}
     # roofline of the dominant kernels: on the DAG path (every component here is numbered oldest
     # first) the scan reads every input cell once and the write stores every output cell once;
@@ -847,7 +904,7 @@ def main():
         bk = b["kprof"]
         phase_ms = sum(bk[k][0] for k in ("fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel"))
         peak, sms = int32_peak_ops(0, r["clocks"].get("sm_max_mhz"))
-        ach = b["executed"] * 2 / (phase_ms / 1e3) / 1e12 if phase_ms > 0 else None
+        ach = b["executed"] * OPS_PER_RELAXATION / (phase_ms / 1e3) / 1e12 if phase_ms > 0 else None
         tr = phase_traffic()
         traffic = sum(tr["bytes_per_launch"][k] * bk[k][1] for k in tr["bytes_per_launch"] if k in bk) if tr else None
         line["blocked_kernels_same_batch"] = {
@@ -859,7 +916,7 @@ def main():
                          "frac": ach / (peak / 1e12) if ach else None,
                          "kernel": "fw_diag_kernel + fw_panel_kernel + fw_tile_kernel",
                          "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock",
-                         "ops_per_relaxation": 2, "executed_relaxations_per_step": b["executed"],
+                         "ops_per_relaxation": OPS_PER_RELAXATION, "executed_relaxations_per_step": b["executed"],
                          "traffic": traffic,
                          "traffic_unit": "DRAM bytes per step of the three phase kernels (per-launch bytes "
                                          "from profiles/fw_phase_traffic.txt x launches)"},
@@ -917,7 +974,7 @@ def main_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": total_t / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic: seeded pedigree components generated in-process",
-            "config": config("CPU run", w), "impl": "reference",
+            "config": config(w), "l2": "CPU run", "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{len(idx)} of {w['csizes'].size} components per step "
                                        f"(smallest of every size octave, sum n^3 = {work:.3e}); C "

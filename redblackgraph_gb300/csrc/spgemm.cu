@@ -793,7 +793,8 @@ namespace {
 
 template <int SEM, bool UNS>
 int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s) {
-    static const int configured = [] {      // once, thread-safe initialisation
+    static PerDeviceOnce once;              // per instantiation, for every device
+    const int configured = once.run([] {
         RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)SP_WARP_SMEM));
         RBG_CUDA_TRY(cudaFuncSetAttribute(sp_warp_kernel<SEM, UNS, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -801,7 +802,7 @@ int run_numeric(SpArgs &a, int merge, int64_t dense, int64_t nc, cudaStream_t s)
         RBG_CUDA_TRY(cudaFuncSetAttribute(sp_block_kernel<SEM, UNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)SP_BLOCK_SMEM));
         return (int)RBG_OK;
-    }();
+    });
     if (configured) return configured;
     const int64_t n = a.n_rows;
     note_launches(2 + (dense > 0 ? 2 : 0));

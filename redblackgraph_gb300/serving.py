@@ -486,9 +486,12 @@ class GpuExecutor:
     The arena is one device buffer; a resident graph is the n x n block at its extent.  Each
     closure slot owns a CUDA stream, a workspace and a host worker thread; lookups have their
     own stream and worker.  ``keep`` copies every closed graph back to the host (tests).
+    ``timeline`` records, per closure batch, (slot, start, end) CUDA events on the slot's stream
+    around its device work, to show when batches overlap on the GPU.
     """
 
-    def __init__(self, arena_bytes: int, slots: int = 2, device=None, keep: bool = False):
+    def __init__(self, arena_bytes: int, slots: int = 2, device=None, keep: bool = False,
+                 timeline: bool = False):
         import threading
         from concurrent.futures import ThreadPoolExecutor
         import torch
@@ -509,6 +512,7 @@ class GpuExecutor:
         self.payloads: dict[int, tuple] = {}
         self.keep = keep
         self.kept: dict[int, np.ndarray] = {}
+        self.timeline = [] if timeline else None
 
     # -- graph payloads (pedigree CSR, generated from (n, seed) and cached)
     def payload(self, gid: int, n: int, seed: int):
@@ -537,12 +541,19 @@ class GpuExecutor:
         torch = self.torch
         try:
             with torch.cuda.stream(self.streams[slot]):
+                if self.timeline is not None:
+                    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                    ev[0].record(self.streams[slot])
                 out = [None] * len(jobs)
                 for dt in (np.dtype(np.int32), np.dtype(np.int64)):
                     idx = [k for k, g in enumerate(residents) if g.dtype == dt]
                     if idx:
                         self._close_group(slot, dt, [jobs[k] for k in idx], [residents[k] for k in idx],
                                           unbatched, out, idx)
+                if self.timeline is not None:
+                    ev[1].record(self.streams[slot])
+                    with self.lock:
+                        self.timeline.append((slot, ev[0], ev[1]))
                 if self.keep:
                     for g in residents:
                         self.kept[g.gid] = self.view(g).cpu().numpy()

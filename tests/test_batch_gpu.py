@@ -245,3 +245,64 @@ def test_dag_path_int64_mixed_batch(native):
         assert r.status == so == 0
         assert (W == Wo).all() and r.diameter == do
     assert [r.path for r in res] == [_lib.PATH_DAG, _lib.PATH_BLOCKED64, _lib.PATH_BLOCKED64, _lib.PATH_DAG]
+
+
+def test_dag_path_calls_on_two_streams_overlap(native):
+    """Two DAG-path batches on two streams from two host threads run at the same time: nothing in
+    the library serialises calls.  Stream 1 first spins for ~150 ms, then closes batch A; while
+    thread 1 waits inside its call, thread 2 closes batch B on stream 2.  B's last event must
+    come before the end of stream 1's spin (so before A even started), and both results equal
+    the oracle's.  Each thread first closes its batch once, so that its workspace and output
+    exist: a device allocation during the measured calls would itself order the two streams."""
+    import threading
+    import time
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.dense import fw_batch, pack
+    from redblackgraph_gb300.device import to_device, to_host
+    mats_a = [synth.pedigree(n, 10, n, dtype=np.int32) for n in (300, 900, 1400)]
+    mats_b = [synth.pedigree(n, 9, n + 1, dtype=np.int32) for n in (250, 700)]
+    fa, sa, oa = pack(mats_a)
+    fb, sb, ob = pack(mats_b)
+    da, db = to_device(fa), to_device(fb)
+    outa, outb = torch.empty_like(da), torch.empty_like(db)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    spin_end = torch.cuda.Event(enable_timing=True)
+    b_end = torch.cuda.Event(enable_timing=True)
+    warm_a, warm_b, entered = threading.Event(), threading.Event(), threading.Event()
+    out = {}
+
+    def first():
+        with torch.cuda.stream(s1):
+            fw_batch(da, sa, oa, out=outa, stream=s1)      # this thread's workspace
+            warm_a.set()
+            warm_b.wait(30)
+            torch.cuda._sleep(int(1.5e8 * 2))              # ~150 ms at 2 GHz: bounded spin
+            spin_end.record(s1)
+            entered.set()
+            out["a"] = fw_batch(da, sa, oa, out=outa, stream=s1)
+
+    def second():
+        warm_a.wait(30)
+        with torch.cuda.stream(s2):
+            fw_batch(db, sb, ob, out=outb, stream=s2)
+        warm_b.set()
+        entered.wait(30)
+        time.sleep(0.01)                                   # thread 1 is inside its call by now
+        with torch.cuda.stream(s2):
+            out["b"] = fw_batch(db, sb, ob, out=outb, stream=s2)
+            b_end.record(s2)
+
+    t1, t2 = threading.Thread(target=first), threading.Thread(target=second)
+    t1.start()
+    t2.start()
+    t2.join(60)
+    t1.join(60)
+    torch.cuda.synchronize()
+    assert spin_end.elapsed_time(b_end) < 0, "batch B waited for batch A"
+    for mats, (o, res), offs, sizes in ((mats_a, out["a"], oa, sa), (mats_b, out["b"], ob, sb)):
+        h = to_host(o)
+        for A, r, k, n in zip(mats, res, offs, sizes):
+            Wo, do, so, _ = O.warshall(A)
+            assert r.path == _lib.PATH_DAG and r.status == so == 0 and r.diameter == do
+            assert (h[k:k + n * n].reshape(n, n) == Wo).all()

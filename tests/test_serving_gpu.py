@@ -142,3 +142,30 @@ def test_served_mutations_match_sequential_oracle(native):
         if g is not None and g.state == "closed":
             assert (ex.view(g).cpu().numpy() == W).all(), gid
     ex.close()
+
+
+def test_batches_on_two_slots_overlap_on_the_gpu(native):
+    """A burst of int32 closures (all on the DAG path) with two closure slots: batches of the two
+    slots run on the GPU at the same time (CUDA events on each slot's stream: one batch starts
+    before the other ends), and every served closure equals the request closed alone."""
+    import torch
+    from redblackgraph_gb300.serving import GpuExecutor, Policy, Request, Server
+    rng = np.random.default_rng(17)
+    reqs = [Request(k, "closure", 0.0005 * k, n=int(rng.integers(1500, 4000)), seed=int(rng.integers(1 << 30)))
+            for k in range(16)]
+    cap = 4 << 30
+    ex = GpuExecutor(arena_bytes=cap, slots=2, keep=True, timeline=True)
+    ex.prepare(reqs)
+    Server(ex, cap, Policy(inflight=2, max_batch=4)).run(reqs)
+    torch.cuda.synchronize()
+    tl = ex.timeline
+    assert len({slot for slot, _, _ in tl}) == 2 and len(tl) >= 4
+    ref = tl[0][1]
+    iv = [(slot, ref.elapsed_time(a), ref.elapsed_time(b)) for slot, a, b in tl]
+    overlaps = [(i, j) for i, (si, ai, bi) in enumerate(iv) for j, (sj, aj, bj) in enumerate(iv)
+                if si != sj and i < j and max(ai, aj) < min(bi, bj)]
+    assert overlaps, iv
+    for r in reqs:
+        _, W, status, diam = _alone(ex.payloads[r.rid], r.n)
+        assert r.result == (status, diam) and (ex.kept[r.rid] == W).all()
+    ex.close()
