@@ -945,9 +945,11 @@ int dag_levels_host(const DagArgs &a, const DagWs &w, cudaStream_t s, int64_t *l
         // level L is empty when the order has not grown past its start (written by fill(L - 1))
         int tail = 0;
         int64_t start = 0;
-        RBG_CUDA_TRY(cudaMemcpyAsync(&tail, &w.cnt->placed, 4, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaMemcpyAsync(&start, w.lb + L, 8, cudaMemcpyDeviceToHost, s));
-        RBG_CUDA_TRY(cudaStreamSynchronize(s));
+        HostStaging hs(s, 256);
+        int rc = hs.down(&tail, &w.cnt->placed, 4);
+        if (!rc) rc = hs.down(&start, w.lb + L, 8);
+        if (!rc) rc = hs.finish();
+        if (rc) return rc;
         if ((int64_t)tail <= start || L >= a.n) break;
     }
     return RBG_OK;
@@ -1044,8 +1046,12 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
     if (n >= (1ll << 31) - 1) return RBG_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int64_t annz = 0;
-    RBG_CUDA_TRY(cudaMemcpyAsync(&annz, A->indptr + n, 8, cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    {
+        HostStaging hs(s, 256);
+        int rc = hs.down(&annz, A->indptr + n, 8);
+        if (!rc) rc = hs.finish();
+        if (rc) return rc;
+    }
     if (workspace_bytes < (int64_t)dag_layout(n, annz, nullptr, nullptr)) return RBG_ERR_NOMEM;
     DagCounters *dc = nullptr;
     int64_t launched = 0;
@@ -1053,8 +1059,12 @@ extern "C" int32_t rbg_dag_closure(const rbg_csr_t *A, void *workspace, int64_t 
                          &launched);
     if (rc) return rc;
     DagCounters c;
-    RBG_CUDA_TRY(cudaMemcpyAsync(&c, dc, sizeof(c), cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    {
+        HostStaging hs(s, 256);
+        rc = hs.down(&c, dc, sizeof(c));
+        if (!rc) rc = hs.finish();
+        if (rc) return rc;
+    }
     *levels = c.nlevels;
     if (c.placed < n) return RBG_ERR_CYCLE;      // vertices on (or below) a cycle were never placed
     if (c.flags & 2) { *nnz = -1; return RBG_ERR_CAPACITY; }

@@ -70,6 +70,75 @@ void note_launches(int64_t k) {
 }
 void launch_recording(bool on) { t_recording = on ? 1 : 0; }
 
+// the calling thread's page-locked staging arena (see HostStaging)
+struct StageArena {
+    unsigned char *p = nullptr;
+    size_t cap = 0, used = 0;
+    bool pending = false;                    // staged uploads may still be in flight
+    int no_alloc = 0;                        // NoHostAlloc guards alive
+    ~StageArena() {
+        if (p) cudaFreeHost(p);
+    }
+    void *take(size_t bytes) {
+        if (no_alloc || !p) return nullptr;
+        const size_t at = align_up(used, 64);
+        if (at + bytes > cap) return nullptr;
+        used = at + bytes;
+        return p + at;
+    }
+};
+static thread_local StageArena t_stage;
+
+NoHostAlloc::NoHostAlloc() { ++t_stage.no_alloc; }
+NoHostAlloc::~NoHostAlloc() { --t_stage.no_alloc; }
+
+HostStaging::HostStaging(cudaStream_t s, size_t hint) : s_(s) {
+    StageArena &a = t_stage;
+    if (a.no_alloc || a.pending || hint <= a.cap) return;
+    if (a.used == 0) {                       // nothing staged: grow (with slack)
+        if (a.p) cudaFreeHost(a.p);
+        a.p = nullptr;
+        a.cap = 0;
+        const size_t want = std::max<size_t>(align_up(hint + hint / 4, 4096), 64 << 10);
+        if (cudaHostAlloc(reinterpret_cast<void **>(&a.p), want, cudaHostAllocDefault) == cudaSuccess) a.cap = want;
+        else a.p = nullptr;
+    }
+}
+
+int HostStaging::up(void *dev, const void *host, size_t bytes) {
+    if (bytes == 0) return RBG_OK;
+    void *st = t_stage.take(bytes);
+    if (!st) {
+        RBG_CUDA_TRY(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, s_));
+        return RBG_OK;
+    }
+    memcpy(st, host, bytes);
+    t_stage.pending = true;
+    RBG_CUDA_TRY(cudaMemcpyAsync(dev, st, bytes, cudaMemcpyHostToDevice, s_));
+    return RBG_OK;
+}
+
+int HostStaging::down(void *host, const void *dev, size_t bytes) {
+    if (bytes == 0) return RBG_OK;
+    void *st = npend_ < 8 ? t_stage.take(bytes) : nullptr;
+    if (!st) {
+        RBG_CUDA_TRY(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s_));
+        return RBG_OK;
+    }
+    RBG_CUDA_TRY(cudaMemcpyAsync(st, dev, bytes, cudaMemcpyDeviceToHost, s_));
+    pend_[npend_++] = Pending{host, st, bytes};
+    return RBG_OK;
+}
+
+int HostStaging::finish() {
+    RBG_CUDA_TRY(cudaStreamSynchronize(s_));
+    for (int k = 0; k < npend_; ++k) memcpy(pend_[k].host, pend_[k].staged, pend_[k].bytes);
+    npend_ = 0;
+    t_stage.used = 0;
+    t_stage.pending = false;
+    return RBG_OK;
+}
+
 // Opt-in per-kernel timing: CUDA events recorded on the launching stream around each launch of
 // the blocked kernels (0 = tile, 1 = panel, 2 = diagonal, 3 = convert + finalize).
 struct KernelTimer {
@@ -892,9 +961,10 @@ static void build_plan(FwPlan &P, int64_t count, const int64_t *sizes, const int
 }
 
 static int read_status(DevStatus *d, DevStatus *h, int count, cudaStream_t stream) {
-    RBG_CUDA_TRY(cudaMemcpyAsync(h, d, (size_t)count * sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
-    RBG_CUDA_TRY(cudaStreamSynchronize(stream));
-    return RBG_OK;
+    HostStaging hs(stream, (size_t)count * sizeof(DevStatus));
+    const int rc = hs.down(h, d, (size_t)count * sizeof(DevStatus));
+    if (rc) return rc;
+    return hs.finish();
 }
 
 template <typename U>
@@ -919,17 +989,15 @@ static int configure_kernels() {
 
 // Upload the plan's tables into the workspace.
 static int upload_plan(const FwPlan &P, unsigned char *ws, cudaStream_t stream) {
-    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_comps, P.comps.data(), P.comps.size() * sizeof(FwComp),
-                                 cudaMemcpyHostToDevice, stream));
-    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_pconv, P.pre_conv.data(), P.pre_conv.size() * 8,
-                                 cudaMemcpyHostToDevice, stream));
-    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ppanel, P.pre_panel.data(), P.pre_panel.size() * 8,
-                                 cudaMemcpyHostToDevice, stream));
-    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ptile, P.pre_tile.data(), P.pre_tile.size() * 8,
-                                 cudaMemcpyHostToDevice, stream));
-    RBG_CUDA_TRY(cudaMemcpyAsync(ws + P.off_ptile_n, P.pre_tile_n.data(), P.pre_tile_n.size() * 8,
-                                 cudaMemcpyHostToDevice, stream));
-    return RBG_OK;
+    const size_t b0 = P.comps.size() * sizeof(FwComp), b1 = P.pre_conv.size() * 8, b2 = P.pre_panel.size() * 8,
+                 b3 = P.pre_tile.size() * 8, b4 = P.pre_tile_n.size() * 8;
+    HostStaging hs(stream, b0 + b1 + b2 + b3 + b4 + 5 * 64);
+    int rc = hs.up(ws + P.off_comps, P.comps.data(), b0);
+    if (!rc) rc = hs.up(ws + P.off_pconv, P.pre_conv.data(), b1);
+    if (!rc) rc = hs.up(ws + P.off_ppanel, P.pre_panel.data(), b2);
+    if (!rc) rc = hs.up(ws + P.off_ptile, P.pre_tile.data(), b3);
+    if (!rc) rc = hs.up(ws + P.off_ptile_n, P.pre_tile_n.data(), b4);
+    return rc;
 }
 
 // Launch the whole blocked closure of a plan (conversion, every round, finalization) on
@@ -1534,6 +1602,7 @@ extern "C" int32_t rbg_fw_dense_noalloc(int32_t dtype, int64_t n, const void *in
     int rc = noalloc_scratch(s, &ws);
     if (rc) return rc;
     mode &= ~RBG_MODE_GRAPH;   // instantiating a graph may take driver memory
+    NoHostAlloc pageable;      // and no page-locked staging: pageable copies only
     rc = RBG_ERR_INVALID;
     RBG_DISPATCH_DTYPE(dtype, T,
         rc = fw_dense_t<T>(n, reinterpret_cast<const T *>(in), ld_in, reinterpret_cast<T *>(out), ld_out,

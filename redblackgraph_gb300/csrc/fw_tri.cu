@@ -614,8 +614,12 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const 
     if (L.pool < 4 * R) return RBG_OK;       // no room for a closure: the other paths decide
     tri_layout(ws, ws_bytes, C, NR, L);
     const TriShape sh{count, R, pre[C], ld_in, ld_out};
-    RBG_CUDA_TRY(cudaMemcpyAsync(L.dc, hc.data(), C * sizeof(TriComp), cudaMemcpyHostToDevice, s));
-    RBG_CUDA_TRY(cudaMemcpyAsync(L.dpre, pre.data(), (C + 1) * 8, cudaMemcpyHostToDevice, s));
+    {
+        HostStaging hs(s, C * sizeof(TriComp) + (C + 1) * 8 + C * sizeof(TriOut) + sizeof(DagCounters) + 256);
+        int rc = hs.up(L.dc, hc.data(), C * sizeof(TriComp));
+        if (!rc) rc = hs.up(L.dpre, pre.data(), (C + 1) * 8);
+        if (rc) return rc;
+    }
 
     DagCounters *dcount = nullptr;
     int64_t fixed_launches = -1;             // >= 0: a graph ran; its level loop is counted below
@@ -656,9 +660,13 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const 
     }
     std::vector<TriOut> h(C);
     DagCounters hd;
-    RBG_CUDA_TRY(cudaMemcpyAsync(h.data(), L.res, C * sizeof(TriOut), cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaMemcpyAsync(&hd, dcount, sizeof(hd), cudaMemcpyDeviceToHost, s));
-    RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    {
+        HostStaging hs(s, C * sizeof(TriOut) + sizeof(DagCounters) + 128);
+        int rc = hs.down(h.data(), L.res, C * sizeof(TriOut));
+        if (!rc) rc = hs.down(&hd, dcount, sizeof(hd));
+        if (!rc) rc = hs.finish();
+        if (rc) return rc;
+    }
     if (fixed_launches >= 0) {
         const int64_t iters = std::max<int64_t>(1, (hd.nlevels + DAG_GRAPH_CHUNK - 1) / DAG_GRAPH_CHUNK);
         note_launches(fixed_launches + iters * (3 * DAG_GRAPH_CHUNK + 1));

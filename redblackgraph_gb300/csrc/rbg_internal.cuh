@@ -67,6 +67,32 @@ private:
     int rc_[kMaxDevices] = {};
 };
 
+// Host <-> device copies of a call's small tables and results through page-locked memory.  A
+// copy from or to pageable memory goes through the driver's staging buffers: a read waits there
+// for its stream and holds up other host threads' pageable copies meanwhile, which serialises
+// calls on different streams.  Each host thread keeps one grow-only page-locked arena instead.
+// up() stages and enqueues an upload; down() enqueues a download whose bytes land in `host` at
+// finish(), which synchronises the stream.  The arena is reused only after finish(), so no staged
+// upload is overwritten while it may still be pending; a request that does not fit, and every
+// request while a NoHostAlloc guard is alive (rbg_fw_dense_noalloc), copies pageable memory.
+class HostStaging {
+public:
+    HostStaging(cudaStream_t s, size_t hint);
+    int up(void *dev, const void *host, size_t bytes);
+    int down(void *host, const void *dev, size_t bytes);
+    int finish();
+
+private:
+    struct Pending { void *host; const void *staged; size_t bytes; };
+    cudaStream_t s_;
+    Pending pend_[8];
+    int npend_ = 0;
+};
+struct NoHostAlloc {
+    NoHostAlloc();
+    ~NoHostAlloc();
+};
+
 // running count of kernel launches issued by this library (rbg_launch_count); while a graph is
 // being recorded (launch_recording(true)) launches are counted when the graph runs instead
 void note_launches(int64_t k);

@@ -38,9 +38,35 @@ constexpr int SEM_CY32 = 1;  // Cython semantics on int32 (the gpu module)
 
 // Products and sums: for SEM_C64 the compute values are the storage values widened to 64 bits
 // (unsigned storage uses the unsigned 64-bit algebra with RED_ONE widened to all ones).
-template <int SEM, bool UNS>
+// NARROW: signed values of 4-byte storage (below 2^31), whose splice mostly fits 32 bits.
+template <int SEM, bool UNS, bool NARROW = false>
 __device__ __forceinline__ long long sp_mul(long long a, long long b, unsigned &ev) {
     if (SEM == SEM_CY32) return (long long)cy_product((int32_t)a, (int32_t)b);
+    if (!UNS) {
+        // signed storage, the cases of pedigree data without the general function's branches
+        // (rbg_math.c.in:48-121): two plain values; a zero; the identities -1 (keeps an even
+        // left value) and 1 (keeps an odd one) on the right; an identity on the left (gives the
+        // right value); two identities (equal: itself, else 0)
+        if (a >= 2 && b >= 2) {
+            if (NARROW) {
+                const unsigned x = (unsigned)a, y = (unsigned)b;
+                const int bp = 31 - __clz((int)y), mx = 31 - __clz((int)x);
+                if (mx + bp < 31) return (long long)((x << bp) | (y ^ (1u << bp)));
+            }
+            const unsigned long long x = (unsigned long long)a, y = (unsigned long long)b;
+            const int bp = 63 - __clzll((long long)y), mx = 63 - __clzll((long long)x);
+            if (mx + bp >= 64) ev |= RBG_EV_OVF_SIZE;
+            const unsigned long long r = (x << bp) | (y ^ (1ull << bp));
+            if (~r == 0) ev |= RBG_EV_OVF_ONES;
+            return (long long)r;
+        }
+        if (a == 0 || b == 0) return 0;
+        const bool ai = a == 1 || a == -1, bi = b == 1 || b == -1;
+        if (bi && a >= 2) return ((a & 1) == (b == 1 ? 1 : 0)) ? a : 0;
+        if (ai && b >= 2) return b;
+        if (ai && bi) return a == b ? a : 0;
+        return (long long)avos_product<int64_t>((int64_t)a, (int64_t)b, ev);   // negative: never returns there
+    }
     // both operands plain values (neither 0, 1, the red one nor, signed, negative): the bit
     // splice with the C core's two overflow tests, without the identity and sign cases
     const unsigned long long x = (unsigned long long)a, y = (unsigned long long)b;
@@ -317,7 +343,20 @@ struct SpHashWarp {
 };
 constexpr unsigned SP_E32 = 0xffffffffu;     // empty mark of v32 (C core encoding)
 constexpr int SP_E32S = 0x7fffffff;          // empty mark of v32 (Cython, signed)
-constexpr size_t SP_WARP_SMEM = sizeof(SpHashWarp) * SP_HWARPS;
+
+// A row whose candidate columns all lie in a window of SP_WIN consecutive columns (the first
+// and last column of every B row it gathers, and of R's row, bound it) folds its products into
+// a dense accumulator over the window instead: no probing, and scanning the window in order
+// writes the row already sorted.  A product outside the window (unsorted input rows) sends the
+// row to the block kernel like a full table does.
+constexpr int SP_WIN = 256;
+struct SpWinWarp {
+    unsigned v32[SP_WIN];
+    unsigned long long v64[SP_WIN];
+    long long rv[SP_WIN];
+};
+constexpr size_t SP_WARP_BYTES = sizeof(SpHashWarp) > sizeof(SpWinWarp) ? sizeof(SpHashWarp) : sizeof(SpWinWarp);
+constexpr size_t SP_WARP_SMEM = SP_WARP_BYTES * SP_HWARPS;
 
 // Slot of column j (inserted if new); -1 when the table is full.
 __device__ __forceinline__ int sp_hash_slot(SpHashWarp &H, unsigned j, int mask) {
@@ -334,8 +373,8 @@ __device__ __forceinline__ int sp_hash_slot(SpHashWarp &H, unsigned j, int mask)
     return -1;
 }
 
-template <int SEM>
-__device__ __forceinline__ void sp_hash_fold(SpHashWarp &H, int slot, long long p) {
+template <int SEM, typename Tab>
+__device__ __forceinline__ void sp_hash_fold(Tab &H, int slot, long long p) {
     if (SEM == SEM_CY32) {
         if (p < (long long)SP_E32S && p >= (long long)INT_MIN) {
             int *v = reinterpret_cast<int *>(&H.v32[slot]);
@@ -355,8 +394,8 @@ __device__ __forceinline__ void sp_hash_fold(SpHashWarp &H, int slot, long long 
 }
 
 // the folded (+) of slot s (0 when no product landed there)
-template <int SEM>
-__device__ __forceinline__ long long sp_hash_value(const SpHashWarp &H, int s) {
+template <int SEM, typename Tab>
+__device__ __forceinline__ long long sp_hash_value(const Tab &H, int s) {
     if (SEM == SEM_CY32) {
         const long long a = (int)H.v32[s] == SP_E32S ? LLONG_MAX : (long long)(int)H.v32[s];
         const long long m = min(a, (long long)H.v64[s]);
@@ -403,27 +442,66 @@ __global__ void __launch_bounds__(SP_HWARPS * 32)
 sp_warp_kernel(SpArgs a, int merge) {
     extern __shared__ __align__(16) unsigned char sp_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    SpHashWarp &H = reinterpret_cast<SpHashWarp *>(sp_smem)[w];
+    SpHashWarp &H = *reinterpret_cast<SpHashWarp *>(sp_smem + (size_t)w * SP_WARP_BYTES);
+    SpWinWarp &Wn = *reinterpret_cast<SpWinWarp *>(sp_smem + (size_t)w * SP_WARP_BYTES);
     unsigned ev = 0;
     const int64_t warps = (int64_t)gridDim.x * SP_HWARPS;
     for (int64_t i = (int64_t)blockIdx.x * SP_HWARPS + w; i < a.n_rows; i += warps) {
         const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
         if (c > SP_BLOCK_CAP) continue;              // the dense kernel takes it
-        int S = 32;
-        while (S < c && S < SP_HASH_SLOTS) S <<= 1;
-        const int mask = S - 1;
-        for (int s = lane; s < S; s += 32) {
-            H.key[s] = SP_NOKEY;
-            H.v32[s] = SEM == SEM_CY32 ? (unsigned)SP_E32S : SP_E32;
-            H.v64[s] = sp_empty<SEM>();
-            H.rv[s] = 0;
+        const bool sq = merge && a.rp;
+        // the row's column window: first and last column of every B row it gathers and of R's row
+        int jlo = INT_MAX, jhi = -1;
+        for (int64_t e = a.ap[i] + lane; e < a.ap[i + 1]; e += 32) {
+            const int k = a.aj[e];
+            const int64_t b0 = a.bp[k], b1 = a.bp[k + 1];
+            if (b1 > b0) {
+                jlo = min(jlo, a.bj[b0]);
+                jhi = max(jhi, a.bj[b1 - 1]);
+            }
+        }
+        if (sq && lane == 0) {
+            const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
+            if (r1 > r0) {
+                jlo = min(jlo, a.rj[r0]);
+                jhi = max(jhi, a.rj[r1 - 1]);
+            }
+        }
+        jlo = __reduce_min_sync(0xffffffffu, jlo);
+        jhi = __reduce_max_sync(0xffffffffu, jhi);
+        const long long width = jhi >= jlo ? (long long)jhi - jlo + 1 : 0;
+        const int span = (int)(width < SP_WIN + 1 ? width : SP_WIN + 1);
+        const bool win = span <= SP_WIN;             // warp-uniform
+        int mask = 0;
+        if (win) {
+            for (int s = lane; s < span; s += 32) {
+                Wn.v32[s] = SEM == SEM_CY32 ? (unsigned)SP_E32S : SP_E32;
+                Wn.v64[s] = sp_empty<SEM>();
+                Wn.rv[s] = 0;
+            }
+        } else {
+            int S = 32;
+            while (S < c && S < SP_HASH_SLOTS) S <<= 1;
+            mask = S - 1;
+            for (int s = lane; s < S; s += 32) {
+                H.key[s] = SP_NOKEY;
+                H.v32[s] = SEM == SEM_CY32 ? (unsigned)SP_E32S : SP_E32;
+                H.v64[s] = sp_empty<SEM>();
+                H.rv[s] = 0;
+            }
         }
         __syncwarp();
+        // slot of column j in the window or the table; -1: the row does not fit
+        auto slot_of = [&](int j) -> int {
+            if (win) return (unsigned)(j - jlo) < (unsigned)span ? j - jlo : -1;
+            return sp_hash_slot(H, (unsigned)j, mask);
+        };
         bool full = false;
-        if (merge && a.rp) {
+        if (sq) {
             for (int64_t e = a.rp[i] + lane; e < a.rp[i + 1]; e += 32) {
-                const int slot = sp_hash_slot(H, (unsigned)a.rj[e], mask);
+                const int slot = slot_of(a.rj[e]);
                 if (slot < 0) full = true;
+                else if (win) Wn.rv[slot] = sp_load_t<BYTES, UNS>(a.rx, e);
                 else H.rv[slot] = sp_load_t<BYTES, UNS>(a.rx, e);
             }
         }
@@ -462,11 +540,12 @@ sp_warp_kernel(SpArgs a, int merge) {
                     const int64_t f = bq + (idx - xq);
                     const int j = a.bj[f];
                     if (!(a.upper && j < i)) {
-                        const long long p = sp_mul<SEM, UNS>(aq, sp_load_t<BYTES, UNS>(a.bx, f), ev);
+                        const long long p = sp_mul<SEM, UNS, BYTES == 4 && !UNS>(aq, sp_load_t<BYTES, UNS>(a.bx, f), ev);
                         if (p != 0) {                // a zero product adds nothing
                             if (j == i && p != -1 && p != 1) ev |= RBG_EV_CYCLE;   // a vertex reaches itself
-                            const int slot = sp_hash_slot(H, (unsigned)j, mask);
+                            const int slot = slot_of(j);
                             if (slot < 0) full = true;
+                            else if (win) sp_hash_fold<SEM>(Wn, slot, p);
                             else sp_hash_fold<SEM>(H, slot, p);
                         }
                     }
@@ -479,7 +558,36 @@ sp_warp_kernel(SpArgs a, int merge) {
             __syncwarp();
             continue;
         }
+        // the value of a slot: the (+) of the products, then for a squaring step the magnitude
+        // merge with R
+        auto value_of = [&](long long sv, long long r) -> long long {
+            const long long s_t = sv == 0 ? 0 : ((SEM == SEM_CY32) ? sv : sp_trunc(sv, BYTES, UNS));
+            if (!merge) return s_t;
+            const long long v = sv == 0 ? r : (r != 0 ? sp_minabs(r, s_t, UNS) : s_t);
+            return (long long)(int)v;                // the merged matrix is int32 (transitive_closure.py:327)
+        };
+        int64_t out = 0;
+        const int64_t base = a.cand_off[i];
+        if (win) {                                   // the window in column order: already sorted
+            for (int q0 = 0; q0 < span; q0 += 32) {
+                const int q = q0 + lane;
+                long long v = 0;
+                if (q < span) v = value_of(sp_hash_value<SEM>(Wn, q), Wn.rv[q]);
+                const bool keep = v != 0;
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int64_t pos = base + out + __popc(bal & ((1u << lane) - 1u));
+                    a.ocol[pos] = jlo + q;
+                    a.oval[pos] = v;
+                }
+                out += __popc(bal);
+            }
+            if (lane == 0) a.rownnz[i] = out;
+            __syncwarp();
+            continue;
+        }
         // the occupied slots, compacted, then sorted by column
+        const int S = mask + 1;
         int nd = 0;
         for (int s0 = 0; s0 < S; s0 += 32) {
             const int s = s0 + lane;
@@ -509,9 +617,6 @@ sp_warp_kernel(SpArgs a, int merge) {
                 __syncwarp();
             }
         }
-        // values: the (+) of the products, then for a squaring step the magnitude merge with R
-        int64_t out = 0;
-        const int64_t base = a.cand_off[i];
         for (int q0 = 0; q0 < nd; q0 += 32) {
             const int q = q0 + lane;
             long long v = 0;
@@ -520,14 +625,7 @@ sp_warp_kernel(SpArgs a, int merge) {
                 const unsigned long long e = H.list[q];
                 const int s = (int)(e & 0xffffffffu);
                 col = (unsigned)(e >> 32);
-                const long long sv = sp_hash_value<SEM>(H, s);
-                const long long s_t = sv == 0 ? 0 : ((SEM == SEM_CY32) ? sv : sp_trunc(sv, BYTES, UNS));
-                if (!merge) v = s_t;
-                else {
-                    const long long r = H.rv[s];
-                    v = sv == 0 ? r : (r != 0 ? sp_minabs(r, s_t, UNS) : s_t);
-                    v = (long long)(int)v;   // the merged matrix is int32 (transitive_closure.py:327)
-                }
+                v = value_of(sp_hash_value<SEM>(H, s), H.rv[s]);
             }
             const bool keep = v != 0;
             const unsigned bal = __ballot_sync(0xffffffffu, keep);
