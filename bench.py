@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving workload (0: skip)")
     ap.add_argument("--serve-count", type=int, default=0, help="requests in the serving stream")
-    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve"], default=None,
+    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve", "anynum"], default=None,
                     help="run one secondary workload alone and print its JSON (profiling cases)")
     ap.add_argument("--secondary", type=int, default=1,
                     help="also measure the per-component plain path, one n=8192 int64 closure and "
@@ -262,12 +262,12 @@ def profile_kernels(fn):
     L = _lib.load()
     L.rbg_profile_begin()
     fn()
-    ms = (ctypes.c_double * 8)()
-    n = (ctypes.c_int64 * 8)()
-    _lib.check(L.rbg_profile_end_slots(ms, n, 8), "profile")
+    ms = (ctypes.c_double * 9)()
+    n = (ctypes.c_int64 * 9)()
+    _lib.check(L.rbg_profile_end_slots(ms, n, 9), "profile")
     names = ["fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel", "convert/finalize",
-             "tri_scan_kernel", "dag_closure", "tri_stats_kernel", "tri_write_kernel"]
-    return {names[k]: (ms[k], int(n[k])) for k in range(8)}
+             "tri_scan_kernel", "dag_closure", "tri_stats_kernel", "tri_write_kernel", "any_numbering_replay"]
+    return {names[k]: (ms[k], int(n[k])) for k in range(9)}
 
 
 def run_ours(args, rank, world, w):
@@ -437,6 +437,87 @@ def run_plain(w):
     torch.cuda.empty_cache()
     return {"value": work / t, "unit": UNIT, "ms_per_step": t * 1e3,
             "how": "rbg_fw_dense once per component over the same 16,761 blocks, one timed pass"}
+
+
+def renumbered(w, seed=23):
+    """The same forest with every component's vertices renumbered at random (a permutation of
+    the component's own vertex ids), so that each dense block has entries on both sides of the
+    diagonal: matrices not numbered in a topological order."""
+    rng = np.random.default_rng(seed)
+    N = w["forest"].shape[0]
+    perm = np.arange(N, dtype=np.int64)              # perm[old] = new
+    for c in range(w["csizes"].size):
+        v = w["order"][w["cstart"][c]:w["cstart"][c + 1]]
+        perm[v] = rng.permutation(v)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(N, dtype=np.int64)         # inv[new] = old
+    f = w["forest"][inv][:, inv].tocsr()
+    f.sort_indices()
+    # each component keeps its vertex set, so the components and their ascending vertex lists
+    # (w["order"]) are unchanged
+    return dict(w, forest=f)
+
+
+def run_any_numbering(w, steps=5):
+    """The headline's components renumbered at random (entries on both sides of the diagonal):
+    the DAG path with the sequential loop replayed on each closure's pattern, against the blocked
+    kernels on the same batch (the path such matrices took before); a sample of components is
+    checked bit-exact against the oracle's sequential loop."""
+    import torch
+    from oracle import oracle as orc
+    from redblackgraph_gb300 import _lib
+    from redblackgraph_gb300.dense import fw_batch
+    from redblackgraph_gb300.device import to_host
+    wr = renumbered(w)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    blocks = build_device_batch(wr, dev)
+    sizes, offsets, buf = blocks.sizes, blocks.offsets, blocks.flat
+    work = float((sizes.astype(np.float64) ** 3).sum())
+    out = torch.empty_like(buf)
+    line = {"how": "rbg_fw_batch on the resident blocks of the same forest with every component's "
+                   "vertices renumbered at random (seeded)", "unit": UNIT}
+    stream = torch.cuda.current_stream()
+    for name, mode in (("dag_path", _lib.MODE_GRAPH), ("blocked_kernels", _lib.MODE_GRAPH | _lib.MODE_NO_DAG)):
+        for _ in range(3):
+            _, res = fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True)
+        assert (res["status"] == 0).all()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / steps
+        kp = profile_kernels(lambda: fw_batch(buf, sizes, offsets, out=out, mode=mode, as_array=True))
+        paths = {{1: "blocked32", 2: "blocked64", 3: "exact", 4: "dag"}.get(int(p), str(p)):
+                 int((res["path"] == p).sum()) for p in np.unique(res["path"])}
+        line[name] = {"value": work / t, "ms_per_step": t * 1e3, "paths": paths,
+                      "kernel_ms_per_step": {k: v[0] for k, v in kp.items() if v[1]}}
+        if name == "dag_path":
+            # oracle sample: the largest component of every size octave up to 1024 vertices
+            # (seconds of the C restatement of the reference's warshall)
+            by_oct = {}
+            for i, n in enumerate(sizes.tolist()):
+                o = octave(n)
+                if n <= 1024 and (o not in by_oct or n > sizes[by_oct[o]]):
+                    by_oct[o] = i
+            idx = sorted(by_oct.values())
+            ok, both = True, 0
+            for i in idx:
+                n, o = int(sizes[i]), int(offsets[i])
+                A = to_host(buf[o:o + n * n]).reshape(n, n)
+                both += int(np.tril(A, -1).any() and np.triu(A, 1).any())
+                Wo, do, so, _ = orc.warshall(A)
+                ok &= so == 0 and int(res["diameter"][i]) == do
+                ok &= bool((to_host(out[o:o + n * n]).reshape(n, n) == Wo).all())
+            line[name]["sample_bit_exact_vs_oracle"] = bool(ok)
+            line[name]["sample"] = (f"{len(idx)} components, the largest of every size octave up to 1024 "
+                                    f"vertices; {both} of them with entries on both sides of the diagonal")
+    line["dag_vs_blocked"] = line["blocked_kernels"]["ms_per_step"] / line["dag_path"]["ms_per_step"]
+    del buf, blocks, out
+    torch.cuda.empty_cache()
+    return line
 
 
 def fullsize_fixture(name):
@@ -852,7 +933,7 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         fn = {"spgemm": run_spgemm_forest, "dag": run_dag_forest, "compose": run_compose,
-              "single": run_single_dense,
+              "single": run_single_dense, "anynum": lambda: run_any_numbering(workload(0)),
               "serve": lambda: run_serving(args.serve_count)}[args.only]
         print(json.dumps(fn()))
         return
@@ -949,6 +1030,7 @@ def main():
         line["spgemm_squaring"] = run_spgemm_forest()
         line["dag_levels"] = run_dag_forest()
         line["relational_composition"] = run_compose()
+        line["any_numbering"] = run_any_numbering(w)
     if args.serve:
         line["serving"] = run_serving(args.serve_count)
     if rank == 0:

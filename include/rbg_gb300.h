@@ -87,8 +87,8 @@ typedef void *rbg_stream_t; /* a cudaStream_t */
 #define RBG_PATH_BLOCKED32 1
 #define RBG_PATH_BLOCKED64 2
 #define RBG_PATH_EXACT 3
-#define RBG_PATH_DAG 4   /* int32 / int64 matrix whose off-diagonal entries all lie on one
-                            side of the diagonal, closed by the DAG closure by levels       */
+#define RBG_PATH_DAG 4   /* int32 / int64 acyclic matrix in the clean regime, closed by the
+                            DAG closure by levels                                          */
 
 typedef struct rbg_result {
     int32_t status;   /* RBG_OK or RBG_ERR_*                                         */
@@ -115,8 +115,9 @@ int32_t rbg_profile_begin(void);
  * receive the summed kernel time and launch count since rbg_profile_begin. */
 int32_t rbg_profile_end(double *ms, int64_t *launches);
 
-/* rbg_profile_end for the first `slots` (1..8) timer slots: 0-3 as above, then the DAG path of
- * rbg_fw_batch: 4 scan, 5 closure by levels (with its CSR), 6 statistics, 7 write. */
+/* rbg_profile_end for the first `slots` (1..9) timer slots: 0-3 as above, then the DAG path of
+ * rbg_fw_batch / rbg_fw_dense: 4 scan, 5 closure by levels (with its CSR), 6 statistics, 7 write,
+ * 8 the replay of matrices in any numbering (pattern, triples, replay). */
 int32_t rbg_profile_end_slots(double *ms, int64_t *launches, int32_t slots);
 
 /* Scratch bytes rbg_fw_dense needs for an n x n matrix of `dtype` under `mode`. */
@@ -179,16 +180,20 @@ int32_t rbg_fw_batch(int32_t dtype, int64_t count, const int64_t *sizes, const i
 /*
  * DAG path of rbg_fw_batch and rbg_fw_dense (RBG_DTYPE_INT32 and RBG_DTYPE_INT64, unless
  * RBG_MODE_NO_DAG, RBG_MODE_TRIANGULAR, RBG_MODE_FORCE_EXACT or RBG_MODE_FORCE_WIDE is given): a
- * matrix whose off-diagonal entries all lie below (or all above) the diagonal, in the clean
- * regime (off-diagonal values 0 or in [2, 2^31), diagonal in {-1, 0, 1}) and of at most 8192
- * rows, is closed through the DAG closure by levels: with its vertices in a topological order
- * the sequential loop's step k only pushes row k into the rows of k's children (below) or pulls
- * k's parents into the rows that reach k (above), so the values are the DAG recurrence's and
- * the diameter comes from each cell's first product in step order.  A product that may reach
- * bit 31 sends the matrix to the blocked kernels.  The path's scratch (row slots, the
- * candidates' CSR, the closure's row pool) is carved from `workspace`; a closure that does not
- * fit leaves its matrices to the blocked kernels.  Every accept / reject decision is made on
- * the device and the results are read back once per call.
+ * matrix in the clean regime (off-diagonal values 0 or in [2, 2^31), diagonal in {-1, 0, 1}),
+ * with at most 16 off-diagonal entries per row and at most 8192 rows, whose graph is acyclic, is
+ * closed through the DAG closure by levels.  With its vertices in a topological order (every
+ * off-diagonal entry below, or every one above, the diagonal) the sequential loop's step k only
+ * pushes row k into the rows of k's children (below) or pulls k's parents into the rows that
+ * reach k (above), so the values are the DAG recurrence's and the diameter comes from each
+ * cell's first product in step order.  In any other numbering the loop is replayed on the
+ * closure's pattern (the triples (i, k, j) of each step with both cells in the pattern), which
+ * gives the same diameter and overflow decision.  A matrix whose loop computes a product
+ * reaching bit 31 continues without the 32-bit lanes: on 64-bit lanes (int64) or on the exact
+ * kernel (int32).  The path's scratch (row slots, the candidates' CSR, the closure's row pool,
+ * the replay's pattern and triples) is carved from `workspace`; a closure that does not fit
+ * leaves its matrices to the blocked kernels.  Every accept / reject decision is made on the
+ * device and the results are read back once per call.
  */
 
 /* Destroy the CUDA graphs RBG_MODE_GRAPH keeps for the DAG path (waits for the device first);

@@ -16,6 +16,7 @@
 namespace rbg {
 
 constexpr int DAG_KIND_NONE = 0, DAG_KIND_BELOW = 1, DAG_KIND_ABOVE = 2;
+constexpr int DAG_KIND_GENERAL = 3;   // entries on both sides of the diagonal (any numbering)
 constexpr int DAG_TOP_MSB = 31;   // lbits - 1 for 32-bit values
 constexpr int DAG_MAX_N = 8192;   // columns of a matrix the per-warp bitmap covers
 
@@ -39,9 +40,10 @@ __device__ __forceinline__ void dag_row_stats(unsigned *bm, int words, int kind,
     __syncwarp();
     const int64_t a0 = aptr[g];
     const int alen = (int)(aptr[g + 1] - a0);
+    const unsigned ncols = (unsigned)words * 32u;
     for (int p = lane; p < alen; p += 32) {          // the row's own values are written first
         const int j = local(acol[a0 + p]);
-        atomicOr(&bm[j >> 5], 1u << (j & 31));
+        if ((unsigned)j < ncols) atomicOr(&bm[j >> 5], 1u << (j & 31));
         fm = max(fm, dag_row_msb(aval[a0 + p]));
     }
     __syncwarp();
@@ -59,7 +61,9 @@ __device__ __forceinline__ void dag_row_stats(unsigned *bm, int words, int kind,
             if (kind == DAG_KIND_BELOW) {
                 const int j = local(ccol[c0 + q]);
                 const unsigned bit = 1u << (j & 31);
-                if (!(bm[j >> 5] & bit)) {
+                if ((unsigned)j >= ncols) {
+                    am = 99;                         // inconsistent: the matrix leaves the DAG path
+                } else if (!(bm[j >> 5] & bit)) {
                     fm = max(fm, pm);
                     atomicOr(&bm[j >> 5], bit);
                 }
@@ -83,7 +87,9 @@ __device__ __forceinline__ void dag_row_stats(unsigned *bm, int words, int kind,
                 const int pm = mk + dag_row_msb(aval[k0 + r]);
                 am = max(am, pm);
                 const unsigned bit = 1u << (j & 31);
-                if (!(bm[j >> 5] & bit)) {
+                if ((unsigned)j >= ncols) {
+                    am = 99;                         // inconsistent: the matrix leaves the DAG path
+                } else if (!(bm[j >> 5] & bit)) {
                     fm = max(fm, pm);
                     atomicOr(&bm[j >> 5], bit);
                 }

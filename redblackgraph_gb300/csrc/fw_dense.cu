@@ -1183,10 +1183,14 @@ static bool dag_path_allowed(uint32_t mode) {
 
 // Single matrix: the DAG path for int32 / int64 matrices numbered in a topological order, else
 // 32-bit lanes, then 64-bit lanes when 64-bit values need them, then the exact sequential-order
-// kernel for anything outside the clean regime, cycles and top-bit products.
+// kernel for anything outside the clean regime, cycles and top-bit products.  A matrix whose
+// loop the DAG path found to compute a product reaching bit 31 (`top_bit`, from the DAG path of
+// this call or of the batch that hands it over) skips the 32-bit lanes, which could only report
+// that risk: int64 goes on with 64-bit lanes, int32 with the exact kernel.
 template <typename T>
 static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_out, uint32_t mode,
-                      unsigned char *ws, size_t ws_bytes, bool try_dag, rbg_result_t *res, cudaStream_t stream) {
+                      unsigned char *ws, size_t ws_bytes, bool try_dag, rbg_result_t *res, cudaStream_t stream,
+                      bool top_bit = false) {
     const bool cython = (mode & RBG_MODE_CYTHON) != 0;
     const int triangular = (mode & RBG_MODE_TRIANGULAR) ? 1 : 0;
     memset(res, 0, sizeof(*res));
@@ -1194,18 +1198,19 @@ static int fw_dense_t(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld_
     if constexpr (std::is_same<T, int32_t>::value || std::is_same<T, int64_t>::value) {
         if (try_dag && dag_path_allowed(mode)) {
             const int64_t zero = 0;
-            char closed = 0;
+            char closed = TRI_OPEN;
             const int rc = tri_batch<T>(1, &n, &zero, &zero, ld_in, ld_out, in, out, res, &closed, ws, ws_bytes, mode,
                                         stream, RowStats());
             if (rc) return rc;
-            if (closed) return RBG_OK;
+            if (closed == TRI_CLOSED) return RBG_OK;
+            top_bit = closed == TRI_TOP_BIT;
         }
     }
     DevStatus h;
     FwPlan P;
     single_plan<uint32_t>(P, n, ld_in, ld_out, triangular, (int)sizeof(T));
-    if (!(mode & RBG_MODE_FORCE_EXACT)) {
-        bool wide = sizeof(T) == 8 && (mode & RBG_MODE_FORCE_WIDE);
+    if (!(mode & RBG_MODE_FORCE_EXACT) && !(top_bit && sizeof(T) == 4)) {
+        bool wide = sizeof(T) == 8 && ((mode & RBG_MODE_FORCE_WIDE) || top_bit);
         if (!wide) {
             int rc = upload_plan(P, ws, stream);
             if (rc) return rc;
@@ -1416,9 +1421,17 @@ static int fw_batch_t(int64_t count, const int64_t *sizes, const int64_t *offset
             if (rc) return rc;
         }
     }
-    std::vector<int64_t> idx;
-    for (int64_t i = 0; i < count; ++i)
-        if (!closed[(size_t)i]) idx.push_back(i);
+    // components the DAG path found to reach bit 31 skip the batched 32-bit pass
+    std::vector<int64_t> idx, top;
+    for (int64_t i = 0; i < count; ++i) {
+        if (closed[(size_t)i] == TRI_OPEN) idx.push_back(i);
+        else if (closed[(size_t)i] == TRI_TOP_BIT) top.push_back(i);
+    }
+    for (int64_t i : top) {
+        const int rc = fw_dense_t<T>(sizes[i], in + offsets[i], sizes[i], out + offsets[i], sizes[i], mode, ws,
+                                     ws_bytes, false, &results[i], stream, true);
+        if (rc) return rc;
+    }
     if (idx.empty()) return RBG_OK;
     const bool whole = (int64_t)idx.size() == count;
     std::vector<int64_t> sub_sizes, sub_offsets;

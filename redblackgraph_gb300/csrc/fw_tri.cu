@@ -1,4 +1,4 @@
-// fw_tri.cu -- dense closure of matrices numbered in a topological order, by the DAG closure.
+// fw_tri.cu -- dense closure of acyclic matrices by the DAG closure.
 //
 // The reference's warshall (redblackgraph/core/src/redblackgraph/warshall.c.in:88-106) runs the
 // sequential loop  for k, i, j: W(i, j) = W(i, j) (+) W(i, k) (x) W(k, j)  over the whole matrix.
@@ -20,11 +20,20 @@
 // (which report the reference's overflow or wrap for 32-bit storage, and carry 64-bit values
 // exactly), as does anything outside the clean regime or the 32-bit value range, a row of more
 // than TRI_CAP entries or n > 8192.  For 64-bit storage no product below bit 31 can overflow, so
-// the values, the diameter and the absence of errors are the reference's as well.
+// the values, the diameter and the absence of errors are the reference's as well.  A matrix the
+// closure went through whose loop does compute a product reaching bit 31 is reported as such
+// (TRI_TOP_BIT): its caller skips the 32-bit lanes, which could only report that risk.
+//
+// A matrix with entries on both sides of the diagonal (an acyclic graph in any numbering) has the
+// same closure values, but which product reaches a cell first depends on the numbering: its
+// sequential loop is replayed on the closure's pattern (the triples (i, k, j) with (i, k) and
+// (k, j) in the pattern, step by step), which gives the exact product MSBs and first values.  A
+// vertex the closure by levels never places (a cycle, or below one) sends its matrix on.
 //
 // Pipeline (one call, every decision on the device): scan the dense rows (clean-regime test,
 // which side of the diagonal, up to TRI_CAP off-diagonal entries per row) -> CSR of the
-// candidate matrices with batch-global row numbers -> closure by levels -> per-row statistics
+// candidate matrices with batch-global row numbers -> closure by levels -> for matrices in any
+// numbering, the transposed pattern, the steps' triples and the replay -> per-row statistics
 // (largest product MSB, largest first-value MSB) -> the dense rows of the accepted matrices
 // written from the closure rows -> one result record per matrix, read back once.  Scratch is
 // carved from the caller's workspace; with RBG_MODE_GRAPH the sequence, level loop included (a
@@ -48,6 +57,7 @@ constexpr int64_t TRI_MAX_N = DAG_MAX_N;     // rows of a matrix on this path (b
 constexpr int TRI_BM_WORDS = (int)(TRI_MAX_N / 32);
 constexpr unsigned TF_UNCLEAN = 1u, TF_BELOW = 2u, TF_ABOVE = 4u, TF_WIDE = 8u;
 constexpr int KIND_NONE = DAG_KIND_NONE, KIND_BELOW = DAG_KIND_BELOW, KIND_ABOVE = DAG_KIND_ABOVE;
+constexpr int KIND_GENERAL = DAG_KIND_GENERAL;
 constexpr int TRI_TOP = DAG_TOP_MSB;         // products reaching bit 31 leave the path
 
 struct TriComp {
@@ -56,7 +66,7 @@ struct TriComp {
 
 // Result of one matrix, written on the device and read back once per call.
 struct TriOut {
-    int32_t accepted, diameter;
+    int32_t verdict, diameter;               // verdict: TRI_OPEN, TRI_CLOSED or TRI_TOP_BIT
     unsigned long long executed;
 };
 
@@ -194,17 +204,21 @@ tri_scan_kernel(const T *__restrict__ in, int64_t ld_in, const TriComp *__restri
 
 // Per matrix: candidate kind from the scan's flags, and the statistics' starting values.
 __global__ void tri_kind_kernel(int count, const TriComp *__restrict__ comps, const unsigned *__restrict__ cflags,
-                                int32_t *__restrict__ ckind, int *__restrict__ cam, int *__restrict__ cfm,
-                                unsigned long long *__restrict__ cprod) {
+                                int general, int32_t *__restrict__ ckind, int *__restrict__ cam, int *__restrict__ cfm,
+                                unsigned long long *__restrict__ cprod, unsigned *__restrict__ cbad,
+                                unsigned *__restrict__ any_gen) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const unsigned f = cflags[i];
         int k = KIND_NONE;
-        if (comps[i].n > 0 && !(f & (TF_UNCLEAN | TF_WIDE)) && !((f & TF_BELOW) && (f & TF_ABOVE)))
-            k = (f & TF_ABOVE) ? KIND_ABOVE : KIND_BELOW;
+        if (comps[i].n > 0 && !(f & (TF_UNCLEAN | TF_WIDE)))
+            k = ((f & TF_BELOW) && (f & TF_ABOVE)) ? (general ? KIND_GENERAL : KIND_NONE)
+                                                  : (f & TF_ABOVE) ? KIND_ABOVE : KIND_BELOW;
         ckind[i] = k;
         cam[i] = -1;
         cfm[i] = -1;
         cprod[i] = 0;
+        cbad[i] = 0;
+        if (k == KIND_GENERAL) atomicOr(any_gen, 1u);
     }
 }
 
@@ -232,11 +246,14 @@ __global__ void tri_csr_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
     }
 }
 
-// The closure by levels left every candidate row in the pool (no pool overflow, every vertex
-// placed); otherwise nothing of this call's DAG path is used.
-__device__ __forceinline__ bool tri_dag_ok(const DagCounters *dc, int64_t R) {
-    return !(dc->flags & 3) && (int64_t)dc->placed >= R;
-}
+// The closure by levels kept every row in the pool (no pool overflow); otherwise nothing of this
+// call's DAG path is used.  A matrix with a row never placed (a cycle: only matrices with entries
+// on both sides of the diagonal can hold one) is marked in cbad.
+__device__ __forceinline__ bool tri_dag_ok(const DagCounters *dc) { return !(dc->flags & 7); }
+
+// A closure row entry outside its matrix (which a consistent closure never holds): the access is
+// skipped and the call's DAG path rejected (flag 4), so the blocked kernels decide.
+constexpr int TRI_BAD_ROW = 4;
 
 // One warp per row of a candidate matrix: the row statistics of dag_rows.cuh, reduced per
 // matrix (largest product MSB, largest first-value MSB, products).
@@ -248,13 +265,13 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, const DagCounters *dc,
                  int *__restrict__ cam, int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
     __shared__ unsigned bm_all[TRI_ROWS][TRI_BM_WORDS];
-    if (!tri_dag_ok(dc, R)) return;          // block-uniform
+    if (!tri_dag_ok(dc)) return;             // block-uniform
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * TRI_ROWS;
     for (int64_t g = (int64_t)blockIdx.x * TRI_ROWS + w; g < R; g += warps) {
         const int ci = row_comp[g];
         const int kind = ckind[ci];
-        if (kind == KIND_NONE) continue;     // warp-uniform
+        if (kind == KIND_NONE || kind == KIND_GENERAL) continue;   // warp-uniform
         const int32_t base = (int32_t)comps[ci].row_base;
         const int words = (int)((comps[ci].n + 31) >> 5);
         int am = -1, fm = -1;
@@ -272,9 +289,251 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
     }
 }
 
-__device__ __forceinline__ bool tri_accepted(int ci, const int32_t *ckind, const int *cam, const DagCounters *dc,
-                                             int64_t R) {
-    return ckind[ci] != KIND_NONE && cam[ci] < TRI_TOP && tri_dag_ok(dc, R);
+
+// ------------------------------------------------------------------------------------------
+// Matrices in any numbering (entries on both sides of the diagonal): the sequential loop
+// replayed on the closure's pattern.
+// ------------------------------------------------------------------------------------------
+// Before step k of the loop, W(i, k) and W(k, j) hold the values of paths whose intermediate
+// vertices are all below k, and every cell the loop ever fills lies in the closure's pattern C
+// (in the clean regime a cell never returns to zero).  Step k therefore touches only the triples
+// (i, k, j) with (i, k) and (k, j) in C (the pattern holds no diagonal, and i != j in a DAG); a
+// triple performs a product when both cells are non-zero at that time.  No triple of a step
+// writes a cell another triple of the step reads ((i, j) = (i', k) would need j = k), so a step's
+// triples run in parallel and the steps in order.  The replay keeps each cell's current value
+// and the largest MSB of the products it performs (an overflow risk sends the matrix to the
+// blocked kernels) and of the first value each cell receives (the diameter); the values the
+// loop ends with are the closure's, which the closure by levels already holds.
+
+// position of column c in the sorted closure row [o, o + len), or -1
+__device__ __forceinline__ int64_t tri_find_col(const int32_t *__restrict__ p_col, int64_t o, int len, int32_t c) {
+    int lo = 0, hi = len - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int32_t v = p_col[o + mid];
+        if (v == c) return o + mid;
+        if (v < c) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool tri_gen_row(int ci, const int32_t *ckind, const unsigned *cbad, const DagCounters *dc,
+                                            const unsigned *gflags) {
+    return ckind[ci] == KIND_GENERAL && !cbad[ci] && tri_dag_ok(dc) && !*gflags;
+}
+
+// One warp per candidate row: a row never placed by the closure by levels (on or below a cycle)
+// marks its matrix; the general matrices' closure rows count their columns.
+__global__ void tri_gen_count_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                                     const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
+                                     const int32_t *__restrict__ p_col, const DagCounters *dc, const unsigned *any_gen,
+                                     unsigned *__restrict__ cbad, int64_t *__restrict__ ccnt) {
+    if (!tri_dag_ok(dc) || !*any_gen) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < R; g += warps) {
+        const int ci = row_comp[g];
+        if (ckind[ci] != KIND_GENERAL) continue;   // warp-uniform
+        const int len = row_len[g];
+        if (len < 0) {
+            if (lane == 0) atomicOr(cbad + ci, 1u);
+            continue;
+        }
+        const int64_t o = row_off[g];
+        for (int q = lane; q < len; q += 32)
+            atomicAdd(reinterpret_cast<unsigned long long *>(ccnt + p_col[o + q]), 1ull);
+    }
+}
+
+// The general matrices' closure pattern transposed: per column, the rows holding it and the pool
+// position of each entry (in any order).
+__global__ void tri_gen_csc_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                                   const unsigned *__restrict__ cbad, const int64_t *__restrict__ row_off,
+                                   const int32_t *__restrict__ row_len, const int32_t *__restrict__ p_col,
+                                   const DagCounters *dc, const unsigned *any_gen, const int64_t *__restrict__ cptr,
+                                   int32_t *__restrict__ ccur, int32_t *__restrict__ csc_row,
+                                   int32_t *__restrict__ csc_pos, int64_t cap, unsigned *gflags) {
+    if (!tri_dag_ok(dc) || !*any_gen) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < R; g += warps) {
+        const int ci = row_comp[g];
+        if (ckind[ci] != KIND_GENERAL || cbad[ci]) continue;   // warp-uniform
+        const int64_t o = row_off[g];
+        const int len = row_len[g];
+        for (int q = lane; q < len; q += 32) {
+            const int32_t c = p_col[o + q];
+            const int64_t at = cptr[c] + atomicAdd(ccur + c, 1);
+            if (at < cap) {
+                csc_row[at] = (int32_t)g;
+                csc_pos[at] = (int32_t)(o + q);
+            } else {
+                atomicOr(gflags, 1u);
+            }
+        }
+    }
+}
+
+// Triples of step k (batch-global vertex g): column g's entries times row g's entries.
+__global__ void tri_gen_tcount_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                                      const unsigned *__restrict__ cbad, const int32_t *__restrict__ row_len,
+                                      const int64_t *__restrict__ cptr, const DagCounters *dc, const unsigned *any_gen,
+                                      const unsigned *gflags, int64_t *__restrict__ tcnt) {
+    const bool on = tri_dag_ok(dc) && *any_gen && !*gflags;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g <= R; g += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = 0;
+        if (on && g < R) {
+            const int ci = row_comp[g];
+            if (ckind[ci] == KIND_GENERAL && !cbad[ci]) c = (cptr[g + 1] - cptr[g]) * (int64_t)row_len[g];
+        }
+        tcnt[g] = c;
+    }
+}
+
+// One warp per vertex k of a general matrix: its step's triples (pool positions of (i, k),
+// (k, j) and (i, j)).
+__global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                                    const unsigned *__restrict__ cbad, const int64_t *__restrict__ row_off,
+                                    const int32_t *__restrict__ row_len, const int32_t *__restrict__ p_col,
+                                    const int64_t *__restrict__ cptr, const int32_t *__restrict__ csc_row,
+                                    const int32_t *__restrict__ csc_pos, const int64_t *__restrict__ tpos,
+                                    const DagCounters *dc, const unsigned *any_gen, int3 *__restrict__ trip,
+                                    int64_t cap, unsigned *gflags) {
+    if (!tri_dag_ok(dc) || !*any_gen || *gflags) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < R; k += warps) {
+        const int ci = row_comp[k];
+        if (ckind[ci] != KIND_GENERAL || cbad[ci]) continue;   // warp-uniform
+        const int64_t c0 = cptr[k], r0 = row_off[k], base = tpos[k];
+        const int cn = (int)(cptr[k + 1] - c0), rn = row_len[k];
+        const int64_t total = (int64_t)cn * rn;
+        if (base + total > cap) {
+            if (lane == 0 && total) atomicOr(gflags, 1u);
+            continue;
+        }
+        for (int64_t t = lane; t < total; t += 32) {
+            const int a = (int)(t / rn), b = (int)(t - (int64_t)a * rn);
+            const int32_t i = csc_row[c0 + a];
+            const int32_t qb = (int32_t)(r0 + b);
+            const int64_t qc = tri_find_col(p_col, row_off[i], row_len[i], p_col[qb]);
+            if (qc < 0) {
+                atomicOr(gflags, 2u);
+                continue;
+            }
+            trip[base + t] = make_int3(csc_pos[c0 + a], qb, (int32_t)qc);
+        }
+    }
+}
+
+// One warp per row of a general matrix: the current values start as A's entries (zero elsewhere
+// in the pattern); A's largest MSB starts the first-value maximum.
+__global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
+                                    const unsigned *__restrict__ cbad, const int64_t *__restrict__ indptr,
+                                    const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
+                                    const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
+                                    const int32_t *__restrict__ p_col, const DagCounters *dc, const unsigned *any_gen,
+                                    unsigned *gflags, int32_t *__restrict__ cur, int *__restrict__ cfm) {
+    if (!tri_dag_ok(dc) || !*any_gen || *gflags) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < R; g += warps) {
+        const int ci = row_comp[g];
+        if (ckind[ci] != KIND_GENERAL || cbad[ci]) continue;   // warp-uniform
+        const int64_t o = row_off[g];
+        const int len = row_len[g];
+        for (int q = lane; q < len; q += 32) cur[o + q] = 0;
+        __syncwarp();
+        int fm = -1;
+        for (int64_t e = indptr[g] + lane; e < indptr[g + 1]; e += 32) {
+            const int64_t q = tri_find_col(p_col, o, len, a_col[e]);
+            if (q < 0) {
+                atomicOr(gflags, 2u);
+                continue;
+            }
+            cur[q] = a_val[e];
+            fm = max(fm, dag_row_msb(a_val[e]));
+        }
+        fm = __reduce_max_sync(0xffffffffu, fm);
+        if (lane == 0 && fm >= 0) atomicMax(cfm + ci, fm);
+    }
+}
+
+// One warp per general matrix: its steps in order (32 step bounds read at a time, the non-empty
+// ones taken by ballot), each step's triples in parallel; the warp barrier between steps orders
+// one step's stores before the next step's loads.
+__global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_t *__restrict__ ckind,
+                                      const unsigned *__restrict__ cbad, const int64_t *__restrict__ tpos,
+                                      const int3 *__restrict__ trip, const DagCounters *dc, const unsigned *any_gen,
+                                      const unsigned *gflags, int32_t *cur, int64_t pool, int *__restrict__ cam,
+                                      int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
+    if (!tri_dag_ok(dc) || !*any_gen) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int ci = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ci < count; ci += warps) {
+        if (!tri_gen_row(ci, ckind, cbad, dc, gflags)) continue;   // warp-uniform
+        const int n = (int)comps[ci].n;
+        const int64_t base = comps[ci].row_base;
+        int top = -1, first = -1;
+        unsigned long long prods = 0;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            const int k = k0 + lane;
+            const int64_t t0 = k < n ? tpos[base + k] : 0, t1 = k < n ? tpos[base + k + 1] : 0;
+            unsigned bal = __ballot_sync(0xffffffffu, t1 > t0);
+            while (bal) {
+                const int b = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const int64_t s0 = __shfl_sync(0xffffffffu, t0, b), s1 = __shfl_sync(0xffffffffu, t1, b);
+                for (int64_t t = s0 + lane; t < s1; t += 32) {
+                    const int3 tr = trip[t];
+                    if ((unsigned)tr.x >= (unsigned)pool || (unsigned)tr.y >= (unsigned)pool ||
+                        (unsigned)tr.z >= (unsigned)pool) {
+                        atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
+                        continue;
+                    }
+                    const int32_t x = cur[tr.x], y = cur[tr.y];
+                    if (x != 0 && y != 0) {
+                        const int mx = msb_u32((uint32_t)x), my = msb_u32((uint32_t)y);
+                        const int pm = mx + my;
+                        top = max(top, pm);
+                        ++prods;
+                        const int32_t pv = (int32_t)(((uint32_t)x << my) | ((uint32_t)y ^ (1u << my)));
+                        const int32_t old = cur[tr.z];
+                        if (old == 0) {
+                            first = max(first, pm);
+                            cur[tr.z] = pv;
+                        } else if (pv < old) {
+                            cur[tr.z] = pv;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        top = __reduce_max_sync(0xffffffffu, top);
+        first = __reduce_max_sync(0xffffffffu, first);
+        for (int o = 16; o > 0; o >>= 1) prods += __shfl_xor_sync(0xffffffffu, prods, o);
+        if (lane == 0) {
+            if (top >= 0) atomicMax(cam + ci, top);
+            if (first >= 0) atomicMax(cfm + ci, first);
+            cprod[ci] += prods;
+        }
+    }
+}
+
+__device__ __forceinline__ bool tri_accepted(int ci, const int32_t *ckind, const int *cam, const unsigned *cbad,
+                                             const DagCounters *dc, const unsigned *gflags) {
+    const int k = ckind[ci];
+    return k != KIND_NONE && cam[ci] < TRI_TOP && !cbad[ci] && tri_dag_ok(dc) && !(k == KIND_GENERAL && *gflags);
+}
+
+// The statistics are complete and some product of the loop reaches bit 31 (the first such
+// product is computed from exact operands, so the test is exact).
+__device__ __forceinline__ bool tri_top_bit(int ci, const int32_t *ckind, const int *cam, const unsigned *cbad,
+                                            const DagCounters *dc, const unsigned *gflags) {
+    const int k = ckind[ci];
+    return k != KIND_NONE && cam[ci] >= TRI_TOP && !cbad[ci] && tri_dag_ok(dc) && !(k == KIND_GENERAL && *gflags);
 }
 
 // One warp per row of an accepted matrix.  Out of place, the whole dense row is written in
@@ -286,14 +545,15 @@ template <typename T>
 __global__ void __launch_bounds__(TRI_THREADS)
 tri_write_kernel(const T *__restrict__ in, int64_t ld_in, T *__restrict__ out, int64_t ld_out,
                  const TriComp *__restrict__ comps, const int64_t *__restrict__ pre, int count,
-                 const int32_t *__restrict__ ckind, const int *__restrict__ cam, const DagCounters *dc, int64_t R,
+                 const int32_t *__restrict__ ckind, const int *__restrict__ cam, const unsigned *__restrict__ cbad,
+                 const DagCounters *dc, const unsigned *gflags,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, RowStats rs) {
     constexpr int SEG = 2048 / (int)sizeof(T);
     constexpr int E = TriVec<T>::E;
     __shared__ __align__(16) T seg_all[TRI_ROWS][SEG];
     const int ci = tri_find(pre, count, blockIdx.x);
-    if (!tri_accepted(ci, ckind, cam, dc, R)) return;   // block-uniform
+    if (!tri_accepted(ci, ckind, cam, cbad, dc, gflags)) return;   // block-uniform
     const TriComp c = comps[ci];
     const int i = (int)(((int64_t)blockIdx.x - pre[ci]) * TRI_ROWS) + (threadIdx.x >> 5);
     if (i >= c.n) return;                    // warp-uniform
@@ -321,6 +581,10 @@ tri_write_kernel(const T *__restrict__ in, int64_t ld_in, T *__restrict__ out, i
         for (int q = lane; q < clen; q += 32) {
             const int j = p_col[c0 + q] - base;
             const int32_t v = p_val[c0 + q];
+            if ((unsigned)j >= (unsigned)n) {
+                atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
+                continue;
+            }
             rout[j] = (T)v;
             mx = max(mx, v);
             mark(j >> 5);
@@ -344,9 +608,13 @@ tri_write_kernel(const T *__restrict__ in, int64_t ld_in, T *__restrict__ out, i
                 }
                 const bool here = j < lim;
                 if (here) {
-                    seg[j + shift - s0] = (T)v;
-                    mx = max(mx, v);
-                    mark(j >> 5);
+                    if (j < 0 || j >= n || j + shift < s0) {   // outside the matrix, or out of order
+                        atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
+                    } else {
+                        seg[j + shift - s0] = (T)v;
+                        mx = max(mx, v);
+                        mark(j >> 5);
+                    }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, here);
                 e += __popc(bal);
@@ -403,10 +671,12 @@ tri_write_kernel(const T *__restrict__ in, int64_t ld_in, T *__restrict__ out, i
 
 __global__ void tri_result_kernel(int count, const int32_t *__restrict__ ckind, const int *__restrict__ cam,
                                   const int *__restrict__ cfm, const unsigned long long *__restrict__ cprod,
-                                  const DagCounters *dc, int64_t R, TriOut *__restrict__ res) {
+                                  const unsigned *__restrict__ cbad, const DagCounters *dc, const unsigned *gflags,
+                                  TriOut *__restrict__ res) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         TriOut o;
-        o.accepted = tri_accepted(i, ckind, cam, dc, R) ? 1 : 0;
+        o.verdict = tri_accepted(i, ckind, cam, cbad, dc, gflags) ? TRI_CLOSED
+                    : tri_top_bit(i, ckind, cam, cbad, dc, gflags) ? TRI_TOP_BIT : TRI_OPEN;
         o.diameter = cfm[i] > 0 ? cfm[i] : 0;
         o.executed = cprod[i];
         res[i] = o;
@@ -429,15 +699,17 @@ struct Carve {
 // row index, and the row pool in whatever remains.
 struct TriLayout {
     TriComp *dc;
-    int64_t *dpre, *indptr, *row_off;
-    unsigned *cflags;
+    int64_t *dpre, *indptr, *row_off, *ccnt, *cptr, *tcnt, *tpos;
+    unsigned *cflags, *cbad, *gflags;        // gflags[0]: the general path's scratch overflowed; [1]: any general
     int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val, *row_len, *p_col, *p_val;
+    int32_t *ccur, *csc_row, *csc_pos, *cur;
+    int3 *trip;
     int *cam, *cfm;
     unsigned long long *cprod;
     TriOut *res;
     void *tmp, *dag_ws;
     size_t scan_tmp;
-    int64_t pool;
+    int64_t pool, csc_cap, trip_cap;
     size_t fixed;                            // bytes before the pool
 };
 
@@ -452,6 +724,8 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     L.cam = cv.take<int>(C);
     L.cfm = cv.take<int>(C);
     L.cprod = cv.take<unsigned long long>(C);
+    L.cbad = cv.take<unsigned>(C);
+    L.gflags = cv.take<unsigned>(2);
     L.res = cv.take<TriOut>(C);
     L.row_cnt = cv.take<int32_t>(NR);
     L.row_comp = cv.take<int32_t>(NR);
@@ -464,11 +738,26 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     L.dag_ws = cv.take<unsigned char>(dag_workspace_for((int64_t)NR, (int64_t)(NR * TRI_CAP)));
     L.row_off = cv.take<int64_t>(NR);
     L.row_len = cv.take<int32_t>(NR);
+    L.ccnt = cv.take<int64_t>(NR + 1);
+    L.cptr = cv.take<int64_t>(NR + 1);
+    L.ccur = cv.take<int32_t>(NR);
+    L.tcnt = cv.take<int64_t>(NR + 1);
+    L.tpos = cv.take<int64_t>(NR + 1);
     L.fixed = align_up(cv.off, 256);
-    const size_t rest = ws_bytes > L.fixed + 256 ? ws_bytes - L.fixed - 256 : 0;
-    L.pool = (int64_t)(rest / 8 / 64 * 64);  // column and value halves
-    L.p_col = base ? reinterpret_cast<int32_t *>(base + L.fixed) : nullptr;
-    L.p_val = base ? reinterpret_cast<int32_t *>(base + align_up(L.fixed + (size_t)L.pool * 4, 256)) : nullptr;
+    // the rest: 40% for the row pool (column, value and the replay's current value per entry),
+    // 15% for the transposed pattern, 45% for the replay's triples
+    const size_t rest = ws_bytes > L.fixed + 2048 ? ws_bytes - L.fixed - 2048 : 0;
+    L.pool = std::min<int64_t>((int64_t)(rest / 10 * 4 / 12 / 64 * 64), (int64_t)INT32_MAX / 64 * 64);
+    L.csc_cap = (int64_t)(rest / 100 * 15 / 8);
+    L.trip_cap = (int64_t)(rest / 100 * 45 / 12);
+    Carve tail{base};
+    tail.off = L.fixed;
+    L.p_col = tail.take<int32_t>((size_t)L.pool);
+    L.p_val = tail.take<int32_t>((size_t)L.pool);
+    L.cur = tail.take<int32_t>((size_t)L.pool);
+    L.csc_row = tail.take<int32_t>((size_t)L.csc_cap);
+    L.csc_pos = tail.take<int32_t>((size_t)L.csc_cap);
+    L.trip = tail.take<int3>((size_t)L.trip_cap);
 }
 
 struct TriShape {
@@ -484,6 +773,7 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     const int64_t R = sh.R;
     const int count = (int)sh.count;
     RBG_CUDA_TRY(cudaMemsetAsync(L.cflags, 0, (size_t)count * 4, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(L.gflags, 0, 8, s));
     // 1. scan
     {
         cudaEvent_t t = timer_begin(4, s);
@@ -496,9 +786,8 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     // 2. CSR of the candidates and their closure by levels
     cudaEvent_t tdag = timer_begin(5, s);
     note_launches(4);
-    tri_kind_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>(count, L.dc, L.cflags,
-                                                                                          L.ckind, L.cam, L.cfm,
-                                                                                          L.cprod);
+    tri_kind_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>(
+        count, L.dc, L.cflags, 1, L.ckind, L.cam, L.cfm, L.cprod, L.cbad, L.gflags + 1);
     tri_count_kernel<<<grid_for(R + 1, 256), 256, 0, s>>>(R, L.row_cnt, L.row_comp, L.ckind, L.indptr);
     size_t tb = L.scan_tmp;
     RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb, L.indptr, L.indptr, (int)(R + 1), s));
@@ -507,10 +796,41 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     RBG_CUDA_TRY(cudaGetLastError());
     *launches += 5;
     rbg_csr_t A{R, R, L.indptr, L.a_col, L.a_val};
+    RBG_CUDA_TRY(cudaMemsetAsync(L.row_len, 0xff, (size_t)R * 4, s));   // -1: never placed
     int rc = dag_enqueue(&A, R * TRI_CAP, L.dag_ws, L.p_col, L.p_val, L.pool, L.row_off, L.row_len, s, captured,
                          dcount, launches);
     if (rc) return rc;
     timer_end(5, tdag, s);
+    // 2b. matrices in any numbering: the loop replayed on the closure's pattern (every kernel
+    // returns at once when the batch holds none)
+    {
+        cudaEvent_t tg = timer_begin(8, s);
+        const DagCounters *dcn = *dcount;
+        const unsigned *any = L.gflags + 1;
+        const int gw = grid_for(R * 32, 256);
+        RBG_CUDA_TRY(cudaMemsetAsync(L.ccnt, 0, (size_t)(R + 1) * 8, s));
+        RBG_CUDA_TRY(cudaMemsetAsync(L.ccur, 0, (size_t)R * 4, s));
+        note_launches(8);
+        tri_gen_count_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.row_off, L.row_len, L.p_col, dcn, any,
+                                                L.cbad, L.ccnt);
+        size_t tb2 = L.scan_tmp;
+        RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.ccnt, L.cptr, (int)(R + 1), s));
+        tri_gen_csc_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.row_off, L.row_len, L.p_col, dcn, any,
+                                              L.cptr, L.ccur, L.csc_row, L.csc_pos, L.csc_cap, L.gflags);
+        tri_gen_tcount_kernel<<<grid_for(R + 1, 256), 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.row_len, L.cptr,
+                                                                  dcn, any, L.gflags, L.tcnt);
+        tb2 = L.scan_tmp;
+        RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.tcnt, L.tpos, (int)(R + 1), s));
+        tri_gen_fill_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.row_off, L.row_len, L.p_col, L.cptr,
+                                               L.csc_row, L.csc_pos, L.tpos, dcn, any, L.trip, L.trip_cap, L.gflags);
+        tri_gen_init_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.indptr, L.a_col, L.a_val, L.row_off,
+                                               L.row_len, L.p_col, dcn, any, L.gflags, L.cur, L.cfm);
+        tri_gen_replay_kernel<<<grid_for((int64_t)count * 32, 256), 256, 0, s>>>(
+            count, L.dc, L.ckind, L.cbad, L.tpos, L.trip, dcn, any, L.gflags, L.cur, L.pool, L.cam, L.cfm, L.cprod);
+        RBG_CUDA_TRY(cudaGetLastError());
+        timer_end(8, tg, s);
+        *launches += 8;
+    }
     // 3. statistics
     {
         cudaEvent_t t = timer_begin(6, s);
@@ -526,10 +846,11 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
         cudaEvent_t t = timer_begin(7, s);
         note_launches(2);
         tri_write_kernel<T><<<(unsigned)sh.ctas, TRI_THREADS, 0, s>>>(in, sh.ld_in, out, sh.ld_out, L.dc, L.dpre,
-                                                                      count, L.ckind, L.cam, *dcount, R, L.row_off,
-                                                                      L.row_len, L.p_col, L.p_val, rs);
+                                                                      count, L.ckind, L.cam, L.cbad, *dcount,
+                                                                      L.gflags, L.row_off, L.row_len, L.p_col,
+                                                                      L.p_val, rs);
         tri_result_kernel<<<(unsigned)std::min<int64_t>((count + 255) / 256, 1024), 256, 0, s>>>(
-            count, L.ckind, L.cam, L.cfm, L.cprod, *dcount, R, L.res);
+            count, L.ckind, L.cam, L.cfm, L.cprod, L.cbad, *dcount, L.gflags, L.res);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(7, t, s);
     }
@@ -672,8 +993,8 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const 
         note_launches(fixed_launches + iters * (3 * DAG_GRAPH_CHUNK + 1));
     }
     for (size_t i = 0; i < C; ++i) {
-        if (!h[i].accepted) continue;
-        closed[i] = 1;
+        closed[i] = (char)h[i].verdict;
+        if (h[i].verdict != TRI_CLOSED) continue;
         rbg_result_t &r = results[i];
         r.status = RBG_OK;
         r.flags = 0;

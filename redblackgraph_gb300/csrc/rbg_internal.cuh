@@ -101,8 +101,9 @@ void launch_recording(bool on);
 // Benchmark timer (rbg_profile_begin / rbg_profile_end_slots): CUDA events around the kernels
 // of each slot, recorded on the launching stream while the timer is on.  Slots: 0 phase-3
 // tiles, 1 panels, 2 diagonal tiles, 3 convert + finalize, 4 DAG path scan, 5 DAG path
-// closure by levels (with its CSR), 6 DAG path statistics, 7 DAG path write.
-constexpr int TIMER_SLOTS = 8;
+// closure by levels (with its CSR), 6 DAG path statistics, 7 DAG path write, 8 DAG path replay
+// of matrices in any numbering (pattern, triples, replay).
+constexpr int TIMER_SLOTS = 9;
 cudaEvent_t timer_begin(int slot, cudaStream_t s);
 void timer_end(int slot, cudaEvent_t start, cudaStream_t s);
 bool timer_on();
@@ -142,13 +143,18 @@ int dag_enqueue(const rbg_csr_t *A, int64_t nnz_bound, void *workspace, int32_t 
                 DagCounters **counters, int64_t *launches);
 constexpr int DAG_GRAPH_CHUNK = 4;           // levels per iteration of the graph's while node
 
-// fw_tri.cu: the components of an int32 or int64 batch whose off-diagonal entries all lie on one
-// side of the diagonal (vertices numbered in a topological order) and are in the clean regime,
-// closed through the DAG closure by levels; sets closed[i] and results[i] for each of them and
-// leaves every other component untouched.  Scratch comes from the caller's workspace (`ws`,
+// fw_tri.cu: the components of an int32 or int64 batch that are acyclic and in the clean regime
+// (at most 16 off-diagonal entries per row, at most 8192 rows), closed through the DAG closure by
+// levels (in any numbering: off the topological order the loop is replayed on the closure's
+// pattern for the diameter and the overflow decision); sets closed[i] = TRI_CLOSED and results[i] for each
+// of them and leaves every other component untouched.  closed[i] = TRI_TOP_BIT marks a component
+// the closure went through completely whose loop computes a product reaching bit 31: 32-bit
+// lanes would only report that risk, so the caller goes on with 64-bit lanes (int64) or the
+// exact kernel (int32).  Scratch comes from the caller's workspace (`ws`,
 // `ws_bytes`); a workspace too small for a closure leaves its components to the other paths.
 // ld_in / ld_out are the row strides of every block (0: each block's own n).  With
 // RBG_MODE_GRAPH in `mode` the whole sequence is replayed from a cached CUDA graph.
+constexpr char TRI_OPEN = 0, TRI_CLOSED = 1, TRI_TOP_BIT = 2;
 template <typename T>
 int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const int64_t *out_off, int64_t ld_in,
               int64_t ld_out, const T *in, T *out, rbg_result_t *results, char *closed, unsigned char *ws,

@@ -170,10 +170,10 @@ def test_dag_path_vs_oracle(native, in_place, dtype):
 
 
 def test_dag_path_mixed_batch_and_opt_out(native):
-    """A batch mixing DAG-path matrices with ones that must take the blocked kernels (entries
-    on both sides, unclean, a cycle, rows of more than 16 entries, values that reach the top
-    bit): every result is the oracle's and lands at its own index; RBG_MODE_NO_DAG gives the
-    same results on the blocked path."""
+    """A batch mixing DAG-path matrices (numbered oldest first, youngest first, or shuffled) with
+    ones that must take the blocked kernels (unclean, a cycle, rows of more than 16 entries,
+    values that reach the top bit): every result is the oracle's and lands at its own index;
+    RBG_MODE_NO_DAG gives the same results on the blocked path."""
     from redblackgraph_gb300 import synth, _lib
     rng = np.random.default_rng(11)
     ped = synth.pedigree(200, 9, 3, dtype=np.int64)
@@ -202,9 +202,9 @@ def test_dag_path_mixed_batch_and_opt_out(native):
             assert (W == Wo).all() and r.diameter == do
     paths = [r.path for r in res]
     dag, blk = _lib.PATH_DAG, _lib.PATH_BLOCKED32
-    assert [paths[k] for k in (0, 1, 2, 3, 5, 6, 7, 8)] == [dag, blk, dag, _lib.PATH_EXACT, blk, dag,
+    assert [paths[k] for k in (0, 1, 2, 3, 5, 6, 7, 8)] == [dag, dag, dag, _lib.PATH_EXACT, blk, dag,
                                                            paths[7], dag], paths
-    assert res[4].status == _lib.RBG_ERR_CYCLE and paths[7] != dag
+    assert res[4].status == _lib.RBG_ERR_CYCLE and paths[4] != dag and paths[7] != dag
     Ws2, res2 = run_batch(mats, mode=_lib.MODE_NO_DAG)
     for W, W2, r, r2 in zip(Ws, Ws2, res, res2):
         assert r2.status == r.status and r2.path != _lib.PATH_DAG
@@ -306,3 +306,44 @@ def test_dag_path_calls_on_two_streams_overlap(native):
             Wo, do, so, _ = O.warshall(A)
             assert r.path == _lib.PATH_DAG and r.status == so == 0 and r.diameter == do
             assert (h[k:k + n * n].reshape(n, n) == Wo).all()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64])
+def test_dag_path_any_numbering_vs_oracle(native, dtype):
+    """Matrices whose vertices are not numbered in a topological order (random relabellings of
+    DAGs and pedigrees, entries on both sides of the diagonal) take the DAG path: the sequential
+    loop replayed on the closure's pattern gives the oracle's values, diameters (each cell's
+    first value in loop order) and errors, in both semantics (Cython: int32); deep ones whose
+    products reach bit 31, and cyclic ones, leave the path with the oracle's results."""
+    from redblackgraph_gb300 import synth, _lib
+    rng = np.random.default_rng(23)
+    mats = []
+    for t in range(70):
+        n = int(rng.integers(2, 80))
+        A = _random_dag(rng, n, rng.uniform(0.03, 0.35))
+        p = rng.permutation(n)
+        mats.append(A[p][:, p].astype(dtype))
+    for n in (120, 600, 1500, 2000):
+        A = synth.pedigree(n, synth.generations_for(n), n + 5, dtype=dtype)
+        p = rng.permutation(n)
+        mats.append(A[p][:, p].copy())
+    cyc = synth.pedigree(150, 8, 41, dtype=dtype)
+    Wc, _, _, _ = O.warshall(cyc)
+    v, u = max(zip(*np.nonzero(np.tril(Wc, -1))), key=lambda t: t[0] - t[1])
+    cyc[u, v] = 2
+    p = rng.permutation(150)
+    mats.append(cyc[p][:, p].copy())
+    semantics = ((0, O.warshall), (_lib.MODE_CYTHON, O.fw_cython)) if dtype == np.int32 else ((0, O.warshall),)
+    for mode, oracle in semantics:
+        expect = [oracle(A) for A in mats]
+        for graph in (0, _lib.MODE_GRAPH):
+            Ws, res = run_batch(mats, mode=mode | graph)
+            dag = 0
+            for A, W, r, (Wo, do, so, _) in zip(mats, Ws, res, expect):
+                assert r.status == so
+                if so == 0:
+                    assert (W == Wo).all() and r.diameter == do
+                dag += r.path == _lib.PATH_DAG
+            assert dag >= 50
+            assert res[-1].status == _lib.RBG_ERR_CYCLE and res[-1].path != _lib.PATH_DAG
+            assert all(r.path == _lib.PATH_DAG for r in res[-5:-1])   # the relabelled pedigrees

@@ -145,12 +145,12 @@ def test_golden_adaptive_and_component_labels(native, golden):
         assert r.diameter == rec["diameter"], rec["name"]
 
 
-@pytest.mark.parametrize("shuffle", [True, False])
-def test_recorded_row_statistics_equal_the_counting_pass(native, shuffle):
+@pytest.mark.parametrize("shuffle,blocked", [(True, True), (True, False), (False, False)])
+def test_recorded_row_statistics_equal_the_counting_pass(native, shuffle, blocked):
     """rbg_fw_batch_rows records, while it writes the result (finalisation of the blocked
-    kernels for shuffled components, the DAG path's writes for components numbered oldest
-    first), the row counts, chunk masks and component maxima that rbg_cc_compact_count would
-    read back from the closed blocks."""
+    kernels with RBG_MODE_NO_DAG, else the DAG path's writes: components numbered oldest first,
+    or shuffled and replayed in their own numbering), the row counts, chunk masks and component
+    maxima that rbg_cc_compact_count would read back from the closed blocks."""
     import ctypes
     import torch
     from redblackgraph_gb300 import synth, _lib
@@ -170,15 +170,11 @@ def test_recorded_row_statistics_equal_the_counting_pass(native, shuffle):
     cmax = torch.zeros(comps.count, dtype=torch.int32, device="cuda")
     stats = _lib.RbgRowStats(comps.start.data_ptr(), comps.sorted_vertex.data_ptr(), row_count.data_ptr(),
                              mask.data_ptr(), cmax.data_ptr())
-    mode = _lib.MODE_CYTHON | _lib.MODE_GRAPH
+    mode = _lib.MODE_CYTHON | _lib.MODE_GRAPH | (_lib.MODE_NO_DAG if blocked else 0)
     _, res = fw_batch(blocks.flat, blocks.sizes, blocks.offsets, out=blocks.flat, mode=mode, as_array=True,
                       row_stats=stats)
     assert (res["status"] == 0).all()
-    if shuffle:     # small components may still come out numbered in a topological order
-        assert np.isin(res["path"], [_lib.PATH_BLOCKED32, _lib.PATH_DAG]).all()
-        assert (res["path"] == _lib.PATH_BLOCKED32).sum() >= 10
-    else:
-        assert (res["path"] == _lib.PATH_DAG).all()
+    assert (res["path"] == (_lib.PATH_BLOCKED32 if blocked else _lib.PATH_DAG)).all()
     _, res2 = fw_batch(ref, blocks.sizes, blocks.offsets, out=ref, mode=mode, as_array=True)
     assert torch.equal(ref, blocks.flat)
     # the counting pass over the same closed blocks

@@ -274,3 +274,20 @@ def test_scalar_tables_on_device(native, golden):
     r2 = np.arange(-1, 4)
     X, Y = np.meshgrid(r2, r2, indexing="ij")
     assert (avos_sum_array(X, Y) == arrays["scalar_sum_table"]).all()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64])
+def test_single_matrix_any_numbering_dag_path(native, dtype):
+    """rbg_fw_dense on relabelled pedigrees (entries on both sides of the diagonal): the DAG path
+    replays the loop in the given numbering; W and diameter equal the oracle's."""
+    from redblackgraph_gb300 import synth, _lib
+    rng = np.random.default_rng(5)
+    for n in (5, 200, 1024, 1800):
+        A = synth.pedigree(n, synth.generations_for(n), n + 9, dtype=dtype)
+        p = rng.permutation(n)
+        A = A[p][:, p].copy()
+        Wo, do, so, _ = O.warshall(A)
+        W, res = gpu_close(A)
+        assert so == 0 and res.status == 0
+        assert (W == Wo).all() and res.diameter == do
+        assert res.path == _lib.PATH_DAG, (n, res.path)

@@ -95,6 +95,27 @@ def _dense_closure(A):
     return sp.csr_matrix(W.astype(np.int32))
 
 
+def _squaring_diameter(P):
+    """The reference's transitive_closure_gpu diameter (gpu/transitive_closure.py:52-72): the
+    number of squarings R <- R (+) R^2 that change R, or floor(log2) of the largest |value| > 1 of
+    the result when that is larger.  The squarings run on the oracle's CSR product; the sum keeps
+    the smaller |value| per cell (R's on a tie)."""
+    R = sorted_csr(sp.csr_matrix(P, dtype=np.int64))
+    changing = 0
+    for t in range(64):
+        S, _ = O.rb_matmul_csr(R, R)
+        S = sorted_csr(sp.csr_matrix(S, dtype=np.int64))
+        Rd, Sd = R.toarray(), S.toarray()
+        take = (Rd == 0) | ((Sd != 0) & (np.abs(Sd) < np.abs(Rd)))
+        N = sorted_csr(sp.csr_matrix(np.where(take, Sd, Rd)))
+        if same(N, R):
+            break
+        R, changing = N, t + 1
+    a = np.abs(R.data)
+    a = a[a > 1]
+    return max(changing, int(np.floor(np.log2(a.max())))) if a.size else changing
+
+
 def test_squaring_closures_match_dense_oracle(native):
     from redblackgraph_gb300 import synth
     from redblackgraph_gb300.sparse import transitive_closure_squaring, transitive_closure_dag_sparse
@@ -116,6 +137,7 @@ def test_squaring_closures_match_dense_oracle(native):
     G = CSRMatrixGPU.from_cpu(P)
     R, diam = transitive_closure_gpu(G)
     assert same(R.to_cpu(), Ep)
+    assert diam == _squaring_diameter(P)
     Rd, dd = transitive_closure_dag_gpu(G)
     assert same(Rd.to_cpu(), Ep) and dd == int(np.floor(np.log2(np.abs(Ep.data).max())))
 

@@ -61,11 +61,14 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(native):
 
 
 def _wide_int64():
-    """A pedigree whose int64 closure values pass 2^31 without overflowing 64 bits (64-bit lanes
-    of the blocked kernels)."""
+    """A pedigree whose last vertex with parents reaches its first parent by an edge value past
+    2^31 (closure values past bit 31): the blocked kernels with 64-bit lanes."""
     from redblackgraph_gb300 import synth
     A = synth.pedigree(200, 10, 9, dtype=np.int64)
-    return np.where(A > 1, A << 8, A)
+    i = int(np.nonzero((A > 1).any(axis=1))[0][-1])
+    p = int(np.nonzero(A[i] > 1)[0][0])
+    A[i, p] <<= 32
+    return A
 
 
 def _unclean_int32(n):
@@ -76,32 +79,37 @@ def _unclean_int32(n):
     return A.astype(np.int32)
 
 
-def test_noalloc_every_path_inside_its_array(native):
+PATH_CASES = ["dag_int32", "blocked64", "exact", "dag_int64"]
+
+
+@pytest.mark.parametrize("case", PATH_CASES)
+def test_noalloc_every_path_inside_its_array(native, case):
     """The fixed array also holds the scratch of the other paths a closure can take: the DAG
     path, the blocked kernels with 64-bit lanes and the exact sequential-order kernel (with its
-    status block).  Each case runs twice in a row and equals the workspace entry point, path
-    included."""
+    status block).  Each case runs twice in a row, takes its path and equals the oracle's
+    sequential loop (values, diameter, status)."""
     import torch
+    from oracle import oracle as O
     from redblackgraph_gb300 import synth, _lib
     from redblackgraph_gb300.device import to_device, to_host
     L = native
-    cases = [(synth.pedigree(900, 15, 3, dtype=np.int32), _lib.PATH_DAG),
-             (_wide_int64(), _lib.PATH_BLOCKED64),
-             (_unclean_int32(300), _lib.PATH_EXACT),
-             (synth.pedigree(_lib.NOALLOC_MAX_N, 20, 4, dtype=np.int64), _lib.PATH_DAG)]
-    for A, path in cases:
-        d = to_device(A)
-        ref_out = torch.empty_like(d)
-        ref = _close_with_workspace(L, _lib, d, ref_out)
-        assert ref.path == path
-        for _ in range(2):
-            out = torch.full_like(d, 5)
-            res = _close_without_workspace(L, _lib, d, out)
-            torch.cuda.synchronize()
-            assert (res.status, res.diameter, res.path) == (ref.status, ref.diameter, ref.path)
-            assert (res.k, res.i, res.j) == (ref.k, ref.i, ref.j)
-            if ref.status == _lib.RBG_OK:
-                assert (to_host(out) == to_host(ref_out)).all()
+    A, path = {"dag_int32": lambda: (synth.pedigree(900, 15, 3, dtype=np.int32), _lib.PATH_DAG),
+               "blocked64": lambda: (_wide_int64(), _lib.PATH_BLOCKED64),
+               "exact": lambda: (_unclean_int32(300), _lib.PATH_EXACT),
+               "dag_int64": lambda: (synth.pedigree(_lib.NOALLOC_MAX_N, 20, 4, dtype=np.int64), _lib.PATH_DAG)}[case]()
+    Wo, do, so, info = O.warshall(A)
+    d = to_device(A)
+    for _ in range(2):
+        out = torch.full_like(d, 5)
+        res = _close_without_workspace(L, _lib, d, out)
+        torch.cuda.synchronize()
+        assert res.path == path
+        assert (res.status, res.diameter) == (so, do)
+        if so == _lib.RBG_OK:
+            assert (to_host(out) == Wo).all()
+        else:
+            assert (res.k, res.i, res.j) == tuple(info[2:5])
+        assert (to_host(d) == A).all()
 
 
 def test_noalloc_refuses_sizes_beyond_its_array(native):
