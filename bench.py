@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving workload (0: skip)")
     ap.add_argument("--serve-count", type=int, default=0, help="requests in the serving stream")
-    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve", "anynum"], default=None,
+    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve", "anynum", "dense"],
+                    default=None,
                     help="run one secondary workload alone and print its JSON (profiling cases)")
     ap.add_argument("--secondary", type=int, default=1,
                     help="also measure the per-component plain path, one n=8192 int64 closure and "
@@ -520,6 +521,69 @@ def run_any_numbering(w, steps=5):
     return line
 
 
+def dense_layered_dag(n, layers, p, seed, dtype=np.int32):
+    """A dense DAG the DAG path does not take (rows of hundreds of entries): vertices in `layers`
+    layers numbered in layer order, every vertex linked to each vertex of an earlier layer with
+    probability p (values 2 / 3), diagonal +-1.  Its closure is dense and its values stay below
+    bit `layers` (one bit per edge of a path)."""
+    rng = np.random.default_rng(seed)
+    layer = np.sort(rng.integers(0, layers, size=n))
+    link = (layer[:, None] > layer[None, :]) & (rng.random((n, n)) < p)
+    A = np.where(link, rng.integers(2, 4, size=(n, n)), 0).astype(dtype)
+    np.fill_diagonal(A, rng.choice(np.array([-1, 1], dtype=dtype), size=n))
+    return A
+
+
+def run_dense_blocked(n=4096, layers=24, p=0.5, seed=5, steps=5):
+    """The blocked Floyd-Warshall kernels on the workload they exist for: one dense layered DAG
+    (n=4096, int32; every row has hundreds of entries, so the DAG path declines it), whose
+    closure is dense, so nearly every tile item runs all 64 steps of its round.  ALU roofline on
+    the executed relaxations; a 1024-vertex instance of the same generator is checked bit-exact
+    against the oracle's sequential loop."""
+    import torch
+    from oracle import oracle as orc
+    from redblackgraph_gb300 import _lib
+    from redblackgraph_gb300.dense import fw_dense
+    from redblackgraph_gb300.device import to_device, to_host
+    stream = torch.cuda.current_stream()
+    small = dense_layered_dag(1024, layers, p, seed + 1)
+    Wo, do, so, _ = orc.warshall(small)
+    ds = to_device(small)
+    Ws, rs = fw_dense(ds)
+    torch.cuda.synchronize()
+    exact = bool(so == 0 and rs.status == 0 and rs.diameter == do and (to_host(Ws) == Wo).all())
+    A = dense_layered_dag(n, layers, p, seed)
+    d = to_device(A)
+    out = torch.empty_like(d)
+    for _ in range(3):
+        _, res = fw_dense(d, out=out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fw_dense(d, out=out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / steps
+    kp = {k: v for k, v in profile_kernels(lambda: fw_dense(d, out=out)).items() if v[1]}
+    phase_ms = sum(kp[k][0] for k in ("fw_tile_kernel", "fw_panel_kernel", "fw_diag_kernel") if k in kp)
+    peak, sms = int32_peak_ops(0, None)
+    alu = res.executed * OPS_PER_RELAXATION / (phase_ms / 1e3) / 1e12 if phase_ms else None
+    nnz_out = int(np.count_nonzero(to_host(out)))
+    return {"workload": f"one dense layered DAG, n={n}, {layers} layers, link probability {p}, int32 "
+                        f"({int(np.count_nonzero(A)) / n:.0f} entries per row, {nnz_out / n / n:.0%} of the "
+                        "closure non-zero)",
+            "value": n ** 3 / t, "unit": UNIT, "ms": t * 1e3, "path": int(res.path), "status": int(res.status),
+            "diameter": int(res.diameter), "executed_relaxations": int(res.executed),
+            "roofline": {"bound": "int32_alu", "unit": "Tops/s", "achieved": alu, "peak": peak / 1e12,
+                         "frac": alu / (peak / 1e12) if alu else None,
+                         "kernel": "fw_diag_kernel + fw_panel_kernel + fw_tile_kernel",
+                         "ops_per_relaxation": OPS_PER_RELAXATION,
+                         "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock"},
+            "kernel_ms": {k: v[0] for k, v in kp.items()},
+            "bit_exact_vs_oracle_n1024": exact}
+
+
 def fullsize_fixture(name):
     """The digest helpers and the reference's digests of one bench input (tests/golden/
     fullsize.json, made by running the reference's own CPU code on that input)."""
@@ -746,6 +810,19 @@ def run_spgemm_forest(seed=7):
     mk, fx = fullsize_fixture("forest2m")
     fixed_point_ok = bool(fx) and mk.csr_digest(A) == fx["input_sha256"] and \
         mk.csr_digest(R.to_scipy()) == fx["closure_sha256"]
+    # the same loop in its semi-naive form (squaring_closure: R (+) D R (+) R D once the last step
+    # changed at most half of R), timed end to end on the stream, host decisions included
+    from redblackgraph_gb300.spgemm import squaring_closure
+    squaring_closure(R0, sem=SEM_C64, seminaive=True)           # warm-up
+    torch.cuda.synchronize()
+    steps = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    Rs, changed = squaring_closure(R0, sem=SEM_C64, steps=steps, seminaive=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    semi_ms = e0.elapsed_time(e1)
+    semi_ok = bool(fx) and mk.csr_digest(Rs.to_scipy()) == fx["closure_sha256"]
     peak = hbm_peak_gbs()
     rows, tb, tms = [], 0.0, 0.0
     for e0, e1, nnz_a, nnz_c, prods in rec:
@@ -775,6 +852,17 @@ def run_spgemm_forest(seed=7):
                          "frac": tb / (tms / 1e3) / 1e9 / peak, "peak_source": "measured copy bandwidth"},
             "first_squaring_bit_exact_vs_oracle": same,
             "bit_exact_vs_reference_fixture": fixed_point_ok,
+            "semi_naive": {"total_ms": semi_ms, "changing_steps": changed,
+                           "steps": [{"form": f, "products": pr, "nnz_in": a, "nnz_out": b} for f, pr, a, b in steps],
+                           "products": int(sum(x[1] for x in steps)),
+                           "full_squaring_products": int(sum(r["products"] for r in rows)),
+                           "vs_full_squaring_loop": (tms / semi_ms) if semi_ms > 0 else None,
+                           "how": "redblackgraph_gb300.spgemm.squaring_closure(seminaive=True), an option "
+                                  "(the drop-ins run the plain loop): the same R after every step, CUDA events "
+                                  "around the whole loop (diff kernels and host decisions included); slower "
+                                  "than the plain loop here because every step still merges all of R and "
+                                  "computes its difference",
+                           "bit_exact_vs_reference_fixture": semi_ok},
             "fixture_note": "the squaring's fixed point against the digest of the reference's Cython DAG "
                             "closure of the same forest (tests/golden/fullsize.json)",
             "cpu_baseline": {"first_product_s": tcpu, "gpu_first_squaring_ms": rows[0]["ms"],
@@ -934,6 +1022,7 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         fn = {"spgemm": run_spgemm_forest, "dag": run_dag_forest, "compose": run_compose,
               "single": run_single_dense, "anynum": lambda: run_any_numbering(workload(0)),
+              "dense": run_dense_blocked,
               "serve": lambda: run_serving(args.serve_count)}[args.only]
         print(json.dumps(fn()))
         return
@@ -1031,6 +1120,7 @@ def main():
         line["dag_levels"] = run_dag_forest()
         line["relational_composition"] = run_compose()
         line["any_numbering"] = run_any_numbering(w)
+        line["dense_blocked"] = run_dense_blocked()
     if args.serve:
         line["serving"] = run_serving(args.serve_count)
     if rank == 0:

@@ -298,6 +298,34 @@ int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, const void *h
                            int32_t *indices, int32_t *data, rbg_stream_t stream);
 
 /*
+ * The entries of X that Y does not hold with the same value: Z = {(i, j, X[i][j]) : (i, j) not
+ * stored in Y, or Y[i][j] != X[i][j]} (values compared as integers; X and Y of any RBG_DTYPE_*,
+ * rows sorted, no duplicates).  The squaring closure's step difference: with Z = R_t minus R_(t-1),
+ * R_(t+1) = R_t (+) R_t^2 equals R_t (+) Z R_t (+) R_t Z, because every product of two entries
+ * that did not change was already folded into R_t (the semi-naive form of the squaring loop of
+ * redblackgraph/sparse/csgraph/transitive_closure.py:198-380 and
+ * redblackgraph/gpu/transitive_closure.py:26-72).  Count step (head sized by
+ * rbg_spgemm_head_bytes; *nnz on the host; synchronises `stream`), then fill step into caller
+ * buffers (Z's values in X's storage type).
+ */
+int32_t rbg_csr_diff_count(int32_t x_dtype, const rbg_csr_t *X, int32_t y_dtype, const rbg_csr_t *Y, void *head,
+                           int64_t head_bytes, int64_t *nnz, rbg_stream_t stream);
+int32_t rbg_csr_diff_fill(int32_t x_dtype, const rbg_csr_t *X, int32_t y_dtype, const rbg_csr_t *Y,
+                          const void *head, int64_t *indptr, int32_t *indices, void *data, rbg_stream_t stream);
+
+/*
+ * Operands of one semi-naive squaring step as a single product: A' = [D R] (n x 2n: row i is D's
+ * row i, then R's row i with its columns moved by n) and B' = [R ; D] (2n x n: R's rows, then
+ * D's), so that A' B' = D R (+) R D, and rbg_spgemm_* on (A', B') with R merged forms
+ * R (+) D R (+) R D in one pass.  D and R: n x n, values of `dtype` (4 or 8 bytes), rows sorted.
+ * Caller buffers: a_indptr n + 1, b_indptr 2n + 1, indices and data nnz(D) + nnz(R) each.
+ * Reads nnz(D) and nnz(R) back (synchronises `stream`), then enqueues the copies.
+ */
+int32_t rbg_spgemm_seminaive_operands(int32_t dtype, const rbg_csr_t *D, const rbg_csr_t *R, int64_t *a_indptr,
+                                      int32_t *a_indices, void *a_data, int64_t *b_indptr, int32_t *b_indices,
+                                      void *b_data, rbg_stream_t stream);
+
+/*
  * Diameter source of the sparse DAG closure: the largest magnitude among the stored entries of A
  * and the candidates A[v][w] (x) C[w][x] (w != v, x over row w of the closure C, Cython int32
  * product), as redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:262-305 keeps it

@@ -121,6 +121,12 @@ SIGNATURES = [
     ("rbg_csr_merge_count", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _I64,
                                    ctypes.POINTER(_I64), _P]),
     ("rbg_csr_merge_fill", _I32, [ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _P, _P, _P, _P]),
+    ("rbg_csr_diff_count", _I32, [_I32, ctypes.POINTER(RbgCsr), _I32, ctypes.POINTER(RbgCsr), _P, _I64,
+                                  ctypes.POINTER(_I64), _P]),
+    ("rbg_csr_diff_fill", _I32, [_I32, ctypes.POINTER(RbgCsr), _I32, ctypes.POINTER(RbgCsr), _P, _P, _P, _P,
+                                 _P]),
+    ("rbg_spgemm_seminaive_operands", _I32, [_I32, ctypes.POINTER(RbgCsr), ctypes.POINTER(RbgCsr), _P, _P, _P,
+                                             _P, _P, _P, _P]),
     ("rbg_avos_matmul_workspace_bytes", _I32, [_I32, _I64, _I64, _I64, ctypes.POINTER(_I64)]),
     ("rbg_avos_matmul", _I32, [_I32, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
                                ctypes.POINTER(_U32), _P]),

@@ -343,6 +343,44 @@ fw_convert_kernel(const T *__restrict__ in_base, U *__restrict__ work_base,
 // ------------------------------------------------------------------------------------------
 // kernel B: phase 3 over BM x BN tiles, register micro-tiles TM x TN, 256 threads
 // ------------------------------------------------------------------------------------------
+// ---- bulk asynchronous copies global -> shared (the TMA unit), completing on an mbarrier
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// every wait is bounded: false when the phase did not complete within the tries
+constexpr int MBAR_TRIES = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < MBAR_TRIES; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// orders this thread's earlier generic accesses to shared memory before later async-proxy ones
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// `bytes` (a multiple of 16) from global `src` to shared `dst` (both 16-byte aligned)
+__device__ __forceinline__ void bulk_to_smem(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
 template <typename U, int BN> struct TileSmem {
     U CPt[FW_B][FW_P];       // CPt[q][i] = d_{t-1}(i, t) for the q-th active step t
     U RPm[FW_B][BN];         // 2^msb(d_{t-1}(t, j)) (0 for zero), q-th active step
@@ -362,12 +400,14 @@ template <typename U, int BN> struct TileSmem {
 // A line mask is meaningful only when its group mask is nonzero (groups with no nonzero line
 // skip the panel pass and leave their line masks and snapshots from an earlier round), and a
 // group's snapshot row t is written only when bit t of its group mask is set.
+// Returns false when the snapshot copies did not complete within the bounded wait (the item's
+// component is then marked RBG_EV_TIMEOUT and the CTA stops taking items).
 template <typename U, int BN, int TM, int TN>
-__device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t local, U *__restrict__ work_base,
+__device__ __forceinline__ bool tile_item(TileSmem<U, BN> &S, int ci, int64_t local, U *__restrict__ work_base,
                                           const unsigned long long *__restrict__ mask_base,
                                           unsigned char *__restrict__ occ_base,
                                           const FwComp *__restrict__ comps, int64_t K0, int lbits,
-                                          DevStatus *st_base) {
+                                          DevStatus *st_base, uint32_t bar, uint32_t &parity) {
     typedef lane<U> L;
     constexpr int BM = FW_P;
     constexpr int TX = BN / TN;           // threads along columns
@@ -418,7 +458,7 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
     }
     __syncthreads();
     const unsigned long long act = S.colAny & S.rowAny;
-    if (act == 0) return;   // uniform across the block
+    if (act == 0) return true;   // uniform across the block
     const int na = __popcll(act);
     if (tid < FW_B) {
         const bool on = (act >> tid) & 1ull;
@@ -457,31 +497,62 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         }
     }
 
-    // ---- stage the active steps' panel snapshots (dead 64-line groups read as zero)
+    // ---- stage the active steps' panel snapshots: every live 64-line piece (the column panel's
+    // two row halves, the row panel's BN / 64 column groups of step t) is one bulk asynchronous
+    // copy into the shared tables, issued by the first warp and completing on the CTA's mbarrier
+    // while the accumulator loads above are in flight; a dead piece (a group without a snapshot
+    // at step t) reads as the encoded zero.  The panel kernel stores snapshots already encoded
+    // (an invalid operand as the encoded zero), so the rows are copied as they are; the row
+    // panel's rows are split into (2^msb, low) pairs in shared memory afterwards.
     {
-        const uint4 inf4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        constexpr int PC = BM / FW_B, PR = BN / FW_B, PP = PC + PR;   // pieces per active step
+        constexpr uint32_t PIECE = FW_B * sizeof(U);                   // bytes per piece
+        static_assert(PC == 2, "a tile is two 64-row groups high");
         const unsigned long long cg0 = gmC[I0 / FW_B], cg1 = gmC[I0 / FW_B + 1];
-        constexpr int VC = BM / PER, VR = BN / PER;      // vectors per staged row
-        for (int e = tid; e < na * VC; e += FW_THREADS) {
-            const int q = e / VC, r = (e % VC) * PER, t = S.active[q];
-            const bool live = (((r < FW_B) ? cg0 : cg1) >> t) & 1ull;
-            const uint4 v = live ? *reinterpret_cast<const uint4 *>(cpbuf + (int64_t)t * np + I0 + r) : inf4;
-            const U *w = reinterpret_cast<const U *>(&v);
-#pragma unroll
-            for (int k = 0; k < PER; ++k) S.CPt[q][r + k] = L::valid(w[k]) ? w[k] : L::inf;
-        }
-        for (int e = tid; e < na * VR; e += FW_THREADS) {
-            const int q = e / VR, c = (e % VR) * PER, t = S.active[q];
-            const bool live = (gmR[(J0 + c) / FW_B] >> t) & 1ull;
-            const uint4 v = live ? *reinterpret_cast<const uint4 *>(rpbuf + (int64_t)t * np + J0 + c) : inf4;
-            const U *w = reinterpret_cast<const U *>(&v);
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                U m, low;
-                L::split(w[k], m, low);
-                S.RPm[q][c + k] = m;
-                S.RPl[q][c + k] = low;
+        auto live = [&](int p, int t) -> bool {
+            const unsigned long long g = p == 0 ? cg0 : p == 1 ? cg1 : gmR[J0 / FW_B + (p - PC)];
+            return (g >> t) & 1ull;
+        };
+        if (tid < 32) {
+            fence_proxy_async_smem();          // the previous item's reads of the tables come first
+            uint32_t bytes = 0;
+            for (int e = tid; e < na * PP; e += 32) {
+                const int q = e / PP, p = e % PP, t = S.active[q];
+                if (!live(p, t)) continue;
+                const U *src = p < PC ? cpbuf + (int64_t)t * np + I0 + p * FW_B
+                                      : rpbuf + (int64_t)t * np + J0 + (p - PC) * FW_B;
+                U *dst = p < PC ? &S.CPt[q][p * FW_B] : &S.RPm[q][(p - PC) * FW_B];
+                bulk_to_smem(smem_u32(dst), src, PIECE, bar);
+                bytes += PIECE;
             }
+            bytes = __reduce_add_sync(0xffffffffu, bytes);
+            if (tid == 0) mbar_arrive_expect_tx(bar, bytes);
+        }
+        const uint4 inf4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        constexpr int VP = FW_B / PER;                                 // 16-byte vectors per piece
+        for (int e = tid; e < na * PP * VP; e += FW_THREADS) {
+            const int piece = e / VP, v = e % VP, q = piece / PP, p = piece % PP;
+            if (live(p, S.active[q])) continue;
+            U *dst = p < PC ? &S.CPt[q][p * FW_B + v * PER] : &S.RPm[q][(p - PC) * FW_B + v * PER];
+            *reinterpret_cast<uint4 *>(dst) = inf4;
+        }
+        const bool landed = mbar_wait(bar, parity);
+        if (__syncthreads_or(!landed)) {
+            // give copies still in flight a bounded time to land before the CTA leaves
+            mbar_wait(bar, parity);
+            if (tid == 0) atomicOr(&st->flags, RBG_EV_TIMEOUT);
+            return false;
+        }
+        parity ^= 1u;
+        for (int e = tid; e < na * (BN / PER); e += FW_THREADS) {
+            const int q = e / (BN / PER), c = (e % (BN / PER)) * PER;
+            const uint4 v = *reinterpret_cast<const uint4 *>(&S.RPm[q][c]);
+            const U *w = reinterpret_cast<const U *>(&v);
+            U m[PER], low[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) L::split(w[k], m[k], low[k]);
+            *reinterpret_cast<uint4 *>(&S.RPm[q][c]) = *reinterpret_cast<const uint4 *>(m);
+            *reinterpret_cast<uint4 *>(&S.RPl[q][c]) = *reinterpret_cast<const uint4 *>(low);
         }
     }
     __syncthreads();
@@ -564,6 +635,7 @@ __device__ __forceinline__ void tile_item(TileSmem<U, BN> &S, int ci, int64_t lo
         }
     }
     flush_status(st, mx, flags);
+    return true;
 }
 
 // Tile worklist: candidate tile (I, J) of this round is an item when some step t has a nonzero
@@ -601,8 +673,14 @@ fw_tile_kernel(U *__restrict__ work_base, const unsigned long long *__restrict__
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem<U, BN> &S = *reinterpret_cast<TileSmem<U, BN> *>(smem_raw);
     __shared__ int s_item;
+    __shared__ __align__(8) unsigned long long s_bar;   // completion of the snapshot copies
+    const uint32_t bar = smem_u32(&s_bar);
+    uint32_t parity = 0;
     const int total = counters[CNT_TILE];
-    if (threadIdx.x == 0) s_item = atomicAdd(&counters[CUR_TILE], 1);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        s_item = atomicAdd(&counters[CUR_TILE], 1);
+    }
     __syncthreads();
     int i = s_item;
     while (i < total) {
@@ -612,7 +690,13 @@ fw_tile_kernel(U *__restrict__ work_base, const unsigned long long *__restrict__
         int nxt = 0;
         if (threadIdx.x == 0) nxt = atomicAdd(&counters[CUR_TILE], 1);
         const int2 e = list[i];
-        tile_item<U, BN, TM, TN>(S, e.x, e.y, work_base, any_base, occ_base, comps, K0, lbits, st_base);
+        const bool ok = tile_item<U, BN, TM, TN>(S, e.x, e.y, work_base, any_base, occ_base, comps, K0, lbits,
+                                                 st_base, bar, parity);
+        if (!ok) {   // uniform: the CTA stops; the item it had claimed next is marked as well
+            if (threadIdx.x == 0 && nxt < total)
+                atomicOr(&st_base[comps[list[nxt].x].status_index].flags, RBG_EV_TIMEOUT);
+            return;
+        }
         if (threadIdx.x == 0) s_item = nxt;
         __syncthreads();
         i = s_item;
@@ -631,8 +715,9 @@ fw_finalize_kernel(const T *__restrict__ in_base, const U *__restrict__ work_bas
                    const unsigned char *__restrict__ occ_base, RowStats rs) {
     const int ci = fw_find(prefix, count, blockIdx.x);
     const FwComp c = comps[ci];
-    // a component that needs another path keeps its input untouched (it may be in place)
-    if (st_base[c.status_index].flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE | RBG_EV_RISK | RBG_EV_CYCLE))
+    // a component that needs another path keeps its input untouched (it may be in place), and
+    // so does one whose closure stopped at a bounded wait
+    if (st_base[c.status_index].flags & (RBG_EV_UNCLEAN | RBG_EV_WIDE | RBG_EV_RISK | RBG_EV_CYCLE | RBG_EV_TIMEOUT))
         return;
     const T *in = in_base + c.in_off;
     const U *work = work_base + c.work_off;
@@ -1170,7 +1255,7 @@ static int exact_dense(int64_t n, const T *in, int64_t ld_in, T *out, int64_t ld
 
 static void result_from_blocked(const DevStatus &h, int path, rbg_result_t *res) {
     res->executed = (int64_t)h.executed;
-    res->status = RBG_OK;
+    res->status = (h.flags & RBG_EV_TIMEOUT) ? RBG_ERR_TIMEOUT : RBG_OK;
     res->flags = h.flags;
     res->diameter = h.mx ? msb_u64(h.mx) : 0;
     res->path = path;

@@ -370,12 +370,17 @@ __device__ __forceinline__ void panel_item(PanelSmem<U> &S, int ci, int local, U
     const unsigned long long anyMask = S.any;
     {
         // t-major, coalesced over the CTA's lines; only the steps some line of this group has
-        // valid are written (the tile kernel reads a snapshot row only under its mask bit)
+        // valid are written (the tile kernel reads a snapshot row only under its mask bit), and
+        // an invalid operand is written as the encoded zero, so that the tile kernel can copy the
+        // rows into shared memory as they are
         U *dst = rowPanel ? rpbuf : cpbuf;
         const int64_t base = (int64_t)cta * PN_LINES;
         for (int e = tid; e < FW_B * PN_LINES; e += PN_THREADS) {
             const int t = e / PN_LINES;
-            if ((anyMask >> t) & 1ull) dst[(int64_t)t * np + base + e % PN_LINES] = S.Z[t][e % PN_LINES];
+            if ((anyMask >> t) & 1ull) {
+                const U z = S.Z[t][e % PN_LINES];
+                dst[(int64_t)t * np + base + e % PN_LINES] = L::valid(z) ? z : L::inf;
+            }
         }
     }
     // write back the cells that changed; the running maximum needs each newly valid cell's

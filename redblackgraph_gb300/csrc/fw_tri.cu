@@ -398,7 +398,7 @@ __global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
                                     const int32_t *__restrict__ row_len, const int32_t *__restrict__ p_col,
                                     const int64_t *__restrict__ cptr, const int32_t *__restrict__ csc_row,
                                     const int32_t *__restrict__ csc_pos, const int64_t *__restrict__ tpos,
-                                    const DagCounters *dc, const unsigned *any_gen, int3 *__restrict__ trip,
+                                    const DagCounters *dc, const unsigned *any_gen, int4 *__restrict__ trip,
                                     int64_t cap, unsigned *gflags) {
     if (!tri_dag_ok(dc) || !*any_gen || *gflags) return;
     const int lane = threadIdx.x & 31;
@@ -422,7 +422,7 @@ __global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
                 atomicOr(gflags, 2u);
                 continue;
             }
-            trip[base + t] = make_int3(csc_pos[c0 + a], qb, (int32_t)qc);
+            trip[base + t] = make_int4(csc_pos[c0 + a], qb, (int32_t)qc, (int32_t)k);
         }
     }
 }
@@ -460,12 +460,14 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
     }
 }
 
-// One warp per general matrix: its steps in order (32 step bounds read at a time, the non-empty
-// ones taken by ballot), each step's triples in parallel; the warp barrier between steps orders
-// one step's stores before the next step's loads.
+// One warp per general matrix: its triples (ordered by step) streamed in chunks of 32, each
+// chunk loaded four chunks ahead so that no step waits for its triples; within a chunk the
+// lanes take the chunk's steps in order (a warp barrier after each), so one step's stores come
+// before the next step's loads.
+constexpr int TRI_PREFETCH = 4;
 __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_t *__restrict__ ckind,
                                       const unsigned *__restrict__ cbad, const int64_t *__restrict__ tpos,
-                                      const int3 *__restrict__ trip, const DagCounters *dc, const unsigned *any_gen,
+                                      const int4 *__restrict__ trip, const DagCounters *dc, const unsigned *any_gen,
                                       const unsigned *gflags, int32_t *cur, int64_t pool, int *__restrict__ cam,
                                       int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
     if (!tri_dag_ok(dc) || !*any_gen) return;
@@ -473,38 +475,47 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int ci = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ci < count; ci += warps) {
         if (!tri_gen_row(ci, ckind, cbad, dc, gflags)) continue;   // warp-uniform
-        const int n = (int)comps[ci].n;
         const int64_t base = comps[ci].row_base;
+        const int64_t T0 = tpos[base], T1 = tpos[base + comps[ci].n];
+        auto fetch = [&](int64_t c) -> int4 {
+            const int64_t t = T0 + c * 32 + lane;
+            return t < T1 ? trip[t] : make_int4(0, 0, 0, INT_MAX);
+        };
+        int4 q[TRI_PREFETCH];
+#pragma unroll
+        for (int d = 0; d < TRI_PREFETCH; ++d) q[d] = fetch(d);
         int top = -1, first = -1;
         unsigned long long prods = 0;
-        for (int k0 = 0; k0 < n; k0 += 32) {
-            const int k = k0 + lane;
-            const int64_t t0 = k < n ? tpos[base + k] : 0, t1 = k < n ? tpos[base + k + 1] : 0;
-            unsigned bal = __ballot_sync(0xffffffffu, t1 > t0);
-            while (bal) {
-                const int b = __ffs(bal) - 1;
-                bal &= bal - 1;
-                const int64_t s0 = __shfl_sync(0xffffffffu, t0, b), s1 = __shfl_sync(0xffffffffu, t1, b);
-                for (int64_t t = s0 + lane; t < s1; t += 32) {
-                    const int3 tr = trip[t];
+        const int64_t chunks = (T1 - T0 + 31) / 32;
+        for (int64_t c = 0; c < chunks; ++c) {
+            const int4 tr = q[0];
+#pragma unroll
+            for (int d = 0; d + 1 < TRI_PREFETCH; ++d) q[d] = q[d + 1];
+            q[TRI_PREFETCH - 1] = fetch(c + TRI_PREFETCH);
+            bool todo = tr.w != INT_MAX;
+            while (true) {
+                const int k = __reduce_min_sync(0xffffffffu, todo ? tr.w : INT_MAX);   // warp-uniform
+                if (k == INT_MAX) break;
+                if (todo && tr.w == k) {
+                    todo = false;
                     if ((unsigned)tr.x >= (unsigned)pool || (unsigned)tr.y >= (unsigned)pool ||
                         (unsigned)tr.z >= (unsigned)pool) {
                         atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
-                        continue;
-                    }
-                    const int32_t x = cur[tr.x], y = cur[tr.y];
-                    if (x != 0 && y != 0) {
-                        const int mx = msb_u32((uint32_t)x), my = msb_u32((uint32_t)y);
-                        const int pm = mx + my;
-                        top = max(top, pm);
-                        ++prods;
-                        const int32_t pv = (int32_t)(((uint32_t)x << my) | ((uint32_t)y ^ (1u << my)));
-                        const int32_t old = cur[tr.z];
-                        if (old == 0) {
-                            first = max(first, pm);
-                            cur[tr.z] = pv;
-                        } else if (pv < old) {
-                            cur[tr.z] = pv;
+                    } else {
+                        // the three cells are read together: one round trip per step
+                        const int32_t x = cur[tr.x], y = cur[tr.y], old = cur[tr.z];
+                        if (x != 0 && y != 0) {
+                            const int mx = msb_u32((uint32_t)x), my = msb_u32((uint32_t)y);
+                            const int pm = mx + my;
+                            top = max(top, pm);
+                            ++prods;
+                            const int32_t pv = (int32_t)(((uint32_t)x << my) | ((uint32_t)y ^ (1u << my)));
+                            if (old == 0) {
+                                first = max(first, pm);
+                                cur[tr.z] = pv;
+                            } else if (pv < old) {
+                                cur[tr.z] = pv;
+                            }
                         }
                     }
                 }
@@ -703,7 +714,7 @@ struct TriLayout {
     unsigned *cflags, *cbad, *gflags;        // gflags[0]: the general path's scratch overflowed; [1]: any general
     int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val, *row_len, *p_col, *p_val;
     int32_t *ccur, *csc_row, *csc_pos, *cur;
-    int3 *trip;
+    int4 *trip;                              // (pool positions of (i, k), (k, j), (i, j); step k)
     int *cam, *cfm;
     unsigned long long *cprod;
     TriOut *res;
@@ -749,7 +760,7 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     const size_t rest = ws_bytes > L.fixed + 2048 ? ws_bytes - L.fixed - 2048 : 0;
     L.pool = std::min<int64_t>((int64_t)(rest / 10 * 4 / 12 / 64 * 64), (int64_t)INT32_MAX / 64 * 64);
     L.csc_cap = (int64_t)(rest / 100 * 15 / 8);
-    L.trip_cap = (int64_t)(rest / 100 * 45 / 12);
+    L.trip_cap = (int64_t)(rest / 100 * 45 / 16);
     Carve tail{base};
     tail.off = L.fixed;
     L.p_col = tail.take<int32_t>((size_t)L.pool);
@@ -757,7 +768,7 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     L.cur = tail.take<int32_t>((size_t)L.pool);
     L.csc_row = tail.take<int32_t>((size_t)L.csc_cap);
     L.csc_pos = tail.take<int32_t>((size_t)L.csc_cap);
-    L.trip = tail.take<int3>((size_t)L.trip_cap);
+    L.trip = tail.take<int4>((size_t)L.trip_cap);
 }
 
 struct TriShape {

@@ -1063,6 +1063,230 @@ extern "C" int32_t rbg_csr_merge_fill(const rbg_csr_t *X, const rbg_csr_t *Y, co
 }
 
 // ------------------------------------------------------------------------------------------
+// Entries that changed between two squarings (the semi-naive squaring's difference)
+// ------------------------------------------------------------------------------------------
+// Z = the entries of X whose column is absent from the same row of Y or holds another value
+// there (values compared as integers, whatever the two storage types).  One warp per row: each
+// lane looks its entry's column up in Y's row by binary search, a ballot packs the kept entries
+// in column order.
+namespace rbg {
+
+__device__ __forceinline__ long long df_load(const void *v, int64_t e, int bytes, bool uns) {
+    if (bytes == 8) return reinterpret_cast<const long long *>(v)[e];
+    if (bytes == 4) return uns ? (long long)reinterpret_cast<const unsigned *>(v)[e]
+                               : (long long)reinterpret_cast<const int *>(v)[e];
+    if (bytes == 2) return uns ? (long long)reinterpret_cast<const unsigned short *>(v)[e]
+                               : (long long)reinterpret_cast<const short *>(v)[e];
+    return uns ? (long long)reinterpret_cast<const unsigned char *>(v)[e]
+               : (long long)reinterpret_cast<const signed char *>(v)[e];
+}
+
+template <bool FILL>
+__global__ void df_kernel(int64_t n, const int64_t *xp, const int *xj, const void *xv, int xb, bool xu,
+                          const int64_t *yp, const int *yj, const void *yv, int yb, bool yu, int64_t *cnt,
+                          const int64_t *zp, int *zj, void *zv) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+        const int64_t x0 = xp[i], x1 = xp[i + 1], y0 = yp[i];
+        const int ylen = (int)(yp[i + 1] - y0);
+        int64_t out = FILL ? zp[i] : 0;
+        for (int64_t e0 = x0; e0 < x1; e0 += 32) {
+            const int64_t e = e0 + lane;
+            bool keep = false;
+            int col = 0;
+            if (e < x1) {
+                col = xj[e];
+                // when Y's row is a subset of X's (a squaring step only adds entries), entry q of
+                // X sits at a position of Y in [q - (|X| - |Y|), q]: look there first, then in the
+                // rest of the row
+                const int q = (int)(e - x0), extra = (int)(x1 - x0) - ylen;
+                auto find = [&](int lo, int hi) -> int {
+                    while (lo <= hi) {
+                        const int mid = (lo + hi) >> 1;
+                        const int c = yj[y0 + mid];
+                        if (c == col) return mid;
+                        if (c < col) lo = mid + 1;
+                        else hi = mid - 1;
+                    }
+                    return -1;
+                };
+                const int nlo = max(0, q - max(extra, 0)), nhi = min(q, ylen - 1);
+                int f = find(nlo, nhi);
+                if (f < 0) {
+                    f = find(0, nlo - 1);
+                    if (f < 0) f = find(nhi + 1, ylen - 1);
+                }
+                keep = f < 0 || df_load(yv, y0 + f, yb, yu) != df_load(xv, e, xb, xu);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (FILL && keep) {
+                const int64_t q = out + __popc(bal & ((1u << lane) - 1u));
+                zj[q] = col;
+                if (xb == 8) {
+                    reinterpret_cast<long long *>(zv)[q] = reinterpret_cast<const long long *>(xv)[e];
+                } else if (xb == 4) {
+                    reinterpret_cast<int *>(zv)[q] = reinterpret_cast<const int *>(xv)[e];
+                } else {
+                    unsigned char *d = reinterpret_cast<unsigned char *>(zv) + q * xb;
+                    const unsigned char *s = reinterpret_cast<const unsigned char *>(xv) + e * xb;
+                    for (int b = 0; b < xb; ++b) d[b] = s[b];
+                }
+            }
+            out += __popc(bal);
+        }
+        if (!FILL && lane == 0) cnt[i] = out;
+    }
+}
+
+bool df_dtype(int32_t dtype, int &bytes, bool &uns) {
+    bytes = dtype_bytes(dtype);
+    uns = dtype == RBG_DTYPE_UINT8 || dtype == RBG_DTYPE_UINT16 || dtype == RBG_DTYPE_UINT32 ||
+          dtype == RBG_DTYPE_UINT64;
+    return bytes > 0;
+}
+
+}  // namespace rbg
+
+extern "C" int32_t rbg_csr_diff_count(int32_t x_dtype, const rbg_csr_t *X, int32_t y_dtype, const rbg_csr_t *Y,
+                                      void *head, int64_t head_bytes, int64_t *nnz, rbg_stream_t stream) {
+    int xb, yb;
+    bool xu, yu;
+    if (!csr_ok(X) || !csr_ok(Y) || !head || !nnz || X->n_rows != Y->n_rows || X->n_cols != Y->n_cols ||
+        !df_dtype(x_dtype, xb, xu) || !df_dtype(y_dtype, yb, yu))
+        return RBG_ERR_INVALID;
+    const int64_t n = X->n_rows;
+    if (head_bytes < (int64_t)head_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
+    Head h;
+    head_layout(n, reinterpret_cast<unsigned char *>(head), &h);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    RBG_CUDA_TRY(cudaMemsetAsync(h.cand_off + n, 0, 8, s));
+    if (n > 0) {
+        note_launches(1);
+        df_kernel<false><<<grid_of(n * 32, 256), 256, 0, s>>>(n, X->indptr, X->indices, X->data, xb, xu, Y->indptr,
+                                                              Y->indices, Y->data, yb, yu, h.cand_off, nullptr,
+                                                              nullptr, nullptr);
+    }
+    RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(h.scan_tmp, h.scan_bytes, h.cand_off, h.cand_off, (int)(n + 1), s));
+    int64_t tot = 0;
+    {
+        HostStaging hs(s, 64);
+        int rc = hs.down(&tot, h.cand_off + n, 8);
+        if (!rc) rc = hs.finish();
+        if (rc) return rc;
+    }
+    *nnz = tot;
+    return RBG_OK;
+}
+
+extern "C" int32_t rbg_csr_diff_fill(int32_t x_dtype, const rbg_csr_t *X, int32_t y_dtype, const rbg_csr_t *Y,
+                                     const void *head, int64_t *indptr, int32_t *indices, void *data,
+                                     rbg_stream_t stream) {
+    int xb, yb;
+    bool xu, yu;
+    if (!csr_ok(X) || !csr_ok(Y) || !head || !indptr || X->n_rows != Y->n_rows || !df_dtype(x_dtype, xb, xu) ||
+        !df_dtype(y_dtype, yb, yu))
+        return RBG_ERR_INVALID;
+    const int64_t n = X->n_rows;
+    Head h;
+    head_layout(n, const_cast<unsigned char *>(reinterpret_cast<const unsigned char *>(head)), &h);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    RBG_CUDA_TRY(cudaMemcpyAsync(indptr, h.cand_off, (size_t)(n + 1) * 8, cudaMemcpyDeviceToDevice, s));
+    if (n > 0) {
+        note_launches(1);
+        df_kernel<true><<<grid_of(n * 32, 256), 256, 0, s>>>(n, X->indptr, X->indices, X->data, xb, xu, Y->indptr,
+                                                             Y->indices, Y->data, yb, yu, nullptr, h.cand_off,
+                                                             indices, data);
+    }
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Operands of the semi-naive squaring step: A' = [D R] (n x 2n), B' = [R ; D] (2n x n), so that
+// A' B' = D R (+) R D and one product with the merge of R forms R (+) D R (+) R D in one pass
+// ------------------------------------------------------------------------------------------
+namespace rbg {
+
+// One warp per row: row i of A' is D's row, then R's row with its columns moved by n (so it
+// stays sorted); A' row pointers are the sums of D's and R's.  The first n + 1 threads also
+// write B''s row pointers (R's, then D's moved by nnz(R)).
+__global__ void sn_operands_kernel(int64_t n, int eb, const int64_t *dp, const int *dj, const void *dv,
+                                   const int64_t *rp, const int *rj, const void *rv, int64_t *ap, int *aj,
+                                   void *av, int64_t *bp) {
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    const int64_t rnnz = rp[n];
+    for (int64_t i = gt; i <= 2 * n; i += nthreads) {
+        if (i <= n) {
+            ap[i] = dp[i] + rp[i];
+            bp[i] = rp[i];
+        } else {
+            bp[i] = rnnz + dp[i - n];
+        }
+    }
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = nthreads >> 5;
+    auto copy = [&](void *dst, int64_t q, const void *src, int64_t e) {
+        if (eb == 8) reinterpret_cast<long long *>(dst)[q] = reinterpret_cast<const long long *>(src)[e];
+        else reinterpret_cast<int *>(dst)[q] = reinterpret_cast<const int *>(src)[e];
+    };
+    for (int64_t i = gt >> 5; i < n; i += warps) {
+        const int64_t d0 = dp[i], d1 = dp[i + 1], r0 = rp[i], r1 = rp[i + 1];
+        const int64_t o = d0 + r0;
+        for (int64_t e = d0 + lane; e < d1; e += 32) {
+            aj[o + (e - d0)] = dj[e];
+            copy(av, o + (e - d0), dv, e);
+        }
+        const int64_t o2 = o + (d1 - d0);
+        for (int64_t e = r0 + lane; e < r1; e += 32) {
+            aj[o2 + (e - r0)] = rj[e] + (int)n;
+            copy(av, o2 + (e - r0), rv, e);
+        }
+    }
+}
+
+}  // namespace rbg
+
+extern "C" int32_t rbg_spgemm_seminaive_operands(int32_t dtype, const rbg_csr_t *D, const rbg_csr_t *R,
+                                                 int64_t *a_indptr, int32_t *a_indices, void *a_data,
+                                                 int64_t *b_indptr, int32_t *b_indices, void *b_data,
+                                                 rbg_stream_t stream) {
+    const int eb = dtype_bytes(dtype);
+    if (!csr_ok(D) || !csr_ok(R) || D->n_rows != R->n_rows || D->n_cols != R->n_cols || R->n_rows != R->n_cols ||
+        (eb != 4 && eb != 8) || !a_indptr || !b_indptr || R->n_rows >= (1ll << 29))
+        return RBG_ERR_INVALID;
+    const int64_t n = R->n_rows;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int64_t nnz[2] = {0, 0};
+    {
+        HostStaging hs(s, 64);
+        int rc = hs.down(&nnz[0], D->indptr + n, 8);
+        if (!rc) rc = hs.down(&nnz[1], R->indptr + n, 8);
+        if (!rc) rc = hs.finish();
+        if (rc) return rc;
+    }
+    const int64_t dn = nnz[0], rn = nnz[1];
+    if ((dn + rn > 0) && (!a_indices || !a_data || !b_indices || !b_data)) return RBG_ERR_INVALID;
+    // B' = [R ; D]: the entries of R, then those of D
+    if (rn > 0) {
+        RBG_CUDA_TRY(cudaMemcpyAsync(b_indices, R->indices, (size_t)rn * 4, cudaMemcpyDeviceToDevice, s));
+        RBG_CUDA_TRY(cudaMemcpyAsync(b_data, R->data, (size_t)rn * eb, cudaMemcpyDeviceToDevice, s));
+    }
+    if (dn > 0) {
+        RBG_CUDA_TRY(cudaMemcpyAsync(b_indices + rn, D->indices, (size_t)dn * 4, cudaMemcpyDeviceToDevice, s));
+        RBG_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<unsigned char *>(b_data) + (size_t)rn * eb, D->data,
+                                     (size_t)dn * eb, cudaMemcpyDeviceToDevice, s));
+    }
+    note_launches(1);
+    sn_operands_kernel<<<grid_of(std::max<int64_t>(n, 1) * 32, 256), 256, 0, s>>>(
+        n, eb, D->indptr, D->indices, D->data, R->indptr, R->indices, R->data, a_indptr, a_indices, a_data,
+        b_indptr);
+    RBG_CUDA_TRY(cudaGetLastError());
+    return RBG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
 // Largest candidate of the DAG closure (the value its diameter is taken from)
 // ------------------------------------------------------------------------------------------
 // The reference's sparse DAG closure (redblackgraph/sparse/csgraph/_transitive_closure_dag.pyx:

@@ -24,16 +24,11 @@ def transitive_closure_gpu(A: CSRMatrixGPU, max_iterations: int = 64) -> Tuple[C
     stable; diameter = max(changing iterations, floor(log2(max |value| > 1)))."""
     if A.nnz == 0:
         return A.copy(), 0
-    R = A
-    diameter = 0
-    for iteration in range(max_iterations):
-        Rn, _, _ = _sp.spgemm(R.device_csr(), R.device_csr(), R=R.device_csr(), upper=R.triangular,
-                              sem=_sp.SEM_CY32)
-        Rn = CSRMatrixGPU.from_device_csr(Rn, triangular=R.triangular)
-        if Rn.device_csr().equal(R.device_csr()):
-            break
-        R = Rn
-        diameter = iteration + 1
+    # the squaring loop in its semi-naive form (same R after every step); the GPU module's
+    # products wrap silently, so no step status is raised
+    Rd, diameter = _sp.squaring_closure(A.device_csr(), max_iterations, _sp.SEM_CY32, upper=A.triangular,
+                                        on_step=lambda rc, flags: None)
+    R = CSRMatrixGPU.from_device_csr(Rd, triangular=A.triangular)
     mv = _max_non_identity(R)
     if mv > 1:
         diameter = max(diameter, int(np.floor(np.log2(mv))))

@@ -47,7 +47,7 @@ def _as_csr(A):
 def _squaring(csr, max_iterations, cycle_error, dag_candidates=False):
     """R <- R (+) R^2 on the GPU until R is stable; returns (rb_matrix int32, max |value|)."""
     import torch
-    from ...spgemm import DeviceCSR, spgemm, SEM_C64
+    from ...spgemm import DeviceCSR, squaring_closure, SEM_C64
     from ... import _lib
     from ..rbm import rb_matrix
     a = csr.copy()
@@ -57,18 +57,15 @@ def _squaring(csr, max_iterations, cycle_error, dag_candidates=False):
         a = a.astype(np.int64)
     if a.dtype.itemsize < 4:
         a = a.astype(np.int32 if a.dtype.kind == "i" else np.uint32)
-    R = DeviceCSR.from_scipy(a)
-    for _ in range(max_iterations):
-        Rn, rc, flags = spgemm(R, R, R=R, sem=SEM_C64)
+
+    def on_step(rc, flags):
         if cycle_error and (flags & _lib.EV_CYCLE):
             from .cycleerror import CycleError
             raise CycleError("Graph contains a cycle", vertex=-1)
         if rc == _lib.RBG_ERR_OVERFLOW:
             raise OverflowError("Avos product results in an overflow.")
-        if Rn.equal(R):
-            R = Rn
-            break
-        R = Rn
+
+    R, _ = squaring_closure(DeviceCSR.from_scipy(a), max_iterations, SEM_C64, on_step=on_step)
     if R.data.dtype != torch.int32:
         R = DeviceCSR(R.indptr, R.indices, R.data.to(torch.int32), R.shape)
     mx_abs = int(R.data.abs().max().item()) if R.nnz else 0

@@ -120,21 +120,100 @@ def spgemm(A: DeviceCSR, B: DeviceCSR, R: DeviceCSR | None = None, upper: bool =
     return DeviceCSR(indptr, indices, data, (n, nc)), rc, flags.value
 
 
-def squaring_closure(A: DeviceCSR, max_iterations: int = 64, sem: int = SEM_C64,
-                     upper: bool = False) -> tuple[DeviceCSR, int]:
-    """R <- R (+) R^2 until R stops changing (at most ``max_iterations`` products).
+def csr_diff(X: DeviceCSR, Y: DeviceCSR, stream=None) -> DeviceCSR:
+    """The entries of X that Y does not hold with the same value (rbg_csr_diff_count / _fill),
+    in X's storage type."""
+    if X.shape != Y.shape:
+        raise ValueError(f"Shape mismatch: {X.shape} vs {Y.shape}")
+    dev = X.indptr.device
+    L = _lib.load()
+    cx, cy = X.cstruct(), Y.cstruct()
+    xd = _lib.dtype_code(numpy_dtype(X.data.dtype))
+    yd = _lib.dtype_code(numpy_dtype(Y.data.dtype))
+    hb = ctypes.c_int64(0)
+    _lib.check(L.rbg_spgemm_head_bytes(X.shape[0], ctypes.byref(hb)), "diff")
+    head = torch.empty(max(hb.value, 256), dtype=torch.uint8, device=dev)
+    nnz = ctypes.c_int64(0)
+    sh = stream_handle(stream)
+    _lib.check(L.rbg_csr_diff_count(xd, ctypes.byref(cx), yd, ctypes.byref(cy), head.data_ptr(), head.numel(),
+                                    ctypes.byref(nnz), sh), "diff_count")
+    n = X.shape[0]
+    indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    indices = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)[:nnz.value]
+    data = torch.empty(max(nnz.value, 1), dtype=X.data.dtype, device=dev)[:nnz.value]
+    _lib.check(L.rbg_csr_diff_fill(xd, ctypes.byref(cx), yd, ctypes.byref(cy), head.data_ptr(), indptr.data_ptr(),
+                                   indices.data_ptr() if nnz.value else indptr.data_ptr(),
+                                   data.data_ptr() if nnz.value else indptr.data_ptr(), sh), "diff_fill")
+    return DeviceCSR(indptr, indices, data, X.shape)
 
-    Returns ``(R, iterations that changed R)``.
+
+def seminaive_operands(D: DeviceCSR, R: DeviceCSR, stream=None) -> tuple[DeviceCSR, DeviceCSR]:
+    """A' = [D R] and B' = [R ; D] (rbg_spgemm_seminaive_operands): A' B' = D R (+) R D."""
+    if D.shape != R.shape or R.shape[0] != R.shape[1]:
+        raise ValueError("D and R must be square and of one shape")
+    if D.data.dtype != R.data.dtype:
+        raise ValueError("D and R must hold one value type")
+    n = R.shape[0]
+    dev = R.indptr.device
+    m = D.nnz + R.nnz
+    a_indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    b_indptr = torch.empty(2 * n + 1, dtype=torch.int64, device=dev)
+    a_ind = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
+    b_ind = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
+    a_dat = torch.empty(max(m, 1), dtype=R.data.dtype, device=dev)
+    b_dat = torch.empty(max(m, 1), dtype=R.data.dtype, device=dev)
+    cd, cr = D.cstruct(), R.cstruct()
+    _lib.check(_lib.load().rbg_spgemm_seminaive_operands(
+        _lib.dtype_code(numpy_dtype(R.data.dtype)), ctypes.byref(cd), ctypes.byref(cr), a_indptr.data_ptr(),
+        a_ind.data_ptr(), a_dat.data_ptr(), b_indptr.data_ptr(), b_ind.data_ptr(), b_dat.data_ptr(),
+        stream_handle(stream)), "seminaive_operands")
+    return (DeviceCSR(a_indptr, a_ind[:m], a_dat[:m], (n, 2 * n)),
+            DeviceCSR(b_indptr, b_ind[:m], b_dat[:m], (2 * n, n)))
+
+
+def squaring_closure(A: DeviceCSR, max_iterations: int = 64, sem: int = SEM_C64, upper: bool = False,
+                     on_step=None, stream=None, steps: list | None = None,
+                     seminaive: bool = False) -> tuple[DeviceCSR, int]:
+    """R <- R (+) R^2 until R stops changing (at most ``max_iterations`` steps).
+
+    ``seminaive`` selects the semi-naive form of a step, which gives the same R: with D the
+    entries the previous step changed, a product of two entries outside D was already formed by
+    that step and folded into R, so R (+) R^2 = R (+) D R (+) R D (the (+) is a minimum and (x) is
+    monotone in each operand, hence distributes over it).  A step takes that form when D holds at
+    most half of R's entries, as the one product [D R] [R ; D] merged with R, and D comes from
+    rbg_csr_diff (which also tests convergence).  It forms fewer products, but each step still
+    merges and rewrites all of R and computes D, which on pedigree forests costs more than the
+    products it saves, so the plain loop (convergence by comparing R) is the default.
+    ``on_step(status, flags)`` sees each step's product status and event flags (it may raise);
+    ``steps``, when given, receives per step (form, products, nnz in, nnz out).
+
+    Returns ``(R, steps that changed R)``; R is the last step's output (int32 values).
     """
-    R = A
+    R, D = A, None
     changed = 0
     for _ in range(max_iterations):
-        Rn, rc, _ = spgemm(R, R, R=R, upper=upper, sem=sem)
-        if rc == _lib.RBG_ERR_OVERFLOW:
+        st = {}
+        if not seminaive or D is None or 2 * D.nnz > R.nnz:
+            Rn, rc, fl = spgemm(R, R, R=R, upper=upper, sem=sem, stream=stream, stats=st)
+            prods, form = st["products"], "square"
+        else:
+            A2, B2 = seminaive_operands(D, R, stream=stream)
+            Rn, rc, fl = spgemm(A2, B2, R=R, upper=upper, sem=sem, stream=stream, stats=st)
+            prods, form = st["products"], "semi-naive"
+        if on_step is not None:
+            on_step(rc, fl)
+        elif rc == _lib.RBG_ERR_OVERFLOW:
             raise OverflowError("Avos product results in an overflow.")
-        if Rn.equal(R):
-            break
+        if steps is not None:
+            steps.append((form, prods, R.nnz, Rn.nnz))
+        if seminaive:
+            D = csr_diff(Rn, R, stream=stream)
+            stable = D.nnz == 0
+        else:
+            stable = Rn.equal(R)
         R = Rn
+        if stable:
+            break
         changed += 1
     return R, changed
 

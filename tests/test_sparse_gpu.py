@@ -294,3 +294,77 @@ def test_dag_closure_tiny(native):
         A = sp.csr_matrix(M.astype(np.int32))
         r = transitive_closure_dag_sparse(A)
         assert same(r.W, A) and r.diameter == 0
+
+
+def test_csr_diff_matches_host(native):
+    """rbg_csr_diff: the entries of X absent from Y or holding another value there, for mixed
+    storage types (an int32 squaring output against its int64 input)."""
+    from redblackgraph_gb300.spgemm import DeviceCSR, csr_diff
+    rng = np.random.default_rng(8)
+    for xdt, ydt in ((np.int32, np.int32), (np.int32, np.int64), (np.int64, np.uint32)):
+        Y = sp.random(700, 500, density=0.02, random_state=5, format="csr")
+        Y.data = rng.integers(2, 60, size=Y.nnz).astype(np.float64)
+        X = Y.copy()
+        X.data[rng.random(X.nnz) < 0.1] += 1                      # changed values
+        extra = sp.random(700, 500, density=0.01, random_state=6, format="csr")
+        extra.data = rng.integers(2, 60, size=extra.nnz).astype(np.float64)
+        X = (X + extra.multiply(Y == 0)).tocsr()                  # new entries
+        X = sorted_csr(X.astype(xdt))
+        Y = sorted_csr(Y.astype(ydt))
+        Z = csr_diff(DeviceCSR.from_scipy(X), DeviceCSR.from_scipy(Y)).to_scipy()
+        Xd, Yd = X.toarray().astype(np.int64), Y.toarray().astype(np.int64)
+        exp = sp.csr_matrix(np.where((Xd != 0) & ((Yd == 0) | (Yd != Xd)), Xd, 0))
+        assert Z.dtype == np.dtype(xdt)
+        assert same(Z.astype(np.int64), exp.astype(np.int64))
+
+
+@pytest.mark.parametrize("sem,upper", [(0, False), (1, False), (1, True)])
+def test_semi_naive_squaring_equals_full_squaring(native, sem, upper):
+    """Every step of the semi-naive loop (R (+) D R (+) R D when the last step changed at most
+    half of R) equals the full step R (+) R^2, on a forest numbered oldest first and on the same
+    forest renumbered at random; the number of changing steps is the full loop's."""
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.spgemm import DeviceCSR, spgemm, squaring_closure
+    A = synth.forest(3000, 14, 6, family=60, reach=3, dtype=np.int32)
+    p = np.random.default_rng(4).permutation(A.shape[0])
+    mats = (A.T, sp.triu(sp.csr_matrix(A[p][:, p]))) if upper else (A, sp.csr_matrix(A[p][:, p]))
+    for M in mats:
+        M = sorted_csr(M)
+        R = DeviceCSR.from_scipy(M)
+        full = []
+        for _ in range(64):
+            Rn, _, _ = spgemm(R, R, R=R, upper=upper, sem=sem)
+            full.append(Rn.to_scipy())
+            if Rn.equal(R):
+                break
+            R = Rn
+        forms = []
+        for t in range(1, len(full) + 1):
+            steps = []
+            Rs, changed = squaring_closure(DeviceCSR.from_scipy(M), max_iterations=t, sem=sem, upper=upper,
+                                           on_step=lambda rc, fl: None, steps=steps, seminaive=True)
+            assert same(Rs.to_scipy(), full[t - 1]), t
+            forms = [s[0] for s in steps]
+        assert changed == len(full) - 1
+        assert "semi-naive" in forms                               # the hybrid used both forms
+
+
+def test_seminaive_operands_form_both_products(native):
+    """[D R] [R ; D] equals D R (+) R D (each product on its own, then merged), values and
+    pattern; the operands' shapes are n x 2n and 2n x n."""
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.spgemm import DeviceCSR, merge_minabs, seminaive_operands, spgemm, SEM_CY32
+    A = synth.forest(2000, 12, 9, family=50, reach=3, dtype=np.int32)
+    R = DeviceCSR.from_scipy(A)
+    R1, _, _ = spgemm(R, R, R=R, sem=SEM_CY32)
+    R2, _, _ = spgemm(R1, R1, R=R1, sem=SEM_CY32)
+    from redblackgraph_gb300.spgemm import csr_diff
+    D = csr_diff(R2, R1)
+    assert D.nnz > 0
+    A2, B2 = seminaive_operands(D, R2)
+    assert A2.shape == (2000, 4000) and B2.shape == (4000, 2000) and A2.nnz == B2.nnz == D.nnz + R2.nnz
+    got, _, _ = spgemm(A2, B2, sem=SEM_CY32)
+    P1, _, _ = spgemm(D, R2, sem=SEM_CY32)
+    P2, _, _ = spgemm(R2, D, sem=SEM_CY32)
+    exp = merge_minabs(P1, P2)
+    assert same(got.to_scipy(), exp.to_scipy())
