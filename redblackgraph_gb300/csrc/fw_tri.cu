@@ -376,28 +376,35 @@ __global__ void tri_gen_csc_kernel(int64_t R, const int32_t *__restrict__ row_co
 }
 
 // Triples of step k (batch-global vertex g): column g's entries times row g's entries.
+// Also the pattern length of every general row (lcnt), whose exclusive scan lays each general
+// matrix's current values out contiguously, row after row.
 __global__ void tri_gen_tcount_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                                       const unsigned *__restrict__ cbad, const int32_t *__restrict__ row_len,
                                       const int64_t *__restrict__ cptr, const DagCounters *dc, const unsigned *any_gen,
-                                      const unsigned *gflags, int64_t *__restrict__ tcnt) {
+                                      const unsigned *gflags, int64_t *__restrict__ tcnt, int64_t *__restrict__ lcnt) {
     const bool on = tri_dag_ok(dc) && *any_gen && !*gflags;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g <= R; g += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = 0;
+        int64_t c = 0, l = 0;
         if (on && g < R) {
             const int ci = row_comp[g];
-            if (ckind[ci] == KIND_GENERAL && !cbad[ci]) c = (cptr[g + 1] - cptr[g]) * (int64_t)row_len[g];
+            if (ckind[ci] == KIND_GENERAL && !cbad[ci]) {
+                c = (cptr[g + 1] - cptr[g]) * (int64_t)row_len[g];
+                l = row_len[g];
+            }
         }
         tcnt[g] = c;
+        lcnt[g] = l;
     }
 }
 
-// One warp per vertex k of a general matrix: its step's triples (pool positions of (i, k),
-// (k, j) and (i, j)).
+// One warp per vertex k of a general matrix: its step's triples, as positions of (i, k), (k, j)
+// and (i, j) among the matrix's current values (row g's entry q at lpos[g] - lpos[first row] + q).
 __global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
-                                    const unsigned *__restrict__ cbad, const int64_t *__restrict__ row_off,
-                                    const int32_t *__restrict__ row_len, const int32_t *__restrict__ p_col,
-                                    const int64_t *__restrict__ cptr, const int32_t *__restrict__ csc_row,
-                                    const int32_t *__restrict__ csc_pos, const int64_t *__restrict__ tpos,
+                                    const unsigned *__restrict__ cbad, const TriComp *__restrict__ comps,
+                                    const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
+                                    const int32_t *__restrict__ p_col, const int64_t *__restrict__ cptr,
+                                    const int32_t *__restrict__ csc_row, const int32_t *__restrict__ csc_pos,
+                                    const int64_t *__restrict__ tpos, const int64_t *__restrict__ lpos,
                                     const DagCounters *dc, const unsigned *any_gen, int4 *__restrict__ trip,
                                     int64_t cap, unsigned *gflags) {
     if (!tri_dag_ok(dc) || !*any_gen || *gflags) return;
@@ -406,7 +413,8 @@ __global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
     for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < R; k += warps) {
         const int ci = row_comp[k];
         if (ckind[ci] != KIND_GENERAL || cbad[ci]) continue;   // warp-uniform
-        const int64_t c0 = cptr[k], r0 = row_off[k], base = tpos[k];
+        const int64_t m0 = lpos[comps[ci].row_base];
+        const int64_t c0 = cptr[k], r0 = row_off[k], base = tpos[k], lk = lpos[k] - m0;
         const int cn = (int)(cptr[k + 1] - c0), rn = row_len[k];
         const int64_t total = (int64_t)cn * rn;
         if (base + total > cap) {
@@ -416,34 +424,36 @@ __global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
         for (int64_t t = lane; t < total; t += 32) {
             const int a = (int)(t / rn), b = (int)(t - (int64_t)a * rn);
             const int32_t i = csc_row[c0 + a];
-            const int32_t qb = (int32_t)(r0 + b);
-            const int64_t qc = tri_find_col(p_col, row_off[i], row_len[i], p_col[qb]);
+            const int64_t oi = row_off[i], li = lpos[i] - m0;
+            const int64_t qc = tri_find_col(p_col, oi, row_len[i], p_col[r0 + b]);
             if (qc < 0) {
                 atomicOr(gflags, 2u);
                 continue;
             }
-            trip[base + t] = make_int4(csc_pos[c0 + a], qb, (int32_t)qc, (int32_t)k);
+            trip[base + t] = make_int4((int32_t)(li + (csc_pos[c0 + a] - oi)), (int32_t)(lk + b),
+                                       (int32_t)(li + (qc - oi)), (int32_t)k);
         }
     }
 }
 
-// One warp per row of a general matrix: the current values start as A's entries (zero elsewhere
-// in the pattern); A's largest MSB starts the first-value maximum.
+// One warp per row of a general matrix: the current values (row g's at lpos[g]) start as A's
+// entries, zero elsewhere in the pattern; A's largest MSB starts the first-value maximum.
 __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                                     const unsigned *__restrict__ cbad, const int64_t *__restrict__ indptr,
                                     const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
                                     const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
-                                    const int32_t *__restrict__ p_col, const DagCounters *dc, const unsigned *any_gen,
-                                    unsigned *gflags, int32_t *__restrict__ cur, int *__restrict__ cfm) {
+                                    const int32_t *__restrict__ p_col, const int64_t *__restrict__ lpos,
+                                    const DagCounters *dc, const unsigned *any_gen, unsigned *gflags,
+                                    int32_t *__restrict__ cur, int *__restrict__ cfm) {
     if (!tri_dag_ok(dc) || !*any_gen || *gflags) return;
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < R; g += warps) {
         const int ci = row_comp[g];
         if (ckind[ci] != KIND_GENERAL || cbad[ci]) continue;   // warp-uniform
-        const int64_t o = row_off[g];
+        const int64_t o = row_off[g], l = lpos[g];
         const int len = row_len[g];
-        for (int q = lane; q < len; q += 32) cur[o + q] = 0;
+        for (int q = lane; q < len; q += 32) cur[l + q] = 0;
         __syncwarp();
         int fm = -1;
         for (int64_t e = indptr[g] + lane; e < indptr[g + 1]; e += 32) {
@@ -452,7 +462,7 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
                 atomicOr(gflags, 2u);
                 continue;
             }
-            cur[q] = a_val[e];
+            cur[l + (q - o)] = a_val[e];
             fm = max(fm, dag_row_msb(a_val[e]));
         }
         fm = __reduce_max_sync(0xffffffffu, fm);
@@ -461,22 +471,29 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
 }
 
 // One warp per general matrix: its triples (ordered by step) streamed in chunks of 32, each
-// chunk loaded four chunks ahead so that no step waits for its triples; within a chunk the
-// lanes take the chunk's steps in order (a warp barrier after each), so one step's stores come
-// before the next step's loads.
-constexpr int TRI_PREFETCH = 4;
+// chunk loaded TRI_PREFETCH chunks ahead so that no step waits for its triples; within a chunk
+// the lanes take the chunk's steps in order (a warp barrier after each), so one step's stores
+// come before the next step's loads.  The matrix's P current values lie contiguously at
+// curg + lpos[first row].  Every matrix replays at once: the chain of steps of the largest ones
+// (a dependent round trip to memory per step) sets the kernel's length; holding a matrix's
+// values in shared memory instead (one warp per CTA, up to 216 KB) left one warp per SM for the
+// largest matrices and took longer in all.
+constexpr int TRI_PREFETCH = 8;
 __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_t *__restrict__ ckind,
                                       const unsigned *__restrict__ cbad, const int64_t *__restrict__ tpos,
-                                      const int4 *__restrict__ trip, const DagCounters *dc, const unsigned *any_gen,
-                                      const unsigned *gflags, int32_t *cur, int64_t pool, int *__restrict__ cam,
-                                      int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
+                                      const int64_t *__restrict__ lpos, const int4 *__restrict__ trip,
+                                      const DagCounters *dc, const unsigned *any_gen, const unsigned *gflags,
+                                      int32_t *curg, int *__restrict__ cam, int *__restrict__ cfm,
+                                      unsigned long long *__restrict__ cprod) {
     if (!tri_dag_ok(dc) || !*any_gen) return;
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int ci = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ci < count; ci += warps) {
         if (!tri_gen_row(ci, ckind, cbad, dc, gflags)) continue;   // warp-uniform
-        const int64_t base = comps[ci].row_base;
-        const int64_t T0 = tpos[base], T1 = tpos[base + comps[ci].n];
+        const int64_t base = comps[ci].row_base, rows = comps[ci].n;
+        const int64_t m0 = lpos[base], P = lpos[base + rows] - m0;
+        int32_t *val = curg + m0;
+        const int64_t T0 = tpos[base], T1 = tpos[base + rows];
         auto fetch = [&](int64_t c) -> int4 {
             const int64_t t = T0 + c * 32 + lane;
             return t < T1 ? trip[t] : make_int4(0, 0, 0, INT_MAX);
@@ -498,12 +515,12 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
                 if (k == INT_MAX) break;
                 if (todo && tr.w == k) {
                     todo = false;
-                    if ((unsigned)tr.x >= (unsigned)pool || (unsigned)tr.y >= (unsigned)pool ||
-                        (unsigned)tr.z >= (unsigned)pool) {
+                    if ((uint64_t)(uint32_t)tr.x >= (uint64_t)P || (uint64_t)(uint32_t)tr.y >= (uint64_t)P ||
+                        (uint64_t)(uint32_t)tr.z >= (uint64_t)P) {
                         atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
                     } else {
                         // the three cells are read together: one round trip per step
-                        const int32_t x = cur[tr.x], y = cur[tr.y], old = cur[tr.z];
+                        const int32_t x = val[tr.x], y = val[tr.y], old = val[tr.z];
                         if (x != 0 && y != 0) {
                             const int mx = msb_u32((uint32_t)x), my = msb_u32((uint32_t)y);
                             const int pm = mx + my;
@@ -512,9 +529,9 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
                             const int32_t pv = (int32_t)(((uint32_t)x << my) | ((uint32_t)y ^ (1u << my)));
                             if (old == 0) {
                                 first = max(first, pm);
-                                cur[tr.z] = pv;
+                                val[tr.z] = pv;
                             } else if (pv < old) {
-                                cur[tr.z] = pv;
+                                val[tr.z] = pv;
                             }
                         }
                     }
@@ -532,6 +549,53 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
         }
     }
 }
+
+// Recorded graphs: the IF node around the replay opens only when the closure by levels went
+// through and some matrix needs the replay; the decision is also kept for the launch count.
+__global__ void tri_gen_gate_kernel(const DagCounters *dc, const unsigned *any_gen, unsigned *ran,
+                                    cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0) return;
+    const unsigned go = (tri_dag_ok(dc) && *any_gen) ? 1u : 0u;
+    *ran = go;
+    cudaGraphSetConditional(h, go);
+}
+
+// Inside the capture on `s`: `gate(h)` launches on s the kernel that sets the condition, then an
+// IF node whose body `body(stream)` records from a second stream captured into it.
+template <typename Gate, typename Body>
+int tri_captured_if(cudaStream_t s, Gate gate, Body body) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    RBG_CUDA_TRY(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps));
+    if (st != cudaStreamCaptureStatusActive || !g) return RBG_ERR_INVALID;
+    cudaGraphConditionalHandle h;
+    RBG_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    gate(h);
+    RBG_CUDA_TRY(cudaGetLastError());
+    RBG_CUDA_TRY(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    RBG_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+    static thread_local cudaStream_t side = nullptr;
+    if (!side) RBG_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    RBG_CUDA_TRY(cudaStreamBeginCaptureToGraph(side, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+    const int rc = body(side);
+    cudaGraph_t got = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(side, &got);
+    if (rc) return rc;
+    if (ee != cudaSuccess) return RBG_ERR_CUDA;
+    RBG_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return RBG_OK;
+}
+
+constexpr int TRI_GEN_LAUNCHES = 9;          // launches of the replay block
 
 __device__ __forceinline__ bool tri_accepted(int ci, const int32_t *ckind, const int *cam, const unsigned *cbad,
                                              const DagCounters *dc, const unsigned *gflags) {
@@ -710,8 +774,9 @@ struct Carve {
 // row index, and the row pool in whatever remains.
 struct TriLayout {
     TriComp *dc;
-    int64_t *dpre, *indptr, *row_off, *ccnt, *cptr, *tcnt, *tpos;
-    unsigned *cflags, *cbad, *gflags;        // gflags[0]: the general path's scratch overflowed; [1]: any general
+    int64_t *dpre, *indptr, *row_off, *ccnt, *cptr, *tcnt, *tpos, *lpos;
+    unsigned *cflags, *cbad, *gflags;        // gflags[0]: the general path's scratch overflowed; [1]: any general;
+                                             // [2]: the replay ran (recorded graphs: its IF node's decision)
     int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val, *row_len, *p_col, *p_val;
     int32_t *ccur, *csc_row, *csc_pos, *cur;
     int4 *trip;                              // (pool positions of (i, k), (k, j), (i, j); step k)
@@ -736,7 +801,7 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     L.cfm = cv.take<int>(C);
     L.cprod = cv.take<unsigned long long>(C);
     L.cbad = cv.take<unsigned>(C);
-    L.gflags = cv.take<unsigned>(2);
+    L.gflags = cv.take<unsigned>(3);
     L.res = cv.take<TriOut>(C);
     L.row_cnt = cv.take<int32_t>(NR);
     L.row_comp = cv.take<int32_t>(NR);
@@ -754,6 +819,7 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     L.ccur = cv.take<int32_t>(NR);
     L.tcnt = cv.take<int64_t>(NR + 1);
     L.tpos = cv.take<int64_t>(NR + 1);
+    L.lpos = cv.take<int64_t>(NR + 1);
     L.fixed = align_up(cv.off, 256);
     // the rest: 40% for the row pool (column, value and the replay's current value per entry),
     // 15% for the transposed pattern, 45% for the replay's triples
@@ -784,7 +850,7 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     const int64_t R = sh.R;
     const int count = (int)sh.count;
     RBG_CUDA_TRY(cudaMemsetAsync(L.cflags, 0, (size_t)count * 4, s));
-    RBG_CUDA_TRY(cudaMemsetAsync(L.gflags, 0, 8, s));
+    RBG_CUDA_TRY(cudaMemsetAsync(L.gflags, 0, 12, s));
     // 1. scan
     {
         cudaEvent_t t = timer_begin(4, s);
@@ -813,7 +879,7 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     if (rc) return rc;
     timer_end(5, tdag, s);
     // 2b. matrices in any numbering: the loop replayed on the closure's pattern (every kernel
-    // returns at once when the batch holds none)
+    // returns at once when the batch holds none; a recorded graph skips the block by an IF node)
     {
         cudaEvent_t tg = timer_begin(8, s);
         const DagCounters *dcn = *dcount;
@@ -821,26 +887,44 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
         const int gw = grid_for(R * 32, 256);
         RBG_CUDA_TRY(cudaMemsetAsync(L.ccnt, 0, (size_t)(R + 1) * 8, s));
         RBG_CUDA_TRY(cudaMemsetAsync(L.ccur, 0, (size_t)R * 4, s));
-        note_launches(8);
-        tri_gen_count_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.row_off, L.row_len, L.p_col, dcn, any,
-                                                L.cbad, L.ccnt);
-        size_t tb2 = L.scan_tmp;
-        RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.ccnt, L.cptr, (int)(R + 1), s));
-        tri_gen_csc_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.row_off, L.row_len, L.p_col, dcn, any,
-                                              L.cptr, L.ccur, L.csc_row, L.csc_pos, L.csc_cap, L.gflags);
-        tri_gen_tcount_kernel<<<grid_for(R + 1, 256), 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.row_len, L.cptr,
-                                                                  dcn, any, L.gflags, L.tcnt);
-        tb2 = L.scan_tmp;
-        RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.tcnt, L.tpos, (int)(R + 1), s));
-        tri_gen_fill_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.row_off, L.row_len, L.p_col, L.cptr,
-                                               L.csc_row, L.csc_pos, L.tpos, dcn, any, L.trip, L.trip_cap, L.gflags);
-        tri_gen_init_kernel<<<gw, 256, 0, s>>>(R, L.row_comp, L.ckind, L.cbad, L.indptr, L.a_col, L.a_val, L.row_off,
-                                               L.row_len, L.p_col, dcn, any, L.gflags, L.cur, L.cfm);
-        tri_gen_replay_kernel<<<grid_for((int64_t)count * 32, 256), 256, 0, s>>>(
-            count, L.dc, L.ckind, L.cbad, L.tpos, L.trip, dcn, any, L.gflags, L.cur, L.pool, L.cam, L.cfm, L.cprod);
-        RBG_CUDA_TRY(cudaGetLastError());
+        auto body = [&](cudaStream_t b) -> int {
+            tri_gen_count_kernel<<<gw, 256, 0, b>>>(R, L.row_comp, L.ckind, L.row_off, L.row_len, L.p_col, dcn, any,
+                                                    L.cbad, L.ccnt);
+            size_t tb2 = L.scan_tmp;
+            RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.ccnt, L.cptr, (int)(R + 1), b));
+            tri_gen_csc_kernel<<<gw, 256, 0, b>>>(R, L.row_comp, L.ckind, L.cbad, L.row_off, L.row_len, L.p_col, dcn,
+                                                  any, L.cptr, L.ccur, L.csc_row, L.csc_pos, L.csc_cap, L.gflags);
+            // (the column counts are scanned already: ccnt now takes the rows' pattern lengths)
+            tri_gen_tcount_kernel<<<grid_for(R + 1, 256), 256, 0, b>>>(R, L.row_comp, L.ckind, L.cbad, L.row_len,
+                                                                      L.cptr, dcn, any, L.gflags, L.tcnt, L.ccnt);
+            tb2 = L.scan_tmp;
+            RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.tcnt, L.tpos, (int)(R + 1), b));
+            tb2 = L.scan_tmp;
+            RBG_CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.tmp, tb2, L.ccnt, L.lpos, (int)(R + 1), b));
+            tri_gen_fill_kernel<<<gw, 256, 0, b>>>(R, L.row_comp, L.ckind, L.cbad, L.dc, L.row_off, L.row_len,
+                                                   L.p_col, L.cptr, L.csc_row, L.csc_pos, L.tpos, L.lpos, dcn, any,
+                                                   L.trip, L.trip_cap, L.gflags);
+            tri_gen_init_kernel<<<gw, 256, 0, b>>>(R, L.row_comp, L.ckind, L.cbad, L.indptr, L.a_col, L.a_val,
+                                                   L.row_off, L.row_len, L.p_col, L.lpos, dcn, any, L.gflags, L.cur,
+                                                   L.cfm);
+            tri_gen_replay_kernel<<<grid_for((int64_t)count * 32, 256), 256, 0, b>>>(
+                count, L.dc, L.ckind, L.cbad, L.tpos, L.lpos, L.trip, dcn, any, L.gflags, L.cur, L.cam, L.cfm,
+                L.cprod);
+            RBG_CUDA_TRY(cudaGetLastError());
+            return (int)RBG_OK;
+        };
+        if (captured) {
+            rc = tri_captured_if(
+                s, [&](cudaGraphConditionalHandle h) { tri_gen_gate_kernel<<<1, 32, 0, s>>>(dcn, any, L.gflags + 2, h); },
+                body);
+            *launches += 1;                  // the gate; the block is counted when it runs
+        } else {
+            note_launches(TRI_GEN_LAUNCHES);
+            rc = body(s);
+            *launches += TRI_GEN_LAUNCHES;
+        }
+        if (rc) return rc;
         timer_end(8, tg, s);
-        *launches += 8;
     }
     // 3. statistics
     {
@@ -992,16 +1076,18 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const 
     }
     std::vector<TriOut> h(C);
     DagCounters hd;
+    unsigned gate_ran = 0;
     {
         HostStaging hs(s, C * sizeof(TriOut) + sizeof(DagCounters) + 128);
         int rc = hs.down(h.data(), L.res, C * sizeof(TriOut));
         if (!rc) rc = hs.down(&hd, dcount, sizeof(hd));
+        if (!rc && fixed_launches >= 0) rc = hs.down(&gate_ran, L.gflags + 2, 4);
         if (!rc) rc = hs.finish();
         if (rc) return rc;
     }
     if (fixed_launches >= 0) {
         const int64_t iters = std::max<int64_t>(1, (hd.nlevels + DAG_GRAPH_CHUNK - 1) / DAG_GRAPH_CHUNK);
-        note_launches(fixed_launches + iters * (3 * DAG_GRAPH_CHUNK + 1));
+        note_launches(fixed_launches + iters * (3 * DAG_GRAPH_CHUNK + 1) + (gate_ran ? TRI_GEN_LAUNCHES : 0));
     }
     for (size_t i = 0; i < C; ++i) {
         closed[i] = (char)h[i].verdict;
