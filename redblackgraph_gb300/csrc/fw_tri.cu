@@ -436,15 +436,16 @@ __global__ void tri_gen_fill_kernel(int64_t R, const int32_t *__restrict__ row_c
     }
 }
 
-// One warp per row of a general matrix: the current values (row g's at lpos[g]) start as A's
-// entries, zero elsewhere in the pattern; A's largest MSB starts the first-value maximum.
+// One warp per row of a general matrix: the current MSBs (row g's at lpos[g]) start as those of
+// A's entries, zero (no value) elsewhere in the pattern; A's largest MSB starts the first-value
+// maximum.
 __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                                     const unsigned *__restrict__ cbad, const int64_t *__restrict__ indptr,
                                     const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
                                     const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                                     const int32_t *__restrict__ p_col, const int64_t *__restrict__ lpos,
                                     const DagCounters *dc, const unsigned *any_gen, unsigned *gflags,
-                                    int32_t *__restrict__ cur, int *__restrict__ cfm) {
+                                    uint8_t *__restrict__ cur, int *__restrict__ cfm) {
     if (!tri_dag_ok(dc) || !*any_gen || *gflags) return;
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -462,7 +463,7 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
                 atomicOr(gflags, 2u);
                 continue;
             }
-            cur[l + (q - o)] = a_val[e];
+            cur[l + (q - o)] = (uint8_t)msb_u32((uint32_t)a_val[e]);   // a clean value: 2 <= v < 2^31
             fm = max(fm, dag_row_msb(a_val[e]));
         }
         fm = __reduce_max_sync(0xffffffffu, fm);
@@ -473,17 +474,18 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
 // One warp per general matrix: its triples (ordered by step) streamed in chunks of 32, each
 // chunk loaded TRI_PREFETCH chunks ahead so that no step waits for its triples; within a chunk
 // the lanes take the chunk's steps in order (a warp barrier after each), so one step's stores
-// come before the next step's loads.  The matrix's P current values lie contiguously at
-// curg + lpos[first row].  Every matrix replays at once: the chain of steps of the largest ones
-// (a dependent round trip to memory per step) sets the kernel's length; holding a matrix's
-// values in shared memory instead (one warp per CTA, up to 216 KB) left one warp per SM for the
-// largest matrices and took longer in all.
+// come before the next step's loads.  A cell is tracked by the MSB of its current value alone
+// (0: no value yet): msb(x (x) y) = msb(x) + msb(y) in the clean regime and msb(min(a, b)) =
+// min(msb(a), msb(b)), so the products' MSBs and each cell's first value, all the replay decides
+// from, come out exactly.  The matrix's P MSBs lie contiguously at curg + lpos[first row], one
+// byte each, so the whole batch's cells stay in L2.  Every matrix replays at once: the chain of
+// steps of the largest ones (a dependent round trip per step) sets the kernel's length.
 constexpr int TRI_PREFETCH = 8;
 __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_t *__restrict__ ckind,
                                       const unsigned *__restrict__ cbad, const int64_t *__restrict__ tpos,
                                       const int64_t *__restrict__ lpos, const int4 *__restrict__ trip,
                                       const DagCounters *dc, const unsigned *any_gen, const unsigned *gflags,
-                                      int32_t *curg, int *__restrict__ cam, int *__restrict__ cfm,
+                                      uint8_t *curg, int *__restrict__ cam, int *__restrict__ cfm,
                                       unsigned long long *__restrict__ cprod) {
     if (!tri_dag_ok(dc) || !*any_gen) return;
     const int lane = threadIdx.x & 31;
@@ -492,7 +494,7 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
         if (!tri_gen_row(ci, ckind, cbad, dc, gflags)) continue;   // warp-uniform
         const int64_t base = comps[ci].row_base, rows = comps[ci].n;
         const int64_t m0 = lpos[base], P = lpos[base + rows] - m0;
-        int32_t *val = curg + m0;
+        uint8_t *val = curg + m0;
         const int64_t T0 = tpos[base], T1 = tpos[base + rows];
         auto fetch = [&](int64_t c) -> int4 {
             const int64_t t = T0 + c * 32 + lane;
@@ -520,18 +522,16 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
                         atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
                     } else {
                         // the three cells are read together: one round trip per step
-                        const int32_t x = val[tr.x], y = val[tr.y], old = val[tr.z];
-                        if (x != 0 && y != 0) {
-                            const int mx = msb_u32((uint32_t)x), my = msb_u32((uint32_t)y);
-                            const int pm = mx + my;
+                        const int mx = val[tr.x], my = val[tr.y], old = val[tr.z];
+                        if (mx != 0 && my != 0) {
+                            const int pm = mx + my;          // the product's MSB
                             top = max(top, pm);
                             ++prods;
-                            const int32_t pv = (int32_t)(((uint32_t)x << my) | ((uint32_t)y ^ (1u << my)));
                             if (old == 0) {
                                 first = max(first, pm);
-                                val[tr.z] = pv;
-                            } else if (pv < old) {
-                                val[tr.z] = pv;
+                                val[tr.z] = (uint8_t)pm;
+                            } else if (pm < old) {
+                                val[tr.z] = (uint8_t)pm;
                             }
                         }
                     }
@@ -778,7 +778,8 @@ struct TriLayout {
     unsigned *cflags, *cbad, *gflags;        // gflags[0]: the general path's scratch overflowed; [1]: any general;
                                              // [2]: the replay ran (recorded graphs: its IF node's decision)
     int32_t *ckind, *row_cnt, *row_comp, *slot_col, *slot_val, *a_col, *a_val, *row_len, *p_col, *p_val;
-    int32_t *ccur, *csc_row, *csc_pos, *cur;
+    int32_t *ccur, *csc_row, *csc_pos;
+    uint8_t *cur;                            // the replay's current MSB per pattern entry
     int4 *trip;                              // (pool positions of (i, k), (k, j), (i, j); step k)
     int *cam, *cfm;
     unsigned long long *cprod;
@@ -821,17 +822,17 @@ void tri_layout(unsigned char *base, size_t ws_bytes, size_t C, size_t NR, TriLa
     L.tpos = cv.take<int64_t>(NR + 1);
     L.lpos = cv.take<int64_t>(NR + 1);
     L.fixed = align_up(cv.off, 256);
-    // the rest: 40% for the row pool (column, value and the replay's current value per entry),
+    // the rest: 40% for the row pool (column, value and the replay's current MSB per entry),
     // 15% for the transposed pattern, 45% for the replay's triples
     const size_t rest = ws_bytes > L.fixed + 2048 ? ws_bytes - L.fixed - 2048 : 0;
-    L.pool = std::min<int64_t>((int64_t)(rest / 10 * 4 / 12 / 64 * 64), (int64_t)INT32_MAX / 64 * 64);
+    L.pool = std::min<int64_t>((int64_t)(rest / 10 * 4 / 9 / 64 * 64), (int64_t)INT32_MAX / 64 * 64);
     L.csc_cap = (int64_t)(rest / 100 * 15 / 8);
     L.trip_cap = (int64_t)(rest / 100 * 45 / 16);
     Carve tail{base};
     tail.off = L.fixed;
     L.p_col = tail.take<int32_t>((size_t)L.pool);
     L.p_val = tail.take<int32_t>((size_t)L.pool);
-    L.cur = tail.take<int32_t>((size_t)L.pool);
+    L.cur = tail.take<uint8_t>((size_t)L.pool);
     L.csc_row = tail.take<int32_t>((size_t)L.csc_cap);
     L.csc_pos = tail.take<int32_t>((size_t)L.csc_cap);
     L.trip = tail.take<int4>((size_t)L.trip_cap);
