@@ -477,40 +477,58 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
 // come before the next step's loads.  A cell is tracked by the MSB of its current value alone
 // (0: no value yet): msb(x (x) y) = msb(x) + msb(y) in the clean regime and msb(min(a, b)) =
 // min(msb(a), msb(b)), so the products' MSBs and each cell's first value, all the replay decides
-// from, come out exactly.  The matrix's P MSBs lie contiguously at curg + lpos[first row], one
-// byte each, so the whole batch's cells stay in L2.  Every matrix replays at once: the chain of
-// steps of the largest ones (a dependent round trip per step) sets the kernel's length.
+// from, come out exactly.  The matrix's P MSBs, one byte each, lie contiguously at
+// curg + lpos[first row].  SMEM: one CTA of one warp per matrix with P <= TRI_SMEM_CELLS copies
+// them into shared memory first (a step then costs a shared-memory round trip, not one to L2);
+// otherwise a warp per matrix with P > TRI_SMEM_CELLS works on them in place.  The chain of steps
+// of the largest matrices (~2,300 non-empty steps) sets the kernel's length.
 constexpr int TRI_PREFETCH = 8;
-__global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_t *__restrict__ ckind,
-                                      const unsigned *__restrict__ cbad, const int64_t *__restrict__ tpos,
-                                      const int64_t *__restrict__ lpos, const int4 *__restrict__ trip,
-                                      const DagCounters *dc, const unsigned *any_gen, const unsigned *gflags,
-                                      uint8_t *curg, int *__restrict__ cam, int *__restrict__ cfm,
-                                      unsigned long long *__restrict__ cprod) {
+constexpr int64_t TRI_SMEM_CELLS = 57344;    // 56 KB of shared memory: four one-warp CTAs per SM
+
+template <bool SMEM>
+__global__ void __launch_bounds__(SMEM ? 32 : 256)
+tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_t *__restrict__ ckind,
+                      const unsigned *__restrict__ cbad, const int64_t *__restrict__ tpos,
+                      const int64_t *__restrict__ lpos, const int4 *__restrict__ trip, const DagCounters *dc,
+                      const unsigned *any_gen, const unsigned *gflags, uint8_t *curg, int *__restrict__ cam,
+                      int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
     if (!tri_dag_ok(dc) || !*any_gen) return;
+    extern __shared__ __align__(16) uint8_t tri_cells[];
     const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int ci = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ci < count; ci += warps) {
+    const int warps = SMEM ? gridDim.x : gridDim.x * (blockDim.x >> 5);
+    const int first_ci = SMEM ? blockIdx.x : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (int ci = first_ci; ci < count; ci += warps) {
         if (!tri_gen_row(ci, ckind, cbad, dc, gflags)) continue;   // warp-uniform
         const int64_t base = comps[ci].row_base, rows = comps[ci].n;
         const int64_t m0 = lpos[base], P = lpos[base + rows] - m0;
+        if (SMEM ? P > TRI_SMEM_CELLS : P <= TRI_SMEM_CELLS) continue;
         uint8_t *val = curg + m0;
+        if (SMEM) {
+            for (int64_t q = lane; q < P; q += 32) tri_cells[q] = val[q];
+            __syncwarp();
+            val = tri_cells;
+        }
         const int64_t T0 = tpos[base], T1 = tpos[base + rows];
         auto fetch = [&](int64_t c) -> int4 {
             const int64_t t = T0 + c * 32 + lane;
             return t < T1 ? trip[t] : make_int4(0, 0, 0, INT_MAX);
         };
+        // a ring of TRI_PREFETCH chunks: slot d holds chunk c0 + d; the slot just taken is
+        // refilled with the chunk TRI_PREFETCH further on (slots are compile-time indices, so no
+        // register holding a load in flight is read before it is needed)
         int4 q[TRI_PREFETCH];
 #pragma unroll
         for (int d = 0; d < TRI_PREFETCH; ++d) q[d] = fetch(d);
         int top = -1, first = -1;
         unsigned long long prods = 0;
         const int64_t chunks = (T1 - T0 + 31) / 32;
-        for (int64_t c = 0; c < chunks; ++c) {
-            const int4 tr = q[0];
+        for (int64_t c0 = 0; c0 < chunks; c0 += TRI_PREFETCH)
 #pragma unroll
-            for (int d = 0; d + 1 < TRI_PREFETCH; ++d) q[d] = q[d + 1];
-            q[TRI_PREFETCH - 1] = fetch(c + TRI_PREFETCH);
+        for (int d = 0; d < TRI_PREFETCH; ++d) {
+            const int64_t c = c0 + d;
+            if (c >= chunks) break;                                   // warp-uniform
+            const int4 tr = q[d];
+            q[d] = fetch(c + TRI_PREFETCH);
             bool todo = tr.w != INT_MAX;
             while (true) {
                 const int k = __reduce_min_sync(0xffffffffu, todo ? tr.w : INT_MAX);   // warp-uniform
@@ -548,6 +566,15 @@ __global__ void tri_gen_replay_kernel(int count, const TriComp *__restrict__ com
             cprod[ci] += prods;
         }
     }
+}
+
+PerDeviceOnce g_tri_configured;
+int tri_configure() {
+    return g_tri_configured.run([] {
+        RBG_CUDA_TRY(cudaFuncSetAttribute(tri_gen_replay_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TRI_SMEM_CELLS));
+        return (int)RBG_OK;
+    });
 }
 
 // Recorded graphs: the IF node around the replay opens only when the closure by levels went
@@ -595,7 +622,7 @@ int tri_captured_if(cudaStream_t s, Gate gate, Body body) {
     return RBG_OK;
 }
 
-constexpr int TRI_GEN_LAUNCHES = 9;          // launches of the replay block
+constexpr int TRI_GEN_LAUNCHES = 10;         // launches of the replay block
 
 __device__ __forceinline__ bool tri_accepted(int ci, const int32_t *ckind, const int *cam, const unsigned *cbad,
                                              const DagCounters *dc, const unsigned *gflags) {
@@ -908,7 +935,10 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
             tri_gen_init_kernel<<<gw, 256, 0, b>>>(R, L.row_comp, L.ckind, L.cbad, L.indptr, L.a_col, L.a_val,
                                                    L.row_off, L.row_len, L.p_col, L.lpos, dcn, any, L.gflags, L.cur,
                                                    L.cfm);
-            tri_gen_replay_kernel<<<grid_for((int64_t)count * 32, 256), 256, 0, b>>>(
+            tri_gen_replay_kernel<true><<<(unsigned)count, 32, (size_t)TRI_SMEM_CELLS, b>>>(
+                count, L.dc, L.ckind, L.cbad, L.tpos, L.lpos, L.trip, dcn, any, L.gflags, L.cur, L.cam, L.cfm,
+                L.cprod);
+            tri_gen_replay_kernel<false><<<grid_for((int64_t)count * 32, 256), 256, 0, b>>>(
                 count, L.dc, L.ckind, L.cbad, L.tpos, L.lpos, L.trip, dcn, any, L.gflags, L.cur, L.cam, L.cfm,
                 L.cprod);
             RBG_CUDA_TRY(cudaGetLastError());
@@ -1015,6 +1045,10 @@ int tri_batch(int64_t count, const int64_t *sizes, const int64_t *in_off, const 
               int64_t ld_out, const T *in, T *out, rbg_result_t *results, char *closed, unsigned char *ws,
               size_t ws_bytes, uint32_t mode, cudaStream_t s, const RowStats &rs) {
     if (count <= 0 || count > INT32_MAX || !ws) return RBG_OK;
+    {
+        const int rc = tri_configure();     // before any capture: kernel attributes per device
+        if (rc) return rc;
+    }
     std::vector<TriComp> hc((size_t)count);
     std::vector<int64_t> pre((size_t)count + 1, 0);
     int64_t R = 0;

@@ -323,8 +323,9 @@ def test_dag_path_any_numbering_vs_oracle(native, dtype):
         A = _random_dag(rng, n, rng.uniform(0.03, 0.35))
         p = rng.permutation(n)
         mats.append(A[p][:, p].astype(dtype))
-    for n in (120, 600, 1500, 2000):
-        A = synth.pedigree(n, synth.generations_for(n), n + 5, dtype=dtype)
+    # (the last one's closure pattern, ~64,000 cells, is past what one CTA replays in shared memory)
+    for n, gens in ((120, None), (600, None), (1500, None), (2000, None), (2000, 100)):
+        A = synth.pedigree(n, gens or synth.generations_for(n), n + 5, dtype=dtype)
         p = rng.permutation(n)
         mats.append(A[p][:, p].copy())
     cyc = synth.pedigree(150, 8, 41, dtype=dtype)
@@ -346,4 +347,4 @@ def test_dag_path_any_numbering_vs_oracle(native, dtype):
                 dag += r.path == _lib.PATH_DAG
             assert dag >= 50
             assert res[-1].status == _lib.RBG_ERR_CYCLE and res[-1].path != _lib.PATH_DAG
-            assert all(r.path == _lib.PATH_DAG for r in res[-5:-1])   # the relabelled pedigrees
+            assert all(r.path == _lib.PATH_DAG for r in res[-6:-1])   # the relabelled pedigrees
