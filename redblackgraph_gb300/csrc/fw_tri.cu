@@ -471,10 +471,10 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
     }
 }
 
-// One warp per general matrix: its triples (ordered by step) streamed in chunks of 32, each
-// chunk loaded TRI_PREFETCH chunks ahead so that no step waits for its triples; within a chunk
-// the lanes take the chunk's steps in order (a warp barrier after each), so one step's stores
-// come before the next step's loads.  A cell is tracked by the MSB of its current value alone
+// One warp per general matrix: its triples (ordered by step) streamed in chunks of TRI_CHUNK,
+// each chunk loaded TRI_PREFETCH chunks ahead so that no step waits for its triples; within a
+// chunk the lanes take the chunk's steps in order (a warp barrier after each), so one step's
+// stores come before the next step's loads.  A cell is tracked by the MSB of its current value alone
 // (0: no value yet): msb(x (x) y) = msb(x) + msb(y) in the clean regime and msb(min(a, b)) =
 // min(msb(a), msb(b)), so the products' MSBs and each cell's first value, all the replay decides
 // from, come out exactly.  The matrix's P MSBs, one byte each, lie contiguously at
@@ -482,7 +482,9 @@ __global__ void tri_gen_init_kernel(int64_t R, const int32_t *__restrict__ row_c
 // them into shared memory first (a step then costs a shared-memory round trip, not one to L2);
 // otherwise a warp per matrix with P > TRI_SMEM_CELLS works on them in place.  The chain of steps
 // of the largest matrices (~2,300 non-empty steps) sets the kernel's length.
-constexpr int TRI_PREFETCH = 8;
+constexpr int TRI_PER_LANE = 4;              // triples of a chunk per lane
+constexpr int TRI_CHUNK = 32 * TRI_PER_LANE;
+constexpr int TRI_PREFETCH = 4;              // chunks in flight
 constexpr int64_t TRI_SMEM_CELLS = 57344;    // 56 KB of shared memory: four one-warp CTAs per SM
 
 template <bool SMEM>
@@ -509,48 +511,63 @@ tri_gen_replay_kernel(int count, const TriComp *__restrict__ comps, const int32_
             val = tri_cells;
         }
         const int64_t T0 = tpos[base], T1 = tpos[base + rows];
-        auto fetch = [&](int64_t c) -> int4 {
-            const int64_t t = T0 + c * 32 + lane;
+        // chunks of TRI_CHUNK triples, triple j of a lane at chunk position 32 j + lane (coalesced
+        // loads; a lane's triples ascend by step); a ring of TRI_PREFETCH chunks in flight, slot d
+        // holding chunk c0 + d and refilled with chunk c0 + d + TRI_PREFETCH once taken (slots are
+        // compile-time indices, so no register awaiting its load is read early)
+        auto fetch = [&](int64_t c, int j) -> int4 {
+            const int64_t t = T0 + c * TRI_CHUNK + 32 * j + lane;
             return t < T1 ? trip[t] : make_int4(0, 0, 0, INT_MAX);
         };
-        // a ring of TRI_PREFETCH chunks: slot d holds chunk c0 + d; the slot just taken is
-        // refilled with the chunk TRI_PREFETCH further on (slots are compile-time indices, so no
-        // register holding a load in flight is read before it is needed)
-        int4 q[TRI_PREFETCH];
+        int4 q[TRI_PREFETCH][TRI_PER_LANE];
 #pragma unroll
-        for (int d = 0; d < TRI_PREFETCH; ++d) q[d] = fetch(d);
+        for (int d = 0; d < TRI_PREFETCH; ++d)
+#pragma unroll
+            for (int j = 0; j < TRI_PER_LANE; ++j) q[d][j] = fetch(d, j);
         int top = -1, first = -1;
         unsigned long long prods = 0;
-        const int64_t chunks = (T1 - T0 + 31) / 32;
+        const int64_t chunks = (T1 - T0 + TRI_CHUNK - 1) / TRI_CHUNK;
         for (int64_t c0 = 0; c0 < chunks; c0 += TRI_PREFETCH)
 #pragma unroll
         for (int d = 0; d < TRI_PREFETCH; ++d) {
             const int64_t c = c0 + d;
             if (c >= chunks) break;                                   // warp-uniform
-            const int4 tr = q[d];
-            q[d] = fetch(c + TRI_PREFETCH);
-            bool todo = tr.w != INT_MAX;
+            int4 tr[TRI_PER_LANE];
+#pragma unroll
+            for (int j = 0; j < TRI_PER_LANE; ++j) {
+                tr[j] = q[d][j];
+                q[d][j] = fetch(c + TRI_PREFETCH, j);
+            }
+            // the chunk's steps in order: each lane does all its triples of the step at once
+            // (a step's triples are independent), then a warp barrier
+            int next = 0;                                             // the lane's first pending triple
             while (true) {
-                const int k = __reduce_min_sync(0xffffffffu, todo ? tr.w : INT_MAX);   // warp-uniform
-                if (k == INT_MAX) break;
-                if (todo && tr.w == k) {
-                    todo = false;
-                    if ((uint64_t)(uint32_t)tr.x >= (uint64_t)P || (uint64_t)(uint32_t)tr.y >= (uint64_t)P ||
-                        (uint64_t)(uint32_t)tr.z >= (uint64_t)P) {
+                int mine = INT_MAX;
+#pragma unroll
+                for (int j = 0; j < TRI_PER_LANE; ++j)
+                    if (j == next) mine = tr[j].w;
+                const int k = __reduce_min_sync(0xffffffffu, next < TRI_PER_LANE ? mine : INT_MAX);
+                if (k == INT_MAX) break;                              // warp-uniform
+#pragma unroll
+                for (int j = 0; j < TRI_PER_LANE; ++j) {
+                    if (j < next || tr[j].w != k) continue;
+                    ++next;
+                    if ((uint64_t)(uint32_t)tr[j].x >= (uint64_t)P || (uint64_t)(uint32_t)tr[j].y >= (uint64_t)P ||
+                        (uint64_t)(uint32_t)tr[j].z >= (uint64_t)P) {
                         atomicOr(const_cast<int *>(&dc->flags), TRI_BAD_ROW);
-                    } else {
-                        // the three cells are read together: one round trip per step
-                        const int mx = val[tr.x], my = val[tr.y], old = val[tr.z];
-                        if (mx != 0 && my != 0) {
-                            const int pm = mx + my;          // the product's MSB
-                            top = max(top, pm);
-                            ++prods;
-                            if (old == 0) {
-                                first = max(first, pm);
-                                val[tr.z] = (uint8_t)pm;
-                            } else if (pm < old) {
-                                val[tr.z] = (uint8_t)pm;
-                            }
+                        continue;
+                    }
+                    // the three cells are read together: one round trip per step
+                    const int mx = val[tr[j].x], my = val[tr[j].y], old = val[tr[j].z];
+                    if (mx != 0 && my != 0) {
+                        const int pm = mx + my;              // the product's MSB
+                        top = max(top, pm);
+                        ++prods;
+                        if (old == 0) {
+                            first = max(first, pm);
+                            val[tr[j].z] = (uint8_t)pm;
+                        } else if (pm < old) {
+                            val[tr[j].z] = (uint8_t)pm;
                         }
                     }
                 }
