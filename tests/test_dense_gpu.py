@@ -291,3 +291,29 @@ def test_single_matrix_any_numbering_dag_path(native, dtype):
         assert so == 0 and res.status == 0
         assert (W == Wo).all() and res.diameter == do
         assert res.path == _lib.PATH_DAG, (n, res.path)
+
+
+def test_kernel_attributes_on_every_device(native):
+    """Kernels with more than 48 KB of shared memory get their attribute on each device the
+    process uses: a blocked closure, a DAG-path closure and a sparse product on device 1 after
+    device 0, each equal to the oracle (needs two visible GPUs)."""
+    import torch
+    from redblackgraph_gb300 import synth, _lib
+    from redblackgraph_gb300.dense import fw_dense
+    from redblackgraph_gb300.device import to_device, to_host
+    from redblackgraph_gb300.spgemm import DeviceCSR, spgemm
+    if torch.cuda.device_count() < 2:
+        pytest.skip("one GPU visible")
+    A = synth.pedigree(500, 12, 3, dtype=np.int32)
+    Wo, do, so, _ = O.warshall(A)
+    Po, _ = O.rb_matmul_csr(A, A)
+    for dev in (0, 1):
+        with torch.cuda.device(dev):
+            d = to_device(A, torch.device("cuda", dev))
+            for mode, path in ((_lib.MODE_NO_DAG, _lib.PATH_BLOCKED32), (0, _lib.PATH_DAG)):
+                out, r = fw_dense(d, mode=mode)
+                torch.cuda.synchronize(dev)
+                assert r.path == path and (to_host(out) == Wo).all() and r.diameter == do
+            M = DeviceCSR.from_scipy(A, device=torch.device("cuda", dev))
+            P, rc, _ = spgemm(M, M)
+            assert rc == 0 and (P.to_scipy() != Po).nnz == 0
