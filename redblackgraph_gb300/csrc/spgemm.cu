@@ -126,6 +126,7 @@ struct SpArgs {
     long long *dense_val; unsigned *dense_mark;         // dense accumulators (SP_DENSE_BLOCKS rows)
     int *big_rows; int *big_count;                      // rows for the block / dense kernels
     unsigned *flags;
+    int2 *win;                                          // per row: first and last column it can reach
 };
 
 __device__ __forceinline__ long long sp_load(const void *x, int64_t i, int bytes, int uns) {
@@ -136,18 +137,34 @@ __device__ __forceinline__ long long sp_load(const void *x, int64_t i, int bytes
 }
 
 // ----------------------------------------------------------------------------- candidates
-// cand[i] = sum over k in A[i] of nnz(B[k]) (+ nnz(R[i]) for a squaring step).  Rows above the
-// warp capacity are listed for the block / dense kernels.
+// cand[i] = sum over k in A[i] of nnz(B[k]) (+ nnz(R[i]) for a squaring step), and the row's
+// column window win[i]: the first and last column of every B row it gathers and of R's row (the
+// numeric pass folds rows whose window spans at most SP_WIN columns into a direct accumulator).
+// Rows above the warp capacity are listed for the block / dense kernels.
 __global__ void sp_count_kernel(SpArgs a, int64_t *cand) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= a.n_rows;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (i == a.n_rows) { cand[i] = 0; continue; }
         int64_t c = 0;
+        int jlo = INT_MAX, jhi = -1;
         for (int64_t e = a.ap[i]; e < a.ap[i + 1]; ++e) {
             const int k = a.aj[e];
-            c += a.bp[k + 1] - a.bp[k];
+            const int64_t b0 = a.bp[k], b1 = a.bp[k + 1];
+            if (b1 > b0) {
+                c += b1 - b0;
+                jlo = min(jlo, a.bj[b0]);
+                jhi = max(jhi, a.bj[b1 - 1]);
+            }
         }
-        if (a.rp) c += a.rp[i + 1] - a.rp[i];
+        if (a.rp) {
+            const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
+            if (r1 > r0) {
+                c += r1 - r0;
+                jlo = min(jlo, a.rj[r0]);
+                jhi = max(jhi, a.rj[r1 - 1]);
+            }
+        }
+        a.win[i] = make_int2(jlo, jhi);
         cand[i] = c;
         if (c > SP_BLOCK_CAP) {      // the dense kernel's rows
             a.big_rows[atomicAdd(a.big_count, 1)] = (int)i;
@@ -450,25 +467,9 @@ sp_warp_kernel(SpArgs a, int merge) {
         const int64_t c = a.cand_off[i + 1] - a.cand_off[i];
         if (c > SP_BLOCK_CAP) continue;              // the dense kernel takes it
         const bool sq = merge && a.rp;
-        // the row's column window: first and last column of every B row it gathers and of R's row
-        int jlo = INT_MAX, jhi = -1;
-        for (int64_t e = a.ap[i] + lane; e < a.ap[i + 1]; e += 32) {
-            const int k = a.aj[e];
-            const int64_t b0 = a.bp[k], b1 = a.bp[k + 1];
-            if (b1 > b0) {
-                jlo = min(jlo, a.bj[b0]);
-                jhi = max(jhi, a.bj[b1 - 1]);
-            }
-        }
-        if (sq && lane == 0) {
-            const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
-            if (r1 > r0) {
-                jlo = min(jlo, a.rj[r0]);
-                jhi = max(jhi, a.rj[r1 - 1]);
-            }
-        }
-        jlo = __reduce_min_sync(0xffffffffu, jlo);
-        jhi = __reduce_max_sync(0xffffffffu, jhi);
+        // the row's column window, from the count pass
+        const int2 wnd = a.win[i];
+        const int jlo = wnd.x, jhi = wnd.y;
         const long long width = jhi >= jlo ? (long long)jhi - jlo + 1 : 0;
         const int span = (int)(width < SP_WIN + 1 ? width : SP_WIN + 1);
         const bool win = span <= SP_WIN;             // warp-uniform
@@ -783,6 +784,7 @@ namespace {
 
 struct Head {   // workspace that lives from rbg_spgemm_count to rbg_spgemm_gather
     int64_t *cand_off;   // n+1
+    int2 *win;           // n: each row's column window
     int *big_rows;       // n
     int *counters;       // [0] big rows, [1] dense rows, [2] flags
     void *scan_tmp;
@@ -800,6 +802,7 @@ size_t head_layout(int64_t n, unsigned char *base, Head *h) {
     auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return base ? base + at : nullptr; };
     unsigned char *p;
     p = take((size_t)(n + 1) * 8); if (h) h->cand_off = reinterpret_cast<int64_t *>(p);
+    p = take((size_t)std::max<int64_t>(n, 1) * 8); if (h) h->win = reinterpret_cast<int2 *>(p);
     p = take((size_t)std::max<int64_t>(n, 1) * 4); if (h) h->big_rows = reinterpret_cast<int *>(p);
     p = take(64); if (h) h->counters = reinterpret_cast<int *>(p);
     const size_t sb = scan_bytes(n);
@@ -872,6 +875,7 @@ extern "C" int32_t rbg_spgemm_count(const rbg_csr_t *A, const rbg_csr_t *B, cons
     fill_args(a, A, B, R, upper);
     a.big_rows = h.big_rows;
     a.big_count = h.counters;
+    a.win = h.win;
     RBG_CUDA_TRY(cudaMemsetAsync(h.counters, 0, 64, s));
     note_launches(2);
     sp_count_kernel<<<grid_of(n + 1, 256), 256, 0, s>>>(a, h.cand_off);
@@ -945,6 +949,7 @@ extern "C" int32_t rbg_spgemm_numeric(int32_t sem, int32_t dtype, const rbg_csr_
     a.ocol = t.ocol; a.oval = t.oval; a.rownnz = t.rownnz;
     a.dense_val = t.dense_val; a.dense_mark = t.dense_mark;
     a.big_rows = h.big_rows; a.big_count = h.counters;
+    a.win = h.win;
     a.flags = reinterpret_cast<unsigned *>(h.counters + 2);
     RBG_CUDA_TRY(cudaMemsetAsync(h.counters + 2, 0, 4, s));
     RBG_CUDA_TRY(cudaMemsetAsync(t.rownnz, 0, (size_t)(n + 1) * 8, s));
