@@ -467,9 +467,12 @@ __global__ void cc_dag_edges_kernel(int64_t n, const int64_t *__restrict__ indpt
     }
 }
 
-// one warp per vertex: the row statistics of dag_rows.cuh and the row's largest final value,
-// reduced per component
-__global__ void __launch_bounds__(32 * CCD_WARPS, 8)
+// the row statistics of dag_rows.cuh and the row's largest final value, reduced per component:
+// a group of DAG_STATS_G lanes per vertex, runs of DAG_STATS_RUN vertices per group, one set of
+// atomics per run and component (each group's bitmap takes 1 KB of shared memory)
+constexpr int CCD_STATS_GROUPS = 32 * CCD_WARPS / DAG_STATS_G;
+constexpr int CCD_STATS_CTAS = 6;
+__global__ void __launch_bounds__(32 * CCD_WARPS, CCD_STATS_CTAS)
 cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t *__restrict__ local,
                     const int64_t *__restrict__ start, const int32_t *__restrict__ sorted_vertex,
                     const int32_t *__restrict__ comp_kind,
@@ -478,37 +481,55 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
                     const int32_t *__restrict__ ccol, const int32_t *__restrict__ cval,
                     const int32_t *__restrict__ diag, int *__restrict__ top, int *__restrict__ first,
                     int *__restrict__ cmax) {
-    __shared__ unsigned bm_all[CCD_WARPS][DAG_MAX_N / 32];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * CCD_WARPS;
-    for (int64_t u = (int64_t)blockIdx.x * CCD_WARPS + w; u < n; u += warps) {
-        const int c = label[u];
-        const int kind = comp_kind[c];
-        if (kind == DAG_KIND_NONE) continue;         // warp-uniform
-        // a component whose vertices span fewer than DAG_MAX_N numbers indexes its bitmap by
-        // vertex - lowest vertex (no gather); otherwise by its local index
-        const int lo = sorted_vertex[start[c]], hi = sorted_vertex[start[c + 1] - 1];
-        int am = -1, fm = -1;
-        unsigned long long prods = 0;
-        auto crow = [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; };
-        if (hi - lo < DAG_MAX_N)
-            dag_row_stats(bm_all[w], (hi - lo + 32) >> 5, kind, u, eptr, ecol, eval, crow, ccol, cval,
-                          [&](int32_t col) { return col - lo; }, lane, am, fm, prods);
-        else
-            dag_row_stats(bm_all[w], (int)((start[c + 1] - start[c] + 31) >> 5), kind, u, eptr, ecol, eval, crow,
-                          ccol, cval, [&](int32_t col) { return local[col]; }, lane, am, fm, prods);
-        int mx = 0;
-        for (int64_t q = row_off[u] + lane; q < row_off[u] + row_len[u]; q += 32) mx = max(mx, cval[q]);
-        if (lane == 0) mx = max(mx, diag[u]);
-        am = __reduce_max_sync(0xffffffffu, am);
-        fm = __reduce_max_sync(0xffffffffu, fm);
-        mx = __reduce_max_sync(0xffffffffu, mx);
-        if (lane == 0) {
-            if (am >= 0) atomicMax(top + c, am);
-            if (fm >= 0) atomicMax(first + c, fm);
-            if (mx > 0) atomicMax(cmax + c, mx);
+    constexpr int G = DAG_STATS_G;
+    __shared__ __align__(16) unsigned bm_all[CCD_STATS_GROUPS][DAG_MAX_N / 32];
+    const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
+    const unsigned gmask = dag_group_mask<G>();
+    int cur = -1, am = -1, fm = -1, mx = 0;  // the component of the run's current rows, its statistics
+    unsigned long long prods = 0;
+    auto flush = [&]() {                     // group-uniform
+        const int am_r = __reduce_max_sync(gmask, am);
+        const int fm_r = __reduce_max_sync(gmask, fm);
+        const int mx_r = __reduce_max_sync(gmask, mx);
+        if (lane == 0 && cur >= 0) {
+            if (am_r >= 0) atomicMax(top + cur, am_r);
+            if (fm_r >= 0) atomicMax(first + cur, fm_r);
+            if (mx_r > 0) atomicMax(cmax + cur, mx_r);
+        }
+    };
+    auto crow = [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; };
+    const int64_t stride = (int64_t)gridDim.x * CCD_STATS_GROUPS * DAG_STATS_RUN;
+    for (int64_t r0 = ((int64_t)blockIdx.x * CCD_STATS_GROUPS + grp) * DAG_STATS_RUN; r0 < n; r0 += stride) {
+        const int64_t r1 = min(n, r0 + DAG_STATS_RUN);
+        for (int64_t u = r0; u < r1; ++u) {
+            const int c = label[u];
+            const int64_t a0 = eptr[u];
+            const int alen = (int)(eptr[u + 1] - a0);
+            const int kind = comp_kind[c];
+            if (kind == DAG_KIND_NONE) continue;     // group-uniform
+            if (c != cur) {
+                flush();
+                cur = c;
+                am = fm = -1;
+                mx = 0;
+            }
+            // a component whose vertices span fewer than DAG_MAX_N numbers indexes its bitmap by
+            // vertex - lowest vertex (no gather); otherwise by its local index
+            const int lo = sorted_vertex[start[c]], hi = sorted_vertex[start[c + 1] - 1];
+            if (hi - lo < DAG_MAX_N)
+                dag_row_stats<G>(bm_all[grp], (hi - lo + 32) >> 5, kind, u, a0, alen, eptr, ecol, eval, crow, ccol,
+                                 cval, [&](int32_t col) { return col - lo; }, lane, gmask, am, fm, prods);
+            else
+                dag_row_stats<G>(bm_all[grp], (int)((start[c + 1] - start[c] + 31) >> 5), kind, u, a0, alen, eptr,
+                                 ecol, eval, crow, ccol, cval, [&](int32_t col) { return local[col]; }, lane, gmask,
+                                 am, fm, prods);
+            const int64_t o = row_off[u];
+            const int len = row_len[u];
+            for (int q = lane; q < len; q += G) mx = max(mx, cval[o + q]);
+            if (lane == 0) mx = max(mx, diag[u]);
         }
     }
+    flush();
 }
 
 __global__ void cc_dag_merge_count_kernel(int64_t n, const int32_t *__restrict__ row_len, const int32_t *__restrict__ diag,
@@ -600,7 +621,9 @@ extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *lab
     }
     if (n == 0) return RBG_OK;
     note_launches(1);
-    cc_dag_stats_kernel<<<grid_for(n * 32, 32 * CCD_WARPS), 32 * CCD_WARPS, 0, s>>>(
+    const int64_t runs = (n + DAG_STATS_RUN * CCD_STATS_GROUPS - 1) / (DAG_STATS_RUN * CCD_STATS_GROUPS);
+    cc_dag_stats_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(runs, (int64_t)sm_count() * CCD_STATS_CTAS)),
+                          32 * CCD_WARPS, 0, s>>>(
         n, label, local, start, sorted_vertex, comp_kind, edges->indptr, edges->indices, static_cast<const int32_t *>(edges->data),
         row_off, row_len, pool_cols, pool_vals, diag, top_msb, first_msb, comp_max);
     RBG_CUDA_TRY(cudaGetLastError());

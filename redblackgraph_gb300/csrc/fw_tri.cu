@@ -255,38 +255,58 @@ __device__ __forceinline__ bool tri_dag_ok(const DagCounters *dc) { return !(dc-
 // skipped and the call's DAG path rejected (flag 4), so the blocked kernels decide.
 constexpr int TRI_BAD_ROW = 4;
 
-// One warp per row of a candidate matrix: the row statistics of dag_rows.cuh, reduced per
-// matrix (largest product MSB, largest first-value MSB, products).
-__global__ void __launch_bounds__(TRI_THREADS, 8)
+// The row statistics of dag_rows.cuh, reduced per matrix (largest product MSB, largest
+// first-value MSB, products): a group of DAG_STATS_G lanes per row, runs of DAG_STATS_RUN rows
+// per group, one set of atomics per run and matrix.  Each group's bitmap takes 1 KB of shared
+// memory, so TRI_STATS_CTAS CTAs of TRI_STATS_GROUPS groups fit on an SM.
+constexpr int TRI_STATS_GROUPS = TRI_THREADS / DAG_STATS_G;
+constexpr int TRI_STATS_CTAS = 6;
+__global__ void __launch_bounds__(TRI_THREADS, TRI_STATS_CTAS)
 tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                  const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
                  const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, const DagCounters *dc,
                  int *__restrict__ cam, int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
-    __shared__ unsigned bm_all[TRI_ROWS][TRI_BM_WORDS];
+    constexpr int G = DAG_STATS_G;
+    __shared__ __align__(16) unsigned bm_all[TRI_STATS_GROUPS][TRI_BM_WORDS];
     if (!tri_dag_ok(dc)) return;             // block-uniform
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * TRI_ROWS;
-    for (int64_t g = (int64_t)blockIdx.x * TRI_ROWS + w; g < R; g += warps) {
-        const int ci = row_comp[g];
-        const int kind = ckind[ci];
-        if (kind == KIND_NONE || kind == KIND_GENERAL) continue;   // warp-uniform
-        const int32_t base = (int32_t)comps[ci].row_base;
-        const int words = (int)((comps[ci].n + 31) >> 5);
-        int am = -1, fm = -1;
-        unsigned long long prods = 0;
-        dag_row_stats(bm_all[w], words, kind, g, indptr, a_col, a_val,
-                      [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; },
-                      p_col, p_val, [&](int32_t col) { return col - base; }, lane, am, fm, prods);
-        am = __reduce_max_sync(0xffffffffu, am);
-        fm = __reduce_max_sync(0xffffffffu, fm);
-        if (lane == 0) {
-            if (am >= 0) atomicMax(cam + ci, am);
-            if (fm >= 0) atomicMax(cfm + ci, fm);
-            if (prods) atomicAdd(cprod + ci, prods);
+    const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
+    const unsigned gmask = dag_group_mask<G>();
+    int cur = -1, am = -1, fm = -1;          // the matrix of the run's current rows, its statistics
+    unsigned long long prods = 0;
+    auto flush = [&]() {                     // group-uniform
+        const int am_r = __reduce_max_sync(gmask, am);
+        const int fm_r = __reduce_max_sync(gmask, fm);
+        if (lane == 0 && cur >= 0) {
+            if (am_r >= 0) atomicMax(cam + cur, am_r);
+            if (fm_r >= 0) atomicMax(cfm + cur, fm_r);
+            if (prods) atomicAdd(cprod + cur, prods);
+        }
+    };
+    auto crow = [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; };
+    const int64_t stride = (int64_t)gridDim.x * TRI_STATS_GROUPS * DAG_STATS_RUN;
+    for (int64_t r0 = ((int64_t)blockIdx.x * TRI_STATS_GROUPS + grp) * DAG_STATS_RUN; r0 < R; r0 += stride) {
+        const int64_t r1 = min(R, r0 + DAG_STATS_RUN);
+        for (int64_t g = r0; g < r1; ++g) {
+            const int ci = row_comp[g];
+            const int64_t a0 = indptr[g];
+            const int alen = (int)(indptr[g + 1] - a0);
+            const int kind = ckind[ci];
+            if (kind == KIND_NONE || kind == KIND_GENERAL) continue;   // group-uniform
+            if (ci != cur) {
+                flush();
+                cur = ci;
+                am = fm = -1;
+                prods = 0;
+            }
+            const int32_t base = (int32_t)comps[ci].row_base;
+            const int words = (int)((comps[ci].n + 31) >> 5);
+            dag_row_stats<G>(bm_all[grp], words, kind, g, a0, alen, indptr, a_col, a_val, crow, p_col, p_val,
+                             [&](int32_t col) { return col - base; }, lane, gmask, am, fm, prods);
         }
     }
+    flush();
 }
 
 
@@ -978,7 +998,9 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     {
         cudaEvent_t t = timer_begin(6, s);
         note_launches(1);
-        tri_stats_kernel<<<grid_for(R * 32, TRI_THREADS), TRI_THREADS, 0, s>>>(
+        const int64_t runs = (R + DAG_STATS_RUN * TRI_STATS_GROUPS - 1) / (DAG_STATS_RUN * TRI_STATS_GROUPS);
+        tri_stats_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(runs, (int64_t)sm_count() * TRI_STATS_CTAS)),
+                           TRI_THREADS, 0, s>>>(
             R, L.row_comp, L.ckind, L.dc, L.indptr, L.a_col, L.a_val, L.row_off, L.row_len, L.p_col, L.p_val, *dcount,
             L.cam, L.cfm, L.cprod);
         RBG_CUDA_TRY(cudaGetLastError());
