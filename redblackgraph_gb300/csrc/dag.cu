@@ -619,10 +619,12 @@ __device__ __forceinline__ DagRec dag_shfl_rec(const DagRec &r, int src) {
     return o;
 }
 
-// Level L's rows of up to 256 candidates, four consecutive rows per warp at a time: four rows of
-// at most 8 candidates fill together (8 lanes each), rows of at most 16 two at a time, larger
-// rows one after the other with the whole warp.  Lanes 8i..8i+7 hold row i's record; the next
-// four records are read before the current rows are filled.  Block 0 closes the level's range.
+// Level L's rows of up to 256 candidates, four consecutive rows per warp at a time, each by its
+// own size: the rows of at most 8 candidates fill together (8 lanes each), then those of at most
+// 16 two at a time, then the larger ones one after the other with the whole warp (deciding by the
+// largest of the four sent three quarters of a pedigree forest's iterations down the slowest
+// path).  Lanes 8i..8i+7 hold row i's record; the next four records are read before the current
+// rows are filled.  Block 0 closes the level's range.
 __global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int64_t L, const int64_t *Lp) {
     if (!dag_level(a, L, Lp)) return;
     extern __shared__ __align__(16) unsigned char dg_smem[];
@@ -654,28 +656,40 @@ __global__ void __launch_bounds__(DG_WARPS * 32) dag_fill_kernel(DagArgs a, int6
             nv = true;
         }
         const bool act = cv && cur.off >= 0 && cur.ub <= DG_WSLOTS;   // else skipped, or the block tier's
-        const int tm = __reduce_max_sync(FULL, act ? cur.ub : 0);
-        if (tm <= 8) {
-            const int nd = dag_group_row<8, 1>(a, act, cur, lane, best);
-            if ((lane & 7) == 0 && act) {
+        const bool lead = (lane & 7) == 0;       // the lane that speaks for its group's row
+        // rows of at most 8 candidates: each 8-lane group fills its own, all at once
+        const bool a8 = act && cur.ub <= 8;
+        if (__any_sync(FULL, a8)) {
+            const int nd = dag_group_row<8, 1>(a, a8, cur, lane, best);
+            if (lead && a8) {
                 a.row_len[cur.v] = nd;
                 written += (unsigned long long)nd;
             }
-        } else if (tm <= 16) {
-            for (int p = 0; p < 2; ++p) {
-                const int src = (2 * p + (lane >> 4)) * 8;
-                const DagRec r = dag_shfl_rec(cur, src);
-                const bool ra = __shfl_sync(FULL, (int)act, src) != 0;
-                const int nd = dag_group_row<16, 1>(a, ra, r, lane, best);
-                if ((lane & 15) == 0 && ra) {
-                    a.row_len[r.v] = nd;
-                    written += (unsigned long long)nd;
-                }
+        }
+        // rows of 9 to 16: two at a time, 16 lanes each
+        unsigned b16 = __ballot_sync(FULL, lead && act && cur.ub > 8 && cur.ub <= 16);
+        while (b16) {
+            const int r0 = __ffs(b16) - 1;
+            b16 &= b16 - 1;
+            const int r1 = b16 ? __ffs(b16) - 1 : -1;
+            if (b16) b16 &= b16 - 1;
+            const bool upper = lane >= 16;
+            const int src = upper ? (r1 >= 0 ? r1 : r0) : r0;
+            const DagRec r = dag_shfl_rec(cur, src);
+            const bool ra = !upper || r1 >= 0;
+            const int nd = dag_group_row<16, 1>(a, ra, r, lane, best);
+            if ((lane & 15) == 0 && ra) {
+                a.row_len[r.v] = nd;
+                written += (unsigned long long)nd;
             }
-        } else {
-            for (int i = 0; i < 4; ++i) {
-                const DagRec r = dag_shfl_rec(cur, 8 * i);
-                if (__shfl_sync(FULL, (int)act, 8 * i) == 0) continue;
+        }
+        // larger rows: one after another with the whole warp
+        unsigned bw = __ballot_sync(FULL, lead && act && cur.ub > 16);
+        while (bw) {
+            const int src = __ffs(bw) - 1;
+            bw &= bw - 1;
+            {
+                const DagRec r = dag_shfl_rec(cur, src);
                 int nd = -1;
                 if (r.ub <= 32) {
                     nd = dag_group_row_runs<32, 1>(a, true, r, lane, best);
@@ -914,9 +928,12 @@ LevelLaunch level_launch() {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, dag_fill_kernel, DG_WARPS * 32, l.wsm) != cudaSuccess || b < 1)
         b = 4;
+    int bd = 0;                              // discovery: one wave of resident CTAs
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, dag_discover_kernel, 256, 0) != cudaSuccess || bd < 1)
+        bd = 4;
     const int sms = sm_count();
     l.fill_grid = sms * b;
-    l.disc_grid = sms * 8;
+    l.disc_grid = sms * bd;
     l.block_grid = sms;
     return l;
 }
