@@ -415,18 +415,35 @@ namespace rbg {
 constexpr unsigned CCD_UNCLEAN = 1u, CCD_BELOW = 2u, CCD_ABOVE = 4u;
 constexpr int CCD_WARPS = 8;
 
-// one warp per component: its rows' diagonal values and off-diagonal nonzero counts, and the
-// component's flags (clean regime, side of the diagonal)
-__global__ void cc_dag_classify_kernel(int64_t ncomp, const int64_t *__restrict__ indptr,
+// one thread per vertex, in the order of the components (position r of sorted_vertex): its row's
+// diagonal value and off-diagonal nonzero count, and its component's flags (clean regime, side of
+// the diagonal), ORed over the warp's lanes of each component into one atomic (a warp per
+// component left the largest components' rows to one warp)
+__global__ void __launch_bounds__(256) cc_dag_classify_kernel(int64_t n, int64_t ncomp,
+                                       const int64_t *__restrict__ indptr,
                                        const int32_t *__restrict__ indices, const int32_t *__restrict__ data,
                                        const int32_t *__restrict__ sorted_vertex, const int64_t *__restrict__ start,
                                        unsigned *__restrict__ comp_flags, int32_t *__restrict__ diag,
                                        int64_t *__restrict__ cnt) {
     const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < ncomp; c += warps) {
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t rb = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); rb < n; rb += step) {
+        const int64_t r = rb + lane;
+        const bool in = r < n;
+        int64_t c = 0;                               // the last component starting at or before rb
+        if (lane == 0) {
+            int64_t lo = 0, hi = ncomp - 1;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi + 1) >> 1;
+                if (start[mid] <= rb) lo = mid;
+                else hi = mid - 1;
+            }
+            c = lo;
+        }
+        c = __shfl_sync(0xffffffffu, c, 0);
         unsigned f = 0;
-        for (int64_t r = start[c] + lane; r < start[c + 1]; r += 32) {
+        if (in) {
+            while (start[c + 1] <= r) ++c;           // start[ncomp] = n > r ends the walk
             const int64_t u = sorted_vertex[r];
             int32_t d = 0;
             int64_t k = 0;
@@ -445,8 +462,15 @@ __global__ void cc_dag_classify_kernel(int64_t ncomp, const int64_t *__restrict_
             diag[u] = d;
             cnt[u] = k;
         }
-        f = __reduce_or_sync(0xffffffffu, f);
-        if (lane == 0) comp_flags[c] = f;
+        unsigned todo = __ballot_sync(0xffffffffu, in);
+        while (todo) {                               // each component of the warp's lanes
+            const int leader = __ffs(todo) - 1;
+            const int64_t cl = __shfl_sync(0xffffffffu, c, leader);
+            const bool mine = in && c == cl;
+            const unsigned fo = __reduce_or_sync(0xffffffffu, mine ? f : 0u);
+            if (lane == leader && fo) atomicOr(comp_flags + cl, fo);
+            todo &= ~__ballot_sync(0xffffffffu, mine);
+        }
     }
 }
 
@@ -486,6 +510,8 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
     const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
     const unsigned gmask = dag_group_mask<G>();
     int cur = -1, am = -1, fm = -1, mx = 0;  // the component of the run's current rows, its statistics
+    int kind = DAG_KIND_NONE, lo = 0, hi = 0;  // and its kind, lowest and highest vertex, and the
+    int lwords = 0;                            // bitmap words of its local indices
     unsigned long long prods = 0;
     auto flush = [&]() {                     // group-uniform
         const int am_r = __reduce_max_sync(gmask, am);
@@ -505,22 +531,25 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
             const int c = label[u];
             const int64_t a0 = eptr[u];
             const int alen = (int)(eptr[u + 1] - a0);
-            const int kind = comp_kind[c];
-            if (kind == DAG_KIND_NONE) continue;     // group-uniform
-            if (c != cur) {
+            if (c != cur) {                          // group-uniform
                 flush();
                 cur = c;
                 am = fm = -1;
                 mx = 0;
+                kind = comp_kind[c];
+                // a component whose vertices span fewer than DAG_MAX_N numbers indexes its
+                // bitmap by vertex - lowest vertex (no gather); otherwise by its local index
+                const int64_t c0 = start[c], csize = start[c + 1] - c0;
+                lo = sorted_vertex[c0];
+                hi = sorted_vertex[c0 + csize - 1];
+                lwords = (int)((min(csize, (int64_t)DAG_MAX_N + 32) + 31) >> 5);   // clamped by the rows
             }
-            // a component whose vertices span fewer than DAG_MAX_N numbers indexes its bitmap by
-            // vertex - lowest vertex (no gather); otherwise by its local index
-            const int lo = sorted_vertex[start[c]], hi = sorted_vertex[start[c + 1] - 1];
+            if (kind == DAG_KIND_NONE) continue;     // group-uniform
             if (hi - lo < DAG_MAX_N)
                 dag_row_stats<G>(bm_all[grp], (hi - lo + 32) >> 5, kind, u, a0, alen, eptr, ecol, eval, crow, ccol,
                                  cval, [&](int32_t col) { return col - lo; }, lane, gmask, am, fm, prods);
             else
-                dag_row_stats<G>(bm_all[grp], (int)((start[c + 1] - start[c] + 31) >> 5), kind, u, a0, alen, eptr,
+                dag_row_stats<G>(bm_all[grp], lwords, kind, u, a0, alen, eptr,
                                  ecol, eval, crow, ccol, cval, [&](int32_t col) { return local[col]; }, lane, gmask,
                                  am, fm, prods);
             const int64_t o = row_off[u];
@@ -538,30 +567,37 @@ __global__ void cc_dag_merge_count_kernel(int64_t n, const int32_t *__restrict__
         cnt[u] = row_len[u] + (diag[u] != 0 ? 1 : 0);
 }
 
-// one warp per vertex: the closure row with the diagonal value put in its place
-__global__ void cc_dag_merge_fill_kernel(int64_t n, const int64_t *__restrict__ row_off,
+// the closure row of each vertex with the diagonal value put in its place: a group of
+// DAG_STATS_G lanes per vertex (a closure row holds about ten entries), runs of consecutive
+// vertices per group
+__global__ void __launch_bounds__(256) cc_dag_merge_fill_kernel(int64_t n, const int64_t *__restrict__ row_off,
                                          const int32_t *__restrict__ row_len, const int32_t *__restrict__ ccol,
                                          const int32_t *__restrict__ cval, const int32_t *__restrict__ diag,
                                          const int64_t *__restrict__ optr, int32_t *__restrict__ ocol,
                                          int32_t *__restrict__ oval) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n; u += warps) {
-        const int64_t c0 = row_off[u], c1 = c0 + row_len[u], o = optr[u];
-        const int32_t d = diag[u];
-        int below = 0;                                  // closure entries left of the diagonal
-        for (int64_t q = c0 + lane; q < c1; q += 32) below += ccol[q] < u;
-        below = __reduce_add_sync(0xffffffffu, below);
-        const int shift = d != 0 ? 1 : 0;
-        if (lane == 0 && d != 0) {
-            ocol[o + below] = (int32_t)u;
-            oval[o + below] = d;
-        }
-        for (int64_t q = c0 + lane; q < c1; q += 32) {
-            const int32_t col = ccol[q];
-            const int64_t at = o + (q - c0) + (col > u ? shift : 0);
-            ocol[at] = col;
-            oval[at] = cval[q];
+    constexpr int G = DAG_STATS_G, GROUPS = 256 / G;
+    const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
+    const unsigned gmask = dag_group_mask<G>();
+    const int64_t stride = (int64_t)gridDim.x * GROUPS * DAG_STATS_RUN;
+    for (int64_t r0 = ((int64_t)blockIdx.x * GROUPS + grp) * DAG_STATS_RUN; r0 < n; r0 += stride) {
+        const int64_t r1 = min(n, r0 + DAG_STATS_RUN);
+        for (int64_t u = r0; u < r1; ++u) {
+            const int64_t c0 = row_off[u], c1 = c0 + row_len[u], o = optr[u];
+            const int32_t d = diag[u];
+            const int shift = d != 0 ? 1 : 0;
+            int below = 0;                           // closure entries left of the diagonal
+            for (int64_t q = c0 + lane; q < c1; q += G) {
+                const int32_t col = ccol[q];
+                below += col < u;
+                const int64_t at = o + (q - c0) + (col > u ? shift : 0);
+                ocol[at] = col;
+                oval[at] = cval[q];
+            }
+            below = __reduce_add_sync(gmask, below);
+            if (lane == 0 && d != 0) {
+                ocol[o + below] = (int32_t)u;
+                oval[o + below] = d;
+            }
         }
     }
 }
@@ -582,8 +618,9 @@ extern "C" int32_t rbg_cc_dag_classify(int64_t n, const int64_t *indptr, const i
     *edges = 0;
     if (n == 0) return RBG_OK;
     note_launches(1);
-    cc_dag_classify_kernel<<<grid_for(ncomp * 32, 256), 256, 0, s>>>(ncomp, indptr, indices, data, sorted_vertex,
-                                                                     start, comp_flags, diag, edge_ptr);
+    RBG_CUDA_TRY(cudaMemsetAsync(comp_flags, 0, (size_t)ncomp * 4, s));
+    cc_dag_classify_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, ncomp, indptr, indices, data, sorted_vertex, start,
+                                                            comp_flags, diag, edge_ptr);
     RBG_CUDA_TRY(cudaGetLastError());
     RBG_CUDA_TRY(cudaMemsetAsync(edge_ptr + n, 0, 8, s));
     size_t tb = w.tmp_bytes;
@@ -659,8 +696,10 @@ extern "C" int32_t rbg_cc_dag_merge_fill(int64_t n, const int64_t *row_off, cons
     if (n == 0) return RBG_OK;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     note_launches(1);
-    cc_dag_merge_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(n, row_off, row_len, pool_cols, pool_vals, diag,
-                                                                   out_indptr, out_indices, out_data);
+    const int64_t runs = (n + DAG_STATS_RUN * 32 - 1) / (DAG_STATS_RUN * 32);
+    cc_dag_merge_fill_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(runs, (int64_t)sm_count() * 8)), 256, 0,
+                               s>>>(n, row_off, row_len, pool_cols, pool_vals, diag, out_indptr, out_indices,
+                                    out_data);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }

@@ -273,7 +273,8 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
     if (!tri_dag_ok(dc)) return;             // block-uniform
     const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
     const unsigned gmask = dag_group_mask<G>();
-    int cur = -1, am = -1, fm = -1;          // the matrix of the run's current rows, its statistics
+    int cur = -1, am = -1, fm = -1;          // the matrix of the run's current rows, its statistics,
+    int kind = KIND_NONE, base = 0, words = 0;   // its kind, first row and bitmap words
     unsigned long long prods = 0;
     auto flush = [&]() {                     // group-uniform
         const int am_r = __reduce_max_sync(gmask, am);
@@ -292,16 +293,16 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
             const int ci = row_comp[g];
             const int64_t a0 = indptr[g];
             const int alen = (int)(indptr[g + 1] - a0);
-            const int kind = ckind[ci];
-            if (kind == KIND_NONE || kind == KIND_GENERAL) continue;   // group-uniform
-            if (ci != cur) {
+            if (ci != cur) {                     // group-uniform
                 flush();
                 cur = ci;
                 am = fm = -1;
                 prods = 0;
+                kind = ckind[ci];
+                base = (int32_t)comps[ci].row_base;
+                words = (int)((comps[ci].n + 31) >> 5);
             }
-            const int32_t base = (int32_t)comps[ci].row_base;
-            const int words = (int)((comps[ci].n + 31) >> 5);
+            if (kind == KIND_NONE || kind == KIND_GENERAL) continue;   // group-uniform
             dag_row_stats<G>(bm_all[grp], words, kind, g, a0, alen, indptr, a_col, a_val, crow, p_col, p_val,
                              [&](int32_t col) { return col - base; }, lane, gmask, am, fm, prods);
         }
