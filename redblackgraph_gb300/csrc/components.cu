@@ -31,6 +31,21 @@ __device__ __forceinline__ int cc_find(const int *parent, int v) {
     return v;
 }
 
+// The root of v, pointing every vertex on the way at its grandparent (path splitting).  A link
+// only ever points at a smaller vertex of the same tree, so the shortcut keeps every tree; a
+// shortcut stored over a concurrent hook of the same vertex undoes that hook, which the hooking
+// thread then sees (its atomicMin did not find a root) and redoes from the new roots.
+__device__ __forceinline__ int cc_find_split(int *parent, int v) {
+    int p = parent[v];
+    while (p != v) {
+        const int gp = parent[p];
+        if (gp != p) parent[v] = gp;
+        v = p;
+        p = gp;
+    }
+    return v;
+}
+
 __global__ void cc_init_kernel(int n, int *parent) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) parent[v] = v;
 }
@@ -41,14 +56,14 @@ __global__ void cc_hook_kernel(int64_t n, const int64_t *indptr, const int *indi
         for (int64_t e = indptr[u]; e < indptr[u + 1]; ++e) {
             const int v = indices[e];
             if (v < 0 || v >= n) continue;            // malformed column index: ignored
-            int ru = cc_find(parent, (int)u), rv = cc_find(parent, v);
+            int ru = cc_find_split(parent, (int)u), rv = cc_find_split(parent, v);
             while (ru != rv) {
                 const int hi = max(ru, rv), lo = min(ru, rv);
                 const int old = atomicMin(&parent[hi], lo);
                 if (old == hi) { *changed = 1; break; }
                 // hi was hooked meanwhile: retry from the new roots
-                ru = cc_find(parent, old);
-                rv = cc_find(parent, lo);
+                ru = cc_find_split(parent, old);
+                rv = cc_find_split(parent, lo);
             }
         }
     }
@@ -297,12 +312,15 @@ extern "C" int32_t rbg_cc_label(int64_t n, const int64_t *indptr, const int32_t 
     cc_label_kernel<<<g, 256, 0, s>>>(ni, w.parent, w.rank, label);
     // group vertices by component, ascending within each (radix sort is stable)
     cc_iota_kernel<<<g, 256, 0, s>>>(ni, w.vid);
-    tb = w.tmp_bytes;
-    RBG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(w.tmp, tb, label, w.keys_out, w.vid, sorted_vertex, ni, 0,
-                                                 32, s));
+    // the labels are below the component count: sort only their low bits
     int nc = 0;
     RBG_CUDA_TRY(cudaMemcpyAsync(&nc, w.rank + n, 4, cudaMemcpyDeviceToHost, s));
     RBG_CUDA_TRY(cudaStreamSynchronize(s));
+    int bits = 1;
+    while (bits < 32 && ((int64_t)1 << bits) < (int64_t)nc) ++bits;
+    tb = w.tmp_bytes;
+    RBG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(w.tmp, tb, label, w.keys_out, w.vid, sorted_vertex, ni, 0,
+                                                 bits, s));
     note_launches(2);
     cc_layout_kernel<<<g, 256, 0, s>>>(ni, w.keys_out, start);
     cc_local_kernel<<<g, 256, 0, s>>>(ni, w.keys_out, sorted_vertex, start, local);
@@ -492,10 +510,10 @@ __global__ void cc_dag_edges_kernel(int64_t n, const int64_t *__restrict__ indpt
 }
 
 // the row statistics of dag_rows.cuh and the row's largest final value, reduced per component:
-// a group of DAG_STATS_G lanes per vertex, runs of DAG_STATS_RUN vertices per group, one set of
-// atomics per run and component (each group's bitmap takes 1 KB of shared memory)
+// a group of DAG_STATS_G lanes per vertex, runs of `run` vertices per group, one set of atomics
+// per run and component (each group's bitmap takes 1 KB of shared memory)
 constexpr int CCD_STATS_GROUPS = 32 * CCD_WARPS / DAG_STATS_G;
-constexpr int CCD_STATS_CTAS = 6;
+constexpr int CCD_STATS_CTAS = 5;
 __global__ void __launch_bounds__(32 * CCD_WARPS, CCD_STATS_CTAS)
 cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t *__restrict__ local,
                     const int64_t *__restrict__ start, const int32_t *__restrict__ sorted_vertex,
@@ -504,7 +522,7 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
                     const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                     const int32_t *__restrict__ ccol, const int32_t *__restrict__ cval,
                     const int32_t *__restrict__ diag, int *__restrict__ top, int *__restrict__ first,
-                    int *__restrict__ cmax) {
+                    int *__restrict__ cmax, int run) {
     constexpr int G = DAG_STATS_G;
     __shared__ __align__(16) unsigned bm_all[CCD_STATS_GROUPS][DAG_MAX_N / 32];
     const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
@@ -524,9 +542,9 @@ cc_dag_stats_kernel(int64_t n, const int32_t *__restrict__ label, const int32_t 
         }
     };
     auto crow = [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; };
-    const int64_t stride = (int64_t)gridDim.x * CCD_STATS_GROUPS * DAG_STATS_RUN;
-    for (int64_t r0 = ((int64_t)blockIdx.x * CCD_STATS_GROUPS + grp) * DAG_STATS_RUN; r0 < n; r0 += stride) {
-        const int64_t r1 = min(n, r0 + DAG_STATS_RUN);
+    const int64_t stride = (int64_t)gridDim.x * CCD_STATS_GROUPS * run;
+    for (int64_t r0 = ((int64_t)blockIdx.x * CCD_STATS_GROUPS + grp) * run; r0 < n; r0 += stride) {
+        const int64_t r1 = min(n, r0 + run);
         for (int64_t u = r0; u < r1; ++u) {
             const int c = label[u];
             const int64_t a0 = eptr[u];
@@ -574,13 +592,13 @@ __global__ void __launch_bounds__(256) cc_dag_merge_fill_kernel(int64_t n, const
                                          const int32_t *__restrict__ row_len, const int32_t *__restrict__ ccol,
                                          const int32_t *__restrict__ cval, const int32_t *__restrict__ diag,
                                          const int64_t *__restrict__ optr, int32_t *__restrict__ ocol,
-                                         int32_t *__restrict__ oval) {
+                                         int32_t *__restrict__ oval, int run) {
     constexpr int G = DAG_STATS_G, GROUPS = 256 / G;
     const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1);
     const unsigned gmask = dag_group_mask<G>();
-    const int64_t stride = (int64_t)gridDim.x * GROUPS * DAG_STATS_RUN;
-    for (int64_t r0 = ((int64_t)blockIdx.x * GROUPS + grp) * DAG_STATS_RUN; r0 < n; r0 += stride) {
-        const int64_t r1 = min(n, r0 + DAG_STATS_RUN);
+    const int64_t stride = (int64_t)gridDim.x * GROUPS * run;
+    for (int64_t r0 = ((int64_t)blockIdx.x * GROUPS + grp) * run; r0 < n; r0 += stride) {
+        const int64_t r1 = min(n, r0 + run);
         for (int64_t u = r0; u < r1; ++u) {
             const int64_t c0 = row_off[u], c1 = c0 + row_len[u], o = optr[u];
             const int32_t d = diag[u];
@@ -658,11 +676,12 @@ extern "C" int32_t rbg_cc_dag_stats(int64_t n, int64_t ncomp, const int32_t *lab
     }
     if (n == 0) return RBG_OK;
     note_launches(1);
-    const int64_t runs = (n + DAG_STATS_RUN * CCD_STATS_GROUPS - 1) / (DAG_STATS_RUN * CCD_STATS_GROUPS);
-    cc_dag_stats_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(runs, (int64_t)sm_count() * CCD_STATS_CTAS)),
-                          32 * CCD_WARPS, 0, s>>>(
+    const int64_t ctas = (int64_t)sm_count() * CCD_STATS_CTAS;
+    const int run = dag_stats_run(n, ctas * CCD_STATS_GROUPS);
+    const int64_t need = (n + (int64_t)run * CCD_STATS_GROUPS - 1) / ((int64_t)run * CCD_STATS_GROUPS);
+    cc_dag_stats_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, ctas)), 32 * CCD_WARPS, 0, s>>>(
         n, label, local, start, sorted_vertex, comp_kind, edges->indptr, edges->indices, static_cast<const int32_t *>(edges->data),
-        row_off, row_len, pool_cols, pool_vals, diag, top_msb, first_msb, comp_max);
+        row_off, row_len, pool_cols, pool_vals, diag, top_msb, first_msb, comp_max, run);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }
@@ -696,10 +715,11 @@ extern "C" int32_t rbg_cc_dag_merge_fill(int64_t n, const int64_t *row_off, cons
     if (n == 0) return RBG_OK;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     note_launches(1);
-    const int64_t runs = (n + DAG_STATS_RUN * 32 - 1) / (DAG_STATS_RUN * 32);
-    cc_dag_merge_fill_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(runs, (int64_t)sm_count() * 8)), 256, 0,
-                               s>>>(n, row_off, row_len, pool_cols, pool_vals, diag, out_indptr, out_indices,
-                                    out_data);
+    const int64_t ctas = (int64_t)sm_count() * 8;
+    const int run = dag_stats_run(n, ctas * 32);
+    const int64_t need = (n + (int64_t)run * 32 - 1) / ((int64_t)run * 32);
+    cc_dag_merge_fill_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, ctas)), 256, 0, s>>>(
+        n, row_off, row_len, pool_cols, pool_vals, diag, out_indptr, out_indices, out_data, run);
     RBG_CUDA_TRY(cudaGetLastError());
     return RBG_OK;
 }

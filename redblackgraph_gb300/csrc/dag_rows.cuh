@@ -12,7 +12,7 @@
 // maximum over the matrix is the loop's diameter.
 //
 // A row is handled by a group of G lanes of one warp (G = 8 for the closures of pedigrees,
-// whose rows hold about ten entries).  The group's kernels give each group runs of
+// whose rows hold about ten entries).  The group's kernels give each group runs of up to
 // DAG_STATS_RUN consecutive rows and keep the statistics of the current matrix in registers, so
 // a run issues its atomics once per matrix instead of once per row.
 #pragma once
@@ -25,7 +25,14 @@ constexpr int DAG_KIND_GENERAL = 3;   // entries on both sides of the diagonal (
 constexpr int DAG_TOP_MSB = 31;   // lbits - 1 for 32-bit values
 constexpr int DAG_MAX_N = 8192;   // columns of a matrix the per-group bitmap covers
 constexpr int DAG_STATS_G = 8;    // lanes per row in the statistics kernels
-constexpr int DAG_STATS_RUN = 16; // consecutive rows a group takes at a time
+constexpr int DAG_STATS_RUN = 16; // most consecutive rows a group takes at a time
+
+// The run length for `rows` rows over `groups` resident groups: DAG_STATS_RUN, shorter when
+// the runs would leave groups idle (one matrix of a few thousand rows).
+inline int dag_stats_run(int64_t rows, int64_t groups) {
+    const int64_t r = rows / (groups > 0 ? groups : 1);
+    return (int)(r < 1 ? 1 : r > DAG_STATS_RUN ? DAG_STATS_RUN : r);
+}
 
 // MSB of an off-diagonal value; a value no clean product yields (zero, or negative after a
 // wrap) counts as reaching the top bit

@@ -256,18 +256,18 @@ __device__ __forceinline__ bool tri_dag_ok(const DagCounters *dc) { return !(dc-
 constexpr int TRI_BAD_ROW = 4;
 
 // The row statistics of dag_rows.cuh, reduced per matrix (largest product MSB, largest
-// first-value MSB, products): a group of DAG_STATS_G lanes per row, runs of DAG_STATS_RUN rows
-// per group, one set of atomics per run and matrix.  Each group's bitmap takes 1 KB of shared
+// first-value MSB, products): a group of DAG_STATS_G lanes per row, runs of `run` rows per
+// group, one set of atomics per run and matrix.  Each group's bitmap takes 1 KB of shared
 // memory, so TRI_STATS_CTAS CTAs of TRI_STATS_GROUPS groups fit on an SM.
 constexpr int TRI_STATS_GROUPS = TRI_THREADS / DAG_STATS_G;
-constexpr int TRI_STATS_CTAS = 6;
+constexpr int TRI_STATS_CTAS = 5;
 __global__ void __launch_bounds__(TRI_THREADS, TRI_STATS_CTAS)
 tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t *__restrict__ ckind,
                  const TriComp *__restrict__ comps, const int64_t *__restrict__ indptr,
                  const int32_t *__restrict__ a_col, const int32_t *__restrict__ a_val,
                  const int64_t *__restrict__ row_off, const int32_t *__restrict__ row_len,
                  const int32_t *__restrict__ p_col, const int32_t *__restrict__ p_val, const DagCounters *dc,
-                 int *__restrict__ cam, int *__restrict__ cfm, unsigned long long *__restrict__ cprod) {
+                 int *__restrict__ cam, int *__restrict__ cfm, unsigned long long *__restrict__ cprod, int run) {
     constexpr int G = DAG_STATS_G;
     __shared__ __align__(16) unsigned bm_all[TRI_STATS_GROUPS][TRI_BM_WORDS];
     if (!tri_dag_ok(dc)) return;             // block-uniform
@@ -286,9 +286,9 @@ tri_stats_kernel(int64_t R, const int32_t *__restrict__ row_comp, const int32_t 
         }
     };
     auto crow = [&](int64_t r, int64_t &off, int &len) { off = row_off[r]; len = row_len[r]; };
-    const int64_t stride = (int64_t)gridDim.x * TRI_STATS_GROUPS * DAG_STATS_RUN;
-    for (int64_t r0 = ((int64_t)blockIdx.x * TRI_STATS_GROUPS + grp) * DAG_STATS_RUN; r0 < R; r0 += stride) {
-        const int64_t r1 = min(R, r0 + DAG_STATS_RUN);
+    const int64_t stride = (int64_t)gridDim.x * TRI_STATS_GROUPS * run;
+    for (int64_t r0 = ((int64_t)blockIdx.x * TRI_STATS_GROUPS + grp) * run; r0 < R; r0 += stride) {
+        const int64_t r1 = min(R, r0 + run);
         for (int64_t g = r0; g < r1; ++g) {
             const int ci = row_comp[g];
             const int64_t a0 = indptr[g];
@@ -999,11 +999,12 @@ int tri_enqueue(const TriShape &sh, const TriLayout &L, const T *in, T *out, cud
     {
         cudaEvent_t t = timer_begin(6, s);
         note_launches(1);
-        const int64_t runs = (R + DAG_STATS_RUN * TRI_STATS_GROUPS - 1) / (DAG_STATS_RUN * TRI_STATS_GROUPS);
-        tri_stats_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(runs, (int64_t)sm_count() * TRI_STATS_CTAS)),
-                           TRI_THREADS, 0, s>>>(
+        const int64_t ctas = (int64_t)sm_count() * TRI_STATS_CTAS;
+        const int run = dag_stats_run(R, ctas * TRI_STATS_GROUPS);
+        const int64_t need = (R + (int64_t)run * TRI_STATS_GROUPS - 1) / ((int64_t)run * TRI_STATS_GROUPS);
+        tri_stats_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, ctas)), TRI_THREADS, 0, s>>>(
             R, L.row_comp, L.ckind, L.dc, L.indptr, L.a_col, L.a_val, L.row_off, L.row_len, L.p_col, L.p_val, *dcount,
-            L.cam, L.cfm, L.cprod);
+            L.cam, L.cfm, L.cprod, run);
         RBG_CUDA_TRY(cudaGetLastError());
         timer_end(6, t, s);
     }
