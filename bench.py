@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--hi", type=int, default=HI, help="largest pedigree size")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving workload (0: skip)")
     ap.add_argument("--serve-count", type=int, default=0, help="requests in the serving stream")
-    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve", "anynum", "dense"],
+    ap.add_argument("--only", choices=["spgemm", "dag", "compose", "single", "serve", "anynum", "dense", "matmul"],
                     default=None,
                     help="run one secondary workload alone and print its JSON (profiling cases)")
     ap.add_argument("--secondary", type=int, default=1,
@@ -225,6 +225,54 @@ def build_device_batch(w, device):
     blocks = densify(ip, ij, iv, comps)
     torch.cuda.synchronize()
     return blocks
+
+
+def run_matmul(n=4096, seed=9, steps=5):
+    """The dense AVOS product (rb.array @, rbg_avos_matmul) on its natural operands: the closure
+    W of one n=4096 pedigree (int32, 18 generations) times the pedigree's own matrix A, the step
+    that extends every ancestor path by one generation.  n^3 products per call; ALU roofline at
+    OPS_PER_RELAXATION int32 operations per product (the product's shift, and, or, and the sum's
+    min).  The same product for a 512-vertex pedigree is checked against the oracle's C-core
+    product."""
+    import torch
+    from oracle import oracle as orc
+    from redblackgraph_gb300 import synth
+    from redblackgraph_gb300.core.avos import matmul_device
+    from redblackgraph_gb300.dense import fw_dense
+    from redblackgraph_gb300.device import to_device, to_host
+    stream = torch.cuda.current_stream()
+    A = synth.pedigree(n, synth.generations_for(n), seed, dtype=np.int32)
+    da = to_device(A)
+    W, res = fw_dense(da)
+    torch.cuda.synchronize()
+    out = torch.empty_like(W)
+    for _ in range(2):
+        _, rc, _ = matmul_device(W, da, out=out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        _, rc, flags = matmul_device(W, da, out=out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / steps
+    As = synth.pedigree(512, synth.generations_for(512), seed + 1, dtype=np.int32)
+    das = to_device(As)
+    Ws, _ = fw_dense(das)
+    Cs, rcs, _ = matmul_device(Ws, das)
+    torch.cuda.synchronize()
+    C, st, _ = orc.matmul(to_host(Ws), As)
+    exact = bool(rc == 0 and rcs == 0 and st == 0 and (to_host(Cs) == C).all())
+    peak, sms = int32_peak_ops(0, None)
+    ach = float(n) ** 3 * OPS_PER_RELAXATION / t / 1e12
+    return {"workload": f"W (x) A: W the closure of one pedigree, n={n}, {synth.generations_for(n)} generations, "
+                        "A its matrix, int32",
+            "value": float(n) ** 3 / t, "unit": "products/s", "ms": t * 1e3, "status": int(rc),
+            "roofline": {"bound": "int32_alu", "unit": "Tops/s", "achieved": ach, "peak": peak / 1e12,
+                         "frac": ach / (peak / 1e12), "kernel": "rbg_avos_matmul",
+                         "ops_per_product": OPS_PER_RELAXATION,
+                         "peak_source": f"nominal: {sms} SMs x 128 int32 lanes x max SM clock"},
+            "bit_exact_vs_oracle_n512": exact}
 
 
 def int32_peak_ops(device_index: int, sm_max_mhz):
@@ -1022,7 +1070,7 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         fn = {"spgemm": run_spgemm_forest, "dag": run_dag_forest, "compose": run_compose,
               "single": run_single_dense, "anynum": lambda: run_any_numbering(workload(0)),
-              "dense": run_dense_blocked,
+              "dense": run_dense_blocked, "matmul": run_matmul,
               "serve": lambda: run_serving(args.serve_count)}[args.only]
         print(json.dumps(fn()))
         return
@@ -1121,6 +1169,10 @@ def main():
         line["relational_composition"] = run_compose()
         line["any_numbering"] = run_any_numbering(w)
         line["dense_blocked"] = run_dense_blocked()
+        try:
+            line["avos_matmul"] = run_matmul()
+        except Exception as exc:                 # a secondary line never costs the headline
+            line["avos_matmul"] = {"error": f"{type(exc).__name__}: {exc}"}
     if args.serve:
         line["serving"] = run_serving(args.serve_count)
     if rank == 0:
