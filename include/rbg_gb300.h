@@ -486,7 +486,9 @@ int32_t rbg_cc_compact_fill(int64_t n, const int32_t *label, const int32_t *loca
 /* comp_flags[c] (device, ncomp): bit 0 outside the clean regime, bit 1 an entry below the
  * diagonal, bit 2 an entry above it; diag (device, n): each row's diagonal value (0 when not
  * stored); edge_ptr (device, n + 1): row pointers of the off-diagonal nonzeros, *edges (host)
- * their number.  Synchronises `stream`. */
+ * their number.  sorted_vertex and start (ncomp + 1 entries, start[ncomp] = n) as rbg_cc_label
+ * writes them; a graph of n > 0 vertices without components is RBG_ERR_INVALID.  Synchronises
+ * `stream`. */
 int32_t rbg_cc_dag_classify(int64_t n, const int64_t *indptr, const int32_t *indices, const int32_t *data,
                             const int32_t *sorted_vertex, const int64_t *start, int64_t ncomp,
                             void *workspace, int64_t workspace_bytes, uint32_t *comp_flags, int32_t *diag,

@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(256) cc_dag_classify_kernel(int64_t n, int64_t
         c = __shfl_sync(0xffffffffu, c, 0);
         unsigned f = 0;
         if (in) {
-            while (start[c + 1] <= r) ++c;           // start[ncomp] = n > r ends the walk
+            while (c + 1 < ncomp && start[c + 1] <= r) ++c;
             const int64_t u = sorted_vertex[r];
             int32_t d = 0;
             int64_t k = 0;
@@ -626,8 +626,8 @@ extern "C" int32_t rbg_cc_dag_classify(int64_t n, const int64_t *indptr, const i
                                        const int32_t *sorted_vertex, const int64_t *start, int64_t ncomp,
                                        void *workspace, int64_t workspace_bytes, uint32_t *comp_flags,
                                        int32_t *diag, int64_t *edge_ptr, int64_t *edges, rbg_stream_t stream) {
-    if (n < 0 || ncomp < 0 || ncomp > n || !workspace || !edges || (n > 0 && (!indptr || !sorted_vertex || !start ||
-                                                                              !comp_flags || !diag || !edge_ptr)))
+    if (n < 0 || ncomp < 0 || ncomp > n || (n > 0 && ncomp == 0) || !workspace || !edges ||
+        (n > 0 && (!indptr || !sorted_vertex || !start || !comp_flags || !diag || !edge_ptr)))
         return RBG_ERR_INVALID;
     if (workspace_bytes < (int64_t)cc_layout(n, nullptr, nullptr)) return RBG_ERR_NOMEM;
     CcWs w;
