@@ -58,3 +58,24 @@ def test_batch_workspace_sizes_are_stable(native):
     bad = np.array([-1], np.int64)
     out = ctypes.c_int64(0)
     assert native.rbg_fw_batch_workspace_bytes(4, 1, bad.ctypes.data, 0, ctypes.byref(out)) != 0
+
+
+def test_cc_dag_classify_refuses_malformed_components(native):
+    """rbg_cc_dag_classify checks its arguments before anything reaches the GPU: a graph of n > 0
+    vertices without components, more components than vertices, or a missing buffer is
+    RBG_ERR_INVALID (every call here fails that check, so nothing is launched)."""
+    from redblackgraph_gb300 import _lib
+    buf = ctypes.create_string_buffer(4096)
+    p = ctypes.addressof(buf)
+    edges = ctypes.c_int64(-1)
+
+    def classify(n, ncomp, start=p, flags=p):
+        return native.rbg_cc_dag_classify(n, p, p, p, p, start, ncomp, p, 4096, flags, p, p,
+                                          ctypes.byref(edges), None)
+
+    assert classify(5, 0) == _lib.RBG_ERR_INVALID
+    assert classify(5, 6) == _lib.RBG_ERR_INVALID
+    assert classify(-1, 0) == _lib.RBG_ERR_INVALID
+    assert classify(5, 2, start=None) == _lib.RBG_ERR_INVALID
+    assert classify(5, 2, flags=None) == _lib.RBG_ERR_INVALID
+    assert edges.value == -1                         # refused before any output was touched
